@@ -1,0 +1,397 @@
+"""Benchmark: batched SRBD-quadruped MPC control ticks on GB300.
+
+Workload (the batched configuration the headline metric is quoted on):
+4096 roll-pitch-yaw SRBD quadruped MPC instances (n = 12, m = 12), horizons
+drawn uniformly from {25, 50, 100}, gait phase offsets uniform on [0, 1),
+forward reference speeds uniform on [-1, 1] m/s, trot gait (period 0.5 s,
+duty 0.6), 5 SQP iterations per solve, warm start from the shifted previous
+solution.  One bench "step" = one control tick of the whole batch (gait
+tables + batched solve + warm-start shift), all resident in HBM.
+
+Prints one JSON line (see the keys below).  `--impl reference` times the CPU
+restatement of the reference's solver path (the oracle, C++ with OpenMP) on
+the host cores instead.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+BATCH = 4096
+HORIZONS = (25, 50, 100)
+SQP_ITERS = 5
+SEED = 7
+DRIFT = 0.0
+
+
+def f_lqr(n, m):
+    """Work-efficient Riccati FLOPs per stage per SQP iteration (backward, forward, costates)."""
+    return 4 * n ** 3 + 8 * n * n * m + 4 * n * m * m + m ** 3 / 3 + 4 * n * n + 2 * n * m
+
+
+def algorithmic_bytes(n, m, horizon, ref_cols, par_cols):
+    """Compulsory HBM bytes of one batched solve: inputs x0, X0, U0, V0,
+    reference, parameter, w; outputs X, U, V, kkt, status (float32/int32)."""
+    N = np.asarray(horizon, dtype=np.int64)
+    per = (n + (N + 1) * n * 2 + N * m + (N + 1) * (ref_cols + par_cols) + 24) + ((N + 1) * n * 2 + N * m + 3 + 1)
+    return int(per.sum() * 4)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--plain-sample", type=int, default=256)
+    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="small run for ncu (no clocks, no CPU, no plain)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU (oracle) timing
+def cpu_solves_per_s(wl, sample, threads):
+    """Time the oracle's FP32 SQP (5 iterations) on `sample` instances of tick 0."""
+    from oracle import oracle as O
+    from mpx_gb300 import problem as P
+    idx = np.arange(min(sample, wl.batch))
+    opts = P.SolverOptions(sqp_iters=SQP_ITERS)
+    t0 = time.perf_counter()
+    O.sqp_solve(wl.desc, opts, wl.x0[idx], wl.X0[idx], wl.U0[idx], wl.V0[idx], wl.reference[idx],
+                wl.parameter[idx], wl.W[idx], wl.horizon[idx], precision=32, n_threads=threads, want_kkt=False)
+    dt = time.perf_counter() - t0
+    return len(idx) / dt, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle (CPU restatement of the path) on host cores."""
+    from mpx_gb300 import problem as P
+    from oracle import oracle as O
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    wl = P.quadruped_workload(args.batch, horizons=HORIZONS, seed=SEED, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
+                              random_phase=True)
+    sample = min(args.cpu_sample, args.batch)
+    for _ in range(max(args.warmup, 0) and 1):
+        cpu_solves_per_s(wl, min(sample, 32), threads)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_solves_per_s(wl, sample, threads)
+        times.append(dt)
+    tot = sum(times)
+    value = sample * args.steps / tot
+    line = {
+        "metric": "MPC solves/s @4096 envs (batched SRBD quadruped, 5 SQP iterations)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded)", "impl": "reference",
+        "config": config_dict(args.batch),
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": "%d instances of tick 0 per step, 5 SQP iterations, FP32, OpenMP over instances"
+                                   % sample},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(batch):
+    return {"workload": "batched SRBD quadruped trot MPC: %d instances, horizons uniform in {25,50,100}, random gait "
+                        "phase, v_ref uniform in [-1,1] m/s, 5 SQP iterations, warm-started control ticks" % batch,
+            "model": "SRBD_RPY12 (n=12, m=12)", "batch": batch, "horizons": list(HORIZONS), "sqp_iters": SQP_ITERS,
+            "l2": "working set larger than L2 (inputs + per-warp scratch)", "parallelism": "replicas"}
+
+
+# ------------------------------------------------------------ GPU arm
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from mpx_gb300 import problem as P
+    from mpx_gb300.tick import TickRunner
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    B = args.batch
+    wl = P.quadruped_workload(B, horizons=HORIZONS, seed=SEED + rank, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
+                              random_phase=True)
+    opts = P.SolverOptions(sqp_iters=SQP_ITERS)
+    tr = TickRunner(wl, opts, device=dev, drift_std=DRIFT)
+    stream = torch.cuda.Stream(device=dev)
+    n, m = wl.desc.n, wl.desc.m
+    with torch.cuda.stream(stream):
+        tr.first_tick(stream)
+        for _ in range(max(args.warmup, 3)):
+            tr.tick(stream)
+    torch.cuda.synchronize()
+    use_graph = not args.no_graph
+    if use_graph:
+        with torch.cuda.stream(stream):
+            tr.capture(stream)
+            tr.replay()
+        torch.cuda.synchronize()
+
+    # ---------------- device-timed steady-state ticks
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    sev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local_rank) if not args.profile else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for k in range(args.steps):
+            if use_graph:
+                tr.replay()
+            else:
+                tr.shift(stream)
+                tr.tables(stream, from_warm_start=True, advance=True)
+                sev[k][0].record(stream)
+                tr.solve(stream)
+                sev[k][1].record(stream)
+            ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    tick_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * B * args.steps / (total_ms / 1000.0)
+
+    # ---------------- solve kernel alone (roofline): ungraphed ticks with events around the solve
+    solve_ms = []
+    with torch.cuda.stream(stream):
+        for k in range(min(args.steps, 10)):
+            tr.shift(stream)
+            tr.tables(stream, from_warm_start=True, advance=True)
+            sev[k][0].record(stream)
+            tr.solve(stream)
+            sev[k][1].record(stream)
+    torch.cuda.synchronize()
+    solve_ms = [sev[k][0].elapsed_time(sev[k][1]) for k in range(min(args.steps, 10))]
+    solve_avg = sum(solve_ms) / len(solve_ms)
+    kkt = tr.out["kkt"][:, 2].float().cpu().numpy()
+    status = tr.out["status"].cpu().numpy()
+
+    # ---------------- end to end through the public API with host buffers
+    x0_host = torch.empty(B, n, pin_memory=True)
+    x0_host.copy_(tr.x0.cpu())
+    res_host = torch.empty(B, m + 4, pin_memory=True)
+    res_dev = torch.empty(B, m + 4, device=dev)
+    e2e_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    e2e_steps = args.steps
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t_host0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        e2e_ev[0].record(stream)
+        for k in range(e2e_steps):
+            tr.x0.copy_(x0_host, non_blocking=True)             # measured states in
+            tr.shift(stream)
+            tr.tables(stream, from_warm_start=False, advance=True)
+            tr.solve(stream)
+            res_dev[:, :m].copy_(tr.U[:, 0, :])                   # first control (the reference's .grf)
+            res_dev[:, m:m + 3].copy_(tr.out["kkt"])
+            res_dev[:, m + 3].copy_(tr.out["status"].float())
+            res_host.copy_(res_dev, non_blocking=True)             # result out
+        e2e_ev[1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e2e_ev[0].elapsed_time(e2e_ev[1])
+    e2e_value = world * B * e2e_steps / (e2e_ms / 1000.0)
+    h2d = B * n * 4
+    d2h = B * (m + 4) * 4
+
+    # ---------------- plain path comparator (one launch per instance)
+    plain = None
+    if args.plain_sample > 0 and not args.profile:
+        ps = min(args.plain_sample, B)
+        sub = P.Workload(wl.desc, wl.x0[:ps], wl.X0[:ps], wl.U0[:ps], wl.V0[:ps], wl.reference[:ps],
+                         wl.parameter[:ps], wl.W[:ps], wl.horizon[:ps], leg_time=wl.leg_time[:ps],
+                         v_ref=wl.v_ref[:ps])
+        tp = TickRunner(sub, opts, device=dev, drift_std=DRIFT)
+        with torch.cuda.stream(stream):
+            tp.first_tick(stream)
+            for _ in range(max(args.warmup, 3)):
+                tp.tick(stream)
+            tp.shift(stream)
+            tp.tables(stream, from_warm_start=True, advance=True)
+        torch.cuda.synchronize()
+        from mpx_gb300 import _lib
+        from mpx_gb300.solver import _stream_handle
+        L = _lib.load()
+        # the whole plain sweep: one launch per instance, back to back
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            pa.record(stream)
+            st = L.mpxg_solve_plain(tp.solver.handle, _stream_handle(stream), ctypes.byref(tp.io))
+            pb.record(stream)
+        torch.cuda.synchronize()
+        assert st == 0
+        plain_ms = pa.elapsed_time(pb)
+        # per-launch latency of single-instance plain solves
+        lat = []
+        nl = min(ps, 64)
+        pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nl)]
+        with torch.cuda.stream(stream):
+            for i in range(nl):
+                sl = slice(i, i + 1)
+                o1 = {k: v[sl] for k, v in tp.out.items()}
+                io1 = tp.solver.io(tp.x0[sl], tp.X[sl], tp.U[sl], tp.V[sl], tp.ref[sl], tp.par[sl], tp.w[sl],
+                                   tp.horizon[sl], o1)
+                pev[i][0].record(stream)
+                st = L.mpxg_solve_plain(tp.solver.handle, _stream_handle(stream), ctypes.byref(io1))
+                pev[i][1].record(stream)
+                assert st == 0
+        torch.cuda.synchronize()
+        lat = [a.elapsed_time(b) for a, b in pev]
+        plain = {"solves_per_s": ps / (plain_ms / 1000.0), "sample": ps, "launches": ps,
+                 "ms_per_solve": plain_ms / ps,
+                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                "what": "one launch of one instance (%d launches timed)" % nl}}
+        tp.solver.close()
+
+    # ---------------- CPU baseline (oracle, rank 0)
+    cpu = None
+    if rank == 0 and not args.no_cpu and not args.profile:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_solves_per_s(wl, args.cpu_sample, threads)
+        cpu = {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": "%d instances of tick 0, 5 SQP iterations, FP32 oracle (C++), OpenMP over instances; %.1f s"
+                         % (min(args.cpu_sample, B), dt)}
+
+    # ---------------- roofline of the solve kernel
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg_bytes = algorithmic_bytes(n, m, wl.horizon, wl.desc.ref_cols, wl.desc.par_cols)
+    achieved = alg_bytes / (solve_avg / 1000.0) / 1e9
+    traffic = None
+    try:
+        tj = _json.load(open(os.path.join(ROOT, "profiles", "sqp_rpy12_traffic.json")))
+        # bytes per (instance x stage) from a small capture, scaled to this launch
+        traffic = float(tj["dram_bytes_per_instance_stage"]) * float(np.sum(wl.horizon))
+    except Exception:
+        traffic = None
+    flops = float(np.sum(wl.horizon)) * SQP_ITERS * f_lqr(n, m)
+    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+
+    line = {
+        "metric": "MPC solves/s @4096 envs (batched SRBD quadruped, 5 SQP iterations)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded)", "config": config_dict(B),
+        "latency_ms": {"p50": float(np.percentile(tick_ms, 50)), "p99": float(np.percentile(tick_ms, 99)),
+                       "what": "per-solve latency = one batched control tick (all instances complete together)"},
+        "plain": plain,
+        "batched_vs_plain": (value / world) / plain["solves_per_s"] if plain else None,
+        "kkt": {"median": float(np.median(kkt)), "p99": float(np.percentile(kkt, 99)),
+                "frac_le_1e-5": float((kkt <= 1e-5).mean()), "status_nonzero": int((status != 0).sum())},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "sqp_kernel<ModelRpy12>",
+                     "solve_ms": solve_avg, "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "fp32": {"achieved_tflops": flops / (solve_avg / 1000.0) / 1e12, "nominal_peak_tflops": fp32_nominal,
+                 "frac": flops / (solve_avg / 1000.0) / 1e12 / fp32_nominal,
+                 "flops": "work-efficient Riccati count per stage per iteration"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": tr.launches_per_tick * args.steps,
+        "graph": use_graph,
+        "clocks": clk,
+        "geometry": tr.solver.geometry(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+/*
+ * mpxg.h — C ABI of the GB300-native batched primal-dual iLQR MPC solver.
+ *
+ * This is the drop-in boundary for the solve call of iit-DLSLab/mpx:
+ *
+ *   optimizers.mpc(cost, dynamics, hessian_approx, limited_memory,
+ *                  reference, parameter, W, x0, X0, U0, V0) -> (X, U, V)
+ *
+ * bound with functools.partial and jax.jit(jax.vmap(...)) at
+ * mpx/utils/mpc_wrapper_srbd.py:68,77,124-132 and
+ * mpx/utils/mpc_wrapper.py:74,150-158,244,346-354.  Python callables cannot
+ * cross a C ABI, so the (cost, dynamics, hessian_approx) triple is selected
+ * by a compiled-in model id; `limited_memory` has no counterpart (accepted and
+ * ignored by the Python layer).  Everything else maps one to one onto
+ * mpxg_batch_io.
+ *
+ * Conventions
+ *  - Every pointer in mpxg_batch_io / mpxg_lq_io is a DEVICE pointer on the
+ *    current CUDA device; arrays are float32, row-major, padded to n_max.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *  - Solve calls are asynchronous on `stream`, allocate nothing and never
+ *    synchronise the host; all device memory is allocated in mpxg_create.
+ *  - A handle is used by one host thread at a time; handles are independent.
+ *  - Numerical trouble does not abort a batch: it is reported per instance in
+ *    status[b] (bits MPXG_INST_*), as the reference reports it through NaNs
+ *    (mpx/utils/mpc_wrapper.py:96,280).
+ */
+#ifndef MPXG_H
+#define MPXG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MPXG_OK = 0,
+  MPXG_ERR_INVALID_ARG = 1,
+  MPXG_ERR_OUT_OF_MEMORY = 2,
+  MPXG_ERR_BUDGET = 3,       /* admission refused: device-memory budget exhausted */
+  MPXG_ERR_CUDA = 4,
+  MPXG_ERR_TIMEOUT = 5,      /* a bounded wait expired */
+  MPXG_ERR_NUMERICAL = 6,
+  MPXG_ERR_NOT_READY = 7,    /* polled result not finished yet */
+  MPXG_ERR_UNSUPPORTED = 8
+} mpxg_status;
+
+/* Compiled-in models (the reference binds them with functools.partial). */
+enum {
+  MPXG_MODEL_SRBD_QUAT13 = 1,   /* mpx/utils/models.py:6-37 + objectives.py:7-75 */
+  MPXG_MODEL_SRBD_RPY12 = 2,    /* same body, roll-pitch-yaw state */
+  MPXG_MODEL_BIPED_WRENCH12 = 3,/* two rectangular feet, 6-D wrenches */
+  MPXG_MODEL_GENERIC_LQ = 4     /* per-stage LQ data (mpxg_lqr_solve) */
+};
+
+/* Per-instance status bits. */
+enum {
+  MPXG_INST_NAN = 1,       /* non-finite result */
+  MPXG_INST_NON_PD = 2,    /* a Q_uu pivot was not positive */
+  MPXG_INST_LS_FAIL = 4,   /* line search took its smallest step */
+  MPXG_INST_BAD_HORIZON = 8 /* horizon[b] outside 1..n_max: instance skipped */
+};
+
+/* Problem description: fixed for the life of a handle.
+ * Replaces the functools.partial bindings of mpx/utils/mpc_wrapper_srbd.py:61-66
+ * (n_contact, N, mass, inertia, inertia^-1, dt). */
+typedef struct {
+  int model;           /* MPXG_MODEL_* */
+  int n, m;            /* state / control dimension (must match the model) */
+  int n_contact;
+  int n_max;           /* largest horizon N of any instance */
+  int batch_max;       /* largest batch per mpxg_solve call */
+  float dt, mass, gravity, mu;
+  float barrier_alpha, barrier_sigma;   /* relaxed friction-cone barrier, objectives.py:7 */
+  float foot_length, foot_width;        /* biped foot plates */
+  int barrier_kind;    /* 0: penalty() of objectives.py:7-13; 1: C2 relaxed log barrier */
+  int barrier_masked;  /* 1: barrier cost applied to stance legs only */
+  float barrier_hess_scale;
+  float inertia[9];    /* row-major */
+  float inertia_inv[9];
+} mpxg_problem_desc;
+
+/* SQP settings (the reference's solver constants are not in its tree). */
+typedef struct {
+  int sqp_iters;       /* SQP iterations per solve */
+  int ls_max_trials;   /* merit line-search trials */
+  float ls_beta, ls_eta, reg, rho0, ls_skip_tol;
+  int compute_kkt;     /* 1: evaluate the KKT residual of the result */
+  int warps_per_block; /* 0: default (tuned) */
+  int blocks_per_sm;   /* 0: default (tuned) */
+} mpxg_solver_opts;
+
+/* One batched solve.  Layout: x0 [B,n]; X,V [B,n_max+1,n]; U [B,n_max,m];
+ * reference [B,n_max+1,ref_cols]; parameter [B,n_max+1,par_cols];
+ * w [B,24] = diagonal of the reference's W [B,24,24] (mpc_wrapper_srbd.py:127);
+ * K [B,n_max,m,n], k [B,n_max,m]: gains of the last SQP step (optional);
+ * kkt [B,3] = (r_prim, r_dual, max) (optional); status [B] (optional).
+ * X_in/U_in/V_in are the warm start (X0, U0, V0 of the reference) and may
+ * alias X/U/V. */
+typedef struct {
+  int batch;
+  const int* horizon;      /* [B] per-instance N (1..n_max) or NULL = n_max */
+  const float* x0;
+  const float* X_in;
+  const float* U_in;
+  const float* V_in;
+  const float* reference;
+  const float* parameter;
+  const float* w;
+  float* X;
+  float* U;
+  float* V;
+  float* K;
+  float* k;
+  float* kkt;
+  int* status;
+} mpxg_batch_io;
+
+typedef struct mpxg_handle mpxg_handle;
+
+/* Create a solver handle; all device memory is allocated here.
+ * Replaces the construction of `self._solve = jax.jit(jax.vmap(work))`
+ * (mpx/utils/mpc_wrapper_srbd.py:68,77). */
+mpxg_status mpxg_create(const mpxg_problem_desc* desc, const mpxg_solver_opts* opts, mpxg_handle** out);
+void mpxg_destroy(mpxg_handle* h);
+
+/* Launch geometry the handle uses for mpxg_solve (persistent grid of
+ * num_sms * blocks_per_sm blocks of warps_per_block warps). */
+mpxg_status mpxg_query_geometry(const mpxg_handle* h, int* warps_per_block, int* blocks_per_sm, int* num_sms);
+
+/* Device bytes mpxg_create allocates for (desc, opts). */
+size_t mpxg_workspace_bytes(const mpxg_problem_desc* desc, const mpxg_solver_opts* opts);
+
+/* Batched solve: all instances in one persistent launch.
+ * Replaces self._solve(reference, parameter, W, x0, X0, U0, V0)
+ * (mpx/utils/mpc_wrapper_srbd.py:124-132). */
+mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io);
+
+/* The plain path: one launch per instance, no batching, no graph (the
+ * comparator of the batched path).  Same inputs and outputs as mpxg_solve. */
+mpxg_status mpxg_solve_plain(mpxg_handle* h, void* stream, const mpxg_batch_io* io);
+
+/* Warm start for the next control tick: X,U,V shifted by `shift` rows with the
+ * last row repeated, per instance horizon (mpx/utils/mpc_wrapper_srbd.py:135-137).
+ * In place is allowed (Xo == X etc.). */
+mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const int* horizon, int shift,
+                                  const float* X, const float* U, const float* V, float* Xo, float* Uo, float* Vo);
+
+/* Gait timer of a batch (mpx/utils/mpc_utils.py:7-14), float32 without fused
+ * multiply-add: leg_time [B, n_legs] updated in place, contact [B, n_legs]. */
+mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_factor, float step_freq, float dt,
+                           float* leg_time, int* contact);
+
+/* SRBD reference generator (mpx/utils/mpc_utils.py:146-270, path with
+ * use_terrain_estimator = False) for a batch.  Inputs [B,...]: t_timer [B,4],
+ * x [B,13], foot [B,12], input [B,7], contact [B,4], liftoff [B,12] (in/out).
+ * Outputs: reference [B,N+1,17], parameter [B,N+1,16], foot_ref_dot [B,N+1,12]
+ * (row stride n_max+1 when n_max > N). */
+mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt, const float* foot0,
+                             float duty_factor, float step_freq, float step_height, float clearence_speed,
+                             const float* t_timer, const float* x, const float* foot, const float* input,
+                             const float* contact, float* liftoff, float* reference, float* parameter,
+                             float* foot_ref_dot);
+
+/* Gait tables of the synthetic trot / walk workloads (one thread per
+ * instance): optionally x0[b] = X0[b,0,:] + drift[b,:] (X0 the shifted warm
+ * start, drift may be NULL), then, when `advance`, one gait-timer step of
+ * leg_time [B, legs]; then for t = 0..horizon[b] the contact flags from t+1
+ * further timer steps (the schedule rule of mpx/utils/mpc_utils.py:187-189),
+ * a CoM reference at v_ref[b] along x at constant `height`, zero attitude
+ * and rate, and feet at `offsets` [legs*3] (HOST array) from the CoM
+ * reference.  Outputs reference [B,n_max+1,ref_cols], parameter
+ * [B,n_max+1,par_cols] of `model`. */
+mpxg_status mpxg_gait_tables(void* stream, int model, int batch, int n_max, const int* horizon, float dt,
+                             float duty_factor, float step_freq, float height, const float* offsets,
+                             const float* X0, const float* drift, float* x0, const float* v_ref, float* leg_time,
+                             int advance, float* reference, float* parameter);
+
+/* Time-varying LQR in absolute coordinates for a batch (isolated KKT/LQR):
+ * x_{t+1} = A_t x_t + B_t u_t + c_t, cost 1/2 x'Qx + x'Mu + 1/2 u'Ru + q'x + r'u,
+ * terminal Q[N], q[N].  A [B,N,n,n], Bm [B,N,n,m], c [B,N,n], Q [B,N+1,n,n],
+ * R [B,N,m,m], M [B,N,n,m], q [B,N+1,n], r [B,N,m], x0 [B,n].
+ * Outputs K [B,N,m,n], k [B,N,m], X [B,N+1,n], U [B,N,m], lam [B,N+1,n]
+ * (costates dV_t/dx_t).  `method`: 0 sequential Riccati, 1 time-parallel
+ * associative scan. */
+typedef struct {
+  int batch, N, n, m;
+  const float *A, *Bm, *c, *Q, *R, *M, *q, *r, *x0;
+  float *K, *k, *X, *U, *lam;
+  float* workspace;  /* device, >= mpxg_lqr_workspace_bytes(batch, N, n, m, method) bytes */
+} mpxg_lq_io;
+size_t mpxg_lqr_workspace_bytes(int batch, int N, int n, int m, int method);
+mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method);
+
+/* Last error message of a handle (or of the library when h is NULL). */
+const char* mpxg_last_error(const mpxg_handle* h);
+const char* mpxg_status_string(int status);
+int mpxg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPXG_H */

@@ -1,0 +1,127 @@
+"""ctypes binding of libmpxg.so (include/mpxg.h).
+
+The library is built in-tree by mpx_gb300/build.py.  There is no CPU
+fallback: if the library is missing or CUDA is unavailable, load() raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+c_int_p = ctypes.POINTER(ctypes.c_int)
+c_float_p = ctypes.POINTER(ctypes.c_float)
+
+MPXG_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "device-memory budget exhausted",
+                4: "CUDA error", 5: "timeout", 6: "numerical failure", 7: "not ready", 8: "unsupported"}
+
+# per-instance status bits
+INST_NAN = 1
+INST_NON_PD = 2
+INST_LS_FAIL = 4
+
+
+class ProblemDesc(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("n", ctypes.c_int), ("m", ctypes.c_int), ("n_contact", ctypes.c_int),
+                ("n_max", ctypes.c_int), ("batch_max", ctypes.c_int),
+                ("dt", ctypes.c_float), ("mass", ctypes.c_float), ("gravity", ctypes.c_float), ("mu", ctypes.c_float),
+                ("barrier_alpha", ctypes.c_float), ("barrier_sigma", ctypes.c_float),
+                ("foot_length", ctypes.c_float), ("foot_width", ctypes.c_float),
+                ("barrier_kind", ctypes.c_int), ("barrier_masked", ctypes.c_int),
+                ("barrier_hess_scale", ctypes.c_float),
+                ("inertia", ctypes.c_float * 9), ("inertia_inv", ctypes.c_float * 9)]
+
+
+class SolverOpts(ctypes.Structure):
+    _fields_ = [("sqp_iters", ctypes.c_int), ("ls_max_trials", ctypes.c_int), ("ls_beta", ctypes.c_float),
+                ("ls_eta", ctypes.c_float), ("reg", ctypes.c_float), ("rho0", ctypes.c_float),
+                ("ls_skip_tol", ctypes.c_float), ("compute_kkt", ctypes.c_int),
+                ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+
+
+class BatchIO(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("horizon", ctypes.c_void_p),
+                ("x0", ctypes.c_void_p), ("X_in", ctypes.c_void_p), ("U_in", ctypes.c_void_p),
+                ("V_in", ctypes.c_void_p), ("reference", ctypes.c_void_p), ("parameter", ctypes.c_void_p),
+                ("w", ctypes.c_void_p), ("X", ctypes.c_void_p), ("U", ctypes.c_void_p), ("V", ctypes.c_void_p),
+                ("K", ctypes.c_void_p), ("k", ctypes.c_void_p), ("kkt", ctypes.c_void_p),
+                ("status", ctypes.c_void_p)]
+
+
+class LqIO(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("N", ctypes.c_int), ("n", ctypes.c_int), ("m", ctypes.c_int)] + \
+               [(k, ctypes.c_void_p) for k in ("A", "Bm", "c", "Q", "R", "M", "q", "r", "x0",
+                                                "K", "k", "X", "U", "lam", "workspace")]
+
+
+# Exported symbols (every entry point declared in include/mpxg.h).
+EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
+           "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
+
+_lib = None
+
+
+class MpxgError(RuntimeError):
+    pass
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libmpxg.so (building it first if its sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise MpxgError("libmpxg.so is not built (%s); run mpx_gb300.build.build()" % path)
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    L.mpxg_create.argtypes = [ctypes.POINTER(ProblemDesc), ctypes.POINTER(SolverOpts), ctypes.POINTER(vp)]
+    L.mpxg_create.restype = ctypes.c_int
+    L.mpxg_destroy.argtypes = [vp]
+    L.mpxg_destroy.restype = None
+    L.mpxg_query_geometry.argtypes = [vp, c_int_p, c_int_p, c_int_p]
+    L.mpxg_query_geometry.restype = ctypes.c_int
+    L.mpxg_workspace_bytes.argtypes = [ctypes.POINTER(ProblemDesc), ctypes.POINTER(SolverOpts)]
+    L.mpxg_workspace_bytes.restype = ctypes.c_size_t
+    for name in ("mpxg_solve", "mpxg_solve_plain"):
+        f = getattr(L, name)
+        f.argtypes = [vp, vp, ctypes.POINTER(BatchIO)]
+        f.restype = ctypes.c_int
+    L.mpxg_shift_warm_start.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
+    L.mpxg_shift_warm_start.restype = ctypes.c_int
+    L.mpxg_timer_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                 vp, vp]
+    L.mpxg_timer_run.restype = ctypes.c_int
+    L.mpxg_refgen_srbd.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, c_float_p,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                   vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.mpxg_refgen_srbd.restype = ctypes.c_int
+    L.mpxg_gait_tables.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_float,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_float, c_float_p,
+                                   vp, vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.mpxg_gait_tables.restype = ctypes.c_int
+    L.mpxg_lqr_workspace_bytes.argtypes = [ctypes.c_int] * 5
+    L.mpxg_lqr_workspace_bytes.restype = ctypes.c_size_t
+    L.mpxg_lqr_solve.argtypes = [vp, ctypes.POINTER(LqIO), ctypes.c_int]
+    L.mpxg_lqr_solve.restype = ctypes.c_int
+    L.mpxg_last_error.argtypes = [vp]
+    L.mpxg_last_error.restype = ctypes.c_char_p
+    L.mpxg_status_string.argtypes = [ctypes.c_int]
+    L.mpxg_status_string.restype = ctypes.c_char_p
+    L.mpxg_version.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def check(status, handle=None, what="mpxg call"):
+    if status != MPXG_OK:
+        L = load()
+        msg = L.mpxg_last_error(handle).decode() if L is not None else ""
+        raise MpxgError("%s failed: %s (%s)" % (what, STATUS_NAMES.get(status, status), msg))

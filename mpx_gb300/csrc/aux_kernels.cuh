@@ -1,0 +1,301 @@
+// Small per-tick kernels around the solve: warm-start shift, gait timer and
+// the SRBD reference generator (one thread per instance).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace mpxg {
+
+// mpx/utils/mpc_wrapper_srbd.py:135-137 per instance horizon: rows [shift..N]
+// move to [0..N-shift], the last row is repeated into the freed tail.
+__global__ void shift_kernel(int batch, int n_max, int nx, int nu, const int* horizon, int shift, const float* X,
+                             const float* U, const float* V, float* Xo, float* Uo, float* Vo) {
+  const int b = blockIdx.x;
+  if (b >= batch) return;
+  const int N = horizon ? horizon[b] : n_max;
+  if (N < 1 || N > n_max) return;
+  const size_t xo = (size_t)b * (n_max + 1) * nx, uo = (size_t)b * n_max * nu;
+  // read everything first when shifting in place: one block owns one instance
+  extern __shared__ float buf[];
+  float* bx = buf;
+  float* bv = bx + (size_t)(N + 1) * nx;
+  float* bu = bv + (size_t)(N + 1) * nx;
+  for (int e = threadIdx.x; e < (N + 1) * nx; e += blockDim.x) { bx[e] = X[xo + e]; bv[e] = V[xo + e]; }
+  for (int e = threadIdx.x; e < N * nu; e += blockDim.x) bu[e] = U[uo + e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < (N + 1) * nx; e += blockDim.x) {
+    const int t = e / nx, i = e - t * nx;
+    const int src = min(t + shift, N);
+    Xo[xo + e] = bx[src * nx + i];
+    Vo[xo + e] = bv[src * nx + i];
+  }
+  for (int e = threadIdx.x; e < N * nu; e += blockDim.x) {
+    const int t = e / nu, i = e - t * nu;
+    const int src = min(t + shift, N - 1);
+    Uo[uo + e] = bu[src * nu + i];
+  }
+}
+
+// mpx/utils/mpc_utils.py:7-14 with explicit round-to-nearest operations (no
+// fused multiply-add), so that the schedule is bit-identical to float32 CPU
+// arithmetic.
+__device__ __forceinline__ void timer_step(float duty, float inc, float& t, int& contact) {
+  t = __fadd_rn(t, inc);
+  if (t > 1.0f) t = __fadd_rn(t, -1.0f);
+  contact = (t < duty) ? 1 : 0;
+}
+
+__global__ void timer_kernel(int n, int n_legs, float duty, float step_freq, float dt, float* leg_time, int* contact) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float inc = __fmul_rn(dt, step_freq);
+  float t = leg_time[e];
+  int c;
+  timer_step(duty, inc, t, c);
+  leg_time[e] = t;
+  contact[e] = c;
+  (void)n_legs;
+}
+
+// ------------------------------------------------------------ reference generator
+// mpx/utils/mpc_utils.py:146-270 (use_terrain_estimator = False), one thread
+// per instance, float32 with one rounding per operation as the Python source
+// writes it (integer powers as square-and-multiply).
+struct RefGenArgs {
+  int batch, N, n_max;
+  float dt;
+  float foot0[12];
+  float duty, step_freq, step_height, clearence;
+  const float *t_timer, *x, *foot, *input, *contact;
+  float *liftoff, *reference, *parameter, *foot_ref_dot;
+};
+
+__device__ __forceinline__ float sq_(float s) { return __fmul_rn(s, s); }
+__device__ __forceinline__ float cu_(float s) { return __fmul_rn(s, sq_(s)); }
+__device__ __forceinline__ float qu_(float s) { const float s2 = sq_(s); return __fmul_rn(s2, s2); }
+#define ADD __fadd_rn
+#define SUB __fsub_rn
+#define MUL __fmul_rn
+#define DIV __fdiv_rn
+
+__device__ __forceinline__ float splineXY(float cur, float fh, float v0, float s) {
+  const float d = SUB(fh, cur);
+  const float a2 = SUB(MUL(3.0f, d), MUL(2.0f, v0));
+  const float a3 = SUB(v0, MUL(2.0f, d));
+  float r = ADD(cur, MUL(v0, s));
+  r = ADD(r, MUL(a2, sq_(s)));
+  return ADD(r, MUL(a3, cu_(s)));
+}
+__device__ __forceinline__ float splineXY_dot(float cur, float fh, float v0, float s) {
+  const float d = SUB(fh, cur);
+  const float a2 = SUB(MUL(3.0f, d), MUL(2.0f, v0));
+  const float a3 = SUB(v0, MUL(2.0f, d));
+  const float r = ADD(MUL(MUL(2.0f, a2), s), MUL(MUL(3.0f, a3), sq_(s)));
+  return ADD(r, v0);
+}
+__device__ __forceinline__ void splineZ_coef(float cur, float fh, float sh, float* a, float* b, float* c) {
+  const float two_v = 1.4f, five_v = 3.5f, four_v = 2.8f;  // 2*0.7, 5*0.7, 4*0.7 rounded to float
+  *a = SUB(SUB(SUB(MUL(16.0f, sh), MUL(8.0f, fh)), MUL(8.0f, cur)), two_v);
+  *b = SUB(ADD(ADD(five_v, MUL(14.0f, fh)), MUL(18.0f, cur)), MUL(32.0f, sh));
+  *c = SUB(SUB(SUB(MUL(16.0f, sh), MUL(5.0f, fh)), MUL(11.0f, cur)), four_v);
+}
+__device__ __forceinline__ float splineZ(float cur, float fh, float sh, float s) {
+  float a, b, c;
+  splineZ_coef(cur, fh, sh, &a, &b, &c);
+  float r = ADD(MUL(a, qu_(s)), MUL(b, cu_(s)));
+  r = ADD(r, MUL(c, sq_(s)));
+  r = ADD(r, MUL(0.7f, s));
+  return ADD(r, cur);
+}
+__device__ __forceinline__ float splineZ_dot(float cur, float fh, float sh, float s) {
+  float a, b, c;
+  splineZ_coef(cur, fh, sh, &a, &b, &c);
+  float r = ADD(MUL(MUL(4.0f, a), cu_(s)), MUL(MUL(3.0f, b), sq_(s)));
+  r = ADD(r, MUL(MUL(2.0f, c), s));
+  return ADD(r, 0.7f);
+}
+
+__global__ void refgen_srbd_kernel(RefGenArgs g) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.batch) return;
+  const int N = g.N, S = g.n_max + 1;
+  const float* x = g.x + b * 13;
+  const float* input = g.input + b * 7;
+  const float* foot = g.foot + b * 12;
+  float* lo = g.liftoff + b * 12;
+  float* ref = g.reference + (size_t)b * S * 17;
+  float* par = g.parameter + (size_t)b * S * 16;
+  float* frd = g.foot_ref_dot + (size_t)b * S * 12;
+  const float q0 = x[3], q1 = x[4], q2 = x[5], q3 = x[6];
+  const float yaw = atan2f(MUL(2.0f, ADD(MUL(q0, q3), MUL(q1, q2))), SUB(1.0f, MUL(2.0f, ADD(MUL(q2, q2), MUL(q3, q3)))));
+  float sy, cy;
+  sincosf(yaw, &sy, &cy);
+  const float Ry[9] = {cy, -sy, 0.0f, sy, cy, 0.0f, 0.0f, 0.0f, 1.0f};
+  const float lzs = ADD(ADD(ADD(lo[2], lo[5]), lo[8]), lo[11]);
+  const float ph = ADD(input[6], DIV(lzs, 4.0f));
+  const float p[3] = {x[0], x[1], ph};
+  float rlv[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    rlv[r] = ADD(ADD(MUL(Ry[3 * r], input[0]), MUL(Ry[3 * r + 1], input[1])), MUL(Ry[3 * r + 2], input[2]));
+  float fp[12];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const float d = ADD(ADD(MUL(g.foot0[3 * i], Ry[3 * r]), MUL(g.foot0[3 * i + 1], Ry[3 * r + 1])),
+                          MUL(g.foot0[3 * i + 2], Ry[3 * r + 2]));
+      fp[3 * i + r] = ADD(p[r], d);
+    }
+  const float inc = MUL(g.dt, g.step_freq);
+  float cur_t[4];
+  int des[4], early[4];
+  const float thr = ADD(0.5f, MUL(0.5f, g.duty));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    cur_t[i] = g.t_timer[b * 4 + i];
+    timer_step(g.duty, inc, cur_t[i], des[i]);
+    early[i] = (des[i] == 0 && g.contact[b * 4 + i] == 1.0f && cur_t[i] > thr) ? 1 : 0;
+  }
+  const float nrm = sqrtf(ADD(ADD(MUL(rlv[0], rlv[0]), MUL(rlv[1], rlv[1])), MUL(rlv[2], rlv[2])));
+  const float den = ADD(nrm, 1e-6f);
+  float isp[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) isp[r] = MUL(DIV(-rlv[r], den), g.clearence);
+  for (int t = 0; t <= N; ++t) {
+    const float tf = MUL((float)t, g.dt);
+    float* rr = ref + t * 17;
+    rr[0] = ADD(MUL(tf, rlv[0]), p[0]);
+    rr[1] = ADD(MUL(tf, rlv[1]), p[1]);
+    rr[2] = ph;
+    rr[3] = 1.0f; rr[4] = 0.0f; rr[5] = 0.0f; rr[6] = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) { rr[7 + r] = rlv[r]; rr[10 + r] = input[3 + r]; }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) { par[t * 16 + 4 + i] = foot[i]; frd[t * 12 + i] = 0.0f; }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { rr[13 + i] = 0.0f; par[t * 16 + i] = 0.0f; }
+  }
+  float lx[4], ly[4], lz[4], nt[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    lx[i] = lo[3 * i]; ly[i] = lo[3 * i + 1]; lz[i] = lo[3 * i + 2];
+    nt[i] = g.t_timer[b * 4 + i];
+  }
+  const float sqh = sqrtf(DIV(input[6], 9.81f));
+  float fh[2][4];
+#pragma unroll
+  for (int d = 0; d < 2; ++d)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float f1 = DIV(MUL(MUL(0.5f, rlv[d]), g.duty), g.step_freq);
+      const float f2 = MUL(sqh, SUB(x[7 + d], rlv[d]));
+      fh[d][i] = ADD(ADD(f1, f2), fp[3 * i + d]);
+    }
+  const float omd = SUB(1.0f, g.duty);
+  for (int t = 0; t <= N; ++t) {
+    const int tp = (t == 0) ? N : t - 1;  // Python index t-1 wraps to the last row
+    const float* fprev = par + tp * 16 + 4;
+    float px[4], py[4], pz[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { px[i] = fprev[3 * i]; py[i] = fprev[3 * i + 1]; pz[i] = fprev[3 * i + 2]; }
+    int cs[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) timer_step(g.duty, inc, nt[i], cs[i]);
+    float prev_c[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) prev_c[i] = par[tp * 16 + i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { ref[t * 17 + 13 + i] = (float)cs[i]; par[t * 16 + i] = (float)cs[i]; }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (cs[i] == 0 && prev_c[i] != 0.0f) { lx[i] = px[i]; ly[i] = py[i]; lz[i] = pz[i]; }
+    float* ft = par + t * 16 + 4;
+    float* fd = frd + t * 12;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float s = DIV(SUB(nt[i], g.duty), omd);
+      const bool stance = (cs[i] > 0) || (early[i] == 1);
+      const float sh = ADD(lz[i], g.step_height);
+      if (stance) {
+        ft[3 * i] = px[i]; ft[3 * i + 1] = py[i]; ft[3 * i + 2] = pz[i];
+        fd[3 * i] = 0.0f; fd[3 * i + 1] = 0.0f; fd[3 * i + 2] = 0.0f;
+      } else {
+        ft[3 * i] = splineXY(lx[i], fh[0][i], isp[0], s);
+        ft[3 * i + 1] = splineXY(ly[i], fh[1][i], isp[1], s);
+        ft[3 * i + 2] = splineZ(lz[i], lz[i], sh, s);
+        fd[3 * i] = splineXY_dot(lx[i], fh[0][i], isp[0], s);
+        fd[3 * i + 1] = splineXY_dot(ly[i], fh[1][i], isp[1], s);
+        fd[3 * i + 2] = splineZ_dot(lz[i], lz[i], sh, s);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) { lo[3 * i] = lx[i]; lo[3 * i + 1] = ly[i]; lo[3 * i + 2] = lz[i]; }
+}
+#undef ADD
+#undef SUB
+#undef MUL
+#undef DIV
+
+// ------------------------------------------------------------ gait tables
+// Reference / parameter tables of the synthetic trot (quadruped) and walk
+// (biped) workloads, one thread per instance: optional x0 update from the
+// shifted warm start plus a drift, one gait-timer step of the stored leg
+// timers (one control tick), then per stage t the contact flags from t+1
+// further timer steps (as mpc_utils.py:187-189 does), a CoM reference moving
+// at v_ref along x at constant height, and feet at fixed offsets from the CoM
+// reference.
+struct GaitArgs {
+  int batch, n_max, nx, legs, ref_cols, par_cols, contact_col;
+  const int* horizon;
+  float dt, duty, step_freq, height;
+  float off[4][3];
+  const float* X0;     // [B, n_max+1, nx] or null: x0 = X0[b,0] + drift[b]
+  const float* drift;  // [B, nx] or null
+  float* x0;           // [B, nx] (in/out)
+  const float* v_ref;  // [B]
+  float* leg_time;     // [B, legs] (in/out)
+  int advance;         // 1: advance leg_time by one timer step first
+  float *reference, *parameter;
+};
+
+__global__ void gait_tables_kernel(GaitArgs g) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.batch) return;
+  const int N = g.horizon ? g.horizon[b] : g.n_max;
+  if (N < 1 || N > g.n_max) return;
+  float* x0 = g.x0 + (size_t)b * g.nx;
+  if (g.X0) {
+    for (int i = 0; i < g.nx; ++i)
+      x0[i] = g.X0[(size_t)b * (g.n_max + 1) * g.nx + i] + (g.drift ? g.drift[(size_t)b * g.nx + i] : 0.0f);
+  }
+  const float inc = __fmul_rn(g.dt, g.step_freq);
+  float lt[4];
+  for (int i = 0; i < g.legs; ++i) {
+    lt[i] = g.leg_time[b * g.legs + i];
+    if (g.advance) { int c; timer_step(g.duty, inc, lt[i], c); g.leg_time[b * g.legs + i] = lt[i]; }
+  }
+  const float v = g.v_ref[b];
+  const float px0 = x0[0], py0 = x0[1];
+  float* ref = g.reference + (size_t)b * (g.n_max + 1) * g.ref_cols;
+  float* par = g.parameter + (size_t)b * (g.n_max + 1) * g.par_cols;
+  for (int t = 0; t <= N; ++t) {
+    float* rr = ref + (size_t)t * g.ref_cols;
+    float* pp = par + (size_t)t * g.par_cols;
+    for (int k = 0; k < g.ref_cols; ++k) rr[k] = 0.0f;
+    const float px = px0 + __fmul_rn(__fmul_rn((float)t, g.dt), v);
+    rr[0] = px; rr[1] = py0; rr[2] = g.height;
+    if (g.nx == 13) { rr[3] = 1.0f; rr[7] = v; } else { rr[6] = v; }
+    for (int i = 0; i < g.legs; ++i) {
+      int c;
+      timer_step(g.duty, inc, lt[i], c);
+      rr[g.contact_col + i] = (float)c;
+      pp[i] = (float)c;
+      pp[g.legs + 3 * i] = px + g.off[i][0];
+      pp[g.legs + 3 * i + 1] = py0 + g.off[i][1];
+      pp[g.legs + 3 * i + 2] = g.height + g.off[i][2];
+    }
+  }
+}
+
+}  // namespace mpxg

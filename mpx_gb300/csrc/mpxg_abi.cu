@@ -1,0 +1,331 @@
+// C ABI of libmpxg.so (declared in include/mpxg.h): handle management and the
+// host side of every launch.  No torch types cross this boundary.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/mpxg.h"
+#include "aux_kernels.cuh"
+#include "lqr_kernels.cuh"
+#include "sqp_kernel.cuh"
+
+using namespace mpxg;
+
+struct mpxg_handle {
+  mpxg_problem_desc desc;
+  mpxg_solver_opts opts;
+  int device = 0;
+  int num_sms = 0;
+  int warps_per_block = 0, blocks_per_sm = 0, total_warps = 0;
+  long long scratch_stride = 0;
+  float* scratch = nullptr;
+  int* counter = nullptr;
+  ModelConst mc;
+  SqpParams sp;
+  std::string err;
+};
+
+static thread_local std::string g_lib_err;
+
+static mpxg_status fail(mpxg_handle* h, mpxg_status st, const std::string& msg) {
+  if (h) h->err = msg; else g_lib_err = msg;
+  return st;
+}
+static mpxg_status cuda_fail(mpxg_handle* h, cudaError_t e, const char* where) {
+  return fail(h, MPXG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <class M>
+static size_t smem_per_warp() { return sizeof(WarpSmem<M>); }
+
+static bool model_dims(int model, int* nx, int* nu) {
+  switch (model) {
+    case MPXG_MODEL_SRBD_QUAT13: *nx = 13; *nu = 12; return true;
+    case MPXG_MODEL_SRBD_RPY12: *nx = 12; *nu = 12; return true;
+    case MPXG_MODEL_BIPED_WRENCH12: *nx = 12; *nu = 12; return true;
+    default: return false;
+  }
+}
+
+static long long scratch_stride_for(int model, int n_max) {
+  switch (model) {
+    case MPXG_MODEL_SRBD_QUAT13: return scratch_floats<ModelQuat13>(n_max);
+    case MPXG_MODEL_SRBD_RPY12: return scratch_floats<ModelRpy12>(n_max);
+    case MPXG_MODEL_BIPED_WRENCH12: return scratch_floats<ModelBiped12>(n_max);
+    default: return 0;
+  }
+}
+
+template <class M>
+static int resident_blocks(int wpb) {
+  int nb = 0;
+  const size_t smem = sizeof(WarpSmem<M>) * (size_t)wpb;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(sqp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sqp_kernel<M>, wpb * 32, smem) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
+}
+
+// Persistent grid: warps_per_block warps per block and as many blocks per SM
+// as stay resident (one instance per warp at a time).
+static void launch_geometry(const mpxg_problem_desc* d, const mpxg_solver_opts* o, int num_sms, int* wpb, int* bps) {
+  *wpb = (o && o->warps_per_block > 0) ? o->warps_per_block : 4;
+  if (o && o->blocks_per_sm > 0) {
+    *bps = o->blocks_per_sm;
+  } else {
+    switch (d->model) {
+      case MPXG_MODEL_SRBD_QUAT13: *bps = resident_blocks<ModelQuat13>(*wpb); break;
+      case MPXG_MODEL_SRBD_RPY12: *bps = resident_blocks<ModelRpy12>(*wpb); break;
+      case MPXG_MODEL_BIPED_WRENCH12: *bps = resident_blocks<ModelBiped12>(*wpb); break;
+      default: *bps = 1;
+    }
+  }
+  (void)num_sms;
+}
+
+extern "C" {
+
+int mpxg_version(void) { return 100; }
+
+const char* mpxg_status_string(int st) {
+  switch (st) {
+    case MPXG_OK: return "ok";
+    case MPXG_ERR_INVALID_ARG: return "invalid argument";
+    case MPXG_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case MPXG_ERR_BUDGET: return "device-memory budget exhausted";
+    case MPXG_ERR_CUDA: return "CUDA error";
+    case MPXG_ERR_TIMEOUT: return "timeout";
+    case MPXG_ERR_NUMERICAL: return "numerical failure";
+    case MPXG_ERR_NOT_READY: return "not ready";
+    case MPXG_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* mpxg_last_error(const mpxg_handle* h) { return h ? h->err.c_str() : g_lib_err.c_str(); }
+
+size_t mpxg_workspace_bytes(const mpxg_problem_desc* d, const mpxg_solver_opts* o) {
+  if (!d) return 0;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  int wpb, bps;
+  launch_geometry(d, o, sms, &wpb, &bps);
+  const long long stride = scratch_stride_for(d->model, d->n_max);
+  return (size_t)stride * sizeof(float) * (size_t)sms * bps * wpb + 256;
+}
+
+mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, mpxg_handle** out) {
+  if (!d || !o || !out) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: null argument");
+  *out = nullptr;
+  int nx, nu;
+  if (!model_dims(d->model, &nx, &nu)) return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_create: unknown model id");
+  if (d->n != nx || d->m != nu) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: n/m do not match the model");
+  if (d->n_max < 1 || d->n_max > 4096) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: n_max out of range");
+  if (d->batch_max < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: batch_max < 1");
+  if (o->sqp_iters < 0 || o->ls_max_trials < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: bad options");
+  if (!(d->dt > 0.0f) || !(d->mass > 0.0f)) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: dt and mass must be > 0");
+  mpxg_handle* h = new mpxg_handle();
+  h->desc = *d;
+  h->opts = *o;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaGetDevice"); }
+  e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaDeviceGetAttribute"); }
+  launch_geometry(d, o, h->num_sms, &h->warps_per_block, &h->blocks_per_sm);
+  h->total_warps = h->num_sms * h->blocks_per_sm * h->warps_per_block;
+  h->scratch_stride = scratch_stride_for(d->model, d->n_max);
+  const size_t bytes = (size_t)h->scratch_stride * sizeof(float) * (size_t)h->total_warps;
+  e = cudaMalloc(&h->scratch, bytes);
+  if (e != cudaSuccess) { delete h; return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_create: scratch allocation failed"); }
+  e = cudaMalloc(&h->counter, 256);
+  if (e != cudaSuccess) { cudaFree(h->scratch); delete h; return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_create: counter allocation failed"); }
+  ModelConst& mc = h->mc;
+  mc.dt = d->dt; mc.mass = d->mass; mc.inv_mass = 1.0f / d->mass; mc.gravity = d->gravity; mc.mu = d->mu;
+  mc.alpha = d->barrier_alpha; mc.sigma = d->barrier_sigma;
+  mc.foot_length = d->foot_length; mc.foot_width = d->foot_width;
+  mc.barrier_kind = d->barrier_kind; mc.barrier_masked = d->barrier_masked;
+  mc.barrier_hess_scale = d->barrier_hess_scale;
+  for (int i = 0; i < 9; ++i) { mc.I[i] = d->inertia[i]; mc.Iinv[i] = d->inertia_inv[i]; }
+  SqpParams& sp = h->sp;
+  sp.sqp_iters = o->sqp_iters; sp.ls_max_trials = o->ls_max_trials; sp.ls_beta = o->ls_beta; sp.ls_eta = o->ls_eta;
+  sp.reg = o->reg; sp.rho0 = o->rho0; sp.ls_skip_tol = o->ls_skip_tol; sp.compute_kkt = o->compute_kkt;
+  *out = h;
+  return MPXG_OK;
+}
+
+/* Launch geometry chosen for a handle: warps per block, blocks per SM, SMs. */
+mpxg_status mpxg_query_geometry(const mpxg_handle* h, int* warps_per_block, int* blocks_per_sm, int* num_sms) {
+  if (!h || !warps_per_block || !blocks_per_sm || !num_sms) return MPXG_ERR_INVALID_ARG;
+  *warps_per_block = h->warps_per_block;
+  *blocks_per_sm = h->blocks_per_sm;
+  *num_sms = h->num_sms;
+  return MPXG_OK;
+}
+
+void mpxg_destroy(mpxg_handle* h) {
+  if (!h) return;
+  if (h->scratch) cudaFree(h->scratch);
+  if (h->counter) cudaFree(h->counter);
+  delete h;
+}
+
+}  // extern "C"
+
+template <class M>
+static mpxg_status launch_sqp(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb) {
+  const size_t smem = smem_per_warp<M>() * (size_t)wpb;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(sqp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
+  }
+  sqp_kernel<M><<<blocks, wpb * 32, smem, st>>>(h->mc, h->sp, bp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "sqp_kernel launch");
+  return MPXG_OK;
+}
+
+static mpxg_status dispatch(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb) {
+  switch (h->desc.model) {
+    case MPXG_MODEL_SRBD_QUAT13: return launch_sqp<ModelQuat13>(h, st, bp, blocks, wpb);
+    case MPXG_MODEL_SRBD_RPY12: return launch_sqp<ModelRpy12>(h, st, bp, blocks, wpb);
+    case MPXG_MODEL_BIPED_WRENCH12: return launch_sqp<ModelBiped12>(h, st, bp, blocks, wpb);
+    default: return fail(h, MPXG_ERR_UNSUPPORTED, "model");
+  }
+}
+
+static mpxg_status check_io(mpxg_handle* h, const mpxg_batch_io* io) {
+  if (!h) return fail(nullptr, MPXG_ERR_INVALID_ARG, "null handle");
+  if (!io) return fail(h, MPXG_ERR_INVALID_ARG, "null io");
+  if (io->batch < 0 || io->batch > h->desc.batch_max) return fail(h, MPXG_ERR_INVALID_ARG, "batch exceeds batch_max");
+  if (!io->x0 || !io->X_in || !io->U_in || !io->V_in || !io->reference || !io->parameter || !io->w || !io->X ||
+      !io->U || !io->V)
+    return fail(h, MPXG_ERR_INVALID_ARG, "required pointer is null");
+  return MPXG_OK;
+}
+
+static BatchPtrs make_ptrs(mpxg_handle* h, const mpxg_batch_io* io) {
+  BatchPtrs bp;
+  bp.batch = io->batch; bp.n_max = h->desc.n_max; bp.horizon = io->horizon;
+  bp.x0 = io->x0; bp.X_in = io->X_in; bp.U_in = io->U_in; bp.V_in = io->V_in;
+  bp.ref = io->reference; bp.par = io->parameter; bp.w = io->w;
+  bp.X = io->X; bp.U = io->U; bp.V = io->V; bp.K = io->K; bp.k = io->k; bp.kkt = io->kkt; bp.status = io->status;
+  bp.counter = h->counter; bp.scratch = h->scratch; bp.scratch_stride = h->scratch_stride;
+  bp.single_instance = -1;
+  return bp;
+}
+
+extern "C" {
+
+mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
+  mpxg_status s = check_io(h, io);
+  if (s != MPXG_OK) return s;
+  if (io->batch == 0) return MPXG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchPtrs bp = make_ptrs(h, io);
+  cudaError_t e = cudaMemsetAsync(h->counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
+  const int wpb = h->warps_per_block;
+  int blocks = h->num_sms * h->blocks_per_sm;
+  const int need = (io->batch + wpb - 1) / wpb;
+  if (need < blocks) blocks = need;
+  return dispatch(h, st, bp, blocks, wpb);
+}
+
+mpxg_status mpxg_solve_plain(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
+  mpxg_status s = check_io(h, io);
+  if (s != MPXG_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchPtrs bp = make_ptrs(h, io);
+  for (int b = 0; b < io->batch; ++b) {
+    bp.single_instance = b;
+    s = dispatch(h, st, bp, 1, 1);
+    if (s != MPXG_OK) return s;
+  }
+  return MPXG_OK;
+}
+
+mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const int* horizon, int shift,
+                                  const float* X, const float* U, const float* V, float* Xo, float* Uo, float* Vo) {
+  if (!h) return fail(nullptr, MPXG_ERR_INVALID_ARG, "null handle");
+  if (batch < 0 || batch > h->desc.batch_max || shift < 0 || !X || !U || !V || !Xo || !Uo || !Vo)
+    return fail(h, MPXG_ERR_INVALID_ARG, "mpxg_shift_warm_start: bad arguments");
+  if (batch == 0 || shift == 0 && X == Xo && U == Uo && V == Vo) return MPXG_OK;
+  const int nx = h->desc.n, nu = h->desc.m, nm = h->desc.n_max;
+  const size_t smem = ((size_t)(nm + 1) * nx * 2 + (size_t)nm * nu) * sizeof(float);
+  if (smem > 200 * 1024) return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_shift_warm_start: horizon too long");
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(shift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
+  }
+  shift_kernel<<<batch, 128, smem, (cudaStream_t)stream>>>(batch, nm, nx, nu, horizon, shift, X, U, V, Xo, Uo, Vo);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "shift_kernel launch");
+}
+
+mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_factor, float step_freq, float dt,
+                           float* leg_time, int* contact) {
+  if (batch < 0 || n_legs < 1 || !leg_time || !contact) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_timer_run");
+  const int n = batch * n_legs;
+  if (n == 0) return MPXG_OK;
+  timer_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(n, n_legs, duty_factor, step_freq, dt, leg_time, contact);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "timer_kernel launch");
+}
+
+mpxg_status mpxg_gait_tables(void* stream, int model, int batch, int n_max, const int* horizon, float dt,
+                             float duty_factor, float step_freq, float height, const float* offsets,
+                             const float* X0, const float* drift, float* x0, const float* v_ref, float* leg_time,
+                             int advance, float* reference, float* parameter) {
+  GaitArgs g;
+  if (model == MPXG_MODEL_SRBD_QUAT13) { g.nx = 13; g.legs = 4; g.ref_cols = 17; g.par_cols = 16; g.contact_col = 13; }
+  else if (model == MPXG_MODEL_SRBD_RPY12) { g.nx = 12; g.legs = 4; g.ref_cols = 16; g.par_cols = 16; g.contact_col = 12; }
+  else if (model == MPXG_MODEL_BIPED_WRENCH12) { g.nx = 12; g.legs = 2; g.ref_cols = 14; g.par_cols = 8; g.contact_col = 12; }
+  else return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_gait_tables: model");
+  if (batch < 0 || n_max < 1 || !offsets || !x0 || !v_ref || !leg_time || !reference || !parameter)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_gait_tables: bad arguments");
+  if (batch == 0) return MPXG_OK;
+  g.batch = batch; g.n_max = n_max; g.horizon = horizon; g.dt = dt; g.duty = duty_factor; g.step_freq = step_freq;
+  g.height = height;
+  for (int i = 0; i < 4; ++i)
+    for (int k = 0; k < 3; ++k) g.off[i][k] = (i < g.legs) ? offsets[3 * i + k] : 0.0f;  // host array
+  g.X0 = X0; g.drift = drift; g.x0 = x0; g.v_ref = v_ref; g.leg_time = leg_time; g.advance = advance;
+  g.reference = reference; g.parameter = parameter;
+  gait_tables_kernel<<<(batch + 127) / 128, 128, 0, (cudaStream_t)stream>>>(g);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "gait_tables_kernel launch");
+}
+
+mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt, const float* foot0,
+                             float duty_factor, float step_freq, float step_height, float clearence_speed,
+                             const float* t_timer, const float* x, const float* foot, const float* input,
+                             const float* contact, float* liftoff, float* reference, float* parameter,
+                             float* foot_ref_dot) {
+  if (batch < 0 || N < 1 || n_max < N || !foot0 || !t_timer || !x || !foot || !input || !contact || !liftoff ||
+      !reference || !parameter || !foot_ref_dot)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_refgen_srbd: bad arguments");
+  if (batch == 0) return MPXG_OK;
+  RefGenArgs g;
+  g.batch = batch; g.N = N; g.n_max = n_max; g.dt = dt;
+  for (int i = 0; i < 12; ++i) g.foot0[i] = foot0[i];  // host array
+  g.duty = duty_factor; g.step_freq = step_freq; g.step_height = step_height; g.clearence = clearence_speed;
+  g.t_timer = t_timer; g.x = x; g.foot = foot; g.input = input; g.contact = contact;
+  g.liftoff = liftoff; g.reference = reference; g.parameter = parameter; g.foot_ref_dot = foot_ref_dot;
+  refgen_srbd_kernel<<<(batch + 127) / 128, 128, 0, (cudaStream_t)stream>>>(g);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "refgen_srbd_kernel launch");
+}
+
+size_t mpxg_lqr_workspace_bytes(int batch, int N, int n, int m, int method) {
+  (void)m;
+  (void)method;
+  if (batch < 0 || N < 1 || n < 1) return 0;
+  return lqr_scratch_bytes(batch, N, n);
+}
+
+mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method) {
+  return lqr_solve_host(stream, io, method, &g_lib_err);
+}
+
+}  // extern "C"

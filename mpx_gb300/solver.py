@@ -1,0 +1,219 @@
+"""Host-side solver object: owns one libmpxg handle and runs batched solves
+on torch CUDA tensors (torch provides device memory and streams only).
+
+    solver = Solver(desc, opts, n_max=100, batch_max=4096)
+    out = solver.solve(x0, X0, U0, V0, reference, parameter, W, horizon)
+
+mirrors `optimizers.mpc(cost, dynamics, hessian_approx, limited_memory,
+reference, parameter, W, x0, X0, U0, V0) -> (X, U, V)` under jax.vmap
+(mpx/utils/mpc_wrapper_srbd.py:68,77,124-132), with the model fixed at
+construction instead of passed as callables.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .problem import NW, ModelDesc, SolverOptions
+
+_F32 = torch.float32
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def problem_desc(desc, n_max, batch_max):
+    d = _lib.ProblemDesc()
+    d.model = int(desc.model); d.n = int(desc.n); d.m = int(desc.m); d.n_contact = int(desc.n_contact)
+    d.n_max = int(n_max); d.batch_max = int(batch_max)
+    d.dt = float(desc.dt); d.mass = float(desc.mass); d.gravity = float(desc.gravity); d.mu = float(desc.mu)
+    d.barrier_alpha = float(desc.barrier_alpha); d.barrier_sigma = float(desc.barrier_sigma)
+    d.foot_length = float(desc.foot_length); d.foot_width = float(desc.foot_width)
+    d.barrier_kind = int(desc.barrier_kind); d.barrier_masked = int(desc.barrier_masked)
+    d.barrier_hess_scale = float(desc.barrier_hess_scale)
+    I = np.asarray(desc.inertia, dtype=np.float64).reshape(9)
+    Ii = np.asarray(desc.inertia_inv, dtype=np.float64).reshape(9)
+    for i in range(9):
+        d.inertia[i] = float(I[i])
+        d.inertia_inv[i] = float(Ii[i])
+    return d
+
+
+def solver_opts(opts, warps_per_block=0, blocks_per_sm=0):
+    o = _lib.SolverOpts()
+    o.sqp_iters = int(opts.sqp_iters); o.ls_max_trials = int(opts.ls_max_trials); o.ls_beta = float(opts.ls_beta)
+    o.ls_eta = float(opts.ls_eta); o.reg = float(opts.reg); o.rho0 = float(opts.rho0)
+    o.ls_skip_tol = float(opts.ls_skip_tol); o.compute_kkt = int(bool(opts.compute_kkt))
+    o.warps_per_block = int(warps_per_block); o.blocks_per_sm = int(blocks_per_sm)
+    return o
+
+
+def weights_diagonal(W, batch=None):
+    """The solver takes the diagonal of the reference's W [B, 24, 24]
+    (mpc_wrapper_srbd.py:127 tiles one W per instance).  Off-diagonal entries
+    are rejected: the compiled models use diagonal weights."""
+    W = torch.as_tensor(W)
+    if W.dim() == 1:
+        w = W.reshape(1, NW)
+    elif W.dim() == 2 and W.shape == (NW, NW):
+        off = W - torch.diag_embed(torch.diagonal(W))
+        if torch.count_nonzero(off).item() != 0:
+            raise ValueError("W must be diagonal for the compiled SRBD models")
+        w = torch.diagonal(W).reshape(1, NW)
+    elif W.dim() == 2 and W.shape[1] == NW:
+        w = W
+    elif W.dim() == 3:
+        d = torch.diagonal(W, dim1=-2, dim2=-1)
+        off = W - torch.diag_embed(d)
+        if torch.count_nonzero(off).item() != 0:
+            raise ValueError("W must be diagonal for the compiled SRBD models")
+        w = d
+    else:
+        raise ValueError("W must be [24,24], [B,24,24], [24] or [B,24]")
+    if batch is not None and w.shape[0] == 1 and batch > 1:
+        w = w.expand(batch, NW)
+    return w
+
+
+class Solver:
+    """One libmpxg handle (fixed model, n_max and batch_max)."""
+
+    def __init__(self, desc: ModelDesc, opts: SolverOptions = None, n_max=50, batch_max=1, device=None,
+                 warps_per_block=0, blocks_per_sm=0):
+        if not torch.cuda.is_available():
+            raise _lib.MpxgError("CUDA is not available: the mpx_gb300 solver has no CPU path")
+        self.L = _lib.load()
+        self.desc = desc
+        self.opts = opts or SolverOptions()
+        self.n_max = int(n_max)
+        self.batch_max = int(batch_max)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self._pd = problem_desc(desc, self.n_max, self.batch_max)
+        self._po = solver_opts(self.opts, warps_per_block, blocks_per_sm)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            st = self.L.mpxg_create(ctypes.byref(self._pd), ctypes.byref(self._po), ctypes.byref(h))
+        _lib.check(st, None, "mpxg_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.L.mpxg_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def geometry(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.L.mpxg_query_geometry(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+                   self.handle, "mpxg_query_geometry")
+        return dict(warps_per_block=a.value, blocks_per_sm=b.value, num_sms=c.value)
+
+    # ------------------------------------------------------------ tensors
+    def _dev(self, a, dtype=_F32):
+        if a is None:
+            return None
+        t = torch.as_tensor(a)
+        if t.device != self.device or t.dtype != dtype:
+            t = t.to(device=self.device, dtype=dtype)
+        return t.contiguous()
+
+    def empty_outputs(self, batch, want_gains=False):
+        n, m, N = self.desc.n, self.desc.m, self.n_max
+        dev = self.device
+        out = dict(X=torch.empty(batch, N + 1, n, device=dev), U=torch.empty(batch, N, m, device=dev),
+                   V=torch.empty(batch, N + 1, n, device=dev), kkt=torch.empty(batch, 3, device=dev),
+                   status=torch.empty(batch, dtype=torch.int32, device=dev))
+        if want_gains:
+            out["K"] = torch.empty(batch, N, m, n, device=dev)
+            out["k"] = torch.empty(batch, N, m, device=dev)
+        return out
+
+    def io(self, x0, X0, U0, V0, reference, parameter, w, horizon, out):
+        io = _lib.BatchIO()
+        io.batch = int(x0.shape[0])
+        io.horizon = _ptr(horizon)
+        io.x0, io.X_in, io.U_in, io.V_in = _ptr(x0), _ptr(X0), _ptr(U0), _ptr(V0)
+        io.reference, io.parameter, io.w = _ptr(reference), _ptr(parameter), _ptr(w)
+        io.X, io.U, io.V = _ptr(out["X"]), _ptr(out["U"]), _ptr(out["V"])
+        io.K, io.k = _ptr(out.get("K")), _ptr(out.get("k"))
+        io.kkt, io.status = _ptr(out.get("kkt")), _ptr(out.get("status"))
+        return io
+
+    def prepare(self, x0, X0, U0, V0, reference, parameter, W, horizon=None):
+        """Move/convert inputs to contiguous float32 device tensors."""
+        B = int(torch.as_tensor(x0).shape[0])
+        x0, X0, U0, V0 = self._dev(x0), self._dev(X0), self._dev(U0), self._dev(V0)
+        reference, parameter = self._dev(reference), self._dev(parameter)
+        w = self._dev(weights_diagonal(torch.as_tensor(W), B)).contiguous()
+        if horizon is not None:
+            horizon = self._dev(horizon, torch.int32)
+        N = self.n_max
+        n, m = self.desc.n, self.desc.m
+        assert X0.shape == (B, N + 1, n) and V0.shape == (B, N + 1, n) and U0.shape == (B, N, m), \
+            "warm start must be padded to n_max=%d" % N
+        assert reference.shape == (B, N + 1, self.desc.ref_cols) and parameter.shape == (B, N + 1, self.desc.par_cols)
+        return x0, X0, U0, V0, reference, parameter, w, horizon
+
+    def solve(self, x0, X0, U0, V0, reference, parameter, W, horizon=None, stream=None, plain=False, out=None,
+              want_gains=False):
+        """Batched (or, with plain=True, one-launch-per-instance) SQP solve.
+        Returns dict with X, U, V, kkt [B,3], status [B] (and K, k)."""
+        x0, X0, U0, V0, reference, parameter, w, horizon = self.prepare(x0, X0, U0, V0, reference, parameter, W,
+                                                                        horizon)
+        B = x0.shape[0]
+        if out is None:
+            out = self.empty_outputs(B, want_gains)
+        io = self.io(x0, X0, U0, V0, reference, parameter, w, horizon, out)
+        fn = self.L.mpxg_solve_plain if plain else self.L.mpxg_solve
+        with torch.cuda.device(self.device):
+            st = fn(self.handle, _stream_handle(stream), ctypes.byref(io))
+        _lib.check(st, self.handle, "mpxg_solve_plain" if plain else "mpxg_solve")
+        out["_keep"] = (x0, X0, U0, V0, reference, parameter, w, horizon)
+        return out
+
+    def shift(self, X, U, V, horizon=None, shift=1, stream=None, out=None):
+        """Warm-start shift (mpc_wrapper_srbd.py:135-137) on the device; in place when out is None."""
+        Xo, Uo, Vo = (X, U, V) if out is None else out
+        st = self.L.mpxg_shift_warm_start(self.handle, _stream_handle(stream), int(X.shape[0]), _ptr(horizon),
+                                          int(shift), _ptr(X), _ptr(U), _ptr(V), _ptr(Xo), _ptr(Uo), _ptr(Vo))
+        _lib.check(st, self.handle, "mpxg_shift_warm_start")
+        return Xo, Uo, Vo
+
+
+def lqr_solve(A, B, c, Q, R, M, q, r, x0, method=0, stream=None):
+    """Batched time-varying LQR (absolute coordinates) on the device.
+    Shapes as in include/mpxg.h mpxg_lqr_solve.  Returns dict K, k, X, U, lam."""
+    L = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t = [torch.as_tensor(a).to(device=dev, dtype=_F32).contiguous() for a in (A, B, c, Q, R, M, q, r, x0)]
+    Bsz, N, n, _ = t[0].shape
+    m = t[1].shape[-1]
+    out = dict(K=torch.empty(Bsz, N, m, n, device=dev), k=torch.empty(Bsz, N, m, device=dev),
+               X=torch.empty(Bsz, N + 1, n, device=dev), U=torch.empty(Bsz, N, m, device=dev),
+               lam=torch.empty(Bsz, N + 1, n, device=dev))
+    ws_bytes = int(L.mpxg_lqr_workspace_bytes(Bsz, N, n, m, method))
+    ws = torch.empty(max(ws_bytes // 4, 1), device=dev)
+    io = _lib.LqIO()
+    io.batch, io.N, io.n, io.m = Bsz, N, n, m
+    for name, ten in zip(("A", "Bm", "c", "Q", "R", "M", "q", "r", "x0"), t):
+        setattr(io, name, _ptr(ten))
+    for name in ("K", "k", "X", "U", "lam"):
+        setattr(io, name, _ptr(out[name]))
+    io.workspace = _ptr(ws)
+    st = L.mpxg_lqr_solve(_stream_handle(stream), ctypes.byref(io), int(method))
+    _lib.check(st, None, "mpxg_lqr_solve")
+    out["_keep"] = (t, ws)
+    return out

@@ -1,0 +1,58 @@
+"""The C ABI library builds, loads and exports every entry point that
+include/mpxg.h declares (no GPU needed: nothing is called)."""
+import ctypes
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "mpxg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set(re.findall(r"\b(mpxg_[a-z_0-9]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    from mpx_gb300 import build
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert len(declared_functions()) >= 10
+
+
+def test_python_binding_lists_every_export():
+    from mpx_gb300 import _lib
+    assert set(declared_functions()) <= set(_lib.EXPORTS), set(declared_functions()) - set(_lib.EXPORTS)
+
+
+def test_version_and_status_strings():
+    from mpx_gb300 import _lib
+    L = _lib.load()
+    assert L.mpxg_version() >= 100
+    assert L.mpxg_status_string(0) == b"ok"
+    assert L.mpxg_status_string(3) == b"device-memory budget exhausted"
+
+
+def test_struct_layouts_match_header():
+    """ctypes mirrors of the ABI structs have the sizes a C compiler gives them."""
+    from mpx_gb300 import _lib
+    import subprocess, tempfile
+    src = r'''
+#include <stdio.h>
+#include "mpxg.h"
+int main(void) {
+  printf("%zu %zu %zu %zu\n", sizeof(mpxg_problem_desc), sizeof(mpxg_solver_opts), sizeof(mpxg_batch_io), sizeof(mpxg_lq_io));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "s.c")
+        exe = os.path.join(d, "s")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", exe, c], check=True)
+        sizes = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert sizes == [ctypes.sizeof(_lib.ProblemDesc), ctypes.sizeof(_lib.SolverOpts), ctypes.sizeof(_lib.BatchIO),
+                     ctypes.sizeof(_lib.LqIO)]

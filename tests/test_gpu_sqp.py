@@ -1,0 +1,121 @@
+"""CUDA SQP kernel vs the CPU oracle (same algorithm, same inputs)."""
+import numpy as np
+import pytest
+import torch
+
+from mpx_gb300 import problem as P
+from mpx_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+MODELS = [P.MODEL_SRBD_RPY12, P.MODEL_SRBD_QUAT13, P.MODEL_BIPED_WRENCH12]
+
+
+def workload(model, B, horizons, seed):
+    if model == P.MODEL_BIPED_WRENCH12:
+        return biped_workload(B, horizons, seed)
+    return P.quadruped_workload(B, horizons=horizons, seed=seed, model=model, v_range=(-1, 1), random_phase=True)
+
+
+def biped_workload(B, horizons, seed):
+    return P.biped_workload(B, horizons=horizons, seed=seed)
+
+
+def gpu_solve(wl, opts, plain=False, want_gains=True):
+    s = Solver(wl.desc, opts, n_max=wl.n_max, batch_max=wl.batch)
+    out = s.solve(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon, plain=plain,
+                  want_gains=want_gains)
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items() if not k.startswith("_")}
+    s.close()
+    return res
+
+
+def rel_err(a, b, horizon, kind):
+    """max |a-b| over the valid rows of each instance, relative to max |b|."""
+    err, scale = 0.0, 0.0
+    for i, N in enumerate(horizon):
+        rows = N + 1 if kind == "x" else N
+        err = max(err, np.abs(a[i, :rows] - b[i, :rows]).max())
+        scale = max(scale, np.abs(b[i, :rows]).max())
+    return err / max(scale, 1e-12)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_one_iteration_matches_oracle_fp64(oracle, cuda, model):
+    wl = workload(model, 8, (10, 20), seed=11)
+    opts = P.SolverOptions(sqp_iters=1)
+    g = gpu_solve(wl, opts)
+    o = oracle.sqp_solve(wl.desc, opts, wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+    for key, kind in (("X", "x"), ("U", "u"), ("V", "x"), ("k", "u")):
+        e = rel_err(g[key], o[key], wl.horizon, kind)
+        assert e < 1e-4, (key, e)
+    e = rel_err(g["K"], o["K"], wl.horizon, "u")
+    assert e < 1e-4, ("K", e)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_five_iterations_match_oracle(oracle, cuda, model):
+    wl = workload(model, 8, (25, 50), seed=12)
+    opts = P.SolverOptions(sqp_iters=5)
+    g = gpu_solve(wl, opts)
+    o = oracle.sqp_solve(wl.desc, opts, wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+    ex = rel_err(g["X"], o["X"], wl.horizon, "x")
+    eu = rel_err(g["U"], o["U"], wl.horizon, "u")
+    assert ex < 1e-3 and eu < 1e-2, (ex, eu)
+    # the GPU result is as good a KKT point as the FP64 one (evaluated in FP64)
+    kg = oracle.kkt_residual(wl.desc, wl.x0, g["X"], g["U"], g["V"], wl.reference, wl.parameter, wl.W, wl.horizon)
+    assert np.all(kg[:, 2] <= np.maximum(2.0 * o["kkt"][:, 2], 1e-4)), (kg[:, 2], o["kkt"][:, 2])
+    assert np.all(g["status"] & 1 == 0)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_device_kkt_matches_fp64_evaluation(oracle, cuda, model):
+    wl = workload(model, 6, (20,), seed=13)
+    g = gpu_solve(wl, P.SolverOptions(sqp_iters=3))
+    kg = oracle.kkt_residual(wl.desc, wl.x0, g["X"], g["U"], g["V"], wl.reference, wl.parameter, wl.W, wl.horizon)
+    np.testing.assert_allclose(g["kkt"][:, 0], kg[:, 0], rtol=0.05, atol=2e-5)
+    np.testing.assert_allclose(g["kkt"][:, 1], kg[:, 1], rtol=0.05, atol=2e-5)
+
+
+def test_plain_path_is_bitwise_identical(cuda):
+    wl = workload(P.MODEL_SRBD_RPY12, 6, (20, 40), seed=14)
+    opts = P.SolverOptions(sqp_iters=3)
+    a = gpu_solve(wl, opts, plain=False)
+    b = gpu_solve(wl, opts, plain=True)
+    for k in ("X", "U", "V", "kkt", "status"):
+        for i, N in enumerate(wl.horizon):
+            rows = N + 1 if k in ("X", "V") else N
+            if k in ("kkt", "status"):
+                assert np.array_equal(a[k][i], b[k][i]), k
+            else:
+                assert np.array_equal(a[k][i, :rows], b[k][i, :rows]), k
+
+
+def test_batch_mix_invariance(cuda):
+    """Each instance's result is identical alone and inside a mixed batch."""
+    wl = workload(P.MODEL_SRBD_RPY12, 12, (25, 50, 100), seed=15)
+    opts = P.SolverOptions(sqp_iters=5)
+    full = gpu_solve(wl, opts)
+    for i in (0, 5, 11):
+        sub = P.Workload(wl.desc, wl.x0[i:i + 1], wl.X0[i:i + 1], wl.U0[i:i + 1], wl.V0[i:i + 1],
+                         wl.reference[i:i + 1], wl.parameter[i:i + 1], wl.W[i:i + 1], wl.horizon[i:i + 1])
+        one = gpu_solve(sub, opts)
+        N = wl.horizon[i]
+        assert np.array_equal(one["X"][0, :N + 1], full["X"][i, :N + 1])
+        assert np.array_equal(one["U"][0, :N], full["U"][i, :N])
+        assert np.array_equal(one["V"][0, :N + 1], full["V"][i, :N + 1])
+
+
+def test_in_place_warm_start(cuda):
+    """X_in may alias X (the reference rebinds X0 = shifted X every tick)."""
+    wl = workload(P.MODEL_SRBD_RPY12, 4, (20,), seed=16)
+    opts = P.SolverOptions(sqp_iters=2)
+    ref = gpu_solve(wl, opts)
+    s = Solver(wl.desc, opts, n_max=wl.n_max, batch_max=4)
+    X = torch.tensor(wl.X0, device="cuda"); U = torch.tensor(wl.U0, device="cuda"); V = torch.tensor(wl.V0, device="cuda")
+    out = s.empty_outputs(4)
+    out["X"], out["U"], out["V"] = X, U, V
+    s.solve(wl.x0, X, U, V, wl.reference, wl.parameter, wl.W, wl.horizon, out=out)
+    torch.cuda.synchronize()
+    assert np.array_equal(X.cpu().numpy(), ref["X"])
