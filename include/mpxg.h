@@ -193,6 +193,20 @@ typedef struct {
 size_t mpxg_lqr_workspace_bytes(int batch, int N, int n, int m, int method);
 mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method);
 
+/* Allocation-free batched solve.  No counterpart in the reference.  For
+ * callers that cannot allocate device memory when they solve (a real-time
+ * loop that forbids cudaMalloc after start-up, or a plugin host that hands
+ * over only input and output buffers): no handle, same inputs and outputs as
+ * mpxg_solve, scratch taken from a 64 MiB static device array that every GPU
+ * loading this library holds until exit.  The array must hold one warp's
+ * scratch per SM, else the call is rejected (MPXG_ERR_INVALID_ARG; for the
+ * 12-state models n_max up to ~150 on a 152-SM GB300).  All calls share that array: calls that overlap on the GPU race,
+ * so serialise them on one stream.  The first call on a device looks up the
+ * array's device address; make it before any stream capture.  Errors are
+ * reported through mpxg_last_error(NULL). */
+mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* desc, const mpxg_solver_opts* opts, void* stream,
+                               const mpxg_batch_io* io);
+
 /* Last error message of a handle (or of the library when h is NULL). */
 const char* mpxg_last_error(const mpxg_handle* h);
 const char* mpxg_status_string(int status);

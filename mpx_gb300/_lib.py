@@ -57,7 +57,7 @@ class LqIO(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
 
 _lib = None
 
@@ -111,6 +111,9 @@ def load(build_if_missing=True):
     L.mpxg_lqr_workspace_bytes.restype = ctypes.c_size_t
     L.mpxg_lqr_solve.argtypes = [vp, ctypes.POINTER(LqIO), ctypes.c_int]
     L.mpxg_lqr_solve.restype = ctypes.c_int
+    L.mpxg_solve_noalloc.argtypes = [ctypes.POINTER(ProblemDesc), ctypes.POINTER(SolverOpts), vp,
+                                     ctypes.POINTER(BatchIO)]
+    L.mpxg_solve_noalloc.restype = ctypes.c_int
     L.mpxg_last_error.argtypes = [vp]
     L.mpxg_last_error.restype = ctypes.c_char_p
     L.mpxg_status_string.argtypes = [ctypes.c_int]

@@ -4,6 +4,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/mpxg.h"
@@ -329,3 +330,144 @@ mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free batched solve.
+//
+// Some callers cannot allocate device memory at solve time: a host process
+// that must not call cudaMalloc after start-up (real-time control loops, where
+// an allocation can block for milliseconds), or a plugin whose host framework
+// owns every allocation and hands the plugin only the input and output buffers
+// (e.g. an XLA custom call without a workspace).  mpxg_solve_noalloc serves
+// them: it needs no handle and takes its per-warp scratch from the file-scope
+// device array below instead of a cudaMalloc'd workspace.
+//
+// Limits and sharing rules:
+//  - the array is kNoAllocScratchBytes (64 MiB) on every GPU that loads this
+//    library, held until the process exits;
+//  - one warp needs scratch_floats(n_max) floats; the array must hold at
+//    least one warp per SM, otherwise the call is rejected with
+//    MPXG_ERR_INVALID_ARG (for the 12-state models that is n_max <= ~150 on a
+//    152-SM GB300); the persistent grid is shrunk to the warps that fit;
+//  - all calls share the array (and the work counter, which each call clears
+//    on its stream first), so two calls that overlap on the GPU race: issue
+//    them on one stream or order them with events;
+//  - the first call on a device resolves the array's device address with
+//    cudaGetSymbolAddress (a host-side symbol is not a device address); make
+//    that first call before any stream capture.
+// ============================================================================
+static constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchBytes / sizeof(float)];
+static __device__ __align__(256) int g_noalloc_counter[64];
+
+namespace {
+struct NoAllocDevice {
+  bool ready = false;
+  float* scratch = nullptr;
+  int* counter = nullptr;
+  int num_sms = 0;
+};
+constexpr int kMaxDevices = 64;
+NoAllocDevice g_noalloc_dev[kMaxDevices];
+std::mutex g_noalloc_mu;
+
+mpxg_status noalloc_setup(int dev, NoAllocDevice** out) {
+  if (dev < 0 || dev >= kMaxDevices) return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_solve_noalloc: device index");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NoAllocDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaGetSymbolAddress(scratch)");
+    d.scratch = static_cast<float*>(p);
+    e = cudaGetSymbolAddress(&p, g_noalloc_counter);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaGetSymbolAddress(counter)");
+    d.counter = static_cast<int*>(p);
+    e = cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaDeviceGetAttribute");
+    d.ready = true;
+  }
+  *out = &d;
+  return MPXG_OK;
+}
+
+template <class M>
+mpxg_status noalloc_launch(const ModelConst& mc, const SqpParams& sp, cudaStream_t st, const BatchPtrs& bp,
+                           int blocks, int wpb) {
+  const size_t smem = sizeof(WarpSmem<M>) * (size_t)wpb;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(sqp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaFuncSetAttribute");
+  }
+  sqp_kernel<M><<<blocks, wpb * 32, smem, st>>>(mc, sp, bp);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "mpxg_solve_noalloc: launch");
+}
+}  // namespace
+
+extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg_solver_opts* o, void* stream,
+                                          const mpxg_batch_io* io) {
+  if (!d || !o || !io) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: null argument");
+  int nx, nu;
+  if (!model_dims(d->model, &nx, &nu)) return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_solve_noalloc: model id");
+  if (d->n != nx || d->m != nu) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: n/m do not match the model");
+  if (d->n_max < 1 || d->n_max > 4096) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: n_max out of range");
+  if (o->sqp_iters < 0 || o->ls_max_trials < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: bad options");
+  if (!(d->dt > 0.0f) || !(d->mass > 0.0f)) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: dt and mass must be > 0");
+  if (io->batch < 0 || !io->x0 || !io->X_in || !io->U_in || !io->V_in || !io->reference || !io->parameter ||
+      !io->w || !io->X || !io->U || !io->V)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: required pointer is null");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaGetDevice");
+  NoAllocDevice* nd = nullptr;
+  mpxg_status s = noalloc_setup(dev, &nd);
+  if (s != MPXG_OK) return s;
+  const long long stride = scratch_stride_for(d->model, d->n_max);
+  const long long warps_fit = (long long)(kNoAllocScratchBytes / sizeof(float)) / stride;
+  if (warps_fit < nd->num_sms)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG,
+                "mpxg_solve_noalloc: n_max too large: one warp needs " + std::to_string(stride * 4) +
+                    " bytes of scratch, the 64 MiB static array must hold one warp per SM (" +
+                    std::to_string(nd->num_sms) + ")");
+  if (io->batch == 0) return MPXG_OK;
+
+  ModelConst mc;
+  mc.dt = d->dt; mc.mass = d->mass; mc.inv_mass = 1.0f / d->mass; mc.gravity = d->gravity; mc.mu = d->mu;
+  mc.alpha = d->barrier_alpha; mc.sigma = d->barrier_sigma;
+  mc.foot_length = d->foot_length; mc.foot_width = d->foot_width;
+  mc.barrier_kind = d->barrier_kind; mc.barrier_masked = d->barrier_masked;
+  mc.barrier_hess_scale = d->barrier_hess_scale;
+  for (int i = 0; i < 9; ++i) { mc.I[i] = d->inertia[i]; mc.Iinv[i] = d->inertia_inv[i]; }
+  SqpParams sp;
+  sp.sqp_iters = o->sqp_iters; sp.ls_max_trials = o->ls_max_trials; sp.ls_beta = o->ls_beta; sp.ls_eta = o->ls_eta;
+  sp.reg = o->reg; sp.rho0 = o->rho0; sp.ls_skip_tol = o->ls_skip_tol; sp.compute_kkt = o->compute_kkt;
+
+  // persistent grid limited by the warps whose scratch fits in the array
+  int wpb = o->warps_per_block > 0 ? o->warps_per_block : 4;
+  long long max_warps = (long long)nd->num_sms * 2 * wpb;
+  if (max_warps > warps_fit) max_warps = warps_fit;
+  if (wpb > max_warps) wpb = (int)max_warps;
+  long long blocks = max_warps / wpb;
+  const long long need = (io->batch + wpb - 1) / wpb;
+  if (blocks > need) blocks = need;
+  if (blocks < 1) blocks = 1;
+
+  BatchPtrs bp;
+  bp.batch = io->batch; bp.n_max = d->n_max; bp.horizon = io->horizon;
+  bp.x0 = io->x0; bp.X_in = io->X_in; bp.U_in = io->U_in; bp.V_in = io->V_in;
+  bp.ref = io->reference; bp.par = io->parameter; bp.w = io->w;
+  bp.X = io->X; bp.U = io->U; bp.V = io->V; bp.K = io->K; bp.k = io->k; bp.kkt = io->kkt; bp.status = io->status;
+  bp.counter = nd->counter; bp.scratch = nd->scratch; bp.scratch_stride = stride;
+  bp.single_instance = -1;
+
+  cudaStream_t st = (cudaStream_t)stream;
+  e = cudaMemsetAsync(nd->counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaMemsetAsync");
+  switch (d->model) {
+    case MPXG_MODEL_SRBD_QUAT13: return noalloc_launch<ModelQuat13>(mc, sp, st, bp, (int)blocks, wpb);
+    case MPXG_MODEL_SRBD_RPY12: return noalloc_launch<ModelRpy12>(mc, sp, st, bp, (int)blocks, wpb);
+    case MPXG_MODEL_BIPED_WRENCH12: return noalloc_launch<ModelBiped12>(mc, sp, st, bp, (int)blocks, wpb);
+    default: return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_solve_noalloc: model");
+  }
+}
