@@ -1,0 +1,515 @@
+"""Generate golden vectors by executing the reference's own Python source.
+
+JAX and MuJoCo are not installable here, so this script runs the reference
+files (mpx/utils/mpc_utils.py, models.py, objectives.py and
+mpx/config/config_srbd.py, read from a reference checkout) under a small
+stand-in for the parts of `jax`, `jax.numpy` and `mujoco.mjx` they use:
+
+  * jax.numpy   -> numpy with JAX's default dtype rules (float32, int32, Python
+                   scalars weakly typed, integer powers by square-and-multiply,
+                   `.at[...].set(...)`);
+  * jax.lax.fori_loop, jax.jit, jax.vmap -> plain Python equivalents;
+  * jax.jacobian / jax.grad -> central finite differences (only used in the
+                   float64 mode, to evaluate the Gauss-Newton Hessian of
+                   objectives.py:39-75);
+  * mujoco.mjx math (quat_to_mat, quat_integrate, quat_sub, norm, normalize)
+                -> restated from their mathematical definition (third-party
+                   code, not present in the reference tree).
+
+Usage:  python tests/golden/make_golden.py /path/to/reference  [out.npz]
+Output: tests/golden/srbd_golden.npz (committed).  The tests never run this
+script; they only read the .npz.
+"""
+import functools
+import importlib.util
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DT = {"f": np.float32, "i": np.int32}
+
+
+# ----------------------------------------------------------------- array type
+def _canon(a):
+    if isinstance(a, np.ndarray) and not isinstance(a, JArr):
+        if a.dtype == np.float64 and DT["f"] == np.float32:
+            return a.astype(np.float32)
+        if a.dtype.kind in "iu" and a.dtype != DT["i"]:
+            return a.astype(DT["i"])
+    return a
+
+
+def _is_float(a):
+    if isinstance(a, float):
+        return True
+    return isinstance(a, np.ndarray) and a.dtype.kind == "f"
+
+
+def _wrap(x):
+    if isinstance(x, tuple):
+        return tuple(_wrap(v) for v in x)
+    if isinstance(x, np.ndarray):
+        x = _canon(np.asarray(x))
+        return x.view(JArr)
+    if isinstance(x, (np.floating, np.integer, np.bool_)):
+        return _wrap(np.asarray(x))
+    return x
+
+
+def _prep(args, float_op=True):
+    args = [np.asarray(a) if isinstance(a, JArr) else a for a in args]
+    args = [_canon(a) if isinstance(a, np.ndarray) else a for a in args]
+    if float_op and any(_is_float(a) for a in args):
+        args = [a.astype(DT["f"]) if isinstance(a, np.ndarray) and a.dtype.kind in "iub" else a for a in args]
+    return args
+
+
+class _At:
+    def __init__(self, arr):
+        self.arr = arr
+
+    def __getitem__(self, idx):
+        arr = self.arr
+
+        class _Setter:
+            def set(self_inner, v):
+                out = np.array(arr, copy=True)
+                out[idx] = np.asarray(v)
+                return _wrap(out)
+        return _Setter()
+
+
+class JArr(np.ndarray):
+    @property
+    def at(self):
+        return _At(self)
+
+    @property
+    def T(self):
+        return _wrap(np.asarray(self).T)
+
+    def __array_ufunc__(self, ufunc, method, *inputs, **kwargs):
+        logical = ufunc in (np.logical_and, np.logical_or, np.logical_not, np.greater, np.less, np.equal,
+                            np.not_equal, np.greater_equal, np.less_equal)
+        args = _prep(inputs, float_op=not logical)
+        if ufunc is np.power and isinstance(args[1], (int, np.integer)) and not isinstance(args[1], bool):
+            return _wrap(_ipow(args[0], int(args[1])))
+        return _wrap(getattr(ufunc, method)(*args, **kwargs))
+
+    def __matmul__(self, other):
+        return _matmul(self, other)
+
+    def __rmatmul__(self, other):
+        return _matmul(other, self)
+
+    def __pow__(self, p):
+        if isinstance(p, (int, np.integer)):
+            return _wrap(_ipow(np.asarray(self), int(p)))
+        return _wrap(np.power(*_prep([self, p])))
+
+
+def _ipow(x, y):
+    """jax.lax.integer_pow: square-and-multiply."""
+    if y == 0:
+        return np.ones_like(x)
+    acc = None
+    while y > 0:
+        if y & 1:
+            acc = x if acc is None else (acc * x).astype(x.dtype)
+        y >>= 1
+        if y > 0:
+            x = (x * x).astype(x.dtype)
+    return acc
+
+
+def _matmul(a, b):
+    a, b = _prep([a, b])
+    a = np.asarray(a); b = np.asarray(b)
+    vec_a, vec_b = a.ndim == 1, b.ndim == 1
+    A = a[None, :] if vec_a else a
+    Bm = b[:, None] if vec_b else b
+    out = np.zeros((A.shape[0], Bm.shape[1]), dtype=np.result_type(A, Bm))
+    for k in range(A.shape[1]):  # sequential accumulation, one rounding per multiply and add
+        out = (out + (A[:, k:k + 1] * Bm[k:k + 1, :]).astype(out.dtype)).astype(out.dtype)
+    if vec_a:
+        out = out[0]
+    if vec_b:
+        out = out[..., 0]
+    return _wrap(out)
+
+
+# ----------------------------------------------------------------- jax.numpy
+def _np_fn(name, float_op=True):
+    f = getattr(np, name)
+
+    @functools.wraps(f)
+    def g(*args, **kw):
+        return _wrap(f(*_prep(args, float_op), **kw))
+    return g
+
+
+def _array(x, dtype=None):
+    if isinstance(x, (list, tuple)):
+        elems = [np.asarray(e) for e in x]
+        kinds = {e.dtype.kind for e in elems}
+        pyfloat = any(isinstance(e, float) for e in x)
+        if dtype is None:
+            dtype = DT["f"] if ("f" in kinds or pyfloat) else (DT["i"] if kinds <= {"i", "u"} else None)
+        return _wrap(np.array([np.asarray(e) for e in x], dtype=dtype))
+    a = np.asarray(x)
+    if dtype is None:
+        dtype = DT["f"] if a.dtype.kind == "f" else (DT["i"] if a.dtype.kind in "iu" else a.dtype)
+    return _wrap(a.astype(dtype))
+
+
+def _where(c, a, b):
+    a2, b2 = _prep([a, b])
+    if isinstance(a2, (int, np.integer)) and isinstance(b2, (int, np.integer)):
+        return _wrap(np.where(np.asarray(c), np.int32(a2), np.int32(b2)))
+    return _wrap(np.where(np.asarray(c), a2, b2))
+
+
+def _sum(x, axis=None):
+    x = np.asarray(_prep([x])[0])
+    if axis is None:
+        x = x.reshape(-1)
+        acc = np.zeros((), dtype=x.dtype)
+        for v in x:
+            acc = (acc + v).astype(x.dtype)
+        return _wrap(acc)
+    return _wrap(np.sum(x, axis=axis))
+
+
+def _norm(x, axis=None):
+    x = np.asarray(_prep([x])[0])
+    return _wrap(np.sqrt(_sum(x * x)))
+
+
+def _zeros(shape, dtype=None):
+    return _wrap(np.zeros(shape, dtype=dtype or DT["f"]))
+
+
+def _ones(shape, dtype=None):
+    return _wrap(np.ones(shape, dtype=dtype or DT["f"]))
+
+
+def _arange(*a):
+    return _wrap(np.arange(*a, dtype=DT["i"]))
+
+
+def _tile(x, reps):
+    return _wrap(np.tile(np.asarray(_prep([x])[0]), reps))
+
+
+def _concatenate(xs, axis=0):
+    xs = _prep(xs)
+    return _wrap(np.concatenate([np.atleast_1d(np.asarray(v)) for v in xs], axis=axis))
+
+
+def _stack(xs, axis=0):
+    return _wrap(np.stack(_prep(xs), axis=axis))
+
+
+def _block_diag(*ms):
+    ms = [np.atleast_2d(np.asarray(_prep([m])[0])) for m in ms]
+    r = sum(m.shape[0] for m in ms)
+    c = sum(m.shape[1] for m in ms)
+    out = np.zeros((r, c), dtype=np.result_type(*ms))
+    i = j = 0
+    for m in ms:
+        out[i:i + m.shape[0], j:j + m.shape[1]] = m
+        i += m.shape[0]; j += m.shape[1]
+    return _wrap(out)
+
+
+def _fori_loop(lo, hi, body, init):
+    carry = init
+    for i in range(lo, hi):
+        carry = body(i, carry)
+    return carry
+
+
+def _jit(f=None, **kw):
+    if f is None:
+        return lambda g: g
+    return f
+
+
+def _vmap(f, in_axes=0):
+    def g(*args):
+        n = np.asarray(args[0]).shape[0]
+        outs = [f(*[np.asarray(a)[i] for a in args]) for i in range(n)]
+        return _wrap(np.stack([np.asarray(o) for o in outs]))
+    return g
+
+
+def _fd_jacobian(f, argnums=0, h=1e-6):
+    """Central-difference Jacobian (float64 mode only)."""
+    def jac(*args):
+        args = list(args)
+        x = np.asarray(args[argnums], dtype=np.float64)
+        f0 = np.asarray(f(*args))
+        J = np.zeros(f0.shape + x.shape)
+        for idx in np.ndindex(x.shape):
+            e = np.zeros_like(x); e[idx] = h
+            ap = list(args); ap[argnums] = _wrap(x + e)
+            am = list(args); am[argnums] = _wrap(x - e)
+            J[(...,) + idx] = (np.asarray(f(*ap)) - np.asarray(f(*am))) / (2 * h)
+        return _wrap(J)
+    return jac
+
+
+def _fd_grad(f, argnums=0, h=1e-3):
+    """Derivative of a scalar function by the 4th-order five-point stencil
+    (nested for grad(grad(.)), so its error must stay small)."""
+    def d(*args):
+        args = list(args)
+        x = np.asarray(args[argnums], dtype=np.float64)
+
+        def at(s):
+            a = list(args)
+            a[argnums] = _wrap(x + s)
+            return np.asarray(f(*a), dtype=np.float64)
+        return _wrap((-at(2 * h) + 8 * at(h) - 8 * at(-h) + at(-2 * h)) / (12 * h))
+    return d
+
+
+# ----------------------------------------------------------------- mjx math
+def _mjx_norm(x, axis=None):
+    x = np.asarray(x)
+    return _wrap(np.sqrt(np.sum(x * x, axis=axis)))
+
+
+def _normalize_with_norm(x):
+    n = _mjx_norm(x)
+    return _wrap(np.asarray(x) / (n + 1e-6 * (n == 0.0))), n
+
+
+def _quat_mul(u, v):
+    u = np.asarray(u); v = np.asarray(v)
+    return _array([u[0] * v[0] - u[1] * v[1] - u[2] * v[2] - u[3] * v[3],
+                   u[0] * v[1] + u[1] * v[0] + u[2] * v[3] - u[3] * v[2],
+                   u[0] * v[2] - u[1] * v[3] + u[2] * v[0] + u[3] * v[1],
+                   u[0] * v[3] + u[1] * v[2] - u[2] * v[1] + u[3] * v[0]])
+
+
+def _quat_to_mat(q):
+    q = np.asarray(q)
+    o = np.outer(q, q)
+    return _array([[o[0, 0] + o[1, 1] - o[2, 2] - o[3, 3], 2 * (o[1, 2] - o[0, 3]), 2 * (o[1, 3] + o[0, 2])],
+                   [2 * (o[1, 2] + o[0, 3]), o[0, 0] - o[1, 1] + o[2, 2] - o[3, 3], 2 * (o[2, 3] - o[0, 1])],
+                   [2 * (o[1, 3] - o[0, 2]), 2 * (o[2, 3] + o[0, 1]), o[0, 0] - o[1, 1] - o[2, 2] + o[3, 3]]])
+
+
+def _quat_integrate(q, v, dt):
+    v, nrm = _normalize_with_norm(v)
+    angle = np.asarray(nrm) * dt
+    s, c = np.sin(angle / 2), np.cos(angle / 2)
+    qr = _concatenate([_array([c]), _wrap(np.asarray(v) * s)])
+    qn = _quat_mul(q, qr)
+    n, _ = _normalize_with_norm(qn)
+    return n
+
+
+def _quat_sub(u, v):
+    vc = _wrap(np.asarray(v) * np.array([1, -1, -1, -1], dtype=np.asarray(v).dtype))
+    q = _quat_mul(vc, u)
+    axis, sin_a_2 = _normalize_with_norm(np.asarray(q)[1:])
+    angle = 2 * np.arctan2(np.asarray(sin_a_2), np.asarray(q)[0])
+    angle = np.where(angle > np.pi, angle - 2 * np.pi, angle)
+    return _wrap(np.asarray(axis) * angle)
+
+
+# ----------------------------------------------------------------- install
+def install_shim():
+    jnp = types.ModuleType("jax.numpy")
+    for name in ("sqrt", "square", "cos", "sin", "arctan2", "arcsin", "log", "clip", "cross", "logical_and",
+                 "logical_or", "logical_not", "ones_like", "diag", "abs", "maximum", "minimum"):
+        setattr(jnp, name, _np_fn(name, float_op=name not in ("logical_and", "logical_or", "logical_not")))
+    jnp.array = _array
+    jnp.where = _where
+    jnp.sum = _sum
+    jnp.zeros = _zeros
+    jnp.ones = _ones
+    jnp.arange = _arange
+    jnp.tile = _tile
+    jnp.concatenate = _concatenate
+    jnp.stack = _stack
+    jnp.pi = np.pi
+    jnp.float32 = np.float32
+    linalg = types.ModuleType("jax.numpy.linalg")
+    linalg.norm = _norm
+    linalg.inv = lambda a: _wrap(np.linalg.inv(np.asarray(a)))
+    jnp.linalg = linalg
+    jax = types.ModuleType("jax")
+    jax.numpy = jnp
+    jax.jit = _jit
+    jax.vmap = _vmap
+    jax.jacobian = _fd_jacobian
+    jax.grad = _fd_grad
+    jax.config = types.SimpleNamespace(update=lambda *a, **k: None)
+    lax = types.ModuleType("jax.lax")
+    lax.fori_loop = _fori_loop
+    jax.lax = lax
+    scipy = types.ModuleType("jax.scipy")
+    sl = types.ModuleType("jax.scipy.linalg")
+    sl.block_diag = _block_diag
+    scipy.linalg = sl
+    st = types.ModuleType("jax.scipy.spatial")
+    stt = types.ModuleType("jax.scipy.spatial.transform")
+    stt.Rotation = None
+    st.transform = stt
+    scipy.spatial = st
+    jax.scipy = scipy
+    mj = types.ModuleType("mujoco")
+    mjx = types.ModuleType("mujoco.mjx")
+    src = types.ModuleType("mujoco.mjx._src")
+    mth = types.ModuleType("mujoco.mjx._src.math")
+    mth.quat_to_mat = _quat_to_mat
+    mth.quat_integrate = _quat_integrate
+    mth.quat_sub = _quat_sub
+    mth.norm = _mjx_norm
+    mth.normalize_with_norm = _normalize_with_norm
+    src.math = mth
+    mjx._src = src
+    mj.mjx = mjx
+    for name, mod in (("jax", jax), ("jax.numpy", jnp), ("jax.numpy.linalg", linalg), ("jax.lax", lax),
+                      ("jax.scipy", scipy), ("jax.scipy.linalg", sl), ("jax.scipy.spatial", st),
+                      ("jax.scipy.spatial.transform", stt), ("mujoco", mj), ("mujoco.mjx", mjx),
+                      ("mujoco.mjx._src", src), ("mujoco.mjx._src.math", mth)):
+        sys.modules[name] = mod
+
+
+def load(ref_root, rel, name):
+    path = os.path.join(ref_root, rel)
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+# ----------------------------------------------------------------- generation
+def main(ref_root, out):
+    install_shim()
+    cfg = load(ref_root, "mpx/config/config_srbd.py", "ref_config_srbd")
+    mu = load(ref_root, "mpx/utils/mpc_utils.py", "ref_mpc_utils")
+    mo = load(ref_root, "mpx/utils/models.py", "ref_models")
+    ob = load(ref_root, "mpx/utils/objectives.py", "ref_objectives")
+    rng = np.random.default_rng(2024)
+    g = {}
+
+    # --- gait timer (mpc_utils.py:7-14), config_srbd gait and the trot of the benchmark
+    for tag, duty, freq in (("srbd", float(cfg.duty_factor), float(cfg.step_freq)), ("trot", 0.6, 2.0)):
+        lt = rng.uniform(0, 1, (32, 4)).astype(np.float32)
+        g["timer_%s_init" % tag] = lt.copy()
+        cs, ts = [], []
+        cur = _wrap(lt)
+        for _ in range(60):
+            c, cur = mu.timer_run(np.float32(duty), np.float32(freq), cur, np.float32(cfg.dt))
+            cs.append(np.asarray(c)); ts.append(np.asarray(cur))
+        g["timer_%s_contact" % tag] = np.stack(cs).astype(np.int32)
+        g["timer_%s_time" % tag] = np.stack(ts).astype(np.float32)
+        g["timer_%s_params" % tag] = np.array([duty, freq, cfg.dt], dtype=np.float32)
+
+    # --- reference generator (mpc_utils.py:146-270) with config_srbd constants
+    foot0 = np.asarray(cfg.p_legs0, dtype=np.float32)
+    R = 12
+    ins = dict(t_timer=rng.uniform(0, 1, (R, 4)), x=np.zeros((R, 13)), foot=np.zeros((R, 12)),
+               input=np.zeros((R, 7)), contact=rng.integers(0, 2, (R, 4)).astype(np.float64),
+               liftoff=np.zeros((R, 12)))
+    for r in range(R):
+        q = rng.normal(0, 0.1, 4); q[0] += 1; q /= np.linalg.norm(q)
+        ins["x"][r] = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], q, rng.normal(0, 0.3, 6)])
+        ins["foot"][r] = foot0 + rng.normal(0, 0.02, 12)
+        ins["input"][r] = np.concatenate([rng.uniform(-1, 1, 3), rng.uniform(-0.5, 0.5, 3), [cfg.robot_height]])
+        ins["liftoff"][r] = ins["foot"][r] + rng.normal(0, 0.01, 12)
+    for k in ins:
+        ins[k] = ins[k].astype(np.float32)
+        g["refgen_in_" + k] = ins[k]
+    outs = {"reference": [], "parameter": [], "liftoff": [], "foot_ref_dot": []}
+    for r in range(R):
+        ref, par, lo, frd = mu.reference_generator_srbd(
+            cfg.use_terrain_estimator, cfg.N, cfg.dt, cfg.n_contact, float(cfg.mass), _wrap(foot0),
+            _wrap(ins["t_timer"][r]), _wrap(ins["x"][r]), _wrap(ins["foot"][r]), _wrap(ins["input"][r]),
+            np.float32(cfg.duty_factor), np.float32(cfg.step_freq), np.float32(cfg.step_height),
+            _wrap(ins["liftoff"][r]), _wrap(ins["contact"][r]), np.float32(cfg.clearence_speed))
+        outs["reference"].append(np.asarray(ref)); outs["parameter"].append(np.asarray(par))
+        outs["liftoff"].append(np.asarray(lo)); outs["foot_ref_dot"].append(np.asarray(frd))
+    for k, v in outs.items():
+        g["refgen_out_" + k] = np.stack(v).astype(np.float32)
+    g["refgen_cfg"] = np.array([cfg.N, cfg.dt, cfg.mass, cfg.duty_factor, cfg.step_freq, cfg.step_height,
+                                cfg.clearence_speed], dtype=np.float64)
+    g["refgen_foot0"] = foot0
+
+    # --- dynamics (models.py:6-37), float32, config_srbd body
+    mass = float(cfg.mass)
+    inertia = np.asarray(cfg.inertia, dtype=np.float32)
+    inertia_inv = np.linalg.inv(np.asarray(cfg.inertia, dtype=np.float64)).astype(np.float32)
+    D = 40
+    xs, us, pars, xn = [], [], [], []
+    for _ in range(D):
+        q = rng.normal(0, 0.2, 4); q[0] += 1; q /= np.linalg.norm(q)
+        x = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], q, rng.normal(0, 0.5, 6)]).astype(np.float32)
+        u = rng.normal(0, 20, 12).astype(np.float32); u[2::3] += 60
+        par = np.concatenate([rng.integers(0, 2, 4), foot0 + rng.normal(0, 0.05, 12)]).astype(np.float32)
+        parameter = np.stack([par, par])
+        xnext = mo.quadruped_srbd_dynamics(mass, _wrap(inertia), _wrap(inertia_inv), float(cfg.dt), _wrap(x),
+                                           _wrap(u), 0, _wrap(parameter))
+        xs.append(x); us.append(u); pars.append(par); xn.append(np.asarray(xnext))
+    g["dyn_x"], g["dyn_u"], g["dyn_par"], g["dyn_xnext"] = [np.stack(a).astype(np.float32) for a in (xs, us, pars, xn)]
+    g["dyn_const"] = np.array([mass, cfg.dt], dtype=np.float64)
+    g["dyn_inertia"] = np.asarray(cfg.inertia, dtype=np.float64)
+
+    # --- stage cost (objectives.py:15-37), float32, config_srbd W
+    W = np.asarray(cfg.W, dtype=np.float32)
+    C = 40
+    cx, cu, cref, cval, cterm = [], [], [], [], []
+    for i in range(C):
+        q = rng.normal(0, 0.2, 4); q[0] += 1; q /= np.linalg.norm(q)
+        x = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], q, rng.normal(0, 0.5, 6)]).astype(np.float32)
+        u = rng.normal(0, 10, 12).astype(np.float32); u[2::3] = np.abs(u[2::3]) * rng.uniform(0, 6)
+        qr = rng.normal(0, 0.1, 4); qr[0] += 1; qr /= np.linalg.norm(qr)
+        refrow = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], qr, rng.normal(0, 0.5, 6),
+                                 rng.integers(0, 2, 4)]).astype(np.float32)
+        reference = np.stack([refrow, refrow])
+        term = (i % 4 == 3)
+        t = 1 if term else 0
+        val = ob.quadruped_srbd_obj(cfg.n_contact, 1, _wrap(W), _wrap(reference), _wrap(x), _wrap(u), t)
+        cx.append(x); cu.append(u); cref.append(refrow); cval.append(float(np.asarray(val))); cterm.append(term)
+    g["cost_x"], g["cost_u"], g["cost_ref"] = [np.stack(a).astype(np.float32) for a in (cx, cu, cref)]
+    g["cost_val"] = np.array(cval, dtype=np.float32)
+    g["cost_terminal"] = np.array(cterm, dtype=np.int32)
+    g["cost_W"] = W
+
+    # --- Gauss-Newton Hessian (objectives.py:39-75), float64 mode with finite-difference autodiff
+    DT["f"] = np.float64
+    H = 20
+    hx, hu, href, hQ, hR, hM = [], [], [], [], [], []
+    for i in range(H):
+        q = rng.normal(0, 0.2, 4); q[0] += 1; q /= np.linalg.norm(q)
+        x = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], q, rng.normal(0, 0.5, 6)])
+        u = rng.normal(0, 10, 12); u[2::3] = np.abs(u[2::3]) * rng.uniform(0.05, 2.0)
+        qr = rng.normal(0, 0.1, 4); qr[0] += 1; qr /= np.linalg.norm(qr)
+        refrow = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], qr, rng.normal(0, 0.5, 6),
+                                 rng.integers(0, 2, 4)])
+        reference = np.stack([refrow, refrow])
+        Q, Rm, M = ob.quadruped_srbd_hessian_gn(cfg.n_contact, _wrap(W.astype(np.float64)), _wrap(reference),
+                                                _wrap(x), _wrap(u), 0)
+        hx.append(x); hu.append(u); href.append(refrow)
+        hQ.append(np.asarray(Q)); hR.append(np.asarray(Rm)); hM.append(np.asarray(M))
+    DT["f"] = np.float32
+    g["hess_x"], g["hess_u"], g["hess_ref"] = [np.stack(a) for a in (hx, hu, href)]
+    g["hess_Q"], g["hess_R"], g["hess_M"] = [np.stack(a) for a in (hQ, hR, hM)]
+    np.savez_compressed(out, **g)
+    print("wrote", out, {k: v.shape for k, v in g.items()})
+
+
+if __name__ == "__main__":
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPX_REFERENCE", "")
+    out = sys.argv[2] if len(sys.argv) > 2 else os.path.join(HERE, "srbd_golden.npz")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "mpx")):
+        sys.exit("usage: make_golden.py <reference checkout containing mpx/> [out.npz]")
+    main(ref_root, out)

@@ -86,3 +86,38 @@ def test_shift_matches_host(cuda):
         assert np.array_equal(Xd[b, :N + 1].cpu().numpy(), Xe[b, :N + 1])
         assert np.array_equal(Ud[b, :N].cpu().numpy(), Ue[b, :N])
         assert np.array_equal(Vd[b, :N + 1].cpu().numpy(), Ve[b, :N + 1])
+
+
+def test_refgen_and_timer_match_golden(cuda):
+    """CUDA gait timer and reference generator against vectors produced by the
+    reference's own source (tests/golden/make_golden.py)."""
+    import os
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "srbd_golden.npz"))
+    L = _lib.load()
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    for tag in ("srbd", "trot"):
+        duty, freq, dt = [float(v) for v in G["timer_%s_params" % tag]]
+        lt = torch.tensor(G["timer_%s_init" % tag], device="cuda")
+        ct = torch.empty(lt.shape, dtype=torch.int32, device="cuda")
+        for k in range(G["timer_%s_contact" % tag].shape[0]):
+            assert L.mpxg_timer_run(None, lt.shape[0], 4, duty, freq, dt, p(lt), p(ct)) == 0
+            torch.cuda.synchronize()
+            assert np.array_equal(ct.cpu().numpy(), G["timer_%s_contact" % tag][k])
+            assert np.array_equal(lt.cpu().numpy().view(np.uint32), G["timer_%s_time" % tag][k].view(np.uint32))
+    N, dt, mass, duty, freq, sh, cl = [float(v) for v in G["refgen_cfg"]]
+    N = int(N)
+    R = G["refgen_in_x"].shape[0]
+    tl = [torch.tensor(G["refgen_in_" + k], device="cuda") for k in ("t_timer", "x", "foot", "input", "contact", "liftoff")]
+    refd = torch.zeros(R, N + 1, 17, device="cuda"); pard = torch.zeros(R, N + 1, 16, device="cuda")
+    frdd = torch.zeros(R, N + 1, 12, device="cuda")
+    f0 = (ctypes.c_float * 12)(*G["refgen_foot0"].tolist())
+    assert L.mpxg_refgen_srbd(None, R, N, N, dt, f0, duty, freq, sh, cl, *[p(t) for t in tl], p(refd), p(pard),
+                              p(frdd)) == 0
+    torch.cuda.synchronize()
+    gref, gpar = G["refgen_out_reference"], G["refgen_out_parameter"]
+    assert np.array_equal(refd.cpu().numpy()[:, :, 13:17], gref[:, :, 13:17])
+    assert np.array_equal(pard.cpu().numpy()[:, :, 0:4], gpar[:, :, 0:4])
+    np.testing.assert_allclose(refd.cpu().numpy(), gref, rtol=2e-6, atol=2e-6)
+    np.testing.assert_allclose(pard.cpu().numpy(), gpar, rtol=2e-6, atol=2e-6)
+    np.testing.assert_allclose(frdd.cpu().numpy(), G["refgen_out_foot_ref_dot"], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(tl[5].cpu().numpy(), G["refgen_out_liftoff"], rtol=2e-6, atol=2e-6)
