@@ -93,3 +93,110 @@ __device__ __forceinline__ int warp_or(int v) {
 }
 
 }  // namespace mpxg
+
+namespace mpxg {
+
+// Forward-mode dual number with K tangents: one lane propagates K directional
+// derivatives at once (K columns of a Jacobian per model evaluation).
+template <int K>
+struct DK {
+  float v;
+  float d[K];
+};
+template <int K> __device__ __forceinline__ DK<K> dk_const(float v) {
+  DK<K> r; r.v = v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = 0.0f;
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator+(const DK<K>& a, const DK<K>& b) {
+  DK<K> r; r.v = a.v + b.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k];
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator-(const DK<K>& a, const DK<K>& b) {
+  DK<K> r; r.v = a.v - b.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k];
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator-(const DK<K>& a) {
+  DK<K> r; r.v = -a.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = -a.d[k];
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator*(const DK<K>& a, const DK<K>& b) {
+  DK<K> r; r.v = a.v * b.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator/(const DK<K>& a, const DK<K>& b) {
+  DK<K> r;
+  const float ib = 1.0f / b.v;
+  r.v = a.v * ib;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator+(const DK<K>& a, float b) { DK<K> r = a; r.v += b; return r; }
+template <int K> __device__ __forceinline__ DK<K> operator+(float b, const DK<K>& a) { DK<K> r = a; r.v += b; return r; }
+template <int K> __device__ __forceinline__ DK<K> operator-(const DK<K>& a, float b) { DK<K> r = a; r.v -= b; return r; }
+template <int K> __device__ __forceinline__ DK<K> operator-(float b, const DK<K>& a) {
+  DK<K> r; r.v = b - a.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = -a.d[k];
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator*(const DK<K>& a, float b) {
+  DK<K> r; r.v = a.v * b;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b;
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> operator*(float b, const DK<K>& a) { return a * b; }
+template <int K> __device__ __forceinline__ DK<K> operator/(const DK<K>& a, float b) { return a * (1.0f / b); }
+template <int K> __device__ __forceinline__ DK<K> operator/(float b, const DK<K>& a) {
+  DK<K> r; r.v = b / a.v;
+  const float s = -r.v / a.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = s * a.d[k];
+  return r;
+}
+template <int K> __device__ __forceinline__ float sval(const DK<K>& x) { return x.v; }
+template <int K> __device__ __forceinline__ DK<K> s_sqrt(const DK<K>& x) {
+  DK<K> r; r.v = sqrtf(x.v);
+  const float s = 0.5f / r.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = x.d[k] * s;
+  return r;
+}
+template <int K> __device__ __forceinline__ void s_sincos(const DK<K>& x, DK<K>* s, DK<K>* c) {
+  float sv, cv;
+  sincosf(x.v, &sv, &cv);
+  s->v = sv; c->v = cv;
+#pragma unroll
+  for (int k = 0; k < K; ++k) { s->d[k] = cv * x.d[k]; c->d[k] = -sv * x.d[k]; }
+}
+template <int K> __device__ __forceinline__ DK<K> s_atan2(const DK<K>& y, const DK<K>& x) {
+  DK<K> r; r.v = atan2f(y.v, x.v);
+  const float den = 1.0f / (x.v * x.v + y.v * y.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = (x.v * y.d[k] - y.v * x.d[k]) * den;
+  return r;
+}
+template <int K> __device__ __forceinline__ DK<K> s_log(const DK<K>& x) {
+  DK<K> r; r.v = logf(x.v);
+  const float s = 1.0f / x.v;
+#pragma unroll
+  for (int k = 0; k < K; ++k) r.d[k] = x.d[k] * s;
+  return r;
+}
+template <> __device__ __forceinline__ DK<1> s_const<DK<1>>(float v) { return dk_const<1>(v); }
+template <> __device__ __forceinline__ DK<2> s_const<DK<2>>(float v) { return dk_const<2>(v); }
+template <> __device__ __forceinline__ DK<3> s_const<DK<3>>(float v) { return dk_const<3>(v); }
+template <> __device__ __forceinline__ DK<4> s_const<DK<4>>(float v) { return dk_const<4>(v); }
+
+}  // namespace mpxg

@@ -227,6 +227,9 @@ __device__ __forceinline__ float cone(float mu, const float* f, float* gc, float
 struct ModelQuat13 {
   static constexpr int NX = 13, NU = 12, NREF = 17, NPAR = 16, LEGS = 4, COFF = 13;
   static constexpr bool IDENT_RES = false;
+  static constexpr int QOFF = 3;  // state indices 3..6 (the quaternion) map to residual rows 3..5
+  // residual row carrying the weight of state index j (j outside the quaternion)
+  __device__ static int wrow(int j) { return j < 3 ? j : j - 1; }
   template <class S>
   __device__ static void dynamics(const ModelConst& mc, const S* x, const S* u, const float* par, S* xn) {
     S F[3], Mw[3], R[9];
@@ -249,6 +252,8 @@ struct ModelQuat13 {
 struct ModelRpy12 {
   static constexpr int NX = 12, NU = 12, NREF = 16, NPAR = 16, LEGS = 4, COFF = 12;
   static constexpr bool IDENT_RES = true;
+  static constexpr int QOFF = 0;
+  __device__ static int wrow(int j) { return j; }
   template <class S>
   __device__ static void dynamics(const ModelConst& mc, const S* x, const S* u, const float* par, S* xn) {
     S F[3], Mw[3], R[9], rd[3];
@@ -269,6 +274,8 @@ struct ModelRpy12 {
 struct ModelBiped12 {
   static constexpr int NX = 12, NU = 12, NREF = 14, NPAR = 8, LEGS = 2, COFF = 12;
   static constexpr bool IDENT_RES = true;
+  static constexpr int QOFF = 0;
+  __device__ static int wrow(int j) { return j; }
   template <class S>
   __device__ static void dynamics(const ModelConst& mc, const S* x, const S* u, const float* par, S* xn) {
     S F[3], Mw[3], R[9], rd[3];
@@ -405,6 +412,66 @@ __device__ __forceinline__ void barrier_lane(const ModelConst& mc, int a, const 
       }
     }
     *grad = g_acc;
+  }
+}
+
+// Barrier terms of leg/foot `leg`: cost value (1/2 included), gradient over
+// the leg's LD controls and its LD x LD Hessian model (kind 0: the reference's
+// Gauss-Newton J^T diag(clip(B'')*contact) J; kind 1: exact second derivative).
+template <class M, int LD>
+__device__ __forceinline__ void barrier_leg(const ModelConst& mc, int leg, const float* u, const float* ref, float* val,
+                                            float* grad, float (*H)[LD]) {
+  const float cont = ref[M::COFF + leg];
+  const float mcost = mc.barrier_masked ? cont : 1.0f;
+  float gc[3], hxx, hxy, hyy;
+#pragma unroll
+  for (int a = 0; a < LD; ++a) {
+    grad[a] = 0.0f;
+#pragma unroll
+    for (int b = 0; b < LD; ++b) H[a][b] = 0.0f;
+  }
+  if (LD == 3) {
+    const float* f = u + 3 * leg;
+    const float c = cone(mc.mu, f, gc, &hxx, &hxy, &hyy);
+    float v, g, h, cv;
+    barrier_terms(mc, c, mcost, cont, &v, &g, &h, &cv);
+    *val = v;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      grad[a] = g * gc[a];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) H[a][b] = h * gc[a] * gc[b];
+    }
+    H[0][0] += -cv * hxx; H[0][1] += -cv * hxy; H[1][0] += -cv * hxy; H[1][1] += -cv * hyy;
+  } else {
+    const float* F = u + 6 * leg;
+    const float* T = u + 6 * leg + 3;
+    const float hl = 0.5f * mc.foot_length, hw = 0.5f * mc.foot_width;
+    const float mz = mc.mu * 0.5f * fminf(mc.foot_length, mc.foot_width);
+    float cs[7];
+    cs[0] = cone(mc.mu, F, gc, &hxx, &hxy, &hyy);
+    cs[1] = hl * F[2] - T[1]; cs[2] = hl * F[2] + T[1];
+    cs[3] = hw * F[2] - T[0]; cs[4] = hw * F[2] + T[0];
+    cs[5] = mz * F[2] - T[2]; cs[6] = mz * F[2] + T[2];
+    const float G[7][6] = {{gc[0], gc[1], gc[2], 0.f, 0.f, 0.f},
+                           {0.f, 0.f, hl, 0.f, -1.f, 0.f}, {0.f, 0.f, hl, 0.f, 1.f, 0.f},
+                           {0.f, 0.f, hw, -1.f, 0.f, 0.f}, {0.f, 0.f, hw, 1.f, 0.f, 0.f},
+                           {0.f, 0.f, mz, 0.f, 0.f, -1.f}, {0.f, 0.f, mz, 0.f, 0.f, 1.f}};
+    float vs = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      float v, g, h, cv;
+      barrier_terms(mc, cs[k], mcost, cont, &v, &g, &h, &cv);
+      vs += v;
+#pragma unroll
+      for (int a = 0; a < LD; ++a) {
+        grad[a] += g * G[k][a];
+#pragma unroll
+        for (int b = 0; b < LD; ++b) H[a][b] += h * G[k][a] * G[k][b];
+      }
+      if (k == 0) { H[0][0] += -cv * hxx; H[0][1] += -cv * hxy; H[1][0] += -cv * hxy; H[1][1] += -cv * hyy; }
+    }
+    *val = vs;
   }
 }
 

@@ -1,21 +1,24 @@
-// Fused primal-dual SQP solve of one MPC instance per warp.
+// Fused primal-dual SQP solve, one MPC instance per warp.
 //
-// One warp owns one instance for the whole solve (all SQP iterations):
-//   backward sweep  t = N..0: per stage, lane j evaluates the dynamics with a
-//                   dual number seeded on direction j (column j of [A|B]),
-//                   lane JA = n+m evaluates the defect c = f(x,u) - x_{t+1};
-//                   the warp forms the augmented stage matrix
-//                       H = G + F^T P F      (F = [A B c; 0 0 1], G = cost model)
-//                   with lane j holding column j, and eliminates the m control
-//                   pivots by Gauss-Jordan: what remains is the new value
-//                   function (P, p) and the gains (K, k) -- one Riccati step.
-//   forward sweep   t = 0..N: du = K dx + k, dx+ = A dx + B du + c, and the
-//                   costates lam = P dx + p (the new duals).
-//   merit search    stage-parallel evaluation (lane = stage) of the augmented
-//                   Lagrangian merit phi = J + V.c + rho/2 |c|^2 at trial steps.
-// The reference solves the same Newton-KKT system of its multiple-shooting SQP
-// (call sites mpx/utils/mpc_wrapper_srbd.py:124-132; the solver module itself is
-// absent from the reference tree).
+// Each SQP iteration (the Newton-KKT step of the reference's multiple-shooting
+// SQP; call sites mpx/utils/mpc_wrapper_srbd.py:124-132, solver module absent
+// from the reference tree) runs four phases inside one warp:
+//
+//  1. linearise   lane = stage (32 stages at a time): dynamics Jacobian [A|B]
+//                 by forward-mode dual numbers with several tangents per pass,
+//                 defect c = f(x,u) - x+, stage cost, gradient, barrier blocks.
+//                 Results go to the warp's scratch (L2-resident).
+//  2. backward    lane = column of the augmented stage matrix
+//                     H = G + F^T P F,   F = [A B c; 0 0 1]
+//                 built from the scratch, then the m control pivots are
+//                 eliminated by 4x4 block Gauss-Jordan: what remains is the new
+//                 value function (P, p) and the gains (K, k).  The closed-loop
+//                 map (A + BK, Bk + c) is stored for phase 3.
+//  3. forward     dx+ = (A+BK) dx + (Bk+c), du = K dx + k and the costates
+//                 lam = P dx + p (the new duals); column partials are reduced
+//                 through shared memory.
+//  4. merit       stage-parallel augmented-Lagrangian merit
+//                 phi = J + V.c + rho/2 |c|^2 with backtracking, then the step.
 #pragma once
 #include "models.cuh"
 
@@ -35,72 +38,309 @@ struct BatchPtrs {
   const float *x0, *X_in, *U_in, *V_in, *ref, *par, *w;
   float *X, *U, *V, *K, *k, *kkt;
   int* status;
-  int* counter;            // work-queue head (zeroed before each launch)
-  float* scratch;          // per-warp scratch
+  int* counter;              // work-queue head (zeroed before each launch)
+  float* scratch;            // per-warp scratch
   long long scratch_stride;  // floats per warp
-  int single_instance;     // >= 0: solve only this instance with warp 0 (plain path)
+  int single_instance;       // >= 0: solve only this instance with warp 0 (plain path)
 };
+
+constexpr int rup4(int v) { return (v + 3) / 4 * 4; }
+
+// n floats from a 16-byte aligned address into registers (float4 where possible)
+template <int N>
+__device__ __forceinline__ void ld_vec(const float* __restrict__ src, float* dst) {
+#pragma unroll
+  for (int q = 0; q < N / 4; ++q) {
+    const float4 v = *reinterpret_cast<const float4*>(src + 4 * q);
+    dst[4 * q] = v.x; dst[4 * q + 1] = v.y; dst[4 * q + 2] = v.z; dst[4 * q + 3] = v.w;
+  }
+#pragma unroll
+  for (int r = (N / 4) * 4; r < N; ++r) dst[r] = src[r];
+}
+template <int N>
+__device__ __forceinline__ void st_vec(float* __restrict__ dst, const float* src) {
+#pragma unroll
+  for (int q = 0; q < N / 4; ++q)
+    *reinterpret_cast<float4*>(dst + 4 * q) = make_float4(src[4 * q], src[4 * q + 1], src[4 * q + 2], src[4 * q + 3]);
+#pragma unroll
+  for (int r = (N / 4) * 4; r < N; ++r) dst[r] = src[r];
+}
 
 template <class M>
 struct Dims {
   static constexpr int NX = M::NX, NU = M::NU;
-  static constexpr int NZ = NX + NU + 1;   // augmented columns: x, u, affine
-  static constexpr int JA = NX + NU;       // affine column / lane
-  static constexpr int NP = NX + 1;        // value-function rows: x, affine
-  static constexpr int LDP = (NP + 3) / 4 * 4;
+  static constexpr int NZ = NX + NU + 1;      // augmented columns: x, u, affine
+  static constexpr int JA = NX + NU;          // affine column / lane
+  static constexpr int NP = NX + 1;           // value-function rows: x, affine
+  static constexpr int LDP = rup4(NP);        // shared / scratch column stride of P
+  static constexpr int FS = rup4(NX);         // scratch column stride of F
+  static constexpr int LD = (M::LEGS == 4) ? 3 : 6;  // controls per leg / foot
+  static constexpr int QB = M::IDENT_RES ? 0 : 4;    // quaternion Gauss-Newton block
+  // per-stage cost data: gradient (NX+NU), barrier blocks, quaternion block, cost value
+  static constexpr int G_GRAD = 0, G_HB = NX + NU, G_QQ = G_HB + M::LEGS * LD * LD, G_L = G_QQ + QB * QB;
+  static constexpr int GS = rup4(G_L + 1);
+  static constexpr int RS = rup4(NU + NX);    // forward-sweep partial row
+  static constexpr int TANG = 2;              // tangents per dual-number pass
 };
 
-// Per-warp shared memory.
 template <class M>
 struct __align__(16) WarpSmem {
   typedef Dims<M> D;
-  float xs[16], us[16], xn[16], ref[20], par[16];
   float w[24];
   float P[D::NP * D::LDP];     // value function of stage t+1, column-major
   float Praw[D::NP * D::LDP];  // unsymmetrised new value function
-  float F[D::NZ * D::LDP];     // columns of the augmented dynamics F
-  float col[32];               // pivot column broadcast
-  float g[32];                 // cost gradient gather
-  float J[D::NX * 12];         // state-residual Jacobian columns
-  float dx[16], du[16];
+  float F[D::NZ * D::LDP];     // columns of the augmented dynamics F of stage t
+  float CT[D::NZ * 4];         // pivot block columns, row-interleaved
+  float red[(D::NX + 1) * D::RS];
+  float G[D::GS];              // cost data of stage t
+  float dx[16];
 };
 
-// Floats of per-warp scratch for horizon n_max.
+// Cooperative, coalesced copy of one contiguous scratch block (FLOATS floats,
+// a multiple of 4) into per-lane float4 registers: lane l holds float4 l, l+32, ...
+template <int FLOATS>
+struct BlockRegs {
+  static constexpr int Q = FLOATS / 4;
+  static constexpr int PER = (Q + 31) / 32;
+  float4 v[PER];
+  __device__ __forceinline__ void load(const float* src, int lane) {
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+      const int q = lane + 32 * r;
+      if (q < Q) v[r] = *reinterpret_cast<const float4*>(src + 4 * q);
+    }
+  }
+  // store with the block's column stride CS remapped to the shared stride SS
+  template <int CS, int SS>
+  __device__ __forceinline__ void store_cols(float* dst, int lane) const {
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+      const int q = lane + 32 * r;
+      if (q < Q) {
+        const int col = (4 * q) / CS, row = (4 * q) - col * CS;
+        *reinterpret_cast<float4*>(dst + col * SS + row) = v[r];
+      }
+    }
+  }
+};
+
 template <class M>
 __host__ __device__ inline long long scratch_floats(int n_max) {
   typedef Dims<M> D;
   long long f = 0;
-  f += (long long)n_max * D::NZ * D::NX;          // F columns (rows 0..NX-1)
-  f += (long long)n_max * D::NP * M::NU;          // [K | k] column-major
-  f += (long long)(n_max + 1) * D::NP * D::NP;    // value functions
-  f += (long long)(n_max + 1) * (D::NX + D::NU);  // cost gradients
-  f += (long long)(n_max + 1) * D::NX * 2;        // dX, lam
-  f += (long long)n_max * M::NU;                  // dU
+  f += (long long)n_max * D::NZ * D::FS;           // F columns (later A+BK, Bk+c) and defects
+  f += (long long)(n_max + 1) * D::GS;             // cost data
+  f += (long long)n_max * D::NP * M::NU;           // [K | k] column-major
+  f += (long long)(n_max + 1) * D::NP * D::LDP;    // value functions
+  f += (long long)(n_max + 1) * D::NX * 2;         // dX, lam
+  f += (long long)n_max * M::NU;                   // dU
   return (f + 31) / 32 * 32;
 }
 
 template <class M>
 struct Scratch {
   typedef Dims<M> D;
-  float *F, *K, *P, *G, *dX, *L, *dU;
+  float *F, *G, *K, *P, *dX, *L, *dU;
   __device__ Scratch(float* base, int n_max) {
     F = base;
-    K = F + (size_t)n_max * D::NZ * D::NX;
+    G = F + (size_t)n_max * D::NZ * D::FS;
+    K = G + (size_t)(n_max + 1) * D::GS;
     P = K + (size_t)n_max * D::NP * M::NU;
-    G = P + (size_t)(n_max + 1) * D::NP * D::NP;
-    dX = G + (size_t)(n_max + 1) * (D::NX + D::NU);
+    dX = P + (size_t)(n_max + 1) * D::NP * D::LDP;
     L = dX + (size_t)(n_max + 1) * D::NX;
     dU = L + (size_t)(n_max + 1) * D::NX;
   }
 };
 
-// Merit contribution of constraint/stage index t (0..N) at step alpha:
-// l_t + V~_t . c~_t + rho/2 |c~_t|^2 (double-free, one lane).
+// ----------------------------------------------------------------- phase 1
+// Stage t (0..N) on one lane.  STORE (KKT = false): write the stage's F
+// columns and cost data to the scratch.  KKT = true: accumulate the primal /
+// dual KKT residuals of the current iterate instead.
+template <class M, bool KKT>
+__device__ __forceinline__ void lin_stage(const ModelConst& mc, int t, int N, const float* x0, const float* X,
+                                          const float* U, const float* V, const float* ref, const float* par,
+                                          const float* w, const Scratch<M>& s, float* lsum, float* rp, float* rd,
+                                          float* gm) {
+  typedef Dims<M> D;
+  constexpr int NX = D::NX, NU = D::NU, JA = D::JA, FS = D::FS, LD = D::LD, TK = D::TANG;
+  const bool term = (t == N);
+  const float* rr = ref + t * M::NREF;
+  float x[NX], u[NU], xn[NX];
+#pragma unroll
+  for (int i = 0; i < NX; ++i) x[i] = X[t * NX + i];
+#pragma unroll
+  for (int a = 0; a < NU; ++a) u[a] = term ? 0.0f : U[t * NU + a];
+#pragma unroll
+  for (int i = 0; i < NX; ++i) xn[i] = term ? 0.0f : X[(t + 1) * NX + i];
+  float vn[NX];
+#pragma unroll
+  for (int i = 0; i < NX; ++i) vn[i] = 0.0f;
+  if (KKT) {
+    if (!term) {
+#pragma unroll
+      for (int i = 0; i < NX; ++i) vn[i] = V[(t + 1) * NX + i];
+    }
+    if (t == 0) {
+#pragma unroll
+      for (int i = 0; i < NX; ++i) *rp = fmaxf(*rp, fabsf(x0[i] - x[i]));
+    }
+  }
+  // ---- cost: tracking residual, gradient, Gauss-Newton blocks, barrier
+  float g[NX + NU];
+  float r[12];
+  M::template state_residual<float>(x, rr, r);
+  float l = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 12; ++a) l += w[a] * r[a] * r[a];
+  float Qq[4][4];
+  if (M::IDENT_RES) {
+#pragma unroll
+    for (int i = 0; i < NX; ++i) g[i] = w[i] * r[i];
+  } else {
+    // quaternion rows of the residual Jacobian by one 4-tangent pass
+    DK<4> qd[4], rq[3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      qd[k].v = x[M::QOFF + k];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) qd[k].d[e] = (e == k) ? 1.0f : 0.0f;
+    }
+    quat_sub(qd, rr + 3, rq);
+#pragma unroll
+    for (int i = 0; i < NX; ++i) {
+      if (i >= M::QOFF && i < M::QOFF + 4) {
+        const int k = i - M::QOFF;
+        g[i] = w[3] * r[3] * rq[0].d[k] + w[4] * r[4] * rq[1].d[k] + w[5] * r[5] * rq[2].d[k];
+      } else {
+        const int a = M::wrow(i);
+        g[i] = w[a] * r[a];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        Qq[i][k] = w[3] * rq[0].d[i] * rq[0].d[k] + w[4] * rq[1].d[i] * rq[1].d[k] + w[5] * rq[2].d[i] * rq[2].d[k];
+  }
+  float Hb[M::LEGS][LD][LD];
+  if (!term) {
+#pragma unroll
+    for (int a = 0; a < NU; ++a) { g[NX + a] = w[12 + a] * u[a]; l += w[12 + a] * u[a] * u[a]; }
+    l *= 0.5f;
+#pragma unroll
+    for (int leg = 0; leg < M::LEGS; ++leg) {
+      float v, gb[LD];
+      barrier_leg<M, LD>(mc, leg, u, rr, &v, gb, Hb[leg]);
+      l += v;
+#pragma unroll
+      for (int a = 0; a < LD; ++a) g[NX + LD * leg + a] += gb[a];
+    }
+  } else {
+    l *= 0.5f;
+#pragma unroll
+    for (int a = 0; a < NU; ++a) g[NX + a] = 0.0f;
+#pragma unroll
+    for (int leg = 0; leg < M::LEGS; ++leg)
+#pragma unroll
+      for (int a = 0; a < LD; ++a)
+#pragma unroll
+        for (int b = 0; b < LD; ++b) Hb[leg][a][b] = 0.0f;
+  }
+  *lsum += l;
+  if (!KKT) {
+    float gv[D::GS];
+#pragma unroll
+    for (int i = 0; i < D::GS; ++i) gv[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NX + NU; ++i) gv[D::G_GRAD + i] = g[i];
+#pragma unroll
+    for (int leg = 0; leg < M::LEGS; ++leg)
+#pragma unroll
+      for (int a = 0; a < LD; ++a)
+#pragma unroll
+        for (int b = 0; b < LD; ++b) gv[D::G_HB + (leg * LD + a) * LD + b] = Hb[leg][a][b];
+    if (D::QB) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) gv[D::G_QQ + i * 4 + k] = Qq[i][k];
+    }
+    gv[D::G_L] = l;
+    st_vec<D::GS>(s.G + (size_t)t * D::GS, gv);
+  } else if (term) {
+#pragma unroll
+    for (int i = 0; i < NX; ++i) {
+      *rd = fmaxf(*rd, fabsf(g[i] - V[t * NX + i]));
+      *gm = fmaxf(*gm, fabsf(g[i]));
+    }
+  }
+  if (term) return;
+  // ---- dynamics: defect and Jacobian columns, TK directions per pass
+  const float* pp = par + t * M::NPAR;
+  float* Ft = s.F + (size_t)t * D::NZ * FS;
+#pragma unroll 1
+  for (int p0 = 0; p0 < NX + NU; p0 += TK) {
+    DK<TK> xd[NX], ud[NU], fd[NX];
+#pragma unroll
+    for (int i = 0; i < NX; ++i) {
+      xd[i].v = x[i];
+#pragma unroll
+      for (int k = 0; k < TK; ++k) xd[i].d[k] = (i == p0 + k) ? 1.0f : 0.0f;
+    }
+#pragma unroll
+    for (int a = 0; a < NU; ++a) {
+      ud[a].v = u[a];
+#pragma unroll
+      for (int k = 0; k < TK; ++k) ud[a].d[k] = (NX + a == p0 + k) ? 1.0f : 0.0f;
+    }
+    M::template dynamics<DK<TK>>(mc, xd, ud, pp, fd);
+    if (!KKT) {
+      if (p0 == 0) {
+        float cv[FS];
+#pragma unroll
+        for (int i = 0; i < FS; ++i) cv[i] = (i < NX) ? fd[i < NX ? i : 0].v - xn[i < NX ? i : 0] : 0.0f;
+        st_vec<FS>(Ft + JA * FS, cv);
+      }
+#pragma unroll
+      for (int k = 0; k < TK; ++k) {
+        const int dir = p0 + k;
+        if (dir < NX + NU) {
+          float cv[FS];
+#pragma unroll
+          for (int i = 0; i < FS; ++i) cv[i] = (i < NX) ? fd[i < NX ? i : 0].d[k] : 0.0f;
+          st_vec<FS>(Ft + dir * FS, cv);
+        }
+      }
+    } else {
+      if (p0 == 0) {
+#pragma unroll
+        for (int i = 0; i < NX; ++i) *rp = fmaxf(*rp, fabsf(fd[i].v - xn[i]));
+      }
+#pragma unroll
+      for (int k = 0; k < TK; ++k) {
+        const int dir = p0 + k;
+        if (dir < NX + NU) {
+          float acc = 0.0f, gd = 0.0f, vt = 0.0f;
+#pragma unroll
+          for (int i = 0; i < NX; ++i) acc += fd[i].d[k] * vn[i];
+#pragma unroll
+          for (int i = 0; i < NX + NU; ++i) gd = (i == dir) ? g[i] : gd;
+          if (dir < NX) vt = V[t * NX + dir];
+          *rd = fmaxf(*rd, fabsf(gd + acc - vt));
+          *gm = fmaxf(*gm, fabsf(gd));
+        }
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------- merit
+// l_t + V~_t . c~_t + rho/2 |c~_t|^2 at step alpha, constraint index t (0..N).
 template <class M>
 __device__ __forceinline__ float merit_stage(const ModelConst& mc, int t, int N, float alpha, float rho,
                                              const float* x0, const float* X, const float* U, const float* V,
-                                             const Scratch<M>& s, const float* ref, const float* par, const float* w,
-                                             float* cmax) {
+                                             const Scratch<M>& s, const float* ref, const float* par,
+                                             const float* w) {
   constexpr int NX = M::NX, NU = M::NU;
   float xt[NX], ut[NU], ct[NX];
 #pragma unroll
@@ -111,6 +351,8 @@ __device__ __forceinline__ float merit_stage(const ModelConst& mc, int t, int N,
     for (int a = 0; a < NU; ++a) ut[a] = U[t * NU + a] + alpha * s.dU[t * NU + a];
     l = stage_cost<M>(mc, xt, ut, ref + t * M::NREF, w, false);
   } else {
+#pragma unroll
+    for (int a = 0; a < NU; ++a) ut[a] = 0.0f;
     l = stage_cost<M>(mc, xt, ut, ref + t * M::NREF, w, true);
   }
   if (t == 0) {
@@ -126,98 +368,92 @@ __device__ __forceinline__ float merit_stage(const ModelConst& mc, int t, int N,
 #pragma unroll
     for (int i = 0; i < NX; ++i) ct[i] = fx[i] - xt[i];
   }
-  float vc = 0.0f, cs = 0.0f, cm = 0.0f;
+  float vc = 0.0f, cs = 0.0f;
 #pragma unroll
   for (int i = 0; i < NX; ++i) {
     const float vt = V[t * NX + i] + alpha * (s.L[t * NX + i] - V[t * NX + i]);
     vc += vt * ct[i];
     cs += ct[i] * ct[i];
-    cm = fmaxf(cm, fabsf(ct[i]));
   }
-  *cmax = cm;
   return l + vc + 0.5f * rho * cs;
 }
 
-// Lane j's column of the stage cost model G (rows 0..NZ-1 except the affine
-// row, which the caller fills with the gradient) and gradient entry g_j.
-// Diagonal weights w[24].  terminal: state block only.
-template <class M>
-__device__ __forceinline__ void cost_column(const ModelConst& mc, WarpSmem<M>& sm, int j, bool terminal,
-                                            float* gcol, float* gj) {
-  typedef Dims<M> D;
-  constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ;
+// ----------------------------------------------------------------- block Gauss-Jordan
+// Eliminate the pivot block S = {s0..s0+3} from the column this lane holds (h):
+// rows S <- D^-1 h[S], other rows h[i] -= H[i,S] D^-1 h[S], with D = H[S,S]
+// (SPD) factored by Cholesky on every lane.
+template <int NZ>
+__device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT, int* status) {
+  __syncwarp();
+  if (lane >= s0 && lane < s0 + 4) {
+    const int k = lane - s0;
 #pragma unroll
-  for (int i = 0; i < NZ; ++i) gcol[i] = 0.0f;
-  *gj = 0.0f;
-  if (j < NX) {
-    // residual Jacobian column j and residual value
-    float rj[12], rv[12];
-    if (M::IDENT_RES) {
+    for (int i = 0; i < NZ; ++i) CT[i * 4 + k] = h[i];
+  }
+  __syncwarp();
+  float Dm[4][4];
 #pragma unroll
-      for (int a = 0; a < 12; ++a) { rv[a] = sm.xs[a] - sm.ref[a]; rj[a] = (a == j) ? 1.0f : 0.0f; }
-    } else {
-      DF xd[NX], r[12];
+  for (int a = 0; a < 4; ++a) {
+    const float4 rowa = *reinterpret_cast<const float4*>(CT + (s0 + a) * 4);
+    Dm[a][0] = rowa.x; Dm[a][1] = rowa.y; Dm[a][2] = rowa.z; Dm[a][3] = rowa.w;
+  }
+  float L[4][4], il[4];
+  bool bad = false;
 #pragma unroll
-      for (int i = 0; i < NX; ++i) xd[i] = mkd(sm.xs[i], i == j ? 1.0f : 0.0f);
-      M::template state_residual<DF>(xd, sm.ref, r);
+  for (int a = 0; a < 4; ++a) {
+    float dsum = Dm[a][a];
 #pragma unroll
-      for (int a = 0; a < 12; ++a) { rv[a] = r[a].v; rj[a] = r[a].d; }
+    for (int k = 0; k < a; ++k) dsum -= L[a][k] * L[a][k];
+    if (!(dsum > 0.0f)) { bad = true; dsum = fmaxf(fabsf(dsum), 1e-20f); }
+    il[a] = rsqrtf(dsum);
+#pragma unroll
+    for (int b = a + 1; b < 4; ++b) {
+      float v = Dm[b][a];
+#pragma unroll
+      for (int k = 0; k < a; ++k) v -= L[b][k] * L[a][k];
+      L[b][a] = v * il[a];
     }
-    float g = 0.0f;
+  }
+  if (bad) *status |= ST_NON_PD;
+  float y[4];
 #pragma unroll
-    for (int a = 0; a < 12; ++a) g += sm.w[a] * rv[a] * rj[a];
-    *gj = g;
-    if (M::IDENT_RES) {
-      const float wj = sm.w[j];
+  for (int a = 0; a < 4; ++a) {
+    float v = 0.0f;
 #pragma unroll
-      for (int i = 0; i < NX; ++i) gcol[i] = (i == j) ? wj : 0.0f;
-    } else {
+    for (int i = 0; i < NZ; ++i) v = (i == s0 + a) ? h[i] : v;
 #pragma unroll
-      for (int a = 0; a < 12; ++a) sm.J[j * 12 + a] = rj[a];
-    }
-  } else if (j < NX + NU && !terminal) {
-    const int a = j - NX;
-    constexpr int LD = (M::LEGS == 4) ? 3 : 6;
-    float hb[LD];
-    float gb;
-    int leg;
-    barrier_lane<M>(mc, a, sm.us, sm.ref, &gb, hb, &leg);
-    const float wa = sm.w[12 + a];
-    *gj = wa * sm.us[a] + gb;
+    for (int k = 0; k < a; ++k) v -= L[a][k] * y[k];
+    y[a] = v * il[a];
+  }
 #pragma unroll
-    for (int b = 0; b < NU; ++b) {
-      float v = 0.0f;
+  for (int a = 3; a >= 0; --a) {
+    float v = y[a];
 #pragma unroll
-      for (int r = 0; r < LD; ++r) v = (b == LD * leg + r) ? hb[r] : v;
-      gcol[NX + b] = v + ((b == a) ? wa : 0.0f);
-    }
+    for (int k = a + 1; k < 4; ++k) v -= L[k][a] * y[k];
+    y[a] = v * il[a];
+  }
+#pragma unroll
+  for (int i = 0; i < NZ; ++i) {
+    const float4 hc = *reinterpret_cast<const float4*>(CT + i * 4);
+    const float upd = hc.x * y[0] + hc.y * y[1] + hc.z * y[2] + hc.w * y[3];
+    float yi = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) yi = (i == s0 + a) ? y[a] : yi;
+    h[i] = (i >= s0 && i < s0 + 4) ? yi : h[i] - upd;
   }
 }
 
-// Gauss-Newton state block for non-identity residuals (needs every lane's
-// column in sm.J; call after __syncwarp()).
-template <class M>
-__device__ __forceinline__ void cost_column_state_block(WarpSmem<M>& sm, int j, float* gcol) {
-  constexpr int NX = M::NX;
-  if (M::IDENT_RES || j >= NX) return;
-  float wr[12];
-#pragma unroll
-  for (int a = 0; a < 12; ++a) wr[a] = sm.w[a] * sm.J[j * 12 + a];
-#pragma unroll
-  for (int i = 0; i < NX; ++i) {
-    float s = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 12; ++a) s += sm.J[i * 12 + a] * wr[a];
-    gcol[i] = s;
-  }
-}
-
+// ----------------------------------------------------------------- one instance
 template <class M>
 __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int b,
                                WarpSmem<M>& sm, float* scr) {
   typedef Dims<M> D;
-  constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP;
+  constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP, FS = D::FS;
+  constexpr int LD = D::LD, RS = D::RS;
+  static_assert(NU % 4 == 0, "block elimination assumes m divisible by 4");
+  static_assert(NX <= 16, "forward reduction assumes n <= 16");
   const int lane = threadIdx.x & 31;
+  const int j = lane;
   const int n_max = bp.n_max;
   const int N = bp.horizon ? bp.horizon[b] : n_max;
   if (N < 1 || N > n_max) {  // invalid horizon: report, touch nothing else
@@ -233,7 +469,6 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   const float* par = bp.par + (size_t)b * (n_max + 1) * M::NPAR;
   Scratch<M> s(scr, n_max);
 
-  // warm start into the outputs (in place when they alias)
   if (bp.X_in != bp.X)
     for (int e = lane; e < (N + 1) * NX; e += 32) X[e] = bp.X_in[xo + e];
   if (bp.V_in != bp.V)
@@ -241,216 +476,260 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   if (bp.U_in != bp.U)
     for (int e = lane; e < N * NU; e += 32) U[e] = bp.U_in[uo + e];
   if (lane < 24) sm.w[lane] = bp.w[(size_t)b * 24 + lane];
+  // zero padding rows of the shared P / F columns (read by the float4 products)
+  for (int e = lane; e < NP * LDP; e += 32) { sm.P[e] = 0.0f; sm.Praw[e] = 0.0f; }
+  for (int e = lane; e < NZ * LDP; e += 32) sm.F[e] = 0.0f;
   __syncwarp();
 
   float rho = sp.rho0;
   int status = 0;
-  const int j = lane;
 
   for (int it = 0; it < sp.sqp_iters; ++it) {
-    // ================================================ backward sweep
-    float J0 = 0.0f;  // stage costs, accumulated on lane JA
+    // ================================================ phase 1: linearise all stages
+    float lsum = 0.0f, dummy = 0.0f;
+    for (int t = lane; t <= N; t += 32)
+      lin_stage<M, false>(mc, t, N, x0, X, U, V, ref, par, sm.w, s, &lsum, &dummy, &dummy, &dummy);
+    const double Jc = warp_sum((double)lsum);
+    __syncwarp();
+    // ================================================ phase 2: backward Riccati
     {
-      // terminal value function P_N = G_N, p_N = g_N
-      for (int e = lane; e < NX; e += 32) sm.xs[e] = X[N * NX + e];
-      for (int e = lane; e < M::NREF; e += 32) sm.ref[e] = ref[N * M::NREF + e];
-      __syncwarp();
-      float gcol[NZ], gj;
-      cost_column<M>(mc, sm, j, true, gcol, &gj);
-      __syncwarp();
-      cost_column_state_block<M>(sm, j, gcol);
+      const float* GN = s.G + (size_t)N * D::GS;
       if (j < NX) {
+        float col[NP];
 #pragma unroll
-        for (int i = 0; i < NX; ++i) sm.P[j * LDP + i] = gcol[i];
-        sm.P[j * LDP + NX] = gj;
+        for (int i = 0; i < NX; ++i) col[i] = 0.0f;
+        if (D::QB && j >= M::QOFF && j < M::QOFF + 4) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) col[M::QOFF + k] = GN[D::G_QQ + (j - M::QOFF) * 4 + k];
+        } else {
+          const float wj = sm.w[M::wrow(j)];
+#pragma unroll
+          for (int i = 0; i < NX; ++i) col[i] = (i == j) ? wj : col[i];
+        }
+        const float gj = GN[D::G_GRAD + j];
+        col[NX] = gj;
+        float* Pn = s.P + (size_t)N * NP * LDP;
+#pragma unroll
+        for (int i = 0; i < NP; ++i) { sm.P[j * LDP + i] = col[i]; Pn[j * LDP + i] = col[i]; }
         sm.P[NX * LDP + j] = gj;
-        s.G[N * (NX + NU) + j] = gj;
+        Pn[NX * LDP + j] = gj;
       }
-      if (j == JA) {
-        sm.P[NX * LDP + NX] = 0.0f;
-        J0 += stage_cost<M>(mc, sm.xs, sm.us, sm.ref, sm.w, true);
-      }
+      if (j == 0) { sm.P[NX * LDP + NX] = 0.0f; s.P[(size_t)N * NP * LDP + NX * LDP + NX] = 0.0f; }
       __syncwarp();
-      if (j < NP) {
-#pragma unroll
-        for (int i = 0; i < NP; ++i) s.P[(size_t)N * NP * NP + j * NP + i] = sm.P[j * LDP + i];
-      }
     }
+    // whole-warp fence: phase-1 stores are complete before the block loads
+    __threadfence_block();
+    __syncwarp();
+    BlockRegs<NZ * FS> fpre;
+    BlockRegs<D::GS> gpre;
+    fpre.load(s.F + (size_t)(N - 1) * NZ * FS, lane);
+    gpre.load(s.G + (size_t)(N - 1) * D::GS, lane);
     for (int t = N - 1; t >= 0; --t) {
-      __syncwarp();
-      for (int e = lane; e < NX; e += 32) { sm.xs[e] = X[t * NX + e]; sm.xn[e] = X[(t + 1) * NX + e]; }
-      for (int e = lane; e < NU; e += 32) sm.us[e] = U[t * NU + e];
-      for (int e = lane; e < M::NREF; e += 32) sm.ref[e] = ref[t * M::NREF + e];
-      for (int e = lane; e < M::NPAR; e += 32) sm.par[e] = par[t * M::NPAR + e];
-      __syncwarp();
-      // ---- linearisation: column j of F and of the cost model G
-      float fcol[NP];
-      if (j < NX + NU) {
-        DF xd[NX], ud[NU], fd[NX];
-#pragma unroll
-        for (int i = 0; i < NX; ++i) xd[i] = mkd(sm.xs[i], i == j ? 1.0f : 0.0f);
-#pragma unroll
-        for (int a = 0; a < NU; ++a) ud[a] = mkd(sm.us[a], NX + a == j ? 1.0f : 0.0f);
-        M::template dynamics<DF>(mc, xd, ud, sm.par, fd);
-#pragma unroll
-        for (int i = 0; i < NX; ++i) fcol[i] = fd[i].d;
-        fcol[NX] = 0.0f;
-      } else if (j == JA) {
-        float fx[NX];
-        M::template dynamics<float>(mc, sm.xs, sm.us, sm.par, fx);
-#pragma unroll
-        for (int i = 0; i < NX; ++i) fcol[i] = fx[i] - sm.xn[i];
-        fcol[NX] = 1.0f;
-        J0 += stage_cost<M>(mc, sm.xs, sm.us, sm.ref, sm.w, false);
-      } else {
-#pragma unroll
-        for (int i = 0; i < NP; ++i) fcol[i] = 0.0f;
+      // ---- stage t's F columns and cost data into shared memory; prefetch t-1
+      fpre.template store_cols<FS, LDP>(sm.F, lane);
+      gpre.template store_cols<D::GS, D::GS>(sm.G, lane);
+      if (t > 0) {
+        fpre.load(s.F + (size_t)(t - 1) * NZ * FS, lane);
+        gpre.load(s.G + (size_t)(t - 1) * D::GS, lane);
       }
-      float gcol[NZ], gj;
-      cost_column<M>(mc, sm, j, false, gcol, &gj);
+      __syncwarp();
+      const float* Gt = sm.G;
+      // ---- column j of F and of the cost model G
+      float fcol[NP], h[NZ];
+#pragma unroll
+      for (int i = 0; i < NP; ++i) fcol[i] = 0.0f;
+#pragma unroll
+      for (int i = 0; i < NZ; ++i) h[i] = 0.0f;
       if (j < NZ) {
 #pragma unroll
-        for (int i = 0; i < NP; ++i) sm.F[j * LDP + i] = fcol[i];
+        for (int q = 0; q < FS / 4; ++q) {
+          const float4 v = *reinterpret_cast<const float4*>(sm.F + j * LDP + 4 * q);
+          if (4 * q < NX) fcol[4 * q] = v.x;
+          if (4 * q + 1 < NX) fcol[4 * q + 1] = v.y;
+          if (4 * q + 2 < NX) fcol[4 * q + 2] = v.z;
+          if (4 * q + 3 < NX) fcol[4 * q + 3] = v.w;
+        }
       }
-      if (j < JA) sm.g[j] = gj;
-      __syncwarp();
-      cost_column_state_block<M>(sm, j, gcol);
-      if (j < JA) {
-        gcol[JA] = gj;
-        s.G[t * (NX + NU) + j] = gj;
+      fcol[NX] = (j == JA) ? 1.0f : 0.0f;
+      if (j < NX) {
+        if (D::QB && j >= M::QOFF && j < M::QOFF + 4) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) h[M::QOFF + k] = Gt[D::G_QQ + (j - M::QOFF) * 4 + k];
+        } else {
+          const float wj = sm.w[M::wrow(j)];
+#pragma unroll
+          for (int i = 0; i < NX; ++i) h[i] = (i == j) ? wj : h[i];
+        }
+        h[JA] = Gt[D::G_GRAD + j];
+      } else if (j < JA) {
+        const int a = j - NX, leg = a / LD, c = a - LD * leg;
+        float hb[LD];
+#pragma unroll
+        for (int r2 = 0; r2 < LD; ++r2) hb[r2] = Gt[D::G_HB + (leg * LD + c) * LD + r2];
+        const float wa = sm.w[12 + a];
+#pragma unroll
+        for (int bb = 0; bb < NU; ++bb) {
+          float v = (bb == a) ? wa : 0.0f;
+#pragma unroll
+          for (int r2 = 0; r2 < LD; ++r2) v += (bb == LD * leg + r2) ? hb[r2] : 0.0f;
+          h[NX + bb] = v;
+        }
+        h[JA] = Gt[D::G_GRAD + j];
       } else if (j == JA) {
 #pragma unroll
-        for (int i = 0; i < JA; ++i) gcol[i] = sm.g[i];
-        gcol[JA] = 0.0f;
+        for (int i = 0; i < JA; ++i) h[i] = Gt[D::G_GRAD + i];
       }
+      if (j == JA) sm.F[JA * LDP + NX] = 1.0f;  // the affine column's last row
+      __syncwarp();
       // ---- T = P F[:, j];  H[:, j] = G[:, j] + F^T T
-      float tv[NP];
+      float tv[LDP];
 #pragma unroll
-      for (int i = 0; i < NP; ++i) tv[i] = 0.0f;
+      for (int i = 0; i < LDP; ++i) tv[i] = 0.0f;
 #pragma unroll
       for (int k = 0; k < NP; ++k) {
         const float fk = fcol[k];
 #pragma unroll
-        for (int i = 0; i < NP; ++i) tv[i] += sm.P[k * LDP + i] * fk;
+        for (int q = 0; q < LDP / 4; ++q) {
+          const float4 pv = *reinterpret_cast<const float4*>(sm.P + k * LDP + 4 * q);
+          tv[4 * q] += pv.x * fk; tv[4 * q + 1] += pv.y * fk; tv[4 * q + 2] += pv.z * fk; tv[4 * q + 3] += pv.w * fk;
+        }
       }
-      float h[NZ];
 #pragma unroll
       for (int i = 0; i < NZ; ++i) {
-        float a = gcol[i];
+        float a = h[i];
 #pragma unroll
-        for (int k = 0; k < NP; ++k) a += sm.F[i * LDP + k] * tv[k];
+        for (int q = 0; q < LDP / 4; ++q) {
+          const float4 fv = *reinterpret_cast<const float4*>(sm.F + i * LDP + 4 * q);
+          a += fv.x * tv[4 * q] + fv.y * tv[4 * q + 1] + fv.z * tv[4 * q + 2] + fv.w * tv[4 * q + 3];
+        }
         h[i] = a;
       }
-      if (j >= NX && j < JA) {
 #pragma unroll
-        for (int a = NX; a < JA; ++a)
-          if (a == j) h[a] += sp.reg;
-      }
-      // ---- Gauss-Jordan elimination of the control pivots
+      for (int a = NX; a < JA; ++a)
+        if (a == j) h[a] += sp.reg;
+      // ---- block Gauss-Jordan elimination of the control pivots
 #pragma unroll
-      for (int p = NX; p < JA; ++p) {
-        __syncwarp();
-        if (lane == p) {
+      for (int s0 = NX; s0 < JA; s0 += 4) gj_block4<NZ>(h, s0, lane, sm.CT, &status);
+      // ---- gains, closed loop, new value function
+      float* Kt = s.K + (size_t)t * NP * NU;
+      float* Fo = s.F + (size_t)t * NZ * FS;
+      if (j < NX || j == JA) {
+        const int col = (j == JA) ? NX : j;
+        float kc[NU];
 #pragma unroll
-          for (int i = 0; i < NZ; ++i) sm.col[i] = h[i];
-        }
-        __syncwarp();
-        float d = sm.col[p];
-        if (!(d > 0.0f)) { status |= ST_NON_PD; d = fmaxf(fabsf(d), 1e-12f); }
-        const float hp = h[p] / d;
+        for (int a = 0; a < NU; ++a) kc[a] = -h[NX + a];
+        st_vec<NU>(Kt + col * NU, kc);
+        // closed loop: (A + B K)[:, j] for state lanes, B k + c for the affine lane
+        float cl[FS];
 #pragma unroll
-        for (int i = 0; i < NZ; ++i)
-          if (i != p) h[i] -= sm.col[i] * hp;
-        h[p] = hp;
-      }
-      // ---- outputs: K, k, new value function (symmetrised)
-      if (j < NX) {
+        for (int i = 0; i < FS; ++i) cl[i] = (i < NX) ? fcol[i < NX ? i : 0] : 0.0f;
 #pragma unroll
-        for (int a = 0; a < NU; ++a) s.K[(size_t)t * NP * NU + j * NU + a] = -h[NX + a];
+        for (int a = 0; a < NU; ++a)
 #pragma unroll
-        for (int i = 0; i < NX; ++i) sm.Praw[j * LDP + i] = h[i];
-      } else if (j == JA) {
+          for (int i = 0; i < NX; ++i) cl[i] += sm.F[(NX + a) * LDP + i] * kc[a];
+        const int slot = (j == JA) ? NX : j;  // A+BK overwrites A, Bk+c goes to the first B slot
+        st_vec<FS>(Fo + slot * FS, cl);
 #pragma unroll
-        for (int a = 0; a < NU; ++a) s.K[(size_t)t * NP * NU + NX * NU + a] = -h[NX + a];
-#pragma unroll
-        for (int i = 0; i < NX; ++i) sm.Praw[NX * LDP + i] = h[i];
-      }
-      if (j < NZ) {
-#pragma unroll
-        for (int i = 0; i < NX; ++i) s.F[(size_t)t * NZ * NX + j * NX + i] = fcol[i];
+        for (int i = 0; i < NX; ++i) sm.Praw[col * LDP + i] = h[i];
       }
       __syncwarp();
-      if (j < NX) {
-        float* Pt = s.P + (size_t)t * NP * NP;
+      {
+        float* Pt = s.P + (size_t)t * NP * LDP;
+        if (j < NX) {
+          float pc[LDP];
 #pragma unroll
-        for (int i = 0; i < NX; ++i) {
-          const float v = 0.5f * (h[i] + sm.Praw[i * LDP + j]);
-          sm.P[j * LDP + i] = v;
-          Pt[j * NP + i] = v;
+          for (int i = 0; i < LDP; ++i) pc[i] = 0.0f;
+#pragma unroll
+          for (int i = 0; i < NX; ++i) pc[i] = 0.5f * (h[i] + sm.Praw[i * LDP + j]);
+          pc[NX] = 0.5f * (h[JA] + sm.Praw[NX * LDP + j]);
+#pragma unroll
+          for (int i = 0; i < NP; ++i) sm.P[j * LDP + i] = pc[i];
+          sm.P[NX * LDP + j] = pc[NX];
+          st_vec<LDP>(Pt + j * LDP, pc);
+          Pt[NX * LDP + j] = pc[NX];
+        } else if (j < LDP) {
+          Pt[NX * LDP + j] = 0.0f;  // [NX][NX] and the padding rows of column NX
+          if (j == NX) sm.P[NX * LDP + NX] = 0.0f;
         }
-        const float pj = 0.5f * (h[JA] + sm.Praw[NX * LDP + j]);
-        sm.P[j * LDP + NX] = pj;
-        sm.P[NX * LDP + j] = pj;
-        Pt[j * NP + NX] = pj;
-        Pt[NX * NP + j] = pj;
       }
-      if (j == 0) {
-        sm.P[NX * LDP + NX] = 0.0f;
-        s.P[(size_t)t * NP * NP + NX * NP + NX] = 0.0f;
-      }
+      __syncwarp();
     }
+    // ================================================ phase 3: forward sweep
+    __threadfence_block();
     __syncwarp();
-    // ================================================ forward sweep
     double a_gd = 0.0, a_lc = 0.0, a_vc = 0.0, a_cs = 0.0;
     float c_cur = 0.0f;
+    BlockRegs<NP * LDP> ppre;
+    BlockRegs<NP * NU> kpre;
+    BlockRegs<NZ * FS> fpre3;
+    BlockRegs<D::GS> gpre3;
+    ppre.load(s.P, lane);
+    kpre.load(s.K, lane);
+    fpre3.load(s.F, lane);
+    gpre3.load(s.G, lane);
     if (lane < NX) {
       c_cur = x0[lane] - X[lane];
       sm.dx[lane] = c_cur;
     }
-    __syncwarp();
     for (int t = 0; t <= N; ++t) {
-      const float* Pt = s.P + (size_t)t * NP * NP;
+      // ---- stage t's value function, gains, closed loop and cost data; prefetch t+1
+      ppre.template store_cols<LDP, LDP>(sm.P, lane);
+      gpre3.template store_cols<D::GS, D::GS>(sm.G, lane);
+      if (t < N) {
+        kpre.template store_cols<NU, NU>(sm.Praw, lane);
+        fpre3.template store_cols<FS, LDP>(sm.F, lane);
+      }
+      if (t + 1 <= N) {
+        ppre.load(s.P + (size_t)(t + 1) * NP * LDP, lane);
+        gpre3.load(s.G + (size_t)(t + 1) * D::GS, lane);
+      }
+      if (t + 1 < N) {
+        kpre.load(s.K + (size_t)(t + 1) * NP * NU, lane);
+        fpre3.load(s.F + (size_t)(t + 1) * NZ * FS, lane);
+      }
+      __syncwarp();
       if (lane < NX) {
-        float lam = Pt[NX * NP + lane];
+        const float dxi = sm.dx[lane];
+        float lam = sm.P[lane * LDP + NX];
 #pragma unroll
-        for (int k = 0; k < NX; ++k) lam += Pt[k * NP + lane] * sm.dx[k];
+        for (int k = 0; k < NX; ++k) lam += sm.P[lane * LDP + k] * sm.dx[k];
         const float vt = V[t * NX + lane];
         a_lc += (double)((lam - 2.0f * vt) * c_cur);
         a_vc += (double)(vt * c_cur);
         a_cs += (double)(c_cur * c_cur);
-        a_gd += (double)(s.G[t * (NX + NU) + lane] * sm.dx[lane]);
+        a_gd += (double)(sm.G[D::G_GRAD + lane] * dxi);
         s.L[t * NX + lane] = lam;
-        s.dX[t * NX + lane] = sm.dx[lane];
+        s.dX[t * NX + lane] = dxi;
       }
       if (t == N) break;
-      const float* Kt = s.K + (size_t)t * NP * NU;
+      if (lane < NX || lane == JA) {
+        const int col = (lane == JA) ? NX : lane;
+        const float sc = (lane == JA) ? 1.0f : sm.dx[col];
+        float* rw = sm.red + col * RS;
+#pragma unroll
+        for (int a = 0; a < NU; ++a) rw[a] = sm.Praw[col * NU + a] * sc;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) rw[NU + i] = sm.F[col * LDP + i] * sc;
+      }
+      __syncwarp();
+      float sum = 0.0f;
       if (lane < NU) {
-        float du = Kt[NX * NU + lane];
 #pragma unroll
-        for (int k = 0; k < NX; ++k) du += Kt[k * NU + lane] * sm.dx[k];
-        sm.du[lane] = du;
-        a_gd += (double)(s.G[t * (NX + NU) + NX + lane] * du);
-        s.dU[t * NU + lane] = du;
+        for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + lane];
+        s.dU[t * NU + lane] = sum;
+        a_gd += (double)(sm.G[D::G_GRAD + NX + lane] * sum);
+      } else if (lane >= 16 && lane < 16 + NX) {
+#pragma unroll
+        for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + NU + (lane - 16)];
       }
+      if (lane < NX) c_cur = sm.F[JA * LDP + lane];  // defect of stage t pairs with V_{t+1}
       __syncwarp();
-      float dxn = 0.0f;
-      if (lane < NX) {
-        const float* Ft = s.F + (size_t)t * NZ * NX;
-        c_cur = Ft[JA * NX + lane];
-        dxn = c_cur;
-#pragma unroll
-        for (int k = 0; k < NX; ++k) dxn += Ft[k * NX + lane] * sm.dx[k];
-#pragma unroll
-        for (int a = 0; a < NU; ++a) dxn += Ft[(NX + a) * NX + lane] * sm.du[a];
-      }
-      __syncwarp();
-      if (lane < NX) sm.dx[lane] = dxn;
+      if (lane >= 16 && lane < 16 + NX) sm.dx[lane - 16] = sum;
       __syncwarp();
     }
     __syncwarp();
     const double gd = warp_sum(a_gd), lc = warp_sum(a_lc), vc = warp_sum(a_vc), cs = warp_sum(a_cs);
-    const double Jc = warp_sum((double)J0);
-    // ================================================ merit line search
+    // ================================================ phase 4: merit line search
     const double G = gd + lc;
     if (cs > 0.0 && G > 0.0) rho = fminf(fmaxf(rho, (float)(2.0 * G / cs)), 1e12f);
     const double dphi = G - (double)rho * cs;
@@ -462,17 +741,14 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
     } else {
       for (int tr = 0; tr < sp.ls_max_trials; ++tr) {
         double acc = 0.0;
-        for (int t = lane; t <= N; t += 32) {
-          float cm;
-          acc += (double)merit_stage<M>(mc, t, N, alpha, rho, x0, X, U, V, s, ref, par, sm.w, &cm);
-        }
+        for (int t = lane; t <= N; t += 32)
+          acc += (double)merit_stage<M>(mc, t, N, alpha, rho, x0, X, U, V, s, ref, par, sm.w);
         const double phi = warp_sum(acc);
         if (phi <= phi0 + (double)sp.ls_eta * alpha * dphi) { accepted = true; break; }
         if (tr + 1 < sp.ls_max_trials) alpha *= sp.ls_beta;
       }
     }
     if (!accepted) status |= ST_LS_FAIL;
-    // ================================================ step
     for (int e = lane; e < (N + 1) * NX; e += 32) {
       X[e] += alpha * s.dX[e];
       V[e] += alpha * (s.L[e] - V[e]);
@@ -485,7 +761,7 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   if (bp.K) {
     float* Ko = bp.K + (size_t)b * n_max * NU * NX;
     for (int e = lane; e < N * NU * NX; e += 32) {
-      const int t = e / (NU * NX), r = e - t * NU * NX, a = r / NX, jj = r - a * NX;
+      const int t = e / (NU * NX), r2 = e - t * NU * NX, a = r2 / NX, jj = r2 - a * NX;
       Ko[e] = s.K[(size_t)t * NP * NU + jj * NU + a];
     }
   }
@@ -496,51 +772,11 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
       ko[e] = s.K[(size_t)t * NP * NU + NX * NU + a];
     }
   }
-
   // ================================================ KKT residual of the result
   if (bp.kkt && sp.compute_kkt) {
-    float rp = 0.0f, rd = 0.0f, gm = 0.0f;
-    if (lane < NX) rp = fabsf(x0[lane] - X[lane]);
-    for (int t = 0; t <= N; ++t) {
-      __syncwarp();
-      for (int e = lane; e < NX; e += 32) {
-        sm.xs[e] = X[t * NX + e];
-        if (t < N) sm.xn[e] = X[(t + 1) * NX + e];
-      }
-      if (t < N) {
-        for (int e = lane; e < NU; e += 32) sm.us[e] = U[t * NU + e];
-        for (int e = lane; e < M::NPAR; e += 32) sm.par[e] = par[t * M::NPAR + e];
-      }
-      for (int e = lane; e < M::NREF; e += 32) sm.ref[e] = ref[t * M::NREF + e];
-      __syncwarp();
-      float gcol[NZ], gj;
-      cost_column<M>(mc, sm, j, t == N, gcol, &gj);
-      if (t == N) {
-        if (j < NX) {
-          rd = fmaxf(rd, fabsf(gj - V[t * NX + j]));
-          gm = fmaxf(gm, fabsf(gj));
-        }
-        break;
-      }
-      if (j < NX + NU) {
-        DF xd[NX], ud[NU], fd[NX];
-#pragma unroll
-        for (int i = 0; i < NX; ++i) xd[i] = mkd(sm.xs[i], i == j ? 1.0f : 0.0f);
-#pragma unroll
-        for (int a = 0; a < NU; ++a) ud[a] = mkd(sm.us[a], NX + a == j ? 1.0f : 0.0f);
-        M::template dynamics<DF>(mc, xd, ud, sm.par, fd);
-        float r = gj;
-#pragma unroll
-        for (int i = 0; i < NX; ++i) r += fd[i].d * V[(t + 1) * NX + i];
-        if (j < NX) r -= V[t * NX + j];
-        rd = fmaxf(rd, fabsf(r));
-        gm = fmaxf(gm, fabsf(gj));
-        if (j == 0) {
-#pragma unroll
-          for (int i = 0; i < NX; ++i) rp = fmaxf(rp, fabsf(fd[i].v - sm.xn[i]));
-        }
-      }
-    }
+    float rp = 0.0f, rd = 0.0f, gm = 0.0f, lsum = 0.0f;
+    for (int t = lane; t <= N; t += 32)
+      lin_stage<M, true>(mc, t, N, x0, X, U, V, ref, par, sm.w, s, &lsum, &rp, &rd, &gm);
     rp = warp_max(rp);
     rd = warp_max(rd);
     gm = warp_max(gm);
@@ -559,10 +795,16 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
     if (!isfinite(U[e])) bad = 1;
   status = warp_or(status | (bad ? ST_NAN : 0));
   if (bp.status && lane == 0) bp.status[b] = status;
+  (void)LD;
 }
 
+// Minimum resident 4-warp blocks per SM the register allocation must allow.
+#ifndef MPXG_SQP_MIN_BLOCKS
+#define MPXG_SQP_MIN_BLOCKS 3
+#endif
+
 template <class M>
-__global__ void sqp_kernel(ModelConst mc, SqpParams sp, BatchPtrs bp) {
+__global__ void __launch_bounds__(128, MPXG_SQP_MIN_BLOCKS) sqp_kernel(ModelConst mc, SqpParams sp, BatchPtrs bp) {
   extern __shared__ float4 smem_raw[];
   WarpSmem<M>* sms = reinterpret_cast<WarpSmem<M>*>(smem_raw);
   const int wib = threadIdx.x >> 5;

@@ -56,13 +56,19 @@ def test_one_iteration_matches_oracle_fp64(oracle, cuda, model):
 
 @pytest.mark.parametrize("model", MODELS)
 def test_five_iterations_match_oracle(oracle, cuda, model):
+    """Cold start, 5 iterations: the iterate is far from converged and float32
+    rounding is amplified, so the GPU is held to the accuracy of the oracle's
+    own float32 run (error vs FP64 at most 2x the oracle-FP32 error + 1e-4)."""
     wl = workload(model, 8, (25, 50), seed=12)
     opts = P.SolverOptions(sqp_iters=5)
     g = gpu_solve(wl, opts)
     o = oracle.sqp_solve(wl.desc, opts, wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
-    ex = rel_err(g["X"], o["X"], wl.horizon, "x")
-    eu = rel_err(g["U"], o["U"], wl.horizon, "u")
-    assert ex < 1e-3 and eu < 1e-2, (ex, eu)
+    o32 = oracle.sqp_solve(wl.desc, opts, wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon,
+                           precision=32)
+    for key, kind in (("X", "x"), ("U", "u")):
+        eg = rel_err(g[key], o[key], wl.horizon, kind)
+        e32 = rel_err(o32[key], o[key], wl.horizon, kind)
+        assert eg <= 2.0 * e32 + 1e-4, (key, eg, e32)
     # the GPU result is as good a KKT point as the FP64 one (evaluated in FP64)
     kg = oracle.kkt_residual(wl.desc, wl.x0, g["X"], g["U"], g["V"], wl.reference, wl.parameter, wl.W, wl.horizon)
     assert np.all(kg[:, 2] <= np.maximum(2.0 * o["kkt"][:, 2], 1e-4)), (kg[:, 2], o["kkt"][:, 2])
@@ -76,6 +82,35 @@ def test_device_kkt_matches_fp64_evaluation(oracle, cuda, model):
     kg = oracle.kkt_residual(wl.desc, wl.x0, g["X"], g["U"], g["V"], wl.reference, wl.parameter, wl.W, wl.horizon)
     np.testing.assert_allclose(g["kkt"][:, 0], kg[:, 0], rtol=0.05, atol=2e-5)
     np.testing.assert_allclose(g["kkt"][:, 1], kg[:, 1], rtol=0.05, atol=2e-5)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_near_converged_parity_1e4(oracle, cuda, model):
+    """From a near-converged warm start (FP64 oracle, 15 iterations) two more
+    SQP iterations on the GPU (FP32) and in the FP64 oracle agree to 1e-4
+    relative for trajectories, gains, feedforward and multipliers."""
+    wl = workload(model, 6, (25, 50), seed=17)
+    o15 = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=15), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
+                           wl.parameter, wl.W, wl.horizon)
+    warm = P.Workload(wl.desc, wl.x0, o15["X"].astype(np.float32), o15["U"].astype(np.float32),
+                      o15["V"].astype(np.float32), wl.reference, wl.parameter, wl.W, wl.horizon)
+    opts = P.SolverOptions(sqp_iters=2)
+    g = gpu_solve(warm, opts)
+    o = oracle.sqp_solve(wl.desc, opts, wl.x0, warm.X0, warm.U0, warm.V0, wl.reference, wl.parameter, wl.W,
+                         wl.horizon)
+    if model == P.MODEL_SRBD_QUAT13:
+        # The quaternion's norm direction is neither penalised nor controllable
+        # (the dynamics renormalise it), so gain components along it are set by
+        # rounding (the FP32 oracle differs from FP64 there by ~2e-3): compare
+        # the gains on the tangent space of the unit quaternion.
+        for res in (g, o):
+            for i, N in enumerate(wl.horizon):
+                for t in range(N):
+                    q = o["X"][i, t, 3:7] / np.linalg.norm(o["X"][i, t, 3:7])
+                    res["K"][i, t][:, 3:7] -= np.outer(res["K"][i, t][:, 3:7] @ q, q)
+    for key, kind in (("X", "x"), ("U", "u"), ("V", "x"), ("K", "u"), ("k", "u")):
+        e = rel_err(g[key], o[key], wl.horizon, kind)
+        assert e < 1e-4, (key, e)
 
 
 def test_plain_path_is_bitwise_identical(cuda):
