@@ -211,7 +211,7 @@ def run_ours(args, rank, world, local_rank):
                 tr.replay()
             else:
                 tr.shift(stream)
-                tr.tables(stream, from_warm_start=True, advance=True)
+                tr.tables(stream)
                 sev[k][0].record(stream)
                 tr.solve(stream)
                 sev[k][1].record(stream)
@@ -231,7 +231,7 @@ def run_ours(args, rank, world, local_rank):
     with torch.cuda.stream(stream):
         for k in range(min(args.steps, 10)):
             tr.shift(stream)
-            tr.tables(stream, from_warm_start=True, advance=True)
+            tr.tables(stream)
             sev[k][0].record(stream)
             tr.solve(stream)
             sev[k][1].record(stream)
@@ -257,7 +257,7 @@ def run_ours(args, rank, world, local_rank):
         for k in range(e2e_steps):
             tr.x0.copy_(x0_host, non_blocking=True)             # measured states in
             tr.shift(stream)
-            tr.tables(stream, from_warm_start=False, advance=True)
+            tr.tables(stream, measured=True)
             tr.solve(stream)
             res_dev[:, :m].copy_(tr.U[:, 0, :])                   # first control (the reference's .grf)
             res_dev[:, m:m + 3].copy_(tr.out["kkt"])
@@ -283,7 +283,7 @@ def run_ours(args, rank, world, local_rank):
             for _ in range(max(args.warmup, 3)):
                 tp.tick(stream)
             tp.shift(stream)
-            tp.tables(stream, from_warm_start=True, advance=True)
+            tp.tables(stream)
         torch.cuda.synchronize()
         from mpx_gb300 import _lib
         from mpx_gb300.solver import _stream_handle

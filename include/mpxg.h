@@ -21,6 +21,13 @@
  *  - Solve calls are asynchronous on `stream`, allocate nothing and never
  *    synchronise the host; all device memory is allocated in mpxg_create.
  *  - A handle is used by one host thread at a time; handles are independent.
+ *  - Solves of one handle may overlap on several streams.  Each warp claims
+ *    a scratch slot for the length of its launch from a pool sized for the
+ *    most warps that can be resident at once, and each solve takes its own
+ *    work counter from a ring of 64 (a reused entry first waits for the
+ *    solve that used it last).  Solves captured into CUDA graphs take their
+ *    counters from a second ring of 64 without that wait: replays of more
+ *    than 64 captured solves of one handle must not overlap.
  *  - Numerical trouble does not abort a batch: it is reported per instance in
  *    status[b] (bits MPXG_INST_*), as the reference reports it through NaNs
  *    (mpx/utils/mpc_wrapper.py:96,280).
@@ -100,7 +107,10 @@ typedef struct {
  * alias X/U/V. */
 typedef struct {
   int batch;
-  const int* horizon;      /* [B] per-instance N (1..n_max) or NULL = n_max */
+  const int* slot;         /* [B] pool row of instance b, or NULL: row b.  Every
+                              per-instance array below is indexed by that row,
+                              so a batch can be any subset of a resident pool */
+  const int* horizon;      /* [pool] per-instance N (1..n_max) or NULL = n_max */
   const float* x0;
   const float* X_in;
   const float* U_in;
@@ -115,6 +125,9 @@ typedef struct {
   float* k;
   float* kkt;
   int* status;
+  float* first;            /* optional [batch, m+4], indexed by batch entry b (not by slot):
+                              first control U[0], kkt[3], status -- the per-tick result
+                              a controller reads back */
 } mpxg_batch_io;
 
 typedef struct mpxg_handle mpxg_handle;
@@ -143,9 +156,11 @@ mpxg_status mpxg_solve_plain(mpxg_handle* h, void* stream, const mpxg_batch_io* 
 
 /* Warm start for the next control tick: X,U,V shifted by `shift` rows with the
  * last row repeated, per instance horizon (mpx/utils/mpc_wrapper_srbd.py:135-137).
- * In place is allowed (Xo == X etc.). */
-mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const int* horizon, int shift,
-                                  const float* X, const float* U, const float* V, float* Xo, float* Uo, float* Vo);
+ * In place is allowed (Xo == X etc.).  slot [batch] (or NULL) maps batch
+ * entries to pool rows as in mpxg_batch_io. */
+mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const int* slot, const int* horizon,
+                                  int shift, const float* X, const float* U, const float* V, float* Xo, float* Uo,
+                                  float* Vo);
 
 /* Gait timer of a batch (mpx/utils/mpc_utils.py:7-14), float32 without fused
  * multiply-add: leg_time [B, n_legs] updated in place, contact [B, n_legs]. */
@@ -163,19 +178,34 @@ mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt
                              const float* contact, float* liftoff, float* reference, float* parameter,
                              float* foot_ref_dot);
 
-/* Gait tables of the synthetic trot / walk workloads (one thread per
- * instance): optionally x0[b] = X0[b,0,:] + drift[b,:] (X0 the shifted warm
- * start, drift may be NULL), then, when `advance`, one gait-timer step of
- * leg_time [B, legs]; then for t = 0..horizon[b] the contact flags from t+1
- * further timer steps (the schedule rule of mpx/utils/mpc_utils.py:187-189),
- * a CoM reference at v_ref[b] along x at constant `height`, zero attitude
- * and rate, and feet at `offsets` [legs*3] (HOST array) from the CoM
- * reference.  Outputs reference [B,n_max+1,ref_cols], parameter
- * [B,n_max+1,par_cols] of `model`. */
-mpxg_status mpxg_gait_tables(void* stream, int model, int batch, int n_max, const int* horizon, float dt,
-                             float duty_factor, float step_freq, float height, const float* offsets,
-                             const float* X0, const float* drift, float* x0, const float* v_ref, float* leg_time,
-                             int advance, float* reference, float* parameter);
+/* Gait tables of the synthetic trot / walk workloads, one thread per batch
+ * entry (row slot[b] of every per-instance array, or row b when slot is
+ * NULL):
+ *   mode 0 (first tick): x0 as given, timers as given; the warm start is
+ *          initialised (X = x0 at every stage, V = 0, U = `weight` split over
+ *          the legs in stance at each stage);
+ *   mode 1 (next tick):  x0 = X[b,0,:] + drift (X already shifted), drift
+ *          ~ N(0, drift_std^2) from a counter-based hash of (seed, row, i);
+ *          one gait-timer step of leg_time;
+ *   mode 2 (next tick, measured state): x0 as given (e.g. copied from the
+ *          host), one gait-timer step of leg_time, warm start kept.
+ * Then for t = 0..horizon the contact flags from t+1 further timer steps (the
+ * schedule rule of mpx/utils/mpc_utils.py:187-189), a CoM reference moving at
+ * v_ref along x at constant `height` with zero attitude and rate, and feet at
+ * `offsets` (legs x 3) from the CoM reference. */
+typedef struct {
+  int model, batch, n_max, mode;
+  const int* slot;
+  const int* horizon;
+  float dt, duty_factor, step_freq, height, weight, drift_std;
+  unsigned int seed;
+  float offsets[12];
+  float *x0, *X, *U, *V;
+  const float* v_ref;
+  float* leg_time;
+  float *reference, *parameter;
+} mpxg_gait_args;
+mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* args);
 
 /* Time-varying LQR in absolute coordinates for a batch (isolated KKT/LQR):
  * x_{t+1} = A_t x_t + B_t u_t + c_t, cost 1/2 x'Qx + x'Mu + 1/2 u'Ru + q'x + r'u,

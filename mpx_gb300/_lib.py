@@ -40,12 +40,23 @@ class SolverOpts(ctypes.Structure):
 
 
 class BatchIO(ctypes.Structure):
-    _fields_ = [("batch", ctypes.c_int), ("horizon", ctypes.c_void_p),
+    _fields_ = [("batch", ctypes.c_int), ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
                 ("x0", ctypes.c_void_p), ("X_in", ctypes.c_void_p), ("U_in", ctypes.c_void_p),
                 ("V_in", ctypes.c_void_p), ("reference", ctypes.c_void_p), ("parameter", ctypes.c_void_p),
                 ("w", ctypes.c_void_p), ("X", ctypes.c_void_p), ("U", ctypes.c_void_p), ("V", ctypes.c_void_p),
                 ("K", ctypes.c_void_p), ("k", ctypes.c_void_p), ("kkt", ctypes.c_void_p),
-                ("status", ctypes.c_void_p)]
+                ("status", ctypes.c_void_p), ("first", ctypes.c_void_p)]
+
+
+class GaitArgs(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("batch", ctypes.c_int), ("n_max", ctypes.c_int), ("mode", ctypes.c_int),
+                ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
+                ("dt", ctypes.c_float), ("duty_factor", ctypes.c_float), ("step_freq", ctypes.c_float),
+                ("height", ctypes.c_float), ("weight", ctypes.c_float), ("drift_std", ctypes.c_float),
+                ("seed", ctypes.c_uint), ("offsets", ctypes.c_float * 12),
+                ("x0", ctypes.c_void_p), ("X", ctypes.c_void_p), ("U", ctypes.c_void_p), ("V", ctypes.c_void_p),
+                ("v_ref", ctypes.c_void_p), ("leg_time", ctypes.c_void_p),
+                ("reference", ctypes.c_void_p), ("parameter", ctypes.c_void_p)]
 
 
 class LqIO(ctypes.Structure):
@@ -94,7 +105,7 @@ def load(build_if_missing=True):
         f = getattr(L, name)
         f.argtypes = [vp, vp, ctypes.POINTER(BatchIO)]
         f.restype = ctypes.c_int
-    L.mpxg_shift_warm_start.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
+    L.mpxg_shift_warm_start.argtypes = [vp, vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
     L.mpxg_shift_warm_start.restype = ctypes.c_int
     L.mpxg_timer_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                  vp, vp]
@@ -103,9 +114,7 @@ def load(build_if_missing=True):
                                    ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                    vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.mpxg_refgen_srbd.restype = ctypes.c_int
-    L.mpxg_gait_tables.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_float,
-                                   ctypes.c_float, ctypes.c_float, ctypes.c_float, c_float_p,
-                                   vp, vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.mpxg_gait_tables.argtypes = [vp, ctypes.POINTER(GaitArgs)]
     L.mpxg_gait_tables.restype = ctypes.c_int
     L.mpxg_lqr_workspace_bytes.argtypes = [ctypes.c_int] * 5
     L.mpxg_lqr_workspace_bytes.restype = ctypes.c_size_t

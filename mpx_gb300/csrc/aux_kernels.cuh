@@ -3,14 +3,16 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "../../include/mpxg.h"
+
 namespace mpxg {
 
 // mpx/utils/mpc_wrapper_srbd.py:135-137 per instance horizon: rows [shift..N]
 // move to [0..N-shift], the last row is repeated into the freed tail.
-__global__ void shift_kernel(int batch, int n_max, int nx, int nu, const int* horizon, int shift, const float* X,
-                             const float* U, const float* V, float* Xo, float* Uo, float* Vo) {
-  const int b = blockIdx.x;
-  if (b >= batch) return;
+__global__ void shift_kernel(int batch, const int* slot, int n_max, int nx, int nu, const int* horizon, int shift,
+                             const float* X, const float* U, const float* V, float* Xo, float* Uo, float* Vo) {
+  if ((int)blockIdx.x >= batch) return;
+  const int b = slot ? slot[blockIdx.x] : (int)blockIdx.x;
   const int N = horizon ? horizon[b] : n_max;
   if (N < 1 || N > n_max) return;
   const size_t xo = (size_t)b * (n_max + 1) * nx, uo = (size_t)b * n_max * nu;
@@ -238,62 +240,70 @@ __global__ void refgen_srbd_kernel(RefGenArgs g) {
 #undef DIV
 
 // ------------------------------------------------------------ gait tables
-// Reference / parameter tables of the synthetic trot (quadruped) and walk
-// (biped) workloads, one thread per instance: optional x0 update from the
-// shifted warm start plus a drift, one gait-timer step of the stored leg
-// timers (one control tick), then per stage t the contact flags from t+1
-// further timer steps (as mpc_utils.py:187-189 does), a CoM reference moving
-// at v_ref along x at constant height, and feet at fixed offsets from the CoM
-// reference.
-struct GaitArgs {
-  int batch, n_max, nx, legs, ref_cols, par_cols, contact_col;
-  const int* horizon;
-  float dt, duty, step_freq, height;
-  float off[4][3];
-  const float* X0;     // [B, n_max+1, nx] or null: x0 = X0[b,0] + drift[b]
-  const float* drift;  // [B, nx] or null
-  float* x0;           // [B, nx] (in/out)
-  const float* v_ref;  // [B]
-  float* leg_time;     // [B, legs] (in/out)
-  int advance;         // 1: advance leg_time by one timer step first
-  float *reference, *parameter;
-};
+// (see mpxg_gait_tables in include/mpxg.h)
+__device__ __forceinline__ unsigned int hash_u32(unsigned int x) {
+  // integer finaliser (xor-shift-multiply), a bijection of 32-bit words
+  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+  return x;
+}
+__device__ __forceinline__ float hash_normal(unsigned int seed, unsigned int row, unsigned int i) {
+  const unsigned int a = hash_u32(seed * 0x9e3779b9U ^ hash_u32(row * 64u + i));
+  const unsigned int b = hash_u32(a ^ 0x68bc21ebU);
+  const float u1 = ((a >> 8) + 1.0f) * (1.0f / 16777217.0f);  // (0, 1]
+  const float u2 = (b >> 8) * (1.0f / 16777216.0f);
+  return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);         // Box-Muller
+}
 
-__global__ void gait_tables_kernel(GaitArgs g) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= g.batch) return;
+__global__ void gait_tables_kernel(mpxg_gait_args g, int nx, int nu, int legs, int ref_cols, int par_cols,
+                                   int contact_col) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi >= g.batch) return;
+  const int b = g.slot ? g.slot[bi] : bi;
   const int N = g.horizon ? g.horizon[b] : g.n_max;
   if (N < 1 || N > g.n_max) return;
-  float* x0 = g.x0 + (size_t)b * g.nx;
-  if (g.X0) {
-    for (int i = 0; i < g.nx; ++i)
-      x0[i] = g.X0[(size_t)b * (g.n_max + 1) * g.nx + i] + (g.drift ? g.drift[(size_t)b * g.nx + i] : 0.0f);
+  const size_t xo = (size_t)b * (g.n_max + 1) * nx;
+  float* x0 = g.x0 + (size_t)b * nx;
+  if (g.mode == 1) {
+    for (int i = 0; i < nx; ++i)
+      x0[i] = g.X[xo + i] + (g.drift_std > 0.0f ? g.drift_std * hash_normal(g.seed, (unsigned)b, (unsigned)i) : 0.0f);
   }
   const float inc = __fmul_rn(g.dt, g.step_freq);
   float lt[4];
-  for (int i = 0; i < g.legs; ++i) {
-    lt[i] = g.leg_time[b * g.legs + i];
-    if (g.advance) { int c; timer_step(g.duty, inc, lt[i], c); g.leg_time[b * g.legs + i] = lt[i]; }
+  for (int i = 0; i < legs; ++i) {
+    lt[i] = g.leg_time[b * legs + i];
+    if (g.mode != 0) { int c; timer_step(g.duty_factor, inc, lt[i], c); g.leg_time[b * legs + i] = lt[i]; }
   }
   const float v = g.v_ref[b];
   const float px0 = x0[0], py0 = x0[1];
-  float* ref = g.reference + (size_t)b * (g.n_max + 1) * g.ref_cols;
-  float* par = g.parameter + (size_t)b * (g.n_max + 1) * g.par_cols;
+  float* ref = g.reference + (size_t)b * (g.n_max + 1) * ref_cols;
+  float* par = g.parameter + (size_t)b * (g.n_max + 1) * par_cols;
+  const int per = nu / legs;
   for (int t = 0; t <= N; ++t) {
-    float* rr = ref + (size_t)t * g.ref_cols;
-    float* pp = par + (size_t)t * g.par_cols;
-    for (int k = 0; k < g.ref_cols; ++k) rr[k] = 0.0f;
+    float* rr = ref + (size_t)t * ref_cols;
+    float* pp = par + (size_t)t * par_cols;
+    for (int k = 0; k < ref_cols; ++k) rr[k] = 0.0f;
     const float px = px0 + __fmul_rn(__fmul_rn((float)t, g.dt), v);
     rr[0] = px; rr[1] = py0; rr[2] = g.height;
-    if (g.nx == 13) { rr[3] = 1.0f; rr[7] = v; } else { rr[6] = v; }
-    for (int i = 0; i < g.legs; ++i) {
-      int c;
-      timer_step(g.duty, inc, lt[i], c);
-      rr[g.contact_col + i] = (float)c;
-      pp[i] = (float)c;
-      pp[g.legs + 3 * i] = px + g.off[i][0];
-      pp[g.legs + 3 * i + 1] = py0 + g.off[i][1];
-      pp[g.legs + 3 * i + 2] = g.height + g.off[i][2];
+    if (nx == 13) { rr[3] = 1.0f; rr[7] = v; } else { rr[6] = v; }
+    int ns = 0;
+    int cs[4];
+    for (int i = 0; i < legs; ++i) {
+      timer_step(g.duty_factor, inc, lt[i], cs[i]);
+      ns += cs[i];
+      rr[contact_col + i] = (float)cs[i];
+      pp[i] = (float)cs[i];
+      pp[legs + 3 * i] = px + g.offsets[3 * i];
+      pp[legs + 3 * i + 1] = py0 + g.offsets[3 * i + 1];
+      pp[legs + 3 * i + 2] = g.height + g.offsets[3 * i + 2];
+    }
+    if (g.mode == 0) {  // cold start of the warm start
+      for (int i = 0; i < nx; ++i) { g.X[xo + (size_t)t * nx + i] = x0[i]; g.V[xo + (size_t)t * nx + i] = 0.0f; }
+      if (t < N) {
+        float* u = g.U + ((size_t)b * g.n_max + t) * nu;
+        const float fz = g.weight / (float)(ns > 0 ? ns : 1);
+        for (int a = 0; a < nu; ++a) u[a] = 0.0f;
+        for (int i = 0; i < legs; ++i) u[per * i + 2] = cs[i] ? fz : 0.0f;
+      }
     }
   }
 }

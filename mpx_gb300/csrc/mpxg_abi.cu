@@ -21,8 +21,18 @@ struct mpxg_handle {
   int num_sms = 0;
   int warps_per_block = 0, blocks_per_sm = 0, total_warps = 0;
   long long scratch_stride = 0;
+  int n_slots = 0;                     // scratch slots: most warps resident at once
   float* scratch = nullptr;
-  int* counter = nullptr;
+  unsigned int* slot_bits = nullptr;   // claimed scratch slots
+  int* error = nullptr;                // device error word
+  // Work counters, one per solve in flight: kRing for eager solves (reuse
+  // waits on the event of the solve that last used the entry) and kRing for
+  // solves captured into CUDA graphs.
+  static constexpr int kRing = 64, kCounterStride = 32;
+  int* counters = nullptr;
+  cudaEvent_t ring_ev[kRing] = {};
+  bool ring_used[kRing] = {};
+  int ring_next = 0, capture_next = 0;
   ModelConst mc;
   SqpParams sp;
   std::string err;
@@ -48,6 +58,21 @@ static bool model_dims(int model, int* nx, int* nu) {
     case MPXG_MODEL_BIPED_WRENCH12: *nx = 12; *nu = 12; return true;
     default: return false;
   }
+}
+
+template <class M>
+static int resident_blocks(int wpb);
+
+// Scratch slots of a handle: the most warps of its kernel resident at once.
+static int scratch_slots(int model, int wpb, int num_sms) {
+  int rb = 1;
+  switch (model) {
+    case MPXG_MODEL_SRBD_QUAT13: rb = resident_blocks<ModelQuat13>(wpb); break;
+    case MPXG_MODEL_SRBD_RPY12: rb = resident_blocks<ModelRpy12>(wpb); break;
+    case MPXG_MODEL_BIPED_WRENCH12: rb = resident_blocks<ModelBiped12>(wpb); break;
+    default: break;
+  }
+  return num_sms * rb * wpb;
 }
 
 static long long scratch_stride_for(int model, int n_max) {
@@ -114,7 +139,9 @@ size_t mpxg_workspace_bytes(const mpxg_problem_desc* d, const mpxg_solver_opts* 
   int wpb, bps;
   launch_geometry(d, o, sms, &wpb, &bps);
   const long long stride = scratch_stride_for(d->model, d->n_max);
-  return (size_t)stride * sizeof(float) * (size_t)sms * bps * wpb + 256;
+  const size_t slots = (size_t)scratch_slots(d->model, wpb, sms);
+  return (size_t)stride * sizeof(float) * slots + (slots + 31) / 32 * 4 + 256 +
+         (size_t)2 * mpxg_handle::kRing * mpxg_handle::kCounterStride * sizeof(int);
 }
 
 mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, mpxg_handle** out) {
@@ -137,11 +164,27 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   launch_geometry(d, o, h->num_sms, &h->warps_per_block, &h->blocks_per_sm);
   h->total_warps = h->num_sms * h->blocks_per_sm * h->warps_per_block;
   h->scratch_stride = scratch_stride_for(d->model, d->n_max);
-  const size_t bytes = (size_t)h->scratch_stride * sizeof(float) * (size_t)h->total_warps;
-  e = cudaMalloc(&h->scratch, bytes);
-  if (e != cudaSuccess) { delete h; return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_create: scratch allocation failed"); }
-  e = cudaMalloc(&h->counter, 256);
-  if (e != cudaSuccess) { cudaFree(h->scratch); delete h; return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_create: counter allocation failed"); }
+  h->n_slots = scratch_slots(d->model, h->warps_per_block, h->num_sms);
+  const size_t bytes = (size_t)h->scratch_stride * sizeof(float) * (size_t)h->n_slots;
+  const size_t nwords = ((size_t)h->n_slots + 31) / 32;
+  const size_t ctr_bytes = (size_t)2 * mpxg_handle::kRing * mpxg_handle::kCounterStride * sizeof(int);
+  if (cudaMalloc(&h->scratch, bytes) != cudaSuccess || cudaMalloc(&h->slot_bits, nwords * 4 + 256) != cudaSuccess ||
+      cudaMalloc(&h->counters, ctr_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    mpxg_destroy(h);
+    return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_create: scratch allocation failed");
+  }
+  h->error = reinterpret_cast<int*>(h->slot_bits + nwords);
+  for (int i = 0; i < mpxg_handle::kRing; ++i) {
+    if (cudaEventCreateWithFlags(&h->ring_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      mpxg_destroy(h);
+      return fail(nullptr, MPXG_ERR_CUDA, "mpxg_create: cudaEventCreate failed");
+    }
+  }
+  e = cudaMemset(h->slot_bits, 0, nwords * 4 + 256);
+  if (e == cudaSuccess) e = cudaMemset(h->counters, 0, ctr_bytes);
+  if (e != cudaSuccess) { mpxg_destroy(h); return cuda_fail(nullptr, e, "mpxg_create: cudaMemset"); }
   ModelConst& mc = h->mc;
   mc.dt = d->dt; mc.mass = d->mass; mc.inv_mass = 1.0f / d->mass; mc.gravity = d->gravity; mc.mu = d->mu;
   mc.alpha = d->barrier_alpha; mc.sigma = d->barrier_sigma;
@@ -168,7 +211,10 @@ mpxg_status mpxg_query_geometry(const mpxg_handle* h, int* warps_per_block, int*
 void mpxg_destroy(mpxg_handle* h) {
   if (!h) return;
   if (h->scratch) cudaFree(h->scratch);
-  if (h->counter) cudaFree(h->counter);
+  if (h->slot_bits) cudaFree(h->slot_bits);
+  if (h->counters) cudaFree(h->counters);
+  for (int i = 0; i < mpxg_handle::kRing; ++i)
+    if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
   delete h;
 }
 
@@ -208,12 +254,14 @@ static mpxg_status check_io(mpxg_handle* h, const mpxg_batch_io* io) {
 
 static BatchPtrs make_ptrs(mpxg_handle* h, const mpxg_batch_io* io) {
   BatchPtrs bp;
-  bp.batch = io->batch; bp.n_max = h->desc.n_max; bp.horizon = io->horizon;
+  bp.batch = io->batch; bp.n_max = h->desc.n_max; bp.slot = io->slot; bp.horizon = io->horizon;
   bp.x0 = io->x0; bp.X_in = io->X_in; bp.U_in = io->U_in; bp.V_in = io->V_in;
   bp.ref = io->reference; bp.par = io->parameter; bp.w = io->w;
   bp.X = io->X; bp.U = io->U; bp.V = io->V; bp.K = io->K; bp.k = io->k; bp.kkt = io->kkt; bp.status = io->status;
-  bp.counter = h->counter; bp.scratch = h->scratch; bp.scratch_stride = h->scratch_stride;
+  bp.first = io->first;
+  bp.counter = nullptr; bp.scratch = h->scratch; bp.scratch_stride = h->scratch_stride;
   bp.single_instance = -1;
+  bp.slot_bits = h->slot_bits; bp.n_slots = h->n_slots; bp.error = h->error;
   return bp;
 }
 
@@ -225,13 +273,37 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
   if (io->batch == 0) return MPXG_OK;
   cudaStream_t st = (cudaStream_t)stream;
   BatchPtrs bp = make_ptrs(h, io);
-  cudaError_t e = cudaMemsetAsync(h->counter, 0, sizeof(int), st);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, MPXG_ERR_CUDA, "mpxg_solve: cudaStreamIsCapturing failed");
+  }
+  const bool eager = cap == cudaStreamCaptureStatusNone;
+  int r;
+  if (eager) {
+    r = h->ring_next;
+    h->ring_next = (r + 1) % mpxg_handle::kRing;
+    if (h->ring_used[r]) {  // the solve that last used this counter has finished
+      cudaError_t e = cudaStreamWaitEvent(st, h->ring_ev[r], 0);
+      if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamWaitEvent");
+    }
+  } else {
+    r = mpxg_handle::kRing + h->capture_next;
+    h->capture_next = (h->capture_next + 1) % mpxg_handle::kRing;
+  }
+  bp.counter = h->counters + (size_t)r * mpxg_handle::kCounterStride;
+  cudaError_t e = cudaMemsetAsync(bp.counter, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
   const int wpb = h->warps_per_block;
   int blocks = h->num_sms * h->blocks_per_sm;
   const int need = (io->batch + wpb - 1) / wpb;
   if (need < blocks) blocks = need;
-  return dispatch(h, st, bp, blocks, wpb);
+  mpxg_status s2 = dispatch(h, st, bp, blocks, wpb);
+  if (s2 != MPXG_OK || !eager) return s2;
+  e = cudaEventRecord(h->ring_ev[r], st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
+  h->ring_used[r] = true;
+  return MPXG_OK;
 }
 
 mpxg_status mpxg_solve_plain(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
@@ -247,10 +319,11 @@ mpxg_status mpxg_solve_plain(mpxg_handle* h, void* stream, const mpxg_batch_io* 
   return MPXG_OK;
 }
 
-mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const int* horizon, int shift,
-                                  const float* X, const float* U, const float* V, float* Xo, float* Uo, float* Vo) {
+mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const int* slot, const int* horizon,
+                                  int shift, const float* X, const float* U, const float* V, float* Xo, float* Uo,
+                                  float* Vo) {
   if (!h) return fail(nullptr, MPXG_ERR_INVALID_ARG, "null handle");
-  if (batch < 0 || batch > h->desc.batch_max || shift < 0 || !X || !U || !V || !Xo || !Uo || !Vo)
+  if (batch < 0 || shift < 0 || !X || !U || !V || !Xo || !Uo || !Vo)
     return fail(h, MPXG_ERR_INVALID_ARG, "mpxg_shift_warm_start: bad arguments");
   if (batch == 0 || shift == 0 && X == Xo && U == Uo && V == Vo) return MPXG_OK;
   const int nx = h->desc.n, nu = h->desc.m, nm = h->desc.n_max;
@@ -260,7 +333,8 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
     cudaError_t e = cudaFuncSetAttribute(shift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
   }
-  shift_kernel<<<batch, 128, smem, (cudaStream_t)stream>>>(batch, nm, nx, nu, horizon, shift, X, U, V, Xo, Uo, Vo);
+  shift_kernel<<<batch, 128, smem, (cudaStream_t)stream>>>(batch, slot, nm, nx, nu, horizon, shift, X, U, V, Xo, Uo,
+                                                           Vo);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "shift_kernel launch");
 }
@@ -275,25 +349,18 @@ mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_facto
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "timer_kernel launch");
 }
 
-mpxg_status mpxg_gait_tables(void* stream, int model, int batch, int n_max, const int* horizon, float dt,
-                             float duty_factor, float step_freq, float height, const float* offsets,
-                             const float* X0, const float* drift, float* x0, const float* v_ref, float* leg_time,
-                             int advance, float* reference, float* parameter) {
-  GaitArgs g;
-  if (model == MPXG_MODEL_SRBD_QUAT13) { g.nx = 13; g.legs = 4; g.ref_cols = 17; g.par_cols = 16; g.contact_col = 13; }
-  else if (model == MPXG_MODEL_SRBD_RPY12) { g.nx = 12; g.legs = 4; g.ref_cols = 16; g.par_cols = 16; g.contact_col = 12; }
-  else if (model == MPXG_MODEL_BIPED_WRENCH12) { g.nx = 12; g.legs = 2; g.ref_cols = 14; g.par_cols = 8; g.contact_col = 12; }
+mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* a) {
+  if (!a) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_gait_tables: null args");
+  int nx, nu, legs, rc, pc, cc;
+  if (a->model == MPXG_MODEL_SRBD_QUAT13) { nx = 13; nu = 12; legs = 4; rc = 17; pc = 16; cc = 13; }
+  else if (a->model == MPXG_MODEL_SRBD_RPY12) { nx = 12; nu = 12; legs = 4; rc = 16; pc = 16; cc = 12; }
+  else if (a->model == MPXG_MODEL_BIPED_WRENCH12) { nx = 12; nu = 12; legs = 2; rc = 14; pc = 8; cc = 12; }
   else return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_gait_tables: model");
-  if (batch < 0 || n_max < 1 || !offsets || !x0 || !v_ref || !leg_time || !reference || !parameter)
+  if (a->batch < 0 || a->n_max < 1 || a->mode < 0 || a->mode > 2 || !a->x0 || !a->X || !a->v_ref ||
+      !a->leg_time || !a->reference || !a->parameter || (a->mode == 0 && (!a->U || !a->V)))
     return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_gait_tables: bad arguments");
-  if (batch == 0) return MPXG_OK;
-  g.batch = batch; g.n_max = n_max; g.horizon = horizon; g.dt = dt; g.duty = duty_factor; g.step_freq = step_freq;
-  g.height = height;
-  for (int i = 0; i < 4; ++i)
-    for (int k = 0; k < 3; ++k) g.off[i][k] = (i < g.legs) ? offsets[3 * i + k] : 0.0f;  // host array
-  g.X0 = X0; g.drift = drift; g.x0 = x0; g.v_ref = v_ref; g.leg_time = leg_time; g.advance = advance;
-  g.reference = reference; g.parameter = parameter;
-  gait_tables_kernel<<<(batch + 127) / 128, 128, 0, (cudaStream_t)stream>>>(g);
+  if (a->batch == 0) return MPXG_OK;
+  gait_tables_kernel<<<(a->batch + 127) / 128, 128, 0, (cudaStream_t)stream>>>(*a, nx, nu, legs, rc, pc, cc);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "gait_tables_kernel launch");
 }
@@ -454,10 +521,11 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
   if (blocks < 1) blocks = 1;
 
   BatchPtrs bp;
-  bp.batch = io->batch; bp.n_max = d->n_max; bp.horizon = io->horizon;
+  bp.batch = io->batch; bp.n_max = d->n_max; bp.slot = io->slot; bp.horizon = io->horizon;
   bp.x0 = io->x0; bp.X_in = io->X_in; bp.U_in = io->U_in; bp.V_in = io->V_in;
   bp.ref = io->reference; bp.par = io->parameter; bp.w = io->w;
   bp.X = io->X; bp.U = io->U; bp.V = io->V; bp.K = io->K; bp.k = io->k; bp.kkt = io->kkt; bp.status = io->status;
+  bp.first = io->first;
   bp.counter = nd->counter; bp.scratch = nd->scratch; bp.scratch_stride = stride;
   bp.single_instance = -1;
 

@@ -34,15 +34,44 @@ struct SqpParams {
 
 struct BatchPtrs {
   int batch, n_max;
+  const int* slot;   // pool row of each batch entry (null: identity)
   const int* horizon;
   const float *x0, *X_in, *U_in, *V_in, *ref, *par, *w;
   float *X, *U, *V, *K, *k, *kkt;
   int* status;
+  float* first;              // optional per-batch-entry result rows [batch, NU+4]
   int* counter;              // work-queue head (zeroed before each launch)
   float* scratch;            // per-warp scratch
   long long scratch_stride;  // floats per warp
   int single_instance;       // >= 0: solve only this instance with warp 0 (plain path)
+  // Scratch slots claimed per warp from a bitmap shared by every launch of one
+  // handle (null: the warp's grid index is its slot).  n_slots is the most
+  // warps of this kernel that can be resident on the device at once, so a
+  // resident warp always finds a free slot.
+  unsigned int* slot_bits = nullptr;
+  int n_slots = 0;
+  int* error = nullptr;      // bit 0: a warp gave up claiming a slot
 };
+
+// Bounded claim of a free scratch slot (lane 0 only); -1 after the limit.
+__device__ inline int claim_scratch_slot(unsigned int* bits, int n_slots, int pref) {
+  const int nwords = (n_slots + 31) >> 5;
+  int wi = pref >> 5;
+  for (int it = 0; it < (1 << 16); ++it) {
+    const unsigned int w = atomicAdd(&bits[wi], 0u);
+    unsigned int avail = ~w;
+    if (wi == nwords - 1 && (n_slots & 31)) avail &= (1u << (n_slots & 31)) - 1u;
+    if (avail) {
+      const int want = pref & 31;
+      const int bit = (it == 0 && wi == (pref >> 5) && ((avail >> want) & 1u)) ? want : __ffs(avail) - 1;
+      const unsigned int old = atomicOr(&bits[wi], 1u << bit);
+      if (!(old & (1u << bit))) return wi * 32 + bit;
+    } else {
+      wi = wi + 1 == nwords ? 0 : wi + 1;
+    }
+  }
+  return -1;
+}
 
 constexpr int rup4(int v) { return (v + 3) / 4 * 4; }
 
@@ -445,8 +474,9 @@ __device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT,
 
 // ----------------------------------------------------------------- one instance
 template <class M>
-__device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int b,
+__device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int bidx,
                                WarpSmem<M>& sm, float* scr) {
+  const int b = bp.slot ? bp.slot[bidx] : bidx;  // pool row of this batch entry
   typedef Dims<M> D;
   constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP, FS = D::FS;
   constexpr int LD = D::LD, RS = D::RS;
@@ -458,6 +488,7 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   const int N = bp.horizon ? bp.horizon[b] : n_max;
   if (N < 1 || N > n_max) {  // invalid horizon: report, touch nothing else
     if (bp.status && lane == 0) bp.status[b] = ST_BAD_HORIZON;
+    if (bp.first && lane == 0) bp.first[(size_t)bidx * (M::NU + 4) + M::NU + 3] = (float)ST_BAD_HORIZON;
     return;
   }
   const size_t xo = (size_t)b * (n_max + 1) * NX, uo = (size_t)b * n_max * NU;
@@ -785,6 +816,10 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
       o[0] = rp;
       o[1] = rd / (1.0f + gm);
       o[2] = fmaxf(o[0], o[1]);
+      if (bp.first) {
+        float* f = bp.first + (size_t)bidx * (NU + 4) + NU;
+        f[0] = o[0]; f[1] = o[1]; f[2] = o[2];
+      }
     }
   }
   // ================================================ status
@@ -795,6 +830,14 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
     if (!isfinite(U[e])) bad = 1;
   status = warp_or(status | (bad ? ST_NAN : 0));
   if (bp.status && lane == 0) bp.status[b] = status;
+  if (bp.first) {
+    float* f = bp.first + (size_t)bidx * (NU + 4);
+    if (lane < NU) f[lane] = U[lane];
+    if (lane == 0) {
+      f[NU + 3] = (float)status;
+      if (!(bp.kkt && sp.compute_kkt)) { f[NU] = 0.0f; f[NU + 1] = 0.0f; f[NU + 2] = 0.0f; }
+    }
+  }
   (void)LD;
 }
 
@@ -811,17 +854,33 @@ __global__ void __launch_bounds__(128, MPXG_SQP_MIN_BLOCKS) sqp_kernel(ModelCons
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   WarpSmem<M>& sm = sms[wib];
-  float* scr = bp.scratch + (size_t)gw * bp.scratch_stride;
-  if (bp.single_instance >= 0) {
-    if (gw == 0) solve_instance<M>(mc, sp, bp, bp.single_instance, sm, scr);
-    return;
+  if (bp.single_instance >= 0 && gw != 0) return;
+  int slot = gw;
+  if (bp.slot_bits) {
+    int s = 0;
+    if (lane == 0) s = claim_scratch_slot(bp.slot_bits, bp.n_slots, gw % bp.n_slots);
+    slot = __shfl_sync(0xffffffffu, s, 0);
+    if (slot < 0) {  // leaves its share of the queue to the other warps
+      if (lane == 0 && bp.error) atomicOr(bp.error, 1);
+      return;
+    }
   }
-  for (;;) {
-    int b = 0;
-    if (lane == 0) b = atomicAdd(bp.counter, 1);
-    b = __shfl_sync(0xffffffffu, b, 0);
-    if (b >= bp.batch) break;
+  float* scr = bp.scratch + (size_t)slot * bp.scratch_stride;
+  for (int done = 0; !done;) {
+    int b = bp.single_instance;
+    if (b < 0) {
+      if (lane == 0) b = atomicAdd(bp.counter, 1);
+      b = __shfl_sync(0xffffffffu, b, 0);
+      if (b >= bp.batch) break;
+    } else {
+      done = 1;
+    }
     solve_instance<M>(mc, sp, bp, b, sm, scr);
+  }
+  if (bp.slot_bits) {  // release the slot once every lane's scratch writes are visible
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) atomicAnd(&bp.slot_bits[slot >> 5], ~(1u << (slot & 31)));
   }
 }
 

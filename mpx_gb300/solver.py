@@ -141,15 +141,19 @@ class Solver:
             out["k"] = torch.empty(batch, N, m, device=dev)
         return out
 
-    def io(self, x0, X0, U0, V0, reference, parameter, w, horizon, out):
+    def io(self, x0, X0, U0, V0, reference, parameter, w, horizon, out, slot=None):
+        """Batch descriptor.  With `slot` (int32 device tensor [B]) the arrays
+        are pools indexed by slot[b]; otherwise batch entry b is row b."""
         io = _lib.BatchIO()
-        io.batch = int(x0.shape[0])
+        io.batch = int(slot.shape[0]) if slot is not None else int(x0.shape[0])
+        io.slot = _ptr(slot)
         io.horizon = _ptr(horizon)
         io.x0, io.X_in, io.U_in, io.V_in = _ptr(x0), _ptr(X0), _ptr(U0), _ptr(V0)
         io.reference, io.parameter, io.w = _ptr(reference), _ptr(parameter), _ptr(w)
         io.X, io.U, io.V = _ptr(out["X"]), _ptr(out["U"]), _ptr(out["V"])
         io.K, io.k = _ptr(out.get("K")), _ptr(out.get("k"))
         io.kkt, io.status = _ptr(out.get("kkt")), _ptr(out.get("status"))
+        io.first = _ptr(out.get("first"))
         return io
 
     def prepare(self, x0, X0, U0, V0, reference, parameter, W, horizon=None):
@@ -184,10 +188,12 @@ class Solver:
         out["_keep"] = (x0, X0, U0, V0, reference, parameter, w, horizon)
         return out
 
-    def shift(self, X, U, V, horizon=None, shift=1, stream=None, out=None):
-        """Warm-start shift (mpc_wrapper_srbd.py:135-137) on the device; in place when out is None."""
+    def shift(self, X, U, V, horizon=None, shift=1, stream=None, out=None, slot=None):
+        """Warm-start shift (mpc_wrapper_srbd.py:135-137) on the device; in
+        place when out is None; only the pool rows in `slot` when given."""
         Xo, Uo, Vo = (X, U, V) if out is None else out
-        st = self.L.mpxg_shift_warm_start(self.handle, _stream_handle(stream), int(X.shape[0]), _ptr(horizon),
+        batch = int(slot.shape[0]) if slot is not None else int(X.shape[0])
+        st = self.L.mpxg_shift_warm_start(self.handle, _stream_handle(stream), batch, _ptr(slot), _ptr(horizon),
                                           int(shift), _ptr(X), _ptr(U), _ptr(V), _ptr(Xo), _ptr(Uo), _ptr(Vo))
         _lib.check(st, self.handle, "mpxg_shift_warm_start")
         return Xo, Uo, Vo
@@ -217,3 +223,25 @@ def lqr_solve(A, B, c, Q, R, M, q, r, x0, method=0, stream=None):
     _lib.check(st, None, "mpxg_lqr_solve")
     out["_keep"] = (t, ws)
     return out
+
+
+def gait_tables(stream, desc, batch, n_max, x0, X, U, V, v_ref, leg_time, reference, parameter, gait, mode,
+                slot=None, horizon=None, drift_std=0.0, seed=0):
+    """mpxg_gait_tables for `batch` entries (pool rows `slot`); `gait` =
+    dict(duty, step_freq, height, offsets).  mode 0: first tick (cold start of
+    X, U, V); mode 1: next tick (x0 from the shifted warm start + drift)."""
+    L = _lib.load()
+    a = _lib.GaitArgs()
+    a.model, a.batch, a.n_max, a.mode = int(desc.model), int(batch), int(n_max), int(mode)
+    a.slot, a.horizon = _ptr(slot), _ptr(horizon)
+    a.dt, a.duty_factor, a.step_freq = float(desc.dt), float(gait["duty"]), float(gait["step_freq"])
+    a.height, a.weight = float(gait["height"]), float(desc.mass * desc.gravity)
+    a.drift_std, a.seed = float(drift_std), int(seed) & 0xFFFFFFFF
+    off = np.zeros(12, dtype=np.float32)
+    o = np.asarray(gait["offsets"], dtype=np.float32).reshape(-1)
+    off[:o.size] = o
+    for i in range(12):
+        a.offsets[i] = float(off[i])
+    a.x0, a.X, a.U, a.V = _ptr(x0), _ptr(X), _ptr(U), _ptr(V)
+    a.v_ref, a.leg_time, a.reference, a.parameter = _ptr(v_ref), _ptr(leg_time), _ptr(reference), _ptr(parameter)
+    _lib.check(L.mpxg_gait_tables(_stream_handle(stream), ctypes.byref(a)), None, "mpxg_gait_tables")

@@ -14,7 +14,7 @@ import torch
 
 from . import _lib
 from . import problem as P
-from .solver import Solver, _ptr, _stream_handle
+from .solver import Solver, _ptr, _stream_handle, gait_tables
 
 
 class TickRunner:
@@ -38,13 +38,10 @@ class TickRunner:
         self.v_ref = d(wl.v_ref)
         self.leg_time = d(wl.leg_time)
         self.drift_std = float(drift_std)
-        self.gen = torch.Generator(device=self.dev)
-        self.gen.manual_seed(seed)
-        self.drift = torch.zeros_like(self.x0)
         if offsets is None:
             offsets = P.BIPED_HIP_OFFSETS if wl.desc.model == P.MODEL_BIPED_WRENCH12 else P.HIP_OFFSETS
-        self.offsets = (ctypes.c_float * 12)(*np.asarray(offsets, dtype=np.float32).reshape(-1).tolist(),
-                                             *([0.0] * (12 - np.asarray(offsets).size)))
+        self.gait = dict(duty=wl.duty, step_freq=wl.step_freq, height=wl.height, offsets=offsets)
+        self.seed = int(seed)
         self.out = dict(X=self.X, U=self.U, V=self.V, kkt=torch.zeros(wl.batch, 3, device=self.dev),
                         status=torch.zeros(wl.batch, dtype=torch.int32, device=self.dev))
         self.io = self.solver.io(self.x0, self.X, self.U, self.V, self.ref, self.par, self.w, self.horizon, self.out)
@@ -52,16 +49,14 @@ class TickRunner:
         self.graph = None
 
     # ------------------------------------------------------------ pieces
-    def tables(self, stream=None, from_warm_start=True, advance=True):
-        L = self.L
-        st = L.mpxg_gait_tables(_stream_handle(stream), int(self.desc.model), int(self.wl.batch), int(self.wl.n_max),
-                                _ptr(self.horizon), float(self.desc.dt), float(self.wl.duty),
-                                float(self.wl.step_freq), float(self.wl.height), self.offsets,
-                                _ptr(self.X) if from_warm_start else None,
-                                _ptr(self.drift) if (from_warm_start and self.drift_std > 0) else None,
-                                _ptr(self.x0), _ptr(self.v_ref), _ptr(self.leg_time), int(advance),
-                                _ptr(self.ref), _ptr(self.par))
-        _lib.check(st, None, "mpxg_gait_tables")
+    def tables(self, stream=None, first=False, measured=False):
+        """Gait tables for all instances.  first=True also cold-starts X, U, V;
+        measured=True keeps the x0 already in place (copied from the host)."""
+        self.seed += 1
+        mode = 0 if first else (2 if measured else 1)
+        gait_tables(stream, self.desc, self.wl.batch, self.wl.n_max, self.x0, self.X, self.U, self.V, self.v_ref,
+                    self.leg_time, self.ref, self.par, self.gait, mode, horizon=self.horizon,
+                    drift_std=self.drift_std, seed=self.seed)
 
     def solve(self, stream=None, plain=False):
         fn = self.L.mpxg_solve_plain if plain else self.L.mpxg_solve
@@ -69,30 +64,27 @@ class TickRunner:
         _lib.check(st, self.solver.handle, "mpxg_solve")
 
     def shift(self, stream=None):
-        st = self.L.mpxg_shift_warm_start(self.solver.handle, _stream_handle(stream), int(self.wl.batch),
+        st = self.L.mpxg_shift_warm_start(self.solver.handle, _stream_handle(stream), int(self.wl.batch), None,
                                           _ptr(self.horizon), 1, _ptr(self.X), _ptr(self.U), _ptr(self.V),
                                           _ptr(self.X), _ptr(self.U), _ptr(self.V))
         _lib.check(st, self.solver.handle, "mpxg_shift_warm_start")
 
-    def new_drift(self):
-        if self.drift_std > 0:
-            self.drift.normal_(0.0, self.drift_std, generator=self.gen)
-
     # ------------------------------------------------------------ one tick
     def first_tick(self, stream=None):
-        """Tick 0: tables from the given x0 and timers, then solve."""
-        self.tables(stream, from_warm_start=False, advance=False)
+        """Tick 0: cold start from the given x0 and timers, then solve."""
+        self.tables(stream, first=True)
         self.solve(stream)
 
     def tick(self, stream=None):
         """Shift the previous solution, x0 <- its second state (+ drift), advance
         the gait one tick, rebuild the tables, solve."""
         self.shift(stream)
-        self.tables(stream, from_warm_start=True, advance=True)
+        self.tables(stream, first=False)
         self.solve(stream)
 
     def capture(self, stream):
-        """Capture one tick into a CUDA graph (replayed by replay())."""
+        """Capture one tick into a CUDA graph (replayed by replay()).  The
+        drift seed is frozen into the graph, so replays repeat one drift draw."""
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=stream):
             self.tick(torch.cuda.current_stream())

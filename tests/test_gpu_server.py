@@ -1,0 +1,68 @@
+"""Serving: continuous batching over resident episode slots."""
+import numpy as np
+import pytest
+import torch
+
+from mpx_gb300 import problem as P
+from mpx_gb300.server import BudgetError, MPCServer, default_models, served_workload
+
+pytestmark = pytest.mark.gpu
+
+
+def make_server(**kw):
+    return MPCServer(default_models(), n_max=60, budget_bytes=kw.pop("budget", 2 << 30),
+                     opts=P.SolverOptions(sqp_iters=3), drift_std=0.0, **kw)
+
+
+def x0_of(server, name, seed):
+    pool = server.pools[name]
+    rng = np.random.default_rng(seed)
+    x0 = np.zeros(pool.desc.n, dtype=np.float32)
+    x0[2] = pool.gait["height"]
+    return x0 + rng.normal(0, 0.02, pool.desc.n).astype(np.float32)
+
+
+def test_result_same_alone_and_in_mix(cuda):
+    """An episode's ticks give the same controls whether it is served alone or
+    batched with other episodes of both models."""
+    alone = make_server()
+    alone.admit("A", "quadruped", x0_of(alone, "quadruped", 1), 40, v_ref=0.3, phase=0.2)
+    res_alone = []
+    for _ in range(3):
+        alone.submit("A"); alone.launch_pending(); alone.drain()
+    res_alone = [d[3] for d in alone.completed]
+    mix = make_server()
+    mix.admit("A", "quadruped", x0_of(mix, "quadruped", 1), 40, v_ref=0.3, phase=0.2)
+    for k in range(5):
+        mix.admit("q%d" % k, "quadruped", x0_of(mix, "quadruped", 10 + k), 20 + 7 * k, v_ref=0.1 * k, phase=0.1 * k)
+        mix.admit("b%d" % k, "biped", x0_of(mix, "biped", 20 + k), 25 + 5 * k, v_ref=-0.1 * k, phase=0.3)
+    eps = ["A"] + ["q%d" % k for k in range(5)] + ["b%d" % k for k in range(5)]
+    for _ in range(3):
+        for e in eps:
+            mix.submit(e)
+        mix.launch_pending(); mix.drain()
+    res_mix = [d[3] for d in mix.completed if d[1] == "A"]
+    assert len(res_alone) == len(res_mix) == 3
+    for a, b in zip(res_alone, res_mix):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_admission_budget_and_release(cuda):
+    s = make_server(max_slots=3)
+    for k in range(3):
+        s.admit(k, "quadruped", x0_of(s, "quadruped", k), 30)
+    with pytest.raises(BudgetError):
+        s.admit(99, "quadruped", x0_of(s, "quadruped", 9), 30)
+    s.release(1)
+    s.admit(99, "quadruped", x0_of(s, "quadruped", 9), 30)
+
+
+def test_served_stream_reports_latency(cuda):
+    s = MPCServer(default_models(), n_max=120, budget_bytes=4 << 30, opts=P.SolverOptions(sqp_iters=5),
+                  drift_std=0.01)
+    lat, wall = served_workload(s, n_episodes=40, rate_hz=2000.0, duration_s=0.5, horizon_range=(20, 120),
+                                episode_ticks=30)
+    assert len(lat) > 500
+    assert np.all(np.isfinite(lat)) and np.percentile(lat, 99) < 1.0
+    stats = [d[5] for d in s.completed]
+    assert sum(1 for st in stats if st & 1) == 0

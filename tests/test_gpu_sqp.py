@@ -88,7 +88,11 @@ def test_device_kkt_matches_fp64_evaluation(oracle, cuda, model):
 def test_near_converged_parity_1e4(oracle, cuda, model):
     """From a near-converged warm start (FP64 oracle, 15 iterations) two more
     SQP iterations on the GPU (FP32) and in the FP64 oracle agree to 1e-4
-    relative for trajectories, gains, feedforward and multipliers."""
+    relative for trajectories, multipliers, gains and feedforward -- or, where
+    float32 itself cannot resolve a quantity that well (the oracle's own FP32
+    run differs more), to within 3x the oracle-FP32 difference.  The
+    feedforward k tends to 0 at convergence, so it is measured on the scale of
+    the controls U."""
     wl = workload(model, 6, (25, 50), seed=17)
     o15 = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=15), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
                            wl.parameter, wl.W, wl.horizon)
@@ -96,21 +100,29 @@ def test_near_converged_parity_1e4(oracle, cuda, model):
                       o15["V"].astype(np.float32), wl.reference, wl.parameter, wl.W, wl.horizon)
     opts = P.SolverOptions(sqp_iters=2)
     g = gpu_solve(warm, opts)
-    o = oracle.sqp_solve(wl.desc, opts, wl.x0, warm.X0, warm.U0, warm.V0, wl.reference, wl.parameter, wl.W,
-                         wl.horizon)
+    args = (wl.desc, opts, wl.x0, warm.X0, warm.U0, warm.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+    o = oracle.sqp_solve(*args)
+    o32 = oracle.sqp_solve(*args, precision=32)
     if model == P.MODEL_SRBD_QUAT13:
-        # The quaternion's norm direction is neither penalised nor controllable
-        # (the dynamics renormalise it), so gain components along it are set by
-        # rounding (the FP32 oracle differs from FP64 there by ~2e-3): compare
-        # the gains on the tangent space of the unit quaternion.
-        for res in (g, o):
+        # gain components along the quaternion's norm direction are not
+        # determined (neither penalised nor controllable): compare on the
+        # tangent space of the unit quaternion
+        for res in (g, o, o32):
             for i, N in enumerate(wl.horizon):
                 for t in range(N):
                     q = o["X"][i, t, 3:7] / np.linalg.norm(o["X"][i, t, 3:7])
                     res["K"][i, t][:, 3:7] -= np.outer(res["K"][i, t][:, 3:7] @ q, q)
+
+    def err(a, b, key, kind):
+        if key != "k":
+            return rel_err(a, b, wl.horizon, kind)
+        e = max(np.abs(a[i, :N] - b[i, :N]).max() for i, N in enumerate(wl.horizon))
+        return e / max(np.abs(o["U"][i, :N]).max() for i, N in enumerate(wl.horizon))
+
     for key, kind in (("X", "x"), ("U", "u"), ("V", "x"), ("K", "u"), ("k", "u")):
-        e = rel_err(g[key], o[key], wl.horizon, kind)
-        assert e < 1e-4, (key, e)
+        eg = err(g[key], o[key], key, kind)
+        e32 = err(o32[key], o[key], key, kind)
+        assert eg < max(1e-4, 3.0 * e32), (key, eg, e32)
 
 
 def test_plain_path_is_bitwise_identical(cuda):
@@ -154,3 +166,37 @@ def test_in_place_warm_start(cuda):
     s.solve(wl.x0, X, U, V, wl.reference, wl.parameter, wl.W, wl.horizon, out=out)
     torch.cuda.synchronize()
     assert np.array_equal(X.cpu().numpy(), ref["X"])
+
+
+def test_overlapping_solves_on_one_handle(cuda):
+    """Solves of one handle issued on four streams at once -- sharing its
+    scratch-slot pool, each with its own work counter -- give the results of
+    the same solves issued one after another.  72 solves wrap the 64-entry
+    counter ring."""
+    wls = [workload(P.MODEL_SRBD_RPY12, 300, (25, 50, 100), seed=30 + i) for i in range(4)]
+    opts = P.SolverOptions(sqp_iters=3)
+    s = Solver(wls[0].desc, opts, n_max=wls[0].n_max, batch_max=300)
+    keys = ("X", "U", "V", "kkt", "status")
+    serial = []
+    for wl in wls:
+        o = s.solve(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+        torch.cuda.synchronize()
+        serial.append({k: o[k].cpu().numpy() for k in keys})
+    streams = [torch.cuda.Stream() for _ in range(4)]
+    outs = []
+    for r in range(18):
+        for i, wl in enumerate(wls):
+            with torch.cuda.stream(streams[i]):
+                outs.append((i, s.solve(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon,
+                                        stream=streams[i])))
+    torch.cuda.synchronize()
+    for i, o in outs:
+        for k in keys:
+            got = o[k].cpu().numpy()
+            for j, N in enumerate(wls[i].horizon):  # rows past the horizon are not outputs
+                rows = N + 1 if k in ("X", "V") else N
+                if k in ("kkt", "status"):
+                    assert np.array_equal(got[j], serial[i][k][j]), k
+                else:
+                    assert np.array_equal(got[j, :rows], serial[i][k][j, :rows]), k
+    s.close()
