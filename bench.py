@@ -50,12 +50,15 @@ def algorithmic_bytes(n, m, horizon, ref_cols, par_cols):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--plain-sample", type=int, default=256)
-    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--cpu-sample", type=int, default=1024, help="instances per step of --impl reference")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-stream section")
+    ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small run for ncu (no clocks, no CPU, no plain)")
@@ -77,7 +80,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
@@ -129,6 +132,40 @@ def cpu_solves_per_s(wl, sample, threads):
     return len(idx) / dt, dt
 
 
+def cpu_bounded(wl, threads, seconds):
+    """Oracle solves/s over a bounded sample: the batch is solved in chunks
+    of 512 instances, cycling through it, until `seconds` have elapsed."""
+    done, tot, i = 0, 0.0, 0
+    cpu_solves_per_s(wl, 32, threads)  # warm-up (thread pool, pages)
+    while tot < seconds:
+        idx = np.arange(i, i + 512) % wl.batch
+        sub = _subset(wl, idx)
+        _, dt = cpu_solves_per_s(sub, len(idx), threads)
+        tot += dt
+        done += len(idx)
+        i = (i + 512) % wl.batch
+    return done / tot, tot, done
+
+
+def _subset(wl, idx):
+    from mpx_gb300 import problem as P
+    return P.Workload(wl.desc, wl.x0[idx], wl.X0[idx], wl.U0[idx], wl.V0[idx], wl.reference[idx], wl.parameter[idx],
+                      wl.W[idx], wl.horizon[idx], leg_time=wl.leg_time[idx], v_ref=wl.v_ref[idx])
+
+
+def host_info():
+    info = {"cpu_count": os.cpu_count()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            k, _, v = ln.partition(":")
+            if k.strip() in ("Architecture", "Model name", "CPU(s)", "Thread(s) per core", "CPU max MHz"):
+                info[k.strip()] = v.strip()
+    except Exception:
+        pass
+    return info
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle (CPU restatement of the path) on host cores."""
     from mpx_gb300 import problem as P
@@ -139,11 +176,12 @@ def run_reference(args, rank, world):
     wl = P.quadruped_workload(args.batch, horizons=HORIZONS, seed=SEED, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
                               random_phase=True)
     sample = min(args.cpu_sample, args.batch)
-    for _ in range(max(args.warmup, 0) and 1):
-        cpu_solves_per_s(wl, min(sample, 32), threads)
+    for _ in range(max(args.warmup, 0)):
+        cpu_solves_per_s(wl, min(sample, 64), threads)
     times = []
-    for _ in range(args.steps):
-        _, dt = cpu_solves_per_s(wl, sample, threads)
+    for k in range(args.steps):  # step k solves the next `sample` instances of the batch
+        idx = (np.arange(sample) + k * sample) % wl.batch
+        _, dt = cpu_solves_per_s(_subset(wl, idx), sample, threads)
         times.append(dt)
     tot = sum(times)
     value = sample * args.steps / tot
@@ -154,8 +192,8 @@ def run_reference(args, rank, world):
         "dtype": "fp32", "data": "synthetic (seeded)", "impl": "reference",
         "config": config_dict(args.batch),
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": "%d instances of tick 0 per step, 5 SQP iterations, FP32, OpenMP over instances"
-                                   % sample},
+                         "sample": "%d instances of the tick-0 batch per step, 5 SQP iterations, FP32 oracle (C++), "
+                                   "OpenMP over instances" % sample, "host": host_info()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -246,6 +284,7 @@ def run_ours(args, rank, world, local_rank):
     x0_host.copy_(tr.x0.cpu())
     res_host = torch.empty(B, m + 4, pin_memory=True)
     res_dev = torch.empty(B, m + 4, device=dev)
+    tr.set_result_rows(res_dev)  # the solve writes [first control | kkt | status] per instance
     e2e_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     e2e_steps = args.steps
     torch.cuda.synchronize()
@@ -259,10 +298,7 @@ def run_ours(args, rank, world, local_rank):
             tr.shift(stream)
             tr.tables(stream, measured=True)
             tr.solve(stream)
-            res_dev[:, :m].copy_(tr.U[:, 0, :])                   # first control (the reference's .grf)
-            res_dev[:, m:m + 3].copy_(tr.out["kkt"])
-            res_dev[:, m + 3].copy_(tr.out["status"].float())
-            res_host.copy_(res_dev, non_blocking=True)             # result out
+            res_host.copy_(res_dev, non_blocking=True)             # result rows out
         e2e_ev[1].record(stream)
     torch.cuda.synchronize()
     e2e_ms = e2e_ev[0].elapsed_time(e2e_ev[1])
@@ -319,14 +355,63 @@ def run_ours(args, rank, world, local_rank):
                                 "what": "one launch of one instance (%d launches timed)" % nl}}
         tp.solver.close()
 
+    # ---------------- the same batch with every horizon N = 50
+    n50 = None
+    if not args.no_n50 and not args.profile:
+        wl50 = P.quadruped_workload(B, horizons=(50,), seed=SEED + rank, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
+                                    random_phase=True)
+        t50 = TickRunner(wl50, opts, device=dev, drift_std=DRIFT)
+        with torch.cuda.stream(stream):
+            t50.first_tick(stream)
+            for _ in range(max(args.warmup, 3)):
+                t50.tick(stream)
+        torch.cuda.synchronize()
+        a50, b50 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a50.record(stream)
+            for _ in range(args.steps):
+                t50.tick(stream)
+            b50.record(stream)
+        torch.cuda.synchronize()
+        ms50 = a50.elapsed_time(b50) / args.steps
+        k50 = t50.out["kkt"][:, 2].float().cpu().numpy()
+        n50 = {"solves_per_s_per_gpu": B / (ms50 / 1000.0), "ms_per_tick": ms50, "horizon": 50,
+               "kkt_frac_le_1e-5": float((k50 <= 1e-5).mean())}
+        t50.solver.close()
+        del t50
+
+    # ---------------- served request stream (continuous batching), rank 0
+    served = None
+    if not args.no_served and not args.profile and rank == 0:
+        from mpx_gb300.server import MPCServer, default_models, served_workload
+        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=4,
+                        device=dev)
+        served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, seed=1)  # warm-up
+        srv.completed.clear()
+        launches0 = srv.launches
+        lat, wall = served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=2.0, seed=2)
+        sk = np.array([d[4][2] for d in srv.completed])
+        sst = np.array([d[5] for d in srv.completed])
+        served = {"offered_req_per_s": 20000.0, "completed_req_per_s": len(lat) / wall, "requests": int(len(lat)),
+                  "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
+                                 "p99": 1e3 * float(np.percentile(lat, 99)),
+                                 "what": "submit to result row on the host, real-time Poisson arrivals"},
+                  "kkt_frac_le_1e-5": float((sk <= 1e-5).mean()), "nan_status": int(((sst & 1) != 0).sum()),
+                  "gpu_launches": srv.launches - launches0,
+                  "workload": "Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, "
+                              "alternating), N uniform in [20, 200], 200-tick episodes, state drift N(0, 0.01^2), "
+                              "8 GB admission budget, 4 streams"}
+        del srv
+
     # ---------------- CPU baseline (oracle, rank 0)
     cpu = None
     if rank == 0 and not args.no_cpu and not args.profile:
         threads = os.cpu_count() or 1
-        v, dt = cpu_solves_per_s(wl, args.cpu_sample, threads)
+        v, dt, done = cpu_bounded(wl, threads, args.cpu_seconds)
         cpu = {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": "%d instances of tick 0, 5 SQP iterations, FP32 oracle (C++), OpenMP over instances; %.1f s"
-                         % (min(args.cpu_sample, B), dt)}
+               "sample": "%d solves (the %d-instance tick-0 batch, repeated) in %.1f s: 5 SQP iterations, FP32 "
+                         "oracle (C++, -O3), OpenMP over instances" % (done, B, dt),
+               "host": host_info()}
 
     # ---------------- roofline of the solve kernel
     import json as _json
@@ -365,6 +450,8 @@ def run_ours(args, rank, world, local_rank):
         "fp32": {"achieved_tflops": flops / (solve_avg / 1000.0) / 1e12, "nominal_peak_tflops": fp32_nominal,
                  "frac": flops / (solve_avg / 1000.0) / 1e12 / fp32_nominal,
                  "flops": "work-efficient Riccati count per stage per iteration"},
+        "n50": n50,
+        "served": served,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": tr.launches_per_tick * args.steps,

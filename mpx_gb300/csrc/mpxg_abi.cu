@@ -30,6 +30,7 @@ struct mpxg_handle {
   // solves captured into CUDA graphs.
   static constexpr int kRing = 64, kCounterStride = 32;
   int* counters = nullptr;
+  int* orders = nullptr;               // per ring entry: batch_max queue-order entries
   cudaEvent_t ring_ev[kRing] = {};
   bool ring_used[kRing] = {};
   int ring_next = 0, capture_next = 0;
@@ -141,7 +142,7 @@ size_t mpxg_workspace_bytes(const mpxg_problem_desc* d, const mpxg_solver_opts* 
   const long long stride = scratch_stride_for(d->model, d->n_max);
   const size_t slots = (size_t)scratch_slots(d->model, wpb, sms);
   return (size_t)stride * sizeof(float) * slots + (slots + 31) / 32 * 4 + 256 +
-         (size_t)2 * mpxg_handle::kRing * mpxg_handle::kCounterStride * sizeof(int);
+         (size_t)2 * mpxg_handle::kRing * (mpxg_handle::kCounterStride + (size_t)d->batch_max) * sizeof(int);
 }
 
 mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, mpxg_handle** out) {
@@ -168,8 +169,9 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   const size_t bytes = (size_t)h->scratch_stride * sizeof(float) * (size_t)h->n_slots;
   const size_t nwords = ((size_t)h->n_slots + 31) / 32;
   const size_t ctr_bytes = (size_t)2 * mpxg_handle::kRing * mpxg_handle::kCounterStride * sizeof(int);
+  const size_t order_bytes = (size_t)2 * mpxg_handle::kRing * (size_t)d->batch_max * sizeof(int);
   if (cudaMalloc(&h->scratch, bytes) != cudaSuccess || cudaMalloc(&h->slot_bits, nwords * 4 + 256) != cudaSuccess ||
-      cudaMalloc(&h->counters, ctr_bytes) != cudaSuccess) {
+      cudaMalloc(&h->counters, ctr_bytes) != cudaSuccess || cudaMalloc(&h->orders, order_bytes) != cudaSuccess) {
     cudaGetLastError();
     mpxg_destroy(h);
     return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_create: scratch allocation failed");
@@ -213,6 +215,7 @@ void mpxg_destroy(mpxg_handle* h) {
   if (h->scratch) cudaFree(h->scratch);
   if (h->slot_bits) cudaFree(h->slot_bits);
   if (h->counters) cudaFree(h->counters);
+  if (h->orders) cudaFree(h->orders);
   for (int i = 0; i < mpxg_handle::kRing; ++i)
     if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
   delete h;
@@ -294,6 +297,14 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
   bp.counter = h->counters + (size_t)r * mpxg_handle::kCounterStride;
   cudaError_t e = cudaMemsetAsync(bp.counter, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
+  if (io->horizon && io->batch > h->total_warps) {  // more instances than warps: longest horizons first
+    int* order = h->orders + (size_t)r * h->desc.batch_max;
+    order_by_horizon_kernel<<<1, 1024, (size_t)(h->desc.n_max + 1) * sizeof(int), st>>>(
+        io->batch, h->desc.n_max, io->slot, io->horizon, order);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, "order_by_horizon_kernel launch");
+    bp.order = order;
+  }
   const int wpb = h->warps_per_block;
   int blocks = h->num_sms * h->blocks_per_sm;
   const int need = (io->batch + wpb - 1) / wpb;

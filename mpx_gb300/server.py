@@ -241,7 +241,7 @@ class MPCServer:
             _lib.check(self.L.mpxg_solve(solver.handle, hs, ctypes.byref(io)), solver.handle, "mpxg_solve")
             res_h[:nb].copy_(res_d[:nb], non_blocking=True)
             ev.record(st)
-        self.launches += (2 if nw else 0) + (1 if nc else 0) + 1
+        self.launches += (2 if nw else 0) + (1 if nc else 0) + solver.launches_per_solve(nb)
         self.inflight.append((ev, pool, batch, stg))
         return nb
 

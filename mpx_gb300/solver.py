@@ -115,6 +115,18 @@ class Solver:
         except Exception:
             pass
 
+    @property
+    def total_warps(self):
+        """Warps of one persistent launch; mpxg_solve orders batches larger
+        than this longest-horizon-first with one extra launch."""
+        if getattr(self, "_total_warps", None) is None:
+            g = self.geometry()
+            self._total_warps = g["warps_per_block"] * g["blocks_per_sm"] * g["num_sms"]
+        return self._total_warps
+
+    def launches_per_solve(self, batch, horizon=True):
+        return 2 if (horizon and batch > self.total_warps) else 1
+
     def geometry(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _lib.check(self.L.mpxg_query_geometry(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),

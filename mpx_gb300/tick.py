@@ -45,8 +45,15 @@ class TickRunner:
         self.out = dict(X=self.X, U=self.U, V=self.V, kkt=torch.zeros(wl.batch, 3, device=self.dev),
                         status=torch.zeros(wl.batch, dtype=torch.int32, device=self.dev))
         self.io = self.solver.io(self.x0, self.X, self.U, self.V, self.ref, self.par, self.w, self.horizon, self.out)
-        self.launches_per_tick = 3
+        self.launches_per_tick = 2 + self.solver.launches_per_solve(wl.batch)  # tables, shift, (order,) solve
         self.graph = None
+
+    def set_result_rows(self, first):
+        """Have each solve also write one row per instance into `first`
+        ([batch, m+4] float32 device tensor: first control, KKT residuals,
+        status) -- the rows a caller copies back to the host each tick."""
+        self.out["first"] = first
+        self.io = self.solver.io(self.x0, self.X, self.U, self.V, self.ref, self.par, self.w, self.horizon, self.out)
 
     # ------------------------------------------------------------ pieces
     def tables(self, stream=None, first=False, measured=False):

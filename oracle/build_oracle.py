@@ -29,7 +29,7 @@ def build(force=False, verbose=False):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp.%d" % os.getpid()
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
            "-o", tmp] + [os.path.join(HERE, s) for s in SOURCES]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

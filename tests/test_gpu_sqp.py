@@ -200,3 +200,24 @@ def test_overlapping_solves_on_one_handle(cuda):
                 else:
                     assert np.array_equal(got[j, :rows], serial[i][k][j, :rows]), k
     s.close()
+
+
+def test_longest_first_order_keeps_results(cuda):
+    """A batch larger than the persistent grid is served longest horizon
+    first (an extra ordering launch); every instance's result is bitwise the
+    one it gets when solved in a small batch."""
+    wl = workload(P.MODEL_SRBD_RPY12, 4000, (25, 50, 100), seed=17)
+    opts = P.SolverOptions(sqp_iters=2)
+    s = Solver(wl.desc, opts, n_max=wl.n_max, batch_max=wl.batch)
+    assert wl.batch > s.total_warps
+    s.close()
+    full = gpu_solve(wl, opts)
+    pick = np.array([0, 1, 2, 999, 2500, 3999])
+    sub = P.Workload(wl.desc, wl.x0[pick], wl.X0[pick], wl.U0[pick], wl.V0[pick], wl.reference[pick],
+                     wl.parameter[pick], wl.W[pick], wl.horizon[pick])
+    few = gpu_solve(sub, opts)
+    for j, i in enumerate(pick):
+        N = wl.horizon[i]
+        assert np.array_equal(few["X"][j, :N + 1], full["X"][i, :N + 1])
+        assert np.array_equal(few["U"][j, :N], full["U"][i, :N])
+        assert np.array_equal(few["status"][j], full["status"][i])
