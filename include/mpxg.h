@@ -164,6 +164,38 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
 
 /* Gait timer of a batch (mpx/utils/mpc_utils.py:7-14), float32 without fused
  * multiply-add: leg_time [B, n_legs] updated in place, contact [B, n_legs]. */
+/* Cost and constraint residuals of trajectories X [batch, n_max+1, n], U
+ * [batch, n_max, m] with the handle's model (replaces
+ * optimizers.model_evaluator_helper(cost, dynamics, x0, X, U) -> (g, c),
+ * called at mpx/utils/mpc_wrapper.py:419-423,452-465):
+ *   g [batch, n_max+1]     g[b,t] = sqrt(l_t), stage cost t (terminal cost
+ *                          at t = N), so sum(g^2) is the objective;
+ *   c [batch, n_max+1, n]  c[b,0] = x0 - X[0], c[b,t] = f(X[t-1], U[t-1]) - X[t],
+ *                          so sum(c^2) is the reference's constraint figure.
+ * Rows past horizon[b] (n_max when horizon is NULL) are zero. */
+mpxg_status mpxg_evaluate(mpxg_handle* h, void* stream, int batch, const int* horizon, const float* x0,
+                          const float* X, const float* U, const float* reference, const float* parameter,
+                          const float* w, float* g, float* c);
+
+/* Opaque operand of the XLA custom call below. */
+typedef struct {
+  mpxg_problem_desc desc;
+  mpxg_solver_opts opts;
+  int batch;
+  int reserved;
+} mpxg_xla_opaque;
+
+/* XLA custom-call target (status-returning custom-call signature: stream,
+ * buffers, opaque, opaque_len, XlaCustomCallStatus*), so a JAX program can
+ * keep the solve inside jax.jit as the reference does with
+ * jax.jit(jax.vmap(optimizers.mpc ...)) (mpx/utils/mpc_wrapper_srbd.py:68,77).
+ * buffers: reference, parameter, w (the diagonal [B,24] of W), x0, X0, U0, V0,
+ * then the results X, U, V, in the reference's argument order.  All horizons
+ * are desc.n_max.  A handle per (device, opaque) is created on first use and
+ * kept.  Errors go to XlaCustomCallStatusSetFailure when the host process
+ * exports it, and to mpxg_last_error(NULL). */
+void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status);
+
 mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_factor, float step_freq, float dt,
                            float* leg_time, int* contact);
 

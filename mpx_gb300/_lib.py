@@ -39,6 +39,10 @@ class SolverOpts(ctypes.Structure):
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
 
 
+class XlaOpaque(ctypes.Structure):
+    _fields_ = [("desc", ProblemDesc), ("opts", SolverOpts), ("batch", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
 class BatchIO(ctypes.Structure):
     _fields_ = [("batch", ctypes.c_int), ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
                 ("x0", ctypes.c_void_p), ("X_in", ctypes.c_void_p), ("U_in", ctypes.c_void_p),
@@ -68,7 +72,7 @@ class LqIO(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
 
 _lib = None
 
@@ -95,6 +99,10 @@ def load(build_if_missing=True):
     vp = ctypes.c_void_p
     L.mpxg_create.argtypes = [ctypes.POINTER(ProblemDesc), ctypes.POINTER(SolverOpts), ctypes.POINTER(vp)]
     L.mpxg_create.restype = ctypes.c_int
+    L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
+    L.mpxg_xla_solve.restype = None
+    L.mpxg_evaluate.argtypes = [vp, vp, ctypes.c_int] + [vp] * 9
+    L.mpxg_evaluate.restype = ctypes.c_int
     L.mpxg_destroy.argtypes = [vp]
     L.mpxg_destroy.restype = None
     L.mpxg_query_geometry.argtypes = [vp, c_int_p, c_int_p, c_int_p]

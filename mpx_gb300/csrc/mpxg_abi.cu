@@ -2,13 +2,17 @@
 // host side of every launch.  No torch types cross this boundary.
 #include <cuda_runtime.h>
 
+#include <dlfcn.h>
+
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
 #include "../../include/mpxg.h"
 #include "aux_kernels.cuh"
+#include "evaluate_kernel.cuh"
 #include "lqr_kernels.cuh"
 #include "sqp_kernel.cuh"
 
@@ -350,6 +354,37 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
   return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "shift_kernel launch");
 }
 
+mpxg_status mpxg_evaluate(mpxg_handle* h, void* stream, int batch, const int* horizon, const float* x0,
+                          const float* X, const float* U, const float* reference, const float* parameter,
+                          const float* w, float* g, float* c) {
+  if (!h) return fail(nullptr, MPXG_ERR_INVALID_ARG, "null handle");
+  if (batch < 0 || batch > h->desc.batch_max || !x0 || !X || !U || !reference || !parameter || !w || !g || !c)
+    return fail(h, MPXG_ERR_INVALID_ARG, "mpxg_evaluate: bad arguments");
+  if (batch == 0) return MPXG_OK;
+  const long long n = (long long)batch * (h->desc.n_max + 1);
+  const int threads = 128;
+  const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nm = h->desc.n_max;
+  switch (h->desc.model) {
+    case MPXG_MODEL_SRBD_QUAT13:
+      evaluate_kernel<ModelQuat13><<<blocks, threads, 0, st>>>(h->mc, batch, nm, horizon, x0, X, U, reference,
+                                                              parameter, w, g, c);
+      break;
+    case MPXG_MODEL_SRBD_RPY12:
+      evaluate_kernel<ModelRpy12><<<blocks, threads, 0, st>>>(h->mc, batch, nm, horizon, x0, X, U, reference,
+                                                             parameter, w, g, c);
+      break;
+    case MPXG_MODEL_BIPED_WRENCH12:
+      evaluate_kernel<ModelBiped12><<<blocks, threads, 0, st>>>(h->mc, batch, nm, horizon, x0, X, U, reference,
+                                                               parameter, w, g, c);
+      break;
+    default: return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_evaluate: model");
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "evaluate_kernel launch");
+}
+
 mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_factor, float step_freq, float dt,
                            float* leg_time, int* contact) {
   if (batch < 0 || n_legs < 1 || !leg_time || !contact) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_timer_run");
@@ -549,4 +584,84 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
     case MPXG_MODEL_BIPED_WRENCH12: return noalloc_launch<ModelBiped12>(mc, sp, st, bp, (int)blocks, wpb);
     default: return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_solve_noalloc: model");
   }
+}
+
+// ============================================================================
+// XLA custom-call target (status-returning custom-call signature).
+//
+// The reference jit-compiles the solve (jax.jit(jax.vmap(...)),
+// mpx/utils/mpc_wrapper_srbd.py:68,77); registering this target with XLA keeps
+// that call inside a compiled JAX program.  Operands and results arrive as
+// device buffers in the order of optimizers.mpc(reference, parameter, W, x0,
+// X0, U0, V0) -> (X, U, V), with W passed as its diagonal [B,24].  The opaque
+// string is an mpxg_xla_opaque; handles are created on first use per
+// (device, opaque) and kept for the life of the process.
+// ============================================================================
+namespace {
+
+std::mutex g_xla_mu;
+std::map<std::string, mpxg_handle*> g_xla_handles;
+
+typedef void (*xla_status_set_failure_fn)(void*, const char*, size_t);
+
+void xla_fail(void* status, const std::string& msg) {
+  g_lib_err = msg;
+  static xla_status_set_failure_fn setter =
+      (xla_status_set_failure_fn)dlsym(RTLD_DEFAULT, "XlaCustomCallStatusSetFailure");
+  if (status && setter) setter(status, msg.c_str(), msg.size());
+}
+
+}  // namespace
+
+extern "C" void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status) {
+  if (!buffers || !opaque || opaque_len != sizeof(mpxg_xla_opaque)) {
+    xla_fail(status, "mpxg_xla_solve: opaque must be an mpxg_xla_opaque (" + std::to_string(sizeof(mpxg_xla_opaque)) +
+                         " bytes), got " + std::to_string(opaque_len));
+    return;
+  }
+  mpxg_xla_opaque op;
+  std::memcpy(&op, opaque, sizeof(op));
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    xla_fail(status, "mpxg_xla_solve: cudaGetDevice failed");
+    return;
+  }
+  if (op.batch < 0 || op.batch > op.desc.batch_max) {
+    xla_fail(status, "mpxg_xla_solve: batch exceeds desc.batch_max");
+    return;
+  }
+  std::string key(reinterpret_cast<const char*>(&dev), sizeof(dev));
+  key.append(reinterpret_cast<const char*>(&op.desc), sizeof(op.desc));
+  key.append(reinterpret_cast<const char*>(&op.opts), sizeof(op.opts));
+  mpxg_handle* h = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_xla_mu);
+    auto it = g_xla_handles.find(key);
+    if (it != g_xla_handles.end()) {
+      h = it->second;
+    } else {
+      mpxg_status st = mpxg_create(&op.desc, &op.opts, &h);
+      if (st != MPXG_OK) {
+        xla_fail(status, std::string("mpxg_xla_solve: mpxg_create: ") + g_lib_err);
+        return;
+      }
+      g_xla_handles[key] = h;
+    }
+  }
+  mpxg_batch_io io;
+  std::memset(&io, 0, sizeof(io));
+  io.batch = op.batch;
+  io.reference = (const float*)buffers[0];
+  io.parameter = (const float*)buffers[1];
+  io.w = (const float*)buffers[2];
+  io.x0 = (const float*)buffers[3];
+  io.X_in = (const float*)buffers[4];
+  io.U_in = (const float*)buffers[5];
+  io.V_in = (const float*)buffers[6];
+  io.X = (float*)buffers[7];
+  io.U = (float*)buffers[8];
+  io.V = (float*)buffers[9];
+  std::lock_guard<std::mutex> lock(g_xla_mu);  // a handle is used by one host thread at a time
+  if (mpxg_solve(h, stream, &io) != MPXG_OK) xla_fail(status, std::string("mpxg_xla_solve: ") + h->err);
 }

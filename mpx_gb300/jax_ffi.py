@@ -1,0 +1,107 @@
+"""JAX binding of the batched solve: libmpxg's `mpxg_xla_solve` as an XLA
+custom call, so a JAX program keeps the solve inside `jax.jit` as the
+reference does with `jax.jit(jax.vmap(optimizers.mpc ...))`
+(mpx/utils/mpc_wrapper_srbd.py:68,77; mpx/utils/mpc_wrapper.py:74).
+
+Registered only when `jax` imports; nothing here runs otherwise.  Usage:
+
+    from mpx_gb300 import jax_ffi
+    solve = jax_ffi.make_mpc(desc, opts, n_max=N, batch=B)   # jit-compatible
+    X, U, V = solve(reference, parameter, W, x0, X0, U0, V0)  # [B, ...] arrays
+
+The call is batched natively ([B, ...] operands, one persistent launch), so
+it replaces the vmapped solve as a whole rather than being vmapped itself.
+W is reduced to its diagonal in the program (the SRBD weights are diagonal,
+mpx/config/config_srbd.py:90).  The custom call uses XLA's status-returning
+legacy signature (api_version 2); the target is registered for the CUDA
+platform through `jax.ffi.register_ffi_target(..., api_version=0)`.
+"""
+import ctypes
+
+from . import _lib
+from .solver import problem_desc, solver_opts
+
+try:  # optional dependency
+    import jax
+    import jax.numpy as jnp
+    from jax.interpreters import mlir
+    from jax.interpreters.mlir import ir
+    try:
+        from jax.extend.core import Primitive
+    except ImportError:  # older jax
+        from jax.core import Primitive
+    HAVE_JAX = True
+except ImportError:
+    HAVE_JAX = False
+
+TARGET = "mpxg_xla_solve"
+_registered = False
+_prim = None
+
+
+def available():
+    return HAVE_JAX
+
+
+def register():
+    """Register the custom-call target with XLA (once)."""
+    global _registered
+    if not HAVE_JAX:
+        raise RuntimeError("jax is not installed; the XLA custom call is unavailable")
+    if _registered:
+        return
+    L = _lib.load()
+    fn = ctypes.cast(L.mpxg_xla_solve, ctypes.c_void_p).value
+    capsule_new = ctypes.pythonapi.PyCapsule_New
+    capsule_new.restype = ctypes.py_object
+    capsule_new.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+    capsule = capsule_new(fn, b"xla._CUSTOM_CALL_TARGET", None)
+    jax.ffi.register_ffi_target(TARGET, capsule, platform="CUDA", api_version=0)
+    _registered = True
+
+
+def opaque_bytes(desc, opts, n_max, batch):
+    op = _lib.XlaOpaque()
+    op.desc = problem_desc(desc, n_max, batch)
+    op.opts = solver_opts(opts)
+    op.batch = int(batch)
+    return bytes(op)
+
+
+def _primitive():
+    global _prim
+    if _prim is not None:
+        return _prim
+    p = Primitive("mpxg_mpc")
+    p.multiple_results = True
+
+    def abstract(reference, parameter, w, x0, X0, U0, V0, *, opaque):
+        return (jax.core.ShapedArray(X0.shape, jnp.float32), jax.core.ShapedArray(U0.shape, jnp.float32),
+                jax.core.ShapedArray(V0.shape, jnp.float32))
+
+    def lowering(ctx, reference, parameter, w, x0, X0, U0, V0, *, opaque):
+        outs = [mlir.aval_to_ir_type(a) for a in ctx.avals_out]
+        call = mlir.custom_call(TARGET, result_types=outs, operands=[reference, parameter, w, x0, X0, U0, V0],
+                                backend_config=opaque, api_version=2, has_side_effect=False)
+        return call.results
+
+    p.def_abstract_eval(abstract)
+    mlir.register_lowering(p, lowering, platform="cuda")
+    _prim = p
+    return p
+
+
+def make_mpc(desc, opts, n_max, batch):
+    """A jit-compatible batched solve (reference, parameter, W, x0, X0, U0, V0)
+    -> (X, U, V) for `batch` instances of horizon n_max."""
+    register()
+    opaque = opaque_bytes(desc, opts, n_max, batch)
+    prim = _primitive()
+
+    def solve(reference, parameter, W, x0, X0, U0, V0):
+        f32 = lambda a: jnp.asarray(a, jnp.float32)
+        w = jnp.diagonal(f32(W), axis1=-2, axis2=-1) if jnp.ndim(W) == 3 else f32(W)
+        return tuple(prim.bind(f32(reference), f32(parameter), w, f32(x0), f32(X0), f32(U0), f32(V0),
+                               opaque=opaque))
+
+    return solve

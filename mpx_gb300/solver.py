@@ -200,6 +200,19 @@ class Solver:
         out["_keep"] = (x0, X0, U0, V0, reference, parameter, w, horizon)
         return out
 
+    def evaluate(self, x0, X, U, reference, parameter, W, horizon=None, stream=None):
+        """(g, c) of trajectories X, U (the reference's model_evaluator_helper,
+        mpc_wrapper.py:419-423,452-465): g [B, n_max+1] with sum(g^2) = the
+        objective, c [B, n_max+1, n] the initial-state and dynamics defects."""
+        x0, X, U, _, reference, parameter, w, horizon = self.prepare(x0, X, U, X, reference, parameter, W, horizon)
+        B = x0.shape[0]
+        g = torch.empty(B, self.n_max + 1, device=self.device)
+        c = torch.empty(B, self.n_max + 1, self.desc.n, device=self.device)
+        st = self.L.mpxg_evaluate(self.handle, _stream_handle(stream), B, _ptr(horizon), _ptr(x0), _ptr(X), _ptr(U),
+                                  _ptr(reference), _ptr(parameter), _ptr(w), _ptr(g), _ptr(c))
+        _lib.check(st, self.handle, "mpxg_evaluate")
+        return g, c
+
     def shift(self, X, U, V, horizon=None, shift=1, stream=None, out=None, slot=None):
         """Warm-start shift (mpc_wrapper_srbd.py:135-137) on the device; in
         place when out is None; only the pool rows in `slot` when given."""

@@ -299,9 +299,10 @@ class MPCControllerWrapper:
             out = one.solve(x0, X, U, V, ref, par, self.w, out=dict(X=X, U=U, V=V, kkt=torch.zeros(1, 3, device=self.dev),
                                                                    status=torch.zeros(1, dtype=torch.int32, device=self.dev)))
             outputs.append(X.clone())
-            c = float(out["kkt"][0, 0].item())
-            cost = float(torch.sum(X * X).item())
-            if last - cost < 1e-3 and c * c < 1e-5:
+            g, c = one.evaluate(x0, X, U, ref, par, self.w)   # model_evaluator_helper (:452)
+            cost = float(torch.sum(g * g).item())
+            csq = float(torch.sum(c * c).item())
+            if last - cost < 1e-3 and csq < 1e-5:
                 break
             last = cost
         self.X0, self.U0, self.V0 = X, U, V

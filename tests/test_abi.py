@@ -44,7 +44,8 @@ def test_struct_layouts_match_header():
 #include <stdio.h>
 #include "mpxg.h"
 int main(void) {
-  printf("%zu %zu %zu %zu\n", sizeof(mpxg_problem_desc), sizeof(mpxg_solver_opts), sizeof(mpxg_batch_io), sizeof(mpxg_lq_io));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(mpxg_problem_desc), sizeof(mpxg_solver_opts), sizeof(mpxg_batch_io),
+         sizeof(mpxg_lq_io), sizeof(mpxg_xla_opaque));
   return 0;
 }
 '''
@@ -55,4 +56,15 @@ int main(void) {
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", exe, c], check=True)
         sizes = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert sizes == [ctypes.sizeof(_lib.ProblemDesc), ctypes.sizeof(_lib.SolverOpts), ctypes.sizeof(_lib.BatchIO),
-                     ctypes.sizeof(_lib.LqIO)]
+                     ctypes.sizeof(_lib.LqIO), ctypes.sizeof(_lib.XlaOpaque)]
+
+
+def test_xla_target_rejects_a_malformed_opaque():
+    """The XLA custom-call target checks its opaque operand before touching
+    the GPU and reports through mpxg_last_error(NULL) (no XLA status setter
+    in this process)."""
+    from mpx_gb300 import _lib
+    L = _lib.load()
+    bufs = (ctypes.c_void_p * 10)()
+    L.mpxg_xla_solve(None, bufs, b"short", 5, None)
+    assert b"mpxg_xla_opaque" in L.mpxg_last_error(None)

@@ -1,0 +1,48 @@
+"""The XLA custom-call target mpxg_xla_solve: opaque packing (CPU) and, on
+the GPU, the same results as mpxg_solve on the same operands."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from mpx_gb300 import _lib, jax_ffi
+from mpx_gb300 import problem as P
+
+
+def test_opaque_packs_desc_opts_and_batch():
+    wl = P.quadruped_workload(3, horizons=(20,), seed=1, model=P.MODEL_SRBD_RPY12)
+    b = jax_ffi.opaque_bytes(wl.desc, P.SolverOptions(sqp_iters=4), 20, 3)
+    assert len(b) == ctypes.sizeof(_lib.XlaOpaque)
+    op = _lib.XlaOpaque.from_buffer_copy(b)
+    assert (op.batch, op.desc.n_max, op.desc.batch_max, op.opts.sqp_iters, op.desc.model) == (3, 20, 3, 4,
+                                                                                                P.MODEL_SRBD_RPY12)
+
+
+def test_jax_binding_is_optional():
+    if not jax_ffi.available():
+        with pytest.raises(RuntimeError):
+            jax_ffi.register()
+
+
+@pytest.mark.gpu
+def test_xla_target_matches_mpxg_solve(cuda):
+    import torch
+    from mpx_gb300.solver import Solver, weights_diagonal
+    wl = P.quadruped_workload(6, horizons=(30,), seed=5, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
+                              random_phase=True)
+    opts = P.SolverOptions(sqp_iters=3)
+    s = Solver(wl.desc, opts, n_max=30, batch_max=6)
+    ref = s.solve(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W)
+    torch.cuda.synchronize()
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to("cuda", torch.float32).contiguous()
+    ins = [d(wl.reference), d(wl.parameter), weights_diagonal(torch.as_tensor(wl.W), 6).to("cuda", torch.float32).contiguous(),
+           d(wl.x0), d(wl.X0), d(wl.U0), d(wl.V0)]
+    outs = [torch.empty_like(ins[4]), torch.empty_like(ins[5]), torch.empty_like(ins[6])]
+    bufs = (ctypes.c_void_p * 10)(*[t.data_ptr() for t in ins + outs])
+    op = jax_ffi.opaque_bytes(wl.desc, opts, 30, 6)
+    L = _lib.load()
+    L.mpxg_xla_solve(None, bufs, op, len(op), None)
+    torch.cuda.synchronize()
+    for got, key in zip(outs, ("X", "U", "V")):
+        assert np.array_equal(got.cpu().numpy(), ref[key].cpu().numpy()), key
+    s.close()
