@@ -210,6 +210,7 @@ def config_dict(batch):
 def run_ours(args, rank, world, local_rank):
     import torch
     from mpx_gb300 import problem as P
+    from mpx_gb300.replicas import max_over_ranks
     from mpx_gb300.tick import TickRunner
 
     torch.cuda.set_device(local_rank)
@@ -258,10 +259,7 @@ def run_ours(args, rank, world, local_rank):
     clk = clocks.stop() if clocks else None
     tick_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, device=dev)  # the job ends with its slowest replica
     value = world * B * args.steps / (total_ms / 1000.0)
 
     # ---------------- solve kernel alone (roofline): ungraphed ticks with events around the solve
@@ -301,7 +299,7 @@ def run_ours(args, rank, world, local_rank):
             res_host.copy_(res_dev, non_blocking=True)             # result rows out
         e2e_ev[1].record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e2e_ev[0].elapsed_time(e2e_ev[1])
+    e2e_ms = max_over_ranks(e2e_ev[0].elapsed_time(e2e_ev[1]), device=dev)
     e2e_value = world * B * e2e_steps / (e2e_ms / 1000.0)
     h2d = B * n * 4
     d2h = B * (m + 4) * 4
