@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream section")
     ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
+    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr"],
+                    help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve")
+    ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small run for ncu (no clocks, no CPU, no plain)")
@@ -461,6 +464,135 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ isolated LQR (KKT) workload
+LQR_B, LQR_N, LQR_NX, LQR_NU = 1024, 128, 24, 12
+
+
+def lqr_data(B, N, n, m, seed, chunk=64):
+    """Seeded random time-varying LQR problems (float32), generated in chunks."""
+    from mpx_gb300 import problem as P
+    parts = [P.random_lq(min(chunk, B - i), n, m, N, seed=seed + i) for i in range(0, B, chunk)]
+    return {k: np.concatenate([p[k] for p in parts], 0).astype(np.float32) for k in parts[0]}
+
+
+def run_lqr(args, rank, world, local_rank):
+    """--workload lqr: the isolated KKT/LQR solve, B=1024 problems with n=24,
+    m=12, N=128 (mpxg_lqr_solve; --lqr-method 0 sequential Riccati, 1 scan)."""
+    import torch
+    from mpx_gb300 import _lib
+    from mpx_gb300.replicas import max_over_ranks
+    from mpx_gb300.solver import _ptr, _stream_handle
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    B, N, n, m = LQR_B, LQR_N, LQR_NX, LQR_NU
+    d = lqr_data(B, N, n, m, seed=11 + 1000 * rank)
+    names = ("A", "B", "c", "Q", "R", "M", "q", "r", "x0")
+    host = {k: torch.from_numpy(d[k]).pin_memory() for k in names}
+    dv = {k: host[k].to(dev) for k in names}
+    outs = dict(K=torch.empty(B, N, m, n, device=dev), k=torch.empty(B, N, m, device=dev),
+                X=torch.empty(B, N + 1, n, device=dev), U=torch.empty(B, N, m, device=dev),
+                lam=torch.empty(B, N + 1, n, device=dev))
+    L = _lib.load()
+    method = int(args.lqr_method)
+    ws = torch.empty(max(int(L.mpxg_lqr_workspace_bytes(B, N, n, m, method)) // 4, 1), device=dev)
+    io = _lib.LqIO()
+    io.batch, io.N, io.n, io.m = B, N, n, m
+    for name, key in zip(("A", "Bm", "c", "Q", "R", "M", "q", "r", "x0"), names):
+        setattr(io, name, _ptr(dv[key]))
+    for key in ("K", "k", "X", "U", "lam"):
+        setattr(io, key, _ptr(outs[key]))
+    io.workspace = _ptr(ws)
+    stream = torch.cuda.Stream(device=dev)
+    hs = _stream_handle(stream)
+
+    def solve():
+        _lib.check(L.mpxg_lqr_solve(hs, ctypes.byref(io), method), None, "mpxg_lqr_solve")
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            solve()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for k in range(args.steps):
+            solve()
+            ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    per = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[-1]), device=dev)
+    value = world * B * args.steps / (total_ms / 1000.0)
+    # end to end: inputs from pinned host memory in, all outputs back
+    out_h = {k: torch.empty(v.shape, pin_memory=True) for k, v in outs.items()}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    esteps = max(2, min(args.steps, 5))
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(esteps):
+            for k in names:
+                dv[k].copy_(host[k], non_blocking=True)
+            solve()
+            for k in outs:
+                out_h[k].copy_(outs[k], non_blocking=True)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), device=dev)
+    h2d = sum(host[k].numel() * 4 for k in names)
+    d2h = sum(v.numel() * 4 for v in outs.values())
+    # roofline: compulsory bytes and work-efficient Riccati FLOPs per launch
+    avg_s = (sum(per) / len(per)) / 1000.0
+    flops = B * N * f_lqr(n, m)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+    gbs = (h2d + d2h) / avg_s / 1e9
+    tfs = flops / avg_s / 1e12
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        done, tot, i = 0, 0.0, 0
+        while tot < args.cpu_seconds:
+            sl = slice(i, i + 64)
+            t0 = time.perf_counter()
+            O.lqr_solve(*[d[k][sl] for k in names], precision=32, n_threads=threads)
+            tot += time.perf_counter() - t0
+            done += 64
+            i = (i + 64) % B
+        cpu = {"value": done / tot, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": "%d LQR solves (64-problem chunks of the batch) in %.1f s: sequential Riccati, FP32 oracle "
+                         "(C++, -O3), OpenMP over problems" % (done, tot), "host": host_info()}
+    line = {
+        "metric": "LQR solves/s (isolated KKT solve, n=24, m=12, N=128, batch 1024)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded)",
+        "config": {"workload": "1024 random time-varying LQR problems, n=24, m=12, N=128 (A = I + 0.05 G rescaled "
+                               "to spectral radius 0.98, B ~ N(0,1/m), Q = M M^T/n + 0.1 I, R = 0.1 I, S = 0)",
+                   "method": ["sequential Riccati", "associative scan"][method],
+                   "l2": "inputs (1.2 GB) larger than L2", "parallelism": "replicas"},
+        "roofline": {"bound": "hbm" if gbs / hbm_peak >= tfs / fp32_nominal else "fp32", "achieved": gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak, "traffic": None,
+                     "algorithmic_bytes": h2d + d2h, "kernel": "mpxg_lqr_solve method %d" % method},
+        "fp32": {"achieved_tflops": tfs, "nominal_peak_tflops": fp32_nominal, "frac": tfs / fp32_nominal,
+                 "flops": "work-efficient Riccati count F_LQR(24,12) = 127,872 per stage"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * B * esteps / (e2e_ms / 1000.0), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps * (1 if method == 0 else 1),
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -472,7 +604,10 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    run_ours(args, rank, world, local_rank)
+    if args.workload == "lqr":
+        run_lqr(args, rank, world, local_rank)
+    else:
+        run_ours(args, rank, world, local_rank)
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()

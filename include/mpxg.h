@@ -168,8 +168,9 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
  * [batch, n_max, m] with the handle's model (replaces
  * optimizers.model_evaluator_helper(cost, dynamics, x0, X, U) -> (g, c),
  * called at mpx/utils/mpc_wrapper.py:419-423,452-465):
- *   g [batch, n_max+1]     g[b,t] = sqrt(l_t), stage cost t (terminal cost
- *                          at t = N), so sum(g^2) is the objective;
+ *   g [batch, n_max+1]     g[b,t] = l_t, the cost of stage t (terminal cost
+ *                          at t = N; may be negative with the relaxed log
+ *                          barrier), so sum(g) is the objective;
  *   c [batch, n_max+1, n]  c[b,0] = x0 - X[0], c[b,t] = f(X[t-1], U[t-1]) - X[t],
  *                          so sum(c^2) is the reference's constraint figure.
  * Rows past horizon[b] (n_max when horizon is NULL) are zero. */

@@ -34,7 +34,7 @@ __global__ void evaluate_kernel(ModelConst mc, int batch, int n_max, const int* 
 #pragma unroll
   for (int a = 0; a < NU; ++a) ut[a] = t < N ? Ub[t * NU + a] : 0.0f;
   const float l = stage_cost<M>(mc, xt, ut, ref + ((size_t)b * (n_max + 1) + t) * M::NREF, w + (size_t)b * 24, t == N);
-  g[idx] = sqrtf(fmaxf(l, 0.0f));
+  g[idx] = l;
   if (t == 0) {
 #pragma unroll
     for (int i = 0; i < NX; ++i) co[i] = x0[(size_t)b * NX + i] - xt[i];

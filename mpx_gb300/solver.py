@@ -202,8 +202,9 @@ class Solver:
 
     def evaluate(self, x0, X, U, reference, parameter, W, horizon=None, stream=None):
         """(g, c) of trajectories X, U (the reference's model_evaluator_helper,
-        mpc_wrapper.py:419-423,452-465): g [B, n_max+1] with sum(g^2) = the
-        objective, c [B, n_max+1, n] the initial-state and dynamics defects."""
+        mpc_wrapper.py:419-423,452-465): g [B, n_max+1] the stage costs (sum =
+        the objective), c [B, n_max+1, n] the initial-state and dynamics
+        defects."""
         x0, X, U, _, reference, parameter, w, horizon = self.prepare(x0, X, U, X, reference, parameter, W, horizon)
         B = x0.shape[0]
         g = torch.empty(B, self.n_max + 1, device=self.device)

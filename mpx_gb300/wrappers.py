@@ -287,7 +287,8 @@ class MPCControllerWrapper:
     def runOffline(self, qpos, qvel, reference, parameter, max_iter=100):
         """mpc_wrapper.py:387-468: repeat single SQP iterations until the
         reference's stop rule  last_cost - cost < 1e-3 and sum(c^2) < 1e-5
-        (:465).  `reference`/`parameter` are the offline tables."""
+        (:465), with cost the objective (sum of the stage costs) and c the
+        defects.  `reference`/`parameter` are the offline tables."""
         x0 = _to_dev(self._state(qpos, qvel).reshape(1, -1), self.dev)
         ref = _to_dev(reference, self.dev).reshape(1, self.N + 1, -1)
         par = _to_dev(parameter, self.dev).reshape(1, self.N + 1, -1)
@@ -300,7 +301,7 @@ class MPCControllerWrapper:
                                                                    status=torch.zeros(1, dtype=torch.int32, device=self.dev)))
             outputs.append(X.clone())
             g, c = one.evaluate(x0, X, U, ref, par, self.w)   # model_evaluator_helper (:452)
-            cost = float(torch.sum(g * g).item())
+            cost = float(torch.sum(g).item())
             csq = float(torch.sum(c * c).item())
             if last - cost < 1e-3 and csq < 1e-5:
                 break

@@ -26,7 +26,7 @@ def test_evaluate_matches_oracle(oracle, cuda, model):
         for t in range(N + 1):
             u = wl.U0[b, t] if t < N else np.zeros(wl.desc.m)
             l = oracle.cost(wl.desc, wl.X0[b, t], u, wl.reference[b, t], wl.W[b], terminal=(t == N))
-            assert abs(g[b, t] ** 2 - l) <= 1e-4 * max(1.0, abs(l)), (b, t, g[b, t] ** 2, l)
+            assert abs(g[b, t] - l) <= 1e-4 * max(1.0, abs(l)), (b, t, g[b, t], l)
             if t == 0:
                 ref_c = wl.x0[b] - wl.X0[b, 0]
             else:
