@@ -245,8 +245,11 @@ mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* args);
  * terminal Q[N], q[N].  A [B,N,n,n], Bm [B,N,n,m], c [B,N,n], Q [B,N+1,n,n],
  * R [B,N,m,m], M [B,N,n,m], q [B,N+1,n], r [B,N,m], x0 [B,n].
  * Outputs K [B,N,m,n], k [B,N,m], X [B,N+1,n], U [B,N,m], lam [B,N+1,n]
- * (costates dV_t/dx_t).  `method`: 0 sequential Riccati, 1 time-parallel
- * associative scan. */
+ * (costates dV_t/dx_t).  `method`: 0 sequential Riccati (one block per
+ * problem); 1 time-parallel associative scan of the value-function recursion
+ * over 8 horizon chunks (one 8-warp block per problem).  Built sizes (n, m):
+ * (24,12) (12,12) (8,4) (4,2).  Stands in for the LQR/KKT step of the absent
+ * primal_dual_ilqr solver (parallel in time, README.md:23-24,29). */
 typedef struct {
   int batch, N, n, m;
   const float *A, *Bm, *c, *Q, *R, *M, *q, *r, *x0;

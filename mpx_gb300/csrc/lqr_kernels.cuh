@@ -12,6 +12,7 @@
 #include <string>
 
 #include "../../include/mpxg.h"
+#include "lqr_scan.cuh"
 
 namespace mpxg {
 
@@ -207,8 +208,16 @@ __global__ void lqr_riccati_kernel(mpxg_lq_io io, float* Pscr) {
 inline size_t lqr_scratch_bytes(int batch, int N, int n) { return (size_t)batch * (N + 1) * (n + 1) * (n + 1) * 4; }
 
 template <int NX, int NU>
-inline cudaError_t launch_lqr(cudaStream_t st, const mpxg_lq_io& io, float* scr) {
-  lqr_riccati_kernel<NX, NU><<<io.batch, LqDims<NX, NU>::NT, 0, st>>>(io, scr);
+inline cudaError_t launch_lqr(cudaStream_t st, const mpxg_lq_io& io, float* scr, int method) {
+  if (method == 1) {
+    const size_t smem = lqscan::scan_smem_bytes<NX, NU>();
+    cudaError_t e = cudaFuncSetAttribute(lqscan::lqr_scan_kernel<NX, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    lqscan::lqr_scan_kernel<NX, NU><<<io.batch, lqscan::kWarps * 32, smem, st>>>(io, scr);
+  } else {
+    lqr_riccati_kernel<NX, NU><<<io.batch, LqDims<NX, NU>::NT, 0, st>>>(io, scr);
+  }
   return cudaGetLastError();
 }
 
@@ -220,18 +229,18 @@ inline mpxg_status lqr_solve_host(void* stream, const mpxg_lq_io* io, int method
     *err = "mpxg_lqr_solve: bad arguments";
     return MPXG_ERR_INVALID_ARG;
   }
-  if (method != 0) {
-    *err = "mpxg_lqr_solve: method not built";
+  if (method != 0 && method != 1) {
+    *err = "mpxg_lqr_solve: method must be 0 (sequential Riccati) or 1 (associative scan)";
     return MPXG_ERR_UNSUPPORTED;
   }
   if (io->batch == 0) return MPXG_OK;
   float* scr = io->workspace;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
-  if (io->n == 24 && io->m == 12) e = launch_lqr<24, 12>(st, *io, scr);
-  else if (io->n == 12 && io->m == 12) e = launch_lqr<12, 12>(st, *io, scr);
-  else if (io->n == 8 && io->m == 4) e = launch_lqr<8, 4>(st, *io, scr);
-  else if (io->n == 4 && io->m == 2) e = launch_lqr<4, 2>(st, *io, scr);
+  if (io->n == 24 && io->m == 12) e = launch_lqr<24, 12>(st, *io, scr, method);
+  else if (io->n == 12 && io->m == 12) e = launch_lqr<12, 12>(st, *io, scr, method);
+  else if (io->n == 8 && io->m == 4) e = launch_lqr<8, 4>(st, *io, scr, method);
+  else if (io->n == 4 && io->m == 2) e = launch_lqr<4, 2>(st, *io, scr, method);
   else {
     *err = "mpxg_lqr_solve: (n, m) not instantiated; built sizes: (24,12) (12,12) (8,4) (4,2)";
     return MPXG_ERR_UNSUPPORTED;
