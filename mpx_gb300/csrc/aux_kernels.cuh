@@ -254,31 +254,56 @@ __device__ __forceinline__ float hash_normal(unsigned int seed, unsigned int row
   return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);         // Box-Muller
 }
 
+// One warp per batch entry, a lane per stage.  A lane reaches its stage's
+// gait timers by replaying the timer steps from the entry's timers, so every
+// stage sees the same float sequence as a sequential sweep.
 __global__ void gait_tables_kernel(mpxg_gait_args g, int nx, int nu, int legs, int ref_cols, int par_cols,
                                    int contact_col) {
-  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (bi >= g.batch) return;
   const int b = g.slot ? g.slot[bi] : bi;
   const int N = g.horizon ? g.horizon[b] : g.n_max;
   if (N < 1 || N > g.n_max) return;
   const size_t xo = (size_t)b * (g.n_max + 1) * nx;
   float* x0 = g.x0 + (size_t)b * nx;
+  // state of this tick: mode 1 takes the shifted warm start plus drift
+  float px0, py0, x0l = 0.0f;
   if (g.mode == 1) {
-    for (int i = 0; i < nx; ++i)
-      x0[i] = g.X[xo + i] + (g.drift_std > 0.0f ? g.drift_std * hash_normal(g.seed, (unsigned)b, (unsigned)i) : 0.0f);
+    const bool dr = g.drift_std > 0.0f;
+    px0 = g.X[xo + 0] + (dr ? g.drift_std * hash_normal(g.seed, (unsigned)b, 0u) : 0.0f);
+    py0 = g.X[xo + 1] + (dr ? g.drift_std * hash_normal(g.seed, (unsigned)b, 1u) : 0.0f);
+    if (lane < nx) x0l = g.X[xo + lane] + (dr ? g.drift_std * hash_normal(g.seed, (unsigned)b, (unsigned)lane) : 0.0f);
+  } else {
+    px0 = x0[0];
+    py0 = x0[1];
+    if (lane < nx) x0l = x0[lane];
   }
+  __syncwarp();
+  if (g.mode == 1 && lane < nx) x0[lane] = x0l;
   const float inc = __fmul_rn(g.dt, g.step_freq);
-  float lt[4];
+  float lt0[4];
   for (int i = 0; i < legs; ++i) {
-    lt[i] = g.leg_time[b * legs + i];
-    if (g.mode != 0) { int c; timer_step(g.duty_factor, inc, lt[i], c); g.leg_time[b * legs + i] = lt[i]; }
+    lt0[i] = g.leg_time[b * legs + i];
+    if (g.mode != 0) { int c; timer_step(g.duty_factor, inc, lt0[i], c); }
   }
+  __syncwarp();
+  if (g.mode != 0 && lane < legs) g.leg_time[b * legs + lane] = lt0[lane < legs ? lane : 0];
   const float v = g.v_ref[b];
-  const float px0 = x0[0], py0 = x0[1];
   float* ref = g.reference + (size_t)b * (g.n_max + 1) * ref_cols;
   float* par = g.parameter + (size_t)b * (g.n_max + 1) * par_cols;
   const int per = nu / legs;
-  for (int t = 0; t <= N; ++t) {
+  // timers at stage `lane` (t = lane + 1 steps from lt0); later stages advance by 32
+  float lt[4];
+  int cs[4];
+  for (int i = 0; i < legs; ++i) {
+    lt[i] = lt0[i];
+    for (int k = 0; k <= lane; ++k) timer_step(g.duty_factor, inc, lt[i], cs[i]);
+  }
+  for (int t = lane; t <= N; t += 32) {
+    if (t != lane)
+      for (int i = 0; i < legs; ++i)
+        for (int k = 0; k < 32; ++k) timer_step(g.duty_factor, inc, lt[i], cs[i]);
     float* rr = ref + (size_t)t * ref_cols;
     float* pp = par + (size_t)t * par_cols;
     for (int k = 0; k < ref_cols; ++k) rr[k] = 0.0f;
@@ -286,9 +311,7 @@ __global__ void gait_tables_kernel(mpxg_gait_args g, int nx, int nu, int legs, i
     rr[0] = px; rr[1] = py0; rr[2] = g.height;
     if (nx == 13) { rr[3] = 1.0f; rr[7] = v; } else { rr[6] = v; }
     int ns = 0;
-    int cs[4];
     for (int i = 0; i < legs; ++i) {
-      timer_step(g.duty_factor, inc, lt[i], cs[i]);
       ns += cs[i];
       rr[contact_col + i] = (float)cs[i];
       pp[i] = (float)cs[i];

@@ -406,7 +406,7 @@ mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* a) {
       !a->leg_time || !a->reference || !a->parameter || (a->mode == 0 && (!a->U || !a->V)))
     return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_gait_tables: bad arguments");
   if (a->batch == 0) return MPXG_OK;
-  gait_tables_kernel<<<(a->batch + 127) / 128, 128, 0, (cudaStream_t)stream>>>(*a, nx, nu, legs, rc, pc, cc);
+  gait_tables_kernel<<<(a->batch + 3) / 4, 128, 0, (cudaStream_t)stream>>>(*a, nx, nu, legs, rc, pc, cc);  // warp per entry
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "gait_tables_kernel launch");
 }

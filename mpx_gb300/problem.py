@@ -207,10 +207,11 @@ def quadruped_tables(desc, x0, leg_time, v_ref, horizon, n_max, duty=0.6, step_f
         ref[:, :, 6] = v_ref[:, None]
         ref[:, :, 12:16] = contacts
     par[:, :, 0:4] = contacts
+    off = HIP_OFFSETS.astype(np.float32)  # float32 sums, as the device tables
     for i in range(4):
-        par[:, :, 4 + 3 * i] = px + HIP_OFFSETS[i, 0]
-        par[:, :, 5 + 3 * i] = py + HIP_OFFSETS[i, 1]
-        par[:, :, 6 + 3 * i] = height + HIP_OFFSETS[i, 2]
+        par[:, :, 4 + 3 * i] = px + off[i, 0]
+        par[:, :, 5 + 3 * i] = py + off[i, 1]
+        par[:, :, 6 + 3 * i] = np.float32(height) + off[i, 2]
     # beyond each instance's horizon the rows are left as computed (never read)
     return ref, par
 
@@ -323,9 +324,10 @@ def biped_tables(desc, x0, leg_time, v_ref, n_max, duty=0.6, step_freq=1.25, hei
     ref[:, :, 2] = height
     ref[:, :, 6] = v_ref[:, None]
     for i in range(2):
-        par[:, :, 2 + 3 * i] = px + BIPED_HIP_OFFSETS[i, 0]
-        par[:, :, 3 + 3 * i] = py + BIPED_HIP_OFFSETS[i, 1]
-        par[:, :, 4 + 3 * i] = height + BIPED_HIP_OFFSETS[i, 2]
+        off = BIPED_HIP_OFFSETS.astype(np.float32)  # float32 sums, as the device tables
+        par[:, :, 2 + 3 * i] = px + off[i, 0]
+        par[:, :, 3 + 3 * i] = py + off[i, 1]
+        par[:, :, 4 + 3 * i] = np.float32(height) + off[i, 2]
     return ref, par
 
 

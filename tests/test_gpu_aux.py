@@ -121,3 +121,53 @@ def test_refgen_and_timer_match_golden(cuda):
     np.testing.assert_allclose(pard.cpu().numpy(), gpar, rtol=2e-6, atol=2e-6)
     np.testing.assert_allclose(frdd.cpu().numpy(), G["refgen_out_foot_ref_dot"], rtol=1e-5, atol=1e-5)
     np.testing.assert_allclose(tl[5].cpu().numpy(), G["refgen_out_liftoff"], rtol=2e-6, atol=2e-6)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_gait_tables_match_host_tables(cuda, mode):
+    """mpxg_gait_tables (warp per entry, lane per stage) reproduces the host
+    trot tables bit for bit, through a slot subset of a pool; mode 0 also
+    cold-starts X, V, U; mode 1 first takes x0 from the warm start and
+    advances the gait timers one tick."""
+    from mpx_gb300.solver import gait_tables
+    rng = np.random.default_rng(9)
+    desc = P.quadruped_rpy12()
+    pool, n_max = 7, 70
+    slots = np.array([5, 0, 3, 6], dtype=np.int32)
+    horizon = rng.integers(1, n_max + 1, size=pool).astype(np.int32)
+    horizon[5] = n_max
+    x0 = rng.normal(0, 0.1, (pool, desc.n)).astype(np.float32)
+    Xw = rng.normal(0, 0.1, (pool, n_max + 1, desc.n)).astype(np.float32)
+    lt = rng.uniform(0, 1, (pool, 4)).astype(np.float32)
+    v = rng.uniform(-1, 1, pool).astype(np.float32)
+    d = lambda a, dt=torch.float32: torch.as_tensor(a).to("cuda", dt).contiguous()
+    tx0, tX, tlt, tv = d(x0), d(Xw), d(lt), d(v)
+    tU = torch.zeros(pool, n_max, desc.m, device="cuda")
+    tV = torch.ones(pool, n_max + 1, desc.n, device="cuda")
+    ref = torch.zeros(pool, n_max + 1, desc.ref_cols, device="cuda")
+    par = torch.zeros(pool, n_max + 1, desc.par_cols, device="cuda")
+    gait = dict(duty=0.6, step_freq=2.0, height=0.30, offsets=P.HIP_OFFSETS)
+    gait_tables(None, desc, len(slots), n_max, tx0, tX, tU, tV, tv, tlt, ref, par, gait, mode,
+                slot=d(slots, torch.int32), horizon=d(horizon, torch.int32))
+    torch.cuda.synchronize()
+    xs = x0.copy()
+    lts = lt.copy()
+    if mode == 1:
+        xs = Xw[:, 0, :].copy()
+        _, lts = P.timer_run_np(0.6, 2.0, lts, desc.dt)
+    href, hpar = P.quadruped_tables(desc, xs, lts, v, horizon, n_max)
+    gref, gpar, gx0, glt = ref.cpu().numpy(), par.cpu().numpy(), tx0.cpu().numpy(), tlt.cpu().numpy()
+    for s in slots:
+        N = horizon[s]
+        assert np.array_equal(gref[s, :N + 1], href[s, :N + 1]), s
+        assert np.array_equal(gpar[s, :N + 1], hpar[s, :N + 1]), s
+        assert np.array_equal(gx0[s], xs[s])
+        assert np.array_equal(glt[s], lts[s] if mode == 1 else lt[s])
+        if mode == 0:
+            gX, gV, gU = tX.cpu().numpy(), tV.cpu().numpy(), tU.cpu().numpy()
+            assert np.array_equal(gX[s, :N + 1], np.repeat(xs[s][None], N + 1, 0))
+            assert not gV[s, :N + 1].any()
+            fz = gU[s, :N, 2::3]
+            assert np.all((fz > 0) == (href[s, :N, 12:16] > 0))
+    untouched = np.setdiff1d(np.arange(pool), slots)
+    assert not gref[untouched].any() and not gpar[untouched].any()
