@@ -385,7 +385,7 @@ def run_ours(args, rank, world, local_rank):
     served = None
     if not args.no_served and not args.profile and rank == 0:
         from mpx_gb300.server import MPCServer, default_models, served_workload
-        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=4,
+        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=16,
                         device=dev)
         served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, seed=1)  # warm-up
         srv.completed.clear()
@@ -401,7 +401,19 @@ def run_ours(args, rank, world, local_rank):
                   "gpu_launches": srv.launches - launches0,
                   "workload": "Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, "
                               "alternating), N uniform in [20, 200], 200-tick episodes, state drift N(0, 0.01^2), "
-                              "8 GB admission budget, 4 streams"}
+                              "8 GB admission budget, 16 streams"}
+        # the same stream with every episode a quadruped at N = 50 (the latency target's case)
+        srv.close()
+        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=16,
+                        device=dev)
+        served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, horizon_range=(50, 50), seed=1,
+                        models=("quadruped",))
+        lat50, wall50 = served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=2.0, horizon_range=(50, 50),
+                                        seed=2, models=("quadruped",))
+        served["n50_quadruped"] = {"completed_req_per_s": len(lat50) / wall50,
+                                   "latency_ms": {"p50": 1e3 * float(np.percentile(lat50, 50)),
+                                                  "p99": 1e3 * float(np.percentile(lat50, 99))}}
+        srv.close()
         del srv
 
     # ---------------- CPU baseline (oracle, rank 0)

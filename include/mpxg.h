@@ -211,9 +211,9 @@ mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt
                              const float* contact, float* liftoff, float* reference, float* parameter,
                              float* foot_ref_dot);
 
-/* Gait tables of the synthetic trot / walk workloads, one thread per batch
- * entry (row slot[b] of every per-instance array, or row b when slot is
- * NULL):
+/* Gait tables of the synthetic trot / walk workloads, one warp per batch
+ * entry and a lane per stage (row slot[b] of every per-instance array, or
+ * row b when slot is NULL):
  *   mode 0 (first tick): x0 as given, timers as given; the warm start is
  *          initialised (X = x0 at every stage, V = 0, U = `weight` split over
  *          the legs in stance at each stage);
@@ -272,6 +272,79 @@ mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method);
  * reported through mpxg_last_error(NULL). */
 mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* desc, const mpxg_solver_opts* opts, void* stream,
                                const mpxg_batch_io* io);
+
+/* ---------------------------------------------------------------- serving
+ * A served MPC stream: each request is one control tick of a persistent
+ * episode (a robot).  The server keeps every admitted episode's warm start
+ * (X, U, V), gait timers, horizon and weights resident on the device in
+ * per-model slot pools sized by a device-memory budget; a tick moves only the
+ * batch's slot ids in and one result row out.  Requests submitted while
+ * earlier batches run form the next batch, launched on the next of `streams`
+ * CUDA streams (continuous batching): per batch, the warm-start shift and
+ * gait tables of its episodes (cold start for new episodes and after a
+ * non-finite result, the NaN fallback of mpx/utils/mpc_wrapper.py:79-98), one
+ * persistent solve over their scattered slots, and one copy of the result
+ * rows.  No counterpart in the reference, which solves one fixed batch per
+ * call (mpx/utils/mpc_wrapper_srbd.py:91-141).
+ * Single-threaded: one host thread drives a server. */
+typedef struct {
+  mpxg_problem_desc desc;   /* n_max and batch_max are set by the server */
+  float duty_factor, step_freq, height;
+  float offsets[12];        /* foot offsets from the CoM reference, per leg (x, y, z) */
+  float phase0[4];          /* gait timer of each leg at phase 0 */
+  float w[24];              /* diagonal cost weights */
+} mpxg_served_model;
+
+typedef struct {
+  int n_models;
+  const mpxg_served_model* models;
+  int n_max;                /* longest horizon of any episode */
+  size_t budget_bytes;      /* device memory for slots + solver scratch, split evenly over the models */
+  int max_slots;            /* cap per model (0: as many as the budget allows) */
+  int streams;              /* concurrent batches (CUDA streams) */
+  float drift_std;          /* per-tick state drift N(0, drift_std^2) added on the device */
+  unsigned int seed;
+  mpxg_solver_opts opts;
+} mpxg_server_desc;
+
+typedef struct {
+  long long ticket;
+  int episode;
+  int status;               /* MPXG_INST_* bits */
+  float u0[12];             /* first control of the solution (m entries used) */
+  float kkt[3];             /* r_prim, r_dual, max */
+} mpxg_result;
+
+typedef struct mpxg_server mpxg_server;
+
+mpxg_status mpxg_server_create(const mpxg_server_desc* desc, mpxg_server** out);
+void mpxg_server_destroy(mpxg_server* s);
+/* Slots of model `model` (the number of episodes it can hold at once). */
+int mpxg_server_capacity(const mpxg_server* s, int model);
+/* Admit an episode: x0 [n] (host), horizon 1..n_max, forward speed v_ref,
+ * gait phase offset.  Returns its id in *episode, or MPXG_ERR_BUDGET when the
+ * model's slots are all taken.  Its first tick cold-starts on the device. */
+mpxg_status mpxg_server_admit(mpxg_server* s, int model, const float* x0, int horizon, float v_ref, float phase,
+                              int* episode);
+/* Cold-start the episode's next tick (from a new x0 when x0 is not NULL). */
+mpxg_status mpxg_server_reset(mpxg_server* s, int episode, const float* x0);
+/* Free the episode's slot once its queued and running ticks are done. */
+mpxg_status mpxg_server_release(mpxg_server* s, int episode);
+/* Queue the episode's next control tick; *ticket identifies its result. */
+mpxg_status mpxg_submit(mpxg_server* s, int episode, long long* ticket);
+/* Collect finished batches and launch queued ticks on free streams (one tick
+ * per episode in flight at a time).  Never blocks; `block` != 0 waits for the
+ * oldest running batch first.  *launched / *finished (may be NULL): ticks
+ * launched / completed by this call. */
+mpxg_status mpxg_server_step(mpxg_server* s, int block, int* launched, int* finished);
+/* The result of `ticket` (MPXG_ERR_NOT_READY until its batch finished; a
+ * result is returned once). */
+mpxg_status mpxg_poll(mpxg_server* s, long long ticket, mpxg_result* result);
+/* Results finished since the last call, up to `max`; *count set. */
+mpxg_status mpxg_server_completed(mpxg_server* s, mpxg_result* results, int max, int* count);
+/* Ticks queued, running; kernel launches issued so far. */
+mpxg_status mpxg_server_stats(const mpxg_server* s, int* queued, int* running, long long* launches);
+const char* mpxg_server_last_error(const mpxg_server* s);
 
 /* Last error message of a handle (or of the library when h is NULL). */
 const char* mpxg_last_error(const mpxg_handle* h);

@@ -43,6 +43,23 @@ class XlaOpaque(ctypes.Structure):
     _fields_ = [("desc", ProblemDesc), ("opts", SolverOpts), ("batch", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
+class ServedModel(ctypes.Structure):
+    _fields_ = [("desc", ProblemDesc), ("duty_factor", ctypes.c_float), ("step_freq", ctypes.c_float),
+                ("height", ctypes.c_float), ("offsets", ctypes.c_float * 12), ("phase0", ctypes.c_float * 4),
+                ("w", ctypes.c_float * 24)]
+
+
+class ServerDesc(ctypes.Structure):
+    _fields_ = [("n_models", ctypes.c_int), ("models", ctypes.POINTER(ServedModel)), ("n_max", ctypes.c_int),
+                ("budget_bytes", ctypes.c_size_t), ("max_slots", ctypes.c_int), ("streams", ctypes.c_int),
+                ("drift_std", ctypes.c_float), ("seed", ctypes.c_uint), ("opts", SolverOpts)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_longlong), ("episode", ctypes.c_int), ("status", ctypes.c_int),
+                ("u0", ctypes.c_float * 12), ("kkt", ctypes.c_float * 3)]
+
+
 class BatchIO(ctypes.Structure):
     _fields_ = [("batch", ctypes.c_int), ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
                 ("x0", ctypes.c_void_p), ("X_in", ctypes.c_void_p), ("U_in", ctypes.c_void_p),
@@ -72,7 +89,10 @@ class LqIO(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve",
+           "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
+           "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll",
+           "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
 
 _lib = None
 
@@ -99,6 +119,25 @@ def load(build_if_missing=True):
     vp = ctypes.c_void_p
     L.mpxg_create.argtypes = [ctypes.POINTER(ProblemDesc), ctypes.POINTER(SolverOpts), ctypes.POINTER(vp)]
     L.mpxg_create.restype = ctypes.c_int
+    ci, cll, cf = ctypes.c_int, ctypes.c_longlong, ctypes.c_float
+    L.mpxg_server_create.argtypes = [ctypes.POINTER(ServerDesc), ctypes.POINTER(vp)]
+    L.mpxg_server_destroy.argtypes = [vp]
+    L.mpxg_server_destroy.restype = None
+    L.mpxg_server_capacity.argtypes = [vp, ci]
+    L.mpxg_server_admit.argtypes = [vp, ci, vp, ci, cf, cf, ctypes.POINTER(ci)]
+    L.mpxg_server_reset.argtypes = [vp, ci, vp]
+    L.mpxg_server_release.argtypes = [vp, ci]
+    L.mpxg_submit.argtypes = [vp, ci, ctypes.POINTER(cll)]
+    L.mpxg_server_step.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
+    L.mpxg_poll.argtypes = [vp, cll, ctypes.POINTER(Result)]
+    L.mpxg_server_completed.argtypes = [vp, ctypes.POINTER(Result), ci, ctypes.POINTER(ci)]
+    L.mpxg_server_stats.argtypes = [vp, ctypes.POINTER(ci), ctypes.POINTER(ci), ctypes.POINTER(cll)]
+    L.mpxg_server_last_error.argtypes = [vp]
+    L.mpxg_server_last_error.restype = ctypes.c_char_p
+    for fn in ("mpxg_server_create", "mpxg_server_capacity", "mpxg_server_admit", "mpxg_server_reset",
+               "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll", "mpxg_server_completed",
+               "mpxg_server_stats"):
+        getattr(L, fn).restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_evaluate.argtypes = [vp, vp, ctypes.c_int] + [vp] * 9

@@ -4,6 +4,7 @@
 
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -23,7 +24,8 @@ struct mpxg_handle {
   mpxg_solver_opts opts;
   int device = 0;
   int num_sms = 0;
-  int warps_per_block = 0, blocks_per_sm = 0, total_warps = 0;
+  int warps_per_block = 0, blocks_per_sm = 0, total_warps = 0;  // throughput variant (large batches)
+  int blocks_per_sm_lat = 0;                                     // latency variant
   long long scratch_stride = 0;
   int n_slots = 0;                     // scratch slots: most warps resident at once
   float* scratch = nullptr;
@@ -66,15 +68,18 @@ static bool model_dims(int model, int* nx, int* nu) {
 }
 
 template <class M>
-static int resident_blocks(int wpb);
+static int resident_blocks(int wpb, bool tput);
 
 // Scratch slots of a handle: the most warps of its kernel resident at once.
 static int scratch_slots(int model, int wpb, int num_sms) {
   int rb = 1;
   switch (model) {
-    case MPXG_MODEL_SRBD_QUAT13: rb = resident_blocks<ModelQuat13>(wpb); break;
-    case MPXG_MODEL_SRBD_RPY12: rb = resident_blocks<ModelRpy12>(wpb); break;
-    case MPXG_MODEL_BIPED_WRENCH12: rb = resident_blocks<ModelBiped12>(wpb); break;
+    case MPXG_MODEL_SRBD_QUAT13:
+      rb = std::max(resident_blocks<ModelQuat13>(wpb, true), resident_blocks<ModelQuat13>(wpb, false)); break;
+    case MPXG_MODEL_SRBD_RPY12:
+      rb = std::max(resident_blocks<ModelRpy12>(wpb, true), resident_blocks<ModelRpy12>(wpb, false)); break;
+    case MPXG_MODEL_BIPED_WRENCH12:
+      rb = std::max(resident_blocks<ModelBiped12>(wpb, true), resident_blocks<ModelBiped12>(wpb, false)); break;
     default: break;
   }
   return num_sms * rb * wpb;
@@ -89,29 +94,42 @@ static long long scratch_stride_for(int model, int n_max) {
   }
 }
 
+// The kernel of a variant; models whose two register budgets coincide use one
+// kernel for both (one instantiation less to compile).
 template <class M>
-static int resident_blocks(int wpb) {
+static void (*sqp_kernel_for(bool tput))(ModelConst, SqpParams, BatchPtrs) {
+  if constexpr (SqpMinBlocks<M>::value != MPXG_SQP_MIN_BLOCKS) {
+    if (tput) return sqp_kernel_tput<M>;
+  }
+  return sqp_kernel<M>;
+}
+
+template <class M>
+static int resident_blocks(int wpb, bool tput) {
   int nb = 0;
   const size_t smem = sizeof(WarpSmem<M>) * (size_t)wpb;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(sqp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sqp_kernel<M>, wpb * 32, smem) != cudaSuccess) return 1;
+  auto fn = sqp_kernel_for<M>(tput);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, wpb * 32, smem) != cudaSuccess) return 1;
   return nb > 0 ? nb : 1;
 }
 
 // Persistent grid: warps_per_block warps per block and as many blocks per SM
-// as stay resident (one instance per warp at a time).
-static void launch_geometry(const mpxg_problem_desc* d, const mpxg_solver_opts* o, int num_sms, int* wpb, int* bps) {
+// as stay resident (one instance per warp at a time), for the throughput
+// variant (*bps) and the latency variant (*bps_lat).
+static void launch_geometry(const mpxg_problem_desc* d, const mpxg_solver_opts* o, int num_sms, int* wpb, int* bps,
+                            int* bps_lat = nullptr) {
   *wpb = (o && o->warps_per_block > 0) ? o->warps_per_block : 4;
-  if (o && o->blocks_per_sm > 0) {
-    *bps = o->blocks_per_sm;
-  } else {
-    switch (d->model) {
-      case MPXG_MODEL_SRBD_QUAT13: *bps = resident_blocks<ModelQuat13>(*wpb); break;
-      case MPXG_MODEL_SRBD_RPY12: *bps = resident_blocks<ModelRpy12>(*wpb); break;
-      case MPXG_MODEL_BIPED_WRENCH12: *bps = resident_blocks<ModelBiped12>(*wpb); break;
-      default: *bps = 1;
-    }
+  int t = 1, l = 1;
+  switch (d->model) {
+    case MPXG_MODEL_SRBD_QUAT13: t = resident_blocks<ModelQuat13>(*wpb, true); l = resident_blocks<ModelQuat13>(*wpb, false); break;
+    case MPXG_MODEL_SRBD_RPY12: t = resident_blocks<ModelRpy12>(*wpb, true); l = resident_blocks<ModelRpy12>(*wpb, false); break;
+    case MPXG_MODEL_BIPED_WRENCH12: t = resident_blocks<ModelBiped12>(*wpb, true); l = resident_blocks<ModelBiped12>(*wpb, false); break;
+    default: break;
   }
+  if (o && o->blocks_per_sm > 0) t = l = o->blocks_per_sm;
+  *bps = t;
+  if (bps_lat) *bps_lat = l;
   (void)num_sms;
 }
 
@@ -166,7 +184,7 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaGetDevice"); }
   e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaDeviceGetAttribute"); }
-  launch_geometry(d, o, h->num_sms, &h->warps_per_block, &h->blocks_per_sm);
+  launch_geometry(d, o, h->num_sms, &h->warps_per_block, &h->blocks_per_sm, &h->blocks_per_sm_lat);
   h->total_warps = h->num_sms * h->blocks_per_sm * h->warps_per_block;
   h->scratch_stride = scratch_stride_for(d->model, d->n_max);
   h->n_slots = scratch_slots(d->model, h->warps_per_block, h->num_sms);
@@ -228,23 +246,25 @@ void mpxg_destroy(mpxg_handle* h) {
 }  // extern "C"
 
 template <class M>
-static mpxg_status launch_sqp(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb) {
+static mpxg_status launch_sqp(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb, bool tput) {
   const size_t smem = smem_per_warp<M>() * (size_t)wpb;
+  auto fn = sqp_kernel_for<M>(tput);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(sqp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
   }
-  sqp_kernel<M><<<blocks, wpb * 32, smem, st>>>(h->mc, h->sp, bp);
+  fn<<<blocks, wpb * 32, smem, st>>>(h->mc, h->sp, bp);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(h, e, "sqp_kernel launch");
   return MPXG_OK;
 }
 
-static mpxg_status dispatch(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb) {
+static mpxg_status dispatch(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb,
+                            bool tput = false) {
   switch (h->desc.model) {
-    case MPXG_MODEL_SRBD_QUAT13: return launch_sqp<ModelQuat13>(h, st, bp, blocks, wpb);
-    case MPXG_MODEL_SRBD_RPY12: return launch_sqp<ModelRpy12>(h, st, bp, blocks, wpb);
-    case MPXG_MODEL_BIPED_WRENCH12: return launch_sqp<ModelBiped12>(h, st, bp, blocks, wpb);
+    case MPXG_MODEL_SRBD_QUAT13: return launch_sqp<ModelQuat13>(h, st, bp, blocks, wpb, tput);
+    case MPXG_MODEL_SRBD_RPY12: return launch_sqp<ModelRpy12>(h, st, bp, blocks, wpb, tput);
+    case MPXG_MODEL_BIPED_WRENCH12: return launch_sqp<ModelBiped12>(h, st, bp, blocks, wpb, tput);
     default: return fail(h, MPXG_ERR_UNSUPPORTED, "model");
   }
 }
@@ -310,10 +330,12 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
     bp.order = order;
   }
   const int wpb = h->warps_per_block;
-  int blocks = h->num_sms * h->blocks_per_sm;
+  // more instances than the latency variant's resident warps: throughput variant
+  const bool tput = io->batch > h->num_sms * h->blocks_per_sm_lat * wpb;
+  int blocks = h->num_sms * (tput ? h->blocks_per_sm : h->blocks_per_sm_lat);
   const int need = (io->batch + wpb - 1) / wpb;
   if (need < blocks) blocks = need;
-  mpxg_status s2 = dispatch(h, st, bp, blocks, wpb);
+  mpxg_status s2 = dispatch(h, st, bp, blocks, wpb, tput);
   if (s2 != MPXG_OK || !eager) return s2;
   e = cudaEventRecord(h->ring_ev[r], st);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
@@ -665,3 +687,8 @@ extern "C" void mpxg_xla_solve(void* stream, void** buffers, const char* opaque,
   std::lock_guard<std::mutex> lock(g_xla_mu);  // a handle is used by one host thread at a time
   if (mpxg_solve(h, stream, &io) != MPXG_OK) xla_fail(status, std::string("mpxg_xla_solve: ") + h->err);
 }
+
+// ============================================================================
+// Served MPC stream (mpxg_server_*): host runtime over the entry points above.
+// ============================================================================
+#include "server.cuh"

@@ -897,10 +897,12 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   (void)LD;
 }
 
-// Minimum resident 4-warp blocks per SM the register allocation must allow:
-// 4 (128 registers, 16 warps per SM) measured 4-7 % faster than 3 (168
-// registers, 12 warps) for the roll-pitch-yaw quadruped despite more spills;
-// the other models keep 3 until measured.
+// Two register budgets of the same kernel.  The latency variant (168
+// registers, 3 blocks = 12 warps per SM) runs a warp fastest and serves
+// batches that fit the grid in one wave and the plain path; the throughput
+// variant (per model, 4 blocks = 16 warps per SM for the roll-pitch-yaw
+// quadruped: 128 registers) hides more latency across warps and serves
+// larger batches: 4-7 % faster there, ~20 % slower per lone warp (spills).
 #ifndef MPXG_SQP_MIN_BLOCKS
 #define MPXG_SQP_MIN_BLOCKS 3
 #endif
@@ -910,7 +912,7 @@ template <>
 struct SqpMinBlocks<ModelRpy12> { static constexpr int value = 4; };
 
 template <class M>
-__global__ void __launch_bounds__(128, SqpMinBlocks<M>::value) sqp_kernel(ModelConst mc, SqpParams sp, BatchPtrs bp) {
+__device__ __forceinline__ void sqp_body(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp) {
   extern __shared__ float4 smem_raw[];
   WarpSmem<M>* sms = reinterpret_cast<WarpSmem<M>*>(smem_raw);
   const int wib = threadIdx.x >> 5;
@@ -948,6 +950,16 @@ __global__ void __launch_bounds__(128, SqpMinBlocks<M>::value) sqp_kernel(ModelC
     __syncwarp();
     if (lane == 0) atomicAnd(&bp.slot_bits[slot >> 5], ~(1u << (slot & 31)));
   }
+}
+
+template <class M>
+__global__ void __launch_bounds__(128, MPXG_SQP_MIN_BLOCKS) sqp_kernel(ModelConst mc, SqpParams sp, BatchPtrs bp) {
+  sqp_body<M>(mc, sp, bp);
+}
+template <class M>
+__global__ void __launch_bounds__(128, SqpMinBlocks<M>::value) sqp_kernel_tput(ModelConst mc, SqpParams sp,
+                                                                              BatchPtrs bp) {
+  sqp_body<M>(mc, sp, bp);
 }
 
 }  // namespace mpxg

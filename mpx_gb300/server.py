@@ -1,22 +1,19 @@
 """Serving: continuous batching of MPC control ticks on one GPU.
 
-Each request is one control tick of a persistent episode (a robot).  The
-server keeps every admitted episode's warm start -- X, U, V, gait timers,
-horizon, weights -- resident on the device in a fixed pool of slots, so a tick
-moves only slot indices in and one result row (first control, KKT residual,
-status) out.  Requests that arrive while earlier batches are still running go
-into the next batch, launched on another CUDA stream so that it overlaps the
-running ones on the device (continuous batching); a batch is one persistent
-solve launch over the scattered pool rows of its requests
-(mpxg_batch_io.slot), preceded by the warm-start shift and the gait tables of
-those rows.  Cold starts and the per-tick state drift are made on the device
-by the gait-table kernel, so the host issues four launches and two copies per
-batch and nothing per request.
+Python face of the native serving runtime (`mpxg_server_*` in
+include/mpxg.h, implemented in mpx_gb300/csrc/server.cuh).  Each request is
+one control tick of a persistent episode (a robot).  The runtime keeps every
+admitted episode's warm start -- X, U, V, gait timers, horizon, weights --
+resident on the device in per-model slot pools, so a tick moves only slot
+ids in and one result row (first control, KKT residual, status) out.
+Requests submitted while earlier batches run form the next batch, launched
+on the next free CUDA stream so that batches overlap on the device
+(continuous batching); a batch is the warm-start shift and gait tables of its
+episodes followed by one persistent solve over their scattered slots.
 
-Admission is by a device-memory budget: pool slots plus the solver scratch
-must fit; an episode that does not fit is refused with BudgetError (the C ABI
-status MPXG_ERR_BUDGET).  A slot whose solve returns non-finite values is
-cold-started at its next tick (the NaN fallback of
+Admission is by a device-memory budget: an episode that does not fit is
+refused with BudgetError (MPXG_ERR_BUDGET).  A slot whose solve returns
+non-finite values is cold-started at its next tick (the NaN fallback of
 mpx/utils/mpc_wrapper.py:79-98,261-282).
 """
 import collections
@@ -28,47 +25,19 @@ import torch
 
 from . import _lib
 from . import problem as P
-from .solver import Solver, _ptr, _stream_handle, gait_tables, problem_desc, solver_opts
+from .solver import problem_desc, solver_opts
+
+MPXG_ERR_INVALID_ARG = 1
+MPXG_ERR_BUDGET = 3
 
 
 class BudgetError(RuntimeError):
     """No slot left inside the device-memory budget (MPXG_ERR_BUDGET)."""
 
 
-Request = collections.namedtuple("Request", "rid episode arrival")
-
-
-def slot_bytes(desc, n_max):
-    """Device bytes of one episode slot."""
-    n, m = desc.n, desc.m
-    f = (n_max + 1) * n * 2 + n_max * m + (n_max + 1) * (desc.ref_cols + desc.par_cols)
-    f += n + 24 + 3 + desc.n_contact + 1     # x0, w, kkt, leg timers, v_ref
-    return 4 * f + 4 * 2                    # + horizon and status
-
-
-class _Pool:
-    """Slots of one model: device arrays with a leading slot dimension."""
-
-    def __init__(self, name, desc, gait, capacity, n_max, opts, dev):
-        self.name, self.desc, self.gait, self.cap, self.n_max, self.dev = name, desc, gait, capacity, n_max, dev
-        n, m, rc, pc = desc.n, desc.m, desc.ref_cols, desc.par_cols
-        z = lambda *s, dt=torch.float32: torch.zeros(*s, device=dev, dtype=dt)
-        self.x0 = z(capacity, n)
-        self.X, self.U, self.V = z(capacity, n_max + 1, n), z(capacity, n_max, m), z(capacity, n_max + 1, n)
-        self.ref, self.par = z(capacity, n_max + 1, rc), z(capacity, n_max + 1, pc)
-        self.w, self.kkt = z(capacity, 24), z(capacity, 3)
-        self.status = z(capacity, dt=torch.int32)
-        self.horizon = torch.ones(capacity, device=dev, dtype=torch.int32)
-        self.v_ref = z(capacity)
-        self.leg_time = z(capacity, desc.n_contact)
-        # one handle serves the batches of every stream: its warps claim
-        # scratch slots per launch and each solve takes its own work counter
-        self.solver = Solver(desc, opts, n_max=n_max, batch_max=capacity, device=dev)
-        self.out = dict(X=self.X, U=self.U, V=self.V, kkt=self.kkt, status=self.status)
-        self.free = list(range(capacity))[::-1]
-        # reusable (pinned slot ids, device slot ids, pinned results, device results, event)
-        self.staging = []
-        self.W = np.diag(gait["W"]).astype(np.float32)
+class _PoolInfo:
+    def __init__(self, index, desc, gait, cap):
+        self.index, self.desc, self.gait, self.cap = index, desc, gait, cap
 
 
 class MPCServer:
@@ -79,200 +48,154 @@ class MPCServer:
     split evenly between the models; each model's pool holds as many slots as
     fit after its solver scratch."""
 
-    def __init__(self, models, n_max=200, budget_bytes=8 << 30, opts=None, streams=4, device=None, drift_std=0.01,
+    def __init__(self, models, n_max=200, budget_bytes=8 << 30, opts=None, streams=16, device=None, drift_std=0.01,
                  seed=0, max_slots=None):
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.opts = opts or P.SolverOptions()
         self.n_max = int(n_max)
         self.L = _lib.load()
-        self.drift_std = float(drift_std)
-        self.seed = int(seed)
-        self.pools = {}
-        share = budget_bytes // max(len(models), 1)
-        for name, (desc, gait) in models.items():
-            scratch = int(self.L.mpxg_workspace_bytes(ctypes.byref(problem_desc(desc, self.n_max, 1)),
-                                                      ctypes.byref(solver_opts(self.opts))))
-            cap = (share - scratch) // slot_bytes(desc, self.n_max)
-            if max_slots is not None:
-                cap = min(cap, int(max_slots))
-            if cap < 1:
-                raise BudgetError("budget %d B leaves no slot for model %s" % (budget_bytes, name))
-            self.pools[name] = _Pool(name, desc, gait, int(cap), self.n_max, self.opts, self.dev)
-        self.episodes = {}          # episode -> [pool name, slot, ticks done, cold start pending, horizon]
-        self.pending = collections.defaultdict(list)
-        self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(streams)]
-        self.next_stream = 0
-        self.inflight = collections.deque()
+        names = list(models)
+        arr = (_lib.ServedModel * len(names))()
+        for i, name in enumerate(names):
+            desc, g = models[name]
+            sm = arr[i]
+            sm.desc = problem_desc(desc, self.n_max, 1)
+            sm.duty_factor, sm.step_freq, sm.height = float(g["duty"]), float(g["step_freq"]), float(g["height"])
+            off = np.zeros(12, dtype=np.float32)
+            o = np.asarray(g["offsets"], dtype=np.float32).reshape(-1)
+            off[:o.size] = o
+            ph = np.zeros(4, dtype=np.float32)
+            p0 = np.asarray(g["phase0"], dtype=np.float32).reshape(-1)
+            ph[:p0.size] = p0
+            w = np.diag(np.asarray(g["W"], dtype=np.float64)).astype(np.float32)
+            for k in range(12):
+                sm.offsets[k] = float(off[k])
+            for k in range(4):
+                sm.phase0[k] = float(ph[k])
+            for k in range(24):
+                sm.w[k] = float(w[k])
+        d = _lib.ServerDesc()
+        d.n_models, d.models, d.n_max = len(names), arr, self.n_max
+        d.budget_bytes, d.max_slots, d.streams = int(budget_bytes), int(max_slots or 0), int(streams)
+        d.drift_std, d.seed, d.opts = float(drift_std), int(seed) & 0xFFFFFFFF, solver_opts(self.opts)
+        self._models = arr
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.dev):
+            st = self.L.mpxg_server_create(ctypes.byref(d), ctypes.byref(h))
+        if st == MPXG_ERR_BUDGET:
+            raise BudgetError(self.L.mpxg_last_error(None).decode())
+        _lib.check(st, None, "mpxg_server_create")
+        self.handle = h
+        self.pools = {name: _PoolInfo(i, models[name][0], models[name][1],
+                                      int(self.L.mpxg_server_capacity(h, i))) for i, name in enumerate(names)}
+        self.streams = int(streams)
+        self.episodes = {}     # key -> episode id
+        self._m = {}           # key -> controls per result row
+        self._arrival = {}     # ticket -> (key, m, arrival time)
         self.completed = []
-        self._rid = 0
-        self.launches = 0
-        self.busy = collections.Counter()   # episode -> ticks queued or in flight
-        self.running = set()                # episodes with a tick in flight
-        self.retiring = set()
+        self._res = (_lib.Result * 4096)()
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.L.mpxg_server_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != 0:
+            raise _lib.MpxgError("%s: %s" % (what, self.L.mpxg_server_last_error(self.handle).decode()))
 
     # ------------------------------------------------------------ admission
     def capacity(self, name):
         return self.pools[name].cap
 
     def admit(self, episode, name, x0, horizon, v_ref=0.0, phase=0.0):
-        """Give `episode` a resident slot or raise BudgetError.  Its first tick
-        cold-starts the warm start from x0 on the device."""
+        """Give `episode` (any hashable key) a resident slot or raise
+        BudgetError.  Its first tick cold-starts the warm start from x0."""
         pool = self.pools[name]
-        if not pool.free:
+        x = np.ascontiguousarray(np.asarray(x0, dtype=np.float32).reshape(-1))
+        eid = ctypes.c_int()
+        st = self.L.mpxg_server_admit(self.handle, pool.index, x.ctypes.data, int(horizon), float(v_ref),
+                                      float(phase), ctypes.byref(eid))
+        if st == MPXG_ERR_BUDGET:
             raise BudgetError("device-memory budget exhausted for model %s (%d slots)" % (name, pool.cap))
-        if not (1 <= int(horizon) <= self.n_max):
-            raise ValueError("horizon must be in 1..%d" % self.n_max)
-        s = pool.free.pop()
-        self.episodes[episode] = [name, s, 0, True, int(horizon)]
-        n, nc = pool.desc.n, pool.desc.n_contact
-        row = np.zeros(n + 2 + nc + 24, dtype=np.float32)
-        row[:n] = np.asarray(x0, dtype=np.float32)
-        row[n] = float(v_ref)
-        row[n + 1] = float(int(horizon))
-        row[n + 2:n + 2 + nc] = np.mod(np.asarray(pool.gait["phase0"]) + phase, 1.0)
-        row[n + 2 + nc:] = pool.W
-        r = torch.from_numpy(row).to(self.dev)
-        with torch.no_grad():
-            pool.x0[s] = r[:n]
-            pool.v_ref[s] = r[n]
-            pool.horizon[s] = r[n + 1].to(torch.int32)
-            pool.leg_time[s] = r[n + 2:n + 2 + nc]
-            pool.w[s] = r[n + 2 + nc:]
-        return s
+        if st == MPXG_ERR_INVALID_ARG:
+            raise ValueError(self.L.mpxg_server_last_error(self.handle).decode())
+        self._check(st, "admit")
+        self.episodes[episode] = eid.value
+        self._m[episode] = pool.desc.m
+        return eid.value
 
     def reset_slot(self, episode, x0=None):
         """Cold-start the episode's next tick (optionally from a new x0)."""
-        name, s = self.episodes[episode][:2]
+        ptr = None
         if x0 is not None:
-            with torch.no_grad():
-                self.pools[name].x0[s] = torch.as_tensor(np.asarray(x0, dtype=np.float32), device=self.dev)
-        self.episodes[episode][3] = True
+            x = np.ascontiguousarray(np.asarray(x0, dtype=np.float32).reshape(-1))
+            ptr = x.ctypes.data
+        self._check(self.L.mpxg_server_reset(self.handle, self.episodes[episode], ptr), "reset")
 
     def release(self, episode):
-        """Free the episode's slot (deferred until its queued and in-flight ticks complete)."""
-        if self.busy.get(episode, 0) > 0:
-            self.retiring.add(episode)
-            return
-        name, s = self.episodes.pop(episode)[:2]
-        self.pools[name].free.append(s)
+        """Free the episode's slot once its queued and running ticks are done."""
+        self._check(self.L.mpxg_server_release(self.handle, self.episodes.pop(episode)), "release")
 
     # ------------------------------------------------------------ requests
     def submit(self, episode, arrival=None):
-        """Queue the next control tick of an admitted episode."""
-        self._rid += 1
-        r = Request(self._rid, episode, time.perf_counter() if arrival is None else arrival)
-        self.pending[self.episodes[episode][0]].append(r)
-        self.busy[episode] += 1
-        return r.rid
+        """Queue the next control tick of an admitted episode; returns its ticket."""
+        t = ctypes.c_longlong()
+        self._check(self.L.mpxg_submit(self.handle, self.episodes[episode], ctypes.byref(t)), "submit")
+        self._arrival[t.value] = (episode, self._m[episode], time.perf_counter() if arrival is None else arrival)
+        return t.value
 
     def launch_pending(self):
-        """Launch one batch per model with every launchable pending request
-        (continuous batching: call whenever requests have arrived)."""
-        n = 0
-        for name, reqs in list(self.pending.items()):
-            if not reqs:
-                continue
-            self.pending[name] = []
-            n += self._launch(self.pools[name], reqs)
-        return n
+        """Launch queued ticks on free streams (and collect finished batches)."""
+        n = ctypes.c_int()
+        self._check(self.L.mpxg_server_step(self.handle, 0, ctypes.byref(n), None), "step")
+        return n.value
 
-    def _staging(self, pool):
-        if pool.staging:
-            return pool.staging.pop()
-        cap = pool.cap
-        return (torch.empty(3 * cap, dtype=torch.int32, pin_memory=True),
-                torch.empty(3 * cap, dtype=torch.int32, device=self.dev),
-                torch.empty(cap, pool.desc.m + 4, pin_memory=True),
-                torch.empty(cap, pool.desc.m + 4, device=self.dev),
-                torch.cuda.Event())
+    def stats(self):
+        """(ticks queued, ticks running, kernel launches so far)."""
+        q, r, launches = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        self._check(self.L.mpxg_server_stats(self.handle, ctypes.byref(q), ctypes.byref(r), ctypes.byref(launches)),
+                    "stats")
+        return q.value, r.value, launches.value
 
-    def _launch(self, pool, reqs):
-        # one tick per episode at a time: a tick whose episode is still in
-        # flight (or repeated in this batch) waits for a later batch
-        seen, batch, later = set(), [], []
-        for r in reqs:
-            (later if (r.episode in seen or r.episode in self.running) else batch).append(r)
-            seen.add(r.episode)
-        if later:
-            self.pending[pool.name].extend(later)
-        if not batch:
-            return 0
-        # longest horizons first: the persistent grid hands out instances in
-        # batch order, so this shortens the batch's tail
-        batch.sort(key=lambda r: -self.episodes[r.episode][4])
-        self.running.update(r.episode for r in batch)
-        k = self.next_stream
-        st, solver = self.streams[k], pool.solver
-        self.next_stream = (k + 1) % len(self.streams)
-        st.wait_stream(torch.cuda.current_stream(self.dev))  # admissions are issued on the current stream
-        nb = len(batch)
-        slots = np.array([self.episodes[r.episode][1] for r in batch], dtype=np.int32)
-        first = np.array([self.episodes[r.episode][3] for r in batch], dtype=bool)
-        for r in batch:
-            self.episodes[r.episode][3] = False
-            self.episodes[r.episode][2] += 1
-        warm_s, cold_s = slots[~first], slots[first]
-        nw, nc = len(warm_s), len(cold_s)
-        stg = self._staging(pool)
-        slot_h, slot_all, res_h, res_d, ev = stg
-        packed = slot_h.numpy()
-        packed[:nb] = slots
-        packed[nb:nb + nw] = warm_s
-        packed[nb + nw:nb + nw + nc] = cold_s
-        self.seed += 1
-        with torch.cuda.stream(st):
-            slot_all[:nb + nw + nc].copy_(slot_h[:nb + nw + nc], non_blocking=True)
-            slot_d = slot_all[:nb]
-            warm = slot_all[nb:nb + nw]
-            cold = slot_all[nb + nw:nb + nw + nc]
-            hs = _stream_handle(st)
-            if nw:
-                _lib.check(self.L.mpxg_shift_warm_start(solver.handle, hs, nw, _ptr(warm), _ptr(pool.horizon), 1,
-                                                        _ptr(pool.X), _ptr(pool.U), _ptr(pool.V), _ptr(pool.X),
-                                                        _ptr(pool.U), _ptr(pool.V)), solver.handle, "shift")
-                gait_tables(st, pool.desc, nw, self.n_max, pool.x0, pool.X, pool.U, pool.V, pool.v_ref,
-                            pool.leg_time, pool.ref, pool.par, pool.gait, 1, slot=warm, horizon=pool.horizon,
-                            drift_std=self.drift_std, seed=self.seed)
-            if nc:
-                gait_tables(st, pool.desc, nc, self.n_max, pool.x0, pool.X, pool.U, pool.V, pool.v_ref,
-                            pool.leg_time, pool.ref, pool.par, pool.gait, 0, slot=cold, horizon=pool.horizon)
-            out = dict(pool.out, first=res_d)
-            io = solver.io(pool.x0, pool.X, pool.U, pool.V, pool.ref, pool.par, pool.w, pool.horizon, out, slot=slot_d)
-            _lib.check(self.L.mpxg_solve(solver.handle, hs, ctypes.byref(io)), solver.handle, "mpxg_solve")
-            res_h[:nb].copy_(res_d[:nb], non_blocking=True)
-            ev.record(st)
-        self.launches += (2 if nw else 0) + (1 if nc else 0) + solver.launches_per_solve(nb)
-        self.inflight.append((ev, pool, batch, stg))
-        return nb
+    @property
+    def launches(self):
+        return self.stats()[2]
 
     def poll(self, block=False):
-        """Collect finished batches; returns [(rid, episode, latency_s, first control, kkt, status)]."""
+        """Make progress (collect finished batches, launch queued ticks) and
+        return the finished ticks as
+        [(ticket, episode, latency_s, first control, kkt, status)]."""
+        self._check(self.L.mpxg_server_step(self.handle, 1 if block else 0, None, None), "step")
+        now = time.perf_counter()
         done = []
-        while self.inflight:
-            ev, pool, batch, stg = self.inflight[0]
-            if not block and not ev.query():
+        while True:
+            cnt = ctypes.c_int()
+            self._check(self.L.mpxg_server_completed(self.handle, self._res, len(self._res), ctypes.byref(cnt)),
+                        "completed")
+            for i in range(cnt.value):
+                r = self._res[i]
+                key, m, arrival = self._arrival.pop(r.ticket)
+                done.append((r.ticket, key, now - arrival, np.array(r.u0[:m], dtype=np.float32),
+                             np.array(r.kkt[:], dtype=np.float32), int(r.status)))
+            if cnt.value < len(self._res):
                 break
-            ev.synchronize()
-            now = time.perf_counter()
-            self.inflight.popleft()
-            res = stg[2][:len(batch)].numpy().copy()
-            pool.staging.append(stg)
-            m = pool.desc.m
-            for i, r in enumerate(batch):
-                status = int(res[i, m + 3])
-                if status & _lib.INST_NAN and r.episode in self.episodes:
-                    self.episodes[r.episode][3] = True  # cold start next tick (NaN fallback)
-                done.append((r.rid, r.episode, now - r.arrival, res[i, :m].copy(), res[i, m:m + 3].copy(), status))
-                self.busy[r.episode] -= 1
-                self.running.discard(r.episode)
-                if r.episode in self.retiring and self.busy[r.episode] == 0:
-                    self.retiring.discard(r.episode)
-                    self.release(r.episode)
         self.completed.extend(done)
         return done
 
     def drain(self):
-        while self.inflight:
+        """Wait for every queued and running tick."""
+        while True:
+            q, r, _ = self.stats()
+            if q == 0 and r == 0:
+                self.poll()
+                return
             self.poll(block=True)
 
 
@@ -317,11 +240,12 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
                 server.release(ep[0])  # deferred until its last tick completes
                 new_episode()
             i += 1
-        if any(server.pending.values()) and len(server.inflight) < len(server.streams):
-            server.launch_pending()
         lat.extend(d[2] for d in server.poll())
-        if i >= len(arrivals) and not any(server.pending.values()) and not server.inflight:
-            break
+        if i >= len(arrivals):
+            q, r, _ = server.stats()
+            if q == 0 and r == 0:
+                lat.extend(d[2] for d in server.poll())
+                break
     wall = time.perf_counter() - t0
     for ep, _ in eps:
         server.release(ep)

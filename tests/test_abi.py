@@ -44,8 +44,9 @@ def test_struct_layouts_match_header():
 #include <stdio.h>
 #include "mpxg.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu\n", sizeof(mpxg_problem_desc), sizeof(mpxg_solver_opts), sizeof(mpxg_batch_io),
-         sizeof(mpxg_lq_io), sizeof(mpxg_xla_opaque));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(mpxg_problem_desc), sizeof(mpxg_solver_opts),
+         sizeof(mpxg_batch_io), sizeof(mpxg_lq_io), sizeof(mpxg_xla_opaque), sizeof(mpxg_served_model),
+         sizeof(mpxg_server_desc), sizeof(mpxg_result));
   return 0;
 }
 '''
@@ -56,7 +57,8 @@ int main(void) {
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", exe, c], check=True)
         sizes = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert sizes == [ctypes.sizeof(_lib.ProblemDesc), ctypes.sizeof(_lib.SolverOpts), ctypes.sizeof(_lib.BatchIO),
-                     ctypes.sizeof(_lib.LqIO), ctypes.sizeof(_lib.XlaOpaque)]
+                     ctypes.sizeof(_lib.LqIO), ctypes.sizeof(_lib.XlaOpaque), ctypes.sizeof(_lib.ServedModel),
+                     ctypes.sizeof(_lib.ServerDesc), ctypes.sizeof(_lib.Result)]
 
 
 def test_xla_target_rejects_a_malformed_opaque():

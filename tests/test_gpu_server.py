@@ -66,3 +66,26 @@ def test_served_stream_reports_latency(cuda):
     assert np.all(np.isfinite(lat)) and np.percentile(lat, 99) < 1.0
     stats = [d[5] for d in s.completed]
     assert sum(1 for st in stats if st & 1) == 0
+
+
+def test_c_poll_returns_each_result_once(cuda):
+    """mpxg_poll: NOT_READY before the batch ran, the result row once after,
+    then the ticket is gone (MPXG_ERR_INVALID_ARG)."""
+    import ctypes
+    from mpx_gb300 import _lib
+    s = make_server()
+    s.admit("E", "quadruped", x0_of(s, "quadruped", 3), 30, v_ref=0.2)
+    L = s.L
+    t = ctypes.c_longlong()
+    assert L.mpxg_submit(s.handle, s.episodes["E"], ctypes.byref(t)) == 0
+    r = _lib.Result()
+    assert L.mpxg_poll(s.handle, t.value, ctypes.byref(r)) == 7     # not launched yet
+    for _ in range(1000):
+        assert L.mpxg_server_step(s.handle, 1, None, None) == 0
+        st = L.mpxg_poll(s.handle, t.value, ctypes.byref(r))
+        if st == 0:
+            break
+    assert st == 0 and r.ticket == t.value and r.episode == s.episodes["E"]
+    assert np.all(np.isfinite(np.array(r.u0[:12]))) and r.status & 1 == 0
+    assert L.mpxg_poll(s.handle, t.value, ctypes.byref(r)) == 1
+    s.close()
