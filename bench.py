@@ -59,8 +59,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream section")
     ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
-    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr"],
-                    help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve")
+    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq"],
+                    help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve; lqr_eq: the "
+                         "equality-constrained n=72 LQ solve")
     ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
@@ -605,6 +606,89 @@ def run_lqr(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_lqr_eq(args, rank, world, local_rank):
+    """--workload lqr_eq: 512 equality-constrained LQ problems, n=72, m=30,
+    12 equality rows per stage, N=100 (mpxg_lqr_eq_solve)."""
+    import torch
+    from mpx_gb300 import _lib
+    from mpx_gb300 import problem as P
+    from mpx_gb300.replicas import max_over_ranks
+    from mpx_gb300.solver import _ptr, _stream_handle
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    B, N, n, m, ne = 512, 100, 72, 30, 12
+    parts = [P.random_lq_eq(min(32, B - i), n, m, ne, N, seed=31 + i + 1000 * rank) for i in range(0, B, 32)]
+    d = {k: np.concatenate([p[k] for p in parts], 0).astype(np.float32) for k in parts[0]}
+    names = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+    dv = {k: torch.from_numpy(d[k]).to(dev) for k in names}
+    outs = dict(K=torch.empty(B, N, m, n, device=dev), k=torch.empty(B, N, m, device=dev),
+                Knu=torch.empty(B, N, ne, n, device=dev), knu=torch.empty(B, N, ne, device=dev),
+                X=torch.empty(B, N + 1, n, device=dev), U=torch.empty(B, N, m, device=dev),
+                lam=torch.empty(B, N + 1, n, device=dev), nu=torch.empty(B, N, ne, device=dev))
+    L = _lib.load()
+    ws = torch.empty(int(L.mpxg_lqr_eq_workspace_bytes(B, N, n)) // 4, device=dev)
+    io = _lib.LqEqIO()
+    io.batch, io.N, io.n, io.m, io.n_eq = B, N, n, m, ne
+    for name, key in zip(("A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0"), names):
+        setattr(io, name, _ptr(dv[key]))
+    for key in outs:
+        setattr(io, key, _ptr(outs[key]))
+    io.workspace = _ptr(ws)
+    stream = torch.cuda.Stream(device=dev)
+    hs = _stream_handle(stream)
+
+    def solve():
+        _lib.check(L.mpxg_lqr_eq_solve(hs, ctypes.byref(io)), None, "mpxg_lqr_eq_solve")
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            solve()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            solve()
+        ev[1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[1]), device=dev)
+    avg_s = total_ms / args.steps / 1000.0
+    # work: Riccati count + the constraint elimination (Schur complement) per stage
+    f_eq = f_lqr(n, m) + 2 * (m * m * ne + m * ne * n + ne * ne * n + ne * n * n)
+    flops = B * N * f_eq
+    in_bytes = sum(dv[k].numel() * 4 for k in names)
+    out_bytes = sum(v.numel() * 4 for v in outs.values())
+    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = (in_bytes + out_bytes) / avg_s / 1e9
+    line = {
+        "metric": "constrained LQR solves/s (n=72, m=30, 12 equality rows, N=100, batch 512)",
+        "value": world * B / avg_s, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded)",
+        "config": {"workload": "512 equality-constrained LQ problems: A = I + 0.1 J (J ~ N(0,1/n), spectral radius "
+                               "<= 1.01), B ~ N(0,0.1/m), Q diagonal log-uniform [1e-2,1e2], R = 1e-3 I, 12 rows "
+                               "[C D] ~ N(0,1) per stage", "parallelism": "replicas"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                     "traffic": None, "algorithmic_bytes": in_bytes + out_bytes, "kernel": "lqr_eq_kernel<72,30,12>"},
+        "fp32": {"achieved_tflops": flops / avg_s / 1e12, "nominal_peak_tflops": fp32_nominal,
+                 "frac": flops / avg_s / 1e12 / fp32_nominal,
+                 "flops": "F_LQR(72,30) + Schur-complement elimination per stage = %d" % f_eq},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -618,6 +702,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.workload == "lqr":
         run_lqr(args, rank, world, local_rank)
+    elif args.workload == "lqr_eq":
+        run_lqr_eq(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1:

@@ -259,6 +259,27 @@ typedef struct {
 size_t mpxg_lqr_workspace_bytes(int batch, int N, int n, int m, int method);
 mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method);
 
+/* Equality-constrained time-varying LQR for a batch (the LQ/KKT step of
+ * large linearised problems; stands in for the absent primal_dual_ilqr
+ * solver's KKT solve, as mpxg_lqr_solve does):
+ *   x_{t+1} = A x + B u + c,  C x + D u = e (n_eq rows),  cost as mpxg_lq_io.
+ * A [B,N,n,n], Bm [B,N,n,m], c [B,N,n], Q [B,N+1,n,n], R [B,N,m,m],
+ * M [B,N,n,m], q [B,N+1,n], r [B,N,m], C [B,N,n_eq,n], D [B,N,n_eq,m],
+ * e [B,N,n_eq], x0 [B,n].  Outputs K [B,N,m,n], k [B,N,m], Knu [B,N,n_eq,n],
+ * knu [B,N,n_eq] (u = K x + k, nu = Knu x + knu), X [B,N+1,n], U [B,N,m],
+ * lam [B,N+1,n] (costates), nu [B,N,n_eq] (multipliers of C x + D u = e,
+ * stationarity l_u + B'lam_{t+1} + D'nu = 0).  D must have full row rank and
+ * R + B'P B be positive definite.  Built sizes (n, m, n_eq): (72,30,12)
+ * (16,8,4) (8,5,2). */
+typedef struct {
+  int batch, N, n, m, n_eq;
+  const float *A, *Bm, *c, *Q, *R, *M, *q, *r, *C, *D, *e, *x0;
+  float *K, *k, *Knu, *knu, *X, *U, *lam, *nu;
+  float* workspace;  /* device, >= mpxg_lqr_eq_workspace_bytes(batch, N, n) bytes */
+} mpxg_lq_eq_io;
+size_t mpxg_lqr_eq_workspace_bytes(int batch, int N, int n);
+mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io);
+
 /* Allocation-free batched solve.  No counterpart in the reference.  For
  * callers that cannot allocate device memory when they solve (a real-time
  * loop that forbids cudaMalloc after start-up, or a plugin host that hands

@@ -60,6 +60,13 @@ class Result(ctypes.Structure):
                 ("u0", ctypes.c_float * 12), ("kkt", ctypes.c_float * 3)]
 
 
+class LqEqIO(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("N", ctypes.c_int), ("n", ctypes.c_int), ("m", ctypes.c_int),
+                ("n_eq", ctypes.c_int)] + [(k, ctypes.c_void_p) for k in (
+                    "A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0",
+                    "K", "k", "Knu", "knu", "X", "U", "lam", "nu", "workspace")]
+
+
 class BatchIO(ctypes.Structure):
     _fields_ = [("batch", ctypes.c_int), ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
                 ("x0", ctypes.c_void_p), ("X_in", ctypes.c_void_p), ("U_in", ctypes.c_void_p),
@@ -89,7 +96,7 @@ class LqIO(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
@@ -138,6 +145,10 @@ def load(build_if_missing=True):
                "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll", "mpxg_server_completed",
                "mpxg_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
+    L.mpxg_lqr_eq_workspace_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.mpxg_lqr_eq_workspace_bytes.restype = ctypes.c_size_t
+    L.mpxg_lqr_eq_solve.argtypes = [vp, ctypes.POINTER(LqEqIO)]
+    L.mpxg_lqr_eq_solve.restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_evaluate.argtypes = [vp, vp, ctypes.c_int] + [vp] * 9

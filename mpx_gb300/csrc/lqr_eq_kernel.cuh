@@ -1,0 +1,400 @@
+// Equality-constrained time-varying LQR (mpxg_lqr_eq_solve): the LQ/KKT
+// step for large linearised problems (n = 72, m = 30, 12 equality rows per
+// stage), in absolute coordinates:
+//   x_{t+1} = A x + B u + c,   C x + D u = e,
+//   l_t = 1/2 x'Q x + x'M u + 1/2 u'R u + q'x + r'u,  l_N = 1/2 x'Q_N x + q_N'x.
+// Stagewise Riccati with the control QP of each stage solved by a Schur
+// complement:
+//   Q_xx = Q + A'P A, Q_ux = M' + B'P A, Q_uu = R + B'P B,
+//   q_x = q + A'(P c + p), q_u = r + B'(P c + p),
+//   Z = Q_uu^-1 Q_ux, g = Q_uu^-1 q_u, W = Q_uu^-1 D', S = D W,
+//   K_nu = S^-1 (C - D Z), k_nu = -S^-1 (D g + e), K = -(Z + W K_nu), k = -(g + W k_nu),
+//   P <- Q_xx + Q_ux'K + C'K_nu,  p <- q_x + Q_ux'k + C'k_nu   (D K = -C).
+// GB300 mapping: one 256-thread block per problem; all stage matrices live in
+// shared memory column-major with odd leading dimensions (~147 KB for
+// n = 72); products are 16 x 16-thread register-tiled block products, the
+// m x m and p x p factorisations are warp Cholesky, the solves one thread per
+// right-hand side.  CUDA-core FP32: the FP32 accuracy the tests ask for would
+// need split-TF32 tensor-core products (three MMAs per product).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/mpxg.h"
+
+namespace mpxg {
+namespace lqeq {
+
+constexpr int kThreads = 256;
+
+// out(r,c) = alpha * sum_l X(r,l) Y(l,c) [+ Add(r,c)]  (column-major; see the
+// transposition flags in the scan kernel's mm).  16 x 16 threads, each a
+// ceil(ROWS/16) x ceil(COLS/16) tile of strided rows and columns.  `out` may
+// alias Add (same element per thread), never X or Y.  Ends with a barrier.
+template <int ROWS, int INNER, int COLS, bool TX, bool TY, bool TA>
+__device__ __forceinline__ void bmm(float* out, int ldo, const float* X, int ldx, const float* Y, int ldy, float alpha,
+                                    const float* Add, int lda) {
+  constexpr int TR = (ROWS + 15) / 16, TC = (COLS + 15) / 16;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[TR][TC];
+#pragma unroll
+  for (int i = 0; i < TR; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j) acc[i][j] = 0.0f;
+#pragma unroll 2
+  for (int l = 0; l < INNER; ++l) {
+    float xa[TR], yb[TC];
+#pragma unroll
+    for (int i = 0; i < TR; ++i) {
+      const int r = ty + 16 * i;
+      xa[i] = (r < ROWS) ? (TX ? X[r * ldx + l] : X[l * ldx + r]) : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+      const int c = tx + 16 * j;
+      yb[j] = (c < COLS) ? (TY ? Y[l * ldy + c] : Y[c * ldy + l]) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < TR; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j) acc[i][j] += xa[i] * yb[j];
+  }
+  __syncthreads();  // every read of X / Y is done before out is written
+#pragma unroll
+  for (int i = 0; i < TR; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+      const int r = ty + 16 * i, c = tx + 16 * j;
+      if (r < ROWS && c < COLS) {
+        float v = alpha * acc[i][j];
+        if (Add) v += TA ? Add[r * lda + c] : Add[c * lda + r];
+        out[c * ldo + r] = v;
+      }
+    }
+  __syncthreads();
+}
+
+// out[r] = alpha * sum_l X(r,l) v[l] + add[r]; out may alias add.
+template <int ROWS, int INNER, bool TX>
+__device__ __forceinline__ void bmv(float* out, const float* X, int ldx, const float* v, float alpha, const float* add) {
+  for (int r = threadIdx.x; r < ROWS; r += kThreads) {
+    float a = 0.0f;
+#pragma unroll 4
+    for (int l = 0; l < INNER; ++l) a += (TX ? X[r * ldx + l] : X[l * ldx + r]) * v[l];
+    out[r] = alpha * a + (add ? add[r] : 0.0f);
+  }
+  __syncthreads();
+}
+
+// Inverse of an N x N symmetric positive definite matrix by warp 0 (N <= 32):
+// Gauss-Jordan on [S | I] with columns lane and lane + 32 in registers.  `out`
+// may alias S (every read precedes every write).
+template <int N>
+__device__ __forceinline__ void spd_inverse(const float* S, int lds, float* out, int ldo) {
+  static_assert(N <= 32, "spd_inverse: pivots on one warp");
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x, j0 = lane, j1 = lane + 32;
+    float c0[N], c1[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      c0[r] = j0 < N ? S[j0 * lds + r] : (j0 < 2 * N && j0 - N == r ? 1.0f : 0.0f);
+      c1[r] = j1 < N ? S[j1 * lds + r] : (j1 < 2 * N && j1 - N == r ? 1.0f : 0.0f);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int p = 0; p < N; ++p) {
+      float pc[N];
+#pragma unroll
+      for (int r = 0; r < N; ++r) pc[r] = __shfl_sync(0xffffffffu, c0[r], p);
+      float d = pc[p];
+      if (!(d > 0.0f)) d = fmaxf(fabsf(d), 1e-30f);
+      const float inv = 1.0f / d;
+      const float v0 = c0[p] * inv, v1 = c1[p] * inv;
+#pragma unroll
+      for (int r = 0; r < N; ++r) {
+        c0[r] = (r == p) ? v0 : c0[r] - pc[r] * v0;
+        c1[r] = (r == p) ? v1 : c1[r] - pc[r] * v1;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      if (j0 >= N && j0 < 2 * N) out[(j0 - N) * ldo + r] = c0[r];
+      if (j1 >= N && j1 < 2 * N) out[(j1 - N) * ldo + r] = c1[r];
+    }
+  }
+  __syncthreads();
+}
+
+// Row-major [ROWS x COLS] global block -> column-major shared memory.
+template <int ROWS, int COLS>
+__device__ __forceinline__ void load_cm(float* dst, int ld, const float* __restrict__ src, float scale = 1.0f) {
+  constexpr int E = ROWS * COLS, PER = (E + kThreads - 1) / kThreads;
+  float v[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = threadIdx.x + kThreads * i;
+    v[i] = (e < E) ? __ldg(src + e) : 0.0f;
+  }
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = threadIdx.x + kThreads * i;
+    if (e < E) dst[(e % COLS) * ld + e / COLS] = scale * v[i];
+  }
+}
+template <int N>
+__device__ __forceinline__ void load_vec(float* dst, const float* __restrict__ src) {
+  for (int i = threadIdx.x; i < N; i += kThreads) dst[i] = __ldg(src + i);
+}
+
+template <int NX, int NU, int NE>
+struct Lay {
+  static constexpr int LX = NX + (NX % 2 == 0 ? 1 : 2), LU = NU + (NU % 2 == 0 ? 1 : 2),
+                       LE = NE + (NE % 2 == 0 ? 1 : 2);
+  static constexpr int P = 0, A = P + NX * LX, PA = A + NX * LX, Q = PA + NX * LX, B = Q + NX * LX, PB = B + NU * LX,
+                       M = PB + NU * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, Z = QUX + NX * LU, W = Z + NX * LU,
+                       C = W + NE * LU, D = C + NX * LE, S = D + NU * LE, T = S + NE * LE, V = T + NX * LE;
+  // vectors, NX + 4 floats each
+  static constexpr int VL = NX + 4;
+  static constexpr int vc = V, vq = vc + VL, vr = vq + VL, ve = vr + VL, vw = ve + VL, vp = vw + VL, vqx = vp + VL,
+                       vqu = vqx + VL, vg = vqu + VL, vh = vg + VL, vkn = vh + VL, vk = vkn + VL, vx = vk + VL,
+                       vu = vx + VL, FLOATS = vu + VL;
+};
+
+template <int NX, int NU, int NE>
+constexpr size_t smem_bytes() { return (size_t)Lay<NX, NU, NE>::FLOATS * sizeof(float); }
+
+template <int NX, int NU, int NE>
+__global__ void __launch_bounds__(kThreads, 1) lqr_eq_kernel(mpxg_lq_eq_io io, float* Pscr) {
+  typedef Lay<NX, NU, NE> L;
+  constexpr int LX = L::LX, LU = L::LU, LE = L::LE;
+  extern __shared__ float4 smem4[];
+  float* s = reinterpret_cast<float*>(smem4);
+  float *P = s + L::P, *sA = s + L::A, *PA = s + L::PA, *sQ = s + L::Q, *sB = s + L::B, *PB = s + L::PB;
+  float *sM = s + L::M, *Quu = s + L::QUU, *Qux = s + L::QUX, *Z = s + L::Z, *W = s + L::W, *sC = s + L::C;
+  float *sD = s + L::D, *S = s + L::S, *T = s + L::T;
+  float *vc = s + L::vc, *vq = s + L::vq, *vr = s + L::vr, *ve = s + L::ve, *vw = s + L::vw, *vp = s + L::vp;
+  float *vqx = s + L::vqx, *vqu = s + L::vqu, *vg = s + L::vg, *vh = s + L::vh, *vkn = s + L::vkn, *vk = s + L::vk;
+  float *vx = s + L::vx, *vu = s + L::vu;
+  const int b = blockIdx.x, N = io.N, tid = threadIdx.x;
+  constexpr int NP = NX + 1;  // workspace rows per stage: P (NX x NX) then p
+  float* Ps = Pscr + (size_t)b * (N + 1) * NP * NX;
+  const size_t sn = (size_t)b * N, sn1 = (size_t)b * (N + 1);
+
+  // ---- terminal value function
+  load_cm<NX, NX>(P, LX, io.Q + (sn1 + N) * NX * NX);
+  load_vec<NX>(vp, io.q + (sn1 + N) * NX);
+  __syncthreads();
+  for (int e = tid; e < NX * NX; e += kThreads) Ps[(size_t)N * NP * NX + e] = P[(e / NX) * LX + e % NX];
+  for (int i = tid; i < NX; i += kThreads) Ps[(size_t)N * NP * NX + NX * NX + i] = vp[i];
+
+  for (int t = N - 1; t >= 0; --t) {
+    // ---- stage data
+    load_cm<NX, NX>(sA, LX, io.A + (sn + t) * NX * NX);
+    load_cm<NX, NU>(sB, LX, io.Bm + (sn + t) * NX * NU);
+    load_cm<NX, NX>(sQ, LX, io.Q + (sn1 + t) * NX * NX);
+    load_cm<NX, NU>(sM, LX, io.M + (sn + t) * NX * NU);
+    load_cm<NU, NU>(Quu, LU, io.R + (sn + t) * NU * NU);
+    load_cm<NE, NX>(sC, LE, io.C + (sn + t) * NE * NX);
+    load_cm<NE, NU>(sD, LE, io.D + (sn + t) * NE * NU);
+    load_vec<NX>(vc, io.c + (sn + t) * NX);
+    load_vec<NX>(vq, io.q + (sn1 + t) * NX);
+    load_vec<NU>(vr, io.r + (sn + t) * NU);
+    load_vec<NE>(ve, io.e + (sn + t) * NE);
+    __syncthreads();
+    // ---- P A, P B, w = P c + p
+    bmm<NX, NX, NX, false, false, false>(PA, LX, P, LX, sA, LX, 1.0f, nullptr, 0);
+    bmm<NX, NX, NU, false, false, false>(PB, LX, P, LX, sB, LX, 1.0f, nullptr, 0);
+    bmv<NX, NX, false>(vw, P, LX, vc, 1.0f, vp);
+    // ---- Q-function blocks
+    bmm<NX, NX, NX, true, false, false>(sQ, LX, sA, LX, PA, LX, 1.0f, sQ, LX);        // Q_xx
+    bmm<NU, NX, NX, true, false, true>(Qux, LU, sB, LX, PA, LX, 1.0f, sM, LX);        // Q_ux = M' + B'PA
+    bmm<NU, NX, NU, true, false, false>(Quu, LU, sB, LX, PB, LX, 1.0f, Quu, LU);      // Q_uu = R + B'PB
+    bmv<NX, NX, true>(vqx, sA, LX, vw, 1.0f, vq);                                     // q_x
+    bmv<NU, NX, true>(vqu, sB, LX, vw, 1.0f, vr);                                     // q_u
+    // ---- G = Q_uu^-1 (into PB); Z = G Q_ux, g = G q_u, W = G D'
+    float* G = PB;
+    spd_inverse<NU>(Quu, LU, G, LU);
+    bmm<NU, NU, NX, false, false, false>(Z, LU, G, LU, Qux, LU, 1.0f, nullptr, 0);
+    bmv<NU, NU, false>(vg, G, LU, vqu, 1.0f, nullptr);
+    bmm<NU, NU, NE, false, true, false>(W, LU, G, LU, sD, LE, 1.0f, nullptr, 0);
+    // ---- S = D W, T = C - D Z, h = D g + e
+    bmm<NE, NU, NE, false, false, false>(S, LE, sD, LE, W, LU, 1.0f, nullptr, 0);
+    bmm<NE, NU, NX, false, false, false>(T, LE, sD, LE, Z, LU, -1.0f, sC, LE);
+    bmv<NE, NU, false>(vh, sD, LE, vg, 1.0f, ve);
+    // ---- K_nu = S^-1 T (into M's buffer), k_nu = -S^-1 h
+    spd_inverse<NE>(S, LE, S, LE);
+    float* Kn = sM;
+    bmm<NE, NE, NX, false, false, false>(Kn, LE, S, LE, T, LE, 1.0f, nullptr, 0);
+    bmv<NE, NE, false>(vkn, S, LE, vh, -1.0f, nullptr);
+    // ---- Z <- Z + W K_nu (K = -Z), g <- g + W k_nu (k = -g)
+    bmm<NU, NE, NX, false, false, false>(Z, LU, W, LU, Kn, LE, 1.0f, Z, LU);
+    bmv<NU, NE, false>(vg, W, LU, vkn, 1.0f, vg);
+    // ---- gains out
+    {
+      float* Ko = io.K + (sn + t) * NU * NX;
+      float* ko = io.k + (sn + t) * NU;
+      float* Kno = io.Knu + (sn + t) * NE * NX;
+      float* kno = io.knu + (sn + t) * NE;
+      for (int e = tid; e < NU * NX; e += kThreads) Ko[e] = -Z[(e % NX) * LU + e / NX];
+      for (int e = tid; e < NE * NX; e += kThreads) Kno[e] = Kn[(e % NX) * LE + e / NX];
+      for (int a = tid; a < NU; a += kThreads) { vk[a] = -vg[a]; ko[a] = -vg[a]; }
+      for (int j = tid; j < NE; j += kThreads) kno[j] = vkn[j];
+    }
+    __syncthreads();
+    // ---- P <- Q_xx - Q_ux' Z + C' K_nu,  p <- q_x + Q_ux' k + C' k_nu
+    bmm<NX, NU, NX, true, false, false>(P, LX, Qux, LU, Z, LU, -1.0f, sQ, LX);
+    bmm<NX, NE, NX, true, false, false>(P, LX, sC, LE, Kn, LE, 1.0f, P, LX);
+    bmv<NX, NU, true>(vp, Qux, LU, vk, 1.0f, vqx);
+    bmv<NX, NE, true>(vp, sC, LE, vkn, 1.0f, vp);
+    for (int e = tid; e < NX * NX; e += kThreads) {  // symmetrise into PA, copy back
+      const int c = e / NX, r = e % NX;
+      PA[c * LX + r] = 0.5f * (P[c * LX + r] + P[r * LX + c]);
+    }
+    __syncthreads();
+    float* Pt = Ps + (size_t)t * NP * NX;
+    for (int e = tid; e < NX * NX; e += kThreads) {
+      const int c = e / NX, r = e % NX;
+      const float v = PA[c * LX + r];
+      P[c * LX + r] = v;
+      Pt[e] = v;  // symmetric: row-major = column-major
+    }
+    for (int i = tid; i < NX; i += kThreads) Pt[NX * NX + i] = vp[i];
+    __syncthreads();
+  }
+
+  // ---- forward: u = K x + k, x+ = A x + B u + c.  Stage t+1's rows are
+  // copied into shared memory (row-major, double-buffered over the backward
+  // pass's buffers) while stage t is computed; a warp per row, lanes over the
+  // row, shuffle reductions.
+  {
+    constexpr int SA = NX * NX, SB = NX * NU, SK = NU * NX, STG = SA + SB + SK + NX + NU;
+    constexpr int STG4 = (STG + 3) / 4;
+    static_assert(2 * STG4 * 4 <= L::V, "forward staging must fit the matrix buffers (below the vectors)");
+    float* stg[2] = {s, s + STG4 * 4};
+    const int wid = tid >> 5, lane = tid & 31;
+    float* X = io.X + sn1 * NX;
+    float* U = io.U + sn * NU;
+    // copy stage t into buffer buf (all threads), element-wise: A | B | K | c | k
+    auto stage_copy = [&](int t, float* buf) {
+      const float* A = io.A + (sn + t) * SA;
+      const float* Bm = io.Bm + (sn + t) * SB;
+      const float* K = io.K + (sn + t) * SK;
+      for (int e = tid; e < SA; e += kThreads) buf[e] = __ldg(A + e);
+      for (int e = tid; e < SB; e += kThreads) buf[SA + e] = __ldg(Bm + e);
+      for (int e = tid; e < SK; e += kThreads) buf[SA + SB + e] = K[e];
+      for (int e = tid; e < NX; e += kThreads) buf[SA + SB + SK + e] = __ldg(io.c + (sn + t) * NX + e);
+      for (int e = tid; e < NU; e += kThreads) buf[SA + SB + SK + NX + e] = io.k[(sn + t) * NU + e];
+    };
+    for (int i = tid; i < NX; i += kThreads) vx[i] = io.x0[(size_t)b * NX + i];
+    stage_copy(0, stg[0]);
+    __syncthreads();
+    for (int t = 0; t < N; ++t) {
+      float* cur = stg[t & 1];
+      // prefetch stage t+1 into registers while this stage computes
+      constexpr int PF = (STG + kThreads - 1) / kThreads;
+      float pre[PF];
+      if (t + 1 < N) {
+        const float* A = io.A + (sn + t + 1) * SA;
+        const float* Bm = io.Bm + (sn + t + 1) * SB;
+        const float* K = io.K + (sn + t + 1) * SK;
+#pragma unroll
+        for (int i = 0; i < PF; ++i) {
+          const int e = tid + kThreads * i;
+          float v = 0.0f;
+          if (e < SA) v = __ldg(A + e);
+          else if (e < SA + SB) v = __ldg(Bm + e - SA);
+          else if (e < SA + SB + SK) v = K[e - SA - SB];
+          else if (e < SA + SB + SK + NX) v = __ldg(io.c + (sn + t + 1) * NX + e - SA - SB - SK);
+          else if (e < STG) v = io.k[(sn + t + 1) * NU + e - SA - SB - SK - NX];
+          pre[i] = v;
+        }
+      }
+      for (int i = tid; i < NX; i += kThreads) X[t * NX + i] = vx[i];
+      // u = K x + k: a warp per row
+      const float* K = cur + SA + SB;
+      for (int a = wid; a < NU; a += kThreads / 32) {
+        float acc = 0.0f;
+        for (int k2 = lane; k2 < NX; k2 += 32) acc += K[a * NX + k2] * vx[k2];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+          const float u = acc + cur[SA + SB + SK + NX + a];
+          vu[a] = u;
+          U[t * NU + a] = u;
+        }
+      }
+      __syncthreads();
+      // x+ = A x + B u + c: a warp per row (results to vq, then copied)
+      const float* A = cur;
+      const float* Bm = cur + SA;
+      for (int i = wid; i < NX; i += kThreads / 32) {
+        float acc = 0.0f;
+        for (int k2 = lane; k2 < NX; k2 += 32) acc += A[i * NX + k2] * vx[k2];
+        for (int k2 = lane; k2 < NU; k2 += 32) acc += Bm[i * NU + k2] * vu[k2];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) vq[i] = acc + cur[SA + SB + SK + i];
+      }
+      if (t + 1 < N) {
+        float* nxt = stg[(t + 1) & 1];
+#pragma unroll
+        for (int i = 0; i < PF; ++i) {
+          const int e = tid + kThreads * i;
+          if (e < STG) nxt[e] = pre[i];
+        }
+      }
+      __syncthreads();
+      for (int i = tid; i < NX; i += kThreads) vx[i] = vq[i];
+      __syncthreads();
+    }
+    for (int i = tid; i < NX; i += kThreads) X[N * NX + i] = vx[i];
+  }
+  __syncthreads();
+  // ---- costates lam_t = P_t x_t + p_t and multipliers nu_t = K_nu x_t + k_nu:
+  // a warp per stage, lanes over each row (coalesced), shuffle reductions
+  {
+    const int wid = tid >> 5, lane = tid & 31;
+    const float* X = io.X + sn1 * NX;
+    for (int t = wid; t <= N; t += kThreads / 32) {
+      const float* Pt = Ps + (size_t)t * NP * NX;
+      float xl[(NX + 31) / 32];
+#pragma unroll
+      for (int q = 0; q < (NX + 31) / 32; ++q) xl[q] = (lane + 32 * q < NX) ? X[(size_t)t * NX + lane + 32 * q] : 0.0f;
+      for (int r = 0; r < NX; ++r) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < (NX + 31) / 32; ++q)
+          if (lane + 32 * q < NX) acc += Pt[(size_t)r * NX + lane + 32 * q] * xl[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) io.lam[(sn1 + t) * NX + r] = acc + Pt[NX * NX + r];
+      }
+      if (t < N) {
+        const float* Knt = io.Knu + (sn + t) * NE * NX;
+        for (int j = 0; j < NE; ++j) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int q = 0; q < (NX + 31) / 32; ++q)
+            if (lane + 32 * q < NX) acc += Knt[(size_t)j * NX + lane + 32 * q] * xl[q];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (lane == 0) io.nu[(sn + t) * NE + j] = acc + io.knu[(sn + t) * NE + j];
+        }
+      }
+    }
+  }
+}
+
+inline size_t lqr_eq_scratch_bytes(int batch, int N, int n) { return (size_t)batch * (N + 1) * (n + 1) * n * 4; }
+
+template <int NX, int NU, int NE>
+inline cudaError_t launch_lqr_eq(cudaStream_t st, const mpxg_lq_eq_io& io) {
+  const size_t smem = smem_bytes<NX, NU, NE>();
+  cudaError_t e = cudaFuncSetAttribute(lqr_eq_kernel<NX, NU, NE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  lqr_eq_kernel<NX, NU, NE><<<io.batch, kThreads, smem, st>>>(io, io.workspace);
+  return cudaGetLastError();
+}
+
+}  // namespace lqeq
+}  // namespace mpxg

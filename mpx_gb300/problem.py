@@ -300,6 +300,31 @@ def random_lq(batch, n, m, N, seed=0, rho=0.98):
     return dict(A=A, B=Bm, c=c, Q=Q, R=R, M=M, q=q, r=r, x0=x0)
 
 
+def random_lq_eq(batch, n=72, m=30, n_eq=12, N=100, seed=0, dt=0.1, rho_cap=1.01):
+    """Large linearised whole-body-sized LQ workload with stage equality
+    constraints C_t x_t + D_t u_t = e_t: A_t = I + dt J_t, J_t ~ N(0, 1/n),
+    spectral radius capped at rho_cap; B_t ~ N(0, 0.1/m); Q_t diagonal,
+    log-uniform in [1e-2, 1e2]; R_t = 1e-3 I; M_t = 0; n_eq constraint rows
+    [C_t D_t] ~ N(0, 1); c_t ~ N(0, 0.1^2), q_t ~ N(0, 1), r_t = 0,
+    e_t ~ N(0, 1), x0 ~ N(0, 1).  float64 arrays."""
+    rng = np.random.default_rng(seed)
+    J = rng.normal(0.0, 1.0 / np.sqrt(n), size=(batch, N, n, n))
+    A = np.eye(n) + dt * J
+    ev = np.abs(np.linalg.eigvals(A)).max(-1)
+    A = A * np.minimum(1.0, rho_cap / ev)[..., None, None]
+    Bm = rng.normal(0.0, np.sqrt(0.1 / m), size=(batch, N, n, m))
+    Q = np.zeros((batch, N + 1, n, n))
+    di = np.arange(n)
+    Q[..., di, di] = 10.0 ** rng.uniform(-2.0, 2.0, size=(batch, N + 1, n))
+    R = np.broadcast_to(1e-3 * np.eye(m), (batch, N, m, m)).copy()
+    M = np.zeros((batch, N, n, m))
+    CD = rng.normal(size=(batch, N, n_eq, n + m))
+    return dict(A=A, B=Bm, c=rng.normal(0.0, 0.1, size=(batch, N, n)), Q=Q, R=R, M=M,
+                q=rng.normal(size=(batch, N + 1, n)), r=np.zeros((batch, N, m)),
+                C=CD[..., :n].copy(), D=CD[..., n:].copy(), e=rng.normal(size=(batch, N, n_eq)),
+                x0=rng.normal(size=(batch, n)))
+
+
 BIPED_HIP_OFFSETS = np.array([[0.0, 0.10, -0.90], [0.0, -0.10, -0.90]])
 WALK_PHASE = np.array([0.0, 0.5])
 

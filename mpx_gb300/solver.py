@@ -251,6 +251,32 @@ def lqr_solve(A, B, c, Q, R, M, q, r, x0, method=0, stream=None):
     return out
 
 
+def lqr_eq_solve(A, B, c, Q, R, M, q, r, C, D, e, x0, stream=None):
+    """Batched equality-constrained LQR on the device (mpxg_lqr_eq_solve).
+    Shapes as in include/mpxg.h.  Returns dict K, k, Knu, knu, X, U, lam, nu."""
+    L = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    names = ("A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+    t = [torch.as_tensor(a).to(device=dev, dtype=_F32).contiguous() for a in (A, B, c, Q, R, M, q, r, C, D, e, x0)]
+    Bsz, N, n, _ = t[0].shape
+    m, ne = t[1].shape[-1], t[8].shape[-2]
+    out = dict(K=torch.empty(Bsz, N, m, n, device=dev), k=torch.empty(Bsz, N, m, device=dev),
+               Knu=torch.empty(Bsz, N, ne, n, device=dev), knu=torch.empty(Bsz, N, ne, device=dev),
+               X=torch.empty(Bsz, N + 1, n, device=dev), U=torch.empty(Bsz, N, m, device=dev),
+               lam=torch.empty(Bsz, N + 1, n, device=dev), nu=torch.empty(Bsz, N, ne, device=dev))
+    ws = torch.empty(max(int(L.mpxg_lqr_eq_workspace_bytes(Bsz, N, n)) // 4, 1), device=dev)
+    io = _lib.LqEqIO()
+    io.batch, io.N, io.n, io.m, io.n_eq = Bsz, N, n, m, ne
+    for name, ten in zip(names, t):
+        setattr(io, name, _ptr(ten))
+    for name in ("K", "k", "Knu", "knu", "X", "U", "lam", "nu"):
+        setattr(io, name, _ptr(out[name]))
+    io.workspace = _ptr(ws)
+    _lib.check(L.mpxg_lqr_eq_solve(_stream_handle(stream), ctypes.byref(io)), None, "mpxg_lqr_eq_solve")
+    out["_keep"] = (t, ws)
+    return out
+
+
 def gait_tables(stream, desc, batch, n_max, x0, X, U, V, v_ref, leg_time, reference, parameter, gait, mode,
                 slot=None, horizon=None, drift_std=0.0, seed=0):
     """mpxg_gait_tables for `batch` entries (pool rows `slot`); `gait` =

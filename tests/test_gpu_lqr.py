@@ -24,3 +24,29 @@ def test_lqr_matches_oracle(oracle, cuda, n, m, N, method):
         a = g[k].cpu().numpy()
         e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
         assert e < 2e-4, (k, e)
+
+
+@pytest.mark.parametrize("n,m,ne,N,B", [(8, 5, 2, 6, 3), (16, 8, 4, 20, 3), (72, 30, 12, 100, 2)])
+def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B):
+    """Equality-constrained LQR on the GPU against the FP64 stagewise Riccati
+    (itself checked against a dense KKT solve on the CPU)."""
+    from mpx_gb300.solver import lqr_eq_solve
+    from oracle.lqr_eq import riccati_eq
+    d = P.random_lq_eq(B, n=n, m=m, n_eq=ne, N=N, seed=n + N)
+    if n == 8:  # a cross term and a control-linear cost exercise the elimination (small
+        # enough that Q - M R^-1 M' stays positive definite with R = 1e-3 I)
+        d["M"] = 0.002 * np.random.default_rng(3).normal(size=d["M"].shape)
+        d["r"] = np.random.default_rng(4).normal(size=d["r"].shape)
+    keys = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+    g = lqr_eq_solve(*[d[k] for k in keys])
+    torch.cuda.synchronize()
+    for b in range(B):
+        o = riccati_eq(*[d[k][b] for k in keys])
+        for k in ("K", "k", "Knu", "knu", "X", "U", "lam", "nu"):
+            a = g[k][b].cpu().numpy()
+            e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
+            assert e < 2e-4, (k, b, e)
+        # constraint residual of the GPU trajectory
+        X, U = g["X"][b].cpu().double().numpy(), g["U"][b].cpu().double().numpy()
+        res = np.einsum("tij,tj->ti", d["C"][b], X[:N]) + np.einsum("tij,tj->ti", d["D"][b], U) - d["e"][b]
+        assert np.abs(res).max() < 1e-3 * max(1.0, np.abs(d["e"][b]).max())
