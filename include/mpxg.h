@@ -164,6 +164,27 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
 
 /* Gait timer of a batch (mpx/utils/mpc_utils.py:7-14), float32 without fused
  * multiply-add: leg_time [B, n_legs] updated in place, contact [B, n_legs]. */
+/* Vector-Jacobian product of converged solutions (the differentiable solve;
+ * the reference describes its solver as differentiable, README.md:26-27).
+ * At the solution X, U (with the duals V, as returned by mpxg_solve) the
+ * implicit-function theorem on the Gauss-Newton KKT system the solve factors
+ * gives, for cotangents gX [B,n_max+1,n], gU [B,n_max,m] of a scalar loss:
+ *   wX, wU, wL  the adjoint solution (H w + A'mu = g, A w = 0, dx_0 = 0;
+ *               wL the costates of that system, [B,n_max+1,n])
+ *   gx0 [B,n]   dLoss/dx0 = mu_0
+ *   gref [B,n_max+1,12]  dLoss/dreference for the 12 tracked state columns
+ *               (models with an identity tracking residual: roll-pitch-yaw
+ *               quadruped, biped), = W * wX.
+ * Any output pointer may be NULL.  Same handle, batch layout and slots as
+ * mpxg_solve; K, k, kkt, first and V_in of mpxg_batch_io are ignored. */
+typedef struct {
+  mpxg_batch_io io;        /* x0, X_in (= X), U_in (= U), V_in, reference, parameter, w, horizon, slot, batch */
+  const float* gX;
+  const float* gU;
+  float *wX, *wU, *wL, *gx0, *gref;
+} mpxg_vjp_io;
+mpxg_status mpxg_solve_vjp(mpxg_handle* h, void* stream, const mpxg_vjp_io* v);
+
 /* Cost and constraint residuals of trajectories X [batch, n_max+1, n], U
  * [batch, n_max, m] with the handle's model (replaces
  * optimizers.model_evaluator_helper(cost, dynamics, x0, X, U) -> (g, c),

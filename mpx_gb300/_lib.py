@@ -76,6 +76,10 @@ class BatchIO(ctypes.Structure):
                 ("status", ctypes.c_void_p), ("first", ctypes.c_void_p)]
 
 
+class VjpIO(ctypes.Structure):
+    _fields_ = [("io", BatchIO)] + [(k, ctypes.c_void_p) for k in ("gX", "gU", "wX", "wU", "wL", "gx0", "gref")]
+
+
 class GaitArgs(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int), ("batch", ctypes.c_int), ("n_max", ctypes.c_int), ("mode", ctypes.c_int),
                 ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
@@ -96,7 +100,7 @@ class LqIO(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
@@ -145,6 +149,8 @@ def load(build_if_missing=True):
                "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll", "mpxg_server_completed",
                "mpxg_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
+    L.mpxg_solve_vjp.argtypes = [vp, vp, ctypes.POINTER(VjpIO)]
+    L.mpxg_solve_vjp.restype = ctypes.c_int
     L.mpxg_lqr_eq_workspace_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.mpxg_lqr_eq_workspace_bytes.restype = ctypes.c_size_t
     L.mpxg_lqr_eq_solve.argtypes = [vp, ctypes.POINTER(LqEqIO)]

@@ -377,6 +377,73 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
   return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "shift_kernel launch");
 }
 
+}  // extern "C"
+
+template <class M>
+static mpxg_status launch_vjp(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb) {
+  const size_t smem = smem_per_warp<M>() * (size_t)wpb;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(sqp_vjp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
+  }
+  sqp_vjp_kernel<M><<<blocks, wpb * 32, smem, st>>>(h->mc, h->sp, bp);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "sqp_vjp_kernel launch");
+}
+
+extern "C" {
+
+mpxg_status mpxg_solve_vjp(mpxg_handle* h, void* stream, const mpxg_vjp_io* v) {
+  if (!v) return fail(h, MPXG_ERR_INVALID_ARG, "mpxg_solve_vjp: null io");
+  mpxg_batch_io io = v->io;
+  io.X = const_cast<float*>(io.X_in);
+  io.U = const_cast<float*>(io.U_in);
+  io.V = const_cast<float*>(io.V_in);
+  mpxg_status s = check_io(h, &io);
+  if (s != MPXG_OK) return s;
+  if (!v->gX || !v->gU) return fail(h, MPXG_ERR_INVALID_ARG, "mpxg_solve_vjp: cotangents gX, gU required");
+  if (io.batch == 0) return MPXG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchPtrs bp = make_ptrs(h, &io);
+  bp.K = nullptr; bp.k = nullptr; bp.kkt = nullptr; bp.first = nullptr; bp.status = io.status;
+  bp.gX = v->gX; bp.gU = v->gU; bp.wX = v->wX; bp.wU = v->wU; bp.wL = v->wL; bp.gx0 = v->gx0; bp.gref = v->gref;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, MPXG_ERR_CUDA, "mpxg_solve_vjp: cudaStreamIsCapturing failed");
+  }
+  int r;
+  if (cap == cudaStreamCaptureStatusNone) {
+    r = h->ring_next;
+    h->ring_next = (r + 1) % mpxg_handle::kRing;
+    if (h->ring_used[r]) {
+      cudaError_t e = cudaStreamWaitEvent(st, h->ring_ev[r], 0);
+      if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamWaitEvent");
+    }
+  } else {
+    r = mpxg_handle::kRing + h->capture_next;
+    h->capture_next = (h->capture_next + 1) % mpxg_handle::kRing;
+  }
+  bp.counter = h->counters + (size_t)r * mpxg_handle::kCounterStride;
+  cudaError_t e = cudaMemsetAsync(bp.counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
+  const int wpb = h->warps_per_block;
+  int blocks = h->num_sms * h->blocks_per_sm_lat;
+  const int need = (io.batch + wpb - 1) / wpb;
+  if (need < blocks) blocks = need;
+  switch (h->desc.model) {
+    case MPXG_MODEL_SRBD_QUAT13: s = launch_vjp<ModelQuat13>(h, st, bp, blocks, wpb); break;
+    case MPXG_MODEL_SRBD_RPY12: s = launch_vjp<ModelRpy12>(h, st, bp, blocks, wpb); break;
+    case MPXG_MODEL_BIPED_WRENCH12: s = launch_vjp<ModelBiped12>(h, st, bp, blocks, wpb); break;
+    default: return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_solve_vjp: model");
+  }
+  if (s != MPXG_OK || cap != cudaStreamCaptureStatusNone) return s;
+  e = cudaEventRecord(h->ring_ev[r], st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
+  h->ring_used[r] = true;
+  return MPXG_OK;
+}
+
 mpxg_status mpxg_evaluate(mpxg_handle* h, void* stream, int batch, const int* horizon, const float* x0,
                           const float* X, const float* U, const float* reference, const float* parameter,
                           const float* w, float* g, float* c) {

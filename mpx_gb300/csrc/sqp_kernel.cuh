@@ -54,6 +54,11 @@ struct BatchPtrs {
   // Optional processing order of the batch entries (longest horizon first):
   // the i-th instance taken from the work queue is batch entry order[i].
   const int* order = nullptr;
+  // Vector-Jacobian product mode (sqp_vjp_kernel): cotangents gX, gU of the
+  // converged X, U in; adjoint solution wX, wU, wL and the gradients with
+  // respect to x0 and to the state reference out.
+  const float *gX = nullptr, *gU = nullptr;
+  float *wX = nullptr, *wU = nullptr, *wL = nullptr, *gx0 = nullptr, *gref = nullptr;
 };
 
 // Counting sort of the batch entries by horizon, longest first, into order[]
@@ -523,7 +528,10 @@ __device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT,
 }
 
 // ----------------------------------------------------------------- one instance
-template <class M>
+// VJP = true: one Gauss-Newton KKT solve at the given (converged) X, U with
+// the gradient replaced by -(cotangents), zero defects and dx_0 = 0 -- the
+// adjoint system of the implicit-function theorem -- instead of the SQP loop.
+template <class M, bool VJP = false>
 __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int bidx,
                                WarpSmem<M>& sm, float* scr) {
   const int b = bp.slot ? bp.slot[bidx] : bidx;  // pool row of this batch entry
@@ -550,11 +558,11 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   const float* par = bp.par + (size_t)b * (n_max + 1) * M::NPAR;
   Scratch<M> s(scr, n_max);
 
-  if (bp.X_in != bp.X)
+  if (!VJP && bp.X_in != bp.X)
     for (int e = lane; e < (N + 1) * NX; e += 32) X[e] = bp.X_in[xo + e];
-  if (bp.V_in != bp.V)
+  if (!VJP && bp.V_in != bp.V)
     for (int e = lane; e < (N + 1) * NX; e += 32) V[e] = bp.V_in[xo + e];
-  if (bp.U_in != bp.U)
+  if (!VJP && bp.U_in != bp.U)
     for (int e = lane; e < N * NU; e += 32) U[e] = bp.U_in[uo + e];
   if (lane < 24) sm.w[lane] = bp.w[(size_t)b * 24 + lane];
   // zero padding rows of the shared P / F columns (read by the float4 products)
@@ -565,13 +573,30 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   float rho = sp.rho0;
   int status = 0;
 
-  for (int it = 0; it < sp.sqp_iters; ++it) {
+  for (int it = 0; it < (VJP ? 1 : sp.sqp_iters); ++it) {
     // ================================================ phase 1: linearise all stages
     float lsum = 0.0f, dummy = 0.0f;
     for (int t = lane; t <= N; t += 32)
       lin_stage<M, false>(mc, t, N, x0, X, U, V, ref, par, sm.w, s, &lsum, &dummy, &dummy, &dummy);
     const double Jc = warp_sum((double)lsum);
     __syncwarp();
+    if (VJP) {  // adjoint right-hand side: gradient <- -cotangent, defects <- 0
+      const float* gx = bp.gX + xo;
+      const float* gu = bp.gU + uo;
+      for (int t = lane; t <= N; t += 32) {
+        float* Gt = s.G + (size_t)t * D::GS;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) Gt[D::G_GRAD + i] = -gx[t * NX + i];
+        if (t < N) {
+#pragma unroll
+          for (int a = 0; a < NU; ++a) Gt[D::G_GRAD + NX + a] = -gu[t * NU + a];
+          float* Fa = s.F + (size_t)t * NZ * FS + JA * FS;
+#pragma unroll
+          for (int i = 0; i < FS; ++i) Fa[i] = 0.0f;
+        }
+      }
+      __syncwarp();
+    }
     // ================================================ phase 2: backward Riccati
     {
       const float* GN = s.G + (size_t)N * D::GS;
@@ -755,7 +780,7 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
     fpre3.load(s.F, lane);
     gpre3.load(s.G, lane);
     if (lane < NX) {
-      c_cur = x0[lane] - X[lane];
+      c_cur = VJP ? 0.0f : x0[lane] - X[lane];
       sm.dx[lane] = c_cur;
     }
     for (int t = 0; t <= N; ++t) {
@@ -816,6 +841,27 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
     }
     __syncwarp();
     const double gd = warp_sum(a_gd), lc = warp_sum(a_lc), vc = warp_sum(a_vc), cs = warp_sum(a_cs);
+    if (VJP) {  // adjoint solution and gradients out; no step is taken
+      __threadfence_block();
+      __syncwarp();
+      float* wx = bp.wX ? bp.wX + xo : nullptr;
+      float* wl = bp.wL ? bp.wL + xo : nullptr;
+      for (int e = lane; e < (N + 1) * NX; e += 32) {
+        if (wx) wx[e] = s.dX[e];
+        if (wl) wl[e] = s.L[e];
+      }
+      if (bp.wU)
+        for (int e = lane; e < N * NU; e += 32) bp.wU[uo + e] = s.dU[e];
+      if (bp.gx0 && lane < NX) bp.gx0[(size_t)b * NX + lane] = -s.L[lane];  // mu_0 = -lambda_0
+      if (bp.gref && M::IDENT_RES) {  // tracking rows: d(grad l)/d(ref) = -W, so g_ref = W w_x
+        float* gr = bp.gref + (size_t)b * (n_max + 1) * 12;
+        for (int e = lane; e < (N + 1) * 12; e += 32) {
+          const int t = e / 12, a = e - 12 * t;
+          gr[e] = sm.w[a] * s.dX[t * NX + a];
+        }
+      }
+      break;
+    }
     // ================================================ phase 4: merit line search
     const double G = gd + lc;
     if (cs > 0.0 && G > 0.0) rho = fminf(fmaxf(rho, (float)(2.0 * G / cs)), 1e12f);
@@ -911,7 +957,7 @@ struct SqpMinBlocks { static constexpr int value = MPXG_SQP_MIN_BLOCKS; };
 template <>
 struct SqpMinBlocks<ModelRpy12> { static constexpr int value = 4; };
 
-template <class M>
+template <class M, bool VJP = false>
 __device__ __forceinline__ void sqp_body(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp) {
   extern __shared__ float4 smem_raw[];
   WarpSmem<M>* sms = reinterpret_cast<WarpSmem<M>*>(smem_raw);
@@ -943,7 +989,7 @@ __device__ __forceinline__ void sqp_body(const ModelConst& mc, const SqpParams& 
     } else {
       done = 1;
     }
-    solve_instance<M>(mc, sp, bp, b, sm, scr);
+    solve_instance<M, VJP>(mc, sp, bp, b, sm, scr);
   }
   if (bp.slot_bits) {  // release the slot once every lane's scratch writes are visible
     __threadfence();
@@ -960,6 +1006,11 @@ template <class M>
 __global__ void __launch_bounds__(128, SqpMinBlocks<M>::value) sqp_kernel_tput(ModelConst mc, SqpParams sp,
                                                                               BatchPtrs bp) {
   sqp_body<M>(mc, sp, bp);
+}
+// Vector-Jacobian product of converged solutions (mpxg_solve_vjp).
+template <class M>
+__global__ void __launch_bounds__(128, MPXG_SQP_MIN_BLOCKS) sqp_vjp_kernel(ModelConst mc, SqpParams sp, BatchPtrs bp) {
+  sqp_body<M, true>(mc, sp, bp);
 }
 
 }  // namespace mpxg

@@ -200,6 +200,31 @@ class Solver:
         out["_keep"] = (x0, X0, U0, V0, reference, parameter, w, horizon)
         return out
 
+    def vjp(self, x0, X, U, V, reference, parameter, W, gX, gU, horizon=None, stream=None):
+        """Vector-Jacobian product of a converged solve (mpxg_solve_vjp):
+        cotangents gX [B,n_max+1,n], gU [B,n_max,m] of a scalar loss of the
+        solution -> dict gx0 [B,n] (dLoss/dx0), gref [B,n_max+1,12]
+        (dLoss/dreference, tracked state columns), and the adjoint solution
+        wX, wU, wL."""
+        x0, X, U, V, reference, parameter, w, horizon = self.prepare(x0, X, U, V, reference, parameter, W, horizon)
+        gX, gU = self._dev(gX), self._dev(gU)
+        B = x0.shape[0]
+        N, n, m = self.n_max, self.desc.n, self.desc.m
+        dev = self.device
+        out = dict(gx0=torch.empty(B, n, device=dev), gref=torch.zeros(B, N + 1, 12, device=dev),
+                   wX=torch.empty(B, N + 1, n, device=dev), wU=torch.empty(B, N, m, device=dev),
+                   wL=torch.empty(B, N + 1, n, device=dev))
+        v = _lib.VjpIO()
+        v.io = self.io(x0, X, U, V, reference, parameter, w, horizon, dict(X=X, U=U, V=V))
+        v.gX, v.gU = _ptr(gX), _ptr(gU)
+        for k in ("wX", "wU", "wL", "gx0", "gref"):
+            setattr(v, k, _ptr(out[k]))
+        with torch.cuda.device(self.device):
+            st = self.L.mpxg_solve_vjp(self.handle, _stream_handle(stream), ctypes.byref(v))
+        _lib.check(st, self.handle, "mpxg_solve_vjp")
+        out["_keep"] = (x0, X, U, V, reference, parameter, w, horizon, gX, gU)
+        return out
+
     def evaluate(self, x0, X, U, reference, parameter, W, horizon=None, stream=None):
         """(g, c) of trajectories X, U (the reference's model_evaluator_helper,
         mpc_wrapper.py:419-423,452-465): g [B, n_max+1] the stage costs (sum =

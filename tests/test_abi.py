@@ -47,7 +47,7 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(mpxg_problem_desc), sizeof(mpxg_solver_opts),
          sizeof(mpxg_batch_io), sizeof(mpxg_lq_io), sizeof(mpxg_xla_opaque), sizeof(mpxg_served_model),
          sizeof(mpxg_server_desc), sizeof(mpxg_result));
-  printf("%zu\n", sizeof(mpxg_lq_eq_io));
+  printf("%zu %zu\n", sizeof(mpxg_lq_eq_io), sizeof(mpxg_vjp_io));
   return 0;
 }
 '''
@@ -59,7 +59,8 @@ int main(void) {
         sizes = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert sizes == [ctypes.sizeof(_lib.ProblemDesc), ctypes.sizeof(_lib.SolverOpts), ctypes.sizeof(_lib.BatchIO),
                      ctypes.sizeof(_lib.LqIO), ctypes.sizeof(_lib.XlaOpaque), ctypes.sizeof(_lib.ServedModel),
-                     ctypes.sizeof(_lib.ServerDesc), ctypes.sizeof(_lib.Result), ctypes.sizeof(_lib.LqEqIO)]
+                     ctypes.sizeof(_lib.ServerDesc), ctypes.sizeof(_lib.Result), ctypes.sizeof(_lib.LqEqIO),
+                     ctypes.sizeof(_lib.VjpIO)]
 
 
 def test_xla_target_rejects_a_malformed_opaque():

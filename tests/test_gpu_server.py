@@ -89,3 +89,34 @@ def test_c_poll_returns_each_result_once(cuda):
     assert np.all(np.isfinite(np.array(r.u0[:12]))) and r.status & 1 == 0
     assert L.mpxg_poll(s.handle, t.value, ctypes.byref(r)) == 1
     s.close()
+
+
+def test_nan_result_then_reset_recovers(cuda):
+    """A non-finite state makes the solve report MPXG_INST_NAN; after
+    reset_slot with a valid state the episode's next tick is cold-started and
+    finite (the NaN fallback of mpc_wrapper.py:79-98)."""
+    s = make_server()
+    bad = x0_of(s, "quadruped", 5)
+    bad[3] = np.nan
+    s.admit("N", "quadruped", bad, 25)
+    s.submit("N"); s.drain()
+    assert s.completed[-1][5] & 1
+    s.reset_slot("N", x0_of(s, "quadruped", 5))
+    s.submit("N"); s.drain()
+    last = s.completed[-1]
+    assert last[5] & 1 == 0 and np.all(np.isfinite(last[3]))
+    s.close()
+
+
+def test_release_waits_for_queued_tick(cuda):
+    """A released episode keeps its slot until its queued tick has run."""
+    s = make_server(max_slots=1)
+    s.admit("A", "quadruped", x0_of(s, "quadruped", 1), 30)
+    s.submit("A")
+    s.release("A")                      # tick still queued: slot stays taken
+    with pytest.raises(BudgetError):
+        s.admit("B", "quadruped", x0_of(s, "quadruped", 2), 30)
+    s.drain()
+    assert len(s.completed) == 1 and s.completed[0][1] == "A"
+    s.admit("B", "quadruped", x0_of(s, "quadruped", 2), 30)   # freed once the tick completed
+    s.close()
