@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream section")
     ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
+    ap.add_argument("--no-autotune", action="store_true", help="use the default launch geometry")
     ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq"],
                     help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve; lqr_eq: the "
                          "equality-constrained n=72 LQ solve")
@@ -223,7 +224,13 @@ def run_ours(args, rank, world, local_rank):
     wl = P.quadruped_workload(B, horizons=HORIZONS, seed=SEED + rank, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
                               random_phase=True)
     opts = P.SolverOptions(sqp_iters=SQP_ITERS)
-    tr = TickRunner(wl, opts, device=dev, drift_std=DRIFT)
+    tuned = None
+    wpb, bps = 0, 0
+    if not args.no_autotune and not args.profile:
+        from mpx_gb300.autotune import tune
+        tuned = tune(wl, opts, device=dev)
+        wpb, bps = tuned["best"]
+    tr = TickRunner(wl, opts, device=dev, drift_std=DRIFT, warps_per_block=wpb, blocks_per_sm=bps)
     stream = torch.cuda.Stream(device=dev)
     n, m = wl.desc.n, wl.desc.m
     with torch.cuda.stream(stream):
@@ -472,6 +479,10 @@ def run_ours(args, rank, world, local_rank):
         "graph": use_graph,
         "clocks": clk,
         "geometry": tr.solver.geometry(),
+        "autotune": None if tuned is None else {
+            "best": {"warps_per_block": tuned["best"][0], "blocks_per_sm": tuned["best"][1] or "auto"},
+            "cached": tuned["cached"],
+            "ms_per_solve": {"%dx%s" % (r["wpb"], r["bps"] or "auto"): r.get("ms") for r in tuned["table"]}},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

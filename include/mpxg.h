@@ -94,7 +94,7 @@ typedef struct {
   int ls_max_trials;   /* merit line-search trials */
   float ls_beta, ls_eta, reg, rho0, ls_skip_tol;
   int compute_kkt;     /* 1: evaluate the KKT residual of the result */
-  int warps_per_block; /* 0: default (tuned) */
+  int warps_per_block; /* 0: default (4); at most 4 */
   int blocks_per_sm;   /* 0: default (tuned) */
 } mpxg_solver_opts;
 

@@ -177,6 +177,8 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (d->n_max < 1 || d->n_max > 4096) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: n_max out of range");
   if (d->batch_max < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: batch_max < 1");
   if (o->sqp_iters < 0 || o->ls_max_trials < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: bad options");
+  if (o->warps_per_block < 0 || o->warps_per_block > 4 || o->blocks_per_sm < 0)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: warps_per_block must be 0..4 (128-thread blocks)");
   if (!(d->dt > 0.0f) || !(d->mass > 0.0f)) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: dt and mass must be > 0");
   mpxg_handle* h = new mpxg_handle();
   h->desc = *d;
