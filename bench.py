@@ -393,14 +393,12 @@ def run_ours(args, rank, world, local_rank):
     served = None
     if not args.no_served and not args.profile and rank == 0:
         from mpx_gb300.server import MPCServer, default_models, served_workload
-        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=16,
+        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
                         device=dev)
         served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, seed=1)  # warm-up
-        srv.completed.clear()
         launches0 = srv.launches
         lat, wall = served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=2.0, seed=2)
-        sk = np.array([d[4][2] for d in srv.completed])
-        sst = np.array([d[5] for d in srv.completed])
+        sk, sst = srv.last_kkt, srv.last_status
         served = {"offered_req_per_s": 20000.0, "completed_req_per_s": len(lat) / wall, "requests": int(len(lat)),
                   "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
                                  "p99": 1e3 * float(np.percentile(lat, 99)),
@@ -409,10 +407,10 @@ def run_ours(args, rank, world, local_rank):
                   "gpu_launches": srv.launches - launches0,
                   "workload": "Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, "
                               "alternating), N uniform in [20, 200], 200-tick episodes, state drift N(0, 0.01^2), "
-                              "8 GB admission budget, 16 streams"}
+                              "8 GB admission budget, 32 streams"}
         # the same stream with every episode a quadruped at N = 50 (the latency target's case)
         srv.close()
-        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=16,
+        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
                         device=dev)
         served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, horizon_range=(50, 50), seed=1,
                         models=("quadruped",))
@@ -421,6 +419,21 @@ def run_ours(args, rank, world, local_rank):
         served["n50_quadruped"] = {"completed_req_per_s": len(lat50) / wall50,
                                    "latency_ms": {"p50": 1e3 * float(np.percentile(lat50, 50)),
                                                   "p99": 1e3 * float(np.percentile(lat50, 99))}}
+        srv.close()
+        # 4096 concurrent N = 50 quadruped episodes served at rising request rates
+        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
+                        device=dev)
+        sweep = []
+        for rate in (50000.0, 150000.0, 300000.0):
+            served_workload(srv, n_episodes=4096, rate_hz=rate, duration_s=0.2, horizon_range=(50, 50), seed=3,
+                            models=("quadruped",))
+            l4, w4 = served_workload(srv, n_episodes=4096, rate_hz=rate, duration_s=1.0, horizon_range=(50, 50),
+                                     seed=4, models=("quadruped",))
+            sweep.append({"offered_req_per_s": rate, "completed_req_per_s": len(l4) / w4,
+                          "latency_ms": {"p50": 1e3 * float(np.percentile(l4, 50)),
+                                         "p99": 1e3 * float(np.percentile(l4, 99))},
+                          "kkt_frac_le_1e-5": float((srv.last_kkt <= 1e-5).mean())})
+        served["envs4096_n50"] = sweep
         srv.close()
         del srv
 

@@ -374,6 +374,10 @@ mpxg_status mpxg_server_reset(mpxg_server* s, int episode, const float* x0);
 mpxg_status mpxg_server_release(mpxg_server* s, int episode);
 /* Queue the episode's next control tick; *ticket identifies its result. */
 mpxg_status mpxg_submit(mpxg_server* s, int episode, long long* ticket);
+/* Queue the next tick of n episodes at once (tickets[i] for episodes[i]);
+ * stops at the first failing episode and returns its status (tickets of the
+ * queued ones are set). */
+mpxg_status mpxg_submit_many(mpxg_server* s, const int* episodes, int n, long long* tickets);
 /* Collect finished batches and launch queued ticks on free streams (one tick
  * per episode in flight at a time).  Never blocks; `block` != 0 waits for the
  * oldest running batch first.  *launched / *finished (may be NULL): ticks

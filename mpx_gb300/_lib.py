@@ -102,7 +102,7 @@ EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
            "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
-           "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll",
+           "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
 
 _lib = None
@@ -139,6 +139,7 @@ def load(build_if_missing=True):
     L.mpxg_server_reset.argtypes = [vp, ci, vp]
     L.mpxg_server_release.argtypes = [vp, ci]
     L.mpxg_submit.argtypes = [vp, ci, ctypes.POINTER(cll)]
+    L.mpxg_submit_many.argtypes = [vp, vp, ci, vp]
     L.mpxg_server_step.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
     L.mpxg_poll.argtypes = [vp, cll, ctypes.POINTER(Result)]
     L.mpxg_server_completed.argtypes = [vp, ctypes.POINTER(Result), ci, ctypes.POINTER(ci)]
@@ -146,7 +147,7 @@ def load(build_if_missing=True):
     L.mpxg_server_last_error.argtypes = [vp]
     L.mpxg_server_last_error.restype = ctypes.c_char_p
     for fn in ("mpxg_server_create", "mpxg_server_capacity", "mpxg_server_admit", "mpxg_server_reset",
-               "mpxg_server_release", "mpxg_submit", "mpxg_server_step", "mpxg_poll", "mpxg_server_completed",
+               "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll", "mpxg_server_completed",
                "mpxg_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
     L.mpxg_solve_vjp.argtypes = [vp, vp, ctypes.POINTER(VjpIO)]

@@ -436,6 +436,15 @@ mpxg_status mpxg_submit(mpxg_server* s, int episode, long long* ticket) {
   return MPXG_OK;
 }
 
+mpxg_status mpxg_submit_many(mpxg_server* s, const int* episodes, int n, long long* tickets) {
+  if (!s || n < 0 || (n > 0 && (!episodes || !tickets))) return MPXG_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i) {
+    mpxg_status r = mpxg_submit(s, episodes[i], tickets + i);
+    if (r != MPXG_OK) return r;
+  }
+  return MPXG_OK;
+}
+
 mpxg_status mpxg_server_step(mpxg_server* s, int block, int* launched, int* finished) {
   using namespace mpxg_srv;
   if (!s) return MPXG_ERR_INVALID_ARG;

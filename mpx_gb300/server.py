@@ -48,7 +48,7 @@ class MPCServer:
     split evenly between the models; each model's pool holds as many slots as
     fit after its solver scratch."""
 
-    def __init__(self, models, n_max=200, budget_bytes=8 << 30, opts=None, streams=16, device=None, drift_std=0.01,
+    def __init__(self, models, n_max=200, budget_bytes=8 << 30, opts=None, streams=32, device=None, drift_std=0.01,
                  seed=0, max_slots=None):
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.opts = opts or P.SolverOptions()
@@ -92,8 +92,15 @@ class MPCServer:
         self.episodes = {}     # key -> episode id
         self._m = {}           # key -> controls per result row
         self._arrival = {}     # ticket -> (key, m, arrival time)
+        self._t_arr = np.zeros(1 << 16)   # ticket -> arrival time (the vectorised poll_fast path)
         self.completed = []
         self._res = (_lib.Result * 4096)()
+        self._res_np = np.frombuffer(self._res, dtype=np.dtype(
+            {"names": ["ticket", "episode", "status", "u0", "kkt"],
+             "formats": ["<i8", "<i4", "<i4", ("<f4", 12), ("<f4", 3)],
+             "offsets": [_lib.Result.ticket.offset, _lib.Result.episode.offset, _lib.Result.status.offset,
+                         _lib.Result.u0.offset, _lib.Result.kkt.offset],
+             "itemsize": ctypes.sizeof(_lib.Result)}))
 
     def close(self):
         if getattr(self, "handle", None) is not None and self.handle.value:
@@ -148,8 +155,32 @@ class MPCServer:
         """Queue the next control tick of an admitted episode; returns its ticket."""
         t = ctypes.c_longlong()
         self._check(self.L.mpxg_submit(self.handle, self.episodes[episode], ctypes.byref(t)), "submit")
-        self._arrival[t.value] = (episode, self._m[episode], time.perf_counter() if arrival is None else arrival)
+        a = time.perf_counter() if arrival is None else arrival
+        self._arrival[t.value] = (episode, self._m[episode], a)
+        self._note_arrival(np.array([t.value]), np.array([a]))
         return t.value
+
+    def _note_arrival(self, tickets, times):
+        top = int(tickets.max())
+        if top >= self._t_arr.shape[0]:
+            grown = np.zeros(max(2 * self._t_arr.shape[0], top + 1))
+            grown[:self._t_arr.shape[0]] = self._t_arr
+            self._t_arr = grown
+        self._t_arr[tickets] = times
+
+    def submit_many(self, episodes, arrival=None):
+        """Queue the next tick of several episodes in one call; returns their tickets."""
+        n = len(episodes)
+        if n == 0:
+            return []
+        ids = np.fromiter((self.episodes[e] for e in episodes), dtype=np.int32, count=n)
+        t = np.empty(n, dtype=np.int64)
+        self._check(self.L.mpxg_submit_many(self.handle, ids.ctypes.data, n, t.ctypes.data), "submit_many")
+        times = np.full(n, time.perf_counter()) if arrival is None else np.asarray(arrival, dtype=np.float64)
+        for k, e in enumerate(episodes):
+            self._arrival[int(t[k])] = (e, self._m[e], times[k])
+        self._note_arrival(t, times)
+        return t.tolist()
 
     def launch_pending(self):
         """Launch queued ticks on free streams (and collect finished batches)."""
@@ -189,6 +220,28 @@ class MPCServer:
         self.completed.extend(done)
         return done
 
+    def poll_fast(self, block=False):
+        """poll() without per-result Python objects: returns (latency_s,
+        status, kkt) arrays of the ticks finished now (for high request
+        rates; the tickets' episodes are not reported)."""
+        self._check(self.L.mpxg_server_step(self.handle, 1 if block else 0, None, None), "step")
+        now = time.perf_counter()
+        lat, st, kk = [], [], []
+        while True:
+            cnt = ctypes.c_int()
+            self._check(self.L.mpxg_server_completed(self.handle, self._res, len(self._res), ctypes.byref(cnt)),
+                        "completed")
+            r = self._res_np[:cnt.value]
+            tk = r["ticket"]
+            lat.append(now - self._t_arr[tk])
+            st.append(r["status"].copy())
+            kk.append(r["kkt"][:, 2].copy())
+            for t in tk.tolist():
+                self._arrival.pop(t, None)
+            if cnt.value < len(self._res):
+                break
+        return np.concatenate(lat), np.concatenate(st), np.concatenate(kk)
+
     def drain(self):
         """Wait for every queued and running tick."""
         while True:
@@ -203,7 +256,9 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
                     models=("quadruped", "biped"), v_range=(-0.5, 0.5)):
     """Poisson request stream (rate_hz) over `n_episodes` concurrent episodes
     of `episode_ticks` ticks; finished episodes are replaced by new ones.
-    Runs in real time; returns (latencies in s, wall time in s)."""
+    Runs in real time; returns (latencies in s, wall time in s); the statuses
+    and KKT residuals of the completed ticks are left in server.last_status
+    and server.last_kkt."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=int(rate_hz * duration_s * 1.2) + 16)
     arrivals = np.cumsum(gaps)
@@ -227,29 +282,39 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
         new_episode()
     t0 = time.perf_counter()
     i = 0
-    lat = []
+    lat, stats, kkts = [], [], []
     while True:
         now = time.perf_counter() - t0
+        keys, arr = [], []
         while i < len(arrivals) and arrivals[i] <= now:
             ep = eps[0]
             eps.rotate(-1)
-            server.submit(ep[0], arrival=t0 + arrivals[i])
+            keys.append(ep[0])
+            arr.append(t0 + arrivals[i])
             ep[1] += 1
             if ep[1] >= episode_ticks:
                 eps.remove(ep)
+                server.submit_many(keys, arr)
+                keys, arr = [], []
                 server.release(ep[0])  # deferred until its last tick completes
                 new_episode()
             i += 1
-        lat.extend(d[2] for d in server.poll())
+        if keys:
+            server.submit_many(keys, arr)
+        la, st, kk = server.poll_fast()
+        lat.append(la); stats.append(st); kkts.append(kk)
         if i >= len(arrivals):
             q, r, _ = server.stats()
             if q == 0 and r == 0:
-                lat.extend(d[2] for d in server.poll())
+                la, st, kk = server.poll_fast()
+                lat.append(la); stats.append(st); kkts.append(kk)
                 break
     wall = time.perf_counter() - t0
+    server.last_status = np.concatenate(stats) if stats else np.zeros(0, np.int32)
+    server.last_kkt = np.concatenate(kkts) if kkts else np.zeros(0, np.float32)
     for ep, _ in eps:
         server.release(ep)
-    return np.asarray(lat), wall
+    return np.concatenate(lat) if lat else np.zeros(0), wall
 
 
 def default_models():

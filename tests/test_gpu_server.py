@@ -64,8 +64,7 @@ def test_served_stream_reports_latency(cuda):
                                 episode_ticks=30)
     assert len(lat) > 500
     assert np.all(np.isfinite(lat)) and np.percentile(lat, 99) < 1.0
-    stats = [d[5] for d in s.completed]
-    assert sum(1 for st in stats if st & 1) == 0
+    assert len(s.last_status) == len(lat) and not np.any(s.last_status & 1)
 
 
 def test_c_poll_returns_each_result_once(cuda):
