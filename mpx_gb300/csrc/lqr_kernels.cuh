@@ -29,7 +29,7 @@ __global__ void lqr_riccati_kernel(mpxg_lq_io io, float* Pscr) {
   constexpr int NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP;
   __shared__ __align__(16) float sP[NP * LDP];
   __shared__ __align__(16) float sF[NZ * LDP];
-  __shared__ float sCol[NZ + 3];
+  __shared__ float sCT[NZ * 4];  // the pivot block's columns, row-major [NZ][BS]
   __shared__ float sx[NP + 3], su[NU + 3];
   const int b = blockIdx.x;
   const int j = threadIdx.x;
@@ -110,23 +110,61 @@ __global__ void lqr_riccati_kernel(mpxg_lq_io io, float* Pscr) {
       for (int k = 0; k < NP; ++k) a += sF[i * LDP + k] * tv[k];
       h[i] = a;
     }
-    // ---- Gauss-Jordan on the control pivots
-#pragma unroll 1
-    for (int p = NX; p < JA; ++p) {
-      __syncthreads();
-      if (j == p) {
+    // ---- Gauss-Jordan on the control pivots, BS at a time: the BS pivot
+    // columns are shared once, every thread factors the BS x BS pivot block
+    // (Cholesky) and eliminates it from its own column (two barriers per
+    // block instead of two per pivot)
+    constexpr int BS = (NU % 4 == 0) ? 4 : ((NU % 2 == 0) ? 2 : 1);
 #pragma unroll
-        for (int i = 0; i < NZ; ++i) sCol[i] = h[i];
+    for (int s0 = NX; s0 < JA; s0 += BS) {
+      __syncthreads();  // every thread is done with the previous block's columns
+      if (j >= s0 && j < s0 + BS) {
+#pragma unroll
+        for (int i = 0; i < NZ; ++i) sCT[i * BS + (j - s0)] = h[i];
       }
       __syncthreads();
-      float d = sCol[p];
-      if (!(d > 0.0f)) d = fmaxf(fabsf(d), 1e-20f);
-      float hp = 0.0f;
+      float Lc[BS][BS], il[BS];  // Cholesky factor; il = 1 / diagonal
 #pragma unroll
-      for (int i = NX; i < JA; ++i) hp = (i == p) ? h[i] : hp;
-      hp = hp / d;
+      for (int a = 0; a < BS; ++a) {
+        float dsum = sCT[(s0 + a) * BS + a];
 #pragma unroll
-      for (int i = 0; i < NZ; ++i) h[i] = (i == p) ? hp : h[i] - sCol[i] * hp;
+        for (int k = 0; k < a; ++k) dsum -= Lc[a][k] * Lc[a][k];
+        if (!(dsum > 0.0f)) dsum = fmaxf(fabsf(dsum), 1e-20f);
+        il[a] = rsqrtf(dsum);
+#pragma unroll
+        for (int c = a + 1; c < BS; ++c) {
+          float v = sCT[(s0 + c) * BS + a];
+#pragma unroll
+          for (int k = 0; k < a; ++k) v -= Lc[c][k] * Lc[a][k];
+          Lc[c][a] = v * il[a];
+        }
+      }
+      float y[BS];
+#pragma unroll
+      for (int a = 0; a < BS; ++a) {
+        float v = h[s0 + a];
+#pragma unroll
+        for (int k = 0; k < a; ++k) v -= Lc[a][k] * y[k];
+        y[a] = v * il[a];
+      }
+#pragma unroll
+      for (int a = BS - 1; a >= 0; --a) {
+        float v = y[a];
+#pragma unroll
+        for (int k = a + 1; k < BS; ++k) v -= Lc[k][a] * y[k];
+        y[a] = v * il[a];
+      }
+#pragma unroll
+      for (int i = 0; i < NZ; ++i) {
+        if (i >= s0 && i < s0 + BS) {
+          h[i] = y[i - s0];
+        } else {
+          float upd = 0.0f;
+#pragma unroll
+          for (int a = 0; a < BS; ++a) upd += sCT[i * BS + a] * y[a];
+          h[i] -= upd;
+        }
+      }
     }
     // ---- gains and new value function
     if (j < NX) {
