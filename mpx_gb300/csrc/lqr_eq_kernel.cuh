@@ -58,7 +58,9 @@ __device__ __forceinline__ void bmm(float* out, int ldo, const float* X, int ldx
 #pragma unroll
       for (int j = 0; j < TC; ++j) acc[i][j] += xa[i] * yb[j];
   }
-  __syncthreads();  // every read of X / Y is done before out is written
+  // out never aliases X or Y (and Add only element by element), so the
+  // results are written without a barrier; the one below orders them before
+  // their readers
 #pragma unroll
   for (int i = 0; i < TR; ++i)
 #pragma unroll
