@@ -217,6 +217,11 @@ typedef struct {
  * kept.  Errors go to XlaCustomCallStatusSetFailure when the host process
  * exports it, and to mpxg_last_error(NULL). */
 void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status);
+/* XLA custom-call target of the backward pass (mpxg_solve_vjp): buffers
+ * reference, parameter, w, x0, X, U, V (the solution), gX, gU (cotangents),
+ * then the results gx0 [B,n] and gref [B,N+1,12].  Same opaque and handle
+ * cache as mpxg_xla_solve. */
+void mpxg_xla_solve_vjp(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status);
 
 mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_factor, float step_freq, float dt,
                            float* leg_time, int* contact);

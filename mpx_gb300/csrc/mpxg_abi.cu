@@ -725,42 +725,45 @@ void xla_fail(void* status, const std::string& msg) {
 
 }  // namespace
 
-extern "C" void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status) {
-  if (!buffers || !opaque || opaque_len != sizeof(mpxg_xla_opaque)) {
-    xla_fail(status, "mpxg_xla_solve: opaque must be an mpxg_xla_opaque (" + std::to_string(sizeof(mpxg_xla_opaque)) +
-                         " bytes), got " + std::to_string(opaque_len));
-    return;
+// Handle of (device, opaque) for the XLA targets, created on first use.
+static mpxg_handle* xla_handle(const char* opaque, size_t opaque_len, void* status, mpxg_xla_opaque* op,
+                               const char* who) {
+  if (!opaque || opaque_len != sizeof(mpxg_xla_opaque)) {
+    xla_fail(status, std::string(who) + ": opaque must be an mpxg_xla_opaque (" +
+                         std::to_string(sizeof(mpxg_xla_opaque)) + " bytes), got " + std::to_string(opaque_len));
+    return nullptr;
   }
-  mpxg_xla_opaque op;
-  std::memcpy(&op, opaque, sizeof(op));
+  std::memcpy(op, opaque, sizeof(*op));
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
-    xla_fail(status, "mpxg_xla_solve: cudaGetDevice failed");
-    return;
+    xla_fail(status, std::string(who) + ": cudaGetDevice failed");
+    return nullptr;
   }
-  if (op.batch < 0 || op.batch > op.desc.batch_max) {
-    xla_fail(status, "mpxg_xla_solve: batch exceeds desc.batch_max");
-    return;
+  if (op->batch < 0 || op->batch > op->desc.batch_max) {
+    xla_fail(status, std::string(who) + ": batch exceeds desc.batch_max");
+    return nullptr;
   }
   std::string key(reinterpret_cast<const char*>(&dev), sizeof(dev));
-  key.append(reinterpret_cast<const char*>(&op.desc), sizeof(op.desc));
-  key.append(reinterpret_cast<const char*>(&op.opts), sizeof(op.opts));
+  key.append(reinterpret_cast<const char*>(&op->desc), sizeof(op->desc));
+  key.append(reinterpret_cast<const char*>(&op->opts), sizeof(op->opts));
+  std::lock_guard<std::mutex> lock(g_xla_mu);
+  auto it = g_xla_handles.find(key);
+  if (it != g_xla_handles.end()) return it->second;
   mpxg_handle* h = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_xla_mu);
-    auto it = g_xla_handles.find(key);
-    if (it != g_xla_handles.end()) {
-      h = it->second;
-    } else {
-      mpxg_status st = mpxg_create(&op.desc, &op.opts, &h);
-      if (st != MPXG_OK) {
-        xla_fail(status, std::string("mpxg_xla_solve: mpxg_create: ") + g_lib_err);
-        return;
-      }
-      g_xla_handles[key] = h;
-    }
+  if (mpxg_create(&op->desc, &op->opts, &h) != MPXG_OK) {
+    xla_fail(status, std::string(who) + ": mpxg_create: " + g_lib_err);
+    return nullptr;
   }
+  g_xla_handles[key] = h;
+  return h;
+}
+
+extern "C" void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status) {
+  mpxg_xla_opaque op;
+  if (!buffers) { xla_fail(status, "mpxg_xla_solve: null buffers"); return; }
+  mpxg_handle* h = xla_handle(opaque, opaque_len, status, &op, "mpxg_xla_solve");
+  if (!h) return;
   mpxg_batch_io io;
   std::memset(&io, 0, sizeof(io));
   io.batch = op.batch;
@@ -776,6 +779,30 @@ extern "C" void mpxg_xla_solve(void* stream, void** buffers, const char* opaque,
   io.V = (float*)buffers[9];
   std::lock_guard<std::mutex> lock(g_xla_mu);  // a handle is used by one host thread at a time
   if (mpxg_solve(h, stream, &io) != MPXG_OK) xla_fail(status, std::string("mpxg_xla_solve: ") + h->err);
+}
+
+extern "C" void mpxg_xla_solve_vjp(void* stream, void** buffers, const char* opaque, size_t opaque_len,
+                                   void* status) {
+  mpxg_xla_opaque op;
+  if (!buffers) { xla_fail(status, "mpxg_xla_solve_vjp: null buffers"); return; }
+  mpxg_handle* h = xla_handle(opaque, opaque_len, status, &op, "mpxg_xla_solve_vjp");
+  if (!h) return;
+  mpxg_vjp_io v;
+  std::memset(&v, 0, sizeof(v));
+  v.io.batch = op.batch;
+  v.io.reference = (const float*)buffers[0];
+  v.io.parameter = (const float*)buffers[1];
+  v.io.w = (const float*)buffers[2];
+  v.io.x0 = (const float*)buffers[3];
+  v.io.X_in = (const float*)buffers[4];
+  v.io.U_in = (const float*)buffers[5];
+  v.io.V_in = (const float*)buffers[6];
+  v.gX = (const float*)buffers[7];
+  v.gU = (const float*)buffers[8];
+  v.gx0 = (float*)buffers[9];
+  v.gref = (float*)buffers[10];
+  std::lock_guard<std::mutex> lock(g_xla_mu);
+  if (mpxg_solve_vjp(h, stream, &v) != MPXG_OK) xla_fail(status, std::string("mpxg_xla_solve_vjp: ") + h->err);
 }
 
 // ============================================================================

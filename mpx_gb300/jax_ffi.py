@@ -11,6 +11,7 @@ Registered only when `jax` imports; nothing here runs otherwise.  Usage:
 
 The call is batched natively ([B, ...] operands, one persistent launch), so
 it replaces the vmapped solve as a whole rather than being vmapped itself.
+It is differentiable (jax.custom_vjp over mpxg_xla_solve_vjp).
 W is reduced to its diagonal in the program (the SRBD weights are diagonal,
 mpx/config/config_srbd.py:90).  The custom call uses XLA's status-returning
 legacy signature (api_version 2); the target is registered for the CUDA
@@ -35,8 +36,10 @@ except ImportError:
     HAVE_JAX = False
 
 TARGET = "mpxg_xla_solve"
+TARGET_VJP = "mpxg_xla_solve_vjp"
 _registered = False
 _prim = None
+_prim_vjp = None
 
 
 def available():
@@ -57,6 +60,9 @@ def register():
     capsule_new.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
     capsule = capsule_new(fn, b"xla._CUSTOM_CALL_TARGET", None)
     jax.ffi.register_ffi_target(TARGET, capsule, platform="CUDA", api_version=0)
+    fn_vjp = ctypes.cast(L.mpxg_xla_solve_vjp, ctypes.c_void_p).value
+    jax.ffi.register_ffi_target(TARGET_VJP, capsule_new(fn_vjp, b"xla._CUSTOM_CALL_TARGET", None), platform="CUDA",
+                                api_version=0)
     _registered = True
 
 
@@ -91,17 +97,60 @@ def _primitive():
     return p
 
 
+def _primitive_vjp():
+    global _prim_vjp
+    if _prim_vjp is not None:
+        return _prim_vjp
+    p = Primitive("mpxg_mpc_vjp")
+    p.multiple_results = True
+
+    def abstract(reference, parameter, w, x0, X, U, V, gX, gU, *, opaque):
+        B, N1 = X.shape[0], X.shape[1]
+        return (jax.core.ShapedArray(x0.shape, jnp.float32), jax.core.ShapedArray((B, N1, 12), jnp.float32))
+
+    def lowering(ctx, *operands, opaque):
+        outs = [mlir.aval_to_ir_type(a) for a in ctx.avals_out]
+        call = mlir.custom_call(TARGET_VJP, result_types=outs, operands=list(operands), backend_config=opaque,
+                                api_version=2, has_side_effect=False)
+        return call.results
+
+    p.def_abstract_eval(abstract)
+    mlir.register_lowering(p, lowering, platform="cuda")
+    _prim_vjp = p
+    return p
+
+
 def make_mpc(desc, opts, n_max, batch):
     """A jit-compatible batched solve (reference, parameter, W, x0, X0, U0, V0)
-    -> (X, U, V) for `batch` instances of horizon n_max."""
+    -> (X, U, V) for `batch` instances of horizon n_max, differentiable with
+    jax.grad / jax.vjp: the backward pass is mpxg_xla_solve_vjp (implicit
+    differentiation of the converged solution), giving gradients with respect
+    to x0 and to the 12 tracked columns of the reference; the warm start,
+    parameter table and weights get zero gradients."""
     register()
     opaque = opaque_bytes(desc, opts, n_max, batch)
-    prim = _primitive()
+    prim, prim_vjp = _primitive(), _primitive_vjp()
+    f32 = lambda a: jnp.asarray(a, jnp.float32)
 
+    def diag(W):
+        return jnp.diagonal(f32(W), axis1=-2, axis2=-1) if jnp.ndim(W) == 3 else f32(W)
+
+    @jax.custom_vjp
     def solve(reference, parameter, W, x0, X0, U0, V0):
-        f32 = lambda a: jnp.asarray(a, jnp.float32)
-        w = jnp.diagonal(f32(W), axis1=-2, axis2=-1) if jnp.ndim(W) == 3 else f32(W)
-        return tuple(prim.bind(f32(reference), f32(parameter), w, f32(x0), f32(X0), f32(U0), f32(V0),
+        return tuple(prim.bind(f32(reference), f32(parameter), diag(W), f32(x0), f32(X0), f32(U0), f32(V0),
                                opaque=opaque))
 
+    def fwd(reference, parameter, W, x0, X0, U0, V0):
+        out = solve(reference, parameter, W, x0, X0, U0, V0)
+        return out, (f32(reference), f32(parameter), diag(W), f32(x0), out, W, X0, U0, V0)
+
+    def bwd(res, cot):
+        reference, parameter, w, x0, (X, U, V), W, X0, U0, V0 = res
+        gX, gU, _ = cot
+        gx0, gref = prim_vjp.bind(reference, parameter, w, x0, X, U, V, f32(gX), f32(gU), opaque=opaque)
+        g_reference = jnp.zeros_like(reference).at[..., :12].set(gref)
+        return (g_reference, jnp.zeros_like(parameter), jnp.zeros_like(f32(W)), gx0, jnp.zeros_like(f32(X0)),
+                jnp.zeros_like(f32(U0)), jnp.zeros_like(f32(V0)))
+
+    solve.defvjp(fwd, bwd)
     return solve

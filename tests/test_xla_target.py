@@ -46,3 +46,33 @@ def test_xla_target_matches_mpxg_solve(cuda):
     for got, key in zip(outs, ("X", "U", "V")):
         assert np.array_equal(got.cpu().numpy(), ref[key].cpu().numpy()), key
     s.close()
+
+
+@pytest.mark.gpu
+def test_xla_vjp_target_matches_solver_vjp(cuda):
+    import torch
+    from mpx_gb300.solver import Solver, weights_diagonal
+    wl = P.quadruped_workload(5, horizons=(20,), seed=6, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
+                              random_phase=True)
+    opts = P.SolverOptions(sqp_iters=6)
+    s = Solver(wl.desc, opts, n_max=20, batch_max=5)
+    sol = s.solve(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W)
+    torch.cuda.synchronize()
+    X, U, V = sol["X"].clone(), sol["U"].clone(), sol["V"].clone()
+    rng = np.random.default_rng(2)
+    gX = torch.tensor(rng.normal(size=X.shape), dtype=torch.float32, device="cuda")
+    gU = torch.tensor(rng.normal(size=U.shape), dtype=torch.float32, device="cuda")
+    ref = s.vjp(wl.x0, X, U, V, wl.reference, wl.parameter, wl.W, gX, gU)
+    torch.cuda.synchronize()
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to("cuda", torch.float32).contiguous()
+    ins = [d(wl.reference), d(wl.parameter), weights_diagonal(torch.as_tensor(wl.W), 5).to("cuda", torch.float32)
+           .contiguous(), d(wl.x0), X, U, V, gX, gU]
+    gx0 = torch.empty(5, 12, device="cuda")
+    gref = torch.empty(5, 21, 12, device="cuda")
+    bufs = (ctypes.c_void_p * 11)(*[t.data_ptr() for t in ins + [gx0, gref]])
+    op = jax_ffi.opaque_bytes(wl.desc, opts, 20, 5)
+    _lib.load().mpxg_xla_solve_vjp(None, bufs, op, len(op), None)
+    torch.cuda.synchronize()
+    assert np.array_equal(gx0.cpu().numpy(), ref["gx0"].cpu().numpy())
+    assert np.array_equal(gref.cpu().numpy(), ref["gref"].cpu().numpy())
+    s.close()
