@@ -954,8 +954,11 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
 #endif
 template <class M>
 struct SqpMinBlocks { static constexpr int value = MPXG_SQP_MIN_BLOCKS; };
+#ifndef MPXG_SQP_TPUT_BLOCKS
+#define MPXG_SQP_TPUT_BLOCKS 4
+#endif
 template <>
-struct SqpMinBlocks<ModelRpy12> { static constexpr int value = 4; };
+struct SqpMinBlocks<ModelRpy12> { static constexpr int value = MPXG_SQP_TPUT_BLOCKS; };
 
 template <class M, bool VJP = false>
 __device__ __forceinline__ void sqp_body(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp) {
