@@ -92,7 +92,10 @@ typedef struct {
 typedef struct {
   int sqp_iters;       /* SQP iterations per solve */
   int ls_max_trials;   /* merit line-search trials */
-  float ls_beta, ls_eta, reg, rho0, ls_skip_tol;
+  float ls_beta, ls_eta, reg, rho0;
+  float ls_skip_tol;   /* a predicted merit decrease below ls_skip_tol * (1 + |merit|)
+                          takes the full step unsearched (1e-7 recommended: larger
+                          values let Gauss-Newton steps cycle near convergence) */
   int compute_kkt;     /* 1: evaluate the KKT residual of the result */
   int warps_per_block; /* 0: default (4); at most 4 */
   int blocks_per_sm;   /* 0: default (tuned) */
@@ -312,9 +315,10 @@ mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io);
  * over only input and output buffers): no handle, same inputs and outputs as
  * mpxg_solve, scratch taken from a 64 MiB static device array that every GPU
  * loading this library holds until exit.  The array must hold one warp's
- * scratch per SM, else the call is rejected (MPXG_ERR_INVALID_ARG; for the
- * 12-state models n_max up to ~150 on a 152-SM GB300).  All calls share that array: calls that overlap on the GPU race,
- * so serialise them on one stream.  The first call on a device looks up the
+ * scratch per SM, else the call is rejected (MPXG_ERR_INVALID_ARG; on a
+ * 152-SM GB300 n_max up to 141 for the roll-pitch-yaw quadruped, 135 for the
+ * biped, 116 for the quaternion model).  All calls share that array: calls
+ * that overlap on the GPU race, so serialise them on one stream.  The first call on a device looks up the
  * array's device address; make it before any stream capture.  Errors are
  * reported through mpxg_last_error(NULL). */
 mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* desc, const mpxg_solver_opts* opts, void* stream,

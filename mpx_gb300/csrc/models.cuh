@@ -52,6 +52,28 @@ __device__ __forceinline__ void rigid_body_step(const ModelConst& mc, const S* p
   for (int i = 0; i < 3; ++i) pn[i] = p[i] + vn[i] * dt;
 }
 
+// The same step as increments (dp, dv, dw) = (p+ - p, v+ - v, w+ - w), never
+// adding the state itself, so that increments at two nearby points differ
+// by their true difference rather than by the rounding of the state.
+template <class S>
+__device__ __forceinline__ void rigid_body_incr(const ModelConst& mc, const S* v, const S* w, const S* R, const S* F,
+                                                const S* Mw, S* dp, S* dv, S* dw) {
+  const float dt = mc.dt;
+  dv[0] = (F[0] * mc.inv_mass) * dt;
+  dv[1] = (F[1] * mc.inv_mass) * dt;
+  dv[2] = (F[2] * mc.inv_mass - mc.gravity) * dt;
+  S Iw[3], gy[3], tb[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Iw[i] = w[0] * mc.I[3 * i] + w[1] * mc.I[3 * i + 1] + w[2] * mc.I[3 * i + 2];
+  cross3(w, Iw, gy);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) tb[i] = R[i] * Mw[0] + R[3 + i] * Mw[1] + R[6 + i] * Mw[2] - gy[i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dw[i] = (tb[0] * mc.Iinv[3 * i] + tb[1] * mc.Iinv[3 * i + 1] + tb[2] * mc.Iinv[3 * i + 2]) * dt;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dp[i] = (v[i] + dv[i]) * dt;
+}
+
 // Net force and moment about the CoM of point forces (quadruped legs).
 template <class S, int LEGS>
 __device__ __forceinline__ void point_wrench(const S* p, const S* u, const float* par, S* F, S* Mw) {
@@ -238,6 +260,19 @@ struct ModelQuat13 {
     rigid_body_step(mc, x, x + 7, x + 10, R, F, Mw, xn, xn + 7, xn + 10);
     quat_integrate(x + 3, xn + 10, mc.dt, xn + 3);
   }
+  // f(x, u) - x; the quaternion rows are the plain difference of the step
+  template <class S>
+  __device__ static void increment(const ModelConst& mc, const S* x, const S* u, const float* par, S* d) {
+    S F[3], Mw[3], R[9], wn[3], qn[4];
+    point_wrench<S, 4>(x, u, par, F, Mw);
+    quat_to_mat(x + 3, R);
+    rigid_body_incr(mc, x + 7, x + 10, R, F, Mw, d, d + 7, d + 10);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) wn[k] = x[10 + k] + d[10 + k];
+    quat_integrate(x + 3, wn, mc.dt, qn);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) d[3 + k] = qn[k] - x[3 + k];
+  }
   // tracking residual of the state (objectives.py:41-61), 12 entries
   template <class S>
   __device__ static void state_residual(const S* x, const float* ref, S* r) {
@@ -264,12 +299,42 @@ struct ModelRpy12 {
 #pragma unroll
     for (int k = 0; k < 3; ++k) xn[3 + k] = x[3 + k] + rd[k] * mc.dt;
   }
+  // f(x, u) - x
+  template <class S>
+  __device__ static void increment(const ModelConst& mc, const S* x, const S* u, const float* par, S* d) {
+    S F[3], Mw[3], R[9], wn[3], rd[3];
+    point_wrench<S, 4>(x, u, par, F, Mw);
+    rpy_to_mat(x + 3, R);
+    rigid_body_incr(mc, x + 6, x + 9, R, F, Mw, d, d + 6, d + 9);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) wn[k] = x[9 + k] + d[9 + k];
+    rpy_rates(x + 3, wn, rd);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[3 + k] = rd[k] * mc.dt;
+  }
   template <class S>
   __device__ static void state_residual(const S* x, const float* ref, S* r) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) r[k] = x[k] - ref[k];
   }
 };
+
+// Net force and moment about the CoM of the biped's two foot wrenches.
+template <class S>
+__device__ __forceinline__ void biped_wrench(const S* x, const S* u, const float* par, S* F, S* Mw) {
+  F[0] = F[1] = F[2] = s_const<S>(0.0f);
+  Mw[0] = Mw[1] = Mw[2] = s_const<S>(0.0f);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float c = par[i];
+    S r[3] = {par[2 + 3 * i] - x[0], par[3 + 3 * i] - x[1], par[4 + 3 * i] - x[2]};
+    S f[3] = {u[6 * i] * c, u[6 * i + 1] * c, u[6 * i + 2] * c};
+    S t[3];
+    cross3(r, f, t);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { F[k] = F[k] + f[k]; Mw[k] = Mw[k] + t[k] + u[6 * i + 3 + k] * c; }
+  }
+}
 
 struct ModelBiped12 {
   static constexpr int NX = 12, NU = 12, NREF = 14, NPAR = 8, LEGS = 2, COFF = 12;
@@ -279,23 +344,25 @@ struct ModelBiped12 {
   template <class S>
   __device__ static void dynamics(const ModelConst& mc, const S* x, const S* u, const float* par, S* xn) {
     S F[3], Mw[3], R[9], rd[3];
-    F[0] = F[1] = F[2] = s_const<S>(0.0f);
-    Mw[0] = Mw[1] = Mw[2] = s_const<S>(0.0f);
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const float c = par[i];
-      S r[3] = {par[2 + 3 * i] - x[0], par[3 + 3 * i] - x[1], par[4 + 3 * i] - x[2]};
-      S f[3] = {u[6 * i] * c, u[6 * i + 1] * c, u[6 * i + 2] * c};
-      S t[3];
-      cross3(r, f, t);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) { F[k] = F[k] + f[k]; Mw[k] = Mw[k] + t[k] + u[6 * i + 3 + k] * c; }
-    }
+    biped_wrench(x, u, par, F, Mw);
     rpy_to_mat(x + 3, R);
     rigid_body_step(mc, x, x + 6, x + 9, R, F, Mw, xn, xn + 6, xn + 9);
     rpy_rates(x + 3, xn + 9, rd);
 #pragma unroll
     for (int k = 0; k < 3; ++k) xn[3 + k] = x[3 + k] + rd[k] * mc.dt;
+  }
+  // f(x, u) - x
+  template <class S>
+  __device__ static void increment(const ModelConst& mc, const S* x, const S* u, const float* par, S* d) {
+    S F[3], Mw[3], R[9], wn[3], rd[3];
+    biped_wrench(x, u, par, F, Mw);
+    rpy_to_mat(x + 3, R);
+    rigid_body_incr(mc, x + 6, x + 9, R, F, Mw, d, d + 6, d + 9);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) wn[k] = x[9 + k] + d[9 + k];
+    rpy_rates(x + 3, wn, rd);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[3 + k] = rd[k] * mc.dt;
   }
   template <class S>
   __device__ static void state_residual(const S* x, const float* ref, S* r) {
@@ -488,6 +555,125 @@ __device__ __forceinline__ float stage_cost(const ModelConst& mc, const float* x
 #pragma unroll
   for (int a = 0; a < M::NU; ++a) acc += w[12 + a] * u[a] * u[a];
   return 0.5f * acc + barrier_cost<M>(mc, u, ref);
+}
+
+// ------------------------------------------------------------ cost differences
+// The merit line search compares phi(alpha) with phi(0).  Near convergence the
+// decrease is far below float32's resolution of phi itself, so the search
+// sums per-stage differences written without cancellation instead of
+// differencing two float32 merits.  In exact arithmetic each function below
+// equals the plain difference of the corresponding cost term.
+
+// Quadratic branch of the barriers: q(c) = a/2 (r^2 - 1), r = (c - 2 sigma)/sigma,
+// for c <= sigma, and 0 above (q is continuous at sigma, where r = -1).
+__device__ __forceinline__ float barrier_q(float a, float sg, float c) {
+  return (c > sg) ? 0.0f : 0.5f * a * ((c - 3.0f * sg) / sg) * ((c - sg) / sg);
+}
+__device__ __forceinline__ float barrier_q_diff(float a, float sg, float c0, float c1, float dc) {
+  if (c0 <= sg && c1 <= sg) return 0.5f * a * (dc / sg) * ((c0 + c1 - 4.0f * sg) / sg);
+  return barrier_q(a, sg, c1) - barrier_q(a, sg, c0);
+}
+
+// 1/2 mask [B(c0 + dc) - B(c0)] of one constraint term (barrier_terms' value).
+__device__ __forceinline__ float barrier_diff(const ModelConst& mc, float c0, float dc, float mask) {
+  if (mask == 0.0f) return 0.0f;
+  const float a = mc.alpha, sg = mc.sigma;
+  const float c1 = c0 + dc;
+  if (mc.barrier_kind == 1) {
+    // B = -a log c above sigma, q(c) - a log sigma at or below it
+    float d;
+    if (c0 > sg && c1 > sg) d = -a * log1pf(dc / c0);
+    else if (c0 <= sg && c1 <= sg) d = barrier_q_diff(a, sg, c0, c1, dc);
+    else if (c0 > sg) d = barrier_q(a, sg, c1) + a * log1pf((c0 - sg) / sg);
+    else d = -a * log1pf((c1 - sg) / sg) - barrier_q(a, sg, c0);
+    return 0.5f * mask * d;
+  }
+  // kind 0: B = clip(clip(q(c) - a log c, 0, 1e8), 1e-6, 1e6); the closed
+  // form holds while no clip is active at either end
+  const BarrierEval b0 = barrier_eval(mc, c0), b1 = barrier_eval(mc, c1);
+  const bool open = c0 > 1e-10f && c1 > 1e-10f && c0 < 1e6f && c1 < 1e6f && b0.val > 1e-6f && b0.val < 1e6f &&
+                    b1.val > 1e-6f && b1.val < 1e6f;
+  if (!open) return 0.5f * mask * (fminf(fmaxf(b1.val, 1e-6f), 1e6f) - fminf(fmaxf(b0.val, 1e-6f), 1e6f));
+  return 0.5f * mask * (barrier_q_diff(a, sg, c0, c1, dc) - a * log1pf(dc / c0));
+}
+
+// Friction cone c = mu fz - s, s = sqrt(fx^2 + fy^2 + 1e-2): value at f and
+// its change for the step df, with ds = d(s^2) / (s0 + s1).
+__device__ __forceinline__ float cone_diff(float mu, const float* f, const float* df, float* dc) {
+  const float s0 = sqrtf(f[0] * f[0] + f[1] * f[1] + 1e-2f);
+  const float g0 = f[0] + df[0], g1 = f[1] + df[1];
+  const float s1 = sqrtf(g0 * g0 + g1 * g1 + 1e-2f);
+  const float ds = (df[0] * (2.0f * f[0] + df[0]) + df[1] * (2.0f * f[1] + df[1])) / (s0 + s1);
+  *dc = mu * df[2] - ds;
+  return mu * f[2] - s0;
+}
+
+// Change of barrier_cost<M> for the control step du.
+template <class M>
+__device__ __forceinline__ float barrier_cost_diff(const ModelConst& mc, const float* u, const float* du,
+                                                   const float* ref) {
+  float acc = 0.0f;
+  if (M::LEGS == 4) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float mcost = mc.barrier_masked ? ref[M::COFF + i] : 1.0f;
+      float dc;
+      const float c0 = cone_diff(mc.mu, u + 3 * i, du + 3 * i, &dc);
+      acc += barrier_diff(mc, c0, dc, mcost);
+    }
+  } else {
+    const float hl = 0.5f * mc.foot_length, hw = 0.5f * mc.foot_width;
+    const float mz = mc.mu * 0.5f * fminf(mc.foot_length, mc.foot_width);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const float mcost = mc.barrier_masked ? ref[M::COFF + i] : 1.0f;
+      const float* F = u + 6 * i;
+      const float* T = u + 6 * i + 3;
+      const float* dF = du + 6 * i;
+      const float* dT = du + 6 * i + 3;
+      float dc;
+      const float c0 = cone_diff(mc.mu, F, dF, &dc);
+      acc += barrier_diff(mc, c0, dc, mcost);
+      acc += barrier_diff(mc, hl * F[2] - T[1], hl * dF[2] - dT[1], mcost);
+      acc += barrier_diff(mc, hl * F[2] + T[1], hl * dF[2] + dT[1], mcost);
+      acc += barrier_diff(mc, hw * F[2] - T[0], hw * dF[2] - dT[0], mcost);
+      acc += barrier_diff(mc, hw * F[2] + T[0], hw * dF[2] + dT[0], mcost);
+      acc += barrier_diff(mc, mz * F[2] - T[2], mz * dF[2] - dT[2], mcost);
+      acc += barrier_diff(mc, mz * F[2] + T[2], mz * dF[2] + dT[2], mcost);
+    }
+  }
+  return acc;
+}
+
+// stage_cost<M>(x + dx, u + du) - stage_cost<M>(x, u).  Tracking and effort
+// terms as 1/2 w d (2 r + d); the quaternion rows of the attitude residual
+// (nonlinear in x) as (r1 - r0)(r1 + r0) of the two residuals.
+template <class M>
+__device__ __forceinline__ float stage_cost_diff(const ModelConst& mc, const float* x, const float* dx, const float* u,
+                                                 const float* du, const float* ref, const float* w, bool terminal) {
+  float acc = 0.0f;
+  if (M::IDENT_RES) {
+#pragma unroll
+    for (int a = 0; a < 12; ++a) acc += w[a] * dx[a] * (2.0f * (x[a] - ref[a]) + dx[a]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < M::NX; ++j) {
+      if (j >= M::QOFF && j < M::QOFF + 4) continue;
+      const int a = M::wrow(j);
+      acc += w[a] * dx[j] * (2.0f * (x[j] - ref[j]) + dx[j]);
+    }
+    float q1[4], r0[3], r1[3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q1[k] = x[M::QOFF + k] + dx[M::QOFF + k];
+    quat_sub(x + M::QOFF, ref + M::QOFF, r0);
+    quat_sub(q1, ref + M::QOFF, r1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc += w[M::QOFF + k] * (r1[k] - r0[k]) * (r1[k] + r0[k]);
+  }
+  if (terminal) return 0.5f * acc;
+#pragma unroll
+  for (int a = 0; a < M::NU; ++a) acc += w[12 + a] * du[a] * (2.0f * u[a] + du[a]);
+  return 0.5f * acc + barrier_cost_diff<M>(mc, u, du, ref);
 }
 
 }  // namespace mpxg

@@ -572,8 +572,9 @@ mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io) {
 //    library, held until the process exits;
 //  - one warp needs scratch_floats(n_max) floats; the array must hold at
 //    least one warp per SM, otherwise the call is rejected with
-//    MPXG_ERR_INVALID_ARG (for the 12-state models that is n_max <= ~150 on a
-//    152-SM GB300); the persistent grid is shrunk to the warps that fit;
+//    MPXG_ERR_INVALID_ARG (on a 152-SM GB300: n_max <= 141 for the
+//    roll-pitch-yaw quadruped, 135 for the biped, 116 for the quaternion
+//    model); the persistent grid is shrunk to the warps that fit;
 //  - all calls share the array (and the work counter, which each call clears
 //    on its stream first), so two calls that overlap on the GPU race: issue
 //    them on one stream or order them with events;

@@ -216,6 +216,7 @@ __host__ __device__ inline long long scratch_floats(int n_max) {
   f += (long long)(n_max + 1) * D::GS;             // cost data
   f += (long long)n_max * D::NP * M::NU;           // [K | k] column-major
   f += (long long)(n_max + 1) * D::NP * D::LDP;    // value functions
+  f += (long long)n_max * D::FS;                   // dynamics increments f - x at the iterate
   f += (long long)(n_max + 1) * D::NX * 2;         // dX, lam
   f += (long long)n_max * M::NU;                   // dU
   return (f + 31) / 32 * 32;
@@ -224,13 +225,14 @@ __host__ __device__ inline long long scratch_floats(int n_max) {
 template <class M>
 struct Scratch {
   typedef Dims<M> D;
-  float *F, *G, *K, *P, *dX, *L, *dU;
+  float *F, *G, *K, *P, *D0, *dX, *L, *dU;
   __device__ Scratch(float* base, int n_max) {
     F = base;
     G = F + (size_t)n_max * D::NZ * D::FS;
     K = G + (size_t)(n_max + 1) * D::GS;
     P = K + (size_t)n_max * D::NP * M::NU;
-    dX = P + (size_t)(n_max + 1) * D::NP * D::LDP;
+    D0 = P + (size_t)(n_max + 1) * D::NP * D::LDP;
+    dX = D0 + (size_t)n_max * D::FS;
     L = dX + (size_t)(n_max + 1) * D::NX;
     dU = L + (size_t)(n_max + 1) * D::NX;
   }
@@ -359,7 +361,8 @@ __device__ __forceinline__ void lin_stage(const ModelConst& mc, int t, int N, co
     }
   }
   if (term) return;
-  // ---- dynamics: defect and Jacobian columns, TK directions per pass
+  // ---- dynamics in increment form f = x + d(x, u): defect, Jacobian columns
+  // (identity + dd/dz) and, for the merit line search, d itself
   const float* pp = par + t * M::NPAR;
   float* Ft = s.F + (size_t)t * D::NZ * FS;
 #pragma unroll 1
@@ -377,13 +380,18 @@ __device__ __forceinline__ void lin_stage(const ModelConst& mc, int t, int N, co
 #pragma unroll
       for (int k = 0; k < TK; ++k) ud[a].d[k] = (NX + a == p0 + k) ? 1.0f : 0.0f;
     }
-    M::template dynamics<DK<TK>>(mc, xd, ud, pp, fd);
+    M::template increment<DK<TK>>(mc, xd, ud, pp, fd);
     if (!KKT) {
       if (p0 == 0) {
-        float cv[FS];
+        float cv[FS], dv[FS];
 #pragma unroll
-        for (int i = 0; i < FS; ++i) cv[i] = (i < NX) ? fd[i < NX ? i : 0].v - xn[i < NX ? i : 0] : 0.0f;
+        for (int i = 0; i < FS; ++i) {
+          const int ii = i < NX ? i : 0;
+          cv[i] = (i < NX) ? (x[ii] + fd[ii].v) - xn[ii] : 0.0f;
+          dv[i] = (i < NX) ? fd[ii].v : 0.0f;
+        }
         st_vec<FS>(Ft + JA * FS, cv);
+        st_vec<FS>(s.D0 + (size_t)t * FS, dv);
       }
 #pragma unroll
       for (int k = 0; k < TK; ++k) {
@@ -391,14 +399,14 @@ __device__ __forceinline__ void lin_stage(const ModelConst& mc, int t, int N, co
         if (dir < NX + NU) {
           float cv[FS];
 #pragma unroll
-          for (int i = 0; i < FS; ++i) cv[i] = (i < NX) ? fd[i < NX ? i : 0].d[k] : 0.0f;
+          for (int i = 0; i < FS; ++i) cv[i] = (i < NX) ? fd[i < NX ? i : 0].d[k] + (i == dir ? 1.0f : 0.0f) : 0.0f;
           st_vec<FS>(Ft + dir * FS, cv);
         }
       }
     } else {
       if (p0 == 0) {
 #pragma unroll
-        for (int i = 0; i < NX; ++i) *rp = fmaxf(*rp, fabsf(fd[i].v - xn[i]));
+        for (int i = 0; i < NX; ++i) *rp = fmaxf(*rp, fabsf((x[i] + fd[i].v) - xn[i]));
       }
 #pragma unroll
       for (int k = 0; k < TK; ++k) {
@@ -406,7 +414,7 @@ __device__ __forceinline__ void lin_stage(const ModelConst& mc, int t, int N, co
         if (dir < NX + NU) {
           float acc = 0.0f, gd = 0.0f, vt = 0.0f;
 #pragma unroll
-          for (int i = 0; i < NX; ++i) acc += fd[i].d[k] * vn[i];
+          for (int i = 0; i < NX; ++i) acc += (fd[i].d[k] + (i == dir ? 1.0f : 0.0f)) * vn[i];
 #pragma unroll
           for (int i = 0; i < NX + NU; ++i) gd = (i == dir) ? g[i] : gd;
           if (dir < NX) vt = V[t * NX + dir];
@@ -419,47 +427,62 @@ __device__ __forceinline__ void lin_stage(const ModelConst& mc, int t, int N, co
 }
 
 // ----------------------------------------------------------------- merit
-// l_t + V~_t . c~_t + rho/2 |c~_t|^2 at step alpha, constraint index t (0..N).
+// Stage t's share of phi(alpha) - phi(0), the merit change along the step
+// (dX, dU, L - V) scaled by alpha, written without cancellation: cost terms by
+// stage_cost_diff, and the defect change from the dynamics increments,
+//   dc_t = alpha dx_{t-1} + [d(x_{t-1} + alpha dx_{t-1}, .) - d(x_{t-1}, .)] - alpha dx_t,
+// d = f - x, so that
+//   d(V.c) = dV.(c0 + dc) + V.dc,  d(|c|^2 / 2) = dc.(2 c0 + dc) / 2.
 template <class M>
-__device__ __forceinline__ float merit_stage(const ModelConst& mc, int t, int N, float alpha, float rho,
-                                             const float* x0, const float* X, const float* U, const float* V,
-                                             const Scratch<M>& s, const float* ref, const float* par,
-                                             const float* w) {
+__device__ __forceinline__ float merit_diff_stage(const ModelConst& mc, int t, int N, float alpha, float rho,
+                                                  const float* x0, const float* X, const float* U, const float* V,
+                                                  const Scratch<M>& s, const float* ref, const float* par,
+                                                  const float* w) {
   constexpr int NX = M::NX, NU = M::NU;
-  float xt[NX], ut[NU], ct[NX];
+  float xt[NX], dxt[NX], c0[NX], dc[NX];
 #pragma unroll
-  for (int i = 0; i < NX; ++i) xt[i] = X[t * NX + i] + alpha * s.dX[t * NX + i];
-  float l;
-  if (t < N) {
+  for (int i = 0; i < NX; ++i) { xt[i] = X[t * NX + i]; dxt[i] = alpha * s.dX[t * NX + i]; }
+  float dl;
+  {
+    float ut[NU], dut[NU];
 #pragma unroll
-    for (int a = 0; a < NU; ++a) ut[a] = U[t * NU + a] + alpha * s.dU[t * NU + a];
-    l = stage_cost<M>(mc, xt, ut, ref + t * M::NREF, w, false);
-  } else {
-#pragma unroll
-    for (int a = 0; a < NU; ++a) ut[a] = 0.0f;
-    l = stage_cost<M>(mc, xt, ut, ref + t * M::NREF, w, true);
+    for (int a = 0; a < NU; ++a) {
+      ut[a] = (t < N) ? U[t * NU + a] : 0.0f;
+      dut[a] = (t < N) ? alpha * s.dU[t * NU + a] : 0.0f;
+    }
+    dl = stage_cost_diff<M>(mc, xt, dxt, ut, dut, ref + t * M::NREF, w, t == N);
   }
   if (t == 0) {
 #pragma unroll
-    for (int i = 0; i < NX; ++i) ct[i] = x0[i] - xt[i];
+    for (int i = 0; i < NX; ++i) { c0[i] = x0[i] - xt[i]; dc[i] = -dxt[i]; }
   } else {
-    float xp[NX], up[NU], fx[NX];
+    float xp[NX], up[NU], d0[NX], d1[NX];
 #pragma unroll
-    for (int i = 0; i < NX; ++i) xp[i] = X[(t - 1) * NX + i] + alpha * s.dX[(t - 1) * NX + i];
+    for (int i = 0; i < NX; ++i) xp[i] = X[(t - 1) * NX + i];
 #pragma unroll
-    for (int a = 0; a < NU; ++a) up[a] = U[(t - 1) * NU + a] + alpha * s.dU[(t - 1) * NU + a];
-    M::template dynamics<float>(mc, xp, up, par + (t - 1) * M::NPAR, fx);
+    for (int a = 0; a < NU; ++a) up[a] = U[(t - 1) * NU + a];
+    const float* pt = par + (t - 1) * M::NPAR;
+    ld_vec<NX>(s.D0 + (size_t)(t - 1) * Dims<M>::FS, d0);  // d(x, u) of phase 1
 #pragma unroll
-    for (int i = 0; i < NX; ++i) ct[i] = fx[i] - xt[i];
+    for (int i = 0; i < NX; ++i) {
+      c0[i] = (xp[i] + d0[i]) - xt[i];
+      dc[i] = alpha * s.dX[(t - 1) * NX + i] - dxt[i];
+      xp[i] += alpha * s.dX[(t - 1) * NX + i];
+    }
+#pragma unroll
+    for (int a = 0; a < NU; ++a) up[a] += alpha * s.dU[(t - 1) * NU + a];
+    M::template increment<float>(mc, xp, up, pt, d1);
+#pragma unroll
+    for (int i = 0; i < NX; ++i) dc[i] += d1[i] - d0[i];
   }
-  float vc = 0.0f, cs = 0.0f;
+  float acc = 0.0f;
 #pragma unroll
   for (int i = 0; i < NX; ++i) {
-    const float vt = V[t * NX + i] + alpha * (s.L[t * NX + i] - V[t * NX + i]);
-    vc += vt * ct[i];
-    cs += ct[i] * ct[i];
+    const float vt = V[t * NX + i];
+    const float dv = alpha * (s.L[t * NX + i] - vt);
+    acc += dv * (c0[i] + dc[i]) + vt * dc[i] + 0.5f * rho * dc[i] * (2.0f * c0[i] + dc[i]);
   }
-  return l + vc + 0.5f * rho * cs;
+  return dl + acc;
 }
 
 // ----------------------------------------------------------------- block Gauss-Jordan
@@ -875,9 +898,9 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
       for (int tr = 0; tr < sp.ls_max_trials; ++tr) {
         double acc = 0.0;
         for (int t = lane; t <= N; t += 32)
-          acc += (double)merit_stage<M>(mc, t, N, alpha, rho, x0, X, U, V, s, ref, par, sm.w);
-        const double phi = warp_sum(acc);
-        if (phi <= phi0 + (double)sp.ls_eta * alpha * dphi) { accepted = true; break; }
+          acc += (double)merit_diff_stage<M>(mc, t, N, alpha, rho, x0, X, U, V, s, ref, par, sm.w);
+        const double dphi_alpha = warp_sum(acc);  // phi(alpha) - phi(0)
+        if (dphi_alpha <= (double)sp.ls_eta * alpha * dphi) { accepted = true; break; }
         if (tr + 1 < sp.ls_max_trials) alpha *= sp.ls_beta;
       }
     }

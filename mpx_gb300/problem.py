@@ -86,7 +86,7 @@ class SolverOptions:
     ls_eta: float = 1e-4        # Armijo constant
     reg: float = 1e-6           # added to the diagonal of Q_uu
     rho0: float = 1.0           # initial augmented-Lagrangian penalty
-    ls_skip_tol: float = 1e-6   # |predicted merit change| below this x (1+|merit|): take the full step
+    ls_skip_tol: float = 1e-7   # |predicted merit change| below this x (1+|merit|): take the full step
     compute_kkt: bool = True    # evaluate the KKT residual of the result on the device
 
 
