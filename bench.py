@@ -63,7 +63,8 @@ def parse():
     ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq"],
                     help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve; lqr_eq: the "
                          "equality-constrained n=72 LQ solve")
-    ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1],
+                    help="lqr: 0 sequential Riccati, 1 associative scan; lqr_eq: 0 tensor cores, 1 CUDA cores")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small run for ncu (no clocks, no CPU, no plain)")
@@ -632,7 +633,8 @@ def run_lqr(args, rank, world, local_rank):
 
 def run_lqr_eq(args, rank, world, local_rank):
     """--workload lqr_eq: 512 equality-constrained LQ problems, n=72, m=30,
-    12 equality rows per stage, N=100 (mpxg_lqr_eq_solve)."""
+    12 equality rows per stage, N=100 (mpxg_lqr_eq_solve_method; --lqr-method
+    0: stage products on the tensor cores, 1: on the CUDA cores)."""
     import torch
     from mpx_gb300 import _lib
     from mpx_gb300 import problem as P
@@ -661,8 +663,10 @@ def run_lqr_eq(args, rank, world, local_rank):
     stream = torch.cuda.Stream(device=dev)
     hs = _stream_handle(stream)
 
+    method = int(args.lqr_method)
+
     def solve():
-        _lib.check(L.mpxg_lqr_eq_solve(hs, ctypes.byref(io)), None, "mpxg_lqr_eq_solve")
+        _lib.check(L.mpxg_lqr_eq_solve_method(hs, ctypes.byref(io), method), None, "mpxg_lqr_eq_solve")
 
     with torch.cuda.stream(stream):
         for _ in range(max(args.warmup, 3)):
@@ -702,13 +706,25 @@ def run_lqr_eq(args, rank, world, local_rank):
                                "<= 1.01), B ~ N(0,0.1/m), Q diagonal log-uniform [1e-2,1e2], R = 1e-3 I, 12 rows "
                                "[C D] ~ N(0,1) per stage", "parallelism": "replicas"},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                     "traffic": None, "algorithmic_bytes": in_bytes + out_bytes, "kernel": "lqr_eq_kernel<72,30,12>"},
+                     "traffic": None, "algorithmic_bytes": in_bytes + out_bytes,
+                     "kernel": ["lqr_eq_tc_kernel<72,30,12>", "lqr_eq_kernel<72,30,12>"][method]},
         "fp32": {"achieved_tflops": flops / avg_s / 1e12, "nominal_peak_tflops": fp32_nominal,
                  "frac": flops / avg_s / 1e12 / fp32_nominal,
                  "flops": "F_LQR(72,30) + Schur-complement elimination per stage = %d" % f_eq},
+        "method": ["tensor cores (tcgen05 split-TF32 stage products)", "CUDA cores (float32)"][method],
         "gpu_launches": args.steps,
         "clocks": clk,
     }
+    if method == 0:
+        # MMA work issued per stage: alpha and beta 128 x 112 x 72, gamma
+        # 128 x 80 x 48 (tiles padded to M = 128), three TF32 MMAs per product
+        mma = 3 * 2 * (2 * 128 * 112 * 72 + 128 * 80 * 48)
+        tf32_peak = float(peaks.get("bf16_tflops", 1900.0)) / 2.0
+        ach = B * N * mma / avg_s / 1e12
+        line["tensor"] = {"achieved_tflops": ach, "peak_tflops": tf32_peak, "frac": ach / tf32_peak,
+                          "peak_source": "TF32 = half the measured bf16 dense rate (MEASURED_PEAKS.json bf16_tflops)",
+                          "flops": "TF32 MMA work issued per stage (padded tiles, 3 MMAs per split product) = %d"
+                                   % mma}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -308,6 +308,13 @@ typedef struct {
 } mpxg_lq_eq_io;
 size_t mpxg_lqr_eq_workspace_bytes(int batch, int N, int n);
 mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io);
+/* The same solve with the stage products' engine chosen: method 0 (what
+ * mpxg_lqr_eq_solve runs) puts the Riccati stage's dense products on the
+ * tensor cores (tcgen05, split-TF32: three TF32 MMAs per float32 product,
+ * float32 accumulation in tensor memory); method 1 runs every product on
+ * the CUDA cores in float32.  A product that does not finish within a
+ * bounded wait leaves that problem's X non-finite. */
+mpxg_status mpxg_lqr_eq_solve_method(void* stream, const mpxg_lq_eq_io* io, int method);
 
 /* Allocation-free batched solve.  No counterpart in the reference.  For
  * callers that cannot allocate device memory when they solve (a real-time

@@ -100,7 +100,7 @@ class LqIO(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_solve_vjp",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
@@ -156,6 +156,8 @@ def load(build_if_missing=True):
     L.mpxg_lqr_eq_workspace_bytes.restype = ctypes.c_size_t
     L.mpxg_lqr_eq_solve.argtypes = [vp, ctypes.POINTER(LqEqIO)]
     L.mpxg_lqr_eq_solve.restype = ctypes.c_int
+    L.mpxg_lqr_eq_solve_method.argtypes = [vp, ctypes.POINTER(LqEqIO), ctypes.c_int]
+    L.mpxg_lqr_eq_solve_method.restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_xla_solve_vjp.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]

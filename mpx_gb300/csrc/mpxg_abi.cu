@@ -14,7 +14,7 @@
 #include "../../include/mpxg.h"
 #include "aux_kernels.cuh"
 #include "evaluate_kernel.cuh"
-#include "lqr_eq_kernel.cuh"
+#include "lqr_eq_tc.cuh"
 #include "lqr_kernels.cuh"
 #include "sqp_kernel.cuh"
 
@@ -539,20 +539,27 @@ size_t mpxg_lqr_eq_workspace_bytes(int batch, int N, int n) {
   return lqeq::lqr_eq_scratch_bytes(batch, N, n);
 }
 
-mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io) {
+mpxg_status mpxg_lqr_eq_solve_method(void* stream, const mpxg_lq_eq_io* io, int method) {
   if (!io || io->batch < 0 || io->N < 1 || !io->A || !io->Bm || !io->c || !io->Q || !io->R || !io->M || !io->q ||
       !io->r || !io->C || !io->D || !io->e || !io->x0 || !io->K || !io->k || !io->Knu || !io->knu || !io->X ||
       !io->U || !io->lam || !io->nu || !io->workspace)
     return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: bad arguments");
+  if (method != 0 && method != 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: method is 0 or 1");
   if (io->batch == 0) return MPXG_OK;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
-  if (io->n == 72 && io->m == 30 && io->n_eq == 12) e = lqeq::launch_lqr_eq<72, 30, 12>(st, *io);
-  else if (io->n == 16 && io->m == 8 && io->n_eq == 4) e = lqeq::launch_lqr_eq<16, 8, 4>(st, *io);
-  else if (io->n == 8 && io->m == 5 && io->n_eq == 2) e = lqeq::launch_lqr_eq<8, 5, 2>(st, *io);
+  const bool tcores = (method == 0);
+  if (io->n == 72 && io->m == 30 && io->n_eq == 12)
+    e = tcores ? lqeq::launch_lqr_eq_tc<72, 30, 12>(st, *io) : lqeq::launch_lqr_eq<72, 30, 12>(st, *io);
+  else if (io->n == 16 && io->m == 8 && io->n_eq == 4)
+    e = tcores ? lqeq::launch_lqr_eq_tc<16, 8, 4>(st, *io) : lqeq::launch_lqr_eq<16, 8, 4>(st, *io);
+  else if (io->n == 8 && io->m == 5 && io->n_eq == 2)
+    e = tcores ? lqeq::launch_lqr_eq_tc<8, 5, 2>(st, *io) : lqeq::launch_lqr_eq<8, 5, 2>(st, *io);
   else return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_lqr_eq_solve: (n, m, n_eq) not built: (72,30,12) (16,8,4) (8,5,2)");
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "lqr_eq_kernel launch");
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "lqr_eq kernel launch");
 }
+
+mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io) { return mpxg_lqr_eq_solve_method(stream, io, 0); }
 
 }  // extern "C"
 

@@ -276,9 +276,10 @@ def lqr_solve(A, B, c, Q, R, M, q, r, x0, method=0, stream=None):
     return out
 
 
-def lqr_eq_solve(A, B, c, Q, R, M, q, r, C, D, e, x0, stream=None):
-    """Batched equality-constrained LQR on the device (mpxg_lqr_eq_solve).
-    Shapes as in include/mpxg.h.  Returns dict K, k, Knu, knu, X, U, lam, nu."""
+def lqr_eq_solve(A, B, c, Q, R, M, q, r, C, D, e, x0, stream=None, method=0):
+    """Batched equality-constrained LQR on the device (mpxg_lqr_eq_solve_method:
+    method 0 = stage products on the tensor cores, 1 = CUDA cores).  Shapes as
+    in include/mpxg.h.  Returns dict K, k, Knu, knu, X, U, lam, nu."""
     L = _lib.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     names = ("A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
@@ -297,7 +298,8 @@ def lqr_eq_solve(A, B, c, Q, R, M, q, r, C, D, e, x0, stream=None):
     for name in ("K", "k", "Knu", "knu", "X", "U", "lam", "nu"):
         setattr(io, name, _ptr(out[name]))
     io.workspace = _ptr(ws)
-    _lib.check(L.mpxg_lqr_eq_solve(_stream_handle(stream), ctypes.byref(io)), None, "mpxg_lqr_eq_solve")
+    _lib.check(L.mpxg_lqr_eq_solve_method(_stream_handle(stream), ctypes.byref(io), int(method)), None,
+               "mpxg_lqr_eq_solve")
     out["_keep"] = (t, ws)
     return out
 

@@ -26,10 +26,13 @@ def test_lqr_matches_oracle(oracle, cuda, n, m, N, method):
         assert e < 2e-4, (k, e)
 
 
+@pytest.mark.parametrize("method", [0, 1])
 @pytest.mark.parametrize("n,m,ne,N,B", [(8, 5, 2, 6, 3), (16, 8, 4, 20, 3), (72, 30, 12, 100, 2)])
-def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B):
+def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B, method):
     """Equality-constrained LQR on the GPU against the FP64 stagewise Riccati
-    (itself checked against a dense KKT solve on the CPU)."""
+    (itself checked against a dense KKT solve on the CPU): method 0 with the
+    stage products on the tensor cores (split TF32), method 1 on the CUDA
+    cores."""
     from mpx_gb300.solver import lqr_eq_solve
     from oracle.lqr_eq import riccati_eq
     d = P.random_lq_eq(B, n=n, m=m, n_eq=ne, N=N, seed=n + N)
@@ -38,7 +41,7 @@ def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B):
         d["M"] = 0.002 * np.random.default_rng(3).normal(size=d["M"].shape)
         d["r"] = np.random.default_rng(4).normal(size=d["r"].shape)
     keys = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
-    g = lqr_eq_solve(*[d[k] for k in keys])
+    g = lqr_eq_solve(*[d[k] for k in keys], method=method)
     torch.cuda.synchronize()
     for b in range(B):
         o = riccati_eq(*[d[k][b] for k in keys])
