@@ -67,8 +67,7 @@ struct TcLay {
   // TS: D [Z | g | W]; KK: [K_nu | k_nu]
   static constexpr int NZW = NX + 1 + NE;
   static constexpr int QUU = 0, QUX = QUU + NU * LU, ZW = QUX + NX * LU, C = ZW + NZW * LU, D = C + NX * LE,
-                       TS = D + NU * LE, KK = TS + NZW * LE, PIV = KK + (NX + 1) * LE,
-                       V = PIV + 2 * (NU > NE ? NU : NE);
+                       TS = D + NU * LE, KK = TS + NZW * LE, PIV = KK + (NX + 1) * LE, V = PIV + 2 * 4 * 32;
   static constexpr int VL = NX + 4;
   static constexpr int vq = V, vr = vq + VL, ve = vr + VL, vp = ve + VL, vqx = vp + VL, vqu = vqx + VL,
                        vkn = vqu + VL, vk = vkn + VL, vx = vk + VL, vu = vx + VL, vt = vu + VL, FLOATS = vt + VL;
@@ -83,6 +82,7 @@ struct TcLay {
   // + 2 KB: a 128-row operand read past the last buffer's used rows (their
   // accumulator rows are never read) stays inside the allocation
   static constexpr uint32_t BYTES = OFF_MR + MR_BYTES + 2048u;
+  static_assert(BYTES <= 232448u, "227 KB of shared memory per block");
   // forward sweep staging (two stages of A | B | K | c | k) over regions F, G
   static constexpr int STG = NX * NX + 2 * NX * NU + NX + NU, STG4 = (STG + 3) / 4;
   static_assert(2u * STG4 * 16u <= OFF_S - OFF_F, "forward staging must fit regions F and G");
@@ -126,31 +126,80 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_older() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Solve S X = Y for a symmetric positive definite S (R x R) by Gauss-Jordan
-// without pivoting over the augmented [S | Y] (NCOL columns), one thread per
-// column, the column in registers: at pivot p its owner publishes column p,
-// every later column is updated.  load(j, v) fills column j; store(j, v)
-// receives the solution columns j >= R.  piv: 2 R floats of shared memory.
+// Solve S X = Y for a symmetric positive definite S (R x R) by block
+// Gauss-Jordan over the augmented [S | Y] (NCOL columns), one thread per
+// column, the column in registers.  Pivots are taken four at a time: the
+// owners of the block's columns publish them (double-buffered panel, one
+// barrier per block), and every later column solves the 4 x 4 pivot block
+// D y = v[block] by Cholesky, then v[i] -= panel[i] . y off the block and
+// v[block] = y.  load(j, v) fills column j; store(j, v) receives the solution
+// columns j >= R.  panel: 2 x 4 x 32 floats of shared memory.
 template <int R, int NCOL, class Load, class Store>
-__device__ __forceinline__ void gj_solve(float* piv, Load load, Store store) {
-  static_assert(NCOL <= kThreads, "one thread per column");
+__device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
+  static_assert(R <= 32 && NCOL <= kThreads, "pivots within 32 rows, one thread per column");
   const int j = threadIdx.x;
   float v[R];
   if (j < NCOL) load(j, v);
 #pragma unroll
-  for (int p = 0; p < R; ++p) {
-    float* pb = piv + (p & 1) * R;
-    if (j == p) {
+  for (int b0 = 0; b0 < R; b0 += 4) {
+    constexpr int B4 = 4;
+    const int bs = (R - b0) < B4 ? (R - b0) : B4;
+    float* pb = panel + ((b0 / 4) & 1) * 4 * 32;
+    if (j >= b0 && j < b0 + bs) {
 #pragma unroll
-      for (int i = 0; i < R; ++i) pb[i] = v[i];
+      for (int i = 0; i < R; ++i) pb[(j - b0) * 32 + i] = v[i];
     }
     __syncthreads();
-    if (j > p && j < NCOL) {
-      float d = pb[p];
-      if (!(d > 0.0f)) d = fmaxf(fabsf(d), 1e-30f);
-      const float f = v[p] / d;
+    if (j >= b0 + bs && j < NCOL) {
+      // pivot block D(r, k) = pb[k * 32 + b0 + r]; Cholesky D = L L'
+      float Lm[4][4], il[4], y[4];
 #pragma unroll
-      for (int i = 0; i < R; ++i) v[i] = (i == p) ? f : v[i] - pb[i] * f;
+      for (int r = 0; r < 4; ++r) {
+        if (r >= bs) continue;
+#pragma unroll
+        for (int k = 0; k <= r; ++k) {
+          float a = pb[k * 32 + b0 + r];
+#pragma unroll
+          for (int q = 0; q < k; ++q) a -= Lm[r][q] * Lm[k][q];
+          if (k == r) {
+            if (!(a > 0.0f)) a = fmaxf(fabsf(a), 1e-30f);
+            il[r] = rsqrtf(a);
+            Lm[r][r] = a * il[r];
+          } else {
+            Lm[r][k] = a * il[k];
+          }
+        }
+      }
+      // y = D^-1 v[block]: L z = v, L' y = z
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if (r >= bs) continue;
+        float a = v[b0 + r];
+#pragma unroll
+        for (int q = 0; q < r; ++q) a -= Lm[r][q] * y[q];
+        y[r] = a * il[r];
+      }
+#pragma unroll
+      for (int r = 3; r >= 0; --r) {
+        if (r >= bs) continue;
+        float a = y[r];
+#pragma unroll
+        for (int q = r + 1; q < 4; ++q)
+          if (q < bs) a -= Lm[q][r] * y[q];
+        y[r] = a * il[r];
+      }
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        if (i >= b0 && i < b0 + bs) continue;
+        float a = v[i];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < bs) a -= pb[k * 32 + i] * y[k];
+        v[i] = a;
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (r < bs) v[b0 + r] = y[r];
     }
   }
   if (j >= R && j < NCOL) store(j, v);
@@ -216,7 +265,7 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     for (int it = 0; it < PIT; ++it) {
       const int e = tid + kThreads * it;
       if (e < NX * (NX / 4)) {
-        const int m = e / (NX / 4), k0 = 4 * (e % (NX / 4));
+        const int m = e % NX, k0 = 4 * (e / NX);  // lanes over rows: conflict-free column reads
         float v[4], h[4], l[4];
         float4 qr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         float qc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -377,43 +426,33 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     }
     cp_async_wait_older();  // M and R have landed (Q may still be in flight)
     __syncthreads();
-    // ---- + M' and + R; Q_ux' into gamma's A operand
-    {
-      constexpr int MIT = (NX * NU + kThreads - 1) / kThreads, RIT = (NU * NU + kThreads - 1) / kThreads;
-#pragma unroll
-      for (int it = 0; it < MIT; ++it) {
-        const int e = tid + kThreads * it;
-        if (e < NX * NU) {
-          const int col = e / NU, a = e % NU;
-          const float qux = Qux[col * LU + a] + sM[e];
-          Qux[col * LU + a] = qux;
-          float h, l;
-          tc::split(qux, &h, &l);
-          const uint32_t o = tc::slab_off(col, a, L::SH);
-          *reinterpret_cast<float*>(Hh + o) = h;
-          *reinterpret_cast<float*>(Hl + o) = l;
-        }
-      }
-#pragma unroll
-      for (int it = 0; it < RIT; ++it) {
-        const int e = tid + kThreads * it;
-        if (e < NU * NU) {
-          const int a = e / NU, bb = e % NU;
-          Quu[bb * LU + a] += sR[e];
-        }
-      }
-    }
-    __syncthreads();
     // ---- elimination (CUDA cores), two column-parallel Gauss-Jordan solves:
     //   Q_uu [Z | g | W] = [Q_ux | q_u | D'];
     //   [S | T | h] = [D W | C - D Z | D g + e],  S [K_nu | -k_nu] = [T | h];
     //   Z += W K_nu (K = -Z), g += W k_nu (k = -g)
+    // (the column loads finish Q_uu = R + B'PB and Q_ux = M' + B'PA, and put
+    // Q_ux' into gamma's A operand in region P)
     gj_solve<NU, NU + L::NZW>(piv, [&](int j, float* v) {
+      if (j < NU) {
 #pragma unroll
-      for (int i = 0; i < NU; ++i)
-        v[i] = j < NU ? Quu[j * LU + i]
-                      : (j < NU + NX ? Qux[(j - NU) * LU + i]
-                                     : (j == NU + NX ? vqu[i] : sD[i * LE + (j - NU - NX - 1)]));
+        for (int i = 0; i < NU; ++i) v[i] = Quu[j * LU + i] + sR[i * NU + j];
+      } else if (j < NU + NX) {
+        const int col = j - NU;
+#pragma unroll
+        for (int i = 0; i < NU; ++i) {
+          const float qux = Qux[col * LU + i] + sM[col * NU + i];
+          Qux[col * LU + i] = qux;
+          v[i] = qux;
+          float h, l;
+          tc::split(qux, &h, &l);
+          const uint32_t o = tc::slab_off(col, i, L::SH);
+          *reinterpret_cast<float*>(Hh + o) = h;
+          *reinterpret_cast<float*>(Hl + o) = l;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < NU; ++i) v[i] = j == NU + NX ? vqu[i] : sD[i * LE + (j - NU - NX - 1)];
+      }
     }, [&](int j, const float* v) {
 #pragma unroll
       for (int i = 0; i < NU; ++i) ZW[(j - NU) * LU + i] = v[i];
