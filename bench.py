@@ -642,7 +642,8 @@ def run_lqr_eq(args, rank, world, local_rank):
     from mpx_gb300.solver import _ptr, _stream_handle
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    B, N, n, m, ne = 512, 100, 72, 30, 12
+    B = 512 if args.batch == BATCH else int(args.batch)  # --batch: a smaller case for profiling
+    N, n, m, ne = 100, 72, 30, 12
     parts = [P.random_lq_eq(min(32, B - i), n, m, ne, N, seed=31 + i + 1000 * rank) for i in range(0, B, 32)]
     d = {k: np.concatenate([p[k] for p in parts], 0).astype(np.float32) for k in parts[0]}
     names = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
@@ -698,7 +699,7 @@ def run_lqr_eq(args, rank, world, local_rank):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     gbs = (in_bytes + out_bytes) / avg_s / 1e9
     line = {
-        "metric": "constrained LQR solves/s (n=72, m=30, 12 equality rows, N=100, batch 512)",
+        "metric": "constrained LQR solves/s (n=72, m=30, 12 equality rows, N=100, batch %d)" % B,
         "value": world * B / avg_s, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic (seeded)",

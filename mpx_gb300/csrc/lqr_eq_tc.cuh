@@ -67,7 +67,8 @@ struct TcLay {
   // TS: D [Z | g | W]; KK: [K_nu | k_nu]
   static constexpr int NZW = NX + 1 + NE;
   static constexpr int QUU = 0, QUX = QUU + NU * LU, ZW = QUX + NX * LU, C = ZW + NZW * LU, D = C + NX * LE,
-                       TS = D + NU * LE, KK = TS + NZW * LE, PIV = KK + (NX + 1) * LE, V = PIV + 2 * 4 * 32;
+                       TS = D + NU * LE, KK = TS + NZW * LE, PIV = (KK + (NX + 1) * LE + 3) / 4 * 4,
+                       V = PIV + 2 * 4 * 32;
   static constexpr int VL = NX + 4;
   static constexpr int vq = V, vr = vq + VL, ve = vr + VL, vp = ve + VL, vqx = vp + VL, vqu = vqx + VL,
                        vkn = vqu + VL, vk = vkn + VL, vx = vk + VL, vu = vx + VL, vt = vu + VL, FLOATS = vt + VL;
@@ -77,8 +78,14 @@ struct TcLay {
   // the stage's Q (row-major) sits in region G behind gamma's B operand
   static constexpr uint32_t OFF_QS = OFF_G + 2u * SL3 * SJ;
   static_assert(2u * SL3 * SJ + (uint32_t)(NX * NX) * 4u <= BYTES_G, "Q must fit region G behind [K ; K_nu]");
+  // the next stage's raw A | B | c, copied into region F behind the float32 P
+  // while the elimination runs (region F is free between beta and gamma)
+  static constexpr uint32_t OFF_RAW = OFF_F + al128((uint32_t)(NX * (NX + 1) * 4));
+  static constexpr uint32_t RAW_BYTES = (uint32_t)(NX * NX + NX * NU + NX) * 4u;
+  static_assert(OFF_RAW + RAW_BYTES <= OFF_F + BYTES_F, "raw stage data must fit region F behind P");
   // asynchronous copies move 16-byte chunks: per-stage sizes must allow them
-  static constexpr bool ASYNC_SIZES = (NX * NX * 4) % 16 == 0 && (NX * NU * 4) % 16 == 0 && (NU * NU * 4) % 16 == 0;
+  static constexpr bool ASYNC_SIZES = (NX * NX * 4) % 16 == 0 && (NX * NU * 4) % 16 == 0 &&
+                                      (NU * NU * 4) % 16 == 0 && (NX * 4) % 16 == 0;
   // + 2 KB: a 128-row operand read past the last buffer's used rows (their
   // accumulator rows are never read) stays inside the allocation
   static constexpr uint32_t BYTES = OFF_MR + MR_BYTES + 2048u;
@@ -133,7 +140,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // barrier per block), and every later column solves the 4 x 4 pivot block
 // D y = v[block] by Cholesky, then v[i] -= panel[i] . y off the block and
 // v[block] = y.  load(j, v) fills column j; store(j, v) receives the solution
-// columns j >= R.  panel: 2 x 4 x 32 floats of shared memory.
+// columns j >= R.  panel: 2 x 32 x 4 floats of shared memory (row i's four
+// pivot-column entries contiguous, one 16-byte broadcast per row).
 template <int R, int NCOL, class Load, class Store>
 __device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
   static_assert(R <= 32 && NCOL <= kThreads, "pivots within 32 rows, one thread per column");
@@ -147,18 +155,20 @@ __device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
     float* pb = panel + ((b0 / 4) & 1) * 4 * 32;
     if (j >= b0 && j < b0 + bs) {
 #pragma unroll
-      for (int i = 0; i < R; ++i) pb[(j - b0) * 32 + i] = v[i];
+      for (int i = 0; i < R; ++i) pb[i * 4 + (j - b0)] = v[i];
     }
     __syncthreads();
     if (j >= b0 + bs && j < NCOL) {
-      // pivot block D(r, k) = pb[k * 32 + b0 + r]; Cholesky D = L L'
+      // pivot block D(r, k) = pb[(b0 + r) * 4 + k]; Cholesky D = L L'
       float Lm[4][4], il[4], y[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         if (r >= bs) continue;
+        const float4 dr = *reinterpret_cast<const float4*>(pb + (b0 + r) * 4);
+        const float drv[4] = {dr.x, dr.y, dr.z, dr.w};
 #pragma unroll
         for (int k = 0; k <= r; ++k) {
-          float a = pb[k * 32 + b0 + r];
+          float a = drv[k];
 #pragma unroll
           for (int q = 0; q < k; ++q) a -= Lm[r][q] * Lm[k][q];
           if (k == r) {
@@ -191,10 +201,12 @@ __device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         if (i >= b0 && i < b0 + bs) continue;
+        const float4 pr = *reinterpret_cast<const float4*>(pb + i * 4);
+        const float prv[4] = {pr.x, pr.y, pr.z, pr.w};
         float a = v[i];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-          if (k < bs) a -= pb[k * 32 + i] * y[k];
+          if (k < bs) a -= prv[k] * y[k];
         v[i] = a;
       }
 #pragma unroll
@@ -230,6 +242,9 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
   float* sM = reinterpret_cast<float*>(smraw + L::OFF_MR);
   float* sR = sM + NX * NU;
   float* sQ = reinterpret_cast<float*>(smraw + L::OFF_QS);
+  float* rawA = reinterpret_cast<float*>(smraw + L::OFF_RAW);
+  float* rawB = rawA + NX * NX;
+  float* rawc = rawB + NX * NU;
   float *vq = s + L::vq, *vr = s + L::vr, *ve = s + L::ve, *vp = s + L::vp, *vqx = s + L::vqx, *vqu = s + L::vqu;
   float *vkn = s + L::vkn, *vk = s + L::vk, *vx = s + L::vx, *vu = s + L::vu;
   float* vt = s + L::vt;
@@ -289,6 +304,13 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     for (int i = tid; i < NX; i += kThreads) Pt[NX * NX + i] = vp[i];
   };
 
+  // the raw A | B | c of stage t into region F (asynchronous when aligned)
+  auto copy_raw = [&](int t) {
+    copy_async(rawA, io.A + (sn + t) * NX * NX, NX * NX, async);
+    copy_async(rawB, io.Bm + (sn + t) * NX * NU, NX * NU, async);
+    copy_async(rawc, io.c + (sn + t) * NX, NX, async);
+  };
+
   // L2 prefetch of one stage's matrices (128-byte lines over the block)
   auto prefetch_stage = [&](int t) {
     auto pf = [&](const float* base, int floats) {
@@ -310,7 +332,11 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     const float* QN = io.Q + (sn1 + N) * NX * NX;
     for (int e = tid; e < NX * NX; e += kThreads) Pst[(e / NX) * (NX + 1) + e % NX] = __ldg(QN + e);
     load_vec<NX>(vp, io.q + (sn1 + N) * NX);
-    if (N >= 1) prefetch_stage(N - 1);
+    if (N >= 1) {
+      prefetch_stage(N - 1);
+      copy_raw(N - 1);
+    }
+    cp_async_commit();
     __syncthreads();
     store_P(N, nullptr);
     __syncthreads();
@@ -318,15 +344,14 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
 
   for (int t = N - 1; t >= 0 && ok; --t) {
     if (t >= 1) prefetch_stage(t - 1);
+    cp_async_wait_all();  // this stage's raw A | B | c (copied during the last one)
+    __syncthreads();
     copy_async(sM, io.M + (sn + t) * NX * NU, NX * NU, async);
     copy_async(sR, io.R + (sn + t) * NU * NU, NU * NU, async);
     cp_async_commit();
-    // ---- stage data: [A | B | c] as operand rows (element (n, k) = F[k][n]),
-    // the equality blocks and the vectors
+    // ---- stage data: [A | B | c] as operand rows (element (n, k) = F[k][n])
+    // from the raw copy, the equality blocks and the vectors
     {
-      const float* A = io.A + (sn + t) * NX * NX;
-      const float* Bm = io.Bm + (sn + t) * NX * NU;
-      const float* c = io.c + (sn + t) * NX;
       constexpr int NF = NX + NU + 1, FE = (NX / 4) * NF, FIT = (FE + kThreads - 1) / kThreads;
       float v[FIT][4];
 #pragma unroll
@@ -336,10 +361,10 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int k = k0 + j;
-          v[it][j] = e >= FE ? 0.0f
-                             : (n < NX ? __ldg(A + k * NX + n) : (n < NX + NU ? __ldg(Bm + k * NU + n - NX) : __ldg(c + k)));
+          v[it][j] = e >= FE ? 0.0f : (n < NX ? rawA[k * NX + n] : (n < NX + NU ? rawB[k * NU + n - NX] : rawc[k]));
         }
       }
+      __syncthreads();  // the slabs overwrite the raw copy
 #pragma unroll
       for (int it = 0; it < FIT; ++it) {
         const int e = tid + kThreads * it;
@@ -398,6 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     }
     if (!(ok = tc_wait(barp, phase))) break;
     copy_async(sQ, io.Q + (sn1 + t) * NX * NX, NX * NX, async);  // region G is free until gamma's operands
+    if (t >= 1) copy_raw(t - 1);  // region F is free until gamma's P
     cp_async_commit();
     // ---- Q-function blocks from D2: q_x = q + A'w (rows < n, column n + m),
     // and rows n .. n + m - 1: B'PA (-> Q_ux), B'PB (-> Q_uu), q_u = r + B'w
@@ -668,7 +694,8 @@ inline cudaError_t launch_lqr_eq_tc(cudaStream_t st, const mpxg_lq_eq_io& io) {
                                        (int)smem);
   if (e != cudaSuccess) return e;
   auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
-  const bool async = TcLay<NX, NU, NE>::ASYNC_SIZES && al16(io.M) && al16(io.R) && al16(io.Q);
+  const bool async = TcLay<NX, NU, NE>::ASYNC_SIZES && al16(io.M) && al16(io.R) && al16(io.Q) && al16(io.A) &&
+                     al16(io.Bm) && al16(io.c);
   lqr_eq_tc_kernel<NX, NU, NE><<<io.batch, kThreads, smem, st>>>(io, io.workspace, async);
   return cudaGetLastError();
 }
