@@ -304,7 +304,7 @@ typedef struct {
   int batch, N, n, m, n_eq;
   const float *A, *Bm, *c, *Q, *R, *M, *q, *r, *C, *D, *e, *x0;
   float *K, *k, *Knu, *knu, *X, *U, *lam, *nu;
-  float* workspace;  /* device, >= mpxg_lqr_eq_workspace_bytes(batch, N, n) bytes */
+  float* workspace;  /* device, >= mpxg_lqr_eq_workspace_bytes(batch, N, n) bytes, 16-byte aligned */
 } mpxg_lq_eq_io;
 size_t mpxg_lqr_eq_workspace_bytes(int batch, int N, int n);
 mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io);

@@ -311,8 +311,10 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     copy_async(rawc, io.c + (sn + t) * NX, NX, async);
   };
 
-  // L2 prefetch of one stage's matrices (128-byte lines over the block)
+  // L2 prefetch of one stage's matrices (128-byte lines over the block; only
+  // with 16-byte aligned inputs, like the asynchronous copies)
   auto prefetch_stage = [&](int t) {
+    if (!async) return;
     auto pf = [&](const float* base, int floats) {
       const char* c = reinterpret_cast<const char*>(base);
       for (int off = tid * 128; off < floats * 4; off += kThreads * 128)

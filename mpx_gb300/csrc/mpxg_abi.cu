@@ -545,6 +545,8 @@ mpxg_status mpxg_lqr_eq_solve_method(void* stream, const mpxg_lq_eq_io* io, int 
       !io->U || !io->lam || !io->nu || !io->workspace)
     return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: bad arguments");
   if (method != 0 && method != 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: method is 0 or 1");
+  if (method == 0 && (reinterpret_cast<uintptr_t>(io->workspace) & 15u) != 0)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: workspace must be 16-byte aligned");
   if (io->batch == 0) return MPXG_OK;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;

@@ -72,3 +72,23 @@ def test_xla_target_rejects_a_malformed_opaque():
     bufs = (ctypes.c_void_p * 10)()
     L.mpxg_xla_solve(None, bufs, b"short", 5, None)
     assert b"mpxg_xla_opaque" in L.mpxg_last_error(None)
+
+
+def test_lqr_eq_rejects_bad_method_and_unaligned_workspace():
+    """mpxg_lqr_eq_solve_method validates before touching the GPU: the method
+    is 0 or 1, and the tensor-core kernel (method 0), which writes the
+    workspace in 16-byte vectors, needs a 16-byte aligned workspace."""
+    from mpx_gb300 import _lib
+    L = _lib.load()
+    io = _lib.LqEqIO()
+    io.batch, io.N, io.n, io.m, io.n_eq = 1, 4, 72, 30, 12
+    fake = 1 << 20  # never dereferenced: the checks fail first
+    for name in ("A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0", "K", "k", "Knu", "knu", "X", "U",
+                 "lam", "nu"):
+        setattr(io, name, ctypes.c_void_p(fake))
+    io.workspace = ctypes.c_void_p(fake + 4)
+    assert L.mpxg_lqr_eq_solve_method(None, ctypes.byref(io), 2) == 1
+    assert b"method" in L.mpxg_last_error(None)
+    assert L.mpxg_lqr_eq_solve_method(None, ctypes.byref(io), 0) == 1
+    assert b"16-byte aligned" in L.mpxg_last_error(None)
+    assert L.mpxg_lqr_eq_solve(None, ctypes.byref(io)) == 1

@@ -53,3 +53,39 @@ def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B, method):
         X, U = g["X"][b].cpu().double().numpy(), g["U"][b].cpu().double().numpy()
         res = np.einsum("tij,tj->ti", d["C"][b], X[:N]) + np.einsum("tij,tj->ti", d["D"][b], U) - d["e"][b]
         assert np.abs(res).max() < 1e-3 * max(1.0, np.abs(d["e"][b]).max())
+
+
+def test_lqr_eq_tensor_cores_unaligned_inputs(cuda):
+    """Inputs at addresses that are not 16-byte aligned take the plain-copy
+    path of the tensor-core kernel (no asynchronous 16-byte copies) and give
+    the same result bit for bit."""
+    import ctypes
+    from mpx_gb300 import _lib
+    from mpx_gb300.solver import _ptr, lqr_eq_solve
+    n, m, ne, N, B = 16, 8, 4, 12, 3
+    d = P.random_lq_eq(B, n=n, m=m, n_eq=ne, N=N, seed=77)
+    keys = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+    ref = lqr_eq_solve(*[d[k] for k in keys], method=0)
+    torch.cuda.synchronize()
+    # the same inputs one float past an aligned base
+    dev = torch.device("cuda")
+    shifted = {}
+    for k in keys:
+        a = torch.as_tensor(d[k], dtype=torch.float32).reshape(-1)
+        buf = torch.zeros(a.numel() + 1, device=dev)
+        buf[1:] = a.to(dev)
+        shifted[k] = buf
+    L = _lib.load()
+    out = {k: torch.empty_like(v) for k, v in ref.items() if not k.startswith("_")}
+    ws = torch.empty(int(L.mpxg_lqr_eq_workspace_bytes(B, N, n)) // 4, device=dev)
+    io = _lib.LqEqIO()
+    io.batch, io.N, io.n, io.m, io.n_eq = B, N, n, m, ne
+    for name, k in zip(("A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0"), keys):
+        setattr(io, name, ctypes.c_void_p(shifted[k].data_ptr() + 4))
+    for k in out:
+        setattr(io, k, _ptr(out[k]))
+    io.workspace = _ptr(ws)
+    assert L.mpxg_lqr_eq_solve_method(None, ctypes.byref(io), 0) == 0
+    torch.cuda.synchronize()
+    for k in out:
+        assert torch.equal(out[k], ref[k]), k
