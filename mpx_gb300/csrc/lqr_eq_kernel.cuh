@@ -161,6 +161,151 @@ struct Lay {
                        vu = vx + VL, FLOATS = vu + VL;
 };
 
+// Forward sweep from x0: u_t = K_t x_t + k_t, x_{t+1} = A_t x_t + B_t u_t + c_t.
+// Each stage's A, B, K (with c, k) is staged in shared memory transposed, with
+// odd leading dimensions, so one thread per output row reads consecutive
+// words and the transposing stores are conflict-free; stage t+1 is loaded
+// into registers while stage t computes (two buffers of FwdLay::STG floats).
+template <int NX, int NU>
+struct FwdLay {
+  static constexpr int LA = NX % 2 ? NX : NX + 1, LK = NU % 2 ? NU : NU + 1;
+  static constexpr int OA = 0, OB = NX * LA, OK = OB + NU * LA, OC = OK + NX * LK, OKK = OC + NX, STG = OKK + NU;
+  static constexpr int SA = NX * NX, SB = NX * NU, SK = NU * NX, SRC = SA + SB + SK + NX + NU;
+  // staged slot of source element e of A | B | K | c | k (each row-major)
+  __device__ static int slot(int e) {
+    if (e < SA) return OA + (e % NX) * LA + e / NX;
+    e -= SA;
+    if (e < SB) return OB + (e % NU) * LA + e / NU;
+    e -= SB;
+    if (e < SK) return OK + (e % NX) * LK + e / NX;
+    e -= SK;
+    return e < NX ? OC + e : OKK + (e - NX);
+  }
+};
+
+template <int NX, int NU>
+__device__ __forceinline__ void forward_sweep(const mpxg_lq_eq_io& io, int b, float* stg0, float* stg1, float* vx,
+                                              float* vu, float* vt) {
+  typedef FwdLay<NX, NU> F;
+  static_assert(NX <= kThreads && NU <= kThreads, "one thread per output row");
+  const int N = io.N, tid = threadIdx.x;
+  const size_t sn = (size_t)b * N, sn1 = (size_t)b * (N + 1);
+  auto src = [&](int t, int e) -> float {
+    if (e < F::SA) return __ldg(io.A + (sn + t) * F::SA + e);
+    e -= F::SA;
+    if (e < F::SB) return __ldg(io.Bm + (sn + t) * F::SB + e);
+    e -= F::SB;
+    if (e < F::SK) return io.K[(sn + t) * F::SK + e];  // written by this kernel
+    e -= F::SK;
+    return e < NX ? __ldg(io.c + (sn + t) * NX + e) : io.k[(sn + t) * NU + e - NX];
+  };
+  constexpr int PF = (F::SRC + kThreads - 1) / kThreads;
+  float* stg[2] = {stg0, stg1};
+  float* X = io.X + sn1 * NX;
+  float* U = io.U + sn * NU;
+  for (int i = tid; i < NX; i += kThreads) vx[i] = io.x0[(size_t)b * NX + i];
+  for (int e = tid; e < F::SRC; e += kThreads) stg[0][F::slot(e)] = src(0, e);
+  __syncthreads();
+  for (int t = 0; t < N; ++t) {
+    const float* cur = stg[t & 1];
+    float pre[PF];
+    if (t + 1 < N) {
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int e = tid + kThreads * q;
+        pre[q] = e < F::SRC ? src(t + 1, e) : 0.0f;
+      }
+    }
+    for (int i = tid; i < NX; i += kThreads) X[t * NX + i] = vx[i];
+    if (tid < NU) {  // u = K x + k
+      const int a = tid;
+      float s0 = cur[F::OKK + a], s1 = 0.0f;
+#pragma unroll 4
+      for (int j = 0; j + 1 < NX; j += 2) {
+        s0 += cur[F::OK + j * F::LK + a] * vx[j];
+        s1 += cur[F::OK + (j + 1) * F::LK + a] * vx[j + 1];
+      }
+      if (NX & 1) s0 += cur[F::OK + (NX - 1) * F::LK + a] * vx[NX - 1];
+      const float u = s0 + s1;
+      vu[a] = u;
+      U[t * NU + a] = u;
+    }
+    __syncthreads();
+    if (tid < NX) {  // x+ = A x + B u + c
+      const int i = tid;
+      float s0 = cur[F::OC + i], s1 = 0.0f;
+#pragma unroll 4
+      for (int j = 0; j + 1 < NX; j += 2) {
+        s0 += cur[F::OA + j * F::LA + i] * vx[j];
+        s1 += cur[F::OA + (j + 1) * F::LA + i] * vx[j + 1];
+      }
+      if (NX & 1) s0 += cur[F::OA + (NX - 1) * F::LA + i] * vx[NX - 1];
+#pragma unroll 2
+      for (int a = 0; a < NU; ++a) s1 += cur[F::OB + a * F::LA + i] * vu[a];
+      vt[i] = s0 + s1;
+    }
+    if (t + 1 < N) {
+      float* nxt = stg[(t + 1) & 1];
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int e = tid + kThreads * q;
+        if (e < F::SRC) nxt[F::slot(e)] = pre[q];
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < NX; i += kThreads) vx[i] = vt[i];
+    __syncthreads();
+  }
+  for (int i = tid; i < NX; i += kThreads) X[N * NX + i] = vx[i];
+}
+
+// Costates lam_t = P_t x_t + p_t and multipliers nu_t = K_nu,t x_t + k_nu,t,
+// a warp per stage.  P_t (workspace, exactly symmetric) is read by columns:
+// lane r accumulates lam[r] = sum_j P[j][r] x[j] with coalesced loads and no
+// reductions; nu by shuffle reductions over its p rows.  xs: (threads / 32)
+// x NX floats of shared memory.
+template <int NX, int NE>
+__device__ __forceinline__ void costates(const mpxg_lq_eq_io& io, int b, const float* Ps, float* xs) {
+  constexpr int NP = NX + 1, Q = (NX + 31) / 32;
+  const int N = io.N, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t sn = (size_t)b * N, sn1 = (size_t)b * (N + 1);
+  const float* X = io.X + sn1 * NX;
+  float* xw = xs + warp * NX;
+  for (int t = warp; t <= N; t += kThreads / 32) {
+    const float* Pt = Ps + (size_t)t * NP * NX;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+      if (lane + 32 * q < NX) xw[lane + 32 * q] = X[(size_t)t * NX + lane + 32 * q];
+    __syncwarp();
+    float acc[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) acc[q] = 0.0f;
+#pragma unroll 4
+    for (int j = 0; j < NX; ++j) {
+      const float xj = xw[j];
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+        if (lane + 32 * q < NX) acc[q] += Pt[(size_t)j * NX + lane + 32 * q] * xj;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+      if (lane + 32 * q < NX) io.lam[(sn1 + t) * NX + lane + 32 * q] = acc[q] + Pt[NX * NX + lane + 32 * q];
+    if (t < N) {
+      const float* Knt = io.Knu + (sn + t) * NE * NX;
+      for (int jr = 0; jr < NE; ++jr) {
+        float a = 0.0f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+          if (lane + 32 * q < NX) a += Knt[(size_t)jr * NX + lane + 32 * q] * xw[lane + 32 * q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) io.nu[(sn + t) * NE + jr] = a + io.knu[(sn + t) * NE + jr];
+      }
+    }
+    __syncwarp();
+  }
+}
+
 template <int NX, int NU, int NE>
 constexpr size_t smem_bytes() { return (size_t)Lay<NX, NU, NE>::FLOATS * sizeof(float); }
 
@@ -263,127 +408,12 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_kernel(mpxg_lq_eq_io io, f
     __syncthreads();
   }
 
-  // ---- forward: u = K x + k, x+ = A x + B u + c.  Stage t+1's rows are
-  // copied into shared memory (row-major, double-buffered over the backward
-  // pass's buffers) while stage t is computed; a warp per row, lanes over the
-  // row, shuffle reductions.
-  {
-    constexpr int SA = NX * NX, SB = NX * NU, SK = NU * NX, STG = SA + SB + SK + NX + NU;
-    constexpr int STG4 = (STG + 3) / 4;
-    static_assert(2 * STG4 * 4 <= L::V, "forward staging must fit the matrix buffers (below the vectors)");
-    float* stg[2] = {s, s + STG4 * 4};
-    const int wid = tid >> 5, lane = tid & 31;
-    float* X = io.X + sn1 * NX;
-    float* U = io.U + sn * NU;
-    // copy stage t into buffer buf (all threads), element-wise: A | B | K | c | k
-    auto stage_copy = [&](int t, float* buf) {
-      const float* A = io.A + (sn + t) * SA;
-      const float* Bm = io.Bm + (sn + t) * SB;
-      const float* K = io.K + (sn + t) * SK;
-      for (int e = tid; e < SA; e += kThreads) buf[e] = __ldg(A + e);
-      for (int e = tid; e < SB; e += kThreads) buf[SA + e] = __ldg(Bm + e);
-      for (int e = tid; e < SK; e += kThreads) buf[SA + SB + e] = K[e];
-      for (int e = tid; e < NX; e += kThreads) buf[SA + SB + SK + e] = __ldg(io.c + (sn + t) * NX + e);
-      for (int e = tid; e < NU; e += kThreads) buf[SA + SB + SK + NX + e] = io.k[(sn + t) * NU + e];
-    };
-    for (int i = tid; i < NX; i += kThreads) vx[i] = io.x0[(size_t)b * NX + i];
-    stage_copy(0, stg[0]);
-    __syncthreads();
-    for (int t = 0; t < N; ++t) {
-      float* cur = stg[t & 1];
-      // prefetch stage t+1 into registers while this stage computes
-      constexpr int PF = (STG + kThreads - 1) / kThreads;
-      float pre[PF];
-      if (t + 1 < N) {
-        const float* A = io.A + (sn + t + 1) * SA;
-        const float* Bm = io.Bm + (sn + t + 1) * SB;
-        const float* K = io.K + (sn + t + 1) * SK;
-#pragma unroll
-        for (int i = 0; i < PF; ++i) {
-          const int e = tid + kThreads * i;
-          float v = 0.0f;
-          if (e < SA) v = __ldg(A + e);
-          else if (e < SA + SB) v = __ldg(Bm + e - SA);
-          else if (e < SA + SB + SK) v = K[e - SA - SB];
-          else if (e < SA + SB + SK + NX) v = __ldg(io.c + (sn + t + 1) * NX + e - SA - SB - SK);
-          else if (e < STG) v = io.k[(sn + t + 1) * NU + e - SA - SB - SK - NX];
-          pre[i] = v;
-        }
-      }
-      for (int i = tid; i < NX; i += kThreads) X[t * NX + i] = vx[i];
-      // u = K x + k: a warp per row
-      const float* K = cur + SA + SB;
-      for (int a = wid; a < NU; a += kThreads / 32) {
-        float acc = 0.0f;
-        for (int k2 = lane; k2 < NX; k2 += 32) acc += K[a * NX + k2] * vx[k2];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-          const float u = acc + cur[SA + SB + SK + NX + a];
-          vu[a] = u;
-          U[t * NU + a] = u;
-        }
-      }
-      __syncthreads();
-      // x+ = A x + B u + c: a warp per row (results to vq, then copied)
-      const float* A = cur;
-      const float* Bm = cur + SA;
-      for (int i = wid; i < NX; i += kThreads / 32) {
-        float acc = 0.0f;
-        for (int k2 = lane; k2 < NX; k2 += 32) acc += A[i * NX + k2] * vx[k2];
-        for (int k2 = lane; k2 < NU; k2 += 32) acc += Bm[i * NU + k2] * vu[k2];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) vq[i] = acc + cur[SA + SB + SK + i];
-      }
-      if (t + 1 < N) {
-        float* nxt = stg[(t + 1) & 1];
-#pragma unroll
-        for (int i = 0; i < PF; ++i) {
-          const int e = tid + kThreads * i;
-          if (e < STG) nxt[e] = pre[i];
-        }
-      }
-      __syncthreads();
-      for (int i = tid; i < NX; i += kThreads) vx[i] = vq[i];
-      __syncthreads();
-    }
-    for (int i = tid; i < NX; i += kThreads) X[N * NX + i] = vx[i];
-  }
+  // ---- forward sweep (staging over the matrix buffers, below the vectors)
+  // and the costates
+  static_assert(2 * FwdLay<NX, NU>::STG <= L::V, "forward staging must fit the matrix buffers (below the vectors)");
+  forward_sweep<NX, NU>(io, b, s, s + FwdLay<NX, NU>::STG, vx, vu, vq);
   __syncthreads();
-  // ---- costates lam_t = P_t x_t + p_t and multipliers nu_t = K_nu x_t + k_nu:
-  // a warp per stage, lanes over each row (coalesced), shuffle reductions
-  {
-    const int wid = tid >> 5, lane = tid & 31;
-    const float* X = io.X + sn1 * NX;
-    for (int t = wid; t <= N; t += kThreads / 32) {
-      const float* Pt = Ps + (size_t)t * NP * NX;
-      float xl[(NX + 31) / 32];
-#pragma unroll
-      for (int q = 0; q < (NX + 31) / 32; ++q) xl[q] = (lane + 32 * q < NX) ? X[(size_t)t * NX + lane + 32 * q] : 0.0f;
-      for (int r = 0; r < NX; ++r) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int q = 0; q < (NX + 31) / 32; ++q)
-          if (lane + 32 * q < NX) acc += Pt[(size_t)r * NX + lane + 32 * q] * xl[q];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) io.lam[(sn1 + t) * NX + r] = acc + Pt[NX * NX + r];
-      }
-      if (t < N) {
-        const float* Knt = io.Knu + (sn + t) * NE * NX;
-        for (int j = 0; j < NE; ++j) {
-          float acc = 0.0f;
-#pragma unroll
-          for (int q = 0; q < (NX + 31) / 32; ++q)
-            if (lane + 32 * q < NX) acc += Knt[(size_t)j * NX + lane + 32 * q] * xl[q];
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          if (lane == 0) io.nu[(sn + t) * NE + j] = acc + io.knu[(sn + t) * NE + j];
-        }
-      }
-    }
-  }
+  costates<NX, NE>(io, b, Ps, s);
 }
 
 inline size_t lqr_eq_scratch_bytes(int batch, int N, int n) { return (size_t)batch * (N + 1) * (n + 1) * n * 4; }

@@ -90,9 +90,10 @@ struct TcLay {
   // accumulator rows are never read) stays inside the allocation
   static constexpr uint32_t BYTES = OFF_MR + MR_BYTES + 2048u;
   static_assert(BYTES <= 232448u, "227 KB of shared memory per block");
-  // forward sweep staging (two stages of A | B | K | c | k) over regions F, G
-  static constexpr int STG = NX * NX + 2 * NX * NU + NX + NU, STG4 = (STG + 3) / 4;
-  static_assert(2u * STG4 * 16u <= OFF_S - OFF_F, "forward staging must fit regions F and G");
+  // forward sweep staging (two stages of A | B | K | c | k) over regions F, G;
+  // the costates' x staging (a warp's NX floats) over the elimination blocks
+  static_assert(2u * FwdLay<NX, NU>::STG * 4u <= OFF_S - OFF_F, "forward staging must fit regions F and G");
+  static_assert((kThreads / 32) * NX <= V, "costate staging must fit the elimination blocks");
 };
 
 template <int NX, int NU, int NE>
@@ -577,116 +578,14 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     return;
   }
 
-  // ---- forward sweep and costates (CUDA cores, as lqr_eq_kernel)
+  // ---- forward sweep (staging over regions F and G) and costates (CUDA
+  // cores, shared with lqr_eq_kernel)
   {
-    constexpr int SA = NX * NX, SB = NX * NU, SK = NU * NX, STG = L::STG, STG4 = L::STG4;
     float* fb = reinterpret_cast<float*>(smraw + L::OFF_F);
-    float* stg[2] = {fb, fb + STG4 * 4};
-    float* X = io.X + sn1 * NX;
-    float* U = io.U + sn * NU;
-    for (int i = tid; i < NX; i += kThreads) vx[i] = io.x0[(size_t)b * NX + i];
-    {
-      float* buf = stg[0];
-      const float* A = io.A + sn * SA;
-      const float* Bm = io.Bm + sn * SB;
-      const float* K = io.K + sn * SK;
-      for (int e = tid; e < SA; e += kThreads) buf[e] = __ldg(A + e);
-      for (int e = tid; e < SB; e += kThreads) buf[SA + e] = __ldg(Bm + e);
-      for (int e = tid; e < SK; e += kThreads) buf[SA + SB + e] = K[e];
-      for (int e = tid; e < NX; e += kThreads) buf[SA + SB + SK + e] = __ldg(io.c + sn * NX + e);
-      for (int e = tid; e < NU; e += kThreads) buf[SA + SB + SK + NX + e] = io.k[sn * NU + e];
-    }
-    __syncthreads();
-    for (int t = 0; t < N; ++t) {
-      float* cur = stg[t & 1];
-      constexpr int PF = (STG + kThreads - 1) / kThreads;
-      float pre[PF];
-      if (t + 1 < N) {
-        const float* A = io.A + (sn + t + 1) * SA;
-        const float* Bm = io.Bm + (sn + t + 1) * SB;
-        const float* K = io.K + (sn + t + 1) * SK;
-#pragma unroll
-        for (int i = 0; i < PF; ++i) {
-          const int e = tid + kThreads * i;
-          float v = 0.0f;
-          if (e < SA) v = __ldg(A + e);
-          else if (e < SA + SB) v = __ldg(Bm + e - SA);
-          else if (e < SA + SB + SK) v = K[e - SA - SB];
-          else if (e < SA + SB + SK + NX) v = __ldg(io.c + (sn + t + 1) * NX + e - SA - SB - SK);
-          else if (e < STG) v = io.k[(sn + t + 1) * NU + e - SA - SB - SK - NX];
-          pre[i] = v;
-        }
-      }
-      for (int i = tid; i < NX; i += kThreads) X[t * NX + i] = vx[i];
-      const float* K = cur + SA + SB;
-      for (int a = warp; a < NU; a += kThreads / 32) {
-        float acc = 0.0f;
-        for (int k2 = lane; k2 < NX; k2 += 32) acc += K[a * NX + k2] * vx[k2];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-          const float u = acc + cur[SA + SB + SK + NX + a];
-          vu[a] = u;
-          U[t * NU + a] = u;
-        }
-      }
-      __syncthreads();
-      const float* A = cur;
-      const float* Bm = cur + SA;
-      for (int i = warp; i < NX; i += kThreads / 32) {
-        float acc = 0.0f;
-        for (int k2 = lane; k2 < NX; k2 += 32) acc += A[i * NX + k2] * vx[k2];
-        for (int k2 = lane; k2 < NU; k2 += 32) acc += Bm[i * NU + k2] * vu[k2];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) vt[i] = acc + cur[SA + SB + SK + i];
-      }
-      if (t + 1 < N) {
-        float* nxt = stg[(t + 1) & 1];
-#pragma unroll
-        for (int i = 0; i < PF; ++i) {
-          const int e = tid + kThreads * i;
-          if (e < STG) nxt[e] = pre[i];
-        }
-      }
-      __syncthreads();
-      for (int i = tid; i < NX; i += kThreads) vx[i] = vt[i];
-      __syncthreads();
-    }
-    for (int i = tid; i < NX; i += kThreads) X[N * NX + i] = vx[i];
+    forward_sweep<NX, NU>(io, b, fb, fb + FwdLay<NX, NU>::STG, vx, vu, vt);
   }
   __syncthreads();
-  // ---- costates lam_t = P_t x_t + p_t and multipliers nu_t = K_nu x_t + k_nu
-  {
-    const float* X = io.X + sn1 * NX;
-    for (int t = warp; t <= N; t += kThreads / 32) {
-      const float* Pt = Ps + (size_t)t * NP * NX;
-      float xl[(NX + 31) / 32];
-#pragma unroll
-      for (int q = 0; q < (NX + 31) / 32; ++q) xl[q] = (lane + 32 * q < NX) ? X[(size_t)t * NX + lane + 32 * q] : 0.0f;
-      for (int r = 0; r < NX; ++r) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int q = 0; q < (NX + 31) / 32; ++q)
-          if (lane + 32 * q < NX) acc += Pt[(size_t)r * NX + lane + 32 * q] * xl[q];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) io.lam[(sn1 + t) * NX + r] = acc + Pt[NX * NX + r];
-      }
-      if (t < N) {
-        const float* Knt = io.Knu + (sn + t) * NE * NX;
-        for (int j = 0; j < NE; ++j) {
-          float acc = 0.0f;
-#pragma unroll
-          for (int q = 0; q < (NX + 31) / 32; ++q)
-            if (lane + 32 * q < NX) acc += Knt[(size_t)j * NX + lane + 32 * q] * xl[q];
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          if (lane == 0) io.nu[(sn + t) * NE + j] = acc + io.knu[(sn + t) * NE + j];
-        }
-      }
-    }
-  }
+  costates<NX, NE>(io, b, Ps, s);
 }
 
 template <int NX, int NU, int NE>
