@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1],
                     help="lqr: 0 sequential Riccati, 1 associative scan; lqr_eq: 0 tensor cores, 1 CUDA cores")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-other", action="store_true", help="skip the short LQ runs attached to the MPC line")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small run for ncu (no clocks, no CPU, no plain)")
     return ap.parse_args()
@@ -405,6 +406,9 @@ def run_ours(args, rank, world, local_rank):
                                  "p99": 1e3 * float(np.percentile(lat, 99)),
                                  "what": "submit to result row on the host, real-time Poisson arrivals"},
                   "kkt_frac_le_1e-5": float((sk <= 1e-5).mean()), "nan_status": int(((sst & 1) != 0).sum()),
+                  "kkt_frac_le_1e-5_by_model": {name: float((sk[srv.last_model == i] <= 1e-5).mean())
+                                                for i, name in enumerate(srv.model_names)
+                                                if (srv.last_model == i).any()},
                   "gpu_launches": srv.launches - launches0,
                   "workload": "Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, "
                               "alternating), N uniform in [20, 200], 200-tick episodes, state drift N(0, 0.01^2), "
@@ -498,8 +502,35 @@ def run_ours(args, rank, world, local_rank):
             "cached": tuned["cached"],
             "ms_per_solve": {"%dx%s" % (r["wpb"], r["bps"] or "auto"): r.get("ms") for r in tuned["table"]}},
     }
+    if not args.no_other and not args.profile:
+        line["other_configs"] = other_configs(args, rank, world, local_rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def other_configs(args, rank, world, local_rank):
+    """Short runs of the two LQ workloads (their full lines: --workload lqr /
+    lqr_eq): the isolated LQR of 1024 x (n=24, m=12, N=128), sequential
+    Riccati, and the constrained LQ of 512 x (n=72, m=30, 12 rows, N=100) on
+    the tensor cores and on the CUDA cores."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup, a.no_cpu, a.batch = 5, 3, True, BATCH
+    out = {}
+    a.lqr_method = 0
+    l1 = run_lqr(a, rank, world, local_rank, emit=False)
+    out["lqr_1024_n24_m12_N128"] = {"metric": "LQR solves/s", "value": l1["value"], "ms_per_step": l1["ms_per_step"],
+                                    "method": "sequential Riccati", "fp32_tflops": l1["fp32"]["achieved_tflops"]}
+    for method, label in ((0, "tensor_cores"), (1, "cuda_cores")):
+        a.lqr_method = method
+        l4 = run_lqr_eq(a, rank, world, local_rank, emit=False)
+        entry = {"metric": "constrained LQR solves/s", "value": l4["value"], "ms_per_step": l4["ms_per_step"],
+                 "kernel": l4["roofline"]["kernel"], "fp32_tflops": l4["fp32"]["achieved_tflops"]}
+        if "tensor" in l4:
+            entry["tf32_mma_tflops"] = l4["tensor"]["achieved_tflops"]
+            entry["tensor_frac"] = l4["tensor"]["frac"]
+        out["lqr_eq_512_n72_m30_p12_N100_" + label] = entry
+    return out
 
 
 # ------------------------------------------------------------ isolated LQR (KKT) workload
@@ -513,7 +544,7 @@ def lqr_data(B, N, n, m, seed, chunk=64):
     return {k: np.concatenate([p[k] for p in parts], 0).astype(np.float32) for k in parts[0]}
 
 
-def run_lqr(args, rank, world, local_rank):
+def run_lqr(args, rank, world, local_rank, emit=True):
     """--workload lqr: the isolated KKT/LQR solve, B=1024 problems with n=24,
     m=12, N=128 (mpxg_lqr_solve; --lqr-method 0 sequential Riccati, 1 scan)."""
     import torch
@@ -627,11 +658,12 @@ def run_lqr(args, rank, world, local_rank):
         "gpu_launches": args.steps * (1 if method == 0 else 1),
         "clocks": clk,
     }
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    return line
 
 
-def run_lqr_eq(args, rank, world, local_rank):
+def run_lqr_eq(args, rank, world, local_rank, emit=True):
     """--workload lqr_eq: 512 equality-constrained LQ problems, n=72, m=30,
     12 equality rows per stage, N=100 (mpxg_lqr_eq_solve_method; --lqr-method
     0: stage products on the tensor cores, 1: on the CUDA cores)."""
@@ -726,8 +758,9 @@ def run_lqr_eq(args, rank, world, local_rank):
                           "peak_source": "TF32 = half the measured bf16 dense rate (MEASURED_PEAKS.json bf16_tflops)",
                           "flops": "TF32 MMA work issued per stage (padded tiles, 3 MMAs per split product) = %d"
                                    % mma}
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def main():

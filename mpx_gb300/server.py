@@ -91,8 +91,11 @@ class MPCServer:
         self.streams = int(streams)
         self.episodes = {}     # key -> episode id
         self._m = {}           # key -> controls per result row
+        self._mi = {}          # key -> model index (order of `models`)
+        self.model_names = list(names)
         self._arrival = {}     # ticket -> (key, m, arrival time)
         self._t_arr = np.zeros(1 << 16)   # ticket -> arrival time (the vectorised poll_fast path)
+        self._t_mod = np.zeros(1 << 16, dtype=np.int8)  # ticket -> model index
         self.completed = []
         self._res = (_lib.Result * 4096)()
         self._res_np = np.frombuffer(self._res, dtype=np.dtype(
@@ -136,6 +139,7 @@ class MPCServer:
         self._check(st, "admit")
         self.episodes[episode] = eid.value
         self._m[episode] = pool.desc.m
+        self._mi[episode] = pool.index
         return eid.value
 
     def reset_slot(self, episode, x0=None):
@@ -157,16 +161,21 @@ class MPCServer:
         self._check(self.L.mpxg_submit(self.handle, self.episodes[episode], ctypes.byref(t)), "submit")
         a = time.perf_counter() if arrival is None else arrival
         self._arrival[t.value] = (episode, self._m[episode], a)
-        self._note_arrival(np.array([t.value]), np.array([a]))
+        self._note_arrival(np.array([t.value]), np.array([a]), np.array([self._mi[episode]], dtype=np.int8))
         return t.value
 
-    def _note_arrival(self, tickets, times):
+    def _note_arrival(self, tickets, times, models):
         top = int(tickets.max())
         if top >= self._t_arr.shape[0]:
-            grown = np.zeros(max(2 * self._t_arr.shape[0], top + 1))
+            size = max(2 * self._t_arr.shape[0], top + 1)
+            grown = np.zeros(size)
             grown[:self._t_arr.shape[0]] = self._t_arr
             self._t_arr = grown
+            gm = np.zeros(size, dtype=np.int8)
+            gm[:self._t_mod.shape[0]] = self._t_mod
+            self._t_mod = gm
         self._t_arr[tickets] = times
+        self._t_mod[tickets] = models
 
     def submit_many(self, episodes, arrival=None):
         """Queue the next tick of several episodes in one call; returns their tickets."""
@@ -179,7 +188,7 @@ class MPCServer:
         times = np.full(n, time.perf_counter()) if arrival is None else np.asarray(arrival, dtype=np.float64)
         for k, e in enumerate(episodes):
             self._arrival[int(t[k])] = (e, self._m[e], times[k])
-        self._note_arrival(t, times)
+        self._note_arrival(t, times, np.fromiter((self._mi[e] for e in episodes), dtype=np.int8, count=n))
         return t.tolist()
 
     def launch_pending(self):
@@ -220,13 +229,14 @@ class MPCServer:
         self.completed.extend(done)
         return done
 
-    def poll_fast(self, block=False):
+    def poll_fast(self, block=False, with_model=False):
         """poll() without per-result Python objects: returns (latency_s,
-        status, kkt) arrays of the ticks finished now (for high request
-        rates; the tickets' episodes are not reported)."""
+        status, kkt) arrays of the ticks finished now, and with_model their
+        model indices (order of `model_names`) as a fourth array (for high
+        request rates; the tickets' episodes are not reported)."""
         self._check(self.L.mpxg_server_step(self.handle, 1 if block else 0, None, None), "step")
         now = time.perf_counter()
-        lat, st, kk = [], [], []
+        lat, st, kk, md = [], [], [], []
         while True:
             cnt = ctypes.c_int()
             self._check(self.L.mpxg_server_completed(self.handle, self._res, len(self._res), ctypes.byref(cnt)),
@@ -236,11 +246,13 @@ class MPCServer:
             lat.append(now - self._t_arr[tk])
             st.append(r["status"].copy())
             kk.append(r["kkt"][:, 2].copy())
+            md.append(self._t_mod[tk])
             for t in tk.tolist():
                 self._arrival.pop(t, None)
             if cnt.value < len(self._res):
                 break
-        return np.concatenate(lat), np.concatenate(st), np.concatenate(kk)
+        out = (np.concatenate(lat), np.concatenate(st), np.concatenate(kk))
+        return out + (np.concatenate(md),) if with_model else out
 
     def drain(self):
         """Wait for every queued and running tick."""
@@ -256,9 +268,9 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
                     models=("quadruped", "biped"), v_range=(-0.5, 0.5)):
     """Poisson request stream (rate_hz) over `n_episodes` concurrent episodes
     of `episode_ticks` ticks; finished episodes are replaced by new ones.
-    Runs in real time; returns (latencies in s, wall time in s); the statuses
-    and KKT residuals of the completed ticks are left in server.last_status
-    and server.last_kkt."""
+    Runs in real time; returns (latencies in s, wall time in s); the statuses,
+    KKT residuals and model indices of the completed ticks are left in
+    server.last_status, server.last_kkt and server.last_model."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=int(rate_hz * duration_s * 1.2) + 16)
     arrivals = np.cumsum(gaps)
@@ -282,7 +294,7 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
         new_episode()
     t0 = time.perf_counter()
     i = 0
-    lat, stats, kkts = [], [], []
+    lat, stats, kkts, mods = [], [], [], []
     while True:
         now = time.perf_counter() - t0
         keys, arr = [], []
@@ -301,17 +313,18 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
             i += 1
         if keys:
             server.submit_many(keys, arr)
-        la, st, kk = server.poll_fast()
-        lat.append(la); stats.append(st); kkts.append(kk)
+        la, st, kk, md = server.poll_fast(with_model=True)
+        lat.append(la); stats.append(st); kkts.append(kk); mods.append(md)
         if i >= len(arrivals):
             q, r, _ = server.stats()
             if q == 0 and r == 0:
-                la, st, kk = server.poll_fast()
-                lat.append(la); stats.append(st); kkts.append(kk)
+                la, st, kk, md = server.poll_fast(with_model=True)
+                lat.append(la); stats.append(st); kkts.append(kk); mods.append(md)
                 break
     wall = time.perf_counter() - t0
     server.last_status = np.concatenate(stats) if stats else np.zeros(0, np.int32)
     server.last_kkt = np.concatenate(kkts) if kkts else np.zeros(0, np.float32)
+    server.last_model = np.concatenate(mods) if mods else np.zeros(0, np.int8)
     for ep, _ in eps:
         server.release(ep)
     return np.concatenate(lat) if lat else np.zeros(0), wall

@@ -65,6 +65,9 @@ def test_served_stream_reports_latency(cuda):
     assert len(lat) > 500
     assert np.all(np.isfinite(lat)) and np.percentile(lat, 99) < 1.0
     assert len(s.last_status) == len(lat) and not np.any(s.last_status & 1)
+    # both models served (alternating episodes), each result tagged with its model
+    assert len(s.last_model) == len(lat)
+    assert set(np.unique(s.last_model).tolist()) == {0, 1} and s.model_names == ["quadruped", "biped"]
 
 
 def test_c_poll_returns_each_result_once(cuda):
