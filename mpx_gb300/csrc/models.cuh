@@ -413,75 +413,6 @@ __device__ __forceinline__ float barrier_cost(const ModelConst& mc, const float*
   return acc;
 }
 
-// For control index a (0..NU-1): d(barrier cost)/du_a and column a of the
-// barrier's Hessian model restricted to the leg/foot that owns u_a:
-// hb[0..LEGDIM-1] are the rows of that leg's controls (leg index *leg).
-template <class M>
-__device__ __forceinline__ float sel3(const float* v, int c) { return c == 0 ? v[0] : (c == 1 ? v[1] : v[2]); }
-
-template <class M>
-__device__ __forceinline__ void barrier_lane(const ModelConst& mc, int a, const float* u, const float* ref, float* grad,
-                                             float* hb, int* leg) {
-  if (M::LEGS == 4) {
-    const int i = a / 3, comp = a - 3 * i;
-    *leg = i;
-    const float cont = ref[M::COFF + i];
-    const float mcost = mc.barrier_masked ? cont : 1.0f;
-    const float f[3] = {u[3 * i], u[3 * i + 1], u[3 * i + 2]};
-    float gc[3], hxx, hxy, hyy;
-    const float c = cone(mc.mu, f, gc, &hxx, &hxy, &hyy);
-    float v, g, h, cv;
-    barrier_terms(mc, c, mcost, cont, &v, &g, &h, &cv);
-    const float gcomp = sel3<M>(gc, comp);
-    *grad = g * gcomp;
-    hb[0] = h * gc[0] * gcomp;
-    hb[1] = h * gc[1] * gcomp;
-    hb[2] = h * gc[2] * gcomp;
-    // exact curvature of the cone (grad^2 c = -grad^2 s); zero for kind 0
-    if (comp == 0) { hb[0] += -cv * hxx; hb[1] += -cv * hxy; }
-    if (comp == 1) { hb[0] += -cv * hxy; hb[1] += -cv * hyy; }
-  } else {
-    const int i = a / 6, comp = a - 6 * i;
-    *leg = i;
-    const float cont = ref[M::COFF + i];
-    const float mcost = mc.barrier_masked ? cont : 1.0f;
-    const float hl = 0.5f * mc.foot_length, hw = 0.5f * mc.foot_width;
-    const float mz = mc.mu * 0.5f * fminf(mc.foot_length, mc.foot_width);
-    const float F[3] = {u[6 * i], u[6 * i + 1], u[6 * i + 2]};
-    const float T[3] = {u[6 * i + 3], u[6 * i + 4], u[6 * i + 5]};
-    float gc[3], hxx, hxy, hyy;
-    float cs[7];
-    cs[0] = cone(mc.mu, F, gc, &hxx, &hxy, &hyy);
-    cs[1] = hl * F[2] - T[1]; cs[2] = hl * F[2] + T[1];
-    cs[3] = hw * F[2] - T[0]; cs[4] = hw * F[2] + T[0];
-    cs[5] = mz * F[2] - T[2]; cs[6] = mz * F[2] + T[2];
-    // constraint gradients over the foot's 6 controls [Fx Fy Fz Tx Ty Tz]
-    const float G[7][6] = {{gc[0], gc[1], gc[2], 0.f, 0.f, 0.f},
-                           {0.f, 0.f, hl, 0.f, -1.f, 0.f}, {0.f, 0.f, hl, 0.f, 1.f, 0.f},
-                           {0.f, 0.f, hw, -1.f, 0.f, 0.f}, {0.f, 0.f, hw, 1.f, 0.f, 0.f},
-                           {0.f, 0.f, mz, 0.f, 0.f, -1.f}, {0.f, 0.f, mz, 0.f, 0.f, 1.f}};
-    float g_acc = 0.0f;
-#pragma unroll
-    for (int b = 0; b < 6; ++b) hb[b] = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-      float v, g, h, cv;
-      barrier_terms(mc, cs[k], mcost, cont, &v, &g, &h, &cv);
-      float gk = 0.0f;
-#pragma unroll
-      for (int b = 0; b < 6; ++b) gk = (b == comp) ? G[k][b] : gk;
-      g_acc += g * gk;
-#pragma unroll
-      for (int b = 0; b < 6; ++b) hb[b] += h * G[k][b] * gk;
-      if (k == 0) {
-        if (comp == 0) { hb[0] += -cv * hxx; hb[1] += -cv * hxy; }
-        if (comp == 1) { hb[0] += -cv * hxy; hb[1] += -cv * hyy; }
-      }
-    }
-    *grad = g_acc;
-  }
-}
-
 // Barrier terms of leg/foot `leg`: cost value (1/2 included), gradient over
 // the leg's LD controls and its LD x LD Hessian model (kind 0: the reference's
 // Gauss-Newton J^T diag(clip(B'')*contact) J; kind 1: exact second derivative).
