@@ -5,8 +5,9 @@
 // from the reference tree) runs four phases inside one warp:
 //
 //  1. linearise   lane = stage (32 stages at a time): dynamics Jacobian [A|B]
-//                 by forward-mode dual numbers with several tangents per pass,
-//                 defect c = f(x,u) - x+, stage cost, gradient, barrier blocks.
+//                 by forward-mode dual numbers with several tangents per pass
+//                 on the increment form f = x + d(x, u), defect
+//                 c = f(x,u) - x+, stage cost, gradient, barrier blocks.
 //                 Results go to the warp's scratch (L2-resident).
 //  2. backward    lane = column of the augmented stage matrix
 //                     H = G + F^T P F,   F = [A B c; 0 0 1]
@@ -19,6 +20,10 @@
 //                 through shared memory.
 //  4. merit       stage-parallel augmented-Lagrangian merit
 //                 phi = J + V.c + rho/2 |c|^2 with backtracking, then the step.
+//                 The Armijo test sums per-stage differences phi(alpha) - phi(0)
+//                 written without cancellation (dynamics increments kept from
+//                 phase 1), so that decreases far below float32's resolution
+//                 of phi itself are still resolved.
 #pragma once
 #include "models.cuh"
 
