@@ -78,10 +78,15 @@ struct TcLay {
   // the stage's Q (row-major) sits in region G behind gamma's B operand
   static constexpr uint32_t OFF_QS = OFF_G + 2u * SL3 * SJ;
   static_assert(2u * SL3 * SJ + (uint32_t)(NX * NX) * 4u <= BYTES_G, "Q must fit region G behind [K ; K_nu]");
-  // the next stage's raw A | B | c, copied into region F behind the float32 P
-  // while the elimination runs (region F is free between beta and gamma)
+  // the next stage's raw A | B | c | C | D | q | r | e (each 16-byte
+  // aligned), copied into region F behind the float32 P while the
+  // elimination runs (region F is free between beta and gamma)
+  static constexpr int r4(int v) { return (v + 3) / 4 * 4; }
+  static constexpr int RA = 0, RB = RA + r4(NX * NX), RC = RB + r4(NX * NU), RCC = RC + r4(NX),
+                       RD = RCC + r4(NE * NX), RQ = RD + r4(NE * NU), RR = RQ + r4(NX), RE = RR + r4(NU),
+                       RAW_FLOATS = RE + r4(NE);
   static constexpr uint32_t OFF_RAW = OFF_F + al128((uint32_t)(NX * (NX + 1) * 4));
-  static constexpr uint32_t RAW_BYTES = (uint32_t)(NX * NX + NX * NU + NX) * 4u;
+  static constexpr uint32_t RAW_BYTES = (uint32_t)RAW_FLOATS * 4u;
   static_assert(OFF_RAW + RAW_BYTES <= OFF_F + BYTES_F, "raw stage data must fit region F behind P");
   // asynchronous copies move 16-byte chunks: per-stage sizes must allow them
   static constexpr bool ASYNC_SIZES = (NX * NX * 4) % 16 == 0 && (NX * NU * 4) % 16 == 0 &&
@@ -116,18 +121,19 @@ __device__ __forceinline__ void tc_handoff() {
   tc::fence_after_sync();
 }
 
-// Global -> shared copy of one stage block by the whole block: 16-byte
-// asynchronous copies (completion per thread through commit groups) when
-// `async` (16-byte aligned source, size a multiple of 16 bytes), else plain
-// loads and stores.
-__device__ __forceinline__ void copy_async(float* dst, const float* src, int floats, bool async) {
-  if (async) {
-    const uint32_t d = tc::smem_u32(dst);
-    const char* g = reinterpret_cast<const char*>(src);
+// Asynchronous global -> shared copy of one stage block by the whole block
+// (completion per thread through commit groups): 16-byte chunks when `vec`
+// (16-byte aligned source and destination, size a multiple of 4 floats),
+// else 4-byte copies.
+__device__ __forceinline__ void copy_async(float* dst, const float* src, int floats, bool vec) {
+  const uint32_t d = tc::smem_u32(dst);
+  const char* g = reinterpret_cast<const char*>(src);
+  if (vec && (floats & 3) == 0) {
     for (int off = threadIdx.x * 16; off < floats * 4; off += kThreads * 16)
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + off), "l"(g + off) : "memory");
   } else {
-    for (int e = threadIdx.x; e < floats; e += kThreads) dst[e] = __ldg(src + e);
+    for (int off = threadIdx.x * 4; off < floats * 4; off += kThreads * 4)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d + off), "l"(g + off) : "memory");
   }
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -243,9 +249,9 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
   float* sM = reinterpret_cast<float*>(smraw + L::OFF_MR);
   float* sR = sM + NX * NU;
   float* sQ = reinterpret_cast<float*>(smraw + L::OFF_QS);
-  float* rawA = reinterpret_cast<float*>(smraw + L::OFF_RAW);
-  float* rawB = rawA + NX * NX;
-  float* rawc = rawB + NX * NU;
+  float* raw = reinterpret_cast<float*>(smraw + L::OFF_RAW);
+  float *rawA = raw + L::RA, *rawB = raw + L::RB, *rawc = raw + L::RC, *rawC = raw + L::RCC, *rawD = raw + L::RD;
+  float *rawq = raw + L::RQ, *rawr = raw + L::RR, *rawe = raw + L::RE;
   float *vq = s + L::vq, *vr = s + L::vr, *ve = s + L::ve, *vp = s + L::vp, *vqx = s + L::vqx, *vqu = s + L::vqu;
   float *vkn = s + L::vkn, *vk = s + L::vk, *vx = s + L::vx, *vu = s + L::vu;
   float* vt = s + L::vt;
@@ -305,11 +311,16 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     for (int i = tid; i < NX; i += kThreads) Pt[NX * NX + i] = vp[i];
   };
 
-  // the raw A | B | c of stage t into region F (asynchronous when aligned)
+  // the raw stage-t data into region F (16-byte chunks when aligned)
   auto copy_raw = [&](int t) {
     copy_async(rawA, io.A + (sn + t) * NX * NX, NX * NX, async);
     copy_async(rawB, io.Bm + (sn + t) * NX * NU, NX * NU, async);
     copy_async(rawc, io.c + (sn + t) * NX, NX, async);
+    copy_async(rawC, io.C + (sn + t) * NE * NX, NE * NX, async);
+    copy_async(rawD, io.D + (sn + t) * NE * NU, NE * NU, async);
+    copy_async(rawq, io.q + (sn1 + t) * NX, NX, async);
+    copy_async(rawr, io.r + (sn + t) * NU, NU, async);
+    copy_async(rawe, io.e + (sn + t) * NE, NE, async);
   };
 
   // L2 prefetch of one stage's matrices (128-byte lines over the block; only
@@ -367,6 +378,12 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
           v[it][j] = e >= FE ? 0.0f : (n < NX ? rawA[k * NX + n] : (n < NX + NU ? rawB[k * NU + n - NX] : rawc[k]));
         }
       }
+      // the equality blocks (column-major) and the vectors from the raw copy
+      for (int e = tid; e < NE * NX; e += kThreads) sC[(e % NX) * LE + e / NX] = rawC[e];
+      for (int e = tid; e < NE * NU; e += kThreads) sD[(e % NU) * LE + e / NU] = rawD[e];
+      for (int i = tid; i < NX; i += kThreads) vq[i] = rawq[i];
+      for (int i = tid; i < NU; i += kThreads) vr[i] = rawr[i];
+      for (int i = tid; i < NE; i += kThreads) ve[i] = rawe[i];
       __syncthreads();  // the slabs overwrite the raw copy
 #pragma unroll
       for (int it = 0; it < FIT; ++it) {
@@ -381,11 +398,6 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
           *reinterpret_cast<float4*>(Fl + o) = make_float4(l[0], l[1], l[2], l[3]);
         }
       }
-      load_cm<NE, NX>(sC, LE, io.C + (sn + t) * NE * NX);
-      load_cm<NE, NU>(sD, LE, io.D + (sn + t) * NE * NU);
-      load_vec<NX>(vq, io.q + (sn1 + t) * NX);
-      load_vec<NU>(vr, io.r + (sn + t) * NU);
-      load_vec<NE>(ve, io.e + (sn + t) * NE);
     }
     tc_handoff();
     // ---- alpha: D1 = P [A | B | c]
@@ -596,7 +608,8 @@ inline cudaError_t launch_lqr_eq_tc(cudaStream_t st, const mpxg_lq_eq_io& io) {
   if (e != cudaSuccess) return e;
   auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
   const bool async = TcLay<NX, NU, NE>::ASYNC_SIZES && al16(io.M) && al16(io.R) && al16(io.Q) && al16(io.A) &&
-                     al16(io.Bm) && al16(io.c);
+                     al16(io.Bm) && al16(io.c) && al16(io.C) && al16(io.D) && al16(io.q) && al16(io.r) &&
+                     al16(io.e);
   lqr_eq_tc_kernel<NX, NU, NE><<<io.batch, kThreads, smem, st>>>(io, io.workspace, async);
   return cudaGetLastError();
 }

@@ -59,9 +59,9 @@ def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B, method):
 
 
 def test_lqr_eq_tensor_cores_unaligned_inputs(cuda):
-    """Inputs at addresses that are not 16-byte aligned take the plain-copy
-    path of the tensor-core kernel (no asynchronous 16-byte copies) and give
-    the same result bit for bit."""
+    """Inputs at addresses that are not 16-byte aligned take the 4-byte copy
+    path of the tensor-core kernel (no 16-byte asynchronous copies, no L2
+    prefetch) and give the same result bit for bit."""
     import ctypes
     from mpx_gb300 import _lib
     from mpx_gb300.solver import _ptr, lqr_eq_solve
