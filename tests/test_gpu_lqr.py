@@ -92,3 +92,22 @@ def test_lqr_eq_tensor_cores_unaligned_inputs(cuda):
     torch.cuda.synchronize()
     for k in out:
         assert torch.equal(out[k], ref[k]), k
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_lqr_eq_two_waves(cuda, method):
+    """300 problems (two waves of one block per SM): sampled problems from
+    both waves match the FP64 oracle like a small batch does."""
+    from mpx_gb300.solver import lqr_eq_solve
+    from oracle.lqr_eq import riccati_eq
+    n, m, ne, N, B = 16, 8, 4, 10, 300
+    d = P.random_lq_eq(B, n=n, m=m, n_eq=ne, N=N, seed=5)
+    keys = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+    g = lqr_eq_solve(*[d[k] for k in keys], method=method)
+    torch.cuda.synchronize()
+    for b in (0, 151, 152, 299):
+        o = riccati_eq(*[d[k][b] for k in keys])
+        for k in ("K", "k", "X", "U", "lam", "nu"):
+            a = g[k][b].cpu().numpy()
+            e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
+            assert e < 2e-4, (k, b, e)
