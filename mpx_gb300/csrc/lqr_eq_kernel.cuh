@@ -10,12 +10,14 @@
 //   Z = Q_uu^-1 Q_ux, g = Q_uu^-1 q_u, W = Q_uu^-1 D', S = D W,
 //   K_nu = S^-1 (C - D Z), k_nu = -S^-1 (D g + e), K = -(Z + W K_nu), k = -(g + W k_nu),
 //   P <- Q_xx + Q_ux'K + C'K_nu,  p <- q_x + Q_ux'k + C'k_nu   (D K = -C).
-// GB300 mapping: one 256-thread block per problem; all stage matrices live in
-// shared memory column-major with odd leading dimensions (~147 KB for
-// n = 72); products are 16 x 16-thread register-tiled block products, the
-// m x m and p x p factorisations are warp Cholesky, the solves one thread per
-// right-hand side.  CUDA-core FP32: the FP32 accuracy the tests ask for would
-// need split-TF32 tensor-core products (three MMAs per product).
+// GB300 mapping (the CUDA-core kernel, method 1 of mpxg_lqr_eq_solve_method;
+// lqr_eq_tc.cuh puts the stage products on the tensor cores): one 256-thread
+// block per problem; all stage matrices live in shared memory column-major
+// with odd leading dimensions (~152 KB for n = 72); products are 16 x
+// 16-thread register-tiled block products; the eliminations with Q_uu and S
+// are column-parallel block Gauss-Jordan solves (4 x 4 Cholesky pivots, a
+// thread per right-hand side), shared with the tensor-core kernel, as are the
+// forward sweep and the costates below.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -87,42 +89,88 @@ __device__ __forceinline__ void bmv(float* out, const float* X, int ldx, const f
   __syncthreads();
 }
 
-// Inverse of an N x N symmetric positive definite matrix by warp 0 (N <= 32):
-// Gauss-Jordan on [S | I] with columns lane and lane + 32 in registers.  `out`
-// may alias S (every read precedes every write).
-template <int N>
-__device__ __forceinline__ void spd_inverse(const float* S, int lds, float* out, int ldo) {
-  static_assert(N <= 32, "spd_inverse: pivots on one warp");
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x, j0 = lane, j1 = lane + 32;
-    float c0[N], c1[N];
+// Solve S X = Y for a symmetric positive definite S (R x R) by block
+// Gauss-Jordan over the augmented [S | Y] (NCOL columns), one thread per
+// column, the column in registers.  Pivots are taken four at a time: the
+// owners of the block's columns publish them (double-buffered panel, one
+// barrier per block), and every later column solves the 4 x 4 pivot block
+// D y = v[block] by Cholesky, then v[i] -= panel[i] . y off the block and
+// v[block] = y.  load(j, v) fills column j; store(j, v) receives the solution
+// columns j >= R.  panel: 2 x 32 x 4 floats of shared memory (row i's four
+// pivot-column entries contiguous, one 16-byte broadcast per row).
+template <int R, int NCOL, class Load, class Store>
+__device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
+  static_assert(R <= 32 && NCOL <= kThreads, "pivots within 32 rows, one thread per column");
+  const int j = threadIdx.x;
+  float v[R];
+  if (j < NCOL) load(j, v);
 #pragma unroll
-    for (int r = 0; r < N; ++r) {
-      c0[r] = j0 < N ? S[j0 * lds + r] : (j0 < 2 * N && j0 - N == r ? 1.0f : 0.0f);
-      c1[r] = j1 < N ? S[j1 * lds + r] : (j1 < 2 * N && j1 - N == r ? 1.0f : 0.0f);
+  for (int b0 = 0; b0 < R; b0 += 4) {
+    constexpr int B4 = 4;
+    const int bs = (R - b0) < B4 ? (R - b0) : B4;
+    float* pb = panel + ((b0 / 4) & 1) * 4 * 32;
+    if (j >= b0 && j < b0 + bs) {
+#pragma unroll
+      for (int i = 0; i < R; ++i) pb[i * 4 + (j - b0)] = v[i];
     }
-    __syncwarp();
+    __syncthreads();
+    if (j >= b0 + bs && j < NCOL) {
+      // pivot block D(r, k) = pb[(b0 + r) * 4 + k]; Cholesky D = L L'
+      float Lm[4][4], il[4], y[4];
 #pragma unroll
-    for (int p = 0; p < N; ++p) {
-      float pc[N];
+      for (int r = 0; r < 4; ++r) {
+        if (r >= bs) continue;
+        const float4 dr = *reinterpret_cast<const float4*>(pb + (b0 + r) * 4);
+        const float drv[4] = {dr.x, dr.y, dr.z, dr.w};
 #pragma unroll
-      for (int r = 0; r < N; ++r) pc[r] = __shfl_sync(0xffffffffu, c0[r], p);
-      float d = pc[p];
-      if (!(d > 0.0f)) d = fmaxf(fabsf(d), 1e-30f);
-      const float inv = 1.0f / d;
-      const float v0 = c0[p] * inv, v1 = c1[p] * inv;
+        for (int k = 0; k <= r; ++k) {
+          float a = drv[k];
 #pragma unroll
-      for (int r = 0; r < N; ++r) {
-        c0[r] = (r == p) ? v0 : c0[r] - pc[r] * v0;
-        c1[r] = (r == p) ? v1 : c1[r] - pc[r] * v1;
+          for (int q = 0; q < k; ++q) a -= Lm[r][q] * Lm[k][q];
+          if (k == r) {
+            if (!(a > 0.0f)) a = fmaxf(fabsf(a), 1e-30f);
+            il[r] = rsqrtf(a);
+            Lm[r][r] = a * il[r];
+          } else {
+            Lm[r][k] = a * il[k];
+          }
+        }
       }
-    }
+      // y = D^-1 v[block]: L z = v, L' y = z
 #pragma unroll
-    for (int r = 0; r < N; ++r) {
-      if (j0 >= N && j0 < 2 * N) out[(j0 - N) * ldo + r] = c0[r];
-      if (j1 >= N && j1 < 2 * N) out[(j1 - N) * ldo + r] = c1[r];
+      for (int r = 0; r < 4; ++r) {
+        if (r >= bs) continue;
+        float a = v[b0 + r];
+#pragma unroll
+        for (int q = 0; q < r; ++q) a -= Lm[r][q] * y[q];
+        y[r] = a * il[r];
+      }
+#pragma unroll
+      for (int r = 3; r >= 0; --r) {
+        if (r >= bs) continue;
+        float a = y[r];
+#pragma unroll
+        for (int q = r + 1; q < 4; ++q)
+          if (q < bs) a -= Lm[q][r] * y[q];
+        y[r] = a * il[r];
+      }
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        if (i >= b0 && i < b0 + bs) continue;
+        const float4 pr = *reinterpret_cast<const float4*>(pb + i * 4);
+        const float prv[4] = {pr.x, pr.y, pr.z, pr.w};
+        float a = v[i];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < bs) a -= prv[k] * y[k];
+        v[i] = a;
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (r < bs) v[b0 + r] = y[r];
     }
   }
+  if (j >= R && j < NCOL) store(j, v);
   __syncthreads();
 }
 
@@ -151,13 +199,17 @@ template <int NX, int NU, int NE>
 struct Lay {
   static constexpr int LX = NX + (NX % 2 == 0 ? 1 : 2), LU = NU + (NU % 2 == 0 ? 1 : 2),
                        LE = NE + (NE % 2 == 0 ? 1 : 2);
+  // ZW: the solution [Z | g | W] of Q_uu [Z | g | W] = [Q_ux | q_u | D'];
+  // TS: D [Z | g | W]; KK: [K_nu | k_nu]; PAN: the Gauss-Jordan pivot panel
+  static constexpr int NZW = NX + 1 + NE;
   static constexpr int P = 0, A = P + NX * LX, PA = A + NX * LX, Q = PA + NX * LX, B = Q + NX * LX, PB = B + NU * LX,
-                       M = PB + NU * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, Z = QUX + NX * LU, W = Z + NX * LU,
-                       C = W + NE * LU, D = C + NX * LE, S = D + NU * LE, T = S + NE * LE, V = T + NX * LE;
+                       M = PB + NU * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, ZW = QUX + NX * LU,
+                       C = ZW + NZW * LU, D = C + NX * LE, TS = D + NU * LE, KK = TS + NZW * LE,
+                       PAN = (KK + (NX + 1) * LE + 3) / 4 * 4, V = PAN + 2 * 4 * 32;
   // vectors, NX + 4 floats each
   static constexpr int VL = NX + 4;
   static constexpr int vc = V, vq = vc + VL, vr = vq + VL, ve = vr + VL, vw = ve + VL, vp = vw + VL, vqx = vp + VL,
-                       vqu = vqx + VL, vg = vqu + VL, vh = vg + VL, vkn = vh + VL, vk = vkn + VL, vx = vk + VL,
+                       vqu = vqx + VL, vkn = vqu + VL, vk = vkn + VL, vx = vk + VL,
                        vu = vx + VL, FLOATS = vu + VL;
 };
 
@@ -316,10 +368,10 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_kernel(mpxg_lq_eq_io io, f
   extern __shared__ float4 smem4[];
   float* s = reinterpret_cast<float*>(smem4);
   float *P = s + L::P, *sA = s + L::A, *PA = s + L::PA, *sQ = s + L::Q, *sB = s + L::B, *PB = s + L::PB;
-  float *sM = s + L::M, *Quu = s + L::QUU, *Qux = s + L::QUX, *Z = s + L::Z, *W = s + L::W, *sC = s + L::C;
-  float *sD = s + L::D, *S = s + L::S, *T = s + L::T;
+  float *sM = s + L::M, *Quu = s + L::QUU, *Qux = s + L::QUX, *ZW = s + L::ZW, *sC = s + L::C;
+  float *sD = s + L::D, *TS = s + L::TS, *KK = s + L::KK, *pan = s + L::PAN;
   float *vc = s + L::vc, *vq = s + L::vq, *vr = s + L::vr, *ve = s + L::ve, *vw = s + L::vw, *vp = s + L::vp;
-  float *vqx = s + L::vqx, *vqu = s + L::vqu, *vg = s + L::vg, *vh = s + L::vh, *vkn = s + L::vkn, *vk = s + L::vk;
+  float *vqx = s + L::vqx, *vqu = s + L::vqu, *vkn = s + L::vkn, *vk = s + L::vk;
   float *vx = s + L::vx, *vu = s + L::vu;
   const int b = blockIdx.x, N = io.N, tid = threadIdx.x;
   constexpr int NP = NX + 1;  // workspace rows per stage: P (NX x NX) then p
@@ -357,39 +409,47 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_kernel(mpxg_lq_eq_io io, f
     bmm<NU, NX, NU, true, false, false>(Quu, LU, sB, LX, PB, LX, 1.0f, Quu, LU);      // Q_uu = R + B'PB
     bmv<NX, NX, true>(vqx, sA, LX, vw, 1.0f, vq);                                     // q_x
     bmv<NU, NX, true>(vqu, sB, LX, vw, 1.0f, vr);                                     // q_u
-    // ---- G = Q_uu^-1 (into PB); Z = G Q_ux, g = G q_u, W = G D'
-    float* G = PB;
-    spd_inverse<NU>(Quu, LU, G, LU);
-    bmm<NU, NU, NX, false, false, false>(Z, LU, G, LU, Qux, LU, 1.0f, nullptr, 0);
-    bmv<NU, NU, false>(vg, G, LU, vqu, 1.0f, nullptr);
-    bmm<NU, NU, NE, false, true, false>(W, LU, G, LU, sD, LE, 1.0f, nullptr, 0);
-    // ---- S = D W, T = C - D Z, h = D g + e
-    bmm<NE, NU, NE, false, false, false>(S, LE, sD, LE, W, LU, 1.0f, nullptr, 0);
-    bmm<NE, NU, NX, false, false, false>(T, LE, sD, LE, Z, LU, -1.0f, sC, LE);
-    bmv<NE, NU, false>(vh, sD, LE, vg, 1.0f, ve);
-    // ---- K_nu = S^-1 T (into M's buffer), k_nu = -S^-1 h
-    spd_inverse<NE>(S, LE, S, LE);
-    float* Kn = sM;
-    bmm<NE, NE, NX, false, false, false>(Kn, LE, S, LE, T, LE, 1.0f, nullptr, 0);
-    bmv<NE, NE, false>(vkn, S, LE, vh, -1.0f, nullptr);
-    // ---- Z <- Z + W K_nu (K = -Z), g <- g + W k_nu (k = -g)
-    bmm<NU, NE, NX, false, false, false>(Z, LU, W, LU, Kn, LE, 1.0f, Z, LU);
-    bmv<NU, NE, false>(vg, W, LU, vkn, 1.0f, vg);
+    // ---- elimination, two column-parallel block Gauss-Jordan solves:
+    //   Q_uu [Z | g | W] = [Q_ux | q_u | D'];
+    //   [S | T | h] = [D W | C - D Z | D g + e],  S [K_nu | -k_nu] = [T | h];
+    //   Z += W K_nu (K = -Z), g += W k_nu (k = -g)
+    gj_solve<NU, NU + L::NZW>(pan, [&](int j, float* v) {
+#pragma unroll
+      for (int i = 0; i < NU; ++i)
+        v[i] = j < NU ? Quu[j * LU + i]
+                      : (j < NU + NX ? Qux[(j - NU) * LU + i]
+                                     : (j == NU + NX ? vqu[i] : sD[i * LE + (j - NU - NX - 1)]));
+    }, [&](int j, const float* v) {
+#pragma unroll
+      for (int i = 0; i < NU; ++i) ZW[(j - NU) * LU + i] = v[i];
+    });
+    bmm<NE, NU, L::NZW, false, false, false>(TS, LE, sD, LE, ZW, LU, 1.0f, nullptr, 0);
+    gj_solve<NE, NE + NX + 1>(pan, [&](int j, float* v) {
+#pragma unroll
+      for (int i = 0; i < NE; ++i)
+        v[i] = j < NE ? TS[(NX + 1 + j) * LE + i]
+                      : (j < NE + NX ? sC[(j - NE) * LE + i] - TS[(j - NE) * LE + i] : TS[NX * LE + i] + ve[i]);
+    }, [&](int j, const float* v) {
+      const float sg = (j == NE + NX) ? -1.0f : 1.0f;
+#pragma unroll
+      for (int i = 0; i < NE; ++i) KK[(j - NE) * LE + i] = sg * v[i];
+    });
+    bmm<NU, NE, NX + 1, false, false, false>(ZW, LU, ZW + (NX + 1) * LU, LU, KK, LE, 1.0f, ZW, LU);
     // ---- gains out
     {
       float* Ko = io.K + (sn + t) * NU * NX;
       float* ko = io.k + (sn + t) * NU;
       float* Kno = io.Knu + (sn + t) * NE * NX;
       float* kno = io.knu + (sn + t) * NE;
-      for (int e = tid; e < NU * NX; e += kThreads) Ko[e] = -Z[(e % NX) * LU + e / NX];
-      for (int e = tid; e < NE * NX; e += kThreads) Kno[e] = Kn[(e % NX) * LE + e / NX];
-      for (int a = tid; a < NU; a += kThreads) { vk[a] = -vg[a]; ko[a] = -vg[a]; }
-      for (int j = tid; j < NE; j += kThreads) kno[j] = vkn[j];
+      for (int e = tid; e < NU * NX; e += kThreads) Ko[e] = -ZW[(e % NX) * LU + e / NX];
+      for (int e = tid; e < NE * NX; e += kThreads) Kno[e] = KK[(e % NX) * LE + e / NX];
+      for (int a = tid; a < NU; a += kThreads) { vk[a] = -ZW[NX * LU + a]; ko[a] = -ZW[NX * LU + a]; }
+      for (int j = tid; j < NE; j += kThreads) { vkn[j] = KK[NX * LE + j]; kno[j] = KK[NX * LE + j]; }
     }
     __syncthreads();
     // ---- P <- Q_xx - Q_ux' Z + C' K_nu,  p <- q_x + Q_ux' k + C' k_nu
-    bmm<NX, NU, NX, true, false, false>(P, LX, Qux, LU, Z, LU, -1.0f, sQ, LX);
-    bmm<NX, NE, NX, true, false, false>(P, LX, sC, LE, Kn, LE, 1.0f, P, LX);
+    bmm<NX, NU, NX, true, false, false>(P, LX, Qux, LU, ZW, LU, -1.0f, sQ, LX);
+    bmm<NX, NE, NX, true, false, false>(P, LX, sC, LE, KK, LE, 1.0f, P, LX);
     bmv<NX, NU, true>(vp, Qux, LU, vk, 1.0f, vqx);
     bmv<NX, NE, true>(vp, sC, LE, vkn, 1.0f, vp);
     for (int e = tid; e < NX * NX; e += kThreads) {  // symmetrise into PA, copy back

@@ -140,91 +140,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_older() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Solve S X = Y for a symmetric positive definite S (R x R) by block
-// Gauss-Jordan over the augmented [S | Y] (NCOL columns), one thread per
-// column, the column in registers.  Pivots are taken four at a time: the
-// owners of the block's columns publish them (double-buffered panel, one
-// barrier per block), and every later column solves the 4 x 4 pivot block
-// D y = v[block] by Cholesky, then v[i] -= panel[i] . y off the block and
-// v[block] = y.  load(j, v) fills column j; store(j, v) receives the solution
-// columns j >= R.  panel: 2 x 32 x 4 floats of shared memory (row i's four
-// pivot-column entries contiguous, one 16-byte broadcast per row).
-template <int R, int NCOL, class Load, class Store>
-__device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
-  static_assert(R <= 32 && NCOL <= kThreads, "pivots within 32 rows, one thread per column");
-  const int j = threadIdx.x;
-  float v[R];
-  if (j < NCOL) load(j, v);
-#pragma unroll
-  for (int b0 = 0; b0 < R; b0 += 4) {
-    constexpr int B4 = 4;
-    const int bs = (R - b0) < B4 ? (R - b0) : B4;
-    float* pb = panel + ((b0 / 4) & 1) * 4 * 32;
-    if (j >= b0 && j < b0 + bs) {
-#pragma unroll
-      for (int i = 0; i < R; ++i) pb[i * 4 + (j - b0)] = v[i];
-    }
-    __syncthreads();
-    if (j >= b0 + bs && j < NCOL) {
-      // pivot block D(r, k) = pb[(b0 + r) * 4 + k]; Cholesky D = L L'
-      float Lm[4][4], il[4], y[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        if (r >= bs) continue;
-        const float4 dr = *reinterpret_cast<const float4*>(pb + (b0 + r) * 4);
-        const float drv[4] = {dr.x, dr.y, dr.z, dr.w};
-#pragma unroll
-        for (int k = 0; k <= r; ++k) {
-          float a = drv[k];
-#pragma unroll
-          for (int q = 0; q < k; ++q) a -= Lm[r][q] * Lm[k][q];
-          if (k == r) {
-            if (!(a > 0.0f)) a = fmaxf(fabsf(a), 1e-30f);
-            il[r] = rsqrtf(a);
-            Lm[r][r] = a * il[r];
-          } else {
-            Lm[r][k] = a * il[k];
-          }
-        }
-      }
-      // y = D^-1 v[block]: L z = v, L' y = z
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        if (r >= bs) continue;
-        float a = v[b0 + r];
-#pragma unroll
-        for (int q = 0; q < r; ++q) a -= Lm[r][q] * y[q];
-        y[r] = a * il[r];
-      }
-#pragma unroll
-      for (int r = 3; r >= 0; --r) {
-        if (r >= bs) continue;
-        float a = y[r];
-#pragma unroll
-        for (int q = r + 1; q < 4; ++q)
-          if (q < bs) a -= Lm[q][r] * y[q];
-        y[r] = a * il[r];
-      }
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        if (i >= b0 && i < b0 + bs) continue;
-        const float4 pr = *reinterpret_cast<const float4*>(pb + i * 4);
-        const float prv[4] = {pr.x, pr.y, pr.z, pr.w};
-        float a = v[i];
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (k < bs) a -= prv[k] * y[k];
-        v[i] = a;
-      }
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-        if (r < bs) v[b0 + r] = y[r];
-    }
-  }
-  if (j >= R && j < NCOL) store(j, v);
-  __syncthreads();
-}
-
 template <int NX, int NU, int NE>
 __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io, float* Pscr, bool async) {
   typedef TcLay<NX, NU, NE> L;

@@ -32,7 +32,9 @@ def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B, method):
     """Equality-constrained LQR on the GPU against the FP64 stagewise Riccati
     (itself checked against a dense KKT solve on the CPU): method 0 with the
     stage products on the tensor cores (split TF32), method 1 on the CUDA
-    cores."""
+    cores.  Bound: 2e-4 relative, or 8x the error of the oracle's own float32
+    run where the problem's conditioning puts float32 itself near that (the
+    N = 1 case: ~3e-5)."""
     from mpx_gb300.solver import lqr_eq_solve
     from oracle.lqr_eq import riccati_eq
     d = P.random_lq_eq(B, n=n, m=m, n_eq=ne, N=N, seed=n + N)
@@ -45,10 +47,12 @@ def test_lqr_eq_matches_oracle(cuda, n, m, ne, N, B, method):
     torch.cuda.synchronize()
     for b in range(B):
         o = riccati_eq(*[d[k][b] for k in keys])
+        o32 = riccati_eq(*[d[k][b] for k in keys], dtype=np.float32)
         for k in ("K", "k", "Knu", "knu", "X", "U", "lam", "nu"):
             a = g[k][b].cpu().numpy()
             e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
-            assert e < 2e-4, (k, b, e)
+            e32 = np.abs(o32[k] - o[k]).max() / np.abs(o[k]).max()
+            assert e < max(2e-4, 8.0 * e32), (k, b, e, e32)
         # constraint residual of the GPU trajectory, relative to the size of
         # the terms it balances (sum |C x| + sum |D u| + |e| per row)
         X, U = g["X"][b].cpu().double().numpy(), g["U"][b].cpu().double().numpy()
@@ -97,7 +101,9 @@ def test_lqr_eq_tensor_cores_unaligned_inputs(cuda):
 @pytest.mark.parametrize("method", [0, 1])
 def test_lqr_eq_two_waves(cuda, method):
     """300 problems (two waves of one block per SM): sampled problems from
-    both waves match the FP64 oracle like a small batch does."""
+    both waves match the FP64 oracle within 2e-4, or within 8x the error of
+    the oracle's own float32 run where a problem's conditioning puts float32
+    itself near that bound."""
     from mpx_gb300.solver import lqr_eq_solve
     from oracle.lqr_eq import riccati_eq
     n, m, ne, N, B = 16, 8, 4, 10, 300
@@ -107,7 +113,9 @@ def test_lqr_eq_two_waves(cuda, method):
     torch.cuda.synchronize()
     for b in (0, 151, 152, 299):
         o = riccati_eq(*[d[k][b] for k in keys])
+        o32 = riccati_eq(*[d[k][b] for k in keys], dtype=np.float32)
         for k in ("K", "k", "X", "U", "lam", "nu"):
             a = g[k][b].cpu().numpy()
             e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
-            assert e < 2e-4, (k, b, e)
+            e32 = np.abs(o32[k] - o[k]).max() / np.abs(o[k]).max()
+            assert e < max(2e-4, 8.0 * e32), (k, b, e, e32)
