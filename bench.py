@@ -366,6 +366,28 @@ def run_ours(args, rank, world, local_rank):
                                 "what": "one launch of one instance (%d launches timed)" % nl}}
         tp.solver.close()
 
+    # ---------------- vector-Jacobian product of the converged 4096-instance solve
+    vjp = None
+    if not args.profile:
+        sx, sX, sU, sV = tr.x0.clone(), tr.X.clone(), tr.U.clone(), tr.V.clone()
+        gen = torch.Generator(device=dev).manual_seed(5)
+        gX = torch.randn(sX.shape, generator=gen, device=dev)
+        gU = torch.randn(sU.shape, generator=gen, device=dev)
+        vst = torch.cuda.current_stream()
+        tr.solver.vjp(sx, sX, sU, sV, tr.ref, tr.par, tr.w, gX, gU, tr.horizon, stream=vst)  # warm-up
+        torch.cuda.synchronize()
+        va, vb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        va.record(vst)
+        for _ in range(10):
+            vout = tr.solver.vjp(sx, sX, sU, sV, tr.ref, tr.par, tr.w, gX, gU, tr.horizon, stream=vst)
+        vb.record(vst)
+        torch.cuda.synchronize()
+        vms = va.elapsed_time(vb) / 10
+        vjp = {"ms_per_batch": vms, "instances_per_s": B / (vms / 1000.0),
+               "what": "mpxg_solve_vjp on the converged %d-instance tick: gradients w.r.t. x0 and the reference "
+                       "for random cotangents of X, U (one adjoint LQR per instance)" % B,
+               "finite": bool(torch.isfinite(vout["gx0"]).all().item())}
+
     # ---------------- the same batch with every horizon N = 50
     n50 = None
     if not args.no_n50 and not args.profile:
@@ -490,6 +512,7 @@ def run_ours(args, rank, world, local_rank):
                  "frac": flops / (solve_avg / 1000.0) / 1e12 / fp32_nominal,
                  "flops": "work-efficient Riccati count per stage per iteration"},
         "n50": n50,
+        "vjp": vjp,
         "served": served,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

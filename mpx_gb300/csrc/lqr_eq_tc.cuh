@@ -9,21 +9,24 @@
 //   beta   D2 = [A | B | c]' [P A | P B | P c + p]   ((n+m+1) x n)(n x (n+m+1))
 //          -> Q_xx - Q, Q_ux - M', Q_uu - R, q_x - q, q_u - r in one product
 //   gamma  D2[0:n, 0:n] += [Q_ux' | C'] [K ; K_nu]   (n x (m+p))((m+p) x n)
-// and P = D2[0:n, 0:n] + Q, symmetrised.  The m x m and p x p inverses, the
-// small products of the elimination (Z, W, S, T, K_nu) and p stay on the
-// CUDA cores.  The stage's cost blocks (M, R, Q) are added to the raw
-// accumulators in coalesced passes, and the next stage's matrices are
-// prefetched into L2 while this one computes.  One 256-thread block per problem: thread 0 issues each product's
-// MMAs and commits them to an mbarrier; the eight warps read the
+// and P = D2[0:n, 0:n] + Q, symmetrised.  The eliminations with Q_uu and S
+// (column-parallel block Gauss-Jordan solves, shared with the CUDA-core
+// kernel), the small products of the elimination and p stay on the CUDA
+// cores.  The stage's cost blocks (M, R, Q) are added to the raw
+// accumulators, and every stage input arrives by cp.async while the previous
+// stage computes.  One 256-thread block per problem: thread 0 issues each
+// product's MMAs and commits them to an mbarrier; the eight warps read the
 // accumulators back (warp w: lanes 32 (w % 4) .., column groups w / 4, + 2).
 //
-// Shared memory (n = 72, m = 30, p = 12: 204 KB) holds the operands in the
+// Shared memory (n = 72, m = 30, p = 12: ~219 KB) holds the operands in the
 // slab layout of tc_tf32.cuh, each as a TF32 hi and lo copy:
 //   region P: P (alpha's A operand), later [Q_ux' | C'] (gamma's A operand);
 //   region F: [A | B | c] as rows (alpha's B operand and beta's A operand),
-//             later the float32 P - Q before symmetrisation;
-//   region G: [PA | PB | Pc + p] as rows (beta's B operand), later [K ; K_nu];
-//   then the column-major blocks and vectors of the elimination.
+//             later the float32 P - Q before symmetrisation, and behind it
+//             the next stage's raw inputs;
+//   region G: [PA | PB | Pc + p] as rows (beta's B operand), later [K ; K_nu]
+//             and the stage's Q;
+//   then the column-major blocks and vectors of the elimination, M and R.
 // The forward sweep and the costates are the CUDA-core code of
 // lqr_eq_kernel.cuh over the same buffers.
 #pragma once
