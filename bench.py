@@ -473,6 +473,10 @@ def run_ours(args, rank, world, local_rank):
                "sample": "%d solves (the %d-instance tick-0 batch, repeated) in %.1f s: 5 SQP iterations, FP32 "
                          "oracle (C++, -O3), OpenMP over instances" % (done, B, dt),
                "host": host_info()}
+        # secondary figure: the same port on one thread
+        v1, dt1, done1 = cpu_bounded(wl, 1, 3.0)
+        cpu["single_thread"] = {"value": v1, "unit": "solves/s", "cores": 1,
+                                "sample": "%d solves in %.1f s, one thread" % (done1, dt1)}
 
     # ---------------- roofline of the solve kernel
     import json as _json
