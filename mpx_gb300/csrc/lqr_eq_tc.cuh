@@ -180,7 +180,10 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
   float* Ps = Pscr + (size_t)b * (N + 1) * NP * NX;
   const size_t sn = (size_t)b * N, sn1 = (size_t)b * (N + 1);
 
-  // ---- tensor memory (D1: columns 0.., D2: columns 128..) and the mbarrier
+  // ---- tensor memory (D1: columns 0.., D2: columns 128..) and the mbarrier.
+  // The allocation cannot wait on another block: ~219 KB of shared memory
+  // keeps one block of this kernel per SM, 256 of the SM's 512 columns are
+  // taken, and no other kernel of the library uses tensor memory.
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), 256);
   if (tid == 0) {
     tc::mbar_init(tc::smem_u32(bar), 1);
