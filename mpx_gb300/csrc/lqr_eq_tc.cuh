@@ -496,9 +496,11 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
   }
 
   // ---- release tensor memory (after a failed wait, first give the MMAs in
-  // flight a bounded time to finish)
+  // flight a bounded time to finish, and let this thread's asynchronous
+  // copies land before the block can exit)
   if (!ok) {
     tc::mbar_wait(barp, (phase - 1u) & 1u, 1 << 22);
+    cp_async_wait_all();
     __syncthreads();
   }
   tc::fence_before_sync();
