@@ -91,37 +91,42 @@ __device__ __forceinline__ void bmv(float* out, const float* X, int ldx, const f
 
 // Solve S X = Y for a symmetric positive definite S (R x R) by block
 // Gauss-Jordan over the augmented [S | Y] (NCOL columns), one thread per
-// column, the column in registers.  Pivots are taken four at a time: the
-// owners of the block's columns publish them (double-buffered panel, one
-// barrier per block), and every later column solves the 4 x 4 pivot block
-// D y = v[block] by Cholesky, then v[i] -= panel[i] . y off the block and
-// v[block] = y.  load(j, v) fills column j; store(j, v) receives the solution
-// columns j >= R.  panel: 2 x 32 x 4 floats of shared memory (row i's four
-// pivot-column entries contiguous, one 16-byte broadcast per row).
-template <int R, int NCOL, class Load, class Store>
+// column, the column in registers.  Pivots are taken BS at a time (BS a
+// multiple of 4): the owners of the block's columns publish them
+// (double-buffered panel, one barrier per block), and every later column
+// solves the BS x BS pivot block D y = v[block] by Cholesky, then
+// v[i] -= panel[i] . y off the block and v[block] = y.  load(j, v) fills
+// column j; store(j, v) receives the solution columns j >= R.  panel:
+// 2 x 32 x BS floats of shared memory, 16-byte aligned (row i's BS
+// pivot-column entries contiguous, read as 16-byte broadcasts).
+template <int R, int NCOL, int BS = 4, class Load, class Store>
 __device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
   static_assert(R <= 32 && NCOL <= kThreads, "pivots within 32 rows, one thread per column");
+  static_assert(BS % 4 == 0, "pivot blocks of a multiple of 4");
   const int j = threadIdx.x;
   float v[R];
   if (j < NCOL) load(j, v);
 #pragma unroll
-  for (int b0 = 0; b0 < R; b0 += 4) {
-    constexpr int B4 = 4;
-    const int bs = (R - b0) < B4 ? (R - b0) : B4;
-    float* pb = panel + ((b0 / 4) & 1) * 4 * 32;
+  for (int b0 = 0; b0 < R; b0 += BS) {
+    const int bs = (R - b0) < BS ? (R - b0) : BS;
+    float* pb = panel + ((b0 / BS) & 1) * BS * 32;
     if (j >= b0 && j < b0 + bs) {
 #pragma unroll
-      for (int i = 0; i < R; ++i) pb[i * 4 + (j - b0)] = v[i];
+      for (int i = 0; i < R; ++i) pb[i * BS + (j - b0)] = v[i];
     }
     __syncthreads();
     if (j >= b0 + bs && j < NCOL) {
-      // pivot block D(r, k) = pb[(b0 + r) * 4 + k]; Cholesky D = L L'
-      float Lm[4][4], il[4], y[4];
+      // pivot block D(r, k) = pb[(b0 + r) * BS + k]; Cholesky D = L L'
+      float Lm[BS][BS], il[BS], y[BS];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
+      for (int r = 0; r < BS; ++r) {
         if (r >= bs) continue;
-        const float4 dr = *reinterpret_cast<const float4*>(pb + (b0 + r) * 4);
-        const float drv[4] = {dr.x, dr.y, dr.z, dr.w};
+        float drv[BS];
+#pragma unroll
+        for (int q4 = 0; q4 < BS / 4; ++q4) {
+          const float4 dr = *reinterpret_cast<const float4*>(pb + (b0 + r) * BS + 4 * q4);
+          drv[4 * q4] = dr.x; drv[4 * q4 + 1] = dr.y; drv[4 * q4 + 2] = dr.z; drv[4 * q4 + 3] = dr.w;
+        }
 #pragma unroll
         for (int k = 0; k <= r; ++k) {
           float a = drv[k];
@@ -138,7 +143,7 @@ __device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
       }
       // y = D^-1 v[block]: L z = v, L' y = z
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
+      for (int r = 0; r < BS; ++r) {
         if (r >= bs) continue;
         float a = v[b0 + r];
 #pragma unroll
@@ -146,27 +151,30 @@ __device__ __forceinline__ void gj_solve(float* panel, Load load, Store store) {
         y[r] = a * il[r];
       }
 #pragma unroll
-      for (int r = 3; r >= 0; --r) {
+      for (int r = BS - 1; r >= 0; --r) {
         if (r >= bs) continue;
         float a = y[r];
 #pragma unroll
-        for (int q = r + 1; q < 4; ++q)
+        for (int q = r + 1; q < BS; ++q)
           if (q < bs) a -= Lm[q][r] * y[q];
         y[r] = a * il[r];
       }
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         if (i >= b0 && i < b0 + bs) continue;
-        const float4 pr = *reinterpret_cast<const float4*>(pb + i * 4);
-        const float prv[4] = {pr.x, pr.y, pr.z, pr.w};
         float a = v[i];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (k < bs) a -= prv[k] * y[k];
+        for (int q4 = 0; q4 < BS / 4; ++q4) {
+          const float4 pr = *reinterpret_cast<const float4*>(pb + i * BS + 4 * q4);
+          const float prv[4] = {pr.x, pr.y, pr.z, pr.w};
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (4 * q4 + k < bs) a -= prv[k] * y[4 * q4 + k];
+        }
         v[i] = a;
       }
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+      for (int r = 0; r < BS; ++r)
         if (r < bs) v[b0 + r] = y[r];
     }
   }
@@ -195,6 +203,9 @@ __device__ __forceinline__ void load_vec(float* dst, const float* __restrict__ s
   for (int i = threadIdx.x; i < N; i += kThreads) dst[i] = __ldg(src + i);
 }
 
+// pivot-block size of the Q_uu elimination (NU up to 30 columns of pivots)
+constexpr int kGjBlock = 8;
+
 template <int NX, int NU, int NE>
 struct Lay {
   static constexpr int LX = NX + (NX % 2 == 0 ? 1 : 2), LU = NU + (NU % 2 == 0 ? 1 : 2),
@@ -205,7 +216,7 @@ struct Lay {
   static constexpr int P = 0, A = P + NX * LX, PA = A + NX * LX, Q = PA + NX * LX, B = Q + NX * LX, PB = B + NU * LX,
                        M = PB + NU * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, ZW = QUX + NX * LU,
                        C = ZW + NZW * LU, D = C + NX * LE, TS = D + NU * LE, KK = TS + NZW * LE,
-                       PAN = (KK + (NX + 1) * LE + 3) / 4 * 4, V = PAN + 2 * 4 * 32;
+                       PAN = (KK + (NX + 1) * LE + 3) / 4 * 4, V = PAN + 2 * kGjBlock * 32;
   // vectors, NX + 4 floats each
   static constexpr int VL = NX + 4;
   static constexpr int vc = V, vq = vc + VL, vr = vq + VL, ve = vr + VL, vw = ve + VL, vp = vw + VL, vqx = vp + VL,
@@ -413,7 +424,7 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_kernel(mpxg_lq_eq_io io, f
     //   Q_uu [Z | g | W] = [Q_ux | q_u | D'];
     //   [S | T | h] = [D W | C - D Z | D g + e],  S [K_nu | -k_nu] = [T | h];
     //   Z += W K_nu (K = -Z), g += W k_nu (k = -g)
-    gj_solve<NU, NU + L::NZW>(pan, [&](int j, float* v) {
+    gj_solve<NU, NU + L::NZW, kGjBlock>(pan, [&](int j, float* v) {
 #pragma unroll
       for (int i = 0; i < NU; ++i)
         v[i] = j < NU ? Quu[j * LU + i]

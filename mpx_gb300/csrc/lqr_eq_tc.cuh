@@ -71,7 +71,7 @@ struct TcLay {
   static constexpr int NZW = NX + 1 + NE;
   static constexpr int QUU = 0, QUX = QUU + NU * LU, ZW = QUX + NX * LU, C = ZW + NZW * LU, D = C + NX * LE,
                        TS = D + NU * LE, KK = TS + NZW * LE, PIV = (KK + (NX + 1) * LE + 3) / 4 * 4,
-                       V = PIV + 2 * 4 * 32;
+                       V = PIV + 2 * kGjBlock * 32;
   static constexpr int VL = NX + 4;
   static constexpr int vq = V, vr = vq + VL, ve = vr + VL, vp = ve + VL, vqx = vp + VL, vqu = vqx + VL,
                        vkn = vqu + VL, vk = vkn + VL, vx = vk + VL, vu = vx + VL, vt = vu + VL, FLOATS = vt + VL;
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 1) lqr_eq_tc_kernel(mpxg_lq_eq_io io
     //   Z += W K_nu (K = -Z), g += W k_nu (k = -g)
     // (the column loads finish Q_uu = R + B'PB and Q_ux = M' + B'PA, and put
     // Q_ux' into gamma's A operand in region P)
-    gj_solve<NU, NU + L::NZW>(piv, [&](int j, float* v) {
+    gj_solve<NU, NU + L::NZW, kGjBlock>(piv, [&](int j, float* v) {
       if (j < NU) {
 #pragma unroll
         for (int i = 0; i < NU; ++i) v[i] = Quu[j * LU + i] + sR[i * NU + j];
