@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream section")
     ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
     ap.add_argument("--no-autotune", action="store_true", help="use the default launch geometry")
-    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq"],
+    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq", "wb"],
                     help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve; lqr_eq: the "
                          "equality-constrained n=72 LQ solve")
     ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1],
@@ -536,10 +536,11 @@ def run_ours(args, rank, world, local_rank):
 
 
 def other_configs(args, rank, world, local_rank):
-    """Short runs of the two LQ workloads (their full lines: --workload lqr /
-    lqr_eq): the isolated LQR of 1024 x (n=24, m=12, N=128), sequential
-    Riccati, and the constrained LQ of 512 x (n=72, m=30, 12 rows, N=100) on
-    the tensor cores and on the CUDA cores."""
+    """Short runs of the other workloads (their full lines: --workload lqr /
+    lqr_eq / wb): the isolated LQR of 1024 x (n=24, m=12, N=128), sequential
+    Riccati; the constrained LQ of 512 x (n=72, m=30, 12 rows, N=100) on the
+    tensor cores and on the CUDA cores; the whole-body interface for 4096
+    aliengo environments."""
     import copy
     a = copy.copy(args)
     a.steps, a.warmup, a.no_cpu, a.batch = 5, 3, True, BATCH
@@ -557,6 +558,9 @@ def other_configs(args, rank, world, local_rank):
             entry["tf32_mma_tflops"] = l4["tensor"]["achieved_tflops"]
             entry["tensor_frac"] = l4["tensor"]["frac"]
         out["lqr_eq_512_n72_m30_p12_N100_" + label] = entry
+    w = run_wb(a, rank, world, local_rank, emit=False)
+    out["wb_interface_4096_aliengo"] = {"metric": "whole-body interface evaluations/s", "value": w["value"],
+                                        "us_per_call": w["us_per_call"], "e2e": w["e2e"]["value"]}
     return out
 
 
@@ -790,6 +794,129 @@ def run_lqr_eq(args, rank, world, local_rank, emit=True):
     return line
 
 
+# ------------------------------------------------------------ whole-body interface workload
+WB_B = 4096
+
+
+def run_wb(args, rank, world, local_rank, emit=True):
+    """--workload wb: the SRBD controller's whole-body torque interface
+    (mpc_utils.py:276-313, mpxg_wb_interface) for 4096 aliengo environments
+    at seeded random states; outputs tau and the contact Jacobians."""
+    import torch
+    from mpx_gb300 import configs, mjcf
+    from mpx_gb300.replicas import max_over_ranks
+    from mpx_gb300.wholebody import WholeBodyModel
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    B = WB_B if args.batch == BATCH else int(args.batch)
+    model = mjcf.load_npz(os.path.join(ROOT, "tests", "golden", "aliengo_wb.npz"))
+    wb = WholeBodyModel(model, device=dev)
+    cfg = configs.srbd_quadruped()
+    rng = np.random.default_rng(41 + 1000 * rank)
+    q0 = np.load(os.path.join(ROOT, "tests", "golden", "aliengo_wb.npz"))["q0"]
+    quat = rng.normal(size=(B, 4))
+    quat /= np.linalg.norm(quat, axis=1, keepdims=True)
+    host = dict(qpos=np.concatenate([rng.normal(size=(B, 3)) * 0.3 + [0, 0, 0.3], quat,
+                                     q0 + rng.normal(size=(B, 12)) * 0.2], axis=1),
+                qvel=rng.normal(size=(B, 18)), grf=rng.normal(size=(B, 12)) * 30,
+                foot_ref=rng.normal(size=(B, 12)) * 0.05, foot_ref_dot=rng.normal(size=(B, 12)) * 0.2)
+    host = {k: torch.from_numpy(v.astype(np.float32)).pin_memory() for k, v in host.items()}
+    host["contact"] = torch.from_numpy(rng.integers(0, 2, size=(B, 4)).astype(np.int32)).pin_memory()
+    dv = {k: v.to(dev) for k, v in host.items()}
+    Kp = torch.as_tensor(cfg.Kp, dtype=torch.float32, device=dev)
+    Kd = torch.as_tensor(cfg.Kd, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def step(d):
+        return wb.interface(d["qpos"], d["qvel"], d["grf"], d["foot_ref"], d["foot_ref_dot"], d["contact"], Kp, Kd,
+                            stream=stream)
+
+    tau_host = torch.empty(B, 12).pin_memory()
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            step(dv)
+    torch.cuda.synchronize()
+    # the per-tick call replayed as CUDA graphs: the kernel alone, and end to
+    # end (host inputs copied in and tau read back inside the graph)
+    g_kernel, g_e2e = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_kernel, stream=stream):
+        step(dv)
+    with torch.cuda.graph(g_e2e, stream=stream):
+        for k in host:
+            dv[k].copy_(host[k], non_blocking=True)
+        tau_e2e, _ = step(dv)
+        tau_host.copy_(tau_e2e, non_blocking=True)
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            g_kernel.replay()
+            g_e2e.replay()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            g_kernel.replay()
+        ev[1].record(stream)
+        ev[2].record(stream)
+        for _ in range(args.steps):
+            g_e2e.replay()
+        ev[3].record(stream)
+        ev[4].record(stream)
+        for _ in range(args.steps):
+            step(dv)
+        ev[5].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    eager_ms = max_over_ranks(ev[4].elapsed_time(ev[5]), device=dev)
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[1]), device=dev)
+    e2e_ms = max_over_ranks(ev[2].elapsed_time(ev[3]), device=dev)
+    avg_s = total_ms / args.steps / 1000.0
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    out_bytes = B * (12 + 18 * 12) * 4
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = (h2d + out_bytes) / avg_s / 1e9
+    line = {
+        "metric": "whole-body interface evaluations/s (aliengo, nv = 18, 4 contacts)",
+        "value": world * B / avg_s, "unit": "evaluations/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "us_per_call": total_ms / args.steps * 1e3,
+        "eager_us_per_call": eager_ms / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded states around the reference's q0)",
+        "config": {"workload": "%d environments: whole_body_interface (mpc_utils.py:276-313) with config_srbd Kp, Kd"
+                               % B, "parallelism": "replicas", "l2": "inputs (%.1f MB) stay in L2: the call is "
+                               "latency-bound" % ((h2d + out_bytes) / 1e6),
+                   "timing": "CUDA graph replays of the call (eager_us_per_call: the Python call per step)"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                     "traffic": None, "algorithmic_bytes": h2d + out_bytes, "kernel": "wb_kernel<true>"},
+        "e2e": {"value": world * B / (e2e_ms / args.steps / 1000.0), "unit": "evaluations/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": B * 12 * 4},
+        "gpu_launches": 3 * args.steps,  # wb_kernel: graph, end-to-end graph, eager
+        "clocks": clk,
+    }
+    if not args.no_cpu and rank == 0:
+        sys.path.insert(0, ROOT)
+        from oracle import wholebody as W
+        n, t0 = 0, time.perf_counter()
+        hq = {k: v.numpy() for k, v in host.items()}
+        while time.perf_counter() - t0 < min(args.cpu_seconds, 5.0) and n < B:
+            W.interface(model, cfg.Kp, cfg.Kd, hq["qpos"][n], hq["qvel"][n], hq["grf"][n], hq["foot_ref"][n],
+                        hq["foot_ref_dot"][n], hq["contact"][n])
+            n += 1
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n / dt, "unit": "evaluations/s", "cores": 1, "kind": "port",
+                                "sample": "%d environments through the float64 numpy oracle (one thread)" % n}
+    if rank == 0 and emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -805,6 +932,8 @@ def main():
         run_lqr(args, rank, world, local_rank)
     elif args.workload == "lqr_eq":
         run_lqr_eq(args, rank, world, local_rank)
+    elif args.workload == "wb":
+        run_wb(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1:

@@ -408,6 +408,62 @@ mpxg_status mpxg_server_completed(mpxg_server* s, mpxg_result* results, int max,
 mpxg_status mpxg_server_stats(const mpxg_server* s, int* queued, int* running, long long* launches);
 const char* mpxg_server_last_error(const mpxg_server* s);
 
+/* ---------------------------------------------------------------- whole body
+ * Rigid-body terms of a floating-base kinematic tree (an MJCF model parsed on
+ * the host: mpx_gb300/mjcf.py) and the whole-body torque interface of the SRBD
+ * controller (mpx/utils/mpc_utils.py:275-313, bound per environment at
+ * mpx/utils/mpc_wrapper_srbd.py:73,80 and called by whole_body_run at
+ * :153-154).  MuJoCo's conventions: qpos = [free joint position (3), unit
+ * quaternion w,x,y,z (4), hinge / slide coordinates], qvel = [world linear
+ * velocity of the free body's origin (3), its angular velocity in its own
+ * frame (3), joint rates]; a hinge rotates its body about the joint axis
+ * through the joint anchor.  Bodies are listed parents first. */
+#define MPXG_WB_MAX_BODY 32
+#define MPXG_WB_MAX_DOF 32
+#define MPXG_WB_MAX_CONTACT 8
+typedef struct {
+  int nbody, nq, nv, n_contact;
+  int parent[MPXG_WB_MAX_BODY];    /* -1 = attached to the world */
+  int jnt_type[MPXG_WB_MAX_BODY];  /* 0 none (welded), 1 free (root only), 2 hinge, 3 slide */
+  int qpos_adr[MPXG_WB_MAX_BODY], dof_adr[MPXG_WB_MAX_BODY];
+  float body_pos[MPXG_WB_MAX_BODY][3], body_quat[MPXG_WB_MAX_BODY][4]; /* in the parent frame */
+  float jnt_pos[MPXG_WB_MAX_BODY][3], jnt_axis[MPXG_WB_MAX_BODY][3];   /* in the body frame, axis unit */
+  float mass[MPXG_WB_MAX_BODY], com[MPXG_WB_MAX_BODY][3];             /* com in the body frame */
+  float inertia[MPXG_WB_MAX_BODY][9]; /* about the com, body frame, row-major */
+  float armature[MPXG_WB_MAX_DOF];    /* added to the mass matrix diagonal */
+  float gravity[3];
+  /* contact point c: a point fixed in body contact_point_body[c] at
+   * contact_point_pos[c] (the MJCF geom), differentiated as attached to
+   * body contact_jac_body[c] (mjx.jac's body argument) */
+  int contact_point_body[MPXG_WB_MAX_CONTACT], contact_jac_body[MPXG_WB_MAX_CONTACT];
+  float contact_point_pos[MPXG_WB_MAX_CONTACT][3];
+} mpxg_wb_model;
+
+/* Per environment b (device arrays, row-major): qpos [B,nq], qvel [B,nv] ->
+ *   M [B,nv,nv]      joint-space inertia with armature (mjx_data.qM),
+ *   bias [B,nv]      Coriolis, centrifugal and gravity forces at qacc = 0
+ *                    (mjx_data.qfrc_bias; passive forces excluded),
+ *   cpos [B,3C]      contact point positions (geom_xpos of the contacts),
+ *   J [B,nv,3C]      translational Jacobians of the contact points, column
+ *                    block c = mjx.jac(..)[0] of contact c,
+ *   cvel [B,3C]      J' qvel.
+ * Any output may be NULL.  One warp per environment. */
+mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, const float* qpos,
+                          const float* qvel, float* M, float* bias, float* cpos, float* J, float* cvel);
+
+/* The whole-body interface (mpc_utils.py:276-313) for a batch:
+ *   a   = Kp (foot_ref - cpos) + Kd (foot_ref_dot - J' qvel)
+ *   tau = (-(J grf))[6:] where contact, (bias + M pinv(J') a)[6:] elsewhere,
+ * with the mask of joint i = contact[i / 3]; requires nv = 6 + 3C with a
+ * free root.  grf, foot_ref, foot_ref_dot [B,3C]; contact [B,C] (int);
+ * Kp, Kd [3C,3C] shared by all environments.  Outputs tau [B,nv-6] and, if
+ * J is not NULL, J [B,nv,3C].  pinv(J') a is J (J'J)^-1 a (J' of full row
+ * rank, which a leg away from a kinematic singularity gives). */
+mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batch, const float* qpos,
+                              const float* qvel, const float* grf, const float* foot_ref,
+                              const float* foot_ref_dot, const int* contact, const float* Kp, const float* Kd,
+                              float* tau, float* J);
+
 /* Last error message of a handle (or of the library when h is NULL). */
 const char* mpxg_last_error(const mpxg_handle* h);
 const char* mpxg_status_string(int status);

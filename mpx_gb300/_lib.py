@@ -97,13 +97,32 @@ class LqIO(ctypes.Structure):
                                                 "K", "k", "X", "U", "lam", "workspace")]
 
 
+WB_MAX_BODY, WB_MAX_DOF, WB_MAX_CONTACT = 32, 32, 8
+
+
+class WbModel(ctypes.Structure):
+    """mpxg_wb_model (include/mpxg.h)."""
+    _B, _C = WB_MAX_BODY, WB_MAX_CONTACT
+    _fields_ = [("nbody", ctypes.c_int), ("nq", ctypes.c_int), ("nv", ctypes.c_int), ("n_contact", ctypes.c_int),
+                ("parent", ctypes.c_int * _B), ("jnt_type", ctypes.c_int * _B), ("qpos_adr", ctypes.c_int * _B),
+                ("dof_adr", ctypes.c_int * _B),
+                ("body_pos", (ctypes.c_float * 3) * _B), ("body_quat", (ctypes.c_float * 4) * _B),
+                ("jnt_pos", (ctypes.c_float * 3) * _B), ("jnt_axis", (ctypes.c_float * 3) * _B),
+                ("mass", ctypes.c_float * _B), ("com", (ctypes.c_float * 3) * _B),
+                ("inertia", (ctypes.c_float * 9) * _B), ("armature", ctypes.c_float * WB_MAX_DOF),
+                ("gravity", ctypes.c_float * 3),
+                ("contact_point_body", ctypes.c_int * _C), ("contact_jac_body", ctypes.c_int * _C),
+                ("contact_point_pos", (ctypes.c_float * 3) * _C)]
+
+
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
            "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
-           "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version"]
+           "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
+           "mpxg_wb_terms", "mpxg_wb_interface"]
 
 _lib = None
 
@@ -158,6 +177,10 @@ def load(build_if_missing=True):
     L.mpxg_lqr_eq_solve.restype = ctypes.c_int
     L.mpxg_lqr_eq_solve_method.argtypes = [vp, ctypes.POINTER(LqEqIO), ctypes.c_int]
     L.mpxg_lqr_eq_solve_method.restype = ctypes.c_int
+    L.mpxg_wb_terms.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 7
+    L.mpxg_wb_terms.restype = ctypes.c_int
+    L.mpxg_wb_interface.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 10
+    L.mpxg_wb_interface.restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_xla_solve_vjp.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]

@@ -17,6 +17,7 @@
 #include "lqr_eq_tc.cuh"
 #include "lqr_kernels.cuh"
 #include "sqp_kernel.cuh"
+#include "wb_kernel.cuh"
 
 using namespace mpxg;
 
@@ -485,6 +486,70 @@ mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_facto
   timer_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(n, n_legs, duty_factor, step_freq, dt, leg_time, contact);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "timer_kernel launch");
+}
+
+// ---------------------------------------------------------------- whole body
+// The checks the whole-body kernel relies on (it indexes shared arrays by
+// these fields without further bounds tests).
+static const char* wb_check(const mpxg_wb_model* m) {
+  using namespace mpxg::wb;
+  if (!m) return "null model";
+  if (m->nbody < 1 || m->nbody > MPXG_WB_MAX_BODY) return "nbody out of range 1..32";
+  if (m->nv < 0 || m->nv > MPXG_WB_MAX_DOF) return "nv out of range 0..32";
+  if (m->nq < 0 || m->nq > MPXG_WB_MAX_DOF + 4) return "nq out of range";
+  if (m->n_contact < 0 || m->n_contact > MPXG_WB_MAX_CONTACT) return "n_contact out of range 0..8";
+  int dof = 0, qp = 0;
+  for (int b = 0; b < m->nbody; ++b) {
+    const int jt = m->jnt_type[b];
+    if (m->parent[b] < -1 || m->parent[b] >= b) return "bodies must be listed parents first";
+    if (jt < 0 || jt > 3) return "unknown joint type";
+    if (jt == 1 && (b != 0 || m->parent[b] != -1)) return "a free joint is allowed on the first body only";
+    if (m->dof_adr[b] != dof || m->qpos_adr[b] != qp) return "dof / qpos addresses must be dense in body order";
+    dof += ndof(jt);
+    qp += nqpos(jt);
+    if (!(m->mass[b] >= 0.0f)) return "negative mass";
+  }
+  if (dof != m->nv || qp != m->nq) return "nv / nq do not match the joints";
+  for (int c = 0; c < m->n_contact; ++c)
+    if (m->contact_point_body[c] < 0 || m->contact_point_body[c] >= m->nbody || m->contact_jac_body[c] < 0 ||
+        m->contact_jac_body[c] >= m->nbody)
+      return "contact body out of range";
+  return nullptr;
+}
+
+mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, const float* qpos, const float* qvel,
+                          float* M, float* bias, float* cpos, float* J, float* cvel) {
+  using namespace mpxg::wb;
+  if (const char* why = wb_check(model)) return fail(nullptr, MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_terms: ") + why);
+  if (batch < 0 || (batch > 0 && (!qpos || !qvel)))
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_wb_terms: bad batch or null state");
+  if (batch == 0) return MPXG_OK;
+  Args a{};
+  a.qpos = qpos; a.qvel = qvel; a.M = M; a.bias = bias; a.cpos = cpos; a.J = J; a.cvel = cvel;
+  wb_kernel<false><<<(batch + kWarps - 1) / kWarps, 32 * kWarps, 0, (cudaStream_t)stream>>>(*model, batch, a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
+}
+
+mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batch, const float* qpos,
+                              const float* qvel, const float* grf, const float* foot_ref, const float* foot_ref_dot,
+                              const int* contact, const float* Kp, const float* Kd, float* tau, float* J) {
+  using namespace mpxg::wb;
+  if (const char* why = wb_check(model))
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_interface: ") + why);
+  if (model->jnt_type[0] != 1 || model->n_contact < 1 || model->nv != 6 + 3 * model->n_contact)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG,
+                "mpxg_wb_interface: needs a free root and nv = 6 + 3 x contacts (one torque row per contact axis)");
+  if (batch < 0 || (batch > 0 && (!qpos || !qvel || !grf || !foot_ref || !foot_ref_dot || !contact || !Kp || !Kd ||
+                                  !tau)))
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_wb_interface: bad batch or null pointer");
+  if (batch == 0) return MPXG_OK;
+  Args a{};
+  a.qpos = qpos; a.qvel = qvel; a.grf = grf; a.foot_ref = foot_ref; a.foot_ref_dot = foot_ref_dot;
+  a.contact = contact; a.Kp = Kp; a.Kd = Kd; a.tau = tau; a.J = J;
+  wb_kernel<true><<<(batch + kWarps - 1) / kWarps, 32 * kWarps, 0, (cudaStream_t)stream>>>(*model, batch, a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
 }
 
 mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* a) {

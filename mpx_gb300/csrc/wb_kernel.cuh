@@ -1,0 +1,451 @@
+// Rigid-body terms of a floating-base kinematic tree and the whole-body torque
+// interface of the SRBD controller (mpx/utils/mpc_utils.py:275-313), one warp
+// per environment.
+//
+// The reference obtains these from MuJoCo XLA (mjx.fwd_position,
+// mjx.fwd_velocity, mjx.jac; mpc_utils.py:279-298).  Here they are computed
+// directly in world coordinates, with spatial vectors taken about one point o
+// (the first body's origin), in four warp-synchronous passes:
+//   1. forward kinematics level by level down the tree (lane = body);
+//   2. the motion axis S_j = (omega; v at o) of every degree of freedom and
+//      each body's spatial inertia about o (lane = body);
+//   3. body velocities V_b = sum S_j qdot_j over the chain, accelerations at
+//      qacc = 0 (gravity as a base acceleration, dS_j/dt = V ×m S_j for
+//      axes fixed in a body), the bias force of each body
+//      F_b = I_b A_b + V_b ×f (I_b V_b), and the subtree sums of the forces
+//      and inertias (lane = body);
+//   4. bias_j = S_j . F_subtree(body(j)) and the composite-rigid-body mass
+//      matrix M_ij = S_i . (I_subtree(body(j)) S_j) for i in the chain of j
+//      (lane = degree of freedom), plus armature on the diagonal.
+// Contact points are geom positions; their translational Jacobian column j is
+// v_j + omega_j × (p - o) when dof j moves the point's body.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/mpxg.h"
+
+namespace mpxg {
+namespace wb {
+
+constexpr int kMB = MPXG_WB_MAX_BODY, kMD = MPXG_WB_MAX_DOF, kMR = 3 * MPXG_WB_MAX_CONTACT;
+constexpr int kWarps = 2;  // environments per block
+
+struct Args {
+  const float *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd;
+  const int* contact;
+  float *M, *bias, *cpos, *J, *cvel, *tau;
+};
+
+struct Warp {
+  float quat[kMB][4], R[kMB][9], xp[kMB][3];
+  float S[kMD][6];                 // per dof: (omega; linear velocity at o)
+  float V[kMB][6], F[kMB][6], Fc[kMB][6];
+  float Ib[kMB][10], Ic[kMB][10];  // (m, h = m c, J_o upper triangle xx xy xz yy yz zz)
+  float M[kMD][kMD + 1];
+  float J[kMD][kMR + 1];
+  float bias[kMD], qpos[kMD + 4], qvel[kMD], w[kMD];
+  float cpos[kMR], cvel[kMR], a[kMR], y[kMR];
+  int dof_body[kMD], depth[kMB];
+  unsigned anc[kMB];               // bit a set: a is b or an ancestor of b
+};
+
+__host__ __device__ __forceinline__ int ndof(int jt) { return jt == 1 ? 6 : (jt >= 2 ? 1 : 0); }
+__host__ __device__ __forceinline__ int nqpos(int jt) { return jt == 1 ? 7 : (jt >= 2 ? 1 : 0); }
+
+__device__ __forceinline__ void cross3(const float* a, const float* b, float* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ void quat_mul(const float* a, const float* b, float* c) {  // c = a b, (w, x, y, z)
+  c[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+  c[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+  c[2] = a[0] * b[2] - a[1] * b[3] + a[2] * b[0] + a[3] * b[1];
+  c[3] = a[0] * b[3] + a[1] * b[2] - a[2] * b[1] + a[3] * b[0];
+}
+// a quaternion of (near) zero norm becomes the identity, as MuJoCo does
+__device__ __forceinline__ void quat_normalize(float* q) {
+  const float n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  if (!(n2 > 1e-30f)) {
+    q[0] = 1.0f; q[1] = q[2] = q[3] = 0.0f;
+    return;
+  }
+  const float s = rsqrtf(n2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] *= s;
+}
+// rotation matrix (row-major, world from body) of a unit quaternion
+__device__ __forceinline__ void quat_mat(const float* q, float* R) {
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
+  R[0] = 1.0f - 2.0f * (y * y + z * z); R[1] = 2.0f * (x * y - w * z); R[2] = 2.0f * (x * z + w * y);
+  R[3] = 2.0f * (x * y + w * z); R[4] = 1.0f - 2.0f * (x * x + z * z); R[5] = 2.0f * (y * z - w * x);
+  R[6] = 2.0f * (x * z - w * y); R[7] = 2.0f * (y * z + w * x); R[8] = 1.0f - 2.0f * (x * x + y * y);
+}
+__device__ __forceinline__ void mat_vec(const float* R, const float* v, float* o) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) o[i] = R[3 * i] * v[0] + R[3 * i + 1] * v[1] + R[3 * i + 2] * v[2];
+}
+// spatial inertia (m, h, J_o) times a motion (w; v): (J w + h × v; m v + w × h)
+__device__ __forceinline__ void inert_mul(const float* I, const float* s, float* o) {
+  const float m = I[0], h[3] = {I[1], I[2], I[3]};
+  const float Jxx = I[4], Jxy = I[5], Jxz = I[6], Jyy = I[7], Jyz = I[8], Jzz = I[9];
+  float hv[3], wh[3];
+  cross3(h, s + 3, hv);
+  cross3(s, h, wh);
+  o[0] = Jxx * s[0] + Jxy * s[1] + Jxz * s[2] + hv[0];
+  o[1] = Jxy * s[0] + Jyy * s[1] + Jyz * s[2] + hv[1];
+  o[2] = Jxz * s[0] + Jyz * s[1] + Jzz * s[2] + hv[2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) o[3 + i] = m * s[3 + i] + wh[i];
+}
+// motion cross motion: (w; v) ×m (w2; v2) = (w × w2; w × v2 + v × w2)
+__device__ __forceinline__ void crm(const float* a, const float* b, float* o) {
+  float t[3];
+  cross3(a, b, o);
+  cross3(a, b + 3, o + 3);
+  cross3(a + 3, b, t);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) o[3 + i] += t[i];
+}
+// motion cross force: (w; v) ×f (n; f) = (w × n + v × f; w × f)
+__device__ __forceinline__ void crf(const float* a, const float* f, float* o) {
+  float t[3];
+  cross3(a, f, o);
+  cross3(a + 3, f + 3, t);
+  cross3(a, f + 3, o + 3);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) o[i] += t[i];
+}
+__device__ __forceinline__ float dot6(const float* a, const float* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
+}
+
+// The model must have passed the host checks of mpxg_wb_terms: parents
+// precede children, one joint per body, the free joint only on body 0, dof and
+// qpos addresses dense in body order, nbody, nv <= 32, nq <= nv + 4, at most
+// 8 contacts on existing bodies.
+template <bool IFACE>
+__global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch, Args a) {
+  __shared__ Warp sw[kWarps];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int env = blockIdx.x * kWarps + wid;
+  if (env >= batch) return;  // the whole warp leaves; no block-wide barrier follows
+  Warp& s = sw[wid];
+  const unsigned full = 0xffffffffu;
+  const int nb = m.nbody, nq = m.nq, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
+  for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * nq + i];
+  if (lane < nv) s.qvel[lane] = a.qvel[(size_t)env * nv + lane];
+  int dep = 0;
+  if (lane < nb) {
+    unsigned mask = 0;
+    int b = lane;
+    for (int g = 0; g < kMB && b >= 0; ++g) {
+      mask |= 1u << b;
+      b = m.parent[b];
+      ++dep;
+    }
+    s.anc[lane] = mask;
+    s.depth[lane] = dep - 1;
+    const int jt = m.jnt_type[lane];
+    for (int k = 0; k < ndof(jt); ++k) s.dof_body[m.dof_adr[lane] + k] = lane;
+  }
+  __syncwarp();
+  // ---- 1. forward kinematics, one tree level per step
+  const int maxd = __reduce_max_sync(full, lane < nb ? dep - 1 : 0);
+  for (int d = 0; d <= maxd; ++d) {
+    if (lane < nb && s.depth[lane] == d) {
+      const int b = lane, p = m.parent[b], jt = m.jnt_type[b];
+      float q[4], x[3];
+      if (jt == 1) {
+        const float* qp = s.qpos + m.qpos_adr[b];
+        x[0] = qp[0]; x[1] = qp[1]; x[2] = qp[2];
+        q[0] = qp[3]; q[1] = qp[4]; q[2] = qp[5]; q[3] = qp[6];
+      } else {
+        float pq[4] = {1.0f, 0.0f, 0.0f, 0.0f}, px[3] = {0.0f, 0.0f, 0.0f};
+        float pR[9] = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+        if (p >= 0) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) pq[i] = s.quat[p][i];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) px[i] = s.xp[p][i];
+#pragma unroll
+          for (int i = 0; i < 9; ++i) pR[i] = s.R[p][i];
+        }
+        float bp[3];
+        mat_vec(pR, m.body_pos[b], bp);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) x[i] = px[i] + bp[i];
+        quat_mul(pq, m.body_quat[b], q);
+        if (jt >= 2) {
+          float Rb[9], t[3];
+          quat_mat(q, Rb);
+          const float qj = s.qpos[m.qpos_adr[b]];
+          if (jt == 2) {  // rotate about the axis through the anchor
+            float anchor[3];
+            mat_vec(Rb, m.jnt_pos[b], t);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) anchor[i] = x[i] + t[i];
+            float sh, ch;
+            sincosf(0.5f * qj, &sh, &ch);
+            const float qa[4] = {ch, sh * m.jnt_axis[b][0], sh * m.jnt_axis[b][1], sh * m.jnt_axis[b][2]};
+            float qn[4];
+            quat_mul(q, qa, qn);
+            quat_normalize(qn);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) q[i] = qn[i];
+            quat_mat(q, Rb);
+            mat_vec(Rb, m.jnt_pos[b], t);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) x[i] = anchor[i] - t[i];
+          } else {  // slide along the axis
+            mat_vec(Rb, m.jnt_axis[b], t);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) x[i] += t[i] * qj;
+          }
+        }
+      }
+      quat_normalize(q);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) s.quat[b][i] = q[i];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) s.xp[b][i] = x[i];
+      quat_mat(q, s.R[b]);
+    }
+    __syncwarp();
+  }
+  const float o[3] = {s.xp[0][0], s.xp[0][1], s.xp[0][2]};
+  // ---- 2. dof axes and body inertias about o
+  if (lane < nb) {
+    const int b = lane, jt = m.jnt_type[b], da = m.dof_adr[b];
+    const float* R = s.R[b];
+    const float* xb = s.xp[b];
+    float c[3];
+    mat_vec(R, m.com[b], c);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) c[i] += xb[i] - o[i];
+    // I_world = R I R'
+    const float* Il = m.inertia[b];
+    float RI[9], Iw[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) RI[3 * i + k] = R[3 * i] * Il[k] + R[3 * i + 1] * Il[3 + k] + R[3 * i + 2] * Il[6 + k];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) Iw[3 * i + k] = RI[3 * i] * R[3 * k] + RI[3 * i + 1] * R[3 * k + 1] + RI[3 * i + 2] * R[3 * k + 2];
+    const float ms = m.mass[b], cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    float* Ib = s.Ib[b];
+    Ib[0] = ms;
+    Ib[1] = ms * c[0]; Ib[2] = ms * c[1]; Ib[3] = ms * c[2];
+    Ib[4] = Iw[0] + ms * (cc - c[0] * c[0]);
+    Ib[5] = 0.5f * (Iw[1] + Iw[3]) - ms * c[0] * c[1];
+    Ib[6] = 0.5f * (Iw[2] + Iw[6]) - ms * c[0] * c[2];
+    Ib[7] = Iw[4] + ms * (cc - c[1] * c[1]);
+    Ib[8] = 0.5f * (Iw[5] + Iw[7]) - ms * c[1] * c[2];
+    Ib[9] = Iw[8] + ms * (cc - c[2] * c[2]);
+    float r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = o[i] - xb[i];
+    if (jt == 1) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float* St = s.S[da + k];
+        St[0] = St[1] = St[2] = 0.0f;
+        St[3] = k == 0 ? 1.0f : 0.0f; St[4] = k == 1 ? 1.0f : 0.0f; St[5] = k == 2 ? 1.0f : 0.0f;
+        float* Sr = s.S[da + 3 + k];
+        Sr[0] = R[k]; Sr[1] = R[3 + k]; Sr[2] = R[6 + k];
+        cross3(Sr, r, Sr + 3);
+      }
+    } else if (jt == 2) {
+      float* Sj = s.S[da];
+      float t[3];
+      mat_vec(R, m.jnt_axis[b], Sj);
+      mat_vec(R, m.jnt_pos[b], t);
+      float ra[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) ra[i] = r[i] - t[i];  // o - anchor
+      cross3(Sj, ra, Sj + 3);
+    } else if (jt == 3) {
+      float* Sj = s.S[da];
+      Sj[0] = Sj[1] = Sj[2] = 0.0f;
+      mat_vec(R, m.jnt_axis[b], Sj + 3);
+    }
+  }
+  __syncwarp();
+  // ---- 3. velocities
+  if (lane < nb) {
+    float Vb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int b = lane;
+    for (int g = 0; g < kMB && b >= 0; ++g, b = m.parent[b]) {
+      const int nd = ndof(m.jnt_type[b]), da = m.dof_adr[b];
+      for (int k = 0; k < nd; ++k) {
+        const float qd = s.qvel[da + k];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) Vb[i] += s.S[da + k][i] * qd;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s.V[lane][i] = Vb[i];
+  }
+  __syncwarp();
+  // accelerations at qacc = 0 and the bias force of each body
+  if (lane < nb) {
+    float A[6] = {0.0f, 0.0f, 0.0f, -m.gravity[0], -m.gravity[1], -m.gravity[2]};
+    int b = lane;
+    for (int g = 0; g < kMB && b >= 0; ++g, b = m.parent[b]) {
+      const int jt = m.jnt_type[b], nd = ndof(jt), da = m.dof_adr[b];
+      // the free joint's translation axes are fixed in the world: no derivative
+      for (int k = (jt == 1 ? 3 : 0); k < nd; ++k) {
+        float t[6];
+        crm(s.V[b], s.S[da + k], t);
+        const float qd = s.qvel[da + k];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) A[i] += t[i] * qd;
+      }
+    }
+    float IA[6], IV[6], t[6];
+    inert_mul(s.Ib[lane], A, IA);
+    inert_mul(s.Ib[lane], s.V[lane], IV);
+    crf(s.V[lane], IV, t);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s.F[lane][i] = IA[i] + t[i];
+  }
+  __syncwarp();
+  // subtree sums
+  if (lane < nb) {
+    float Fc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, Ic[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) Ic[i] = 0.0f;
+    for (int d = lane; d < nb; ++d) {
+      if ((s.anc[d] >> lane) & 1u) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) Fc[i] += s.F[d][i];
+#pragma unroll
+        for (int i = 0; i < 10; ++i) Ic[i] += s.Ib[d][i];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s.Fc[lane][i] = Fc[i];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) s.Ic[lane][i] = Ic[i];
+  }
+  // contact points
+  if (lane < nc) {
+    const int gb = m.contact_point_body[lane];
+    float t[3];
+    mat_vec(s.R[gb], m.contact_point_pos[lane], t);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s.cpos[3 * lane + i] = s.xp[gb][i] + t[i];
+  }
+  __syncwarp();
+  // ---- 4. bias forces, mass matrix and contact Jacobians (lane = dof)
+  if (lane < nv) {
+    const int j = lane, bj = s.dof_body[j];
+    s.bias[j] = dot6(s.S[j], s.Fc[bj]);
+    float Fj[6];
+    inert_mul(s.Ic[bj], s.S[j], Fj);
+    for (int i = 0; i <= j; ++i) {
+      const float v = ((s.anc[bj] >> s.dof_body[i]) & 1u) ? dot6(s.S[i], Fj) : 0.0f;
+      s.M[i][j] = v;
+      s.M[j][i] = v;
+    }
+    s.M[j][j] += m.armature[j];
+    for (int c = 0; c < nc; ++c) {
+      float jp[3] = {0.0f, 0.0f, 0.0f};
+      if ((s.anc[m.contact_jac_body[c]] >> bj) & 1u) {
+        float r[3], t[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) r[i] = s.cpos[3 * c + i] - o[i];
+        cross3(s.S[j], r, t);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) jp[i] = s.S[j][3 + i] + t[i];
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) s.J[j][3 * c + i] = jp[i];
+    }
+  }
+  __syncwarp();
+  if (lane < nr) {
+    float v = 0.0f;
+    for (int j = 0; j < nv; ++j) v += s.J[j][lane] * s.qvel[j];
+    s.cvel[lane] = v;
+  }
+  __syncwarp();
+  if (!IFACE) {
+    const size_t e = (size_t)env;
+    if (a.M)
+      for (int i = lane; i < nv * nv; i += 32) a.M[e * nv * nv + i] = s.M[i / nv][i % nv];
+    if (a.bias && lane < nv) a.bias[e * nv + lane] = s.bias[lane];
+    if (a.cpos && lane < nr) a.cpos[e * nr + lane] = s.cpos[lane];
+    if (a.cvel && lane < nr) a.cvel[e * nr + lane] = s.cvel[lane];
+    if (a.J)
+      for (int i = lane; i < nv * nr; i += 32) a.J[e * nv * nr + i] = s.J[i / nr][i % nr];
+    return;
+  }
+  // ---- the interface (mpc_utils.py:300-311)
+  const size_t e = (size_t)env;
+  if (lane < nr) {
+    float v = 0.0f;
+    for (int q = 0; q < nr; ++q)
+      v += a.Kp[lane * nr + q] * (a.foot_ref[e * nr + q] - s.cpos[q]) +
+           a.Kd[lane * nr + q] * (a.foot_ref_dot[e * nr + q] - s.cvel[q]);
+    s.a[lane] = v;
+  }
+  __syncwarp();
+  // y = (J'J)^-1 a by Gauss-Jordan on [J'J | a], lane c holding column c
+  float col[kMR];
+#pragma unroll
+  for (int i = 0; i < kMR; ++i) {
+    float g = 0.0f;
+    if (i < nr) {
+      if (lane < nr) {
+        for (int j = 0; j < nv; ++j) g += s.J[j][i] * s.J[j][lane];
+      } else if (lane == nr) {
+        g = s.a[i];
+      }
+    }
+    col[i] = g;
+  }
+#pragma unroll
+  for (int k = 0; k < kMR; ++k) {
+    if (k < nr) {
+      const float dk = __shfl_sync(full, col[k], k);
+      const float yk = col[k] / dk;
+#pragma unroll
+      for (int i = 0; i < kMR; ++i) {
+        if (i < nr && i != k) {
+          const float gik = __shfl_sync(full, col[i], k);
+          col[i] -= gik * yk;
+        }
+      }
+      col[k] = yk;
+    }
+  }
+  if (lane == nr) {
+#pragma unroll
+    for (int i = 0; i < kMR; ++i)
+      if (i < nr) s.y[i] = col[i];
+  }
+  __syncwarp();
+  if (lane < nv) {  // w = pinv(J') a = J y
+    float v = 0.0f;
+    for (int r = 0; r < nr; ++r) v += s.J[lane][r] * s.y[r];
+    s.w[lane] = v;
+  }
+  __syncwarp();
+  if (lane >= 6 && lane < nv) {
+    const int j = lane;
+    float mw = 0.0f, jg = 0.0f;
+    for (int i = 0; i < nv; ++i) mw += s.M[j][i] * s.w[i];
+    for (int r = 0; r < nr; ++r) jg += s.J[j][r] * a.grf[e * nr + r];
+    const float fb = s.bias[j] + mw, mpc = -jg;
+    const float msk = (float)a.contact[e * nc + (j - 6) / 3];
+    a.tau[e * (nv - 6) + (j - 6)] = mpc * msk + (1.0f - msk) * fb;
+  }
+  if (a.J)
+    for (int i = lane; i < nv * nr; i += 32) a.J[e * nv * nr + i] = s.J[i / nr][i % nr];
+}
+
+}  // namespace wb
+}  // namespace mpxg

@@ -1,0 +1,72 @@
+"""Whole-body rigid-body terms and the SRBD controller's whole-body torque
+interface on the GPU (mpx/utils/mpc_utils.py:275-313), through
+mpxg_wb_terms / mpxg_wb_interface of libmpxg.
+
+    wb = WholeBodyModel.from_mjcf("aliengo.xml", ["FL", "FR", "RL", "RR"],
+                                  ["FL_calf", "FR_calf", "RL_calf", "RR_calf"])
+    tau, J = wb.interface(qpos, qvel, grf, foot_ref, foot_ref_dot, contact, Kp, Kd)
+
+All arrays are batched over environments on the model's device (float32;
+contact int32).  There is no CPU path: without the library the calls raise.
+"""
+import torch
+
+from . import _lib
+from . import mjcf
+from .solver import _ptr, _stream_handle
+
+
+def _dev(a, dev, dtype=torch.float32):
+    if isinstance(a, torch.Tensor):
+        return a.to(device=dev, dtype=dtype).contiguous()
+    return torch.as_tensor(a, dtype=dtype, device=dev).contiguous()
+
+
+class WholeBodyModel:
+    def __init__(self, model, device=None):
+        """model: an mjcf.RigidBodyModel with contacts set."""
+        if model.contact_point_body is None:
+            raise ValueError("the model needs contact points (mjcf.RigidBodyModel.with_contacts)")
+        self.model = model
+        self.struct = model.to_struct()
+        self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.nq, self.nv, self.nc = model.nq, model.nv, len(model.contact_point_body)
+        self.L = _lib.load()
+
+    @classmethod
+    def from_mjcf(cls, path, contact_geoms, contact_bodies, device=None):
+        return cls(mjcf.parse(path, contact_geoms, contact_bodies), device=device)
+
+    def terms(self, qpos, qvel, stream=None):
+        """dict M [B,nv,nv], bias [B,nv], cpos [B,3C], J [B,nv,3C], cvel [B,3C]."""
+        qpos = _dev(qpos, self.dev).reshape(-1, self.nq)
+        qvel = _dev(qvel, self.dev).reshape(-1, self.nv)
+        B, nv, nr = qpos.shape[0], self.nv, 3 * self.nc
+        if qvel.shape[0] != B:
+            raise ValueError("qpos and qvel batch sizes differ")
+        out = dict(M=torch.empty(B, nv, nv, device=self.dev), bias=torch.empty(B, nv, device=self.dev),
+                   cpos=torch.empty(B, nr, device=self.dev), J=torch.empty(B, nv, nr, device=self.dev),
+                   cvel=torch.empty(B, nr, device=self.dev))
+        _lib.check(self.L.mpxg_wb_terms(_stream_handle(stream), _lib.ctypes.byref(self.struct), B, _ptr(qpos),
+                                        _ptr(qvel), _ptr(out["M"]), _ptr(out["bias"]), _ptr(out["cpos"]),
+                                        _ptr(out["J"]), _ptr(out["cvel"])), None, "mpxg_wb_terms")
+        return out
+
+    def interface(self, qpos, qvel, grf, foot_ref, foot_ref_dot, contact, Kp, Kd, stream=None, with_jacobian=True):
+        """mpc_utils.py:276-313 for every environment -> (tau [B,nv-6], J [B,nv,3C] or None)."""
+        qpos = _dev(qpos, self.dev).reshape(-1, self.nq)
+        B, nr = qpos.shape[0], 3 * self.nc
+        qvel = _dev(qvel, self.dev).reshape(B, self.nv)
+        grf = _dev(grf, self.dev).reshape(B, nr)
+        foot_ref = _dev(foot_ref, self.dev).reshape(B, nr)
+        foot_ref_dot = _dev(foot_ref_dot, self.dev).reshape(B, nr)
+        contact = _dev(contact, self.dev, torch.int32).reshape(B, self.nc)
+        Kp = _dev(Kp, self.dev).reshape(nr, nr)
+        Kd = _dev(Kd, self.dev).reshape(nr, nr)
+        tau = torch.empty(B, self.nv - 6, device=self.dev)
+        J = torch.empty(B, self.nv, nr, device=self.dev) if with_jacobian else None
+        _lib.check(self.L.mpxg_wb_interface(_stream_handle(stream), _lib.ctypes.byref(self.struct), B, _ptr(qpos),
+                                            _ptr(qvel), _ptr(grf), _ptr(foot_ref), _ptr(foot_ref_dot),
+                                            _ptr(contact), _ptr(Kp), _ptr(Kd), _ptr(tau), _ptr(J)), None,
+                   "mpxg_wb_interface")
+        return tau, J

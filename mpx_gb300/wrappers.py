@@ -18,15 +18,21 @@ Differences from the reference, by necessity:
   * `limited_memory` is accepted and ignored.
   * MuJoCo is not available: foot positions that the reference computes with
     mujoco forward kinematics (mpc_wrapper.py:313-316) are passed in by the
-    caller (`foot_op`), and the whole-body torque mapping (mpc_utils.py:275-313,
-    MJX Jacobians) is not provided -- `whole_body_run` raises.
+    caller (`foot_op`).  The whole-body torque mapping (mpc_utils.py:275-313)
+    runs on libmpxg's own rigid-body kernel (mpx_gb300.wholebody) over the
+    robot's MJCF (`config.model_path`, read by mpx_gb300.mjcf) or a model
+    passed as `wb_model`.
 """
+import os
+
 import numpy as np
 import torch
 
 from . import _lib
+from . import mjcf
 from . import problem as P
 from .solver import Solver, _ptr, _stream_handle
+from .wholebody import WholeBodyModel
 
 
 def _to_dev(a, dev, dtype=torch.float32):
@@ -90,10 +96,18 @@ class BatchedMPCControllerWrapper:
     mpc_frequency, timer_t, duty_factor, step_freq, step_height,
     clearence_speed, p0, quat0, p_legs0, n, mass, inertia, u_ref, W, ...)."""
 
-    def __init__(self, config, n_env, opts=None, device=None, limited_memory=False):
+    def __init__(self, config, n_env, opts=None, device=None, limited_memory=False, wb_model=None):
+        """wb_model: an mjcf.RigidBodyModel for whole_body_run (default: the
+        MJCF at config.model_path with config.contact_frame / body_name)."""
         self.config = config
         self.n_env = int(n_env)
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        path = getattr(config, "model_path", None)
+        if wb_model is None and path and os.path.exists(path):
+            wb_model = mjcf.parse(path, list(config.contact_frame), list(config.body_name))
+        self.wb = WholeBodyModel(wb_model, device=self.dev) if wb_model is not None else None
+        self.Kp = _to_dev(np.asarray(getattr(config, "Kp", np.zeros((12, 12))), dtype=np.float32), self.dev)
+        self.Kd = _to_dev(np.asarray(getattr(config, "Kd", np.zeros((12, 12))), dtype=np.float32), self.dev)
         self.mpc_frequency = float(config.mpc_frequency)
         self.shift = int(1 / (config.dt * config.mpc_frequency))
         self.N = int(config.N)
@@ -189,7 +203,19 @@ class BatchedMPCControllerWrapper:
         return self.run(x0_torch, input_torch, foot_op_torch, contact_torch)
 
     def whole_body_run(self, qpos, qvel):
-        raise NotImplementedError("whole-body control needs MJX Jacobians, which this package does not provide")
+        """mpc_wrapper_srbd.py:153-154: joint torques for every environment from
+        the last tick's grf, foot references and contact flags
+        (mpc_utils.py:276-313).  qpos [n_env,nq], qvel [n_env,nv] ->
+        (tau [n_env,nv-6], J [n_env,nv,12])."""
+        if self.wb is None:
+            raise RuntimeError("no whole-body model: set config.model_path to the robot's MJCF or pass wb_model=")
+        return self.wb.interface(qpos, qvel, self.grf, self.foot_ref, self.foot_ref_dot, self.contact, self.Kp,
+                                 self.Kd)
+
+    def torch_whole_body_run(self, qpos, qvel):
+        """mpc_wrapper_srbd.py:156-160 (which hands the (tau, J) pair to DLPack);
+        returns the torque tensor."""
+        return self.whole_body_run(qpos, qvel)[0]
 
 
 # ----------------------------------------------------------------- single-instance wrapper

@@ -1,0 +1,254 @@
+"""Whole-body rigid-body terms and torque interface, CPU oracle (test
+infrastructure, not the product).  Only tests/ and bench.py's CPU baseline
+import it.
+
+Restates, in float64 and from the mechanics rather than from MuJoCo's
+recursive algorithms, what the reference takes from MuJoCo XLA in
+mpx/utils/mpc_utils.py:276-313 (whole_body_interface):
+
+  * forward kinematics with 4x4 homogeneous transforms (body frame in the
+    parent, then the joint: a hinge rotates about its axis through its anchor,
+    a slide translates along it, a free joint sets position and orientation);
+  * for every body b its centre-of-mass Jacobian Jv_b and angular Jacobian
+    Jw_b (geometric columns: hinge a x (p - anchor) / a, slide a / 0, free
+    translation e_k / 0, free rotation R e_k x (p - x_root) / R e_k: qvel's
+    angular part is in the free body's frame);
+  * M = sum_b m_b Jv_b' Jv_b + Jw_b' I_b Jw_b + diag(armature)      (mjx qM)
+  * bias = sum_b Jv_b' m_b (dJv_b qdot - g) + Jw_b' (I_b dJw_b qdot + w_b x I_b w_b)
+    with dJ qdot the analytic time derivative of the columns at qacc = 0
+    (axes fixed in a body turn with that body's angular velocity; anchors
+    move with their body)                                            (mjx qfrc_bias)
+  * contact points: geom positions, translational Jacobians of the point
+    attached to the named body                                       (mjx.jac)
+  * the interface formula of mpc_utils.py:300-311 with numpy's pinv, as the
+    reference uses jnp.linalg.pinv.
+
+MuJoCo cannot run here, so parity is pinned (tests/test_oracle_wholebody.py)
+by the reference's own numbers for this model -- the foot positions
+config_srbd.py:38-43 lists for aliengo at q0 -- and by identities of the
+mechanics: M against the kinetic energy of finite-differenced body motion,
+dJ qdot against the second difference of the point trajectory at qacc = 0,
+gravity forces against the potential energy gradient, and the power balance
+qdot' bias(g = 0) = 1/2 qdot' (dM/dt) qdot.
+"""
+import numpy as np
+
+FREE, HINGE, SLIDE = 1, 2, 3
+_NDOF = {0: 0, 1: 6, 2: 1, 3: 1}
+
+
+def _qmat(q):
+    w, x, y, z = np.asarray(q, dtype=np.float64) / np.linalg.norm(q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def _rot_axis(a, th):
+    """Rodrigues rotation about unit axis a by th."""
+    a = np.asarray(a, dtype=np.float64)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * (K @ K)
+
+
+def _T(R, p):
+    T = np.eye(4)
+    T[:3, :3] = R
+    T[:3, 3] = p
+    return T
+
+
+def kinematics(model, qpos):
+    """World transforms [nb,4,4] of the body frames."""
+    nb = model.nbody
+    qadr = model.qpos_adr
+    T = np.zeros((nb, 4, 4))
+    for b in range(nb):
+        p = model.parent[b]
+        Tp = np.eye(4) if p < 0 else T[p]
+        jt = int(model.jnt_type[b])
+        if jt == FREE:
+            a = qadr[b]
+            T[b] = _T(_qmat(qpos[a + 3:a + 7]), qpos[a:a + 3])
+            continue
+        Tb = Tp @ _T(_qmat(model.body_quat[b]), model.body_pos[b])
+        if jt == HINGE:
+            th = qpos[qadr[b]]
+            # rotate about the joint axis through the joint position (body frame)
+            Tj = _T(np.eye(3), model.jnt_pos[b]) @ _T(_rot_axis(model.jnt_axis[b], th), np.zeros(3)) @ \
+                _T(np.eye(3), -model.jnt_pos[b])
+            Tb = Tb @ Tj
+        elif jt == SLIDE:
+            Tb = Tb @ _T(np.eye(3), model.jnt_axis[b] * qpos[qadr[b]])
+        T[b] = Tb
+    return T
+
+
+def _chain(model, b):
+    out = []
+    while b >= 0:
+        out.append(b)
+        b = int(model.parent[b])
+    return out
+
+
+def _columns(model, T, b, point):
+    """Geometric Jacobian columns of a point attached to body b:
+    list of (dof, angular axis, linear column, kind, anchor, owner body)."""
+    dadr = model.dof_adr
+    cols = []
+    for a in _chain(model, b):
+        jt = int(model.jnt_type[a])
+        R, x = T[a][:3, :3], T[a][:3, 3]
+        d = dadr[a]
+        if jt == FREE:
+            for k in range(3):
+                e = np.zeros(3); e[k] = 1.0
+                cols.append((d + k, np.zeros(3), e, "ft", x, a))
+            for k in range(3):
+                ax = R[:, k]
+                cols.append((d + 3 + k, ax, np.cross(ax, point - x), "rot", x, a))
+        elif jt == HINGE:
+            ax = R @ model.jnt_axis[a]
+            anchor = x + R @ model.jnt_pos[a]
+            cols.append((d, ax, np.cross(ax, point - anchor), "rot", anchor, a))
+        elif jt == SLIDE:
+            ax = R @ model.jnt_axis[a]
+            cols.append((d, np.zeros(3), ax, "slide", x, a))
+    return cols
+
+
+def point_jacobian(model, T, b, point):
+    """(Jp [3,nv], Jr [3,nv]) of a world point attached to body b."""
+    nv = model.nv
+    Jp, Jr = np.zeros((3, nv)), np.zeros((3, nv))
+    for d, w, v, _, _, _ in _columns(model, T, b, point):
+        Jp[:, d] = v
+        Jr[:, d] = w
+    return Jp, Jr
+
+
+def _body_velocity(model, T, qvel):
+    """Angular velocity and origin-point linear velocity of every body."""
+    nb = model.nbody
+    W, Vx = np.zeros((nb, 3)), np.zeros((nb, 3))
+    for b in range(nb):
+        Jp, Jr = point_jacobian(model, T, b, T[b][:3, 3])
+        W[b], Vx[b] = Jr @ qvel, Jp @ qvel
+    return W, Vx
+
+
+def _point_velocity(model, T, qvel, b, p):
+    Jp, _ = point_jacobian(model, T, b, p)
+    return Jp @ qvel
+
+
+def _dJ_qdot(model, T, qvel, W, b, p):
+    """(dJp qdot, dJr qdot) of a point p attached to body b at qacc = 0."""
+    vp = _point_velocity(model, T, qvel, b, p)
+    ap, aw = np.zeros(3), np.zeros(3)
+    for d, w, v, kind, anchor, owner in _columns(model, T, b, p):
+        qd = qvel[d]
+        if kind == "ft":
+            continue
+        if kind == "slide":
+            ap += np.cross(W[owner], v) * qd
+            continue
+        wdot = np.cross(W[owner], w)               # the axis turns with its body
+        van = _point_velocity(model, T, qvel, owner, anchor)
+        ap += (np.cross(wdot, p - anchor) + np.cross(w, vp - van)) * qd
+        aw += wdot * qd
+    return ap, aw
+
+
+def terms(model, qpos, qvel):
+    """dict M [nv,nv], bias [nv], cpos [3C], J [nv,3C], cvel [3C] (float64)."""
+    qpos = np.asarray(qpos, dtype=np.float64)
+    qvel = np.asarray(qvel, dtype=np.float64)
+    nb, nv = model.nbody, model.nv
+    T = kinematics(model, qpos)
+    W, _ = _body_velocity(model, T, qvel)
+    M = np.diag(np.asarray(model.armature, dtype=np.float64)).copy()
+    bias = np.zeros(nv)
+    g = np.asarray(model.gravity, dtype=np.float64)
+    for b in range(nb):
+        R, x = T[b][:3, :3], T[b][:3, 3]
+        c = x + R @ model.com[b]
+        Iw = R @ model.inertia[b] @ R.T
+        m = float(model.mass[b])
+        Jv, Jw = point_jacobian(model, T, b, c)
+        M += m * Jv.T @ Jv + Jw.T @ Iw @ Jw
+        av, aw = _dJ_qdot(model, T, qvel, W, b, c)
+        w = Jw @ qvel
+        bias += Jv.T @ (m * (av - g)) + Jw.T @ (Iw @ aw + np.cross(w, Iw @ w))
+    nc = 0 if model.contact_point_body is None else len(model.contact_point_body)
+    cpos = np.zeros(3 * nc)
+    J = np.zeros((nv, 3 * nc))
+    for ci in range(nc):
+        gb = int(model.contact_point_body[ci])
+        p = T[gb][:3, :3] @ model.contact_point_pos[ci] + T[gb][:3, 3]
+        cpos[3 * ci:3 * ci + 3] = p
+        Jp, _ = point_jacobian(model, T, int(model.contact_jac_body[ci]), p)
+        J[:, 3 * ci:3 * ci + 3] = Jp.T
+    return dict(M=M, bias=bias, cpos=cpos, J=J, cvel=J.T @ qvel, T=T)
+
+
+def interface(model, Kp, Kd, qpos, qvel, grf, foot_ref, foot_ref_dot, contact):
+    """mpx/utils/mpc_utils.py:276-313 for one environment -> (tau, J)."""
+    t = terms(model, qpos, qvel)
+    M, D, J = t["M"], t["bias"], t["J"]
+    current_leg, current_leg_dot = t["cpos"], J.T @ np.asarray(qvel, dtype=np.float64)
+    a = np.asarray(Kp) @ (np.asarray(foot_ref) - current_leg) + np.asarray(Kd) @ (np.asarray(foot_ref_dot) -
+                                                                                  current_leg_dot)
+    tau_fb_lin = D[6:] + (M @ np.linalg.pinv(J.T) @ a)[6:]
+    tau_mpc = -(J @ np.asarray(grf, dtype=np.float64))[6:]
+    mask = np.repeat(np.asarray(contact, dtype=np.float64), 3)
+    return tau_mpc * mask + (1 - mask) * tau_fb_lin, J
+
+
+# ----------------------------------------------------------------- identities used to pin the oracle
+def integrate(model, qpos, qvel, h):
+    """qpos after time h at constant qvel (MuJoCo's qacc = 0 motion): free
+    position + h v, orientation q * exp(h w_body / 2), joints + h qdot."""
+    q = np.array(qpos, dtype=np.float64)
+    qadr, dadr = model.qpos_adr, model.dof_adr
+    for b in range(model.nbody):
+        jt = int(model.jnt_type[b])
+        a, d = qadr[b], dadr[b]
+        if jt == FREE:
+            q[a:a + 3] += h * qvel[d:d + 3]
+            w = np.asarray(qvel[d + 3:d + 6], dtype=np.float64)
+            th = np.linalg.norm(w) * h
+            dq = np.array([1.0, 0, 0, 0]) if th == 0 else np.concatenate([[np.cos(th / 2)],
+                                                                           np.sin(th / 2) * w / np.linalg.norm(w)])
+            w1, x1, y1, z1 = q[a + 3:a + 7]
+            w2, x2, y2, z2 = dq
+            q[a + 3:a + 7] = [w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+                              w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2]
+        elif jt in (HINGE, SLIDE):
+            q[a] += h * qvel[d]
+    return q
+
+
+def kinetic_energy_fd(model, qpos, qvel, h=1e-5):
+    """Kinetic energy from central differences of the body motion."""
+    Tm, Tp = kinematics(model, integrate(model, qpos, qvel, -h)), kinematics(model, integrate(model, qpos, qvel, h))
+    T0 = kinematics(model, qpos)
+    E = 0.0
+    for b in range(model.nbody):
+        cm = Tm[b][:3, :3] @ model.com[b] + Tm[b][:3, 3]
+        cp = Tp[b][:3, :3] @ model.com[b] + Tp[b][:3, 3]
+        v = (cp - cm) / (2 * h)
+        dR = (Tp[b][:3, :3] - Tm[b][:3, :3]) / (2 * h)
+        R = T0[b][:3, :3]
+        Wx = dR @ R.T
+        w = np.array([Wx[2, 1] - Wx[1, 2], Wx[0, 2] - Wx[2, 0], Wx[1, 0] - Wx[0, 1]]) / 2
+        Iw = R @ model.inertia[b] @ R.T
+        E += 0.5 * model.mass[b] * v @ v + 0.5 * w @ Iw @ w
+    return E
+
+
+def potential_energy(model, qpos):
+    T = kinematics(model, qpos)
+    g = np.asarray(model.gravity, dtype=np.float64)
+    return -sum(model.mass[b] * g @ (T[b][:3, :3] @ model.com[b] + T[b][:3, 3]) for b in range(model.nbody))

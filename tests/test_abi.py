@@ -41,6 +41,7 @@ def test_struct_layouts_match_header():
     from mpx_gb300 import _lib
     import subprocess, tempfile
     src = r'''
+#include <stddef.h>
 #include <stdio.h>
 #include "mpxg.h"
 int main(void) {
@@ -48,6 +49,8 @@ int main(void) {
          sizeof(mpxg_batch_io), sizeof(mpxg_lq_io), sizeof(mpxg_xla_opaque), sizeof(mpxg_served_model),
          sizeof(mpxg_server_desc), sizeof(mpxg_result));
   printf("%zu %zu\n", sizeof(mpxg_lq_eq_io), sizeof(mpxg_vjp_io));
+  printf("%zu %zu %zu\n", sizeof(mpxg_wb_model), offsetof(mpxg_wb_model, gravity),
+         offsetof(mpxg_wb_model, contact_point_pos));
   return 0;
 }
 '''
@@ -60,7 +63,8 @@ int main(void) {
     assert sizes == [ctypes.sizeof(_lib.ProblemDesc), ctypes.sizeof(_lib.SolverOpts), ctypes.sizeof(_lib.BatchIO),
                      ctypes.sizeof(_lib.LqIO), ctypes.sizeof(_lib.XlaOpaque), ctypes.sizeof(_lib.ServedModel),
                      ctypes.sizeof(_lib.ServerDesc), ctypes.sizeof(_lib.Result), ctypes.sizeof(_lib.LqEqIO),
-                     ctypes.sizeof(_lib.VjpIO)]
+                     ctypes.sizeof(_lib.VjpIO), ctypes.sizeof(_lib.WbModel), _lib.WbModel.gravity.offset,
+                     _lib.WbModel.contact_point_pos.offset]
 
 
 def test_xla_target_rejects_a_malformed_opaque():
@@ -92,3 +96,41 @@ def test_lqr_eq_rejects_bad_method_and_unaligned_workspace():
     assert L.mpxg_lqr_eq_solve_method(None, ctypes.byref(io), 0) == 1
     assert b"16-byte aligned" in L.mpxg_last_error(None)
     assert L.mpxg_lqr_eq_solve(None, ctypes.byref(io)) == 1
+
+
+def test_wb_calls_reject_malformed_models():
+    """mpxg_wb_terms / mpxg_wb_interface check the model before any launch
+    (the kernel indexes its shared arrays by these fields)."""
+    from mpx_gb300 import _lib, mjcf
+    L = _lib.load()
+    model = mjcf.load_npz(os.path.join(ROOT, "tests", "golden", "aliengo_wb.npz"))
+    fake = ctypes.c_void_p(1 << 20)  # never dereferenced: the checks fail first
+
+    def terms(S):
+        return L.mpxg_wb_terms(None, ctypes.byref(S), 4, fake, fake, fake, fake, fake, fake, fake)
+
+    def iface(S):
+        return L.mpxg_wb_interface(None, ctypes.byref(S), 4, *([fake] * 10))
+
+    S = model.to_struct()
+    S.parent[3] = 5                      # a child listed before its parent
+    assert terms(S) == 1 and b"parents first" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    S.nv = 17
+    assert terms(S) == 1 and b"nv / nq" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    S.dof_adr[2] = 8
+    assert terms(S) == 1 and b"dense" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    S.contact_jac_body[1] = 13
+    assert terms(S) == 1 and b"contact body" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    S.jnt_type[4] = 1                    # a second free joint
+    assert terms(S) == 1 and b"free joint" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    S.n_contact = 3                      # nv != 6 + 3 x contacts
+    assert iface(S) == 1 and b"free root" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    assert L.mpxg_wb_interface(None, ctypes.byref(S), 4, *([fake] * 8), None, fake) == 1  # tau NULL
+    assert b"null pointer" in L.mpxg_last_error(None)
+    assert L.mpxg_wb_terms(None, ctypes.byref(S), 0, None, None, None, None, None, None, None) == 0

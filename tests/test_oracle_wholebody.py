@@ -1,0 +1,166 @@
+"""The whole-body oracle (oracle/wholebody.py) and the MJCF reader.
+
+The oracle is pinned by the reference's own numbers for its model (the
+aliengo foot positions at q0 that mpx/config/config_srbd.py:38-43 lists,
+x to 8 digits) and by identities of the mechanics that hold whatever
+algorithm computes M and qfrc_bias."""
+import copy
+import os
+
+import numpy as np
+import pytest
+
+from mpx_gb300 import mjcf
+from oracle import wholebody as W
+
+FIX = os.path.join(os.path.dirname(__file__), "golden", "aliengo_wb.npz")
+
+
+@pytest.fixture(scope="module")
+def model():
+    return mjcf.load_npz(FIX)
+
+
+def random_state(model, rng, spread=0.3):
+    q0 = np.load(FIX)["q0"]
+    quat = rng.normal(size=4)
+    qpos = np.concatenate([rng.normal(size=3) * spread, quat / np.linalg.norm(quat), q0 + rng.normal(size=12) * 0.2])
+    return qpos, rng.normal(size=model.nv)
+
+
+def test_feet_at_q0_match_the_reference_config(model):
+    z = np.load(FIX)
+    qpos = np.concatenate([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0], z["q0"]])
+    feet = W.terms(model, qpos, np.zeros(model.nv))["cpos"].reshape(4, 3)
+    ref = z["p_legs0"].reshape(4, 3)
+    assert np.abs(feet[:, 0] - ref[:, 0]).max() < 1e-8      # listed to 8 digits
+    assert np.abs(feet[:, 1] - ref[:, 1]).max() < 1e-3      # listed to 3 digits
+
+
+def test_model_totals(model):
+    assert model.nbody == 13 and model.nv == 18 and model.nq == 19
+    assert abs(model.mass.sum() - 24.638) < 1e-9
+    assert np.allclose(model.armature, [0.0] * 6 + [0.01] * 12)   # <freejoint/> takes no armature
+    assert np.allclose(model.gravity, [0.0, 0.0, -9.806])
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_mass_matrix_is_the_kinetic_energy(model, seed):
+    """1/2 v'(M - armature)v equals the kinetic energy of the finite-differenced
+    body motion, for several velocities (which pins the quadratic form)."""
+    rng = np.random.default_rng(seed)
+    qpos, _ = random_state(model, rng)
+    M = W.terms(model, qpos, np.zeros(model.nv))["M"]
+    assert np.abs(M - M.T).max() < 1e-12
+    assert np.linalg.eigvalsh(M).min() > 0
+    Mb = M - np.diag(model.armature)
+    for _ in range(4):
+        v = rng.normal(size=model.nv)
+        ke = W.kinetic_energy_fd(model, qpos, v)
+        assert abs(0.5 * v @ Mb @ v - ke) <= 1e-7 * ke
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_velocity_product_terms_match_second_differences(model, seed):
+    """dJ qdot of every contact point and every body's centre of mass equals
+    the second difference of the point along the qacc = 0 motion."""
+    rng = np.random.default_rng(10 + seed)
+    qpos, qvel = random_state(model, rng)
+    T = W.kinematics(model, qpos)
+    Wb, _ = W._body_velocity(model, T, qvel)
+    h = 1e-4
+    Tp, Tm = W.kinematics(model, W.integrate(model, qpos, qvel, h)), W.kinematics(model, W.integrate(model, qpos, qvel, -h))
+    for b in range(model.nbody):
+        pt = lambda TT: TT[b][:3, :3] @ model.com[b] + TT[b][:3, 3]
+        a_fd = (pt(Tp) - 2 * pt(T) + pt(Tm)) / h ** 2
+        a_an, w_an = W._dJ_qdot(model, T, qvel, Wb, b, pt(T))
+        assert np.abs(a_fd - a_an).max() < 1e-5 * (1 + np.abs(a_an).max())
+        # angular: d/dt of the body's angular velocity
+        def omega(s):
+            TT = W.kinematics(model, W.integrate(model, qpos, qvel, s))
+            return W._body_velocity(model, TT, qvel)[0][b]
+        wd_fd = (omega(h) - omega(-h)) / (2 * h)
+        assert np.abs(wd_fd - w_an).max() < 1e-5 * (1 + np.abs(w_an).max())
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_gravity_forces_are_the_potential_gradient(model, seed):
+    rng = np.random.default_rng(20 + seed)
+    qpos, _ = random_state(model, rng)
+    bias = W.terms(model, qpos, np.zeros(model.nv))["bias"]
+    h = 1e-6
+    grad = np.array([(W.potential_energy(model, W.integrate(model, qpos, e, h)) -
+                      W.potential_energy(model, W.integrate(model, qpos, e, -h))) / (2 * h) for e in np.eye(model.nv)])
+    assert np.abs(bias - grad).max() < 1e-6 * np.abs(grad).max()
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_power_balance(model, seed):
+    """qdot' bias(g = 0) = 1/2 qdot' (dM/dt) qdot at qacc = 0."""
+    rng = np.random.default_rng(30 + seed)
+    qpos, qvel = random_state(model, rng)
+    m0 = copy.deepcopy(model)
+    m0.gravity = np.zeros(3)
+    b0 = W.terms(m0, qpos, qvel)["bias"]
+    h = 1e-5
+    dM = (W.terms(model, W.integrate(model, qpos, qvel, h), qvel)["M"] -
+          W.terms(model, W.integrate(model, qpos, qvel, -h), qvel)["M"]) / (2 * h)
+    lhs, rhs = qvel @ b0, 0.5 * qvel @ dM @ qvel
+    assert abs(lhs - rhs) < 1e-6 * (1 + abs(rhs))
+
+
+def test_jacobian_is_the_point_velocity(model):
+    rng = np.random.default_rng(40)
+    qpos, qvel = random_state(model, rng)
+    t = W.terms(model, qpos, qvel)
+    h = 1e-6
+    fd = (W.terms(model, W.integrate(model, qpos, qvel, h), qvel)["cpos"] -
+          W.terms(model, W.integrate(model, qpos, qvel, -h), qvel)["cpos"]) / (2 * h)
+    assert np.abs(fd - t["cvel"]).max() < 1e-7
+
+
+def test_interface_pinv_equals_normal_equations(model):
+    """pinv(J') a = J (J'J)^-1 a for the full-rank J' of a standing robot: the
+    kernel's formula gives the reference's jnp.linalg.pinv result."""
+    rng = np.random.default_rng(50)
+    for _ in range(5):
+        qpos, qvel = random_state(model, rng)
+        J = W.terms(model, qpos, qvel)["J"]
+        a = rng.normal(size=12)
+        assert np.allclose(np.linalg.pinv(J.T) @ a, J @ np.linalg.solve(J.T @ J, a), rtol=1e-9, atol=1e-10)
+
+
+def test_interface_mask_selects_mpc_or_feedback(model):
+    rng = np.random.default_rng(60)
+    qpos, qvel = random_state(model, rng)
+    Kp, Kd = np.diag([100.0] * 12), np.diag([5.0] * 12)
+    grf, fr, frd = rng.normal(size=12) * 50, rng.normal(size=12) * 0.1, rng.normal(size=12) * 0.1
+    t_all, J = W.interface(model, Kp, Kd, qpos, qvel, grf, fr, frd, [1, 1, 1, 1])
+    t_none, _ = W.interface(model, Kp, Kd, qpos, qvel, grf, fr, frd, [0, 0, 0, 0])
+    t_mix, _ = W.interface(model, Kp, Kd, qpos, qvel, grf, fr, frd, [1, 0, 0, 1])
+    assert np.allclose(t_all, -(J @ grf)[6:])
+    assert np.allclose(t_mix, np.concatenate([t_all[:3], t_none[3:9], t_all[9:]]))
+
+
+MJCF = open(os.path.join(os.path.dirname(__file__), "golden", "slider_arm.xml")).read()
+
+
+def test_reader_resolves_defaults_orientations_and_geoms():
+    m = mjcf.parse(MJCF, ["tip"], ["slider"])
+    assert m.body_names == ["base", "link", "slider"]
+    assert list(m.jnt_type) == [mjcf.JNT_FREE, mjcf.JNT_HINGE, mjcf.JNT_SLIDE]
+    assert np.allclose(m.armature, [0.0] * 6 + [0.05, 0.02])      # childclass, then class="main"
+    assert np.allclose(m.jnt_axis[1], [0, 1, 0]) and np.allclose(m.jnt_pos[1], [0, 0, 0.05])
+    assert np.allclose(m.body_quat[0], [np.cos(np.pi / 4), 0, 0, np.sin(np.pi / 4)])
+    assert np.allclose(m.inertia[0], [[0.1, 0.01, 0], [0.01, 0.2, 0], [0, 0, 0.3]])
+    assert np.allclose(m.contact_point_pos[0], [0, 0, -0.05])
+    assert m.nq == 9 and m.nv == 8
+
+
+def test_reader_rejects_what_it_cannot_represent():
+    two = MJCF.replace('<joint name="j1" pos="0 0 0.05"/>', '<joint name="j1"/><joint name="j1b"/>')
+    with pytest.raises(NotImplementedError):
+        mjcf.parse(two)
+    no_inertial = MJCF.replace('<inertial pos="0 0 -0.1" mass="1" diaginertia="0.01 0.01 0.001"/>', '<geom size="0.1"/>')
+    with pytest.raises(NotImplementedError):
+        mjcf.parse(no_inertial)
