@@ -517,6 +517,19 @@ static const char* wb_check(const mpxg_wb_model* m) {
   return nullptr;
 }
 
+// The smallest capacity the (checked) model fits.
+extern "C++" {
+template <bool IFACE>
+static cudaError_t wb_launch(const mpxg_wb_model& m, int batch, const mpxg::wb::Args& a, cudaStream_t st) {
+  using namespace mpxg::wb;
+  if (m.nbody <= CapQuad::MB && m.nv <= CapQuad::MD && m.nq <= CapQuad::MD + 4 && 3 * m.n_contact <= CapQuad::MR)
+    wb_kernel<IFACE, CapQuad><<<(batch + CapQuad::NW - 1) / CapQuad::NW, 32 * CapQuad::NW, 0, st>>>(m, batch, a);
+  else
+    wb_kernel<IFACE, CapAny><<<(batch + CapAny::NW - 1) / CapAny::NW, 32 * CapAny::NW, 0, st>>>(m, batch, a);
+  return cudaGetLastError();
+}
+}
+
 mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, const float* qpos, const float* qvel,
                           float* M, float* bias, float* cpos, float* J, float* cvel) {
   using namespace mpxg::wb;
@@ -526,8 +539,7 @@ mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, c
   if (batch == 0) return MPXG_OK;
   Args a{};
   a.qpos = qpos; a.qvel = qvel; a.M = M; a.bias = bias; a.cpos = cpos; a.J = J; a.cvel = cvel;
-  wb_kernel<false><<<(batch + kWarps - 1) / kWarps, 32 * kWarps, 0, (cudaStream_t)stream>>>(*model, batch, a);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = wb_launch<false>(*model, batch, a, (cudaStream_t)stream);
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
 }
 
@@ -547,8 +559,7 @@ mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batc
   Args a{};
   a.qpos = qpos; a.qvel = qvel; a.grf = grf; a.foot_ref = foot_ref; a.foot_ref_dot = foot_ref_dot;
   a.contact = contact; a.Kp = Kp; a.Kd = Kd; a.tau = tau; a.J = J;
-  wb_kernel<true><<<(batch + kWarps - 1) / kWarps, 32 * kWarps, 0, (cudaStream_t)stream>>>(*model, batch, a);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = wb_launch<true>(*model, batch, a, (cudaStream_t)stream);
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
 }
 

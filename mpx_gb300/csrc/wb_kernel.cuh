@@ -27,8 +27,16 @@
 namespace mpxg {
 namespace wb {
 
-constexpr int kMB = MPXG_WB_MAX_BODY, kMD = MPXG_WB_MAX_DOF, kMR = 3 * MPXG_WB_MAX_CONTACT;
-constexpr int kWarps = 2;  // environments per block
+// Shared-memory capacities of the two instantiations: any model the ABI
+// accepts, and models up to 16 bodies, 20 dofs and 4 contacts (a quadruped
+// with a floating base and 12 joints), whose smaller per-warp footprint lets
+// 27 environments share an SM (4096 in one wave on 152 SMs).
+template <int MB_, int MD_, int MC_, int NW_, int MINB_>
+struct Cap {
+  static constexpr int MB = MB_, MD = MD_, MR = 3 * MC_, NW = NW_, MINB = MINB_;
+};
+using CapAny = Cap<MPXG_WB_MAX_BODY, MPXG_WB_MAX_DOF, MPXG_WB_MAX_CONTACT, 2, 1>;
+using CapQuad = Cap<16, 20, 4, 3, 9>;
 
 struct Args {
   const float *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd;
@@ -36,17 +44,19 @@ struct Args {
   float *M, *bias, *cpos, *J, *cvel, *tau;
 };
 
+template <class C>
 struct Warp {
-  float quat[kMB][4], R[kMB][9], xp[kMB][3];
-  float S[kMD][6];                 // per dof: (omega; linear velocity at o)
-  float V[kMB][6], F[kMB][6], Fc[kMB][6];
-  float Ib[kMB][10], Ic[kMB][10];  // (m, h = m c, J_o upper triangle xx xy xz yy yz zz)
-  float M[kMD][kMD + 1];
-  float J[kMD][kMR + 1];
-  float bias[kMD], qpos[kMD + 4], qvel[kMD], w[kMD];
-  float cpos[kMR], cvel[kMR], a[kMR], y[kMR];
-  int dof_body[kMD], depth[kMB];
-  unsigned anc[kMB];               // bit a set: a is b or an ancestor of b
+  static constexpr int MB = C::MB, MD = C::MD, MR = C::MR;
+  float quat[MB][4], R[MB][9], xp[MB][3];
+  float S[MD][6];                 // per dof: (omega; linear velocity at o)
+  float V[MB][6], F[MB][6], Fc[MB][6];
+  float Ib[MB][10], Ic[MB][10];   // (m, h = m c, J_o upper triangle xx xy xz yy yz zz)
+  float M[MD][MD + 1];
+  float J[MD][MR + 1];
+  float bias[MD], qpos[MD + 4], qvel[MD], w[MD];
+  float cpos[MR], cvel[MR], a[MR], y[MR];
+  int dof_body[MD], depth[MB], par[MB], jtyp[MB], dadr[MB];
+  unsigned anc[MB];               // bit a set: a is b or an ancestor of b
 };
 
 __host__ __device__ __forceinline__ int ndof(int jt) { return jt == 1 ? 6 : (jt >= 2 ? 1 : 0); }
@@ -120,41 +130,51 @@ __device__ __forceinline__ float dot6(const float* a, const float* b) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
 }
 
-// The model must have passed the host checks of mpxg_wb_terms: parents
+// The model must have passed the host checks of mpxg_wb_terms (parents
 // precede children, one joint per body, the free joint only on body 0, dof and
-// qpos addresses dense in body order, nbody, nv <= 32, nq <= nv + 4, at most
-// 8 contacts on existing bodies.
-template <bool IFACE>
-__global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch, Args a) {
-  __shared__ Warp sw[kWarps];
+// qpos addresses dense in body order, contacts on existing bodies) and fit the
+// capacity C: nbody <= MB, nv <= MD, nq <= MD + 4, 3 x contacts <= MR.
+template <bool IFACE, class C>
+__global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch,
+                                                                 Args a) {
+  constexpr int MB = C::MB, MR = C::MR;
+  __shared__ Warp<C> sw[C::NW];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int env = blockIdx.x * kWarps + wid;
+  const int env = blockIdx.x * C::NW + wid;
   if (env >= batch) return;  // the whole warp leaves; no block-wide barrier follows
-  Warp& s = sw[wid];
+  Warp<C>& s = sw[wid];
   const unsigned full = 0xffffffffu;
   const int nb = m.nbody, nq = m.nq, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
   for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * nq + i];
   if (lane < nv) s.qvel[lane] = a.qvel[(size_t)env * nv + lane];
+  // the tree's indices in shared memory: the chain walks below read them at
+  // lane-dependent positions
+  if (lane < nb) {
+    s.par[lane] = m.parent[lane];
+    s.jtyp[lane] = m.jnt_type[lane];
+    s.dadr[lane] = m.dof_adr[lane];
+  }
+  __syncwarp();
   int dep = 0;
   if (lane < nb) {
     unsigned mask = 0;
     int b = lane;
-    for (int g = 0; g < kMB && b >= 0; ++g) {
+    for (int g = 0; g < MB && b >= 0; ++g) {
       mask |= 1u << b;
-      b = m.parent[b];
+      b = s.par[b];
       ++dep;
     }
     s.anc[lane] = mask;
     s.depth[lane] = dep - 1;
-    const int jt = m.jnt_type[lane];
-    for (int k = 0; k < ndof(jt); ++k) s.dof_body[m.dof_adr[lane] + k] = lane;
+    const int jt = s.jtyp[lane];
+    for (int k = 0; k < ndof(jt); ++k) s.dof_body[s.dadr[lane] + k] = lane;
   }
   __syncwarp();
   // ---- 1. forward kinematics, one tree level per step
   const int maxd = __reduce_max_sync(full, lane < nb ? dep - 1 : 0);
   for (int d = 0; d <= maxd; ++d) {
     if (lane < nb && s.depth[lane] == d) {
-      const int b = lane, p = m.parent[b], jt = m.jnt_type[b];
+      const int b = lane, p = s.par[b], jt = s.jtyp[b];
       float q[4], x[3];
       if (jt == 1) {
         const float* qp = s.qpos + m.qpos_adr[b];
@@ -216,7 +236,7 @@ __global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__
   const float o[3] = {s.xp[0][0], s.xp[0][1], s.xp[0][2]};
   // ---- 2. dof axes and body inertias about o
   if (lane < nb) {
-    const int b = lane, jt = m.jnt_type[b], da = m.dof_adr[b];
+    const int b = lane, jt = s.jtyp[b], da = s.dadr[b];
     const float* R = s.R[b];
     const float* xb = s.xp[b];
     float c[3];
@@ -277,8 +297,8 @@ __global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__
   if (lane < nb) {
     float Vb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int b = lane;
-    for (int g = 0; g < kMB && b >= 0; ++g, b = m.parent[b]) {
-      const int nd = ndof(m.jnt_type[b]), da = m.dof_adr[b];
+    for (int g = 0; g < MB && b >= 0; ++g, b = s.par[b]) {
+      const int nd = ndof(s.jtyp[b]), da = s.dadr[b];
       for (int k = 0; k < nd; ++k) {
         const float qd = s.qvel[da + k];
 #pragma unroll
@@ -293,8 +313,8 @@ __global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__
   if (lane < nb) {
     float A[6] = {0.0f, 0.0f, 0.0f, -m.gravity[0], -m.gravity[1], -m.gravity[2]};
     int b = lane;
-    for (int g = 0; g < kMB && b >= 0; ++g, b = m.parent[b]) {
-      const int jt = m.jnt_type[b], nd = ndof(jt), da = m.dof_adr[b];
+    for (int g = 0; g < MB && b >= 0; ++g, b = s.par[b]) {
+      const int jt = s.jtyp[b], nd = ndof(jt), da = s.dadr[b];
       // the free joint's translation axes are fixed in the world: no derivative
       for (int k = (jt == 1 ? 3 : 0); k < nd; ++k) {
         float t[6];
@@ -394,9 +414,9 @@ __global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__
   }
   __syncwarp();
   // y = (J'J)^-1 a by Gauss-Jordan on [J'J | a], lane c holding column c
-  float col[kMR];
+  float col[MR];
 #pragma unroll
-  for (int i = 0; i < kMR; ++i) {
+  for (int i = 0; i < MR; ++i) {
     float g = 0.0f;
     if (i < nr) {
       if (lane < nr) {
@@ -408,12 +428,12 @@ __global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__
     col[i] = g;
   }
 #pragma unroll
-  for (int k = 0; k < kMR; ++k) {
+  for (int k = 0; k < MR; ++k) {
     if (k < nr) {
       const float dk = __shfl_sync(full, col[k], k);
       const float yk = col[k] / dk;
 #pragma unroll
-      for (int i = 0; i < kMR; ++i) {
+      for (int i = 0; i < MR; ++i) {
         if (i < nr && i != k) {
           const float gik = __shfl_sync(full, col[i], k);
           col[i] -= gik * yk;
@@ -424,7 +444,7 @@ __global__ void __launch_bounds__(32 * kWarps) wb_kernel(const __grid_constant__
   }
   if (lane == nr) {
 #pragma unroll
-    for (int i = 0; i < kMR; ++i)
+    for (int i = 0; i < MR; ++i)
       if (i < nr) s.y[i] = col[i];
   }
   __syncwarp();

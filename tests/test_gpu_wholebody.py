@@ -142,3 +142,59 @@ def test_srbd_wrapper_whole_body_run(cuda):
         assert close(tau[b], rt, 5e-5), b
     assert torch.equal(wr.torch_whole_body_run(torch.as_tensor(qpos), torch.as_tensor(qvel)),
                        torch.as_tensor(tau, device=cuda))
+
+
+def hexapod_mjcf():
+    """A floating base with six 3-joint legs (19 bodies, 24 dofs, 6 feet):
+    larger than the compact kernel capacity, so the general one runs."""
+    legs = []
+    for i in range(6):
+        ang = 60.0 * i + 30.0
+        x, y = 0.25 * np.cos(np.radians(ang)), 0.15 * np.sin(np.radians(ang))
+        legs.append('''
+      <body name="L%d_hip" pos="%.4f %.4f 0" euler="0 0 %.1f">
+        <joint name="L%d_a" axis="0 0 1"/>
+        <inertial pos="0.03 0 0" mass="0.4" diaginertia="0.001 0.0012 0.0009"/>
+        <body name="L%d_thigh" pos="0.06 0 0">
+          <joint name="L%d_b" axis="0 1 0"/>
+          <inertial pos="0.05 0 -0.01" quat="0.9 0.1 0 0.2" mass="0.3" diaginertia="0.002 0.0021 0.0004"/>
+          <body name="L%d_shin" pos="0.12 0 0" euler="0 30 0">
+            <joint name="L%d_c" axis="0 1 0" pos="0 0 0.01"/>
+            <inertial pos="0 0 -0.08" mass="0.15" diaginertia="0.0015 0.0015 0.0001"/>
+            <geom name="F%d" size="0.02" pos="0 0 -0.16"/>
+          </body>
+        </body>
+      </body>''' % (i, x, y, ang, i, i, i, i, i, i))
+    return '''<mujoco><compiler angle="degree"/><default><joint armature="0.005"/></default><worldbody>
+      <body name="torso" pos="0 0 0.3"><freejoint/>
+        <inertial pos="0.01 0 0" mass="4" diaginertia="0.05 0.08 0.1"/>%s
+      </body></worldbody></mujoco>''' % "".join(legs)
+
+
+def test_general_capacity_model_matches_oracle(cuda):
+    model = mjcf.parse(hexapod_mjcf(), ["F%d" % i for i in range(6)], ["L%d_shin" % i for i in range(6)])
+    assert model.nbody == 19 and model.nv == 24 and len(model.contact_point_body) == 6
+    wb = WholeBodyModel(model, device=cuda)
+    B = 41
+    rng = np.random.default_rng(9)
+    quat = rng.normal(size=(B, 4))
+    quat /= np.linalg.norm(quat, axis=1, keepdims=True)
+    qpos = np.concatenate([rng.normal(size=(B, 3)) * 0.3, quat,
+                           np.tile([0.0, 0.5, -1.2], (B, 6)) + rng.normal(size=(B, 18)) * 0.3], axis=1)
+    qpos, qvel = qpos.astype(np.float32), rng.normal(size=(B, 24)).astype(np.float32)
+    out = {k: v.cpu().numpy() for k, v in wb.terms(qpos, qvel).items()}
+    Kp, Kd = np.diag([80.0] * 18), np.diag([4.0] * 18)
+    grf = (rng.normal(size=(B, 18)) * 10).astype(np.float32)
+    fr = (rng.normal(size=(B, 18)) * 0.05).astype(np.float32)
+    frd = (rng.normal(size=(B, 18)) * 0.2).astype(np.float32)
+    contact = rng.integers(0, 2, size=(B, 6)).astype(np.int32)
+    tau, _ = wb.interface(qpos, qvel, grf, fr, frd, contact, Kp, Kd)
+    tau = tau.cpu().numpy()
+    for b in range(B):
+        ref = W.terms(model, qpos[b], qvel[b])
+        for k in ("M", "bias", "cpos", "J", "cvel"):
+            assert close(out[k][b], ref[k], 2e-5), (k, b)
+        rt, _ = W.interface(model, Kp, Kd, qpos[b], qvel[b], grf[b], fr[b], frd[b], contact[b])
+        # cond(J'J) reaches 5.5e3 on these states: float32 evaluation of the
+        # interface formula alone moves tau by up to 5e-5 relative
+        assert close(tau[b], rt, 5e-4), b
