@@ -11,8 +11,8 @@ interface):
   * `<inertial>`: `mass`, `pos`, orientation, `diaginertia` or `fullinertia`;
   * one joint per body: `<freejoint/>` (no armature: MuJoCo's shortcut for a
     free joint with zero armature, damping and friction loss) or `<joint>`
-    with `type` hinge / slide / free, `axis`, `pos`, `armature`, resolved
-    through the `<default>` classes (`class`, `childclass`);
+    with `type` hinge / slide / free, `axis`, `pos`, `ref`, `armature`,
+    resolved through the `<default>` classes (`class`, `childclass`);
   * `<option gravity>`;
   * the named geoms used as contact points (their `pos`, or the middle of
     `fromto`).
@@ -295,8 +295,24 @@ def parse(source, contact_geoms=None, contact_bodies=None):
             jt.append(t)
             jpos.append(_vec(defaults.get(j, "joint", "pos", cls) or "0 0 0", 3) if t != JNT_FREE else np.zeros(3))
             ax = _vec(defaults.get(j, "joint", "axis", cls) or "0 0 1", 3)
-            jaxis.append(ax / np.linalg.norm(ax))
+            ax = ax / np.linalg.norm(ax)
+            jaxis.append(ax)
             armature.extend([arm] * _NDOF[t])
+            # MuJoCo measures a hinge / slide coordinate from the joint's
+            # `ref`.  Rotations about one axis commute, so the offset folds
+            # into the body's rest pose: the body turns by -ref about the axis
+            # through the anchor (or moves by -ref along it), and q then
+            # enters the kinematics as it is.
+            ref = float(defaults.get(j, "joint", "ref", cls) or 0.0)
+            if ref != 0.0 and t == JNT_HINGE:
+                deg = compiler.get("angle", "degree") == "degree"
+                th = -ref * (np.pi / 180.0 if deg else 1.0)
+                Rb = quat_to_mat(bquat[-1])
+                anchor = bpos[-1] + Rb @ jpos[-1]
+                bquat[-1] = _quat_mul(bquat[-1], _axis_quat(ax, th))
+                bpos[-1] = anchor - quat_to_mat(bquat[-1]) @ jpos[-1]
+            elif ref != 0.0 and t == JNT_SLIDE:
+                bpos[-1] = bpos[-1] - quat_to_mat(bquat[-1]) @ ax * ref
         for g in own_geoms:
             gname = g.get("name")
             if gname is None:

@@ -164,3 +164,52 @@ def test_reader_rejects_what_it_cannot_represent():
     no_inertial = MJCF.replace('<inertial pos="0 0 -0.1" mass="1" diaginertia="0.01 0.01 0.001"/>', '<geom size="0.1"/>')
     with pytest.raises(NotImplementedError):
         mjcf.parse(no_inertial)
+
+
+def test_reader_folds_joint_ref_into_the_rest_pose():
+    """A hinge (slide) with `ref` at coordinate q places its body as the same
+    joint without `ref` at q - ref (MuJoCo's qpos - qpos0)."""
+    with_ref = MJCF.replace('<joint name="j1" pos="0 0 0.05"/>', '<joint name="j1" pos="0 0 0.05" ref="25"/>')
+    with_ref = with_ref.replace('type="slide" axis="0 0 1"', 'type="slide" axis="0 0 1" ref="0.03"')
+    a, b = mjcf.parse(with_ref, ["tip"], ["slider"]), mjcf.parse(MJCF, ["tip"], ["slider"])
+    rng = np.random.default_rng(70)
+    for _ in range(3):
+        quat = rng.normal(size=4)
+        qpos = np.concatenate([rng.normal(size=3), quat / np.linalg.norm(quat), rng.normal(size=2)])
+        shifted = qpos.copy()
+        shifted[7] -= np.radians(25.0)
+        shifted[8] -= 0.03
+        qvel = rng.normal(size=8)
+        ta, tb = W.terms(a, qpos, qvel), W.terms(b, shifted, qvel)
+        for k in ("M", "bias", "cpos", "J"):
+            assert np.allclose(ta[k], tb[k], atol=1e-12), k
+
+
+def test_reader_orientation_forms():
+    """quat, axisangle and euler (intrinsic lower case, extrinsic upper case,
+    degrees or radians) give the same frames."""
+    base = '<mujoco><compiler angle="%s" %s/><worldbody><body name="b" %s>' \
+           '<inertial pos="0 0 0" mass="1" diaginertia="1 1 1"/></body></worldbody></mujoco>'
+    q_xyz = mjcf._quat_mul(mjcf._quat_mul(mjcf._axis_quat([1, 0, 0], 0.3), mjcf._axis_quat([0, 1, 0], -0.2)),
+                           mjcf._axis_quat([0, 0, 1], 0.5))
+    forms = [base % ("radian", "", 'quat="%.17g %.17g %.17g %.17g"' % tuple(q_xyz)),
+             base % ("radian", "", 'euler="0.3 -0.2 0.5"'),
+             base % ("degree", "", 'euler="%.17g %.17g %.17g"' % tuple(np.degrees([0.3, -0.2, 0.5]))),
+             base % ("radian", 'eulerseq="ZYX"', 'euler="0.5 -0.2 0.3"')]
+    for f in forms:
+        q = mjcf.parse(f).body_quat[0]
+        assert np.allclose(mjcf.quat_to_mat(q), mjcf.quat_to_mat(q_xyz), atol=1e-12), f
+    aa = mjcf.parse(base % ("degree", "", 'axisangle="0 0 1 90"')).body_quat[0]
+    assert np.allclose(mjcf.quat_to_mat(aa), [[0, -1, 0], [1, 0, 0], [0, 0, 1]], atol=1e-12)
+
+
+def test_reader_default_classes_inherit():
+    xml = '''<mujoco><default><joint armature="0.1" axis="1 0 0"/>
+      <default class="a"><joint armature="0.2"/><default class="b"><joint axis="0 1 0"/></default></default>
+    </default><worldbody><body name="r"><freejoint/><inertial pos="0 0 0" mass="1" diaginertia="1 1 1"/>
+      <body name="c1" childclass="b"><joint/><inertial pos="0 0 0" mass="1" diaginertia="1 1 1"/>
+        <body name="c2"><joint class="a"/><inertial pos="0 0 0" mass="1" diaginertia="1 1 1"/></body>
+      </body></body></worldbody></mujoco>'''
+    m = mjcf.parse(xml)
+    assert np.allclose(m.armature[6:], [0.2, 0.2])           # b inherits a's armature
+    assert np.allclose(m.jnt_axis[1], [0, 1, 0]) and np.allclose(m.jnt_axis[2], [1, 0, 0])
