@@ -252,3 +252,190 @@ def potential_energy(model, qpos):
     T = kinematics(model, qpos)
     g = np.asarray(model.gravity, dtype=np.float64)
     return -sum(model.mass[b] * g @ (T[b][:3, :3] @ model.com[b] + T[b][:3, 3]) for b in range(model.nbody))
+
+
+# ----------------------------------------------------------------- the whole-body MPC model
+# quadruped_wb_dynamics (mpx/utils/models.py:39-117) and its cost and
+# Gauss-Newton Hessian (mpx/utils/objectives.py:77-203), the model the
+# reference's whole-body configurations (config_aliengo.py:66-68,
+# config_go2.py:67-69) hand to its solver.  State x = [p (3), quat (4),
+# q (nj), v (3), omega (3, body frame), dq (nj), foot positions (3C),
+# grf (3C)], control u = joint torques (nj).
+
+
+def _qmul(a, b):
+    w1, x1, y1, z1 = a
+    w2, x2, y2, z2 = b
+    return np.array([w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+                     w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2])
+
+
+def quat_integrate(q, w, dt):
+    """q * exp(w dt / 2) renormalised, w in the body frame (mjx math)."""
+    w = np.asarray(w, dtype=np.float64)
+    n = np.linalg.norm(w)
+    axis = w / n if n > 0 else np.zeros(3)
+    half = 0.5 * n * dt
+    out = _qmul(np.asarray(q, dtype=np.float64), np.concatenate([[np.cos(half)], np.sin(half) * axis]))
+    return out / np.linalg.norm(out)
+
+
+def quat_sub(u, v):
+    """The rotation vector of conj(v) * u, angle in (-pi, pi] (mjx math)."""
+    q = _qmul(np.asarray(v, dtype=np.float64) * [1, -1, -1, -1], np.asarray(u, dtype=np.float64))
+    n = np.linalg.norm(q[1:])
+    axis = q[1:] / n if n > 0 else np.zeros(3)
+    ang = 2 * np.arctan2(n, q[0])
+    if ang > np.pi:
+        ang -= 2 * np.pi
+    return axis * ang
+
+
+def quat_sub_jacobian(u, v):
+    """d quat_sub(u, v) / du (3 x 4), from the chain rule through conj(v) * u
+    and the logarithm (theta = 2 atan2(|w|, s), result theta w / |w|)."""
+    vc = np.asarray(v, dtype=np.float64) * [1, -1, -1, -1]
+    a0, a1, a2, a3 = vc
+    L = np.array([[a0, -a1, -a2, -a3], [a1, a0, -a3, a2], [a2, a3, a0, -a1], [a3, -a2, a1, a0]])
+    q = L @ np.asarray(u, dtype=np.float64)
+    s, w = q[0], q[1:]
+    n = np.linalg.norm(w)
+    th = 2 * np.arctan2(n, s)
+    if th > np.pi:
+        th -= 2 * np.pi
+    a = w / n
+    r2 = s * s + n * n
+    d_ds = a * (-2 * n / r2)
+    d_dw = np.outer(a, a) * (2 * s / r2) + th * (np.eye(3) - np.outer(a, a)) / n
+    return np.column_stack([d_ds, d_dw]) @ L
+
+
+def wb_dynamics(model, dt, x, u, contact, alpha=25.0):
+    """models.py:39-117: contact forces that hold the feet (Baumgarte-
+    stabilised at the velocity level, -2 alpha J'v), masked by contact, then a
+    semi-implicit Euler step; the new state carries the feet at the current
+    configuration and the forces."""
+    x = np.asarray(x, dtype=np.float64)
+    nv = model.nv
+    nq = nv + 1
+    qpos, qvel = x[:nq], x[nq:nq + nv]
+    t = terms(model, qpos, qvel)
+    M, D, J, feet = t["M"], t["bias"], t["J"], t["cpos"]
+    tau = np.concatenate([np.zeros(6), np.asarray(u, dtype=np.float64)])
+    solve = lambda b: np.linalg.solve(M, b)
+    A = J.T @ solve(J)
+    rhs = -J.T @ solve(tau - D) - 2 * alpha * (J.T @ qvel)
+    grf = np.linalg.solve(A, rhs) * np.repeat(np.asarray(contact, dtype=np.float64), 3)
+    v = qvel + solve(tau - D + J @ grf) * dt
+    p = qpos[:3] + v[:3] * dt
+    quat = quat_integrate(qpos[3:7], v[3:6], dt)
+    q = qpos[7:] + v[6:] * dt
+    return np.concatenate([p, quat, q, v, feet, grf])
+
+
+def penalty(c, alpha=0.1, sigma=5.0):
+    """objectives.py:7-13: relaxed log barrier, clipped to [0, 1e8]."""
+    c = np.asarray(c, dtype=np.float64)
+    logb = -alpha * np.log(np.clip(c, 1e-10, 1e6))
+    quad = alpha / 2 * (np.square((c - 2 * sigma) / sigma) - 1)
+    return np.clip(np.where(c > sigma, logb, quad + logb), 0, 1e8)
+
+
+def penalty_dd(c, alpha=0.1, sigma=5.0):
+    """Second derivative of penalty() where it is smooth (0 where clipped)."""
+    c = np.asarray(c, dtype=np.float64)
+    logdd = np.where((c > 1e-10) & (c < 1e6), alpha / np.square(c), 0.0)
+    dd = np.where(c > sigma, logdd, alpha / sigma ** 2 + logdd)
+    raw = np.where(c > sigma, -alpha * np.log(np.clip(c, 1e-10, 1e6)),
+                   alpha / 2 * (np.square((c - 2 * sigma) / sigma) - 1) - alpha * np.log(np.clip(c, 1e-10, 1e6)))
+    return np.where((raw > 0) & (raw < 1e8), dd, 0.0)
+
+
+def _wb_split(nj, nc, x, u):
+    o = {}
+    o["p"], o["quat"], o["q"] = x[:3], x[3:7], x[7:7 + nj]
+    o["dp"], o["omega"], o["dq"] = x[7 + nj:10 + nj], x[10 + nj:13 + nj], x[13 + nj:13 + 2 * nj]
+    o["p_leg"], o["grf"] = x[13 + 2 * nj:13 + 2 * nj + 3 * nc], x[13 + 2 * nj + 3 * nc:]
+    o["tau"] = u[:nj]
+    return o
+
+
+def _wb_ref(nj, nc, r):
+    return dict(p=r[:3], quat=r[3:7], q=r[7:7 + nj], dp=r[7 + nj:10 + nj], omega=r[10 + nj:13 + nj],
+                p_leg=r[13 + nj:13 + nj + 3 * nc], contact=r[13 + nj + 3 * nc:13 + nj + 4 * nc],
+                grf=r[13 + nj + 4 * nc:13 + nj + 7 * nc])
+
+
+def _limits(nj, v, bound):
+    """kron(I, [-1, 1])' v + bound + 1e-2: [bound - v_0, bound + v_0, ...]."""
+    out = np.empty(2 * nj)
+    out[0::2], out[1::2] = -v, v
+    return out + bound + 1e-2
+
+
+def wb_stage_cost(swing_tracking, nj, nc, W, ref_row, x, u, terminal):
+    """objectives.py:77-144 (one stage; terminal = the t == N branch)."""
+    W = np.asarray(W, dtype=np.float64)
+    s = _wb_split(nj, nc, np.asarray(x, dtype=np.float64), np.asarray(u, dtype=np.float64))
+    r = _wb_ref(nj, nc, np.asarray(ref_row, dtype=np.float64))
+    quad = lambda e, a, b: e @ W[a:b, a:b] @ e
+    eq = quat_sub(s["quat"], r["quat"])
+    cost = quad(s["p"] - r["p"], 0, 3) + quad(eq, 3, 6) + quad(s["q"] - r["q"], 6, 6 + nj) + \
+        quad(s["dp"] - r["dp"], 6 + nj, 9 + nj) + quad(s["omega"] - r["omega"], 9 + nj, 12 + nj) + \
+        quad(s["dq"], 12 + nj, 12 + 2 * nj)
+    if terminal:
+        return 0.5 * cost
+    cmap = np.ones(3 * nc) if swing_tracking else np.repeat(r["contact"], 3)
+    a = 12 + 2 * nj
+    cost += quad(cmap * (s["p_leg"] - r["p_leg"]), a, a + 3 * nc)
+    a += 3 * nc
+    cost += quad(s["tau"], a, a + nj)
+    a += nj
+    cost += quad(s["grf"] - r["grf"], a, a + 3 * nc)
+    g = s["grf"]
+    cone = penalty(0.5 * g[2::3] - np.sqrt(np.square(g[1::3]) + np.square(g[0::3]) + 1e-2))
+    cost += np.sum(penalty(_limits(nj, s["tau"], 44.0), 1, 1)) + np.sum(cone * r["contact"]) + \
+        np.sum(penalty(_limits(nj, s["dq"], 10.0), 1, 1))
+    return 0.5 * cost
+
+
+def wb_hessian_gn(swing_tracking, nj, nc, W, ref_row, x, u):
+    """objectives.py:146-203: (H_xx, H_uu, H_xu) = J_x'W J_x + barrier terms,
+    J_u'W J_u + torque barrier, J_x'W J_u, with the residual's Jacobians
+    formed analytically."""
+    W = np.asarray(W, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    u = np.asarray(u, dtype=np.float64)
+    r = _wb_ref(nj, nc, np.asarray(ref_row, dtype=np.float64))
+    n, m, R = x.size, u.size, W.shape[0]
+    Jx, Ju = np.zeros((R, n)), np.zeros((R, m))
+    Jx[0:3, 0:3] = np.eye(3)
+    Jx[3:6, 3:7] = quat_sub_jacobian(x[3:7], r["quat"])
+    Jx[6:6 + nj, 7:7 + nj] = np.eye(nj)
+    Jx[6 + nj:12 + nj, 7 + nj:13 + nj] = np.eye(6)
+    Jx[12 + nj:12 + 2 * nj, 13 + nj:13 + 2 * nj] = np.eye(nj)
+    cmap = np.ones(3 * nc) if swing_tracking else np.repeat(r["contact"], 3)
+    a = 12 + 2 * nj
+    Jx[a:a + 3 * nc, 13 + 2 * nj:13 + 2 * nj + 3 * nc] = np.diag(cmap)
+    Ju[a + 3 * nc:a + 3 * nc + nj, :nj] = np.eye(nj)
+    b = a + 3 * nc + nj
+    Jx[b:b + 3 * nc, 13 + 2 * nj + 3 * nc:] = np.eye(3 * nc)
+    Hx, Hu, Hxu = Jx.T @ W @ Jx, Ju.T @ W @ Ju, Jx.T @ W @ Ju
+    # friction cone (with 1e-1 under the root here, objectives.py:184-188)
+    g0 = 13 + 2 * nj + 3 * nc
+    g = x[g0:]
+    sq = np.sqrt(np.square(g[1::3]) + np.square(g[0::3]) + 1e-1)
+    cone = 0.5 * g[2::3] - sq
+    Jf = np.zeros((nc, n))
+    for i in range(nc):
+        Jf[i, g0 + 3 * i] = -g[3 * i] / sq[i]
+        Jf[i, g0 + 3 * i + 1] = -g[3 * i + 1] / sq[i]
+        Jf[i, g0 + 3 * i + 2] = 0.5
+    Hx += Jf.T @ np.diag(np.clip(penalty_dd(cone), -1e6, 1e6) * r["contact"]) @ Jf
+    K = np.zeros((2 * nj, nj))
+    K[0::2, :], K[1::2, :] = -np.eye(nj), np.eye(nj)
+    Hu += K.T @ np.diag(np.clip(penalty_dd(_limits(nj, u[:nj], 44.0), 1, 1), -1e6, 1e6)) @ K
+    Js = np.zeros((2 * nj, n))
+    Js[:, 13 + nj:13 + 2 * nj] = K
+    Hx += Js.T @ np.diag(np.clip(penalty_dd(_limits(nj, x[13 + nj:13 + 2 * nj], 10.0)), -1e6, 1e6)) @ Js
+    return Hx, Hu, Hxu

@@ -14,11 +14,22 @@ stand-in for the parts of `jax`, `jax.numpy` and `mujoco.mjx` they use:
                    objectives.py:39-75);
   * mujoco.mjx math (quat_to_mat, quat_integrate, quat_sub, norm, normalize)
                 -> restated from their mathematical definition (third-party
-                   code, not present in the reference tree).
+                   code, not present in the reference tree);
+  * jax.scipy.linalg.cho_factor / cho_solve -> scipy's.
 
-Usage:  python tests/golden/make_golden.py /path/to/reference  [out.npz]
-Output: tests/golden/srbd_golden.npz (committed).  The tests never run this
-script; they only read the .npz.
+With --wb it runs the whole-body MPC model of config_aliengo.py instead:
+quadruped_wb_dynamics (models.py:39-117), quadruped_wb_obj and
+quadruped_wb_hessian_gn (objectives.py:77-203).  mjx.make_data,
+fwd_position, fwd_velocity and jac are then stood in for by the float64
+rigid-body oracle (oracle/wholebody.py) on the aliengo MJCF.  Those vectors
+therefore pin the model's own formulas (the contact-force solve, the masking,
+the integration, the cost and its Hessian) to the reference's source.  The
+rigid-body terms themselves are pinned separately
+(tests/test_oracle_wholebody.py).
+
+Usage:  python tests/golden/make_golden.py /path/to/reference [--wb] [out.npz]
+Output: tests/golden/srbd_golden.npz, or tests/golden/wb_golden.npz with --wb
+(committed).  The tests never run this script; they only read the .npz.
 """
 import functools
 import importlib.util
@@ -27,6 +38,7 @@ import sys
 import types
 
 import numpy as np
+import scipy.linalg as scipy_linalg
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DT = {"f": np.float32, "i": np.int32}
@@ -95,9 +107,15 @@ class JArr(np.ndarray):
         logical = ufunc in (np.logical_and, np.logical_or, np.logical_not, np.greater, np.less, np.equal,
                             np.not_equal, np.greater_equal, np.less_equal)
         args = _prep(inputs, float_op=not logical)
+        out = kwargs.pop("out", None)
         if ufunc is np.power and isinstance(args[1], (int, np.integer)) and not isinstance(args[1], bool):
-            return _wrap(_ipow(args[0], int(args[1])))
-        return _wrap(getattr(ufunc, method)(*args, **kwargs))
+            res = _ipow(args[0], int(args[1]))
+        else:
+            res = getattr(ufunc, method)(*args, **kwargs)
+        if out is not None:  # in-place operators (a += b): write through the plain view
+            np.asarray(out[0])[...] = res
+            return out[0]
+        return _wrap(res)
 
     def __matmul__(self, other):
         return _matmul(self, other)
@@ -265,14 +283,14 @@ def _fd_jacobian(f, argnums=0, h=1e-6):
 def _fd_grad(f, argnums=0, h=1e-3):
     """Derivative of a scalar function by the 4th-order five-point stencil
     (nested for grad(grad(.)), so its error must stay small)."""
-    def d(*args):
+    def d(*args, **kw):
         args = list(args)
         x = np.asarray(args[argnums], dtype=np.float64)
 
         def at(s):
             a = list(args)
             a[argnums] = _wrap(x + s)
-            return np.asarray(f(*a), dtype=np.float64)
+            return np.asarray(f(*a, **kw), dtype=np.float64)
         return _wrap((-at(2 * h) + 8 * at(h) - 8 * at(-h) + at(-2 * h)) / (12 * h))
     return d
 
@@ -340,6 +358,8 @@ def install_shim():
     jnp.stack = _stack
     jnp.pi = np.pi
     jnp.float32 = np.float32
+    jnp.kron = lambda a, b: _wrap(np.kron(*_prep([a, b])))
+    jnp.eye = lambda n, dtype=None: _wrap(np.eye(n, dtype=DT["f"]))
     linalg = types.ModuleType("jax.numpy.linalg")
     linalg.norm = _norm
     linalg.inv = lambda a: _wrap(np.linalg.inv(np.asarray(a)))
@@ -357,6 +377,9 @@ def install_shim():
     scipy = types.ModuleType("jax.scipy")
     sl = types.ModuleType("jax.scipy.linalg")
     sl.block_diag = _block_diag
+    sl.cho_factor = lambda a, lower=False: (_wrap(np.asarray(scipy_linalg.cho_factor(np.asarray(a), lower=lower)[0])),
+                                            lower)
+    sl.cho_solve = lambda cl, b: _wrap(scipy_linalg.cho_solve((np.asarray(cl[0]), cl[1]), np.asarray(b)))
     scipy.linalg = sl
     st = types.ModuleType("jax.scipy.spatial")
     stt = types.ModuleType("jax.scipy.spatial.transform")
@@ -507,9 +530,144 @@ def main(ref_root, out):
     print("wrote", out, {k: v.shape for k, v in g.items()})
 
 
+# ----------------------------------------------------------------- whole-body model
+class _FakeMjxData:
+    """The fields of an mjx Data that models.py:39-117 reads, computed by the
+    float64 rigid-body oracle (oracle/wholebody.py) for the parsed model."""
+
+    def __init__(self, model, qpos=None, qvel=None):
+        self.model, self.qpos, self.qvel = model, qpos, qvel
+
+    def replace(self, qpos=None, qvel=None):
+        return _FakeMjxData(self.model, self.qpos if qpos is None else qpos, self.qvel if qvel is None else qvel)
+
+
+def _install_fake_mjx():
+    """mjx.make_data / fwd_position / fwd_velocity / jac over the oracle:
+    qLD is the upper Cholesky factor U of qM (qM = U'U), which is what the
+    reference's cho_solve((qLD, False), .) needs; geom_xpos rows are the
+    contact points in the model's contact order."""
+    sys.path.insert(0, os.path.join(HERE, "..", ".."))
+    from oracle import wholebody as Wb
+    mjx = sys.modules["mujoco.mjx"]
+
+    def fwd_position(m, d):
+        t = Wb.terms(m, np.asarray(d.qpos, dtype=np.float64), np.zeros(m.nv))
+        d.qM = _wrap(t["M"])
+        d.qLD = _wrap(np.linalg.cholesky(t["M"]).T)
+        d.geom_xpos = _wrap(t["cpos"].reshape(-1, 3))
+        d.T = Wb.kinematics(m, np.asarray(d.qpos, dtype=np.float64))
+        return d
+
+    def fwd_velocity(m, d):
+        t = Wb.terms(m, np.asarray(d.qpos, dtype=np.float64), np.asarray(d.qvel, dtype=np.float64))
+        d.qfrc_bias = _wrap(t["bias"])
+        return d
+
+    def jac(m, d, point, body_id):
+        Jp, Jr = Wb.point_jacobian(m, d.T, int(body_id), np.asarray(point, dtype=np.float64))
+        return _wrap(Jp.T), _wrap(Jr.T)
+
+    mjx.make_data = lambda model: _FakeMjxData(model)
+    mjx.fwd_position = fwd_position
+    mjx.fwd_velocity = fwd_velocity
+    mjx.jac = jac
+
+
+def main_wb(ref_root, out):
+    """Golden vectors of the whole-body MPC model: quadruped_wb_dynamics
+    (models.py:39-117, float64, over the oracle's rigid-body terms for the
+    aliengo model), quadruped_wb_obj (objectives.py:77-144, float32) and
+    quadruped_wb_hessian_gn (objectives.py:146-203, float64 with
+    finite-difference autodiff), with config_aliengo's W."""
+    install_shim()
+    _install_fake_mjx()
+    sys.path.insert(0, os.path.join(HERE, "..", ".."))
+    from mpx_gb300 import mjcf
+    mo = load(ref_root, "mpx/utils/models.py", "ref_models")
+    ob = load(ref_root, "mpx/utils/objectives.py", "ref_objectives")
+    pkg, utils = types.ModuleType("mpx"), types.ModuleType("mpx.utils")
+    utils.models, utils.objectives, pkg.utils = mo, ob, utils
+    sys.modules.update({"mpx": pkg, "mpx.utils": utils, "mpx.utils.models": mo, "mpx.utils.objectives": ob})
+    cfg = load(ref_root, "mpx/config/config_aliengo.py", "ref_config_aliengo")
+    model = mjcf.parse(os.path.join(ref_root, "mpx", "data", "aliengo", "aliengo.xml"), list(cfg.contact_frame),
+                       list(cfg.body_name))
+    nj, nc = int(cfg.n_joints), int(cfg.n_contact)
+    rng = np.random.default_rng(77)
+    q0 = np.asarray(cfg.q0, dtype=np.float64) if hasattr(cfg, "q0") else np.tile([0.0, 0.8, -1.6], 4)
+    g = {"wb_dt": np.float64(cfg.dt), "wb_W": np.asarray(cfg.W, dtype=np.float64)}
+
+    def rand_state():
+        quat = rng.normal(0, 0.2, 4); quat[0] += 1; quat /= np.linalg.norm(quat)
+        qpos = np.concatenate([rng.normal(0, 0.05, 3) + [0, 0, 0.33], quat, q0 + rng.normal(0, 0.2, nj)])
+        qvel = rng.normal(0, 0.5, nj + 6)
+        return np.concatenate([qpos, qvel, rng.normal(0, 0.1, 3 * nc), rng.normal(0, 20, 3 * nc)])
+
+    # dynamics, float64
+    DT["f"] = np.float64
+    xs, us, cs, xn = [], [], [], []
+    for _ in range(12):
+        x = rand_state()
+        u = rng.normal(0, 10, nj)
+        c = rng.integers(0, 2, nc).astype(np.float64)
+        par = np.stack([np.concatenate([c, np.zeros(12)])] * 2)
+        x1 = mo.quadruped_wb_dynamics(model, model, list(range(nc)), [int(b) for b in model.contact_jac_body], nj,
+                                      float(cfg.dt), _wrap(x), _wrap(u), 0, _wrap(par))
+        xs.append(x); us.append(u); cs.append(c); xn.append(np.asarray(x1))
+    g["wbdyn_x"], g["wbdyn_u"], g["wbdyn_contact"], g["wbdyn_xnext"] = [np.stack(a) for a in (xs, us, cs, xn)]
+
+    def rand_ref():
+        quat = rng.normal(0, 0.2, 4); quat[0] += 1; quat /= np.linalg.norm(quat)
+        return np.concatenate([rng.normal(0, 0.05, 3) + [0, 0, 0.33], quat, q0 + rng.normal(0, 0.1, nj),
+                               rng.normal(0, 0.3, 6), rng.normal(0, 0.1, 3 * nc), rng.integers(0, 2, nc),
+                               rng.normal(0, 20, 3 * nc)])
+
+    # cost, float32 (the reference's dtype), both swing-tracking settings
+    DT["f"] = np.float32
+    W32 = np.asarray(cfg.W, dtype=np.float32)
+    cx, cu, cr, cv, ct, cst = [], [], [], [], [], []
+    for i in range(24):
+        x = rand_state().astype(np.float32)
+        x[13 + 2 * nj + 3 * nc + 2::3] = np.abs(x[13 + 2 * nj + 3 * nc + 2::3]) + 5.0   # vertical forces
+        u = rng.normal(0, 15, nj).astype(np.float32)
+        ref = rand_ref().astype(np.float32)
+        term, swing = (i % 4 == 3), bool(i % 2)
+        val = ob.quadruped_wb_obj(swing, nj, nc, 1, _wrap(W32), _wrap(np.stack([ref, ref])), _wrap(x), _wrap(u),
+                                  1 if term else 0)
+        cx.append(x); cu.append(u); cr.append(ref); cv.append(float(np.asarray(val))); ct.append(term)
+        cst.append(swing)
+    g["wbcost_x"], g["wbcost_u"], g["wbcost_ref"] = [np.stack(a) for a in (cx, cu, cr)]
+    g["wbcost_val"] = np.array(cv, dtype=np.float32)
+    g["wbcost_terminal"] = np.array(ct, dtype=np.int32)
+    g["wbcost_swing"] = np.array(cst, dtype=np.int32)
+
+    # Gauss-Newton Hessian, float64
+    DT["f"] = np.float64
+    hx, hu, hr, hs, hQ, hR, hM = [], [], [], [], [], [], []
+    for i in range(8):
+        x = rand_state()
+        x[13 + 2 * nj + 3 * nc + 2::3] = np.abs(x[13 + 2 * nj + 3 * nc + 2::3]) * 0.1 + 0.5  # cone near its edge
+        x[13 + nj:13 + 2 * nj] = rng.uniform(-9.0, 9.0, nj)                                   # speeds near limits
+        u = rng.uniform(-43.0, 43.0, nj)
+        ref = rand_ref()
+        swing = bool(i % 2)
+        Q, Rm, M = ob.quadruped_wb_hessian_gn(swing, nj, nc, _wrap(np.asarray(cfg.W, dtype=np.float64)),
+                                              _wrap(np.stack([ref, ref])), _wrap(x), _wrap(u), 0)
+        hx.append(x); hu.append(u); hr.append(ref); hs.append(swing)
+        hQ.append(np.asarray(Q)); hR.append(np.asarray(Rm)); hM.append(np.asarray(M))
+    DT["f"] = np.float32
+    g["wbhess_x"], g["wbhess_u"], g["wbhess_ref"] = [np.stack(a) for a in (hx, hu, hr)]
+    g["wbhess_swing"] = np.array(hs, dtype=np.int32)
+    g["wbhess_Q"], g["wbhess_R"], g["wbhess_M"] = [np.stack(a) for a in (hQ, hR, hM)]
+    np.savez_compressed(out, **g)
+    print("wrote", out)
+
+
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPX_REFERENCE", "")
-    out = sys.argv[2] if len(sys.argv) > 2 else os.path.join(HERE, "srbd_golden.npz")
+    wb = "--wb" in sys.argv
+    argv = [a for a in sys.argv[1:] if a != "--wb"]
+    ref_root = argv[0] if argv else os.environ.get("MPX_REFERENCE", "")
+    out = argv[1] if len(argv) > 1 else os.path.join(HERE, "wb_golden.npz" if wb else "srbd_golden.npz")
     if not ref_root or not os.path.isdir(os.path.join(ref_root, "mpx")):
-        sys.exit("usage: make_golden.py <reference checkout containing mpx/> [out.npz]")
-    main(ref_root, out)
+        sys.exit("usage: make_golden.py <reference checkout containing mpx/> [--wb] [out.npz]")
+    (main_wb if wb else main)(ref_root, out)

@@ -213,3 +213,71 @@ def test_reader_default_classes_inherit():
     m = mjcf.parse(xml)
     assert np.allclose(m.armature[6:], [0.2, 0.2])           # b inherits a's armature
     assert np.allclose(m.jnt_axis[1], [0, 1, 0]) and np.allclose(m.jnt_axis[2], [1, 0, 0])
+
+
+# ----------------------------------------------------------------- the whole-body MPC model
+WBG = np.load(os.path.join(os.path.dirname(__file__), "golden", "wb_golden.npz"))
+
+
+def test_wb_dynamics_matches_the_reference_code(model):
+    """quadruped_wb_dynamics (models.py:39-117) executed from the reference's
+    source over the oracle's rigid-body terms (tests/golden/make_golden.py
+    --wb): the contact-force solve, masking and integration agree."""
+    dt = float(WBG["wb_dt"])
+    for x, u, c, xn in zip(WBG["wbdyn_x"], WBG["wbdyn_u"], WBG["wbdyn_contact"], WBG["wbdyn_xnext"]):
+        assert np.abs(W.wb_dynamics(model, dt, x, u, c) - xn).max() < 1e-9 * (1 + np.abs(xn).max())
+
+
+def test_wb_dynamics_identities(model):
+    """All feet in contact: 2 alpha dt = 1 (alpha = 25, dt = 0.02), so the
+    Baumgarte term brings the feet to rest, J'v+ = 0.  No contact: a free
+    semi-implicit Euler step, v+ = v + M^-1 (tau - bias) dt."""
+    dt = float(WBG["wb_dt"])
+    rng = np.random.default_rng(80)
+    for _ in range(3):
+        qpos, qvel = random_state(model, rng)
+        x = np.concatenate([qpos, qvel, np.zeros(24)])
+        u = rng.normal(0, 10, 12)
+        x1 = W.wb_dynamics(model, dt, x, u, np.ones(4))
+        J1 = W.terms(model, qpos, qvel)["J"]
+        assert np.abs(J1.T @ x1[19:37]).max() < 1e-9 * (1 + np.abs(qvel).max())
+        x0 = W.wb_dynamics(model, dt, x, u, np.zeros(4))
+        t = W.terms(model, qpos, qvel)
+        v = qvel + np.linalg.solve(t["M"], np.concatenate([np.zeros(6), u]) - t["bias"]) * dt
+        assert np.allclose(x0[19:37], v, rtol=1e-12, atol=1e-12)
+        assert np.allclose(x0[49:], 0.0)
+        assert np.allclose(x0[37:49], t["cpos"])
+        assert np.allclose(x0[7:19], qpos[7:] + v[6:] * dt)
+        assert abs(np.linalg.norm(x0[3:7]) - 1) < 1e-12
+
+
+def test_wb_cost_matches_the_reference_code():
+    """quadruped_wb_obj (objectives.py:77-144), float32 in the reference,
+    with config_aliengo's W, stage and terminal, both swing-tracking modes."""
+    Wm = WBG["wb_W"].astype(np.float32)
+    for x, u, r, v, t, s in zip(WBG["wbcost_x"], WBG["wbcost_u"], WBG["wbcost_ref"], WBG["wbcost_val"],
+                                WBG["wbcost_terminal"], WBG["wbcost_swing"]):
+        o = W.wb_stage_cost(bool(s), 12, 4, Wm, r, x, u, bool(t))
+        assert abs(o - v) <= 1e-6 * max(1.0, abs(v))
+
+
+def test_wb_hessian_matches_the_reference_code():
+    """quadruped_wb_hessian_gn (objectives.py:146-203), float64 with
+    finite-difference autodiff in the generator: the analytic restatement
+    agrees to the differences' accuracy."""
+    for x, u, r, s, Q, R, M in zip(WBG["wbhess_x"], WBG["wbhess_u"], WBG["wbhess_ref"], WBG["wbhess_swing"],
+                                   WBG["wbhess_Q"], WBG["wbhess_R"], WBG["wbhess_M"]):
+        Hx, Hu, Hxu = W.wb_hessian_gn(bool(s), 12, 4, WBG["wb_W"], r, x, u)
+        assert np.abs(Hx - Q).max() <= 1e-7 * np.abs(Q).max()
+        assert np.abs(Hu - R).max() <= 1e-6 * np.abs(R).max()
+        assert np.abs(Hxu - M).max() <= 1e-9
+
+
+def test_quat_sub_jacobian():
+    rng = np.random.default_rng(90)
+    for _ in range(10):
+        u, v = rng.normal(size=4), rng.normal(size=4)
+        u, v = u / np.linalg.norm(u), v / np.linalg.norm(v)
+        h = 1e-7
+        fd = np.column_stack([(W.quat_sub(u + h * e, v) - W.quat_sub(u - h * e, v)) / (2 * h) for e in np.eye(4)])
+        assert np.abs(W.quat_sub_jacobian(u, v) - fd).max() < 1e-6
