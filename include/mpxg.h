@@ -464,6 +464,22 @@ mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batc
                               const float* foot_ref_dot, const int* contact, const float* Kp, const float* Kd,
                               float* tau, float* J);
 
+/* One step of the whole-body MPC model of the reference's whole-body
+ * configurations (quadruped_wb_dynamics, mpx/utils/models.py:39-117; bound at
+ * config_aliengo.py:68, config_go2.py:69) for a batch:
+ *   x [B, nq + nv + 6C] = [qpos, qvel, contact points, contact forces],
+ *   u [B, nv - 6] joint torques, contact [B, C] (int, the reference's
+ *   parameter[t, :C]) ->
+ *   x_next [B, nq + nv + 6C] = [qpos+, qvel+, contact points at x, forces],
+ * with forces f from (J'M^-1 J) f = -J'M^-1 (tau - bias) - 2 alpha J'qdot
+ * (alpha = 25 in the reference), masked by contact, then
+ * qvel+ = qvel + M^-1 (tau - bias + J f) dt and a semi-implicit Euler step of
+ * qpos (the free joint's quaternion by its body-frame rate).  Requires a free
+ * root, hinge or slide joints elsewhere, 3C <= nv and nv + 3C + 1 <= 32.  The
+ * contact-point and force entries of x are not read. */
+mpxg_status mpxg_wb_step(void* stream, const mpxg_wb_model* model, int batch, float dt, float alpha, const float* x,
+                         const float* u, const int* contact, float* x_next);
+
 /* Last error message of a handle (or of the library when h is NULL). */
 const char* mpxg_last_error(const mpxg_handle* h);
 const char* mpxg_status_string(int status);

@@ -122,7 +122,7 @@ EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
-           "mpxg_wb_terms", "mpxg_wb_interface"]
+           "mpxg_wb_terms", "mpxg_wb_interface", "mpxg_wb_step"]
 
 _lib = None
 
@@ -181,6 +181,8 @@ def load(build_if_missing=True):
     L.mpxg_wb_terms.restype = ctypes.c_int
     L.mpxg_wb_interface.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 10
     L.mpxg_wb_interface.restype = ctypes.c_int
+    L.mpxg_wb_step.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int, ctypes.c_float, ctypes.c_float] + [vp] * 4
+    L.mpxg_wb_step.restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_xla_solve_vjp.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]

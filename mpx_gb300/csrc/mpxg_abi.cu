@@ -519,13 +519,13 @@ static const char* wb_check(const mpxg_wb_model* m) {
 
 // The smallest capacity the (checked) model fits.
 extern "C++" {
-template <bool IFACE>
+template <int MODE>
 static cudaError_t wb_launch(const mpxg_wb_model& m, int batch, const mpxg::wb::Args& a, cudaStream_t st) {
   using namespace mpxg::wb;
   if (m.nbody <= CapQuad::MB && m.nv <= CapQuad::MD && m.nq <= CapQuad::MD + 4 && 3 * m.n_contact <= CapQuad::MR)
-    wb_kernel<IFACE, CapQuad><<<(batch + CapQuad::NW - 1) / CapQuad::NW, 32 * CapQuad::NW, 0, st>>>(m, batch, a);
+    wb_kernel<MODE, CapQuad><<<(batch + CapQuad::NW - 1) / CapQuad::NW, 32 * CapQuad::NW, 0, st>>>(m, batch, a);
   else
-    wb_kernel<IFACE, CapAny><<<(batch + CapAny::NW - 1) / CapAny::NW, 32 * CapAny::NW, 0, st>>>(m, batch, a);
+    wb_kernel<MODE, CapAny><<<(batch + CapAny::NW - 1) / CapAny::NW, 32 * CapAny::NW, 0, st>>>(m, batch, a);
   return cudaGetLastError();
 }
 }
@@ -539,7 +539,8 @@ mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, c
   if (batch == 0) return MPXG_OK;
   Args a{};
   a.qpos = qpos; a.qvel = qvel; a.M = M; a.bias = bias; a.cpos = cpos; a.J = J; a.cvel = cvel;
-  cudaError_t e = wb_launch<false>(*model, batch, a, (cudaStream_t)stream);
+  a.sq = model->nq; a.sv = model->nv;
+  cudaError_t e = wb_launch<MODE_TERMS>(*model, batch, a, (cudaStream_t)stream);
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
 }
 
@@ -559,7 +560,28 @@ mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batc
   Args a{};
   a.qpos = qpos; a.qvel = qvel; a.grf = grf; a.foot_ref = foot_ref; a.foot_ref_dot = foot_ref_dot;
   a.contact = contact; a.Kp = Kp; a.Kd = Kd; a.tau = tau; a.J = J;
-  cudaError_t e = wb_launch<true>(*model, batch, a, (cudaStream_t)stream);
+  a.sq = model->nq; a.sv = model->nv;
+  cudaError_t e = wb_launch<MODE_INTERFACE>(*model, batch, a, (cudaStream_t)stream);
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
+}
+
+mpxg_status mpxg_wb_step(void* stream, const mpxg_wb_model* model, int batch, float dt, float alpha, const float* x,
+                         const float* u, const int* contact, float* x_next) {
+  using namespace mpxg::wb;
+  if (const char* why = wb_check(model)) return fail(nullptr, MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_step: ") + why);
+  const int nv = model->nv, nr = 3 * model->n_contact;
+  if (model->jnt_type[0] != 1 || model->nq != nv + 1 || model->n_contact < 1 || nr > nv || nv + nr + 1 > 32)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG,
+                "mpxg_wb_step: needs a free root, hinge or slide joints elsewhere, 3 x contacts <= nv and "
+                "nv + 3 x contacts + 1 <= 32");
+  if (batch < 0 || (batch > 0 && (!x || !u || !contact || !x_next)) || !(dt > 0.0f))
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_wb_step: bad batch, dt or null pointer");
+  if (batch == 0) return MPXG_OK;
+  Args a{};
+  const int nx = model->nq + nv + 2 * nr;
+  a.qpos = x; a.qvel = x + model->nq; a.sq = nx; a.sv = nx;
+  a.u = u; a.contact = contact; a.x_next = x_next; a.dt = dt; a.alpha = alpha;
+  cudaError_t e = wb_launch<MODE_STEP>(*model, batch, a, (cudaStream_t)stream);
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
 }
 

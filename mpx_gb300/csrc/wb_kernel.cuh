@@ -39,10 +39,14 @@ using CapAny = Cap<MPXG_WB_MAX_BODY, MPXG_WB_MAX_DOF, MPXG_WB_MAX_CONTACT, 2, 1>
 using CapQuad = Cap<16, 20, 4, 3, 9>;
 
 struct Args {
-  const float *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd;
+  const float *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd, *u;
   const int* contact;
-  float *M, *bias, *cpos, *J, *cvel, *tau;
+  float *M, *bias, *cpos, *J, *cvel, *tau, *x_next;
+  int sq, sv;        // row strides of qpos and qvel (floats)
+  float dt, alpha;   // the dynamics step
 };
+
+enum { MODE_TERMS = 0, MODE_INTERFACE = 1, MODE_STEP = 2 };
 
 template <class C>
 struct Warp {
@@ -130,11 +134,132 @@ __device__ __forceinline__ float dot6(const float* a, const float* b) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
 }
 
+// Gauss-Jordan elimination of the first n pivots of a column-distributed
+// matrix: lane c holds column c in col[0..N).  Without pivoting (the matrices
+// here are symmetric positive definite); afterwards the columns right of the
+// pivots hold the solutions.
+template <int N>
+__device__ __forceinline__ void gj_lanes(float (&col)[N], int n) {
+  const unsigned full = 0xffffffffu;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    if (k < n) {
+      const float dk = __shfl_sync(full, col[k], k);
+      const float yk = col[k] / dk;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        if (i < n && i != k) {
+          const float gik = __shfl_sync(full, col[i], k);
+          col[i] -= gik * yk;
+        }
+      }
+      col[k] = yk;
+    }
+  }
+}
+
+// One step of the whole-body model (mpx/utils/models.py:39-117) from the
+// terms already in shared memory (M, bias, J, contact points at x):
+//   Y = M^-1 J, z = M^-1 (tau - bias), tau = [0 (6), u],
+//   (J'Y) f = -J'z - 2 alpha J'qdot,   f masked by contact,
+//   v+ = qdot + (z + Y f) dt,  p+ = p + v+ dt,  quat+ = quat * exp(w+ dt / 2),
+//   q+ = q + dq+ dt;  x+ = [p+, quat+, q+, v+, contact points at x, f].
+// Requires a free root, nq = nv + 1 and nv + 3 C + 1 <= 32 (host checks).
+template <class C>
+__device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C>& s, const Args& a, size_t e, int lane) {
+  constexpr int MD = C::MD, MR = C::MR;
+  const int nv = m.nv, nq = m.nq, nc = m.n_contact, nr = 3 * nc;
+  // [M | J | tau - bias], lane c holding column c
+  float col[MD];
+#pragma unroll
+  for (int i = 0; i < MD; ++i) {
+    float g = 0.0f;
+    if (i < nv) {
+      if (lane < nv)
+        g = s.M[i][lane];
+      else if (lane < nv + nr)
+        g = s.J[i][lane - nv];
+      else if (lane == nv + nr)
+        g = (i >= 6 ? a.u[e * (nv - 6) + (i - 6)] : 0.0f) - s.bias[i];
+    }
+    col[i] = g;
+  }
+  gj_lanes<MD>(col, nv);
+  __syncwarp();
+  // Y over the mass matrix's storage, z in w
+  if (lane >= nv && lane < nv + nr) {
+#pragma unroll
+    for (int i = 0; i < MD; ++i)
+      if (i < nv) s.M[i][lane - nv] = col[i];
+  } else if (lane == nv + nr) {
+#pragma unroll
+    for (int i = 0; i < MD; ++i)
+      if (i < nv) s.w[i] = col[i];
+  }
+  __syncwarp();
+  // [J'Y | -J'z - 2 alpha J'qdot] over the contact rows
+  float c2[MR];
+#pragma unroll
+  for (int r = 0; r < MR; ++r) {
+    float g = 0.0f;
+    if (r < nr) {
+      if (lane < nr) {
+        for (int i = 0; i < nv; ++i) g += s.J[i][r] * s.M[i][lane];
+      } else if (lane == nr) {
+        float jz = 0.0f, jv = 0.0f;
+        for (int i = 0; i < nv; ++i) {
+          jz += s.J[i][r] * s.w[i];
+          jv += s.J[i][r] * s.qvel[i];
+        }
+        g = -jz - 2.0f * a.alpha * jv;
+      }
+    }
+    c2[r] = g;
+  }
+  gj_lanes<MR>(c2, nr);
+  if (lane == nr) {
+#pragma unroll
+    for (int r = 0; r < MR; ++r)
+      if (r < nr) s.y[r] = c2[r] * (float)a.contact[e * nc + r / 3];
+  }
+  __syncwarp();
+  // v+ (in the bias storage, no longer needed)
+  if (lane < nv) {
+    float acc = s.w[lane];
+    for (int r = 0; r < nr; ++r) acc += s.M[lane][r] * s.y[r];
+    s.bias[lane] = s.qvel[lane] + acc * a.dt;
+  }
+  __syncwarp();
+  const int nx = nq + nv + 2 * nr;
+  float* xo = a.x_next + e * nx;
+  const float dt = a.dt;
+  if (lane < 3) xo[lane] = s.qpos[lane] + s.bias[lane] * dt;
+  if (lane == 3) {  // quat * exp(w dt / 2), w in the body frame, renormalised
+    const float w0 = s.bias[3], w1 = s.bias[4], w2 = s.bias[5];
+    const float n = sqrtf(w0 * w0 + w1 * w1 + w2 * w2);
+    const float inv = n > 0.0f ? 1.0f / n : 0.0f;
+    float sh, ch;
+    sincosf(0.5f * n * dt, &sh, &ch);
+    const float qr[4] = {ch, w0 * inv * sh, w1 * inv * sh, w2 * inv * sh};
+    float qn[4];
+    quat_mul(s.qpos + 3, qr, qn);
+    quat_normalize(qn);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) xo[3 + i] = qn[i];
+  }
+  for (int j = lane; j < nq - 7; j += 32) xo[7 + j] = s.qpos[7 + j] + s.bias[6 + j] * dt;
+  if (lane < nv) xo[nq + lane] = s.bias[lane];
+  if (lane < nr) {
+    xo[nq + nv + lane] = s.cpos[lane];
+    xo[nq + nv + nr + lane] = s.y[lane];
+  }
+}
+
 // The model must have passed the host checks of mpxg_wb_terms (parents
 // precede children, one joint per body, the free joint only on body 0, dof and
 // qpos addresses dense in body order, contacts on existing bodies) and fit the
 // capacity C: nbody <= MB, nv <= MD, nq <= MD + 4, 3 x contacts <= MR.
-template <bool IFACE, class C>
+template <int MODE, class C>
 __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch,
                                                                  Args a) {
   constexpr int MB = C::MB, MR = C::MR;
@@ -145,8 +270,8 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   Warp<C>& s = sw[wid];
   const unsigned full = 0xffffffffu;
   const int nb = m.nbody, nq = m.nq, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
-  for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * nq + i];
-  if (lane < nv) s.qvel[lane] = a.qvel[(size_t)env * nv + lane];
+  for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * a.sq + i];
+  if (lane < nv) s.qvel[lane] = a.qvel[(size_t)env * a.sv + lane];
   // the tree's indices in shared memory: the chain walks below read them at
   // lane-dependent positions
   if (lane < nb) {
@@ -392,7 +517,7 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
     s.cvel[lane] = v;
   }
   __syncwarp();
-  if (!IFACE) {
+  if constexpr (MODE == MODE_TERMS) {
     const size_t e = (size_t)env;
     if (a.M)
       for (int i = lane; i < nv * nv; i += 32) a.M[e * nv * nv + i] = s.M[i / nv][i % nv];
@@ -403,8 +528,12 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
       for (int i = lane; i < nv * nr; i += 32) a.J[e * nv * nr + i] = s.J[i / nr][i % nr];
     return;
   }
-  // ---- the interface (mpc_utils.py:300-311)
   const size_t e = (size_t)env;
+  if constexpr (MODE == MODE_STEP) {
+    step(m, s, a, e, lane);
+    return;
+  }
+  // ---- the interface (mpc_utils.py:300-311)
   if (lane < nr) {
     float v = 0.0f;
     for (int q = 0; q < nr; ++q)
@@ -427,21 +556,7 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
     }
     col[i] = g;
   }
-#pragma unroll
-  for (int k = 0; k < MR; ++k) {
-    if (k < nr) {
-      const float dk = __shfl_sync(full, col[k], k);
-      const float yk = col[k] / dk;
-#pragma unroll
-      for (int i = 0; i < MR; ++i) {
-        if (i < nr && i != k) {
-          const float gik = __shfl_sync(full, col[i], k);
-          col[i] -= gik * yk;
-        }
-      }
-      col[k] = yk;
-    }
-  }
+  gj_lanes<MR>(col, nr);
   if (lane == nr) {
 #pragma unroll
     for (int i = 0; i < MR; ++i)

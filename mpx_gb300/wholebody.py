@@ -70,3 +70,19 @@ class WholeBodyModel:
                                             _ptr(contact), _ptr(Kp), _ptr(Kd), _ptr(tau), _ptr(J)), None,
                    "mpxg_wb_interface")
         return tau, J
+
+    def step(self, x, u, contact, dt, alpha=25.0, stream=None):
+        """One step of the whole-body MPC model (mpx/utils/models.py:39-117)
+        for every row: x [B, nq + nv + 6C], u [B, nv - 6], contact [B, C] ->
+        x_next [B, nq + nv + 6C]."""
+        nr = 3 * self.nc
+        nx = self.nq + self.nv + 2 * nr
+        x = _dev(x, self.dev).reshape(-1, nx)
+        B = x.shape[0]
+        u = _dev(u, self.dev).reshape(B, self.nv - 6)
+        contact = _dev(contact, self.dev, torch.int32).reshape(B, self.nc)
+        out = torch.empty(B, nx, device=self.dev)
+        _lib.check(self.L.mpxg_wb_step(_stream_handle(stream), _lib.ctypes.byref(self.struct), B, float(dt),
+                                       float(alpha), _ptr(x), _ptr(u), _ptr(contact), _ptr(out)), None,
+                   "mpxg_wb_step")
+        return out

@@ -134,3 +134,21 @@ def test_wb_calls_reject_malformed_models():
     assert L.mpxg_wb_interface(None, ctypes.byref(S), 4, *([fake] * 8), None, fake) == 1  # tau NULL
     assert b"null pointer" in L.mpxg_last_error(None)
     assert L.mpxg_wb_terms(None, ctypes.byref(S), 0, None, None, None, None, None, None, None) == 0
+
+
+def test_wb_step_rejects_what_it_cannot_hold():
+    """mpxg_wb_step needs nv + 3 x contacts + 1 <= 32 (one lane per column of
+    [M | J | tau - bias]) and a positive dt; it checks before any launch."""
+    from mpx_gb300 import _lib, mjcf
+    L = _lib.load()
+    model = mjcf.load_npz(os.path.join(ROOT, "tests", "golden", "aliengo_wb.npz"))
+    fake = ctypes.c_void_p(1 << 20)  # never dereferenced: the checks fail first
+    S = model.to_struct()
+    assert L.mpxg_wb_step(None, ctypes.byref(S), 4, 0.0, 25.0, fake, fake, fake, fake) == 1
+    assert b"dt" in L.mpxg_last_error(None)
+    S.n_contact = 5                      # 18 + 15 + 1 > 32
+    S.contact_point_body[4] = S.contact_jac_body[4] = 3
+    assert L.mpxg_wb_step(None, ctypes.byref(S), 4, 0.02, 25.0, fake, fake, fake, fake) == 1
+    assert b"<= 32" in L.mpxg_last_error(None)
+    S = model.to_struct()
+    assert L.mpxg_wb_step(None, ctypes.byref(S), 0, 0.02, 25.0, None, None, None, None) == 0

@@ -198,3 +198,46 @@ def test_general_capacity_model_matches_oracle(cuda):
         # cond(J'J) reaches 5.5e3 on these states: float32 evaluation of the
         # interface formula alone moves tau by up to 5e-5 relative
         assert close(tau[b], rt, 5e-4), b
+
+
+def step_states(B, seed):
+    rng = np.random.default_rng(seed)
+    q0 = np.load(FIX)["q0"]
+    quat = rng.normal(0, 0.2, (B, 4))
+    quat[:, 0] += 1
+    quat /= np.linalg.norm(quat, axis=1, keepdims=True)
+    qpos = np.concatenate([rng.normal(0, 0.05, (B, 3)) + [0, 0, 0.33], quat, q0 + rng.normal(0, 0.2, (B, 12))], 1)
+    x = np.concatenate([qpos, rng.normal(0, 0.5, (B, 18)), np.zeros((B, 24))], 1).astype(np.float32)
+    return x, rng.normal(0, 10, (B, 12)).astype(np.float32), rng
+
+
+def test_step_matches_oracle(cuda):
+    """mpxg_wb_step against the oracle's quadruped_wb_dynamics (which is
+    pinned to the reference's source, tests/test_oracle_wholebody.py).
+    float32 evaluation alone moves v+ and the forces by up to 9e-7 relative."""
+    model = mjcf.load_npz(FIX)
+    wb = WholeBodyModel(model, device=cuda)
+    B = 67
+    x, u, rng = step_states(B, 21)
+    contact = rng.integers(0, 2, (B, 4)).astype(np.int32)
+    xn = wb.step(x, u, contact, 0.02).cpu().numpy()
+    for b in range(B):
+        ref = W.wb_dynamics(model, 0.02, x[b], u[b], contact[b])
+        assert close(xn[b, :19], ref[:19], 2e-6), b          # qpos+
+        assert close(xn[b, 19:37], ref[19:37], 2e-5), b      # qvel+
+        assert close(xn[b, 37:49], ref[37:49], 2e-6), b      # contact points
+        assert close(xn[b, 49:], ref[49:], 2e-5), b          # forces
+
+
+def test_step_with_every_foot_in_contact_stops_the_feet(cuda):
+    """2 alpha dt = 1 for the reference's alpha = 25, dt = 0.02: the feet's
+    velocities after the step, J(x)' v+, vanish."""
+    model = mjcf.load_npz(FIX)
+    wb = WholeBodyModel(model, device=cuda)
+    B = 32
+    x, u, _ = step_states(B, 22)
+    xn = wb.step(x, u, np.ones((B, 4), dtype=np.int32), 0.02)
+    J = wb.terms(x[:, :19], x[:, 19:37])["J"]
+    jv0 = (J.transpose(1, 2) @ torch.as_tensor(x[:, 19:37], device=cuda).unsqueeze(-1)).abs().amax(dim=(1, 2))
+    jv1 = (J.transpose(1, 2) @ xn[:, 19:37].unsqueeze(-1)).abs().amax(dim=(1, 2))
+    assert bool((jv1 <= 1e-4 * (1 + jv0)).all())
