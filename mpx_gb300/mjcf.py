@@ -15,13 +15,17 @@ interface):
     resolved through the `<default>` classes (`class`, `childclass`);
   * `<option gravity>`;
   * the named geoms used as contact points (their `pos`, or the middle of
-    `fromto`).
+    `fromto`);
+  * `<include file=...>` (the included file's top-level children take the
+    element's place, paths relative to the including file), and repeated
+    `<worldbody>` / `<default>` sections, read in order.
 
 Everything else (meshes, visuals, actuators, sensors, limits, damping and
 friction loss, which do not enter M or qfrc_bias) is ignored.  Bodies without
 an `<inertial>` element would need MuJoCo's inertia-from-geom compilation and
 are rejected unless they carry no geoms of their own.
 """
+import os
 import xml.etree.ElementTree as ET
 from dataclasses import dataclass, field
 
@@ -165,15 +169,37 @@ def quat_to_mat(q):
                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
 
 
+def _expand_includes(el, base_dir, depth=0):
+    """Replace every <include file=...> below el by the children of the
+    included file's root element (recursively)."""
+    if depth > 16:
+        raise ValueError("MJCF includes nest deeper than 16 levels")
+    i = 0
+    while i < len(el):
+        child = el[i]
+        if child.tag == "include":
+            if base_dir is None:
+                raise ValueError("<include> needs the model to be read from a file")
+            path = os.path.join(base_dir, child.get("file"))
+            inc = ET.parse(path).getroot()
+            _expand_includes(inc, os.path.dirname(path), depth + 1)
+            el.remove(child)
+            for k, c in enumerate(list(inc)):
+                el.insert(i + k, c)
+            i += len(inc)
+        else:
+            _expand_includes(child, base_dir, depth)
+            i += 1
+
+
 class _Defaults:
     """MJCF default classes: class name -> tag -> {attribute: value}, each
     class inheriting its parent class's values."""
 
     def __init__(self, root):
         self.cls = {"main": {}}
-        top = root.find("default")
-        if top is not None:
-            self._walk(top, "main", {})
+        for top in root.findall("default"):
+            self._walk(top, "main", self.cls["main"])
 
     def _walk(self, el, name, inherited):
         own = {tag: dict(attrs) for tag, attrs in inherited.items()}
@@ -224,13 +250,19 @@ def _orientation(el, compiler):
 def parse(source, contact_geoms=None, contact_bodies=None):
     """Read an MJCF file path (or XML text starting with '<') into a
     RigidBodyModel; contact_geoms / contact_bodies as in with_contacts()."""
-    root = ET.fromstring(source) if source.lstrip().startswith("<") else ET.parse(source).getroot()
+    if source.lstrip().startswith("<"):
+        root, base_dir = ET.fromstring(source), None
+    else:
+        root, base_dir = ET.parse(source).getroot(), os.path.dirname(os.path.abspath(source))
+    _expand_includes(root, base_dir)
     compiler = {}
     for c in root.findall("compiler"):
         compiler.update(c.attrib)
     defaults = _Defaults(root)
-    opt = root.find("option")
-    gravity = _vec(opt.get("gravity"), 3) if opt is not None and "gravity" in opt.attrib else np.array([0, 0, -9.81])
+    gravity = np.array([0, 0, -9.81])
+    for opt in root.findall("option"):
+        if "gravity" in opt.attrib:
+            gravity = _vec(opt.get("gravity"), 3)
     names, parent, bpos, bquat = [], [], [], []
     jt, jpos, jaxis, jnames, armature = [], [], [], [], []
     mass, com, inertia = [], [], []
@@ -326,11 +358,12 @@ def parse(source, contact_geoms=None, contact_bodies=None):
         for child in el.findall("body"):
             visit(child, b, cls)
 
-    world = root.find("worldbody")
-    if world is None:
+    worlds = root.findall("worldbody")
+    if not worlds:
         raise ValueError("no <worldbody>")
-    for child in world.findall("body"):
-        visit(child, -1, "main")
+    for world in worlds:
+        for child in world.findall("body"):
+            visit(child, -1, "main")
     model = RigidBodyModel(
         body_names=names, parent=np.asarray(parent, dtype=np.int64), body_pos=np.asarray(bpos),
         body_quat=np.asarray(bquat), jnt_type=np.asarray(jt, dtype=np.int64), jnt_pos=np.asarray(jpos),

@@ -281,3 +281,18 @@ def test_quat_sub_jacobian():
         h = 1e-7
         fd = np.column_stack([(W.quat_sub(u + h * e, v) - W.quat_sub(u - h * e, v)) / (2 * h) for e in np.eye(4)])
         assert np.abs(W.quat_sub_jacobian(u, v) - fd).max() < 1e-6
+
+
+def test_reader_follows_includes_and_repeated_sections():
+    """<include> splices the included file's sections in place; a second
+    <worldbody> adds its bodies after the first (here a welded box)."""
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    arm = mjcf.parse(os.path.join(here, "slider_arm.xml"), ["tip"], ["slider"])
+    scene = mjcf.parse(os.path.join(here, "slider_scene.xml"), ["tip"], ["slider"])
+    assert scene.body_names == arm.body_names + ["box"]
+    assert scene.jnt_type[-1] == mjcf.JNT_NONE and scene.parent[-1] == -1
+    for k in ("body_pos", "body_quat", "mass", "com", "inertia", "armature", "gravity", "contact_point_pos"):
+        a, b = getattr(arm, k), getattr(scene, k)
+        assert np.array_equal(a, b[:len(a)] if k in ("body_pos", "body_quat", "mass", "com", "inertia") else b), k
+    with pytest.raises(ValueError):
+        mjcf.parse(open(os.path.join(here, "slider_scene.xml")).read())   # text has no directory for the include
