@@ -310,27 +310,38 @@ def quat_sub_jacobian(u, v):
     return np.column_stack([d_ds, d_dw]) @ L
 
 
-def wb_dynamics(model, dt, x, u, contact, alpha=25.0):
-    """models.py:39-117: contact forces that hold the feet (Baumgarte-
-    stabilised at the velocity level, -2 alpha J'v), masked by contact, then a
-    semi-implicit Euler step; the new state carries the feet at the current
-    configuration and the forces."""
+def wb_dynamics(model, dt, x, u, contact, alpha=25.0, eps=0.0, forces_in_u=False):
+    """One step of the reference's whole-body models, with
+    nj = nv - 6 joints and C contact points:
+      quadruped_wb_dynamics (models.py:39-117): alpha = 25, eps = 0;
+      h1_wb_dynamics (models.py:119-168): alpha = 5, eps = 1e-3;
+      talos_wb_dynamics (models.py:170-216): forces_in_u (the forces are the
+        controls u[nj:]; no force solve; the next state carries no forces).
+    Otherwise the contact forces hold the feet, stabilised at the velocity
+    level (Baumgarte, -2 alpha J'v), from (J'M^-1 J + eps I) f = rhs, masked
+    by contact; then a semi-implicit Euler step.  The new state carries the
+    contact points at the current configuration (and the forces)."""
     x = np.asarray(x, dtype=np.float64)
+    u = np.asarray(u, dtype=np.float64)
     nv = model.nv
-    nq = nv + 1
+    nq, nj = nv + 1, nv - 6
     qpos, qvel = x[:nq], x[nq:nq + nv]
     t = terms(model, qpos, qvel)
     M, D, J, feet = t["M"], t["bias"], t["J"], t["cpos"]
-    tau = np.concatenate([np.zeros(6), np.asarray(u, dtype=np.float64)])
+    tau = np.concatenate([np.zeros(6), u[:nj]])
+    mask = np.repeat(np.asarray(contact, dtype=np.float64), 3)
     solve = lambda b: np.linalg.solve(M, b)
-    A = J.T @ solve(J)
-    rhs = -J.T @ solve(tau - D) - 2 * alpha * (J.T @ qvel)
-    grf = np.linalg.solve(A, rhs) * np.repeat(np.asarray(contact, dtype=np.float64), 3)
+    if forces_in_u:
+        grf = u[nj:] * mask
+    else:
+        A = J.T @ solve(J) + eps * np.eye(J.shape[1])
+        rhs = -J.T @ solve(tau - D) - 2 * alpha * (J.T @ qvel)
+        grf = np.linalg.solve(A, rhs) * mask
     v = qvel + solve(tau - D + J @ grf) * dt
     p = qpos[:3] + v[:3] * dt
     quat = quat_integrate(qpos[3:7], v[3:6], dt)
     q = qpos[7:] + v[6:] * dt
-    return np.concatenate([p, quat, q, v, feet, grf])
+    return np.concatenate([p, quat, q, v, feet] + ([] if forces_in_u else [grf]))
 
 
 def penalty(c, alpha=0.1, sigma=5.0):

@@ -17,9 +17,12 @@ stand-in for the parts of `jax`, `jax.numpy` and `mujoco.mjx` they use:
                    code, not present in the reference tree);
   * jax.scipy.linalg.cho_factor / cho_solve -> scipy's.
 
-With --wb it runs the whole-body MPC model of config_aliengo.py instead:
-quadruped_wb_dynamics (models.py:39-117), quadruped_wb_obj and
-quadruped_wb_hessian_gn (objectives.py:77-203).  mjx.make_data,
+With --wb it runs the whole-body MPC models instead.  These are the
+quadruped of config_aliengo.py (quadruped_wb_dynamics, models.py:39-117;
+quadruped_wb_obj and quadruped_wb_hessian_gn, objectives.py:77-203) and the
+humanoid dynamics of config_h1.py and config_talos.py (h1_wb_dynamics and
+talos_wb_dynamics, models.py:119-216).  The humanoids run on the models of
+tests/golden/{h1,talos}_wb.npz, written by make_wb_fixture.py.  mjx.make_data,
 fwd_position, fwd_velocity and jac are then stood in for by the float64
 rigid-body oracle (oracle/wholebody.py) on the aliengo MJCF.  Those vectors
 therefore pin the model's own formulas (the contact-force solve, the masking,
@@ -655,6 +658,30 @@ def main_wb(ref_root, out):
                                               _wrap(np.stack([ref, ref])), _wrap(x), _wrap(u), 0)
         hx.append(x); hu.append(u); hr.append(ref); hs.append(swing)
         hQ.append(np.asarray(Q)); hR.append(np.asarray(Rm)); hM.append(np.asarray(M))
+    # the humanoid dynamics (h1_wb_dynamics, models.py:119-168; talos_wb_dynamics,
+    # models.py:170-216) on the fixtures' models, float64
+    rng2 = np.random.default_rng(78)
+    for name, fn, forces_in_u in (("h1", mo.h1_wb_dynamics, False), ("talos", mo.talos_wb_dynamics, True)):
+        fx = np.load(os.path.join(HERE, "%s_wb.npz" % name))
+        hm = mjcf.load_npz(os.path.join(HERE, "%s_wb.npz" % name))
+        nvh, nch = hm.nv, len(hm.contact_point_body)
+        njh = nvh - 6
+        bodies = [int(hm.contact_jac_body[0]), int(hm.contact_jac_body[-1])]
+        xs, us, cs, xn = [], [], [], []
+        for _ in range(8):
+            quat = rng2.normal(0, 0.1, 4); quat[0] += 1; quat /= np.linalg.norm(quat)
+            qpos = np.concatenate([fx["p0"] + rng2.normal(0, 0.02, 3), quat, fx["q0"] + rng2.normal(0, 0.1, njh)])
+            x = np.concatenate([qpos, rng2.normal(0, 0.3, nvh), np.zeros(3 * nch if forces_in_u else 6 * nch)])
+            u = rng2.normal(0, 10, njh)
+            if forces_in_u:
+                f = rng2.normal(0, 20, 3 * nch); f[2::3] = np.abs(f[2::3]) + 50
+                u = np.concatenate([u, f])
+            c = rng2.integers(0, 2, nch).astype(np.float64)
+            par = np.stack([np.concatenate([c, np.zeros(8)])] * 2)
+            x1 = fn(hm, hm, list(range(nch)), bodies, njh, float(cfg.dt), _wrap(x), _wrap(u), 0, _wrap(par))
+            xs.append(x); us.append(u); cs.append(c); xn.append(np.asarray(x1))
+        g[name + "dyn_x"], g[name + "dyn_u"], g[name + "dyn_contact"], g[name + "dyn_xnext"] = \
+            [np.stack(a) for a in (xs, us, cs, xn)]
     DT["f"] = np.float32
     g["wbhess_x"], g["wbhess_u"], g["wbhess_ref"] = [np.stack(a) for a in (hx, hu, hr)]
     g["wbhess_swing"] = np.array(hs, dtype=np.int32)

@@ -296,3 +296,38 @@ def test_reader_follows_includes_and_repeated_sections():
         assert np.array_equal(a, b[:len(a)] if k in ("body_pos", "body_quat", "mass", "com", "inertia") else b), k
     with pytest.raises(ValueError):
         mjcf.parse(open(os.path.join(here, "slider_scene.xml")).read())   # text has no directory for the include
+
+
+@pytest.mark.parametrize("name,kw", [("h1", dict(alpha=5.0, eps=1e-3)), ("talos", dict(forces_in_u=True))])
+def test_humanoid_dynamics_match_the_reference_code(name, kw):
+    """h1_wb_dynamics (models.py:119-168: alpha = 5, J'M^-1 J regularised by
+    1e-3 I) and talos_wb_dynamics (models.py:170-216: the contact forces are
+    controls), run from the reference's source over the oracle's rigid-body
+    terms, against the oracle's restatement."""
+    hm = mjcf.load_npz(os.path.join(os.path.dirname(__file__), "golden", "%s_wb.npz" % name))
+    dt = float(WBG["wb_dt"])
+    for x, u, c, xn in zip(WBG[name + "dyn_x"], WBG[name + "dyn_u"], WBG[name + "dyn_contact"],
+                           WBG[name + "dyn_xnext"]):
+        out = W.wb_dynamics(hm, dt, x, u, c, **kw)
+        assert out.shape == xn.shape
+        assert np.abs(out - xn).max() < 1e-9 * (1 + np.abs(xn).max())
+
+
+@pytest.mark.parametrize("name", ["h1", "talos"])
+def test_humanoid_models_are_consistent(name):
+    """The h1 and talos fixtures pass the mechanics checks the aliengo model
+    passes: M is the kinetic energy, gravity forces the potential gradient."""
+    hm = mjcf.load_npz(os.path.join(os.path.dirname(__file__), "golden", "%s_wb.npz" % name))
+    fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "%s_wb.npz" % name))
+    rng = np.random.default_rng(3)
+    quat = rng.normal(0, 0.1, 4); quat[0] += 1; quat /= np.linalg.norm(quat)
+    qpos = np.concatenate([fx["p0"], quat, fx["q0"] + rng.normal(0, 0.1, hm.nv - 6)])
+    M = W.terms(hm, qpos, np.zeros(hm.nv))["M"]
+    v = rng.normal(size=hm.nv)
+    ke = W.kinetic_energy_fd(hm, qpos, v)
+    assert abs(0.5 * v @ (M - np.diag(hm.armature)) @ v - ke) <= 1e-7 * ke
+    bias = W.terms(hm, qpos, np.zeros(hm.nv))["bias"]
+    h = 1e-6
+    grad = np.array([(W.potential_energy(hm, W.integrate(hm, qpos, e, h)) -
+                      W.potential_energy(hm, W.integrate(hm, qpos, e, -h))) / (2 * h) for e in np.eye(hm.nv)])
+    assert np.abs(bias - grad).max() < 1e-6 * np.abs(grad).max()
