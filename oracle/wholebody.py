@@ -450,3 +450,53 @@ def wb_hessian_gn(swing_tracking, nj, nc, W, ref_row, x, u):
     Js[:, 13 + nj:13 + 2 * nj] = K
     Hx += Js.T @ np.diag(np.clip(penalty_dd(_limits(nj, x[13 + nj:13 + 2 * nj], 10.0)), -1e6, 1e6)) @ Js
     return Hx, Hu, Hxu
+
+
+def humanoid_residual_jacobians(forces_in_u, nj, nc, ref_row, x, u):
+    """Residual r = [p - p_ref, quat_sub(quat, quat_ref), q - q_ref,
+    v - v_ref, w - w_ref, dq, p_leg - p_leg_ref, tau, grf - grf_ref] of
+    h1_wb_obj / talos_wb_obj (objectives.py:204-250, 325-376), with its
+    Jacobians.  The forces are state entries (h1) or controls u[nj:]
+    (talos, forces_in_u)."""
+    x = np.asarray(x, dtype=np.float64)
+    u = np.asarray(u, dtype=np.float64)
+    rr = _wb_ref(nj, nc, np.asarray(ref_row, dtype=np.float64))
+    grf = u[nj:] if forces_in_u else x[13 + 2 * nj + 3 * nc:]
+    r = np.concatenate([x[:3] - rr["p"], quat_sub(x[3:7], rr["quat"]), x[7:7 + nj] - rr["q"],
+                        x[7 + nj:10 + nj] - rr["dp"], x[10 + nj:13 + nj] - rr["omega"], x[13 + nj:13 + 2 * nj],
+                        x[13 + 2 * nj:13 + 2 * nj + 3 * nc] - rr["p_leg"], u[:nj], grf - rr["grf"]])
+    R = r.size
+    Jx, Ju = np.zeros((R, x.size)), np.zeros((R, u.size))
+    Jx[0:3, 0:3] = np.eye(3)
+    Jx[3:6, 3:7] = quat_sub_jacobian(x[3:7], rr["quat"])
+    Jx[6:12 + 2 * nj, 7:13 + 2 * nj] = np.eye(6 + 2 * nj)
+    a = 12 + 2 * nj
+    Jx[a:a + 3 * nc, 13 + 2 * nj:13 + 2 * nj + 3 * nc] = np.eye(3 * nc)
+    Ju[a + 3 * nc:a + 3 * nc + nj, :nj] = np.eye(nj)
+    b = a + 3 * nc + nj
+    if forces_in_u:
+        Ju[b:b + 3 * nc, nj:] = np.eye(3 * nc)
+    else:
+        Jx[b:b + 3 * nc, 13 + 2 * nj + 3 * nc:] = np.eye(3 * nc)
+    return r, Jx, Ju
+
+
+def humanoid_stage_cost(forces_in_u, nj, nc, W, ref_row, x, u, terminal):
+    """h1_wb_obj / talos_wb_obj: 1/2 r'W r (stage), or its first six blocks
+    (terminal, the t == N branch).  Their barriers are commented out in the
+    reference; the friction cone is computed but unused."""
+    W = np.asarray(W, dtype=np.float64)
+    r, _, _ = humanoid_residual_jacobians(forces_in_u, nj, nc, ref_row, x, u)
+    if terminal:
+        k = 12 + 2 * nj
+        return 0.5 * r[:k] @ W[:k, :k] @ r[:k]
+    return 0.5 * r @ W @ r
+
+
+def humanoid_hessian_gn(forces_in_u, nj, nc, W, ref_row, x, u):
+    """h1_wb_hessian_gn / talos_wb_hessian_gn (objectives.py:252-323,
+    378-450): J_x'W J_x, J_u'W J_u, J_x'W J_u.  The friction-cone term they
+    compute is not added to what they return."""
+    W = np.asarray(W, dtype=np.float64)
+    _, Jx, Ju = humanoid_residual_jacobians(forces_in_u, nj, nc, ref_row, x, u)
+    return Jx.T @ W @ Jx, Ju.T @ W @ Ju, Jx.T @ W @ Ju

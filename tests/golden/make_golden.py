@@ -20,8 +20,9 @@ stand-in for the parts of `jax`, `jax.numpy` and `mujoco.mjx` they use:
 With --wb it runs the whole-body MPC models instead.  These are the
 quadruped of config_aliengo.py (quadruped_wb_dynamics, models.py:39-117;
 quadruped_wb_obj and quadruped_wb_hessian_gn, objectives.py:77-203) and the
-humanoid dynamics of config_h1.py and config_talos.py (h1_wb_dynamics and
-talos_wb_dynamics, models.py:119-216).  The humanoids run on the models of
+humanoid models of config_h1.py and config_talos.py (h1_wb_dynamics and
+talos_wb_dynamics, models.py:119-216; their costs and Gauss-Newton Hessians,
+objectives.py:204-450).  The humanoids run on the models of
 tests/golden/{h1,talos}_wb.npz, written by make_wb_fixture.py.  mjx.make_data,
 fwd_position, fwd_velocity and jac are then stood in for by the float64
 rigid-body oracle (oracle/wholebody.py) on the aliengo MJCF.  Those vectors
@@ -682,6 +683,40 @@ def main_wb(ref_root, out):
             xs.append(x); us.append(u); cs.append(c); xn.append(np.asarray(x1))
         g[name + "dyn_x"], g[name + "dyn_u"], g[name + "dyn_contact"], g[name + "dyn_xnext"] = \
             [np.stack(a) for a in (xs, us, cs, xn)]
+    # the humanoid costs (h1_wb_obj / talos_wb_obj, float32) and Gauss-Newton
+    # Hessians (h1_wb_hessian_gn / talos_wb_hessian_gn, float64), with the
+    # configs' W
+    rng3 = np.random.default_rng(79)
+    for name, obj, hes, forces_in_u in (("h1", ob.h1_wb_obj, ob.h1_wb_hessian_gn, False),
+                                        ("talos", ob.talos_wb_obj, ob.talos_wb_hessian_gn, True)):
+        hc = load(ref_root, "mpx/config/config_%s.py" % name, "ref_config_" + name)
+        fx = np.load(os.path.join(HERE, "%s_wb.npz" % name))
+        njh, nch = int(hc.n_joints), int(hc.n_contact)
+        Wh = np.asarray(hc.W, dtype=np.float64)
+        g[name + "_W"] = Wh
+        ex, eu, er, ev, et, eQ, eR, eM = [], [], [], [], [], [], [], []
+        for i in range(10):
+            quat = rng3.normal(0, 0.1, 4); quat[0] += 1; quat /= np.linalg.norm(quat)
+            qpos = np.concatenate([fx["p0"] + rng3.normal(0, 0.02, 3), quat, fx["q0"] + rng3.normal(0, 0.1, njh)])
+            x = np.concatenate([qpos, rng3.normal(0, 0.3, njh + 6), rng3.normal(0, 0.1, 3 * nch)] +
+                               ([] if forces_in_u else [rng3.normal(0, 50, 3 * nch)]))
+            u = np.concatenate([rng3.normal(0, 20, njh)] + ([rng3.normal(0, 50, 3 * nch)] if forces_in_u else []))
+            qr = rng3.normal(0, 0.1, 4); qr[0] += 1; qr /= np.linalg.norm(qr)
+            ref = np.concatenate([fx["p0"] + rng3.normal(0, 0.02, 3), qr, fx["q0"] + rng3.normal(0, 0.1, njh),
+                                  rng3.normal(0, 0.3, 6), rng3.normal(0, 0.1, 3 * nch), rng3.integers(0, 2, nch),
+                                  rng3.normal(0, 50, 3 * nch)])
+            term = (i % 3 == 2)
+            DT["f"] = np.float32
+            val = obj(njh, nch, 1, _wrap(Wh.astype(np.float32)), _wrap(np.stack([ref, ref]).astype(np.float32)),
+                      _wrap(x.astype(np.float32)), _wrap(u.astype(np.float32)), 1 if term else 0)
+            DT["f"] = np.float64
+            Q, Rm, M = hes(njh, nch, _wrap(Wh), _wrap(np.stack([ref, ref])), _wrap(x), _wrap(u), 0)
+            ex.append(x); eu.append(u); er.append(ref); ev.append(float(np.asarray(val))); et.append(term)
+            eQ.append(np.asarray(Q)); eR.append(np.asarray(Rm)); eM.append(np.asarray(M))
+        g[name + "cost_x"], g[name + "cost_u"], g[name + "cost_ref"] = [np.stack(a) for a in (ex, eu, er)]
+        g[name + "cost_val"] = np.array(ev, dtype=np.float32)
+        g[name + "cost_terminal"] = np.array(et, dtype=np.int32)
+        g[name + "hess_Q"], g[name + "hess_R"], g[name + "hess_M"] = [np.stack(a) for a in (eQ, eR, eM)]
     DT["f"] = np.float32
     g["wbhess_x"], g["wbhess_u"], g["wbhess_ref"] = [np.stack(a) for a in (hx, hu, hr)]
     g["wbhess_swing"] = np.array(hs, dtype=np.int32)

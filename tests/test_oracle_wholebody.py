@@ -331,3 +331,23 @@ def test_humanoid_models_are_consistent(name):
     grad = np.array([(W.potential_energy(hm, W.integrate(hm, qpos, e, h)) -
                       W.potential_energy(hm, W.integrate(hm, qpos, e, -h))) / (2 * h) for e in np.eye(hm.nv)])
     assert np.abs(bias - grad).max() < 1e-6 * np.abs(grad).max()
+
+
+@pytest.mark.parametrize("name,forces_in_u", [("h1", False), ("talos", True)])
+def test_humanoid_cost_and_hessian_match_the_reference_code(name, forces_in_u):
+    """h1_wb_obj / talos_wb_obj (float32 in the reference) and
+    h1_wb_hessian_gn / talos_wb_hessian_gn (float64, finite-difference
+    autodiff in the generator) with config_h1 / config_talos's W."""
+    Wh = WBG[name + "_W"]
+    nc = 4 if name == "h1" else 8
+    nj = (WBG[name + "cost_ref"].shape[1] - 13 - 7 * nc)
+    for i, (x, u, r, v, t) in enumerate(zip(WBG[name + "cost_x"], WBG[name + "cost_u"], WBG[name + "cost_ref"],
+                                            WBG[name + "cost_val"], WBG[name + "cost_terminal"])):
+        o = W.humanoid_stage_cost(forces_in_u, nj, nc, Wh.astype(np.float32), r.astype(np.float32),
+                                  x.astype(np.float32), u.astype(np.float32), bool(t))
+        assert abs(o - v) <= 2e-6 * max(1.0, abs(v)), i
+        Hx, Hu, Hxu = W.humanoid_hessian_gn(forces_in_u, nj, nc, Wh, r, x, u)
+        Q, R, M = WBG[name + "hess_Q"][i], WBG[name + "hess_R"][i], WBG[name + "hess_M"][i]
+        assert np.abs(Hx - Q).max() <= 1e-7 * np.abs(Q).max(), i
+        assert np.abs(Hu - R).max() <= 1e-7 * np.abs(R).max(), i
+        assert np.abs(Hxu - M).max() <= 1e-7 * (1 + np.abs(M).max()), i
