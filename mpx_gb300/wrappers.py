@@ -2,9 +2,13 @@
 
   BatchedMPCControllerWrapper  <- mpx/utils/mpc_wrapper_srbd.py:19-175  (SRBD, batched)
   MPCControllerWrapper         <- mpx/utils/mpc_wrapper.py:194-468      (single instance)
-  BatchedDataMPCWrapper        <- mpx/utils/mpc_wrapper.py:16-192       (mpx_data + run(data, x0, input))
+  BatchedDataMPCWrapper        <- mpx/utils/mpc_wrapper.py:29-192       (make_data + run(data, x0, input))
+  mpx_data                     <- mpx/utils/mpc_wrapper.py:16-27        (the data record)
   mpc(...) / make_mpc(...)     <- optimizers.mpc as bound with functools.partial
                                   (mpx/utils/mpc_wrapper_srbd.py:68,77)
+
+mpx_gb300.mpc_wrapper and mpx_gb300.mpc_wrapper_srbd export these classes
+under the reference modules' own names.
 
 Every per-tick step of the reference's `run()` -- gait timer, reference
 generator, solve, warm-start shift -- runs as a CUDA kernel of libmpxg on
@@ -310,11 +314,22 @@ class MPCControllerWrapper:
         self._set_warm(x0)
         print("MPC Controller Reset")
 
-    def runOffline(self, qpos, qvel, reference, parameter, max_iter=100):
+    def runOffline(self, qpos, qvel, reference=None, parameter=None, max_iter=100):
         """mpc_wrapper.py:387-468: repeat single SQP iterations until the
         reference's stop rule  last_cost - cost < 1e-3 and sum(c^2) < 1e-5
         (:465), with cost the objective (sum of the stage costs) and c the
-        defects.  `reference`/`parameter` are the offline tables."""
+        defects.  `reference`/`parameter` are the offline tables
+        ([N+1, 17] and [N+1, 16] for the compiled SRBD model); by default
+        they come, as in the reference (:411), from
+        config.reference(N+1, dt, n_joints, n_contact, p_legs0, q0)."""
+        if reference is None or parameter is None:
+            make = getattr(self.config, "reference", None)
+            if make is None:
+                raise ValueError("runOffline needs the offline tables: pass reference and parameter, or give the "
+                                 "config a reference(N+1, dt, n_joints, n_contact, p_legs0, q0) function")
+            reference, parameter = make(self.N + 1, self.config.dt, getattr(self.config, "n_joints", 12),
+                                        getattr(self.config, "n_contact", 4), self.config.p_legs0,
+                                        getattr(self.config, "q0", None))
         x0 = _to_dev(self._state(qpos, qvel).reshape(1, -1), self.dev)
         ref = _to_dev(reference, self.dev).reshape(1, self.N + 1, -1)
         par = _to_dev(parameter, self.dev).reshape(1, self.N + 1, -1)
@@ -336,10 +351,32 @@ class MPCControllerWrapper:
         return X, U, reference, outputs
 
 
+class mpx_data(dict):
+    """The controller record of mpx/utils/mpc_wrapper.py:16-27 (dt,
+    duty_factor, step_freq, step_height, contact_time, liftoff, X0, U0, V0, W,
+    grf), for all environments at once: the array fields are device tensors
+    with a leading env dimension.  Fields read as items (data["X0"]) or, as
+    on the reference's flax PyTreeNode, as attributes (data.X0), and
+    replace(**fields) returns an updated copy."""
+
+    FIELDS = ("dt", "duty_factor", "step_freq", "step_height", "contact_time", "liftoff", "X0", "U0", "V0", "W",
+              "grf")
+
+    def __getattr__(self, name):
+        try:
+            return self[name]
+        except KeyError:
+            raise AttributeError(name) from None
+
+    def replace(self, **fields):
+        return mpx_data(self, **fields)
+
+
 class BatchedDataMPCWrapper:
     """The mpx_data API of mpx/utils/mpc_wrapper.py:16-192: a per-environment
     data record and run(data, x0, input) -> (data, grf), on a compiled SRBD
-    model.  `data` is a dict of device tensors with a leading env dimension."""
+    model.  `data` is an mpx_data (a dict of device tensors with a leading env
+    dimension); a plain dict with the same keys is accepted too."""
 
     def __init__(self, config, n_env, limited_memory=False, opts=None, device=None, desc=None):
         self.config = config
@@ -361,7 +398,7 @@ class BatchedDataMPCWrapper:
         B, N = self.n_env, self.N
         dev = self.dev
         W = np.diag(np.asarray(self.config.W, dtype=np.float64)).astype(np.float32)
-        return dict(
+        return mpx_data(
             dt=float(self.config.dt), duty_factor=float(self.config.duty_factor),
             step_freq=float(self.config.step_freq), step_height=float(self.config.step_height),
             contact_time=_to_dev(np.tile(np.asarray(self.config.timer_t, dtype=np.float32), (B, 1)), dev),
@@ -406,14 +443,18 @@ class BatchedDataMPCWrapper:
             U0n[nan] = u_ref.reshape(1, 1, -1).expand(int(nan.sum()), N, -1)
             V0n[nan] = 0.0
         grf = torch.where(nan.unsqueeze(1), data["U0"][:, 1, :], U[:, 0, :])
-        data = dict(data, X0=X0n, U0=U0n, V0=V0n, contact_time=ct, liftoff=lo, grf=grf)
+        data = mpx_data(data, X0=X0n, U0=U0n, V0=V0n, contact_time=ct, liftoff=lo, grf=grf)
         return data, grf
 
-    def reset(self, data, x0, foot=None):
-        """mpc_wrapper.py:172-192."""
+    def reset(self, data, qpos, qvel=None, foot=None):
+        """mpc_wrapper.py:172-192, called as there with (data, qpos, qvel,
+        foot): the compiled model's state is the floating base, qpos[:, :7]
+        followed by qvel[:, :6].  Called as (data, x0), qpos is that state."""
         B, N, dev = self.n_env, self.N, self.dev
-        x0 = _to_dev(x0, dev).reshape(B, -1)
-        return dict(data, contact_time=_to_dev(np.tile(np.asarray(self.config.timer_t, dtype=np.float32), (B, 1)), dev),
+        x0 = _to_dev(qpos, dev).reshape(B, -1)
+        if qvel is not None:
+            x0 = torch.cat([x0[:, :7], _to_dev(qvel, dev).reshape(B, -1)[:, :6]], 1).contiguous()
+        return mpx_data(data, contact_time=_to_dev(np.tile(np.asarray(self.config.timer_t, dtype=np.float32), (B, 1)), dev),
                     liftoff=_to_dev(foot, dev).reshape(B, 12) if foot is not None else torch.zeros(B, 12, device=dev),
                     X0=x0.unsqueeze(1).expand(-1, N + 1, -1).contiguous(),
                     U0=_to_dev(np.tile(np.asarray(self.config.u_ref, dtype=np.float32), (B, N, 1)), dev),

@@ -1,0 +1,111 @@
+"""The wrapper API against the reference's (CPU; no kernel runs).
+
+A caller of the reference switches by its import line: mpx_gb300.mpc_wrapper
+and mpx_gb300.mpc_wrapper_srbd export the reference modules' names, and each
+method takes the reference's parameters, in the reference's order, first.
+"""
+import inspect
+import types
+
+import numpy as np
+import torch
+
+from mpx_gb300 import mpc_wrapper, mpc_wrapper_srbd, wrappers
+
+# (class, method) -> the reference's parameters after self
+REFERENCE_SIGNATURES = {
+    # mpx/utils/mpc_wrapper_srbd.py:20,91,143,153,156,162
+    (mpc_wrapper_srbd.BatchedMPCControllerWrapper, "__init__"): ["config", "n_env"],
+    (mpc_wrapper_srbd.BatchedMPCControllerWrapper, "run"): ["x0", "input", "foot_op", "contact"],
+    (mpc_wrapper_srbd.BatchedMPCControllerWrapper, "torch_run"): ["x0_torch", "input_torch", "foot_op_torch"],
+    (mpc_wrapper_srbd.BatchedMPCControllerWrapper, "whole_body_run"): ["qpos", "qvel"],
+    (mpc_wrapper_srbd.BatchedMPCControllerWrapper, "torch_whole_body_run"): ["qpos", "qvel"],
+    (mpc_wrapper_srbd.BatchedMPCControllerWrapper, "reset"): [],
+    # mpx/utils/mpc_wrapper.py:30,100,115,172
+    (mpc_wrapper.BatchedMPCControllerWrapper, "__init__"): ["config", "n_env", "limited_memory"],
+    (mpc_wrapper.BatchedMPCControllerWrapper, "make_data"): [],
+    (mpc_wrapper.BatchedMPCControllerWrapper, "run"): ["data", "x0", "input"],
+    (mpc_wrapper.BatchedMPCControllerWrapper, "reset"): ["data", "qpos", "qvel", "foot"],
+    # mpx/utils/mpc_wrapper.py:195,297,367,387
+    (mpc_wrapper.MPCControllerWrapper, "__init__"): ["config", "limited_memory"],
+    (mpc_wrapper.MPCControllerWrapper, "run"): ["qpos", "qvel", "input", "contact"],
+    (mpc_wrapper.MPCControllerWrapper, "reset"): ["qpos", "qvel"],
+    (mpc_wrapper.MPCControllerWrapper, "runOffline"): ["qpos", "qvel"],
+}
+
+
+def test_reference_module_names():
+    assert mpc_wrapper_srbd.BatchedMPCControllerWrapper is wrappers.BatchedMPCControllerWrapper
+    assert mpc_wrapper.BatchedMPCControllerWrapper is wrappers.BatchedDataMPCWrapper
+    assert mpc_wrapper.MPCControllerWrapper is wrappers.MPCControllerWrapper
+    assert mpc_wrapper.mpx_data is wrappers.mpx_data
+
+
+def test_reference_parameters_come_first_in_order():
+    for (cls, name), ref in REFERENCE_SIGNATURES.items():
+        params = list(inspect.signature(getattr(cls, name)).parameters.values())[1:]
+        assert [p.name for p in params[:len(ref)]] == ref, (cls.__name__, name)
+        # anything we add after the reference's parameters has a default
+        for p in params[len(ref):]:
+            assert p.default is not inspect.Parameter.empty, (cls.__name__, name, p.name)
+
+
+def test_mpx_data_record():
+    # mpx/utils/mpc_wrapper.py:16-27
+    assert wrappers.mpx_data.FIELDS == ("dt", "duty_factor", "step_freq", "step_height", "contact_time", "liftoff",
+                                        "X0", "U0", "V0", "W", "grf")
+    d = wrappers.mpx_data(dt=0.02, X0=torch.zeros(2, 3, 4))
+    assert d.dt == 0.02 and d["dt"] == 0.02 and d.X0 is d["X0"]
+    e = d.replace(dt=0.01)
+    assert isinstance(e, wrappers.mpx_data) and e.dt == 0.01 and d.dt == 0.02 and e.X0 is d.X0
+    try:
+        d.grf
+    except AttributeError:
+        pass
+    else:
+        raise AssertionError("a missing field must raise AttributeError")
+
+
+def _cpu_data_wrapper(B=3, N=5):
+    """A BatchedDataMPCWrapper with its host state on the CPU (no solver)."""
+    w = object.__new__(wrappers.BatchedDataMPCWrapper)
+    w.n_env, w.N, w.dev = B, N, torch.device("cpu")
+    w.config = types.SimpleNamespace(timer_t=np.array([0.5, 0.0, 0.0, 0.5]), u_ref=np.arange(12.0))
+    w.desc = types.SimpleNamespace(n=13)
+    return w
+
+
+def test_data_reset_with_the_reference_arguments():
+    """reset(data, qpos, qvel, foot) as in mpc_wrapper.py:172-192: the state
+    is the floating base qpos[:, :7] ++ qvel[:, :6]; the same as reset(data,
+    x0) with that state."""
+    B, N = 3, 5
+    w = _cpu_data_wrapper(B, N)
+    rng = np.random.default_rng(0)
+    qpos = rng.normal(size=(B, 19)).astype(np.float32)
+    qvel = rng.normal(size=(B, 18)).astype(np.float32)
+    foot = rng.normal(size=(B, 12)).astype(np.float32)
+    d = w.reset(wrappers.mpx_data(dt=0.02), qpos, qvel, foot)
+    x0 = np.concatenate([qpos[:, :7], qvel[:, :6]], 1)
+    assert isinstance(d, wrappers.mpx_data) and d.dt == 0.02
+    assert d.X0.shape == (B, N + 1, 13)
+    assert np.array_equal(d.X0.numpy(), np.repeat(x0[:, None], N + 1, 1))
+    assert np.array_equal(d.liftoff.numpy(), foot)
+    assert np.array_equal(d.U0.numpy(), np.tile(np.arange(12.0, dtype=np.float32), (B, N, 1)))
+    assert np.array_equal(d.contact_time.numpy(), np.tile(np.float32([0.5, 0, 0, 0.5]), (B, 1)))
+    assert not d.V0.any() and not d.grf.any()
+    d2 = w.reset(wrappers.mpx_data(dt=0.02), x0, foot=foot)
+    for k in ("X0", "U0", "V0", "liftoff", "contact_time", "grf"):
+        assert torch.equal(d[k], d2[k]), k
+
+
+def test_run_offline_without_tables_says_what_it_needs():
+    w = object.__new__(wrappers.MPCControllerWrapper)
+    w.config = types.SimpleNamespace(dt=0.02, p_legs0=np.zeros(12))
+    w.N = 5
+    try:
+        w.runOffline(np.zeros(19), np.zeros(18))
+    except ValueError as e:
+        assert "reference and parameter" in str(e)
+    else:
+        raise AssertionError("runOffline without tables must raise ValueError")
