@@ -76,3 +76,27 @@ def test_xla_vjp_target_matches_solver_vjp(cuda):
     assert np.array_equal(gx0.cpu().numpy(), ref["gx0"].cpu().numpy())
     assert np.array_equal(gref.cpu().numpy(), ref["gref"].cpu().numpy())
     s.close()
+
+
+def test_register_hands_xla_the_library_entry_points(monkeypatch):
+    """register() with a stand-in for jax.ffi: each target is registered once,
+    for the CUDA platform with the legacy custom-call API, as a capsule named
+    as XLA expects that carries the address of libmpxg's own entry point."""
+    import types
+    calls = []
+    fake = types.SimpleNamespace(ffi=types.SimpleNamespace(
+        register_ffi_target=lambda name, cap, platform, api_version: calls.append((name, cap, platform, api_version))))
+    monkeypatch.setattr(jax_ffi, "HAVE_JAX", True)
+    monkeypatch.setattr(jax_ffi, "jax", fake, raising=False)
+    monkeypatch.setattr(jax_ffi, "_registered", False)
+    jax_ffi.register()
+    jax_ffi.register()  # idempotent
+    L = _lib.load()
+    get = ctypes.pythonapi.PyCapsule_GetPointer
+    get.restype, get.argtypes = ctypes.c_void_p, [ctypes.py_object, ctypes.c_char_p]
+    want = {jax_ffi.TARGET: ctypes.cast(L.mpxg_xla_solve, ctypes.c_void_p).value,
+            jax_ffi.TARGET_VJP: ctypes.cast(L.mpxg_xla_solve_vjp, ctypes.c_void_p).value}
+    assert [c[0] for c in calls] == [jax_ffi.TARGET, jax_ffi.TARGET_VJP]
+    for name, cap, platform, api_version in calls:
+        assert (platform, api_version) == ("CUDA", 0)
+        assert get(cap, b"xla._CUSTOM_CALL_TARGET") == want[name]
