@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = ["oracle_capi.cpp"]
-HEADERS = ["oracle.hpp", "refgen.hpp"]
+HEADERS = ["oracle.hpp", "refgen.hpp", "flops.hpp"]
 
 
 def needs_build():

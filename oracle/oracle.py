@@ -206,6 +206,16 @@ def linearize(desc, x, u, ref, par, W, terminal=False):
     return A, Bm, fx, g, H, float(l[0])
 
 
+def stage_flops(desc, x, u, ref, par, W):
+    """Model FLOPs of one non-terminal stage at (x, u), counted on the
+    oracle's model functions with the counting scalar of flops.hpp: dict of
+    dyn_value, dyn_jacobian, cost_value, linearisation and trial."""
+    out = np.zeros(5)
+    lib().orc_stage_flops(ctypes.byref(make_model(desc)), _dp(_f64(x)), _dp(_f64(u)), _dp(_f64(ref)),
+                          _dp(_f64(par)), _dp(_f64(W)), _dp(out))
+    return dict(zip(("dyn_value", "dyn_jacobian", "cost_value", "linearisation", "trial"), out.tolist()))
+
+
 def penalty(desc, c):
     return lib().orc_penalty(ctypes.byref(make_model(desc)), float(c))
 

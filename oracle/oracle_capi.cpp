@@ -9,6 +9,7 @@
 #include <omp.h>
 #endif
 
+#include "flops.hpp"
 #include "oracle.hpp"
 #include "refgen.hpp"
 
@@ -239,6 +240,14 @@ int orc_refgen_srbd(int N, float dt, float mass, const float* foot0, float duty_
   g.duty_factor = duty_factor; g.step_freq = step_freq; g.step_height = step_height; g.clearence_speed = clearence_speed;
   refgen_srbd(g, t_timer, x, foot, input, contact, liftoff, reference, parameter, foot_ref_dot);
   return 0;
+}
+
+// Model FLOPs of one non-terminal stage at (x, u) (flops.hpp): out = {f,
+// f with [A B], l, the linearisation, one line-search trial}.
+void orc_stage_flops(const orc_model* md, const double* x, const double* u, const double* ref, const double* par,
+                     const double* W, double* out) {
+  const flopcount::StageCount c = flopcount::count_stage(to_mp(md), x, u, ref, par, W);
+  out[0] = c.dyn_value; out[1] = c.dyn_jacobian; out[2] = c.cost_value; out[3] = c.linearisation; out[4] = c.trial;
 }
 
 int orc_num_threads(void) {
