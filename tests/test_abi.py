@@ -152,3 +152,59 @@ def test_wb_step_rejects_what_it_cannot_hold():
     assert b"<= 32" in L.mpxg_last_error(None)
     S = model.to_struct()
     assert L.mpxg_wb_step(None, ctypes.byref(S), 0, 0.02, 25.0, None, None, None, None) == 0
+
+
+def _declarations():
+    """(return type, name, [parameter types]) of every function in mpxg.h."""
+    text = open(os.path.join(ROOT, "include", "mpxg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = []
+    for ret, name, params in re.findall(r"([A-Za-z_][\w\s\*]*?)\b(mpxg_[a-z_0-9]+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        types = []
+        for p in params.split(","):
+            p = " ".join(p.replace("*", " * ").split())
+            if p in ("", "void"):
+                continue
+            words = p.split()
+            if words[-1] != "*":
+                words = words[:-1]  # the parameter's name
+            types.append(" ".join(words))
+        ret = " ".join(ret.replace("*", " * ").split()[-3:])
+        out.append((ret, name, types))
+    return out
+
+
+def _c_kind(t):
+    if t.endswith("*"):
+        return "pointer"
+    return {"int": "int", "mpxg_status": "int", "float": "float", "double": "double", "long long": "int64",
+            "size_t": "size_t"}[t.replace("const ", "")]
+
+
+def _ctypes_kind(ct):
+    if ct in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(ct, "_type_") and isinstance(ct._type_, type):
+        return "pointer"
+    if ct is None:
+        return "void"
+    return {ctypes.c_int: "int", ctypes.c_float: "float", ctypes.c_double: "double", ctypes.c_longlong: "int64",
+            ctypes.c_size_t: "size_t"}[ct]
+
+
+def test_python_binding_matches_every_declared_signature():
+    """Each entry point that the Python layer binds passes its arguments as
+    mpxg.h declares them (count and C kind: pointer, int, float, 64-bit
+    integer, size_t) and reads a size_t result as size_t, so no argument is
+    truncated or passed in the wrong register class."""
+    from mpx_gb300 import _lib
+    L = _lib.load()
+    decls = _declarations()
+    assert len(decls) == len(declared_functions())
+    for ret, name, params in decls:
+        f = getattr(L, name)
+        assert f.argtypes is not None or not params, name
+        assert [_ctypes_kind(a) for a in f.argtypes or []] == [_c_kind(t) for t in params], name
+        if ret.endswith("size_t"):
+            assert f.restype is ctypes.c_size_t, name
+        if ret.endswith("*") and "char" in ret:
+            assert f.restype is ctypes.c_char_p, name
