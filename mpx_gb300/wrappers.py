@@ -56,6 +56,23 @@ def _cfg(config, name, default=None):
     return v
 
 
+def _save_state(obj, names):
+    return {k: getattr(obj, k).detach().to("cpu", copy=True) for k in names}
+
+
+def _load_state(obj, names, state):
+    new = {}
+    for k in names:
+        cur = getattr(obj, k)
+        src = torch.as_tensor(state[k])
+        if tuple(src.shape) != tuple(cur.shape):
+            raise ValueError("load_state: %s has shape %s, this controller holds %s"
+                             % (k, tuple(src.shape), tuple(cur.shape)))
+        new[k] = src.to(device=cur.device, dtype=cur.dtype).contiguous().clone()
+    for k, v in new.items():
+        setattr(obj, k, v)
+
+
 # ----------------------------------------------------------------- functional API
 def make_mpc(desc, opts=None, n_max=None, batch_max=1, device=None):
     """The equivalent of `jax.vmap(partial(optimizers.mpc, cost, dynamics,
@@ -199,6 +216,23 @@ class BatchedMPCControllerWrapper:
         self._keep = (x0, inp, foot, cont)
         return 0
 
+    # resident state carried from tick to tick (warm start, gait timers,
+    # liftoff positions) and the last tick's outputs
+    STATE = ("batch_X0", "batch_U0", "batch_V0", "contact_time", "liftoff", "contact", "grf", "foot_ref",
+             "foot_ref_dot")
+
+    def save_state(self):
+        """Checkpoint of the controller between ticks as host tensors.  The
+        reference keeps the same state in wrapper attributes
+        (mpc_wrapper_srbd.py:56-58,82-88) and writes no files.
+        load_state() resumes from it here or on another wrapper with the same
+        config and n_env (another process or GPU)."""
+        return _save_state(self, self.STATE)
+
+    def load_state(self, state):
+        """Resume from save_state(); the next run() continues that episode."""
+        _load_state(self, self.STATE, state)
+
     def torch_run(self, x0_torch, input_torch, foot_op_torch, contact_torch=None):
         """mpc_wrapper_srbd.py:143-151 (which calls run() without `contact`);
         here contact defaults to the gait schedule's current contact."""
@@ -295,6 +329,17 @@ class MPCControllerWrapper:
         q = (X[0, 0] if not self._nan else self.X0[0, 1]).cpu().numpy()[:7]
         dq = (X[0, 1] if not self._nan else self.X0[0, 1]).cpu().numpy()[7:13]
         return grf, q, dq
+
+    STATE = ("X0", "U0", "V0", "contact_time", "liftoff")
+
+    def save_state(self):
+        """Checkpoint of the warm start and gait state as host tensors (the
+        reference keeps them in attributes, mpc_wrapper.py:367-385)."""
+        return _save_state(self, self.STATE)
+
+    def load_state(self, state):
+        """Resume from save_state()."""
+        _load_state(self, self.STATE, state)
 
     def _update_and_extract(self, X, U, V, x0):
         """mpc_wrapper.py:261-282: shift the warm start, or on NaN in U[0,0]

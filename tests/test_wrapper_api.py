@@ -109,3 +109,51 @@ def test_run_offline_without_tables_says_what_it_needs():
         assert "reference and parameter" in str(e)
     else:
         raise AssertionError("runOffline without tables must raise ValueError")
+
+
+def test_save_and_load_state_round_trip():
+    """save_state() checkpoints the tick-to-tick state as host tensors;
+    load_state() restores it with the holder's device and dtype, into a
+    wrapper of the same shape, and refuses a checkpoint of another shape."""
+    rng = np.random.default_rng(1)
+    B, N = 3, 6
+
+    def srbd():
+        w = object.__new__(wrappers.BatchedMPCControllerWrapper)
+        w.batch_X0, w.batch_U0, w.batch_V0 = (torch.zeros(B, N + 1, 13), torch.zeros(B, N, 12),
+                                              torch.zeros(B, N + 1, 13))
+        w.contact_time, w.liftoff = torch.zeros(B, 4), torch.zeros(B, 12)
+        w.contact = torch.zeros(B, 4, dtype=torch.int32)
+        w.grf, w.foot_ref, w.foot_ref_dot = torch.zeros(B, 12), torch.zeros(B, 12), torch.zeros(B, 12)
+        return w
+
+    a = srbd()
+    for k in a.STATE:
+        t = getattr(a, k)
+        setattr(a, k, torch.as_tensor(rng.normal(size=t.shape) * 5).to(t.dtype))
+    st = a.save_state()
+    assert set(st) == set(a.STATE) and all(v.device.type == "cpu" for v in st.values())
+    b = srbd()
+    b.load_state(st)
+    for k in a.STATE:
+        assert torch.equal(getattr(a, k), getattr(b, k)) and getattr(b, k).dtype == getattr(a, k).dtype, k
+    a.batch_X0 += 1  # the checkpoint is a copy
+    assert not torch.equal(a.batch_X0, st["batch_X0"])
+    small = srbd()
+    small.batch_X0 = torch.zeros(B, N, 13)
+    try:
+        small.load_state(st)
+    except ValueError as e:
+        assert "batch_X0" in str(e)
+    else:
+        raise AssertionError("a checkpoint of another shape must be refused")
+    # nothing was replaced by the refused load
+    assert small.batch_X0.shape == (B, N, 13) and not small.contact_time.any()
+
+    s = object.__new__(wrappers.MPCControllerWrapper)
+    s.X0, s.U0, s.V0 = torch.ones(1, N + 1, 13), torch.ones(1, N, 12), torch.ones(1, N + 1, 13)
+    s.contact_time, s.liftoff = torch.full((1, 4), 0.25), torch.ones(1, 12)
+    st = s.save_state()
+    s.X0 = torch.zeros(1, N + 1, 13)
+    s.load_state(st)
+    assert torch.equal(s.X0, torch.ones(1, N + 1, 13))
