@@ -6,7 +6,10 @@ from mpx_gb300 import problem as P
 
 
 def _stage(model, seed):
-    wl = P.quadruped_workload(1, horizons=(10,), seed=seed, model=model)
+    if model == P.MODEL_BIPED_WRENCH12:
+        wl = P.biped_workload(1, horizons=(10,), seed=seed)
+    else:
+        wl = P.quadruped_workload(1, horizons=(10,), seed=seed, model=model)
     rng = np.random.default_rng(seed)
     x = wl.X0[0, 3].astype(np.float64) + 0.05 * rng.standard_normal(wl.desc.n)
     if model == P.MODEL_SRBD_QUAT13:
@@ -15,7 +18,7 @@ def _stage(model, seed):
     return wl, x, u, wl.reference[0, 3].astype(np.float64), wl.parameter[0, 3].astype(np.float64)
 
 
-@pytest.mark.parametrize("model", [P.MODEL_SRBD_QUAT13, P.MODEL_SRBD_RPY12])
+@pytest.mark.parametrize("model", [P.MODEL_SRBD_QUAT13, P.MODEL_SRBD_RPY12, P.MODEL_BIPED_WRENCH12])
 def test_dynamics_jacobian_fd(oracle, model):
     wl, x, u, ref, par = _stage(model, 3)
     A, B, fx, g, H, l = oracle.linearize(wl.desc, x, u, ref, par, wl.W[0])
@@ -30,7 +33,7 @@ def test_dynamics_jacobian_fd(oracle, model):
         np.testing.assert_allclose(B[:, j], col, atol=1e-6, rtol=1e-5)
 
 
-@pytest.mark.parametrize("model", [P.MODEL_SRBD_QUAT13, P.MODEL_SRBD_RPY12])
+@pytest.mark.parametrize("model", [P.MODEL_SRBD_QUAT13, P.MODEL_SRBD_RPY12, P.MODEL_BIPED_WRENCH12])
 def test_cost_gradient_fd(oracle, model):
     wl, x, u, ref, par = _stage(model, 4)
     A, B, fx, g, H, l = oracle.linearize(wl.desc, x, u, ref, par, wl.W[0])
@@ -44,12 +47,21 @@ def test_cost_gradient_fd(oracle, model):
         assert abs(g[j] - fd) <= 1e-5 * max(1.0, abs(fd)), j
 
 
-def test_relaxed_barrier_hessian_is_exact(oracle):
+@pytest.mark.parametrize("model", [P.MODEL_SRBD_RPY12, P.MODEL_BIPED_WRENCH12])
+def test_relaxed_barrier_hessian_is_exact(oracle, model):
     """For the relaxed barrier (kind 1) the control block of the Hessian model
-    is the exact second derivative of the cost (the tracking part is quadratic)."""
-    wl, x, u, ref, par = _stage(P.MODEL_SRBD_RPY12, 5)
-    ref = ref.copy(); ref[12:16] = 1.0  # all legs in stance
-    u[2::3] = np.abs(u[2::3]) + 20.0
+    is the exact second derivative of the cost (the tracking part is quadratic).
+    The biped's constraints add the centre-of-pressure and torsion bounds of
+    its foot plates, linear in the wrench."""
+    wl, x, u, ref, par = _stage(model, 5)
+    ref = ref.copy()
+    if model == P.MODEL_BIPED_WRENCH12:
+        ref[12:14] = 1.0  # both feet in stance
+        u[2::6] = np.abs(u[2::6]) + 300.0
+        u[3::6] *= 0.1; u[4::6] *= 0.1; u[5::6] *= 0.1
+    else:
+        ref[12:16] = 1.0  # all legs in stance
+        u[2::3] = np.abs(u[2::3]) + 20.0
     A, B, fx, g, H, l = oracle.linearize(wl.desc, x, u, ref, par, wl.W[0])
     n = wl.desc.n
     h = 1e-5
