@@ -94,8 +94,11 @@ class MPCServer:
         self._mi = {}          # key -> model index (order of `models`)
         self.model_names = list(names)
         self._arrival = {}     # ticket -> (key, m, arrival time)
-        self._t_arr = np.zeros(1 << 16)   # ticket -> arrival time (the vectorised poll_fast path)
-        self._t_mod = np.zeros(1 << 16, dtype=np.int8)  # ticket -> model index
+        # arrival time and model index of tickets _t_base, _t_base + 1, ...
+        # (the vectorised poll_fast path)
+        self._t_arr = np.zeros(1 << 16)
+        self._t_mod = np.zeros(1 << 16, dtype=np.int8)
+        self._t_base = 0
         self.completed = []
         self._res = (_lib.Result * 4096)()
         self._res_np = np.frombuffer(self._res, dtype=np.dtype(
@@ -165,17 +168,33 @@ class MPCServer:
         return t.value
 
     def _note_arrival(self, tickets, times, models):
+        """Record the arrival time and model of new tickets.  The arrays cover
+        the tickets from the oldest one still outstanding upwards: when a
+        ticket runs past their end they are shifted down to that ticket (and
+        doubled only if the tickets in flight need it), so their size follows
+        the tickets in flight, not the tickets ever issued."""
         top = int(tickets.max())
-        if top >= self._t_arr.shape[0]:
-            size = max(2 * self._t_arr.shape[0], top + 1)
-            grown = np.zeros(size)
-            grown[:self._t_arr.shape[0]] = self._t_arr
-            self._t_arr = grown
-            gm = np.zeros(size, dtype=np.int8)
-            gm[:self._t_mod.shape[0]] = self._t_mod
-            self._t_mod = gm
-        self._t_arr[tickets] = times
-        self._t_mod[tickets] = models
+        size = self._t_arr.shape[0]
+        if top - self._t_base >= size:
+            low = min(self._arrival) if self._arrival else int(tickets.min())
+            new = size
+            while top - low >= new:
+                new *= 2
+            live = self._t_base + size - low  # entries [low, old end) stay
+            arr = np.zeros(new)
+            mod = np.zeros(new, dtype=np.int8)
+            if live > 0:
+                arr[:live] = self._t_arr[low - self._t_base:]
+                mod[:live] = self._t_mod[low - self._t_base:]
+            self._t_arr, self._t_mod, self._t_base = arr, mod, low
+        idx = tickets - self._t_base
+        self._t_arr[idx] = times
+        self._t_mod[idx] = models
+
+    def _arrivals(self, tickets):
+        """(arrival times, model indices) of outstanding tickets."""
+        idx = tickets - self._t_base
+        return self._t_arr[idx], self._t_mod[idx]
 
     def submit_many(self, episodes, arrival=None):
         """Queue the next tick of several episodes in one call; returns their tickets."""
@@ -243,10 +262,11 @@ class MPCServer:
                         "completed")
             r = self._res_np[:cnt.value]
             tk = r["ticket"]
-            lat.append(now - self._t_arr[tk])
+            t_arr, t_mod = self._arrivals(tk)
+            lat.append(now - t_arr)
             st.append(r["status"].copy())
             kk.append(r["kkt"][:, 2].copy())
-            md.append(self._t_mod[tk])
+            md.append(t_mod)
             for t in tk.tolist():
                 self._arrival.pop(t, None)
             if cnt.value < len(self._res):
