@@ -46,10 +46,11 @@ class MPCServer:
     models: {name: (ModelDesc, gait)} with gait = dict(duty, step_freq, height,
     offsets (legs x 3), W (24 x 24 diagonal), phase0 (legs,)).  The budget is
     split evenly between the models; each model's pool holds as many slots as
-    fit after its solver scratch."""
+    fit after its solver scratch.  `completed` keeps the last `keep_completed`
+    results that poll() returned, oldest first."""
 
     def __init__(self, models, n_max=200, budget_bytes=8 << 30, opts=None, streams=32, device=None, drift_std=0.01,
-                 seed=0, max_slots=None):
+                 seed=0, max_slots=None, keep_completed=1 << 16):
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.opts = opts or P.SolverOptions()
         self.n_max = int(n_max)
@@ -99,7 +100,7 @@ class MPCServer:
         self._t_arr = np.zeros(1 << 16)
         self._t_mod = np.zeros(1 << 16, dtype=np.int8)
         self._t_base = 0
-        self.completed = []
+        self.completed = collections.deque(maxlen=int(keep_completed))
         self._res = (_lib.Result * 4096)()
         self._res_np = np.frombuffer(self._res, dtype=np.dtype(
             {"names": ["ticket", "episode", "status", "u0", "kkt"],

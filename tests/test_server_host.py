@@ -65,3 +65,4 @@ def test_a_burst_larger_than_the_arrays_grows_them():
     a, m = s._arrivals(tk)
     assert np.array_equal(a, tk * 0.5) and np.array_equal(m, tk % 2)
     assert s._t_arr.shape[0] >= 100
+
