@@ -83,6 +83,21 @@ def weights_diagonal(W, batch=None):
     return w
 
 
+def check_shapes(desc, n_max, batch, **arrays):
+    """Raise ValueError unless every given array has the shape the kernels
+    index it with ([batch, ...], padded to n_max): the device reads these
+    buffers without bounds of its own, so a short one would be read past its
+    end.  (A check that python -O cannot strip.)"""
+    N, n, m = n_max, desc.n, desc.m
+    want = dict(x0=(batch, n), X0=(batch, N + 1, n), U0=(batch, N, m), V0=(batch, N + 1, n),
+                reference=(batch, N + 1, desc.ref_cols), parameter=(batch, N + 1, desc.par_cols), w=(batch, NW),
+                horizon=(batch,))
+    for name, a in arrays.items():
+        if a is not None and tuple(a.shape) != want[name]:
+            raise ValueError("%s has shape %s; the solve needs %s (batch %d, padded to n_max = %d)"
+                             % (name, tuple(a.shape), want[name], batch, N))
+
+
 class Solver:
     """One libmpxg handle (fixed model, n_max and batch_max)."""
 
@@ -176,11 +191,8 @@ class Solver:
         w = self._dev(weights_diagonal(torch.as_tensor(W), B)).contiguous()
         if horizon is not None:
             horizon = self._dev(horizon, torch.int32)
-        N = self.n_max
-        n, m = self.desc.n, self.desc.m
-        assert X0.shape == (B, N + 1, n) and V0.shape == (B, N + 1, n) and U0.shape == (B, N, m), \
-            "warm start must be padded to n_max=%d" % N
-        assert reference.shape == (B, N + 1, self.desc.ref_cols) and parameter.shape == (B, N + 1, self.desc.par_cols)
+        check_shapes(self.desc, self.n_max, B, x0=x0, X0=X0, U0=U0, V0=V0, reference=reference, parameter=parameter,
+                     w=w, horizon=horizon)
         return x0, X0, U0, V0, reference, parameter, w, horizon
 
     def solve(self, x0, X0, U0, V0, reference, parameter, W, horizon=None, stream=None, plain=False, out=None,

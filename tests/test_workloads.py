@@ -95,3 +95,25 @@ def test_large_lq():
     assert np.all(d["R"] == 1e-3 * np.eye(30))
     assert np.abs(np.linalg.eigvals(d["A"])).max() <= 1.01 + 1e-9
     assert abs(d["B"].std() - np.sqrt(0.1 / 30)) < 0.003
+
+
+def test_solver_shape_check_accepts_the_workloads_and_names_a_short_buffer():
+    """Solver.prepare's check (raised, not asserted) passes every workload
+    as built and rejects a buffer shorter than the kernels index."""
+    import pytest
+    import torch
+    from mpx_gb300.solver import check_shapes, weights_diagonal
+    for wl in (P.quadruped_workload(6, horizons=(10, 20), seed=1, model=P.MODEL_SRBD_RPY12),
+               P.quadruped_workload(3, horizons=(15,), seed=2, model=P.MODEL_SRBD_QUAT13),
+               P.biped_workload(4, horizons=(12, 30), seed=3)):
+        B = wl.batch
+        arrays = dict(x0=wl.x0, X0=wl.X0, U0=wl.U0, V0=wl.V0, reference=wl.reference, parameter=wl.parameter,
+                      w=weights_diagonal(torch.as_tensor(wl.W), B), horizon=wl.horizon)
+        check_shapes(wl.desc, wl.n_max, B, **arrays)
+        for name in arrays:
+            short = dict(arrays)
+            short[name] = np.asarray(arrays[name])[:B - 1]
+            with pytest.raises(ValueError, match=name):
+                check_shapes(wl.desc, wl.n_max, B, **short)
+        with pytest.raises(ValueError, match="X0"):
+            check_shapes(wl.desc, wl.n_max + 1, B, X0=wl.X0)
