@@ -208,3 +208,33 @@ def test_python_binding_matches_every_declared_signature():
             assert f.restype is ctypes.c_size_t, name
         if ret.endswith("*") and "char" in ret:
             assert f.restype is ctypes.c_char_p, name
+
+
+def test_no_cpu_fallback():
+    """Without a GPU the product path refuses to run rather than computing
+    on the CPU: the Python solver raises, and the C ABI returns a CUDA error
+    status from mpxg_create (no handle); a missing library raises on load."""
+    import pytest
+    import torch
+    from mpx_gb300 import _lib, problem as P
+    from mpx_gb300.solver import Solver, problem_desc, solver_opts
+    if torch.cuda.is_available():
+        pytest.skip("this machine has a GPU")
+    desc = P.quadruped_rpy12()
+    with pytest.raises(_lib.MpxgError, match="no CPU path"):
+        Solver(desc, P.SolverOptions(), n_max=10, batch_max=2)
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    pd, po = problem_desc(desc, 10, 2), solver_opts(P.SolverOptions())
+    st = L.mpxg_create(ctypes.byref(pd), ctypes.byref(po), ctypes.byref(h))
+    assert st == 4 and not h.value  # MPXG_ERR_CUDA
+    assert b"cuda" in L.mpxg_last_error(None).lower()
+
+
+def test_missing_library_raises(monkeypatch, tmp_path):
+    import pytest
+    from mpx_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib._build, "LIB", str(tmp_path / "libmpxg.so"))
+    with pytest.raises(_lib.MpxgError, match="not built"):
+        _lib.load(build_if_missing=False)
