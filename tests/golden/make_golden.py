@@ -725,10 +725,19 @@ def main_wb(ref_root, out):
     print("wrote", out)
 
 
+# Where the reference checkout is read from unless given on the command line
+# or in MPX_REFERENCE.
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_root():
+    return os.environ.get("MPX_REFERENCE", DEFAULT_REFERENCE)
+
+
 if __name__ == "__main__":
     wb = "--wb" in sys.argv
     argv = [a for a in sys.argv[1:] if a != "--wb"]
-    ref_root = argv[0] if argv else os.environ.get("MPX_REFERENCE", "")
+    ref_root = argv[0] if argv else reference_root()
     out = argv[1] if len(argv) > 1 else os.path.join(HERE, "wb_golden.npz" if wb else "srbd_golden.npz")
     if not ref_root or not os.path.isdir(os.path.join(ref_root, "mpx")):
         sys.exit("usage: make_golden.py <reference checkout containing mpx/> [--wb] [out.npz]")
