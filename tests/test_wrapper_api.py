@@ -64,6 +64,11 @@ def test_mpx_data_record():
         pass
     else:
         raise AssertionError("a missing field must raise AttributeError")
+    # copies and pickles as a record of the same type
+    import copy
+    import pickle
+    for e2 in (copy.copy(e), copy.deepcopy(e), pickle.loads(pickle.dumps(e))):
+        assert isinstance(e2, wrappers.mpx_data) and e2.dt == 0.01 and torch.equal(e2.X0, e.X0)
 
 
 def _cpu_data_wrapper(B=3, N=5):
