@@ -47,6 +47,14 @@ def f_lqr(n, m):
 MODEL_FLOPS_RPY12 = 1449
 
 
+def status_bits(status):
+    """Instances with each per-instance status bit set (1 non-finite, 2
+    non-positive pivot, 4 line search at its smallest step, 8 bad horizon)."""
+    st = np.asarray(status).astype(np.int64)
+    return {name: int(((st & bit) != 0).sum())
+            for name, bit in (("nonfinite", 1), ("pivot", 2), ("line_search", 4), ("bad_horizon", 8))}
+
+
 def algorithmic_bytes(n, m, horizon, ref_cols, par_cols):
     """Compulsory HBM bytes of one batched solve: inputs x0, X0, U0, V0,
     reference, parameter, w; outputs X, U, V, kkt, status (float32/int32)."""
@@ -517,7 +525,8 @@ def run_ours(args, rank, world, local_rank):
         "plain": plain,
         "batched_vs_plain": (value / world) / plain["solves_per_s"] if plain else None,
         "kkt": {"median": float(np.median(kkt)), "p99": float(np.percentile(kkt, 99)),
-                "frac_le_1e-5": float((kkt <= 1e-5).mean()), "status_nonzero": int((status != 0).sum())},
+                "frac_le_1e-5": float((kkt <= 1e-5).mean()), "status_nonzero": int((status != 0).sum()),
+                "status_bits": status_bits(status)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "sqp_kernel<ModelRpy12>",
                      "solve_ms": solve_avg, "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},

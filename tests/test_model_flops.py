@@ -53,3 +53,13 @@ def test_count_properties():
     assert all(len(v) == 1 for v in by_contact.values())
     legs = {sum(k): next(iter(v))[3] for k, v in by_contact.items()}
     assert len(legs) >= 2 and all(legs[a] < legs[b] for a in legs for b in legs if a < b)
+
+
+def test_status_bits_counts_each_flag_of_the_header():
+    """The bench line's status_bits counts instances per MPXG_INST_* bit
+    (include/mpxg.h: 1 non-finite, 2 non-positive pivot, 4 line search at
+    its smallest step, 8 bad horizon)."""
+    st = np.array([0, 1, 2, 3, 4, 12, 0, 8], dtype=np.int32)
+    assert bench.status_bits(st) == {"nonfinite": 2, "pivot": 2, "line_search": 2, "bad_horizon": 2}
+    assert bench.status_bits(np.zeros(5, dtype=np.int32)) == {"nonfinite": 0, "pivot": 0, "line_search": 0,
+                                                               "bad_horizon": 0}
