@@ -1,4 +1,4 @@
-"""The model-FLOP figure of the roofline (CPU).
+"""The model-FLOP figure of the roofline and the bench line's status counts (CPU).
 
 The bench's FP32 work per stage and SQP iteration is the work-efficient
 Riccati count plus the model work of the stage, counted by running the
