@@ -75,6 +75,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream section")
     ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
+    ap.add_argument("--no-dropin", action="store_true", help="skip the drop-in wrapper end-to-end section")
     ap.add_argument("--no-autotune", action="store_true", help="use the default launch geometry")
     ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq", "wb"],
                     help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve; lqr_eq: the "
@@ -142,38 +143,59 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU (oracle) timing
-def cpu_solves_per_s(wl, sample, threads):
-    """Time the oracle's FP32 SQP (5 iterations) on `sample` instances of tick 0."""
-    from oracle import oracle as O
-    from mpx_gb300 import problem as P
-    idx = np.arange(min(sample, wl.batch))
-    opts = P.SolverOptions(sqp_iters=SQP_ITERS)
-    t0 = time.perf_counter()
-    O.sqp_solve(wl.desc, opts, wl.x0[idx], wl.X0[idx], wl.U0[idx], wl.V0[idx], wl.reference[idx],
-                wl.parameter[idx], wl.W[idx], wl.horizon[idx], precision=32, n_threads=threads, want_kkt=False)
-    dt = time.perf_counter() - t0
-    return len(idx) / dt, dt
+class CpuTicks:
+    """The oracle port ticking a sample of the batch the way the GPU arm ticks
+    the whole batch: warm-start shift, x0 <- the shifted X[0] (no drift), gait
+    timers advanced one tick, tables rebuilt, FP32 SQP solve (5 iterations)
+    with OpenMP over instances.  Tick 0 is the cold start."""
 
+    def __init__(self, wl, idx, threads):
+        from mpx_gb300 import problem as P
+        self.P = P
+        self.wl = _subset(wl, idx)
+        self.threads = threads
+        w = self.wl
+        self.x0, self.X, self.U, self.V = w.x0.copy(), w.X0.copy(), w.U0.copy(), w.V0.copy()
+        self.ref, self.par, self.lt = w.reference, w.parameter, w.leg_time.copy()
+        self.ticks = 0
 
-def cpu_bounded(wl, threads, seconds):
-    """Oracle solves/s over a bounded sample: the batch is solved in chunks
-    of 512 instances, cycling through it, until `seconds` have elapsed."""
-    done, tot, i = 0, 0.0, 0
-    cpu_solves_per_s(wl, 32, threads)  # warm-up (thread pool, pages)
-    while tot < seconds:
-        idx = np.arange(i, i + 512) % wl.batch
-        sub = _subset(wl, idx)
-        _, dt = cpu_solves_per_s(sub, len(idx), threads)
-        tot += dt
-        done += len(idx)
-        i = (i + 512) % wl.batch
-    return done / tot, tot, done
+    def tick(self):
+        """One control tick of the sample; returns its wall time in s."""
+        from oracle import oracle as O
+        P, w = self.P, self.wl
+        t0 = time.perf_counter()
+        if self.ticks > 0:
+            self.X, self.U, self.V = P.shift_warm_start(self.X, self.U, self.V, w.horizon)
+            _, self.lt = P.timer_run_np(w.duty, w.step_freq, self.lt, w.desc.dt)
+            self.x0 = self.X[:, 0].astype(np.float32)
+            self.ref, self.par = P.quadruped_tables(w.desc, self.x0, self.lt, w.v_ref, w.horizon, w.n_max,
+                                                    duty=w.duty, step_freq=w.step_freq, height=w.height)
+        out = O.sqp_solve(w.desc, P.SolverOptions(sqp_iters=SQP_ITERS), self.x0, self.X, self.U, self.V, self.ref,
+                          self.par, w.W, w.horizon, precision=32, n_threads=self.threads, want_kkt=False)
+        self.X, self.U, self.V = (out[k].astype(np.float32) for k in ("X", "U", "V"))
+        self.ticks += 1
+        return time.perf_counter() - t0
 
 
 def _subset(wl, idx):
     from mpx_gb300 import problem as P
     return P.Workload(wl.desc, wl.x0[idx], wl.X0[idx], wl.U0[idx], wl.V0[idx], wl.reference[idx], wl.parameter[idx],
-                      wl.W[idx], wl.horizon[idx], leg_time=wl.leg_time[idx], v_ref=wl.v_ref[idx])
+                      wl.W[idx], wl.horizon[idx], leg_time=wl.leg_time[idx], v_ref=wl.v_ref[idx], duty=wl.duty,
+                      step_freq=wl.step_freq, height=wl.height)
+
+
+def cpu_warm_ticks(wl, threads, seconds, sample=512, warm=3):
+    """Oracle solves/s of warm-started steady-state ticks: `sample` instances
+    of the batch are ticked `warm` times untimed (cold start first), then
+    timed tick after tick until `seconds` have elapsed."""
+    ct = CpuTicks(wl, np.arange(min(sample, wl.batch)), threads)
+    for _ in range(warm):
+        ct.tick()
+    tot, done = 0.0, 0
+    while tot < seconds:
+        tot += ct.tick()
+        done += ct.wl.batch
+    return done / tot, tot, done
 
 
 def host_info():
@@ -190,22 +212,19 @@ def host_info():
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the oracle (CPU restatement of the path) on host cores."""
+    """--impl reference: the oracle (CPU restatement of the path) on host
+    cores, ticking a sample of the same workload warm as the GPU arm does."""
     from mpx_gb300 import problem as P
-    from oracle import oracle as O
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     wl = P.quadruped_workload(args.batch, horizons=HORIZONS, seed=SEED, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
                               random_phase=True)
     sample = min(args.cpu_sample, args.batch)
-    for _ in range(max(args.warmup, 0)):
-        cpu_solves_per_s(wl, min(sample, 64), threads)
-    times = []
-    for k in range(args.steps):  # step k solves the next `sample` instances of the batch
-        idx = (np.arange(sample) + k * sample) % wl.batch
-        _, dt = cpu_solves_per_s(_subset(wl, idx), sample, threads)
-        times.append(dt)
+    ct = CpuTicks(wl, np.arange(sample), threads)
+    for _ in range(max(args.warmup, 3)):  # cold start, then warm ticks
+        ct.tick()
+    times = [ct.tick() for _ in range(args.steps)]
     tot = sum(times)
     value = sample * args.steps / tot
     line = {
@@ -215,11 +234,165 @@ def run_reference(args, rank, world):
         "dtype": "fp32", "data": "synthetic (seeded)", "impl": "reference",
         "config": config_dict(args.batch),
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": "%d instances of the tick-0 batch per step, 5 SQP iterations, FP32 oracle (C++), "
-                                   "OpenMP over instances" % sample, "host": host_info()},
+                         "sample": "the first %d instances of the batch ticked warm (shift, timers, tables, FP32 "
+                                   "SQP of 5 iterations; %d untimed ticks from the cold start first), one tick per "
+                                   "step; FP32 oracle (C++), OpenMP over instances" % (sample, max(args.warmup, 3)),
+                         "host": host_info()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _rel_errors(a, o, horizon):
+    """Max |a - o| over each instance's valid rows of X, U, V, K, k, relative to
+    max |o| (k relative to max |U|: the feedforward tends to 0 at convergence)."""
+    out = {}
+    for key in ("X", "U", "V", "K", "k"):
+        rows = (lambda N: N + 1) if key in ("X", "V") else (lambda N: N)
+        err = max(float(np.abs(a[key][i, :rows(N)] - o[key][i, :rows(N)]).max()) for i, N in enumerate(horizon))
+        ref = "U" if key == "k" else key
+        scale = max(float(np.abs(o[ref][i, :rows(N)]).max()) for i, N in enumerate(horizon))
+        out[key] = err / max(scale, 1e-30)
+    return out
+
+
+def fp64_error(tr, opts, stream, sample=64):
+    """Error of one steady-state tick of the benchmarked batch against the FP64
+    oracle on the same inputs, for `sample` instances drawn from the batch; the
+    oracle's own FP32 run on those inputs gives float32's floor.  The tick's
+    solution is kept as the batch's state."""
+    import torch
+    from oracle import oracle as O
+    with torch.cuda.stream(stream):
+        tr.shift(stream)
+        tr.tables(stream)
+    torch.cuda.synchronize()
+    idx = np.sort(np.random.default_rng(11).choice(tr.wl.batch, size=min(sample, tr.wl.batch), replace=False))
+    ins = {k: getattr(tr, k)[idx].cpu().numpy() for k in ("x0", "X", "U", "V", "ref", "par", "w", "horizon")}
+    with torch.cuda.stream(stream):
+        out = tr.solver.solve(tr.x0, tr.X, tr.U, tr.V, tr.ref, tr.par, tr.w, tr.horizon, stream=stream,
+                              want_gains=True)
+        for k in ("X", "U", "V"):
+            tr.out[k].copy_(out[k])
+    torch.cuda.synchronize()
+    g = {k: out[k][idx].cpu().numpy() for k in ("X", "U", "V", "K", "k")}
+    W = np.stack([np.diag(w) for w in ins["w"]])
+    a = (tr.desc, opts, ins["x0"], ins["X"], ins["U"], ins["V"], ins["ref"], ins["par"], W, ins["horizon"])
+    o = O.sqp_solve(*a)
+    o32 = O.sqp_solve(*a, precision=32)
+    kg = O.kkt_residual(tr.desc, ins["x0"], g["X"], g["U"], g["V"], ins["ref"], ins["par"], W, ins["horizon"])
+    return {"sample": int(len(idx)), "gpu_vs_fp64": _rel_errors(g, o, ins["horizon"]),
+            "oracle_fp32_vs_fp64": _rel_errors(o32, o, ins["horizon"]),
+            "kkt_fp64_eval": {"gpu_max": float(kg[:, 2].max()), "oracle_fp64_max": float(o["kkt"][:, 2].max())},
+            "what": "one warm tick of the benchmarked batch re-solved with gains; max |gpu - fp64| over each "
+                    "instance's valid rows, relative to max |fp64| (k relative to max |U|), over %d sampled "
+                    "instances" % len(idx)}
+
+
+def dropin_wrapper(dev, steps, warmup, n_env=BATCH):
+    """End to end through the drop-in API: BatchedMPCControllerWrapper.run (the
+    interface of mpx/utils/mpc_wrapper_srbd.py:91-141) on the reference's SRBD
+    model and config (quaternion state, N = 25, the reference's barrier) for
+    n_env environments.  Every tick passes host numpy arrays in (x0, input,
+    foot_op, contact) and reads the first controls back, plus the plan's next
+    state, foot references and contact flags, which stand in for the
+    simulator's measurements at the next tick."""
+    import torch
+    from mpx_gb300 import configs
+    from mpx_gb300.wrappers import BatchedMPCControllerWrapper
+    cfg = configs.srbd_quadruped()
+    w = BatchedMPCControllerWrapper(cfg, n_env, device=dev)
+    rng = np.random.default_rng(5)
+    x0 = np.tile(w.initial_state, (n_env, 1)).astype(np.float32)
+    x0[:, :3] += rng.normal(0.0, 0.01, (n_env, 3)).astype(np.float32)
+    inp = np.zeros((n_env, 7), dtype=np.float32)
+    inp[:, 0] = rng.uniform(-0.5, 0.5, n_env)
+    inp[:, 6] = cfg.robot_height
+    foot = (np.tile(cfg.p_legs0, (n_env, 1)) + np.tile(x0[:, :3], (1, 4)) * np.array([1, 1, 0] * 4)).astype(np.float32)
+    contact = np.ones((n_env, 4), dtype=np.float32)
+    state = {"x0": x0, "foot": foot, "contact": contact}
+
+    def tick():
+        w.run(state["x0"], inp, state["foot"], state["contact"])
+        grf = w.grf.cpu().numpy()
+        state["x0"] = w.X[:, 1].cpu().numpy()
+        state["foot"] = w.foot_ref.cpu().numpy()
+        state["contact"] = w.contact.cpu().numpy().astype(np.float32)
+        return grf
+
+    for _ in range(max(warmup, 3)):
+        tick()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        tick()
+    wall = time.perf_counter() - t0
+    kkt = w.kkt[:, 2].cpu().numpy()
+    res = {"value": n_env * steps / wall, "unit": "solves/s", "ms_per_tick": 1e3 * wall / steps,
+           "h2d_bytes_per_step": n_env * (13 + 7 + 12 + 4) * 4, "d2h_bytes_per_step": n_env * (12 + 13 + 12 + 4) * 4,
+           "kkt_frac_le_1e-5": float((kkt <= 1e-5).mean()), "kkt_median": float(np.median(kkt)),
+           "what": "%d environments through BatchedMPCControllerWrapper.run with host numpy arrays every tick "
+                   "(timer, reference generator, solve, shift: 4 launches), host wall clock; model SRBD_QUAT13 "
+                   "with the reference's barrier, config mpx/config/config_srbd.py (N = 25)" % n_env}
+    w.solver.close()
+    return res
+
+
+def _served_entry(srv, lat, wall, offered):
+    sk = srv.last_kkt
+    return {"offered_req_per_s": offered, "completed_req_per_s": len(lat) / wall, "requests": int(len(lat)),
+            "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)), "p99": 1e3 * float(np.percentile(lat, 99))},
+            "kkt_frac_le_1e-5": float((sk <= 1e-5).mean()),
+            "nan_status": int(((srv.last_status & 1) != 0).sum())}
+
+
+def run_served(dev, opts):
+    """Served request streams (continuous batching).  Latency is submit to
+    result row on the host, with real-time Poisson arrivals; every measured
+    window continues episodes that were already running, so it sees the
+    stream's steady state rather than a cold start of every episode."""
+    from mpx_gb300.server import EpisodeStream, MPCServer, default_models, served_workload
+    out = {}
+    # config 3: the mixed stream, 200-tick episodes with state drift
+    srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
+                    device=dev)
+    es = EpisodeStream(srv, seed=1)
+    launches0 = None
+    served_workload(srv, 400, 20000.0, 0.5, seed=1, stream=es, stagger=True)
+    launches0 = srv.launches
+    lat, wall = served_workload(srv, 400, 20000.0, 2.0, seed=2, stream=es, stagger=True)
+    e = _served_entry(srv, lat, wall, 20000.0)
+    e["kkt_frac_le_1e-5_by_model"] = {name: float((srv.last_kkt[srv.last_model == i] <= 1e-5).mean())
+                                      for i, name in enumerate(srv.model_names) if (srv.last_model == i).any()}
+    e["gpu_launches"] = srv.launches - launches0
+    e["workload"] = ("Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, alternating), "
+                     "N uniform in [20, 200], 200-tick episodes at staggered ages (ended episodes are replaced by "
+                     "cold ones), state drift N(0, 0.01^2) per tick, 8 GB admission budget, 32 streams; 0.5 s "
+                     "warm-up of the same episodes, then 2 s measured")
+    out.update(e)
+    es.close()
+    srv.close()
+    # the latency target's case: 4096 robots (N = 50 quadruped episodes that keep running) at rising rates
+    for drift, key in ((0.0, "envs4096_n50"), (0.01, "envs4096_n50_drift")):
+        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=drift, streams=32,
+                        device=dev)
+        es = EpisodeStream(srv, seed=3)
+        kw = dict(horizon_range=(50, 50), models=("quadruped",), episode_ticks=1 << 30, stream=es)
+        served_workload(srv, 4096, 300000.0, 4096 * 10 / 300000.0, seed=3, **kw)  # ~10 ticks per robot first
+        sweep = []
+        for rate in ((50000.0, 150000.0, 300000.0) if drift == 0.0 else (150000.0,)):
+            served_workload(srv, 4096, rate, 0.2, seed=4, **kw)
+            l4, w4 = served_workload(srv, 4096, rate, 1.0, seed=5, **kw)
+            sweep.append(_served_entry(srv, l4, w4, rate))
+        out[key] = {"sweep": sweep,
+                    "workload": "4096 concurrent quadruped SRBD episodes, N = 50, 5 SQP iterations, %s; each tick "
+                                "x0 <- X[1] of the shifted warm start%s; 32 streams; ~10 ticks per robot before the "
+                                "first window, 0.2 s warm-up per rate, 1 s measured" %
+                                ("no drift" if drift == 0.0 else "drift N(0, 0.01^2)",
+                                 "" if drift == 0.0 else " + drift")}
+        es.close()
+        srv.close()
+    return out
 
 
 def config_dict(batch):
@@ -305,6 +478,9 @@ def run_ours(args, rank, world, local_rank):
     solve_avg = sum(solve_ms) / len(solve_ms)
     kkt = tr.out["kkt"][:, 2].float().cpu().numpy()
     status = tr.out["status"].cpu().numpy()
+
+    # ---------------- the batch's error against the FP64 oracle (64 sampled instances)
+    fp64 = fp64_error(tr, opts, stream) if (not args.profile and rank == 0) else None
 
     # ---------------- end to end through the public API with host buffers
     x0_host = torch.empty(B, n, pin_memory=True)
@@ -432,67 +608,27 @@ def run_ours(args, rank, world, local_rank):
     # ---------------- served request stream (continuous batching), rank 0
     served = None
     if not args.no_served and not args.profile and rank == 0:
-        from mpx_gb300.server import MPCServer, default_models, served_workload
-        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
-                        device=dev)
-        served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, seed=1)  # warm-up
-        launches0 = srv.launches
-        lat, wall = served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=2.0, seed=2)
-        sk, sst = srv.last_kkt, srv.last_status
-        served = {"offered_req_per_s": 20000.0, "completed_req_per_s": len(lat) / wall, "requests": int(len(lat)),
-                  "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
-                                 "p99": 1e3 * float(np.percentile(lat, 99)),
-                                 "what": "submit to result row on the host, real-time Poisson arrivals"},
-                  "kkt_frac_le_1e-5": float((sk <= 1e-5).mean()), "nan_status": int(((sst & 1) != 0).sum()),
-                  "kkt_frac_le_1e-5_by_model": {name: float((sk[srv.last_model == i] <= 1e-5).mean())
-                                                for i, name in enumerate(srv.model_names)
-                                                if (srv.last_model == i).any()},
-                  "gpu_launches": srv.launches - launches0,
-                  "workload": "Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, "
-                              "alternating), N uniform in [20, 200], 200-tick episodes, state drift N(0, 0.01^2), "
-                              "8 GB admission budget, 32 streams"}
-        # the same stream with every episode a quadruped at N = 50 (the latency target's case)
-        srv.close()
-        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
-                        device=dev)
-        served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=0.3, horizon_range=(50, 50), seed=1,
-                        models=("quadruped",))
-        lat50, wall50 = served_workload(srv, n_episodes=400, rate_hz=20000.0, duration_s=2.0, horizon_range=(50, 50),
-                                        seed=2, models=("quadruped",))
-        served["n50_quadruped"] = {"completed_req_per_s": len(lat50) / wall50,
-                                   "latency_ms": {"p50": 1e3 * float(np.percentile(lat50, 50)),
-                                                  "p99": 1e3 * float(np.percentile(lat50, 99))}}
-        srv.close()
-        # 4096 concurrent N = 50 quadruped episodes served at rising request rates
-        srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
-                        device=dev)
-        sweep = []
-        for rate in (50000.0, 150000.0, 300000.0):
-            served_workload(srv, n_episodes=4096, rate_hz=rate, duration_s=0.2, horizon_range=(50, 50), seed=3,
-                            models=("quadruped",))
-            l4, w4 = served_workload(srv, n_episodes=4096, rate_hz=rate, duration_s=1.0, horizon_range=(50, 50),
-                                     seed=4, models=("quadruped",))
-            sweep.append({"offered_req_per_s": rate, "completed_req_per_s": len(l4) / w4,
-                          "latency_ms": {"p50": 1e3 * float(np.percentile(l4, 50)),
-                                         "p99": 1e3 * float(np.percentile(l4, 99))},
-                          "kkt_frac_le_1e-5": float((srv.last_kkt <= 1e-5).mean())})
-        served["envs4096_n50"] = sweep
-        srv.close()
-        del srv
+        served = run_served(dev, opts)
+
+    # ---------------- end to end through the drop-in wrapper API (reference model and config)
+    dropin = None
+    if not args.profile and rank == 0 and not args.no_dropin:
+        dropin = dropin_wrapper(dev, min(args.steps, 20), args.warmup)
 
     # ---------------- CPU baseline (oracle, rank 0)
     cpu = None
     if rank == 0 and not args.no_cpu and not args.profile:
         threads = os.cpu_count() or 1
-        v, dt, done = cpu_bounded(wl, threads, args.cpu_seconds)
+        v, dt, done = cpu_warm_ticks(wl, threads, args.cpu_seconds, sample=min(1024, B))
         cpu = {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": "%d solves (the %d-instance tick-0 batch, repeated) in %.1f s: 5 SQP iterations, FP32 "
-                         "oracle (C++, -O3), OpenMP over instances" % (done, B, dt),
+               "sample": "%d solves in %.1f s: the first %d instances of the batch ticked warm (shift, timers, "
+                         "tables, 5 SQP iterations) after 3 untimed ticks from the cold start; FP32 oracle (C++, "
+                         "-O3), OpenMP over instances" % (done, dt, min(1024, B)),
                "host": host_info()}
         # secondary figure: the same port on one thread
-        v1, dt1, done1 = cpu_bounded(wl, 1, 3.0)
+        v1, dt1, done1 = cpu_warm_ticks(wl, 1, 3.0, sample=64)
         cpu["single_thread"] = {"value": v1, "unit": "solves/s", "cores": 1,
-                                "sample": "%d solves in %.1f s, one thread" % (done1, dt1)}
+                                "sample": "%d solves in %.1f s (64 instances ticked warm), one thread" % (done1, dt1)}
 
     # ---------------- roofline of the solve kernel
     import json as _json
@@ -537,6 +673,8 @@ def run_ours(args, rank, world, local_rank):
                  "achieved_tflops_with_model": (flops + model_flops) / (solve_avg / 1000.0) / 1e12,
                  "frac_with_model": (flops + model_flops) / (solve_avg / 1000.0) / 1e12 / fp32_nominal},
         "n50": n50,
+        "fp64_error": fp64,
+        "e2e_dropin": dropin,
         "vjp": vjp,
         "served": served,
         "cpu_baseline": cpu,

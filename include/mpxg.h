@@ -86,6 +86,9 @@ typedef struct {
   float barrier_hess_scale;
   float inertia[9];    /* row-major */
   float inertia_inv[9];
+  float cone_eps2;     /* smoothing of the friction cone's tangential norm,
+                          c = mu fz - sqrt(fx^2 + fy^2 + cone_eps2) (N^2); 0 selects
+                          the reference's 1e-2 (objectives.py:29) */
 } mpxg_problem_desc;
 
 /* SQP settings (the reference's solver constants are not in its tree). */
@@ -216,14 +219,22 @@ typedef struct {
  * jax.jit(jax.vmap(optimizers.mpc ...)) (mpx/utils/mpc_wrapper_srbd.py:68,77).
  * buffers: reference, parameter, w (the diagonal [B,24] of W), x0, X0, U0, V0,
  * then the results X, U, V, in the reference's argument order.  All horizons
- * are desc.n_max.  A handle per (device, opaque) is created on first use and
- * kept.  Errors go to XlaCustomCallStatusSetFailure when the host process
+ * are desc.n_max.  The call allocates nothing: it uses the handle that
+ * mpxg_xla_prepare made for (current device, opaque), and fails when there is
+ * none.  Errors go to XlaCustomCallStatusSetFailure when the host process
  * exports it, and to mpxg_last_error(NULL). */
 void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status);
+/* Creates (once) the handle of (current device, opaque) that the XLA targets
+ * use, so that device memory is allocated when the program is built rather
+ * than inside the custom call (where XLA may be capturing a command buffer).
+ * Replaces the one-time jit compilation of the solve,
+ * jax.jit(jax.vmap(partial(optimizers.mpc, ...))) (mpx/utils/mpc_wrapper_srbd.py:68,77).
+ * Call it with each device the program runs on current. */
+mpxg_status mpxg_xla_prepare(const char* opaque, size_t opaque_len);
 /* XLA custom-call target of the backward pass (mpxg_solve_vjp): buffers
  * reference, parameter, w, x0, X, U, V (the solution), gX, gU (cotangents),
- * then the results gx0 [B,n] and gref [B,N+1,12].  Same opaque and handle
- * cache as mpxg_xla_solve. */
+ * then the results gx0 [B,n] and gref [B,N+1,12].  Same opaque and prepared
+ * handle as mpxg_xla_solve. */
 void mpxg_xla_solve_vjp(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status);
 
 mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_factor, float step_freq, float dt,
@@ -326,8 +337,10 @@ mpxg_status mpxg_lqr_eq_solve_method(void* stream, const mpxg_lq_eq_io* io, int 
  * 152-SM GB300 n_max up to 141 for the roll-pitch-yaw quadruped, 135 for the
  * biped, 116 for the quaternion model).  All calls share that array: calls
  * that overlap on the GPU race, so serialise them on one stream.  The first call on a device looks up the
- * array's device address; make it before any stream capture.  Errors are
- * reported through mpxg_last_error(NULL). */
+ * array's device address; make it before any stream capture.  That address is
+ * kept for the life of the process, so after a cudaDeviceReset the entry point
+ * must not be called again in that process.  warps_per_block is 0..4, as for
+ * mpxg_create.  Errors are reported through mpxg_last_error(NULL). */
 mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* desc, const mpxg_solver_opts* opts, void* stream,
                                const mpxg_batch_io* io);
 

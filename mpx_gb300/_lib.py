@@ -29,7 +29,7 @@ class ProblemDesc(ctypes.Structure):
                 ("foot_length", ctypes.c_float), ("foot_width", ctypes.c_float),
                 ("barrier_kind", ctypes.c_int), ("barrier_masked", ctypes.c_int),
                 ("barrier_hess_scale", ctypes.c_float),
-                ("inertia", ctypes.c_float * 9), ("inertia_inv", ctypes.c_float * 9)]
+                ("inertia", ctypes.c_float * 9), ("inertia_inv", ctypes.c_float * 9), ("cone_eps2", ctypes.c_float)]
 
 
 class SolverOpts(ctypes.Structure):
@@ -118,7 +118,7 @@ class WbModel(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_solve_vjp",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_xla_prepare", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
@@ -187,6 +187,8 @@ def load(build_if_missing=True):
     L.mpxg_xla_solve.restype = None
     L.mpxg_xla_solve_vjp.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve_vjp.restype = None
+    L.mpxg_xla_prepare.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.mpxg_xla_prepare.restype = ctypes.c_int
     L.mpxg_evaluate.argtypes = [vp, vp, ctypes.c_int] + [vp] * 9
     L.mpxg_evaluate.restype = ctypes.c_int
     L.mpxg_destroy.argtypes = [vp]

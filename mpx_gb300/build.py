@@ -1,9 +1,12 @@
 """Build recipe of libmpxg.so (the CUDA hot path and its C ABI).
 
-One translation unit, compiled for sm_103a only, in-tree into
-mpx_gb300/_build/libmpxg.so.  No torch headers are involved: the library is a
-plain C ABI over CUDA runtime calls, loaded with ctypes.
+Each translation unit under csrc/ (one per SQP model, the LQ solves, the
+whole-body kernels and the host ABI) is compiled for sm_103a only, in
+parallel, then linked in-tree into mpx_gb300/_build/libmpxg.so.  No torch
+headers are involved: the library is a plain C ABI over CUDA runtime calls,
+loaded with ctypes.
 """
+import concurrent.futures
 import os
 import shutil
 import subprocess
@@ -14,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmpxg.so")
-SOURCES = ["mpxg_abi.cu"]
+SOURCES = ["mpxg_abi.cu", "sqp_rpy12.cu", "sqp_quat13.cu", "sqp_biped12.cu", "lqr.cu", "lqr_eq.cu", "wb.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -43,14 +46,29 @@ def build(force=False, verbose=False, extra_flags=()):
     if not force and not needs_build():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
-    tmp = LIB + ".tmp.%d" % os.getpid()
-    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
-           "-Xptxas", "-warn-spills", "-I", os.path.join(ROOT, "include"), "-o", tmp,
-           *[os.path.join(CSRC, s) for s in SOURCES], *extra_flags]
-    if verbose:
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
+    nvcc = _nvcc()
+    tag = "%d" % os.getpid()
+    common = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills",
+              "-I", os.path.join(ROOT, "include"), *extra_flags]
+
+    def compile_one(src):
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".%s.o" % tag)
+        cmd = common + ["-c", "-o", obj, os.path.join(CSRC, src)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+        return obj
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB + ".tmp." + tag
+    try:
+        subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs], check=True)
+        os.replace(tmp, LIB)
+    finally:
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
     return LIB
 
 

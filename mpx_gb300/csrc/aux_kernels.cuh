@@ -331,4 +331,52 @@ __global__ void gait_tables_kernel(mpxg_gait_args g, int nx, int nu, int legs, i
   }
 }
 
+// ------------------------------------------------------------ queue order
+// Counting sort of the batch entries by horizon, longest first, into order[]
+// (one block).  Entries with an invalid horizon go last.  Serving the
+// persistent grid's queue longest-first shortens the tail of a batch whose
+// horizons differ (list scheduling, longest processing time first).
+__global__ void __launch_bounds__(1024) order_by_horizon_kernel(int batch, int n_max, const int* __restrict__ slot,
+                                                                const int* __restrict__ horizon, int* __restrict__ order) {
+  extern __shared__ int bins[];       // n_max + 1 bins: bin j holds horizon n_max - j; bin n_max: invalid
+  __shared__ int warp_tot[32];
+  const int nb = n_max + 1;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) bins[j] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
+    const int h = horizon[slot ? slot[i] : i];
+    atomicAdd(&bins[(h >= 1 && h <= n_max) ? n_max - h : n_max], 1);
+  }
+  __syncthreads();
+  // exclusive scan of bins: each thread scans a contiguous chunk
+  const int chunk = (nb + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * chunk, hi = min(lo + chunk, nb);
+  int local = 0;
+  for (int j = lo; j < hi; ++j) local += bins[j];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += v;
+    }
+    warp_tot[lane] = t;  // inclusive over warps
+  }
+  __syncthreads();
+  int run = (wid > 0 ? warp_tot[wid - 1] : 0) + incl - local;
+  for (int j = lo; j < hi; ++j) { const int c = bins[j]; bins[j] = run; run += c; }
+  __syncthreads();
+  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
+    const int h = horizon[slot ? slot[i] : i];
+    order[atomicAdd(&bins[(h >= 1 && h <= n_max) ? n_max - h : n_max], 1)] = i;
+  }
+}
+
 }  // namespace mpxg

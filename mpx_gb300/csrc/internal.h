@@ -1,0 +1,57 @@
+// Declarations shared by the translation units of libmpxg.so (host code
+// only; never installed).  Each model's SQP kernels are compiled in a unit
+// of their own (sqp_<model>.cu) and reached through a table of launchers,
+// so that the units compile in parallel.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/mpxg.h"
+
+namespace mpxg {
+
+struct ModelConst;
+struct SqpParams;
+struct BatchPtrs;
+
+// Launchers of one compiled model's kernels.
+struct SqpOps {
+  size_t smem_per_warp;                         // dynamic shared memory per warp of the SQP kernels
+  long long (*scratch_floats)(int n_max);       // per-warp scratch of one solve
+  int (*resident_blocks)(int wpb, bool tput);   // blocks per SM of the latency / throughput variant
+  // persistent SQP launch (latency variant, or the throughput variant if tput)
+  cudaError_t (*launch)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks, int wpb,
+                        bool tput, cudaStream_t st);
+  cudaError_t (*launch_vjp)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks, int wpb,
+                            cudaStream_t st);
+  cudaError_t (*launch_evaluate)(const ModelConst& mc, int batch, int n_max, const int* horizon, const float* x0,
+                                 const float* X, const float* U, const float* reference, const float* parameter,
+                                 const float* w, float* g, float* c, cudaStream_t st);
+};
+
+const SqpOps& sqp_ops_quat13();
+const SqpOps& sqp_ops_rpy12();
+const SqpOps& sqp_ops_biped12();
+
+// The table of a model id (null for an unknown id).
+inline const SqpOps* sqp_ops(int model) {
+  switch (model) {
+    case MPXG_MODEL_SRBD_QUAT13: return &sqp_ops_quat13();
+    case MPXG_MODEL_SRBD_RPY12: return &sqp_ops_rpy12();
+    case MPXG_MODEL_BIPED_WRENCH12: return &sqp_ops_biped12();
+    default: return nullptr;
+  }
+}
+
+// The library's last error of this host thread (mpxg_last_error(NULL)).
+std::string& lib_error();
+inline mpxg_status lib_fail(mpxg_status st, const std::string& msg) {
+  lib_error() = msg;
+  return st;
+}
+inline mpxg_status lib_cuda_fail(cudaError_t e, const char* where) {
+  return lib_fail(MPXG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace mpxg

@@ -20,6 +20,7 @@ struct ModelConst {
   int barrier_kind, barrier_masked;
   float barrier_hess_scale;
   float I[9], Iinv[9];
+  float cone_eps2;                // smoothing of the cone's tangential norm (N^2)
 };
 
 // ------------------------------------------------------------ rigid body
@@ -234,10 +235,12 @@ __device__ __forceinline__ void barrier_terms(const ModelConst& mc, float c, flo
   }
 }
 
-// Friction cone c = mu fz - sqrt(fx^2 + fy^2 + 1e-2) (objectives.py:29,66):
-// value, gradient wrt (fx, fy, fz) and Hessian of the sqrt term (xy block).
-__device__ __forceinline__ float cone(float mu, const float* f, float* gc, float* hxx, float* hxy, float* hyy) {
-  const float s2 = f[0] * f[0] + f[1] * f[1] + 1e-2f;
+// Friction cone c = mu fz - sqrt(fx^2 + fy^2 + eps2) (objectives.py:29,66, where
+// eps2 = 1e-2): value, gradient wrt (fx, fy, fz) and Hessian of the sqrt term
+// (xy block).
+__device__ __forceinline__ float cone(float mu, float eps2, const float* f, float* gc, float* hxx, float* hxy,
+                                      float* hyy) {
+  const float s2 = f[0] * f[0] + f[1] * f[1] + eps2;
   const float s = sqrtf(s2);
   gc[0] = -f[0] / s; gc[1] = -f[1] / s; gc[2] = mu;
   const float s3 = s2 * s;
@@ -382,7 +385,7 @@ __device__ __forceinline__ float barrier_cost(const ModelConst& mc, const float*
       const float cont = ref[M::COFF + i];
       const float mcost = mc.barrier_masked ? cont : 1.0f;
       float gc[3], hxx, hxy, hyy;
-      const float c = cone(mc.mu, u + 3 * i, gc, &hxx, &hxy, &hyy);
+      const float c = cone(mc.mu, mc.cone_eps2, u + 3 * i, gc, &hxx, &hxy, &hyy);
       float v, g, h, cv;
       barrier_terms(mc, c, mcost, cont, &v, &g, &h, &cv);
       acc += v;
@@ -398,7 +401,7 @@ __device__ __forceinline__ float barrier_cost(const ModelConst& mc, const float*
       const float* T = u + 6 * i + 3;
       float gc[3], hxx, hxy, hyy;
       float cs[7];
-      cs[0] = cone(mc.mu, F, gc, &hxx, &hxy, &hyy);
+      cs[0] = cone(mc.mu, mc.cone_eps2, F, gc, &hxx, &hxy, &hyy);
       cs[1] = hl * F[2] - T[1]; cs[2] = hl * F[2] + T[1];
       cs[3] = hw * F[2] - T[0]; cs[4] = hw * F[2] + T[0];
       cs[5] = mz * F[2] - T[2]; cs[6] = mz * F[2] + T[2];
@@ -430,7 +433,7 @@ __device__ __forceinline__ void barrier_leg(const ModelConst& mc, int leg, const
   }
   if (LD == 3) {
     const float* f = u + 3 * leg;
-    const float c = cone(mc.mu, f, gc, &hxx, &hxy, &hyy);
+    const float c = cone(mc.mu, mc.cone_eps2, f, gc, &hxx, &hxy, &hyy);
     float v, g, h, cv;
     barrier_terms(mc, c, mcost, cont, &v, &g, &h, &cv);
     *val = v;
@@ -447,7 +450,7 @@ __device__ __forceinline__ void barrier_leg(const ModelConst& mc, int leg, const
     const float hl = 0.5f * mc.foot_length, hw = 0.5f * mc.foot_width;
     const float mz = mc.mu * 0.5f * fminf(mc.foot_length, mc.foot_width);
     float cs[7];
-    cs[0] = cone(mc.mu, F, gc, &hxx, &hxy, &hyy);
+    cs[0] = cone(mc.mu, mc.cone_eps2, F, gc, &hxx, &hxy, &hyy);
     cs[1] = hl * F[2] - T[1]; cs[2] = hl * F[2] + T[1];
     cs[3] = hw * F[2] - T[0]; cs[4] = hw * F[2] + T[0];
     cs[5] = mz * F[2] - T[2]; cs[6] = mz * F[2] + T[2];
@@ -528,12 +531,12 @@ __device__ __forceinline__ float barrier_diff(const ModelConst& mc, float c0, fl
   return 0.5f * mask * (barrier_q_diff(a, sg, c0, c1, dc) - a * log1pf(dc / c0));
 }
 
-// Friction cone c = mu fz - s, s = sqrt(fx^2 + fy^2 + 1e-2): value at f and
+// Friction cone c = mu fz - s, s = sqrt(fx^2 + fy^2 + eps2): value at f and
 // its change for the step df, with ds = d(s^2) / (s0 + s1).
-__device__ __forceinline__ float cone_diff(float mu, const float* f, const float* df, float* dc) {
-  const float s0 = sqrtf(f[0] * f[0] + f[1] * f[1] + 1e-2f);
+__device__ __forceinline__ float cone_diff(float mu, float eps2, const float* f, const float* df, float* dc) {
+  const float s0 = sqrtf(f[0] * f[0] + f[1] * f[1] + eps2);
   const float g0 = f[0] + df[0], g1 = f[1] + df[1];
-  const float s1 = sqrtf(g0 * g0 + g1 * g1 + 1e-2f);
+  const float s1 = sqrtf(g0 * g0 + g1 * g1 + eps2);
   const float ds = (df[0] * (2.0f * f[0] + df[0]) + df[1] * (2.0f * f[1] + df[1])) / (s0 + s1);
   *dc = mu * df[2] - ds;
   return mu * f[2] - s0;
@@ -549,7 +552,7 @@ __device__ __forceinline__ float barrier_cost_diff(const ModelConst& mc, const f
     for (int i = 0; i < 4; ++i) {
       const float mcost = mc.barrier_masked ? ref[M::COFF + i] : 1.0f;
       float dc;
-      const float c0 = cone_diff(mc.mu, u + 3 * i, du + 3 * i, &dc);
+      const float c0 = cone_diff(mc.mu, mc.cone_eps2, u + 3 * i, du + 3 * i, &dc);
       acc += barrier_diff(mc, c0, dc, mcost);
     }
   } else {
@@ -563,7 +566,7 @@ __device__ __forceinline__ float barrier_cost_diff(const ModelConst& mc, const f
       const float* dF = du + 6 * i;
       const float* dT = du + 6 * i + 3;
       float dc;
-      const float c0 = cone_diff(mc.mu, F, dF, &dc);
+      const float c0 = cone_diff(mc.mu, mc.cone_eps2, F, dF, &dc);
       acc += barrier_diff(mc, c0, dc, mcost);
       acc += barrier_diff(mc, hl * F[2] - T[1], hl * dF[2] - dT[1], mcost);
       acc += barrier_diff(mc, hl * F[2] + T[1], hl * dF[2] + dT[1], mcost);

@@ -1,5 +1,8 @@
-// C ABI of libmpxg.so (declared in include/mpxg.h): handle management and the
-// host side of every launch.  No torch types cross this boundary.
+// C ABI of libmpxg.so (declared in include/mpxg.h): handle management, the
+// host side of the SQP launches (kernels in sqp_<model>.cu), the per-tick
+// auxiliary kernels, the allocation-free solve, the XLA targets and the
+// serving runtime.  The LQ solves are in lqr.cu and lqr_eq.cu, the
+// whole-body kernels in wb.cu.  No torch types cross this boundary.
 #include <cuda_runtime.h>
 
 #include <dlfcn.h>
@@ -13,11 +16,8 @@
 
 #include "../../include/mpxg.h"
 #include "aux_kernels.cuh"
-#include "evaluate_kernel.cuh"
-#include "lqr_eq_tc.cuh"
-#include "lqr_kernels.cuh"
-#include "sqp_kernel.cuh"
-#include "wb_kernel.cuh"
+#include "internal.h"
+#include "sqp_kernel.cuh"  // the structs the launchers take; the kernels are compiled in sqp_<model>.cu
 
 using namespace mpxg;
 
@@ -48,6 +48,7 @@ struct mpxg_handle {
 };
 
 static thread_local std::string g_lib_err;
+std::string& mpxg::lib_error() { return g_lib_err; }
 
 static mpxg_status fail(mpxg_handle* h, mpxg_status st, const std::string& msg) {
   if (h) h->err = msg; else g_lib_err = msg;
@@ -56,9 +57,6 @@ static mpxg_status fail(mpxg_handle* h, mpxg_status st, const std::string& msg) 
 static mpxg_status cuda_fail(mpxg_handle* h, cudaError_t e, const char* where) {
   return fail(h, MPXG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
-
-template <class M>
-static size_t smem_per_warp() { return sizeof(WarpSmem<M>); }
 
 static bool model_dims(int model, int* nx, int* nu) {
   switch (model) {
@@ -69,70 +67,46 @@ static bool model_dims(int model, int* nx, int* nu) {
   }
 }
 
-template <class M>
-static int resident_blocks(int wpb, bool tput);
-
 // Scratch slots of a handle: the most warps of its kernel resident at once.
 static int scratch_slots(int model, int wpb, int num_sms) {
-  int rb = 1;
-  switch (model) {
-    case MPXG_MODEL_SRBD_QUAT13:
-      rb = std::max(resident_blocks<ModelQuat13>(wpb, true), resident_blocks<ModelQuat13>(wpb, false)); break;
-    case MPXG_MODEL_SRBD_RPY12:
-      rb = std::max(resident_blocks<ModelRpy12>(wpb, true), resident_blocks<ModelRpy12>(wpb, false)); break;
-    case MPXG_MODEL_BIPED_WRENCH12:
-      rb = std::max(resident_blocks<ModelBiped12>(wpb, true), resident_blocks<ModelBiped12>(wpb, false)); break;
-    default: break;
-  }
+  const SqpOps* ops = sqp_ops(model);
+  if (!ops) return 0;
+  const int rb = std::max(ops->resident_blocks(wpb, true), ops->resident_blocks(wpb, false));
   return num_sms * rb * wpb;
 }
 
 static long long scratch_stride_for(int model, int n_max) {
-  switch (model) {
-    case MPXG_MODEL_SRBD_QUAT13: return scratch_floats<ModelQuat13>(n_max);
-    case MPXG_MODEL_SRBD_RPY12: return scratch_floats<ModelRpy12>(n_max);
-    case MPXG_MODEL_BIPED_WRENCH12: return scratch_floats<ModelBiped12>(n_max);
-    default: return 0;
-  }
+  const SqpOps* ops = sqp_ops(model);
+  return ops ? ops->scratch_floats(n_max) : 0;
 }
 
-// The kernel of a variant; models whose two register budgets coincide use one
-// kernel for both (one instantiation less to compile).
-template <class M>
-static void (*sqp_kernel_for(bool tput))(ModelConst, SqpParams, BatchPtrs) {
-  if constexpr (SqpMinBlocks<M>::value != MPXG_SQP_MIN_BLOCKS) {
-    if (tput) return sqp_kernel_tput<M>;
-  }
-  return sqp_kernel<M>;
-}
-
-template <class M>
-static int resident_blocks(int wpb, bool tput) {
-  int nb = 0;
-  const size_t smem = sizeof(WarpSmem<M>) * (size_t)wpb;
-  auto fn = sqp_kernel_for<M>(tput);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, wpb * 32, smem) != cudaSuccess) return 1;
-  return nb > 0 ? nb : 1;
+// Kernel constants of a model description.
+static ModelConst model_const(const mpxg_problem_desc* d) {
+  ModelConst mc;
+  mc.dt = d->dt; mc.mass = d->mass; mc.inv_mass = 1.0f / d->mass; mc.gravity = d->gravity; mc.mu = d->mu;
+  mc.alpha = d->barrier_alpha; mc.sigma = d->barrier_sigma;
+  mc.foot_length = d->foot_length; mc.foot_width = d->foot_width;
+  mc.barrier_kind = d->barrier_kind; mc.barrier_masked = d->barrier_masked;
+  mc.barrier_hess_scale = d->barrier_hess_scale;
+  for (int i = 0; i < 9; ++i) { mc.I[i] = d->inertia[i]; mc.Iinv[i] = d->inertia_inv[i]; }
+  mc.cone_eps2 = d->cone_eps2 > 0.0f ? d->cone_eps2 : 1e-2f;
+  return mc;
 }
 
 // Persistent grid: warps_per_block warps per block and as many blocks per SM
 // as stay resident (one instance per warp at a time), for the throughput
 // variant (*bps) and the latency variant (*bps_lat).
-static void launch_geometry(const mpxg_problem_desc* d, const mpxg_solver_opts* o, int num_sms, int* wpb, int* bps,
+static void launch_geometry(const mpxg_problem_desc* d, const mpxg_solver_opts* o, int* wpb, int* bps,
                             int* bps_lat = nullptr) {
   *wpb = (o && o->warps_per_block > 0) ? o->warps_per_block : 4;
   int t = 1, l = 1;
-  switch (d->model) {
-    case MPXG_MODEL_SRBD_QUAT13: t = resident_blocks<ModelQuat13>(*wpb, true); l = resident_blocks<ModelQuat13>(*wpb, false); break;
-    case MPXG_MODEL_SRBD_RPY12: t = resident_blocks<ModelRpy12>(*wpb, true); l = resident_blocks<ModelRpy12>(*wpb, false); break;
-    case MPXG_MODEL_BIPED_WRENCH12: t = resident_blocks<ModelBiped12>(*wpb, true); l = resident_blocks<ModelBiped12>(*wpb, false); break;
-    default: break;
+  if (const SqpOps* ops = sqp_ops(d->model)) {
+    t = ops->resident_blocks(*wpb, true);
+    l = ops->resident_blocks(*wpb, false);
   }
   if (o && o->blocks_per_sm > 0) t = l = o->blocks_per_sm;
   *bps = t;
   if (bps_lat) *bps_lat = l;
-  (void)num_sms;
 }
 
 extern "C" {
@@ -162,7 +136,7 @@ size_t mpxg_workspace_bytes(const mpxg_problem_desc* d, const mpxg_solver_opts* 
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   int wpb, bps;
-  launch_geometry(d, o, sms, &wpb, &bps);
+  launch_geometry(d, o, &wpb, &bps);
   const long long stride = scratch_stride_for(d->model, d->n_max);
   const size_t slots = (size_t)scratch_slots(d->model, wpb, sms);
   return (size_t)stride * sizeof(float) * slots + (slots + 31) / 32 * 4 + 256 +
@@ -188,7 +162,7 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaGetDevice"); }
   e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaDeviceGetAttribute"); }
-  launch_geometry(d, o, h->num_sms, &h->warps_per_block, &h->blocks_per_sm, &h->blocks_per_sm_lat);
+  launch_geometry(d, o, &h->warps_per_block, &h->blocks_per_sm, &h->blocks_per_sm_lat);
   h->total_warps = h->num_sms * h->blocks_per_sm * h->warps_per_block;
   h->scratch_stride = scratch_stride_for(d->model, d->n_max);
   h->n_slots = scratch_slots(d->model, h->warps_per_block, h->num_sms);
@@ -213,13 +187,7 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   e = cudaMemset(h->slot_bits, 0, nwords * 4 + 256);
   if (e == cudaSuccess) e = cudaMemset(h->counters, 0, ctr_bytes);
   if (e != cudaSuccess) { mpxg_destroy(h); return cuda_fail(nullptr, e, "mpxg_create: cudaMemset"); }
-  ModelConst& mc = h->mc;
-  mc.dt = d->dt; mc.mass = d->mass; mc.inv_mass = 1.0f / d->mass; mc.gravity = d->gravity; mc.mu = d->mu;
-  mc.alpha = d->barrier_alpha; mc.sigma = d->barrier_sigma;
-  mc.foot_length = d->foot_length; mc.foot_width = d->foot_width;
-  mc.barrier_kind = d->barrier_kind; mc.barrier_masked = d->barrier_masked;
-  mc.barrier_hess_scale = d->barrier_hess_scale;
-  for (int i = 0; i < 9; ++i) { mc.I[i] = d->inertia[i]; mc.Iinv[i] = d->inertia_inv[i]; }
+  h->mc = model_const(d);
   SqpParams& sp = h->sp;
   sp.sqp_iters = o->sqp_iters; sp.ls_max_trials = o->ls_max_trials; sp.ls_beta = o->ls_beta; sp.ls_eta = o->ls_eta;
   sp.reg = o->reg; sp.rho0 = o->rho0; sp.ls_skip_tol = o->ls_skip_tol; sp.compute_kkt = o->compute_kkt;
@@ -249,28 +217,12 @@ void mpxg_destroy(mpxg_handle* h) {
 
 }  // extern "C"
 
-template <class M>
-static mpxg_status launch_sqp(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb, bool tput) {
-  const size_t smem = smem_per_warp<M>() * (size_t)wpb;
-  auto fn = sqp_kernel_for<M>(tput);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
-  }
-  fn<<<blocks, wpb * 32, smem, st>>>(h->mc, h->sp, bp);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(h, e, "sqp_kernel launch");
-  return MPXG_OK;
-}
-
 static mpxg_status dispatch(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb,
                             bool tput = false) {
-  switch (h->desc.model) {
-    case MPXG_MODEL_SRBD_QUAT13: return launch_sqp<ModelQuat13>(h, st, bp, blocks, wpb, tput);
-    case MPXG_MODEL_SRBD_RPY12: return launch_sqp<ModelRpy12>(h, st, bp, blocks, wpb, tput);
-    case MPXG_MODEL_BIPED_WRENCH12: return launch_sqp<ModelBiped12>(h, st, bp, blocks, wpb, tput);
-    default: return fail(h, MPXG_ERR_UNSUPPORTED, "model");
-  }
+  const SqpOps* ops = sqp_ops(h->desc.model);
+  if (!ops) return fail(h, MPXG_ERR_UNSUPPORTED, "model");
+  const cudaError_t e = ops->launch(h->mc, h->sp, bp, blocks, wpb, tput, st);
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "sqp_kernel launch");
 }
 
 static mpxg_status check_io(mpxg_handle* h, const mpxg_batch_io* io) {
@@ -382,18 +334,6 @@ mpxg_status mpxg_shift_warm_start(mpxg_handle* h, void* stream, int batch, const
 
 }  // extern "C"
 
-template <class M>
-static mpxg_status launch_vjp(mpxg_handle* h, cudaStream_t st, const BatchPtrs& bp, int blocks, int wpb) {
-  const size_t smem = smem_per_warp<M>() * (size_t)wpb;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(sqp_vjp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute");
-  }
-  sqp_vjp_kernel<M><<<blocks, wpb * 32, smem, st>>>(h->mc, h->sp, bp);
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "sqp_vjp_kernel launch");
-}
-
 extern "C" {
 
 mpxg_status mpxg_solve_vjp(mpxg_handle* h, void* stream, const mpxg_vjp_io* v) {
@@ -434,12 +374,10 @@ mpxg_status mpxg_solve_vjp(mpxg_handle* h, void* stream, const mpxg_vjp_io* v) {
   int blocks = h->num_sms * h->blocks_per_sm_lat;
   const int need = (io.batch + wpb - 1) / wpb;
   if (need < blocks) blocks = need;
-  switch (h->desc.model) {
-    case MPXG_MODEL_SRBD_QUAT13: s = launch_vjp<ModelQuat13>(h, st, bp, blocks, wpb); break;
-    case MPXG_MODEL_SRBD_RPY12: s = launch_vjp<ModelRpy12>(h, st, bp, blocks, wpb); break;
-    case MPXG_MODEL_BIPED_WRENCH12: s = launch_vjp<ModelBiped12>(h, st, bp, blocks, wpb); break;
-    default: return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_solve_vjp: model");
-  }
+  const SqpOps* ops = sqp_ops(h->desc.model);
+  if (!ops) return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_solve_vjp: model");
+  e = ops->launch_vjp(h->mc, h->sp, bp, blocks, wpb, st);
+  s = e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "sqp_vjp_kernel launch");
   if (s != MPXG_OK || cap != cudaStreamCaptureStatusNone) return s;
   e = cudaEventRecord(h->ring_ev[r], st);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
@@ -454,27 +392,10 @@ mpxg_status mpxg_evaluate(mpxg_handle* h, void* stream, int batch, const int* ho
   if (batch < 0 || batch > h->desc.batch_max || !x0 || !X || !U || !reference || !parameter || !w || !g || !c)
     return fail(h, MPXG_ERR_INVALID_ARG, "mpxg_evaluate: bad arguments");
   if (batch == 0) return MPXG_OK;
-  const long long n = (long long)batch * (h->desc.n_max + 1);
-  const int threads = 128;
-  const unsigned blocks = (unsigned)((n + threads - 1) / threads);
-  cudaStream_t st = (cudaStream_t)stream;
-  const int nm = h->desc.n_max;
-  switch (h->desc.model) {
-    case MPXG_MODEL_SRBD_QUAT13:
-      evaluate_kernel<ModelQuat13><<<blocks, threads, 0, st>>>(h->mc, batch, nm, horizon, x0, X, U, reference,
-                                                              parameter, w, g, c);
-      break;
-    case MPXG_MODEL_SRBD_RPY12:
-      evaluate_kernel<ModelRpy12><<<blocks, threads, 0, st>>>(h->mc, batch, nm, horizon, x0, X, U, reference,
-                                                             parameter, w, g, c);
-      break;
-    case MPXG_MODEL_BIPED_WRENCH12:
-      evaluate_kernel<ModelBiped12><<<blocks, threads, 0, st>>>(h->mc, batch, nm, horizon, x0, X, U, reference,
-                                                               parameter, w, g, c);
-      break;
-    default: return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_evaluate: model");
-  }
-  cudaError_t e = cudaGetLastError();
+  const SqpOps* ops = sqp_ops(h->desc.model);
+  if (!ops) return fail(h, MPXG_ERR_UNSUPPORTED, "mpxg_evaluate: model");
+  const cudaError_t e = ops->launch_evaluate(h->mc, batch, h->desc.n_max, horizon, x0, X, U, reference, parameter,
+                                             w, g, c, (cudaStream_t)stream);
   return e == cudaSuccess ? MPXG_OK : cuda_fail(h, e, "evaluate_kernel launch");
 }
 
@@ -486,103 +407,6 @@ mpxg_status mpxg_timer_run(void* stream, int batch, int n_legs, float duty_facto
   timer_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(n, n_legs, duty_factor, step_freq, dt, leg_time, contact);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "timer_kernel launch");
-}
-
-// ---------------------------------------------------------------- whole body
-// The checks the whole-body kernel relies on (it indexes shared arrays by
-// these fields without further bounds tests).
-static const char* wb_check(const mpxg_wb_model* m) {
-  using namespace mpxg::wb;
-  if (!m) return "null model";
-  if (m->nbody < 1 || m->nbody > MPXG_WB_MAX_BODY) return "nbody out of range 1..32";
-  if (m->nv < 0 || m->nv > MPXG_WB_MAX_DOF) return "nv out of range 0..32";
-  if (m->nq < 0 || m->nq > MPXG_WB_MAX_DOF + 4) return "nq out of range";
-  if (m->n_contact < 0 || m->n_contact > MPXG_WB_MAX_CONTACT) return "n_contact out of range 0..8";
-  int dof = 0, qp = 0;
-  for (int b = 0; b < m->nbody; ++b) {
-    const int jt = m->jnt_type[b];
-    if (m->parent[b] < -1 || m->parent[b] >= b) return "bodies must be listed parents first";
-    if (jt < 0 || jt > 3) return "unknown joint type";
-    if (jt == 1 && (b != 0 || m->parent[b] != -1)) return "a free joint is allowed on the first body only";
-    if (m->dof_adr[b] != dof || m->qpos_adr[b] != qp) return "dof / qpos addresses must be dense in body order";
-    dof += ndof(jt);
-    qp += nqpos(jt);
-    if (!(m->mass[b] >= 0.0f)) return "negative mass";
-  }
-  if (dof != m->nv || qp != m->nq) return "nv / nq do not match the joints";
-  for (int c = 0; c < m->n_contact; ++c)
-    if (m->contact_point_body[c] < 0 || m->contact_point_body[c] >= m->nbody || m->contact_jac_body[c] < 0 ||
-        m->contact_jac_body[c] >= m->nbody)
-      return "contact body out of range";
-  return nullptr;
-}
-
-// The smallest capacity the (checked) model fits.
-extern "C++" {
-template <int MODE>
-static cudaError_t wb_launch(const mpxg_wb_model& m, int batch, const mpxg::wb::Args& a, cudaStream_t st) {
-  using namespace mpxg::wb;
-  if (m.nbody <= CapQuad::MB && m.nv <= CapQuad::MD && m.nq <= CapQuad::MD + 4 && 3 * m.n_contact <= CapQuad::MR)
-    wb_kernel<MODE, CapQuad><<<(batch + CapQuad::NW - 1) / CapQuad::NW, 32 * CapQuad::NW, 0, st>>>(m, batch, a);
-  else
-    wb_kernel<MODE, CapAny><<<(batch + CapAny::NW - 1) / CapAny::NW, 32 * CapAny::NW, 0, st>>>(m, batch, a);
-  return cudaGetLastError();
-}
-}
-
-mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, const float* qpos, const float* qvel,
-                          float* M, float* bias, float* cpos, float* J, float* cvel) {
-  using namespace mpxg::wb;
-  if (const char* why = wb_check(model)) return fail(nullptr, MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_terms: ") + why);
-  if (batch < 0 || (batch > 0 && (!qpos || !qvel)))
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_wb_terms: bad batch or null state");
-  if (batch == 0) return MPXG_OK;
-  Args a{};
-  a.qpos = qpos; a.qvel = qvel; a.M = M; a.bias = bias; a.cpos = cpos; a.J = J; a.cvel = cvel;
-  a.sq = model->nq; a.sv = model->nv;
-  cudaError_t e = wb_launch<MODE_TERMS>(*model, batch, a, (cudaStream_t)stream);
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
-}
-
-mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batch, const float* qpos,
-                              const float* qvel, const float* grf, const float* foot_ref, const float* foot_ref_dot,
-                              const int* contact, const float* Kp, const float* Kd, float* tau, float* J) {
-  using namespace mpxg::wb;
-  if (const char* why = wb_check(model))
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_interface: ") + why);
-  if (model->jnt_type[0] != 1 || model->n_contact < 1 || model->nv != 6 + 3 * model->n_contact)
-    return fail(nullptr, MPXG_ERR_INVALID_ARG,
-                "mpxg_wb_interface: needs a free root and nv = 6 + 3 x contacts (one torque row per contact axis)");
-  if (batch < 0 || (batch > 0 && (!qpos || !qvel || !grf || !foot_ref || !foot_ref_dot || !contact || !Kp || !Kd ||
-                                  !tau)))
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_wb_interface: bad batch or null pointer");
-  if (batch == 0) return MPXG_OK;
-  Args a{};
-  a.qpos = qpos; a.qvel = qvel; a.grf = grf; a.foot_ref = foot_ref; a.foot_ref_dot = foot_ref_dot;
-  a.contact = contact; a.Kp = Kp; a.Kd = Kd; a.tau = tau; a.J = J;
-  a.sq = model->nq; a.sv = model->nv;
-  cudaError_t e = wb_launch<MODE_INTERFACE>(*model, batch, a, (cudaStream_t)stream);
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
-}
-
-mpxg_status mpxg_wb_step(void* stream, const mpxg_wb_model* model, int batch, float dt, float alpha, const float* x,
-                         const float* u, const int* contact, float* x_next) {
-  using namespace mpxg::wb;
-  if (const char* why = wb_check(model)) return fail(nullptr, MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_step: ") + why);
-  const int nv = model->nv, nr = 3 * model->n_contact;
-  if (model->jnt_type[0] != 1 || model->nq != nv + 1 || model->n_contact < 1 || nr > nv || nv + nr + 1 > 32)
-    return fail(nullptr, MPXG_ERR_INVALID_ARG,
-                "mpxg_wb_step: needs a free root, hinge or slide joints elsewhere, 3 x contacts <= nv and "
-                "nv + 3 x contacts + 1 <= 32");
-  if (batch < 0 || (batch > 0 && (!x || !u || !contact || !x_next)) || !(dt > 0.0f))
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_wb_step: bad batch, dt or null pointer");
-  if (batch == 0) return MPXG_OK;
-  Args a{};
-  const int nx = model->nq + nv + 2 * nr;
-  a.qpos = x; a.qvel = x + model->nq; a.sq = nx; a.sv = nx;
-  a.u = u; a.contact = contact; a.x_next = x_next; a.dt = dt; a.alpha = alpha;
-  cudaError_t e = wb_launch<MODE_STEP>(*model, batch, a, (cudaStream_t)stream);
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "wb_kernel launch");
 }
 
 mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* a) {
@@ -621,46 +445,6 @@ mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "refgen_srbd_kernel launch");
 }
 
-size_t mpxg_lqr_workspace_bytes(int batch, int N, int n, int m, int method) {
-  (void)m;
-  (void)method;
-  if (batch < 0 || N < 1 || n < 1) return 0;
-  return lqr_scratch_bytes(batch, N, n);
-}
-
-mpxg_status mpxg_lqr_solve(void* stream, const mpxg_lq_io* io, int method) {
-  return lqr_solve_host(stream, io, method, &g_lib_err);
-}
-
-size_t mpxg_lqr_eq_workspace_bytes(int batch, int N, int n) {
-  if (batch < 0 || N < 1 || n < 1) return 0;
-  return lqeq::lqr_eq_scratch_bytes(batch, N, n);
-}
-
-mpxg_status mpxg_lqr_eq_solve_method(void* stream, const mpxg_lq_eq_io* io, int method) {
-  if (!io || io->batch < 0 || io->N < 1 || !io->A || !io->Bm || !io->c || !io->Q || !io->R || !io->M || !io->q ||
-      !io->r || !io->C || !io->D || !io->e || !io->x0 || !io->K || !io->k || !io->Knu || !io->knu || !io->X ||
-      !io->U || !io->lam || !io->nu || !io->workspace)
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: bad arguments");
-  if (method != 0 && method != 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: method is 0 or 1");
-  if (method == 0 && (reinterpret_cast<uintptr_t>(io->workspace) & 15u) != 0)
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_lqr_eq_solve: workspace must be 16-byte aligned");
-  if (io->batch == 0) return MPXG_OK;
-  cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e;
-  const bool tcores = (method == 0);
-  if (io->n == 72 && io->m == 30 && io->n_eq == 12)
-    e = tcores ? lqeq::launch_lqr_eq_tc<72, 30, 12>(st, *io) : lqeq::launch_lqr_eq<72, 30, 12>(st, *io);
-  else if (io->n == 16 && io->m == 8 && io->n_eq == 4)
-    e = tcores ? lqeq::launch_lqr_eq_tc<16, 8, 4>(st, *io) : lqeq::launch_lqr_eq<16, 8, 4>(st, *io);
-  else if (io->n == 8 && io->m == 5 && io->n_eq == 2)
-    e = tcores ? lqeq::launch_lqr_eq_tc<8, 5, 2>(st, *io) : lqeq::launch_lqr_eq<8, 5, 2>(st, *io);
-  else return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_lqr_eq_solve: (n, m, n_eq) not built: (72,30,12) (16,8,4) (8,5,2)");
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "lqr_eq kernel launch");
-}
-
-mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io) { return mpxg_lqr_eq_solve_method(stream, io, 0); }
-
 }  // extern "C"
 
 // ============================================================================
@@ -687,7 +471,10 @@ mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io) { return mp
 //    them on one stream or order them with events;
 //  - the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (a host-side symbol is not a device address); make
-//    that first call before any stream capture.
+//    that first call before any stream capture;
+//  - the resolved address is kept for the life of the process: after a
+//    cudaDeviceReset (or anything else that destroys the device's primary
+//    context) this entry point must not be called again in that process.
 // ============================================================================
 static constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchBytes / sizeof(float)];
@@ -724,18 +511,6 @@ mpxg_status noalloc_setup(int dev, NoAllocDevice** out) {
   return MPXG_OK;
 }
 
-template <class M>
-mpxg_status noalloc_launch(const ModelConst& mc, const SqpParams& sp, cudaStream_t st, const BatchPtrs& bp,
-                           int blocks, int wpb) {
-  const size_t smem = sizeof(WarpSmem<M>) * (size_t)wpb;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(sqp_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaFuncSetAttribute");
-  }
-  sqp_kernel<M><<<blocks, wpb * 32, smem, st>>>(mc, sp, bp);
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "mpxg_solve_noalloc: launch");
-}
 }  // namespace
 
 extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg_solver_opts* o, void* stream,
@@ -746,6 +521,8 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
   if (d->n != nx || d->m != nu) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: n/m do not match the model");
   if (d->n_max < 1 || d->n_max > 4096) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: n_max out of range");
   if (o->sqp_iters < 0 || o->ls_max_trials < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: bad options");
+  if (o->warps_per_block < 0 || o->warps_per_block > 4 || o->blocks_per_sm < 0)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: warps_per_block must be 0..4 (128-thread blocks)");
   if (!(d->dt > 0.0f) || !(d->mass > 0.0f)) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_noalloc: dt and mass must be > 0");
   if (io->batch < 0 || !io->x0 || !io->X_in || !io->U_in || !io->V_in || !io->reference || !io->parameter ||
       !io->w || !io->X || !io->U || !io->V)
@@ -765,13 +542,7 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
                     std::to_string(nd->num_sms) + ")");
   if (io->batch == 0) return MPXG_OK;
 
-  ModelConst mc;
-  mc.dt = d->dt; mc.mass = d->mass; mc.inv_mass = 1.0f / d->mass; mc.gravity = d->gravity; mc.mu = d->mu;
-  mc.alpha = d->barrier_alpha; mc.sigma = d->barrier_sigma;
-  mc.foot_length = d->foot_length; mc.foot_width = d->foot_width;
-  mc.barrier_kind = d->barrier_kind; mc.barrier_masked = d->barrier_masked;
-  mc.barrier_hess_scale = d->barrier_hess_scale;
-  for (int i = 0; i < 9; ++i) { mc.I[i] = d->inertia[i]; mc.Iinv[i] = d->inertia_inv[i]; }
+  const ModelConst mc = model_const(d);
   SqpParams sp;
   sp.sqp_iters = o->sqp_iters; sp.ls_max_trials = o->ls_max_trials; sp.ls_beta = o->ls_beta; sp.ls_eta = o->ls_eta;
   sp.reg = o->reg; sp.rho0 = o->rho0; sp.ls_skip_tol = o->ls_skip_tol; sp.compute_kkt = o->compute_kkt;
@@ -798,12 +569,8 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
   cudaStream_t st = (cudaStream_t)stream;
   e = cudaMemsetAsync(nd->counter, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpxg_solve_noalloc: cudaMemsetAsync");
-  switch (d->model) {
-    case MPXG_MODEL_SRBD_QUAT13: return noalloc_launch<ModelQuat13>(mc, sp, st, bp, (int)blocks, wpb);
-    case MPXG_MODEL_SRBD_RPY12: return noalloc_launch<ModelRpy12>(mc, sp, st, bp, (int)blocks, wpb);
-    case MPXG_MODEL_BIPED_WRENCH12: return noalloc_launch<ModelBiped12>(mc, sp, st, bp, (int)blocks, wpb);
-    default: return fail(nullptr, MPXG_ERR_UNSUPPORTED, "mpxg_solve_noalloc: model");
-  }
+  e = sqp_ops(d->model)->launch(mc, sp, bp, (int)blocks, wpb, /*tput=*/false, st);
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "mpxg_solve_noalloc: launch");
 }
 
 // ============================================================================
@@ -814,8 +581,11 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
 // that call inside a compiled JAX program.  Operands and results arrive as
 // device buffers in the order of optimizers.mpc(reference, parameter, W, x0,
 // X0, U0, V0) -> (X, U, V), with W passed as its diagonal [B,24].  The opaque
-// string is an mpxg_xla_opaque; handles are created on first use per
-// (device, opaque) and kept for the life of the process.
+// string is an mpxg_xla_opaque.  The handle of each (device, opaque) is
+// created by mpxg_xla_prepare ahead of the jitted program's first run (the
+// JAX binding calls it when it builds the solve), so the custom call itself
+// allocates nothing: it may run under XLA's command-buffer capture, where a
+// cudaMalloc would fail.  Handles are kept for the life of the process.
 // ============================================================================
 namespace {
 
@@ -833,38 +603,60 @@ void xla_fail(void* status, const std::string& msg) {
 
 }  // namespace
 
-// Handle of (device, opaque) for the XLA targets, created on first use.
-static mpxg_handle* xla_handle(const char* opaque, size_t opaque_len, void* status, mpxg_xla_opaque* op,
-                               const char* who) {
+// Checked opaque of an XLA call and the handle key of (current device, opaque).
+static bool xla_key(const char* opaque, size_t opaque_len, mpxg_xla_opaque* op, std::string* key, std::string* err,
+                    const char* who) {
   if (!opaque || opaque_len != sizeof(mpxg_xla_opaque)) {
-    xla_fail(status, std::string(who) + ": opaque must be an mpxg_xla_opaque (" +
-                         std::to_string(sizeof(mpxg_xla_opaque)) + " bytes), got " + std::to_string(opaque_len));
-    return nullptr;
+    *err = std::string(who) + ": opaque must be an mpxg_xla_opaque (" + std::to_string(sizeof(mpxg_xla_opaque)) +
+           " bytes), got " + std::to_string(opaque_len);
+    return false;
   }
   std::memcpy(op, opaque, sizeof(*op));
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
-    xla_fail(status, std::string(who) + ": cudaGetDevice failed");
-    return nullptr;
+    *err = std::string(who) + ": cudaGetDevice failed";
+    return false;
   }
   if (op->batch < 0 || op->batch > op->desc.batch_max) {
-    xla_fail(status, std::string(who) + ": batch exceeds desc.batch_max");
+    *err = std::string(who) + ": batch exceeds desc.batch_max";
+    return false;
+  }
+  key->assign(reinterpret_cast<const char*>(&dev), sizeof(dev));
+  key->append(reinterpret_cast<const char*>(&op->desc), sizeof(op->desc));
+  key->append(reinterpret_cast<const char*>(&op->opts), sizeof(op->opts));
+  return true;
+}
+
+// Handle of (device, opaque) prepared by mpxg_xla_prepare; null (and the
+// failure reported to XLA) when there is none.
+static mpxg_handle* xla_handle(const char* opaque, size_t opaque_len, void* status, mpxg_xla_opaque* op,
+                               const char* who) {
+  std::string key, err;
+  if (!xla_key(opaque, opaque_len, op, &key, &err, who)) {
+    xla_fail(status, err);
     return nullptr;
   }
-  std::string key(reinterpret_cast<const char*>(&dev), sizeof(dev));
-  key.append(reinterpret_cast<const char*>(&op->desc), sizeof(op->desc));
-  key.append(reinterpret_cast<const char*>(&op->opts), sizeof(op->opts));
   std::lock_guard<std::mutex> lock(g_xla_mu);
   auto it = g_xla_handles.find(key);
   if (it != g_xla_handles.end()) return it->second;
+  xla_fail(status, std::string(who) + ": no handle for this opaque on this device: call mpxg_xla_prepare with it "
+                                      "(and this device current) before the program runs");
+  return nullptr;
+}
+
+extern "C" mpxg_status mpxg_xla_prepare(const char* opaque, size_t opaque_len) {
+  mpxg_xla_opaque op;
+  std::string key, err;
+  if (!xla_key(opaque, opaque_len, &op, &key, &err, "mpxg_xla_prepare"))
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, err);
+  std::lock_guard<std::mutex> lock(g_xla_mu);
+  if (g_xla_handles.count(key)) return MPXG_OK;
   mpxg_handle* h = nullptr;
-  if (mpxg_create(&op->desc, &op->opts, &h) != MPXG_OK) {
-    xla_fail(status, std::string(who) + ": mpxg_create: " + g_lib_err);
-    return nullptr;
-  }
+  const mpxg_status s = mpxg_create(&op.desc, &op.opts, &h);
+  if (s != MPXG_OK) return s;
   g_xla_handles[key] = h;
-  return h;
+  return MPXG_OK;
 }
 
 extern "C" void mpxg_xla_solve(void* stream, void** buffers, const char* opaque, size_t opaque_len, void* status) {

@@ -1,0 +1,5 @@
+// SQP, vector-Jacobian-product and evaluation kernels of the roll-pitch-yaw SRBD model
+// (a unit of its own so that the models compile in parallel).
+#include "sqp_ops.cuh"
+
+MPXG_DEFINE_SQP_OPS(mpxg::ModelRpy12, rpy12)

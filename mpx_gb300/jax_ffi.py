@@ -74,6 +74,20 @@ def opaque_bytes(desc, opts, n_max, batch):
     return bytes(op)
 
 
+def prepare(opaque, devices=(None,)):
+    """Create the device workspace of an opaque on each CUDA device (None:
+    the current one) now, so that the custom call allocates nothing when the
+    jitted program runs."""
+    import torch
+    L = _lib.load()
+    for d in devices:
+        if d is None:
+            _lib.check(L.mpxg_xla_prepare(opaque, len(opaque)), None, "mpxg_xla_prepare")
+        else:
+            with torch.cuda.device(d):
+                _lib.check(L.mpxg_xla_prepare(opaque, len(opaque)), None, "mpxg_xla_prepare")
+
+
 def _primitive():
     global _prim
     if _prim is not None:
@@ -120,15 +134,18 @@ def _primitive_vjp():
     return p
 
 
-def make_mpc(desc, opts, n_max, batch):
+def make_mpc(desc, opts, n_max, batch, devices=(None,)):
     """A jit-compatible batched solve (reference, parameter, W, x0, X0, U0, V0)
     -> (X, U, V) for `batch` instances of horizon n_max, differentiable with
     jax.grad / jax.vjp: the backward pass is mpxg_xla_solve_vjp (implicit
     differentiation of the converged solution), giving gradients with respect
     to x0 and to the 12 tracked columns of the reference; the warm start,
-    parameter table and weights get zero gradients."""
+    parameter table and weights get zero gradients.  The device workspace is
+    created here, on each of `devices` (CUDA indices; None: the current
+    device), so the custom calls allocate nothing when the program runs."""
     register()
     opaque = opaque_bytes(desc, opts, n_max, batch)
+    prepare(opaque, devices)
     prim, prim_vjp = _primitive(), _primitive_vjp()
     f32 = lambda a: jnp.asarray(a, jnp.float32)
 

@@ -60,6 +60,7 @@ class ModelDesc:
     barrier_kind: int = 0           # 0: penalty() of objectives.py:7-13; 1: C2 relaxed log barrier
     barrier_masked: int = 0         # 1: barrier cost multiplied by the stage contact flag
     barrier_hess_scale: float = 1.0 # factor on the barrier's Gauss-Newton curvature
+    cone_eps2: float = 1e-2         # friction cone sqrt(fx^2 + fy^2 + cone_eps2) (objectives.py:29: 1e-2)
 
     @property
     def inertia_inv(self):
@@ -110,16 +111,23 @@ def quadruped_rpy12(mu=0.6):
     """Quadruped SRBD with roll-pitch-yaw state: mass 15 kg, inertia
     diag(0.10, 0.25, 0.30) kg m^2, dt 0.02 s, friction 0.6.  The friction
     cone enters as a C2 relaxed log barrier (quadratic below delta = 5 N),
-    applied to legs in stance, with its exact curvature in the Hessian."""
+    applied to legs in stance, with its exact curvature in the Hessian.  The
+    cone's tangential norm is smoothed over 1 N, sqrt(fx^2 + fy^2 + 1), where
+    the reference smooths over 0.1 N (objectives.py:29): at 0.1 N the cone's
+    curvature near zero tangential force is 10 per N, Newton steps on forces
+    of a few N overshoot it, and the merit line search then cuts them to a
+    quarter iteration after iteration."""
     return ModelDesc(MODEL_SRBD_RPY12, 12, 12, dt=0.02, mass=15.0, inertia=np.diag([0.10, 0.25, 0.30]),
-                     n_contact=4, mu=mu, barrier_kind=1, barrier_masked=1)
+                     n_contact=4, mu=mu, barrier_kind=1, barrier_masked=1, cone_eps2=1.0)
 
 
 def biped_wrench12(mu=0.6):
     """SRBD biped: mass 60 kg, inertia diag(6, 5, 1.5) kg m^2, two 0.2 x 0.1 m
-    foot plates each carrying a 6-D wrench [F, tau]."""
+    foot plates each carrying a 6-D wrench [F, tau].  The cone is smoothed
+    over 1 N, as for the roll-pitch-yaw quadruped."""
     return ModelDesc(MODEL_BIPED_WRENCH12, 12, 12, dt=0.02, mass=60.0, inertia=np.diag([6.0, 5.0, 1.5]),
-                     n_contact=2, mu=mu, foot_length=0.2, foot_width=0.1, barrier_kind=1, barrier_masked=1)
+                     n_contact=2, mu=mu, foot_length=0.2, foot_width=0.1, barrier_kind=1, barrier_masked=1,
+                     cone_eps2=1.0)
 
 
 def generic_lq(n, m):

@@ -285,34 +285,59 @@ class MPCServer:
             self.poll(block=True)
 
 
+class EpisodeStream:
+    """Concurrent episodes of a served stream, carried from one call of
+    served_workload to the next (so that a measured window can start with
+    episodes already warm).  close() releases the episodes still open."""
+
+    def __init__(self, server, seed=0):
+        self.server = server
+        self.rng = np.random.default_rng(seed)
+        self.eps = collections.deque()
+        self.counter = 0
+        self.seed = seed
+
+    def close(self):
+        for ep, _ in self.eps:
+            self.server.release(ep)
+        self.eps.clear()
+
+
 def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_range=(20, 200), episode_ticks=200,
-                    models=("quadruped", "biped"), v_range=(-0.5, 0.5)):
+                    models=("quadruped", "biped"), v_range=(-0.5, 0.5), stream=None, stagger=False):
     """Poisson request stream (rate_hz) over `n_episodes` concurrent episodes
     of `episode_ticks` ticks; finished episodes are replaced by new ones.
     Runs in real time; returns (latencies in s, wall time in s); the statuses,
     KKT residuals and model indices of the completed ticks are left in
-    server.last_status, server.last_kkt and server.last_model."""
+    server.last_status, server.last_kkt and server.last_model.
+
+    stream: an EpisodeStream to continue (its episodes stay open at return,
+    and new ones are admitted only up to n_episodes); None: fresh episodes,
+    all released at return.  stagger: the episodes admitted to fill the
+    stream start at uniformly drawn ages, so that their ends (and their
+    successors' cold starts) spread over time as in a steady stream."""
+    own = stream is None
+    st = EpisodeStream(server, seed) if own else stream
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, size=int(rate_hz * duration_s * 1.2) + 16)
     arrivals = np.cumsum(gaps)
     arrivals = arrivals[arrivals < duration_s]
-    eps = collections.deque()
-    counter = [0]
+    eps = st.eps
 
-    def new_episode():
-        counter[0] += 1
-        name = models[counter[0] % len(models)]
+    def new_episode(age=0):
+        st.counter += 1
+        name = models[st.counter % len(models)]
         pool = server.pools[name]
         x0 = np.zeros(pool.desc.n, dtype=np.float32)
         x0[2] = pool.gait["height"]
-        x0 += rng.normal(0, 0.02, pool.desc.n).astype(np.float32)
-        hz = int(rng.integers(horizon_range[0], horizon_range[1] + 1))
-        ep = ("ep", seed, counter[0])
-        server.admit(ep, name, x0, hz, v_ref=float(rng.uniform(*v_range)), phase=float(rng.uniform()))
-        eps.append([ep, 0])
+        x0 += st.rng.normal(0, 0.02, pool.desc.n).astype(np.float32)
+        hz = int(st.rng.integers(horizon_range[0], horizon_range[1] + 1))
+        ep = ("ep", st.seed, st.counter)
+        server.admit(ep, name, x0, hz, v_ref=float(st.rng.uniform(*v_range)), phase=float(st.rng.uniform()))
+        eps.append([ep, age])
 
-    for _ in range(n_episodes):
-        new_episode()
+    while len(eps) < n_episodes:
+        new_episode(int(st.rng.integers(0, episode_ticks)) if stagger else 0)
     t0 = time.perf_counter()
     i = 0
     lat, stats, kkts, mods = [], [], [], []
@@ -334,20 +359,20 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
             i += 1
         if keys:
             server.submit_many(keys, arr)
-        la, st, kk, md = server.poll_fast(with_model=True)
-        lat.append(la); stats.append(st); kkts.append(kk); mods.append(md)
+        la, stt, kk, md = server.poll_fast(with_model=True)
+        lat.append(la); stats.append(stt); kkts.append(kk); mods.append(md)
         if i >= len(arrivals):
             q, r, _ = server.stats()
             if q == 0 and r == 0:
-                la, st, kk, md = server.poll_fast(with_model=True)
-                lat.append(la); stats.append(st); kkts.append(kk); mods.append(md)
+                la, stt, kk, md = server.poll_fast(with_model=True)
+                lat.append(la); stats.append(stt); kkts.append(kk); mods.append(md)
                 break
     wall = time.perf_counter() - t0
     server.last_status = np.concatenate(stats) if stats else np.zeros(0, np.int32)
     server.last_kkt = np.concatenate(kkts) if kkts else np.zeros(0, np.float32)
     server.last_model = np.concatenate(mods) if mods else np.zeros(0, np.int8)
-    for ep, _ in eps:
-        server.release(ep)
+    if own:
+        st.close()
     return np.concatenate(lat) if lat else np.zeros(0), wall
 
 

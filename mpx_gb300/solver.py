@@ -39,6 +39,7 @@ def problem_desc(desc, n_max, batch_max):
     d.foot_length = float(desc.foot_length); d.foot_width = float(desc.foot_width)
     d.barrier_kind = int(desc.barrier_kind); d.barrier_masked = int(desc.barrier_masked)
     d.barrier_hess_scale = float(desc.barrier_hess_scale)
+    d.cone_eps2 = float(desc.cone_eps2)
     I = np.asarray(desc.inertia, dtype=np.float64).reshape(9)
     Ii = np.asarray(desc.inertia_inv, dtype=np.float64).reshape(9)
     for i in range(9):

@@ -211,7 +211,7 @@ inline StageCount count_stage(const ModelParams& mp, const double* x, const doub
     for (int i = 0; i < legs; ++i) {
       if (ref[contact_off + i] == 0.0) continue;
       const Flop fx_ = var(u[stride * i]), fy_ = var(u[stride * i + 1]), cv = var(cu[cstride * i].v);
-      const Flop s2 = fx_ * fx_ + fy_ * fy_ + Flop(1e-2), s = sqrt(s2), s3 = s2 * s;
+      const Flop s2 = fx_ * fx_ + fy_ * fy_ + Flop(mp.cone_eps2), s = sqrt(s2), s3 = s2 * s;
       const Flop dpen = cv.v > mp.barrier_sigma ? Flop(-mp.barrier_alpha) / cv
                                                 : Flop(mp.barrier_alpha / (mp.barrier_sigma * mp.barrier_sigma)) *
                                                       (cv - Flop(2.0 * mp.barrier_sigma));

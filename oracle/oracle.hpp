@@ -140,6 +140,7 @@ struct ModelParams {
   double barrier_hess_scale;  // GN barrier curvature factor (1.0 as objectives.py:73)
   double inertia[9];     // row-major body inertia
   double inertia_inv[9]; // its inverse (host-inverted like mpc_wrapper_srbd.py:66)
+  double cone_eps2 = 1e-2;  // friction cone sqrt(fx^2 + fy^2 + cone_eps2) (objectives.py:29: 1e-2)
 };
 
 // Column counts of the per-stage reference / parameter tables.
@@ -392,7 +393,7 @@ inline int constraints(const ModelParams& mp, const S* u, S* c, int* foot_of) {
     for (int i = 0; i < 2; ++i) {
       const S* F = u + 6 * i; const S* tq = u + 6 * i + 3;
       S* o = c + 7 * i;
-      o[0] = cs<S>(mp.mu) * F[2] - sqrt(F[0] * F[0] + F[1] * F[1] + cs<S>(1e-2));
+      o[0] = cs<S>(mp.mu) * F[2] - sqrt(F[0] * F[0] + F[1] * F[1] + cs<S>(mp.cone_eps2));
       o[1] = cs<S>(hl) * F[2] - tq[1];
       o[2] = cs<S>(hl) * F[2] + tq[1];
       o[3] = cs<S>(hw) * F[2] - tq[0];
@@ -404,7 +405,7 @@ inline int constraints(const ModelParams& mp, const S* u, S* c, int* foot_of) {
     return 14;
   }
   for (int i = 0; i < 4; ++i) {
-    c[i] = cs<S>(mp.mu) * u[3 * i + 2] - sqrt(u[3 * i + 1] * u[3 * i + 1] + u[3 * i] * u[3 * i] + cs<S>(1e-2));
+    c[i] = cs<S>(mp.mu) * u[3 * i + 2] - sqrt(u[3 * i + 1] * u[3 * i + 1] + u[3 * i] * u[3 * i] + cs<S>(mp.cone_eps2));
     foot_of[i] = i;
   }
   return 4;
@@ -589,7 +590,7 @@ void linearize_stage(const ModelParams& mp, int t, bool terminal, const T* x, co
     }
     if (mp.barrier_kind == 1) {
       // exact curvature of the friction cones: 1/2 a beta'(c) grad^2 c, with
-      // c = mu fz - sqrt(fx^2 + fy^2 + 1e-2) (positive semidefinite, since beta' < 0)
+      // c = mu fz - sqrt(fx^2 + fy^2 + cone_eps2) (positive semidefinite, since beta' < 0)
       const int legs = (mp.model == MODEL_BIPED_WRENCH12) ? 2 : 4;
       const int stride = (mp.model == MODEL_BIPED_WRENCH12) ? 6 : 3;
       const int cstride = (mp.model == MODEL_BIPED_WRENCH12) ? 7 : 1;
@@ -600,7 +601,7 @@ void linearize_stage(const ModelParams& mp, int t, bool terminal, const T* x, co
         const double c = double(cv[cstride * i]);
         const double dpen = (c > mp.barrier_sigma) ? -mp.barrier_alpha / c
                                                    : mp.barrier_alpha * (c - 2.0 * mp.barrier_sigma) / (mp.barrier_sigma * mp.barrier_sigma);
-        const double s2 = fx * fx + fy * fy + 1e-2, s = std::sqrt(s2), s3 = s2 * s;
+        const double s2 = fx * fx + fy * fy + mp.cone_eps2, s = std::sqrt(s2), s3 = s2 * s;
         const double hxx = (s2 - fx * fx) / s3, hxy = -fx * fy / s3, hyy = (s2 - fy * fy) / s3;
         const double w = -0.5 * dpen * ck;  // grad^2 c = -grad^2 s
         const int a = n + stride * i;

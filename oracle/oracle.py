@@ -34,7 +34,7 @@ class OrcModel(ctypes.Structure):
                 ("mu", ctypes.c_double), ("barrier_alpha", ctypes.c_double), ("barrier_sigma", ctypes.c_double),
                 ("foot_length", ctypes.c_double), ("foot_width", ctypes.c_double),
                 ("barrier_kind", ctypes.c_int), ("barrier_masked", ctypes.c_int), ("barrier_hess_scale", ctypes.c_double),
-                ("inertia", ctypes.c_double * 9), ("inertia_inv", ctypes.c_double * 9)]
+                ("inertia", ctypes.c_double * 9), ("inertia_inv", ctypes.c_double * 9), ("cone_eps2", ctypes.c_double)]
 
 
 class OrcOpts(ctypes.Structure):
@@ -104,6 +104,7 @@ def make_model(desc):
     md.barrier_kind = int(getattr(desc, "barrier_kind", 0))
     md.barrier_masked = int(getattr(desc, "barrier_masked", 0))
     md.barrier_hess_scale = float(getattr(desc, "barrier_hess_scale", 1.0))
+    md.cone_eps2 = float(getattr(desc, "cone_eps2", 1e-2))
     I = np.asarray(getattr(desc, "inertia", np.eye(3)), dtype=np.float64).reshape(9)
     Ii = np.asarray(getattr(desc, "inertia_inv", np.linalg.inv(I.reshape(3, 3))), dtype=np.float64).reshape(9)
     for i in range(9):

@@ -25,6 +25,7 @@ typedef struct {
   int barrier_masked;
   double barrier_hess_scale;
   double inertia[9], inertia_inv[9];
+  double cone_eps2;
 } orc_model;
 
 typedef struct {
@@ -47,6 +48,7 @@ static ModelParams to_mp(const orc_model* d) {
   mp.foot_length = d->foot_length; mp.foot_width = d->foot_width;
   mp.barrier_kind = d->barrier_kind; mp.barrier_masked = d->barrier_masked; mp.barrier_hess_scale = d->barrier_hess_scale;
   for (int i = 0; i < 9; ++i) { mp.inertia[i] = d->inertia[i]; mp.inertia_inv[i] = d->inertia_inv[i]; }
+  mp.cone_eps2 = d->cone_eps2 > 0.0 ? d->cone_eps2 : 1e-2;
   return mp;
 }
 static Opts to_opts(const orc_opts* o) {

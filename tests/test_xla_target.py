@@ -18,6 +18,12 @@ def test_opaque_packs_desc_opts_and_batch():
                                                                                                 P.MODEL_SRBD_RPY12)
 
 
+def test_prepare_rejects_a_malformed_opaque():
+    L = _lib.load()
+    assert L.mpxg_xla_prepare(b"short", 5) == 1
+    assert b"mpxg_xla_opaque" in L.mpxg_last_error(None)
+
+
 def test_jax_binding_is_optional():
     if not jax_ffi.available():
         with pytest.raises(RuntimeError):
@@ -41,8 +47,24 @@ def test_xla_target_matches_mpxg_solve(cuda):
     bufs = (ctypes.c_void_p * 10)(*[t.data_ptr() for t in ins + outs])
     op = jax_ffi.opaque_bytes(wl.desc, opts, 30, 6)
     L = _lib.load()
+    # without a prepared handle the custom call fails and allocates nothing
+    for o in outs:
+        o.fill_(7.0)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     L.mpxg_xla_solve(None, bufs, op, len(op), None)
     torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert b"mpxg_xla_prepare" in L.mpxg_last_error(None)
+    assert all(bool((o == 7.0).all()) for o in outs)
+    # prepared when the program is built; the custom call then allocates nothing
+    assert L.mpxg_xla_prepare(op, len(op)) == 0, L.mpxg_last_error(None)
+    assert L.mpxg_xla_prepare(op, len(op)) == 0  # once per (device, opaque)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    L.mpxg_xla_solve(None, bufs, op, len(op), None)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free1
     for got, key in zip(outs, ("X", "U", "V")):
         assert np.array_equal(got.cpu().numpy(), ref[key].cpu().numpy()), key
     s.close()
@@ -71,6 +93,7 @@ def test_xla_vjp_target_matches_solver_vjp(cuda):
     gref = torch.empty(5, 21, 12, device="cuda")
     bufs = (ctypes.c_void_p * 11)(*[t.data_ptr() for t in ins + [gx0, gref]])
     op = jax_ffi.opaque_bytes(wl.desc, opts, 20, 5)
+    jax_ffi.prepare(op)
     _lib.load().mpxg_xla_solve_vjp(None, bufs, op, len(op), None)
     torch.cuda.synchronize()
     assert np.array_equal(gx0.cpu().numpy(), ref["gx0"].cpu().numpy())
