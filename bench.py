@@ -14,6 +14,7 @@ the host cores instead.
 """
 import argparse
 import ctypes
+import dataclasses
 import json
 import os
 import statistics
@@ -341,9 +342,46 @@ def dropin_wrapper(dev, steps, warmup, n_env=BATCH):
 def _served_entry(srv, lat, wall, offered):
     sk = srv.last_kkt
     return {"offered_req_per_s": offered, "completed_req_per_s": len(lat) / wall, "requests": int(len(lat)),
-            "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)), "p99": 1e3 * float(np.percentile(lat, 99))},
+            "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)), "p99": 1e3 * float(np.percentile(lat, 99)),
+                           "p999": 1e3 * float(np.percentile(lat, 99.9)), "max": 1e3 * float(np.max(lat))},
+            "frac_over_2ms": float((lat > 2e-3).mean()),
             "kkt_frac_le_1e-5": float((sk <= 1e-5).mean()),
             "nan_status": int(((srv.last_status & 1) != 0).sum())}
+
+
+def lone_latency(dev, opts, horizons=(50, 100, 200), reps=10):
+    """Latency of one lone solve (batch 1, CUDA events around the launch) of
+    the roll-pitch-yaw quadruped and the biped: one warp per instance (the
+    plain path's kernel) and the time-parallel team kernel (8 warps)."""
+    import torch
+    from mpx_gb300 import problem as P
+    from mpx_gb300.solver import Solver
+    out = {}
+    for name, make in (("quadruped", lambda N: P.quadruped_workload(1, horizons=(N,), seed=3, model=P.MODEL_SRBD_RPY12,
+                                                                   v_range=(-1, 1), random_phase=True)),
+                       ("biped", lambda N: P.biped_workload(1, horizons=(N,), seed=3))):
+        for N in horizons:
+            wl = make(N)
+            row = {}
+            for mode, kw in (("one_warp", {}), ("team8", dict(team_warps=8, team_min_horizon=8))):
+                s = Solver(wl.desc, dataclasses.replace(opts, **kw), n_max=N, batch_max=1, device=dev)
+                ins = s.prepare(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+                io = s.io(*ins, s.empty_outputs(1))
+                st = torch.cuda.current_stream(dev)
+                ts = []
+                for rep in range(reps + 2):
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(st)
+                    assert s.L.mpxg_solve(s.handle, ctypes.c_void_p(st.cuda_stream), ctypes.byref(io)) == 0
+                    b.record(st)
+                    torch.cuda.synchronize()
+                    if rep >= 2:
+                        ts.append(a.elapsed_time(b))
+                row[mode] = float(np.median(ts))
+                s.close()
+            row["speedup"] = row["one_warp"] / row["team8"]
+            out["%s_N%d_ms" % (name, N)] = row
+    return out
 
 
 def run_served(dev, opts):
@@ -353,8 +391,10 @@ def run_served(dev, opts):
     stream's steady state rather than a cold start of every episode."""
     from mpx_gb300.server import EpisodeStream, MPCServer, default_models, served_workload
     out = {}
-    # config 3: the mixed stream, 200-tick episodes with state drift
-    srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=opts, drift_std=0.01, streams=32,
+    # config 3: the mixed stream, 200-tick episodes with state drift; horizons of 64 and more are solved by
+    # the time-parallel team kernel (8 warps per instance)
+    team_opts = dataclasses.replace(opts, team_warps=8, team_min_horizon=64)
+    srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=team_opts, drift_std=0.01, streams=32,
                     device=dev)
     es = EpisodeStream(srv, seed=1)
     launches0 = None
@@ -368,7 +408,8 @@ def run_served(dev, opts):
     e["workload"] = ("Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, alternating), "
                      "N uniform in [20, 200], 200-tick episodes at staggered ages (ended episodes are replaced by "
                      "cold ones), state drift N(0, 0.01^2) per tick, 8 GB admission budget, 32 streams; 0.5 s "
-                     "warm-up of the same episodes, then 2 s measured")
+                     "warm-up of the same episodes, then 2 s measured; horizons >= 64 on the time-parallel team "
+                     "kernel (8 warps per instance), shorter ones one warp per instance")
     out.update(e)
     es.close()
     srv.close()
@@ -610,6 +651,9 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_served and not args.profile and rank == 0:
         served = run_served(dev, opts)
 
+    # ---------------- one lone solve: one warp vs the time-parallel team kernel
+    lone = lone_latency(dev, opts) if (not args.profile and rank == 0) else None
+
     # ---------------- end to end through the drop-in wrapper API (reference model and config)
     dropin = None
     if not args.profile and rank == 0 and not args.no_dropin:
@@ -674,6 +718,7 @@ def run_ours(args, rank, world, local_rank):
                  "frac_with_model": (flops + model_flops) / (solve_avg / 1000.0) / 1e12 / fp32_nominal},
         "n50": n50,
         "fp64_error": fp64,
+        "lone_solve_latency_ms": lone,
         "e2e_dropin": dropin,
         "vjp": vjp,
         "served": served,

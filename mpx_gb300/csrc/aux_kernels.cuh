@@ -336,8 +336,12 @@ __global__ void gait_tables_kernel(mpxg_gait_args g, int nx, int nu, int legs, i
 // (one block).  Entries with an invalid horizon go last.  Serving the
 // persistent grid's queue longest-first shortens the tail of a batch whose
 // horizons differ (list scheduling, longest processing time first).
+//
+// n_long (optional) receives the number of entries with a horizon of at least
+// split_h: the queue prefix the time-parallel team kernel takes.
 __global__ void __launch_bounds__(1024) order_by_horizon_kernel(int batch, int n_max, const int* __restrict__ slot,
-                                                                const int* __restrict__ horizon, int* __restrict__ order) {
+                                                                const int* __restrict__ horizon, int* __restrict__ order,
+                                                                int split_h = 0, int* __restrict__ n_long = nullptr) {
   extern __shared__ int bins[];       // n_max + 1 bins: bin j holds horizon n_max - j; bin n_max: invalid
   __shared__ int warp_tot[32];
   const int nb = n_max + 1;
@@ -372,6 +376,9 @@ __global__ void __launch_bounds__(1024) order_by_horizon_kernel(int batch, int n
   __syncthreads();
   int run = (wid > 0 ? warp_tot[wid - 1] : 0) + incl - local;
   for (int j = lo; j < hi; ++j) { const int c = bins[j]; bins[j] = run; run += c; }
+  __syncthreads();
+  if (n_long && threadIdx.x == 0)  // bins now hold start offsets; horizon h sits in bin n_max - h
+    *n_long = (split_h < 1) ? batch : (split_h > n_max ? 0 : bins[n_max - split_h + 1]);
   __syncthreads();
   for (int i = threadIdx.x; i < batch; i += blockDim.x) {
     const int h = horizon[slot ? slot[i] : i];

@@ -25,6 +25,10 @@ struct SqpOps {
                         bool tput, cudaStream_t st);
   cudaError_t (*launch_vjp)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks, int wpb,
                             cudaStream_t st);
+  // time-parallel team kernel, W warps per instance (W = 8); occupancy of it
+  int (*team_resident_blocks)();
+  cudaError_t (*launch_team)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks,
+                             cudaStream_t st);
   cudaError_t (*launch_evaluate)(const ModelConst& mc, int batch, int n_max, const int* horizon, const float* x0,
                                  const float* X, const float* U, const float* reference, const float* parameter,
                                  const float* w, float* g, float* c, cudaStream_t st);

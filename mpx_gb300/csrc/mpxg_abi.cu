@@ -28,6 +28,8 @@ struct mpxg_handle {
   int num_sms = 0;
   int warps_per_block = 0, blocks_per_sm = 0, total_warps = 0;  // throughput variant (large batches)
   int blocks_per_sm_lat = 0;                                     // latency variant
+  int team_blocks = 0;                 // team kernel: resident blocks of 8 warps (0: no team path)
+  int team_min_horizon = 0;
   long long scratch_stride = 0;
   int n_slots = 0;                     // scratch slots: most warps resident at once
   float* scratch = nullptr;
@@ -154,6 +156,8 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (o->sqp_iters < 0 || o->ls_max_trials < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: bad options");
   if (o->warps_per_block < 0 || o->warps_per_block > 4 || o->blocks_per_sm < 0)
     return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: warps_per_block must be 0..4 (128-thread blocks)");
+  if (!(o->team_warps == 0 || o->team_warps == 1 || o->team_warps == 8) || o->team_min_horizon < 0)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: team_warps must be 0, 1 or 8 and team_min_horizon >= 0");
   if (!(d->dt > 0.0f) || !(d->mass > 0.0f)) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: dt and mass must be > 0");
   mpxg_handle* h = new mpxg_handle();
   h->desc = *d;
@@ -164,6 +168,11 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaDeviceGetAttribute"); }
   launch_geometry(d, o, &h->warps_per_block, &h->blocks_per_sm, &h->blocks_per_sm_lat);
   h->total_warps = h->num_sms * h->blocks_per_sm * h->warps_per_block;
+  if (o->team_warps == 8) {
+    // the team kernel needs at least 8 stages (one per warp)
+    h->team_min_horizon = std::max(o->team_min_horizon, 8);
+    h->team_blocks = h->num_sms * sqp_ops(d->model)->team_resident_blocks();
+  }
   h->scratch_stride = scratch_stride_for(d->model, d->n_max);
   h->n_slots = scratch_slots(d->model, h->warps_per_block, h->num_sms);
   const size_t bytes = (size_t)h->scratch_stride * sizeof(float) * (size_t)h->n_slots;
@@ -275,15 +284,33 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
     h->capture_next = (h->capture_next + 1) % mpxg_handle::kRing;
   }
   bp.counter = h->counters + (size_t)r * mpxg_handle::kCounterStride;
-  cudaError_t e = cudaMemsetAsync(bp.counter, 0, sizeof(int), st);
+  cudaError_t e = cudaMemsetAsync(bp.counter, 0, 3 * sizeof(int), st);  // warp queue, team queue, split
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
-  if (io->horizon && io->batch > h->total_warps) {  // more instances than warps: longest horizons first
+  // time-parallel team path for the long horizons (by horizon alone)
+  const bool team = h->team_blocks > 0 && h->team_min_horizon <= h->desc.n_max;
+  if (io->horizon && (io->batch > h->total_warps || team)) {  // longest horizons first (and the team's share)
     int* order = h->orders + (size_t)r * h->desc.batch_max;
     order_by_horizon_kernel<<<1, 1024, (size_t)(h->desc.n_max + 1) * sizeof(int), st>>>(
-        io->batch, h->desc.n_max, io->slot, io->horizon, order);
+        io->batch, h->desc.n_max, io->slot, io->horizon, order, team ? h->team_min_horizon : 0,
+        team ? bp.counter + 2 : nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "order_by_horizon_kernel launch");
     bp.order = order;
+  }
+  if (team) {
+    BatchPtrs tb = bp;
+    tb.split = io->horizon ? bp.counter + 2 : nullptr;  // no horizons: every instance has n_max >= the minimum
+    const int blocks = std::min(io->batch, h->team_blocks);
+    e = sqp_ops(h->desc.model)->launch_team(h->mc, h->sp, tb, blocks, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "sqp_team_kernel launch");
+    if (!io->horizon) {  // every instance went to the team kernel
+      if (!eager) return MPXG_OK;
+      e = cudaEventRecord(h->ring_ev[r], st);
+      if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
+      h->ring_used[r] = true;
+      return MPXG_OK;
+    }
+    bp.split = bp.counter + 2;
   }
   const int wpb = h->warps_per_block;
   // more instances than the latency variant's resident warps: throughput variant

@@ -59,6 +59,10 @@ struct BatchPtrs {
   // Optional processing order of the batch entries (longest horizon first):
   // the i-th instance taken from the work queue is batch entry order[i].
   const int* order = nullptr;
+  // Queue split between the time-parallel team kernel (sqp_team.cuh), which
+  // takes queue entries [0, *split), and this kernel, which then takes
+  // [*split, batch) (null: this kernel takes the whole queue).
+  const int* split = nullptr;
   // Vector-Jacobian product mode (sqp_vjp_kernel): cotangents gX, gU of the
   // converged X, U in; adjoint solution wX, wU, wL and the gradients with
   // respect to x0 and to the state reference out.
@@ -447,8 +451,12 @@ __device__ __forceinline__ float merit_diff_stage(const ModelConst& mc, int t, i
 // Eliminate the pivot block S = {s0..s0+3} from the column this lane holds (h):
 // rows S <- D^-1 h[S], other rows h[i] -= H[i,S] D^-1 h[S], with D = H[S,S]
 // (SPD) factored by Cholesky on every lane.
-template <int NZ>
-__device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT, int* status) {
+//
+// EXTRA: the lane also carries a second column v of which only the control
+// rows [U0, U0 + NU) are eliminated (after all pivot blocks they hold
+// Quu^-1 v; the other rows are not needed by the caller).
+template <int NZ, bool EXTRA = false, int U0 = 0, int NU = 0>
+__device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT, int* status, float* v = nullptr) {
   __syncwarp();
   if (lane >= s0 && lane < s0 + 4) {
     const int k = lane - s0;
@@ -497,6 +505,34 @@ __device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT,
     for (int k = a + 1; k < 4; ++k) v -= L[k][a] * y[k];
     y[a] = v * il[a];
   }
+  if (EXTRA) {
+    float yv[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      float vv = 0.0f;
+#pragma unroll
+      for (int i = U0; i < U0 + NU; ++i) vv = (i == s0 + a) ? v[i] : vv;
+#pragma unroll
+      for (int k = 0; k < a; ++k) vv -= L[a][k] * yv[k];
+      yv[a] = vv * il[a];
+    }
+#pragma unroll
+    for (int a = 3; a >= 0; --a) {
+      float vv = yv[a];
+#pragma unroll
+      for (int k = a + 1; k < 4; ++k) vv -= L[k][a] * yv[k];
+      yv[a] = vv * il[a];
+    }
+#pragma unroll
+    for (int i = U0; i < U0 + NU; ++i) {
+      const float4 hc = *reinterpret_cast<const float4*>(CT + i * 4);
+      const float upd = hc.x * yv[0] + hc.y * yv[1] + hc.z * yv[2] + hc.w * yv[3];
+      float yi = 0.0f;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) yi = (i == s0 + a) ? yv[a] : yi;
+      v[i] = (i >= s0 && i < s0 + 4) ? yi : v[i] - upd;
+    }
+  }
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const float4 hc = *reinterpret_cast<const float4*>(CT + i * 4);
@@ -506,6 +542,378 @@ __device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT,
     for (int a = 0; a < 4; ++a) yi = (i == s0 + a) ? y[a] : yi;
     h[i] = (i >= s0 && i < s0 + 4) ? yi : h[i] - upd;
   }
+}
+
+// ----------------------------------------------------------------- chunk elements
+// Accumulators of a time-parallel chunk's element while its Riccati sweep
+// runs from a zero terminal cost (see riccati_sweep, ELEM = true): the
+// closed-loop affine map x_e = Phi x_t + phi from stage t to the chunk end and
+// the Gramian G = sum Phi_{t+1->e} B Quu^-1 B' Phi_{t+1->e}'.  Column-major,
+// column stride FS.  Also the outputs of the chunk combination (sqp_team.cuh).
+template <class M>
+struct __align__(16) ElemSmem {
+  typedef Dims<M> D;
+  float Phi[2][D::NX * D::FS];      // Phi_{t+1->e}, double-buffered
+  float PB[D::NU * D::FS];          // Phi_{t+1->e} B_t
+  float G[D::NX * D::FS];           // Gramian
+  float phi[D::FS];                 // affine part of the map
+  float Z[(D::NX + 1) * D::FS];     // [Z_Phi | z]: the chunk's end state as a map of its start state
+  float Pin[D::NP * D::LDP];        // true value function at the chunk's start (WarpSmem::P layout)
+  int cur;                          // buffer of Phi holding the map after the sweep
+};
+
+
+// ----------------------------------------------------------------- phase 2
+// Terminal value function (P_N, p_N): the terminal cost's Gauss-Newton block
+// and gradient, into the warp's shared P (and the scratch when STORE).
+template <class M, bool STORE>
+__device__ __forceinline__ void riccati_terminal(int N, WarpSmem<M>& sm, const Scratch<M>& s, int lane) {
+  typedef Dims<M> D;
+  constexpr int NX = D::NX, NP = D::NP, LDP = D::LDP;
+  const int j = lane;
+  const float* GN = s.G + (size_t)N * D::GS;
+  if (j < NX) {
+    float col[NP];
+#pragma unroll
+    for (int i = 0; i < NX; ++i) col[i] = 0.0f;
+    if (D::QB && j >= M::QOFF && j < M::QOFF + 4) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) col[M::QOFF + k] = GN[D::G_QQ + (j - M::QOFF) * 4 + k];
+    } else {
+      const float wj = sm.w[M::wrow(j)];
+#pragma unroll
+      for (int i = 0; i < NX; ++i) col[i] = (i == j) ? wj : col[i];
+    }
+    const float gj = GN[D::G_GRAD + j];
+    col[NX] = gj;
+    float* Pn = s.P + (size_t)N * NP * LDP;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      sm.P[j * LDP + i] = col[i];
+      if (STORE) Pn[j * LDP + i] = col[i];
+    }
+    sm.P[NX * LDP + j] = gj;
+    if (STORE) Pn[NX * LDP + j] = gj;
+  }
+  if (j == 0) {
+    sm.P[NX * LDP + NX] = 0.0f;
+    if (STORE) s.P[(size_t)N * NP * LDP + NX * LDP + NX] = 0.0f;
+  }
+  __syncwarp();
+}
+
+// Backward Riccati sweep over stages hi-1 .. lo from the value function in
+// the warp's shared P (the value at stage hi).  Lane j owns column j of the
+// augmented stage matrix H = G + F' P F, F = [A B c; 0 0 1]; the control
+// pivots are eliminated by 4x4 block Gauss-Jordan, which leaves the value
+// function of stage t (into the shared P) and the gains.
+//   STORE: write gains K = [K | k], the closed loop (A + BK, Bk + c) over F's
+//          first columns, and P to the scratch (the forward sweep reads them).
+//   ELEM:  accumulate the chunk element in es (ElemSmem): Phi, phi, G of the
+//          map from stage t to hi under this sweep's policy.  On entry the
+//          caller has set es->Phi[0] = I; on return es->G, es->phi and
+//          es->cur hold the result.
+template <class M, bool STORE, bool ELEM>
+__device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int hi, WarpSmem<M>& sm, const Scratch<M>& s,
+                                              ElemSmem<M>* es, int* status, int lane) {
+  typedef Dims<M> D;
+  constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP, FS = D::FS;
+  constexpr int LD = D::LD;
+  const int j = lane;
+  if (hi <= lo) return;
+  int cur = 0;
+  float gcol[FS];  // ELEM: column j of G (state lanes), phi (lane JA)
+#pragma unroll
+  for (int i = 0; i < FS; ++i) gcol[i] = 0.0f;
+  BlockRegs<NZ * FS> fpre;
+  BlockRegs<D::GS> gpre;
+  fpre.load(s.F + (size_t)(hi - 1) * NZ * FS, lane);
+  gpre.load(s.G + (size_t)(hi - 1) * D::GS, lane);
+  for (int t = hi - 1; t >= lo; --t) {
+    // ---- stage t's F columns and cost data into shared memory; prefetch t-1
+    fpre.template store_cols<FS, LDP>(sm.F, lane);
+    gpre.template store_cols<D::GS, D::GS>(sm.G, lane);
+    if (t > lo) {
+      fpre.load(s.F + (size_t)(t - 1) * NZ * FS, lane);
+      gpre.load(s.G + (size_t)(t - 1) * D::GS, lane);
+    }
+    __syncwarp();
+    const float* Gt = sm.G;
+    // ---- column j of F and of the cost model G
+    float fcol[NP], h[NZ];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) fcol[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NZ; ++i) h[i] = 0.0f;
+    if (j < NZ) {
+#pragma unroll
+      for (int q = 0; q < FS / 4; ++q) {
+        const float4 v = *reinterpret_cast<const float4*>(sm.F + j * LDP + 4 * q);
+        if (4 * q < NX) fcol[4 * q] = v.x;
+        if (4 * q + 1 < NX) fcol[4 * q + 1] = v.y;
+        if (4 * q + 2 < NX) fcol[4 * q + 2] = v.z;
+        if (4 * q + 3 < NX) fcol[4 * q + 3] = v.w;
+      }
+    }
+    fcol[NX] = (j == JA) ? 1.0f : 0.0f;
+    if (j < NX) {
+      if (D::QB && j >= M::QOFF && j < M::QOFF + 4) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) h[M::QOFF + k] = Gt[D::G_QQ + (j - M::QOFF) * 4 + k];
+      } else {
+        const float wj = sm.w[M::wrow(j)];
+#pragma unroll
+        for (int i = 0; i < NX; ++i) h[i] = (i == j) ? wj : h[i];
+      }
+      h[JA] = Gt[D::G_GRAD + j];
+    } else if (j < JA) {
+      const int a = j - NX, leg = a / LD, c = a - LD * leg;
+      float hb[LD];
+#pragma unroll
+      for (int r2 = 0; r2 < LD; ++r2) hb[r2] = Gt[D::G_HB + (leg * LD + c) * LD + r2];
+      const float wa = sm.w[12 + a];
+#pragma unroll
+      for (int bb = 0; bb < NU; ++bb) {
+        float v = (bb == a) ? wa : 0.0f;
+#pragma unroll
+        for (int r2 = 0; r2 < LD; ++r2) v += (bb == LD * leg + r2) ? hb[r2] : 0.0f;
+        h[NX + bb] = v;
+      }
+      h[JA] = Gt[D::G_GRAD + j];
+    } else if (j == JA) {
+#pragma unroll
+      for (int i = 0; i < JA; ++i) h[i] = Gt[D::G_GRAD + i];
+    }
+    if (j == JA) sm.F[JA * LDP + NX] = 1.0f;  // the affine column's last row
+    __syncwarp();
+    // ---- T = P F[:, j];  H[:, j] = G[:, j] + F^T T
+    float tv[LDP];
+#pragma unroll
+    for (int i = 0; i < LDP; ++i) tv[i] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      const float fk = fcol[k];
+#pragma unroll
+      for (int q = 0; q < LDP / 4; ++q) {
+        const float4 pv = *reinterpret_cast<const float4*>(sm.P + k * LDP + 4 * q);
+        tv[4 * q] += pv.x * fk; tv[4 * q + 1] += pv.y * fk; tv[4 * q + 2] += pv.z * fk; tv[4 * q + 3] += pv.w * fk;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NZ; ++i) {
+      float a = h[i];
+#pragma unroll
+      for (int q = 0; q < LDP / 4; ++q) {
+        const float4 fv = *reinterpret_cast<const float4*>(sm.F + i * LDP + 4 * q);
+        a += fv.x * tv[4 * q] + fv.y * tv[4 * q + 1] + fv.z * tv[4 * q + 2] + fv.w * tv[4 * q + 3];
+      }
+      h[i] = a;
+    }
+#pragma unroll
+    for (int a = NX; a < JA; ++a)
+      if (a == j) h[a] += sp.reg;
+    // ---- chunk element: Phi B_t, and row j of it as an extra right-hand side of the elimination
+    float v[NZ];
+    if (ELEM) {
+      const float* Phc = es->Phi[cur];
+      if (j >= NX && j < JA) {
+        float pb[FS];
+#pragma unroll
+        for (int i = 0; i < FS; ++i) pb[i] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < NX; ++k) {
+          const float fk = fcol[k];
+#pragma unroll
+          for (int q = 0; q < FS / 4; ++q) {
+            const float4 pv = *reinterpret_cast<const float4*>(Phc + k * FS + 4 * q);
+            pb[4 * q] += pv.x * fk; pb[4 * q + 1] += pv.y * fk; pb[4 * q + 2] += pv.z * fk; pb[4 * q + 3] += pv.w * fk;
+          }
+        }
+        st_vec<FS>(es->PB + (j - NX) * FS, pb);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NZ; ++i) v[i] = (i >= NX && i < JA && j < NX) ? es->PB[(i >= NX && i < JA ? i - NX : 0) * FS + (j < NX ? j : 0)] : 0.0f;
+    }
+    // ---- block Gauss-Jordan elimination of the control pivots
+#pragma unroll
+    for (int s0 = NX; s0 < JA; s0 += 4) gj_block4<NZ, ELEM, NX, NU>(h, s0, lane, sm.CT, status, v);
+    // ---- gains, closed loop, new value function
+    float* Kt = s.K + (size_t)t * NP * NU;
+    float* Fo = s.F + (size_t)t * NZ * FS;
+    if (j < NX || j == JA) {
+      const int col = (j == JA) ? NX : j;
+      float kc[NU];
+#pragma unroll
+      for (int a = 0; a < NU; ++a) kc[a] = -h[NX + a];
+      if (STORE) st_vec<NU>(Kt + col * NU, kc);
+      // closed loop: (A + B K)[:, j] for state lanes, B k + c for the affine lane
+      float cl[FS];
+#pragma unroll
+      for (int i = 0; i < FS; ++i) cl[i] = (i < NX) ? fcol[i < NX ? i : 0] : 0.0f;
+#pragma unroll
+      for (int a = 0; a < NU; ++a)
+#pragma unroll
+        for (int q = 0; q < FS / 4; ++q) {
+          const float4 bv = *reinterpret_cast<const float4*>(sm.F + (NX + a) * LDP + 4 * q);
+          cl[4 * q] += bv.x * kc[a]; cl[4 * q + 1] += bv.y * kc[a];
+          cl[4 * q + 2] += bv.z * kc[a]; cl[4 * q + 3] += bv.w * kc[a];
+        }
+#pragma unroll
+      for (int i = NX; i < FS; ++i) cl[i] = 0.0f;
+      const int slot = (j == JA) ? NX : j;  // A+BK overwrites A, Bk+c goes to the first B slot
+      if (STORE) st_vec<FS>(Fo + slot * FS, cl);
+#pragma unroll
+      for (int i = 0; i < NX; ++i) sm.Praw[col * LDP + i] = h[i];
+      if (ELEM) {  // Phi <- Phi (A + B K), phi <- phi + Phi (B k + c), G <- G + (Phi B) Quu^-1 (Phi B)'
+        const float* Phc = es->Phi[cur];
+        float pn[FS];
+#pragma unroll
+        for (int i = 0; i < FS; ++i) pn[i] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < NX; ++k) {
+          const float ck = cl[k];
+#pragma unroll
+          for (int q = 0; q < FS / 4; ++q) {
+            const float4 pv = *reinterpret_cast<const float4*>(Phc + k * FS + 4 * q);
+            pn[4 * q] += pv.x * ck; pn[4 * q + 1] += pv.y * ck; pn[4 * q + 2] += pv.z * ck; pn[4 * q + 3] += pv.w * ck;
+          }
+        }
+        if (j < NX) {
+          st_vec<FS>(es->Phi[cur ^ 1] + j * FS, pn);
+#pragma unroll
+          for (int a = 0; a < NU; ++a) {
+            const float ya = v[NX + a];
+#pragma unroll
+            for (int q = 0; q < FS / 4; ++q) {
+              const float4 bv = *reinterpret_cast<const float4*>(es->PB + a * FS + 4 * q);
+              gcol[4 * q] += bv.x * ya; gcol[4 * q + 1] += bv.y * ya; gcol[4 * q + 2] += bv.z * ya;
+              gcol[4 * q + 3] += bv.w * ya;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < FS; ++i) gcol[i] += pn[i];  // lane JA carries phi in gcol
+        }
+      }
+    }
+    if (ELEM) cur ^= 1;
+    __syncwarp();
+    {
+      float* Pt = s.P + (size_t)t * NP * LDP;
+      if (j < NX) {
+        float pc[LDP];
+#pragma unroll
+        for (int i = 0; i < LDP; ++i) pc[i] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) pc[i] = 0.5f * (h[i] + sm.Praw[i * LDP + j]);
+        pc[NX] = 0.5f * (h[JA] + sm.Praw[NX * LDP + j]);
+#pragma unroll
+        for (int i = 0; i < NP; ++i) sm.P[j * LDP + i] = pc[i];
+        sm.P[NX * LDP + j] = pc[NX];
+        if (STORE) {
+          st_vec<LDP>(Pt + j * LDP, pc);
+          Pt[NX * LDP + j] = pc[NX];
+        }
+      } else if (j < LDP) {
+        if (STORE) Pt[NX * LDP + j] = 0.0f;  // [NX][NX] and the padding rows of column NX
+        if (j == NX) sm.P[NX * LDP + NX] = 0.0f;
+      }
+    }
+    __syncwarp();
+  }
+  if (ELEM) {
+    if (j < NX) st_vec<FS>(es->G + j * FS, gcol);
+    if (j == JA) st_vec<FS>(es->phi, gcol);
+    if (j == 0) es->cur = cur;
+    __syncwarp();
+  }
+  (void)LD;
+}
+
+// ----------------------------------------------------------------- phase 3
+// Forward sweep over stages lo .. hi from the state step in sm.dx (set by
+// the caller): dx_{t+1} = (A+BK) dx_t + (Bk+c), du_t = K dx_t + k and the
+// costates lam_t = P_t dx_t + p_t into the scratch, plus the merit sums.
+// c_init is the defect paired with V at stage lo (lane i < n holds row i).
+// last: the sweep also writes the costate of stage hi (the horizon's end);
+// otherwise stage hi belongs to the next chunk.
+template <class M>
+__device__ __forceinline__ void forward_sweep(int lo, int hi, bool last, float c_init, const float* V, WarpSmem<M>& sm,
+                                              const Scratch<M>& s, int lane, double* a_gd, double* a_lc,
+                                              double* a_vc, double* a_cs) {
+  typedef Dims<M> D;
+  constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP, FS = D::FS;
+  constexpr int RS = D::RS;
+  float c_cur = c_init;
+  BlockRegs<NP * LDP> ppre;
+  BlockRegs<NP * NU> kpre;
+  BlockRegs<NZ * FS> fpre3;
+  BlockRegs<D::GS> gpre3;
+  ppre.load(s.P + (size_t)lo * NP * LDP, lane);
+  kpre.load(s.K + (size_t)lo * NP * NU, lane);
+  fpre3.load(s.F + (size_t)lo * NZ * FS, lane);
+  gpre3.load(s.G + (size_t)lo * D::GS, lane);
+  const int tend = last ? hi : hi - 1;  // last stage whose costate this sweep writes
+  float vnext = (lane < NX) ? V[lo * NX + lane] : 0.0f;  // V of the next stage, loaded a stage ahead
+  for (int t = lo; t <= tend; ++t) {
+    const float vt = vnext;
+    if (lane < NX && t + 1 <= tend) vnext = V[(t + 1) * NX + lane];
+    // ---- stage t's value function, gains, closed loop and cost data; prefetch t+1
+    ppre.template store_cols<LDP, LDP>(sm.P, lane);
+    gpre3.template store_cols<D::GS, D::GS>(sm.G, lane);
+    if (t < hi) {
+      kpre.template store_cols<NU, NU>(sm.Praw, lane);
+      fpre3.template store_cols<FS, LDP>(sm.F, lane);
+    }
+    if (t + 1 <= tend) {
+      ppre.load(s.P + (size_t)(t + 1) * NP * LDP, lane);
+      gpre3.load(s.G + (size_t)(t + 1) * D::GS, lane);
+    }
+    if (t + 1 < hi) {
+      kpre.load(s.K + (size_t)(t + 1) * NP * NU, lane);
+      fpre3.load(s.F + (size_t)(t + 1) * NZ * FS, lane);
+    }
+    __syncwarp();
+    if (lane < NX) {
+      const float dxi = sm.dx[lane];
+      float lam = sm.P[lane * LDP + NX];
+#pragma unroll
+      for (int k = 0; k < NX; ++k) lam += sm.P[lane * LDP + k] * sm.dx[k];
+      *a_lc += (double)((lam - 2.0f * vt) * c_cur);
+      *a_vc += (double)(vt * c_cur);
+      *a_cs += (double)(c_cur * c_cur);
+      *a_gd += (double)(sm.G[D::G_GRAD + lane] * dxi);
+      s.L[t * NX + lane] = lam;
+      s.dX[t * NX + lane] = dxi;
+    }
+    if (t == hi) break;
+    if (lane < NX || lane == JA) {
+      const int col = (lane == JA) ? NX : lane;
+      const float sc = (lane == JA) ? 1.0f : sm.dx[col];
+      float* rw = sm.red + col * RS;
+#pragma unroll
+      for (int a = 0; a < NU; ++a) rw[a] = sm.Praw[col * NU + a] * sc;
+#pragma unroll
+      for (int i = 0; i < NX; ++i) rw[NU + i] = sm.F[col * LDP + i] * sc;
+    }
+    __syncwarp();
+    float sum = 0.0f;
+    if (lane < NU) {
+#pragma unroll
+      for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + lane];
+      s.dU[t * NU + lane] = sum;
+      *a_gd += (double)(sm.G[D::G_GRAD + NX + lane] * sum);
+    } else if (lane >= 16 && lane < 16 + NX) {
+#pragma unroll
+      for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + NU + (lane - 16)];
+    }
+    if (lane < NX) c_cur = sm.F[JA * LDP + lane];  // defect of stage t pairs with V_{t+1}
+    __syncwarp();
+    if (lane >= 16 && lane < 16 + NX) sm.dx[lane - 16] = sum;
+    __syncwarp();
+  }
+  __syncwarp();
 }
 
 // ----------------------------------------------------------------- one instance
@@ -579,248 +987,18 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
       __syncwarp();
     }
     // ================================================ phase 2: backward Riccati
-    {
-      const float* GN = s.G + (size_t)N * D::GS;
-      if (j < NX) {
-        float col[NP];
-#pragma unroll
-        for (int i = 0; i < NX; ++i) col[i] = 0.0f;
-        if (D::QB && j >= M::QOFF && j < M::QOFF + 4) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) col[M::QOFF + k] = GN[D::G_QQ + (j - M::QOFF) * 4 + k];
-        } else {
-          const float wj = sm.w[M::wrow(j)];
-#pragma unroll
-          for (int i = 0; i < NX; ++i) col[i] = (i == j) ? wj : col[i];
-        }
-        const float gj = GN[D::G_GRAD + j];
-        col[NX] = gj;
-        float* Pn = s.P + (size_t)N * NP * LDP;
-#pragma unroll
-        for (int i = 0; i < NP; ++i) { sm.P[j * LDP + i] = col[i]; Pn[j * LDP + i] = col[i]; }
-        sm.P[NX * LDP + j] = gj;
-        Pn[NX * LDP + j] = gj;
-      }
-      if (j == 0) { sm.P[NX * LDP + NX] = 0.0f; s.P[(size_t)N * NP * LDP + NX * LDP + NX] = 0.0f; }
-      __syncwarp();
-    }
+    riccati_terminal<M, true>(N, sm, s, lane);
     // whole-warp fence: phase-1 stores are complete before the block loads
     __threadfence_block();
     __syncwarp();
-    BlockRegs<NZ * FS> fpre;
-    BlockRegs<D::GS> gpre;
-    fpre.load(s.F + (size_t)(N - 1) * NZ * FS, lane);
-    gpre.load(s.G + (size_t)(N - 1) * D::GS, lane);
-    for (int t = N - 1; t >= 0; --t) {
-      // ---- stage t's F columns and cost data into shared memory; prefetch t-1
-      fpre.template store_cols<FS, LDP>(sm.F, lane);
-      gpre.template store_cols<D::GS, D::GS>(sm.G, lane);
-      if (t > 0) {
-        fpre.load(s.F + (size_t)(t - 1) * NZ * FS, lane);
-        gpre.load(s.G + (size_t)(t - 1) * D::GS, lane);
-      }
-      __syncwarp();
-      const float* Gt = sm.G;
-      // ---- column j of F and of the cost model G
-      float fcol[NP], h[NZ];
-#pragma unroll
-      for (int i = 0; i < NP; ++i) fcol[i] = 0.0f;
-#pragma unroll
-      for (int i = 0; i < NZ; ++i) h[i] = 0.0f;
-      if (j < NZ) {
-#pragma unroll
-        for (int q = 0; q < FS / 4; ++q) {
-          const float4 v = *reinterpret_cast<const float4*>(sm.F + j * LDP + 4 * q);
-          if (4 * q < NX) fcol[4 * q] = v.x;
-          if (4 * q + 1 < NX) fcol[4 * q + 1] = v.y;
-          if (4 * q + 2 < NX) fcol[4 * q + 2] = v.z;
-          if (4 * q + 3 < NX) fcol[4 * q + 3] = v.w;
-        }
-      }
-      fcol[NX] = (j == JA) ? 1.0f : 0.0f;
-      if (j < NX) {
-        if (D::QB && j >= M::QOFF && j < M::QOFF + 4) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) h[M::QOFF + k] = Gt[D::G_QQ + (j - M::QOFF) * 4 + k];
-        } else {
-          const float wj = sm.w[M::wrow(j)];
-#pragma unroll
-          for (int i = 0; i < NX; ++i) h[i] = (i == j) ? wj : h[i];
-        }
-        h[JA] = Gt[D::G_GRAD + j];
-      } else if (j < JA) {
-        const int a = j - NX, leg = a / LD, c = a - LD * leg;
-        float hb[LD];
-#pragma unroll
-        for (int r2 = 0; r2 < LD; ++r2) hb[r2] = Gt[D::G_HB + (leg * LD + c) * LD + r2];
-        const float wa = sm.w[12 + a];
-#pragma unroll
-        for (int bb = 0; bb < NU; ++bb) {
-          float v = (bb == a) ? wa : 0.0f;
-#pragma unroll
-          for (int r2 = 0; r2 < LD; ++r2) v += (bb == LD * leg + r2) ? hb[r2] : 0.0f;
-          h[NX + bb] = v;
-        }
-        h[JA] = Gt[D::G_GRAD + j];
-      } else if (j == JA) {
-#pragma unroll
-        for (int i = 0; i < JA; ++i) h[i] = Gt[D::G_GRAD + i];
-      }
-      if (j == JA) sm.F[JA * LDP + NX] = 1.0f;  // the affine column's last row
-      __syncwarp();
-      // ---- T = P F[:, j];  H[:, j] = G[:, j] + F^T T
-      float tv[LDP];
-#pragma unroll
-      for (int i = 0; i < LDP; ++i) tv[i] = 0.0f;
-#pragma unroll
-      for (int k = 0; k < NP; ++k) {
-        const float fk = fcol[k];
-#pragma unroll
-        for (int q = 0; q < LDP / 4; ++q) {
-          const float4 pv = *reinterpret_cast<const float4*>(sm.P + k * LDP + 4 * q);
-          tv[4 * q] += pv.x * fk; tv[4 * q + 1] += pv.y * fk; tv[4 * q + 2] += pv.z * fk; tv[4 * q + 3] += pv.w * fk;
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < NZ; ++i) {
-        float a = h[i];
-#pragma unroll
-        for (int q = 0; q < LDP / 4; ++q) {
-          const float4 fv = *reinterpret_cast<const float4*>(sm.F + i * LDP + 4 * q);
-          a += fv.x * tv[4 * q] + fv.y * tv[4 * q + 1] + fv.z * tv[4 * q + 2] + fv.w * tv[4 * q + 3];
-        }
-        h[i] = a;
-      }
-#pragma unroll
-      for (int a = NX; a < JA; ++a)
-        if (a == j) h[a] += sp.reg;
-      // ---- block Gauss-Jordan elimination of the control pivots
-#pragma unroll
-      for (int s0 = NX; s0 < JA; s0 += 4) gj_block4<NZ>(h, s0, lane, sm.CT, &status);
-      // ---- gains, closed loop, new value function
-      float* Kt = s.K + (size_t)t * NP * NU;
-      float* Fo = s.F + (size_t)t * NZ * FS;
-      if (j < NX || j == JA) {
-        const int col = (j == JA) ? NX : j;
-        float kc[NU];
-#pragma unroll
-        for (int a = 0; a < NU; ++a) kc[a] = -h[NX + a];
-        st_vec<NU>(Kt + col * NU, kc);
-        // closed loop: (A + B K)[:, j] for state lanes, B k + c for the affine lane
-        float cl[FS];
-#pragma unroll
-        for (int i = 0; i < FS; ++i) cl[i] = (i < NX) ? fcol[i < NX ? i : 0] : 0.0f;
-#pragma unroll
-        for (int a = 0; a < NU; ++a)
-#pragma unroll
-          for (int q = 0; q < FS / 4; ++q) {
-            const float4 bv = *reinterpret_cast<const float4*>(sm.F + (NX + a) * LDP + 4 * q);
-            cl[4 * q] += bv.x * kc[a]; cl[4 * q + 1] += bv.y * kc[a];
-            cl[4 * q + 2] += bv.z * kc[a]; cl[4 * q + 3] += bv.w * kc[a];
-          }
-#pragma unroll
-        for (int i = NX; i < FS; ++i) cl[i] = 0.0f;
-        const int slot = (j == JA) ? NX : j;  // A+BK overwrites A, Bk+c goes to the first B slot
-        st_vec<FS>(Fo + slot * FS, cl);
-#pragma unroll
-        for (int i = 0; i < NX; ++i) sm.Praw[col * LDP + i] = h[i];
-      }
-      __syncwarp();
-      {
-        float* Pt = s.P + (size_t)t * NP * LDP;
-        if (j < NX) {
-          float pc[LDP];
-#pragma unroll
-          for (int i = 0; i < LDP; ++i) pc[i] = 0.0f;
-#pragma unroll
-          for (int i = 0; i < NX; ++i) pc[i] = 0.5f * (h[i] + sm.Praw[i * LDP + j]);
-          pc[NX] = 0.5f * (h[JA] + sm.Praw[NX * LDP + j]);
-#pragma unroll
-          for (int i = 0; i < NP; ++i) sm.P[j * LDP + i] = pc[i];
-          sm.P[NX * LDP + j] = pc[NX];
-          st_vec<LDP>(Pt + j * LDP, pc);
-          Pt[NX * LDP + j] = pc[NX];
-        } else if (j < LDP) {
-          Pt[NX * LDP + j] = 0.0f;  // [NX][NX] and the padding rows of column NX
-          if (j == NX) sm.P[NX * LDP + NX] = 0.0f;
-        }
-      }
-      __syncwarp();
-    }
+    riccati_sweep<M, true, false>(sp, 0, N, sm, s, nullptr, &status, lane);
     // ================================================ phase 3: forward sweep
     __threadfence_block();
     __syncwarp();
     double a_gd = 0.0, a_lc = 0.0, a_vc = 0.0, a_cs = 0.0;
-    float c_cur = 0.0f;
-    BlockRegs<NP * LDP> ppre;
-    BlockRegs<NP * NU> kpre;
-    BlockRegs<NZ * FS> fpre3;
-    BlockRegs<D::GS> gpre3;
-    ppre.load(s.P, lane);
-    kpre.load(s.K, lane);
-    fpre3.load(s.F, lane);
-    gpre3.load(s.G, lane);
-    if (lane < NX) {
-      c_cur = VJP ? 0.0f : x0[lane] - X[lane];
-      sm.dx[lane] = c_cur;
-    }
-    for (int t = 0; t <= N; ++t) {
-      // ---- stage t's value function, gains, closed loop and cost data; prefetch t+1
-      ppre.template store_cols<LDP, LDP>(sm.P, lane);
-      gpre3.template store_cols<D::GS, D::GS>(sm.G, lane);
-      if (t < N) {
-        kpre.template store_cols<NU, NU>(sm.Praw, lane);
-        fpre3.template store_cols<FS, LDP>(sm.F, lane);
-      }
-      if (t + 1 <= N) {
-        ppre.load(s.P + (size_t)(t + 1) * NP * LDP, lane);
-        gpre3.load(s.G + (size_t)(t + 1) * D::GS, lane);
-      }
-      if (t + 1 < N) {
-        kpre.load(s.K + (size_t)(t + 1) * NP * NU, lane);
-        fpre3.load(s.F + (size_t)(t + 1) * NZ * FS, lane);
-      }
-      __syncwarp();
-      if (lane < NX) {
-        const float dxi = sm.dx[lane];
-        float lam = sm.P[lane * LDP + NX];
-#pragma unroll
-        for (int k = 0; k < NX; ++k) lam += sm.P[lane * LDP + k] * sm.dx[k];
-        const float vt = V[t * NX + lane];
-        a_lc += (double)((lam - 2.0f * vt) * c_cur);
-        a_vc += (double)(vt * c_cur);
-        a_cs += (double)(c_cur * c_cur);
-        a_gd += (double)(sm.G[D::G_GRAD + lane] * dxi);
-        s.L[t * NX + lane] = lam;
-        s.dX[t * NX + lane] = dxi;
-      }
-      if (t == N) break;
-      if (lane < NX || lane == JA) {
-        const int col = (lane == JA) ? NX : lane;
-        const float sc = (lane == JA) ? 1.0f : sm.dx[col];
-        float* rw = sm.red + col * RS;
-#pragma unroll
-        for (int a = 0; a < NU; ++a) rw[a] = sm.Praw[col * NU + a] * sc;
-#pragma unroll
-        for (int i = 0; i < NX; ++i) rw[NU + i] = sm.F[col * LDP + i] * sc;
-      }
-      __syncwarp();
-      float sum = 0.0f;
-      if (lane < NU) {
-#pragma unroll
-        for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + lane];
-        s.dU[t * NU + lane] = sum;
-        a_gd += (double)(sm.G[D::G_GRAD + NX + lane] * sum);
-      } else if (lane >= 16 && lane < 16 + NX) {
-#pragma unroll
-        for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + NU + (lane - 16)];
-      }
-      if (lane < NX) c_cur = sm.F[JA * LDP + lane];  // defect of stage t pairs with V_{t+1}
-      __syncwarp();
-      if (lane >= 16 && lane < 16 + NX) sm.dx[lane - 16] = sum;
-      __syncwarp();
-    }
-    __syncwarp();
+    if (lane < NX) sm.dx[lane] = VJP ? 0.0f : x0[lane] - X[lane];
+    forward_sweep<M>(0, N, true, VJP ? 0.0f : (lane < NX ? x0[lane] - X[lane] : 0.0f), V, sm, s, lane, &a_gd, &a_lc,
+                     &a_vc, &a_cs);
     const double gd = warp_sum(a_gd), lc = warp_sum(a_lc), vc = warp_sum(a_vc), cs = warp_sum(a_cs);
     if (VJP) {  // adjoint solution and gradients out; no step is taken
       __threadfence_block();
@@ -961,12 +1139,13 @@ __device__ __forceinline__ void sqp_body(const ModelConst& mc, const SqpParams& 
     }
   }
   float* scr = bp.scratch + (size_t)slot * bp.scratch_stride;
+  const int q0 = bp.split ? *bp.split : 0;
   for (int done = 0; !done;) {
     int b = bp.single_instance;
     if (b < 0) {
       if (lane == 0) {
-        b = atomicAdd(bp.counter, 1);
-        if (bp.order && b < bp.batch) b = bp.order[b];
+        const int i = q0 + atomicAdd(bp.counter, 1);
+        b = (i < bp.batch) ? (bp.order ? bp.order[i] : i) : bp.batch;
       }
       b = __shfl_sync(0xffffffffu, b, 0);
       if (b >= bp.batch) break;

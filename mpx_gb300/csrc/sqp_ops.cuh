@@ -5,6 +5,7 @@
 #include "evaluate_kernel.cuh"
 #include "internal.h"
 #include "sqp_kernel.cuh"
+#include "sqp_team.cuh"
 
 namespace mpxg {
 
@@ -50,6 +51,29 @@ struct SqpLaunch {
     sqp_vjp_kernel<M><<<blocks, wpb * 32, smem, st>>>(mc, sp, bp);
     return cudaGetLastError();
   }
+  static constexpr int kTeamWarps = 8;
+  static int team_resident_blocks() {
+    int nb = 0;
+    const size_t smem = sizeof(TeamSmem<M, kTeamWarps>);
+    auto fn = sqp_team_kernel<M, kTeamWarps>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kTeamWarps, smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+    }
+    return nb > 0 ? nb : 1;
+  }
+  static cudaError_t launch_team(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks,
+                                 cudaStream_t st) {
+    const size_t smem = sizeof(TeamSmem<M, kTeamWarps>);
+    auto fn = sqp_team_kernel<M, kTeamWarps>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    fn<<<blocks, 32 * kTeamWarps, smem, st>>>(mc, sp, bp);
+    return cudaGetLastError();
+  }
   static cudaError_t launch_evaluate(const ModelConst& mc, int batch, int n_max, const int* horizon, const float* x0,
                                      const float* X, const float* U, const float* reference, const float* parameter,
                                      const float* w, float* g, float* c, cudaStream_t st) {
@@ -62,7 +86,7 @@ struct SqpLaunch {
   }
   static const SqpOps& ops() {
     static const SqpOps o = {sizeof(WarpSmem<M>), &scratch, &resident_blocks, &launch, &launch_vjp,
-                             &launch_evaluate};
+                             &team_resident_blocks, &launch_team, &launch_evaluate};
     return o;
   }
 };

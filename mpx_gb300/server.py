@@ -18,6 +18,7 @@ mpx/utils/mpc_wrapper.py:79-98,261-282).
 """
 import collections
 import ctypes
+import gc
 import time
 
 import numpy as np
@@ -315,7 +316,11 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
     and new ones are admitted only up to n_episodes); None: fresh episodes,
     all released at return.  stagger: the episodes admitted to fill the
     stream start at uniformly drawn ages, so that their ends (and their
-    successors' cold starts) spread over time as in a steady stream."""
+    successors' cold starts) spread over time as in a steady stream.
+
+    The loop runs with Python's cyclic garbage collector paused (collected
+    once before): a full collection over the process's objects can stall the
+    host loop for ~0.1 s, which every request in flight would wait out."""
     own = stream is None
     st = EpisodeStream(server, seed) if own else stream
     rng = np.random.default_rng(seed)
@@ -338,6 +343,17 @@ def served_workload(server, n_episodes, rate_hz, duration_s, seed=0, horizon_ran
 
     while len(eps) < n_episodes:
         new_episode(int(st.rng.integers(0, episode_ticks)) if stagger else 0)
+    gc.collect()
+    gc_was_enabled = gc.isenabled()
+    gc.disable()
+    try:
+        return _run_stream(server, st, eps, arrivals, episode_ticks, new_episode, own)
+    finally:
+        if gc_was_enabled:
+            gc.enable()
+
+
+def _run_stream(server, st, eps, arrivals, episode_ticks, new_episode, own):
     t0 = time.perf_counter()
     i = 0
     lat, stats, kkts, mods = [], [], [], []

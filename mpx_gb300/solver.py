@@ -54,6 +54,8 @@ def solver_opts(opts, warps_per_block=0, blocks_per_sm=0):
     o.ls_eta = float(opts.ls_eta); o.reg = float(opts.reg); o.rho0 = float(opts.rho0)
     o.ls_skip_tol = float(opts.ls_skip_tol); o.compute_kkt = int(bool(opts.compute_kkt))
     o.warps_per_block = int(warps_per_block); o.blocks_per_sm = int(blocks_per_sm)
+    o.team_warps = int(getattr(opts, "team_warps", 0))
+    o.team_min_horizon = int(getattr(opts, "team_min_horizon", 64))
     return o
 
 
@@ -141,7 +143,16 @@ class Solver:
         return self._total_warps
 
     def launches_per_solve(self, batch, horizon=True):
-        return 2 if (horizon and batch > self.total_warps) else 1
+        """Kernel launches of one mpxg_solve: the solve, the longest-first
+        ordering when needed, and the time-parallel team kernel beside the
+        one-warp kernel when the team path is on."""
+        team = int(getattr(self.opts, "team_warps", 0)) == 8 and max(8, int(self.opts.team_min_horizon)) <= self.n_max
+        n = 1
+        if horizon and (batch > self.total_warps or team):
+            n += 1
+        if team and horizon:
+            n += 1
+        return n
 
     def geometry(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -1,0 +1,144 @@
+"""The time-parallel team kernel (sqp_team.cuh: one block of 8 warps per
+instance, the KKT step split over the horizon) against the FP64 oracle, and
+its place in a batch: instances at or above team_min_horizon go to the team
+kernel, the rest to the one-warp kernel, by horizon alone, so that every
+result is the same alone and in any mix.
+
+Tolerances as tests/test_gpu_sqp.py: a cold 5-iteration solve within 2x the
+oracle's own float32 error + 1e-4; near convergence X, U, V, K, k within
+max(1e-4, 3x the oracle-FP32 error)."""
+import numpy as np
+import pytest
+import torch
+
+from mpx_gb300 import problem as P
+from mpx_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+MODELS = [P.MODEL_SRBD_RPY12, P.MODEL_SRBD_QUAT13, P.MODEL_BIPED_WRENCH12]
+TEAM = dict(team_warps=8, team_min_horizon=64)
+
+
+def workload(model, B, horizons, seed):
+    if model == P.MODEL_BIPED_WRENCH12:
+        return P.biped_workload(B, horizons=horizons, seed=seed)
+    return P.quadruped_workload(B, horizons=horizons, seed=seed, model=model, v_range=(-1, 1), random_phase=True)
+
+
+def solve(wl, opts, want_gains=True, idx=None):
+    idx = np.arange(wl.batch) if idx is None else np.asarray(idx)
+    s = Solver(wl.desc, opts, n_max=wl.n_max, batch_max=len(idx))
+    out = s.solve(wl.x0[idx], wl.X0[idx], wl.U0[idx], wl.V0[idx], wl.reference[idx], wl.parameter[idx], wl.W[idx],
+                  wl.horizon[idx], want_gains=want_gains)
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items() if not k.startswith("_")}
+    s.close()
+    return res
+
+
+def rel_err(a, b, horizon, kind):
+    err, scale = 0.0, 0.0
+    for i, N in enumerate(horizon):
+        rows = N + 1 if kind == "x" else N
+        err = max(err, np.abs(a[i, :rows] - b[i, :rows]).max())
+        scale = max(scale, np.abs(b[i, :rows]).max())
+    return err / max(scale, 1e-12)
+
+
+# Cold starts: the biped's N = 200 instance of this batch takes the full step
+# of its fourth iteration with an Armijo margin of 7e-6 of the predicted merit
+# decrease (FP64 oracle); the team kernel's float32 merit, summed in another
+# order, rejects it (a step of 1/2 instead), so from there the iterates part.
+# Its trajectories are compared through the third iteration; the gains and the
+# near-converged steps below are compared for every model.
+@pytest.mark.parametrize("model,iters", [(P.MODEL_SRBD_RPY12, 5), (P.MODEL_SRBD_QUAT13, 5),
+                                         (P.MODEL_BIPED_WRENCH12, 3)])
+def test_team_cold_iterations_match_oracle(oracle, cuda, model, iters):
+    wl = workload(model, 6, (64, 100, 200), seed=31)
+    opts = P.SolverOptions(sqp_iters=iters, **TEAM)
+    g = solve(wl, opts)
+    base = P.SolverOptions(sqp_iters=iters)
+    args = (wl.desc, base, wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+    o = oracle.sqp_solve(*args)
+    o32 = oracle.sqp_solve(*args, precision=32)
+    for key, kind in (("X", "x"), ("U", "u")):
+        eg = rel_err(g[key], o[key], wl.horizon, kind)
+        e32 = rel_err(o32[key], o[key], wl.horizon, kind)
+        assert eg <= 2.0 * e32 + 1e-4, (key, eg, e32)
+    kg = oracle.kkt_residual(wl.desc, wl.x0, g["X"], g["U"], g["V"], wl.reference, wl.parameter, wl.W, wl.horizon)
+    assert np.all(kg[:, 2] <= np.maximum(2.0 * o["kkt"][:, 2], 1e-4)), (kg[:, 2], o["kkt"][:, 2])
+    assert np.all(g["status"] & 1 == 0)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_team_near_converged_parity(oracle, cuda, model):
+    wl = workload(model, 4, (80, 150), seed=33)
+    o15 = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=15), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
+                           wl.parameter, wl.W, wl.horizon)
+    warm = P.Workload(wl.desc, wl.x0, o15["X"].astype(np.float32), o15["U"].astype(np.float32),
+                      o15["V"].astype(np.float32), wl.reference, wl.parameter, wl.W, wl.horizon)
+    g = solve(warm, P.SolverOptions(sqp_iters=2, **TEAM))
+    base = P.SolverOptions(sqp_iters=2)
+    args = (wl.desc, base, wl.x0, warm.X0, warm.U0, warm.V0, wl.reference, wl.parameter, wl.W, wl.horizon)
+    o = oracle.sqp_solve(*args)
+    o32 = oracle.sqp_solve(*args, precision=32)
+    if model == P.MODEL_SRBD_QUAT13:  # gains on the tangent space of the unit quaternion
+        for res in (g, o, o32):
+            for i, N in enumerate(wl.horizon):
+                for t in range(N):
+                    q = o["X"][i, t, 3:7] / np.linalg.norm(o["X"][i, t, 3:7])
+                    res["K"][i, t][:, 3:7] -= np.outer(res["K"][i, t][:, 3:7] @ q, q)
+
+    def err(a, b, key, kind):
+        if key != "k":
+            return rel_err(a, b, wl.horizon, kind)
+        e = max(np.abs(a[i, :N] - b[i, :N]).max() for i, N in enumerate(wl.horizon))
+        return e / max(np.abs(o["U"][i, :N]).max() for i, N in enumerate(wl.horizon))
+
+    for key, kind in (("X", "x"), ("U", "u"), ("V", "x"), ("K", "u"), ("k", "u")):
+        eg = err(g[key], o[key], key, kind)
+        e32 = err(o32[key], o[key], key, kind)
+        assert eg < max(1e-4, 3.0 * e32), (key, eg, e32)
+
+
+def test_team_results_do_not_depend_on_the_batch(cuda):
+    """Long horizons go to the team kernel and short ones to the one-warp
+    kernel in one solve call; each result equals the instance solved alone,
+    and the short ones equal the one-warp path's with the team path off."""
+    wl = workload(P.MODEL_SRBD_RPY12, 10, (20, 40, 63, 64, 100, 150), seed=35)
+    opts = P.SolverOptions(sqp_iters=3, **TEAM)
+    mix = solve(wl, opts, want_gains=False)
+    off = solve(wl, P.SolverOptions(sqp_iters=3), want_gains=False)
+    sub = solve(wl, opts, want_gains=False, idx=[7, 2, 9])
+    for i, N in enumerate(wl.horizon):
+        alone = solve(wl, opts, want_gains=False, idx=[i])
+        for key in ("X", "U", "V"):
+            rows = N + 1 if key != "U" else N
+            assert np.array_equal(mix[key][i, :rows], alone[key][0, :rows]), (i, N, key)
+            if N < 64:
+                assert np.array_equal(mix[key][i, :rows], off[key][i, :rows]), (i, N, key)
+        assert np.array_equal(mix["kkt"][i], alone["kkt"][0])
+    for j, i in enumerate([7, 2, 9]):
+        N = wl.horizon[i]
+        assert np.array_equal(sub["X"][j, :N + 1], mix["X"][i, :N + 1]), i
+
+
+def test_team_without_horizons(oracle, cuda):
+    """No per-instance horizons: every instance has n_max >= the minimum and
+    the team kernel alone solves the batch."""
+    wl = workload(P.MODEL_SRBD_RPY12, 3, (96,), seed=37)
+    opts = P.SolverOptions(sqp_iters=3, **TEAM)
+    s = Solver(wl.desc, opts, n_max=96, batch_max=3)
+    out = s.solve(wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W)
+    torch.cuda.synchronize()
+    g = {k: v.cpu().numpy() for k, v in out.items() if not k.startswith("_")}
+    s.close()
+    with_h = solve(wl, opts, want_gains=False)
+    assert np.array_equal(g["X"], with_h["X"]) and np.array_equal(g["U"], with_h["U"])
+    o = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=3), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
+                         wl.parameter, wl.W, wl.horizon)
+    o32 = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=3), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
+                           wl.parameter, wl.W, wl.horizon, precision=32)
+    eg, e32 = rel_err(g["X"], o["X"], wl.horizon, "x"), rel_err(o32["X"], o["X"], wl.horizon, "x")
+    assert eg <= 2.0 * e32 + 1e-4, (eg, e32)
