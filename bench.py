@@ -391,28 +391,31 @@ def run_served(dev, opts):
     stream's steady state rather than a cold start of every episode."""
     from mpx_gb300.server import EpisodeStream, MPCServer, default_models, served_workload
     out = {}
-    # config 3: the mixed stream, 200-tick episodes with state drift; horizons of 64 and more are solved by
-    # the time-parallel team kernel (8 warps per instance)
-    team_opts = dataclasses.replace(opts, team_warps=8, team_min_horizon=64)
-    srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=team_opts, drift_std=0.01, streams=32,
-                    device=dev)
-    es = EpisodeStream(srv, seed=1)
-    launches0 = None
-    served_workload(srv, 400, 20000.0, 0.5, seed=1, stream=es, stagger=True)
-    launches0 = srv.launches
-    lat, wall = served_workload(srv, 400, 20000.0, 2.0, seed=2, stream=es, stagger=True)
-    e = _served_entry(srv, lat, wall, 20000.0)
-    e["kkt_frac_le_1e-5_by_model"] = {name: float((srv.last_kkt[srv.last_model == i] <= 1e-5).mean())
-                                      for i, name in enumerate(srv.model_names) if (srv.last_model == i).any()}
-    e["gpu_launches"] = srv.launches - launches0
-    e["workload"] = ("Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, alternating), "
-                     "N uniform in [20, 200], 200-tick episodes at staggered ages (ended episodes are replaced by "
-                     "cold ones), state drift N(0, 0.01^2) per tick, 8 GB admission budget, 32 streams; 0.5 s "
-                     "warm-up of the same episodes, then 2 s measured; horizons >= 64 on the time-parallel team "
-                     "kernel (8 warps per instance), shorter ones one warp per instance")
-    out.update(e)
-    es.close()
-    srv.close()
+    # config 3: the mixed stream, 200-tick episodes with state drift, one warp per instance; then the same
+    # stream with horizons of 64 and more on the time-parallel team kernel (8 warps per instance)
+    for key, o3 in (("mixed", opts), ("mixed_team8", dataclasses.replace(opts, team_warps=8, team_min_horizon=64))):
+        srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=o3, drift_std=0.01, streams=32,
+                        device=dev)
+        es = EpisodeStream(srv, seed=1)
+        served_workload(srv, 400, 20000.0, 0.5, seed=1, stream=es, stagger=True)
+        launches0 = srv.launches
+        lat, wall = served_workload(srv, 400, 20000.0, 2.0, seed=2, stream=es, stagger=True)
+        e = _served_entry(srv, lat, wall, 20000.0)
+        e["kkt_frac_le_1e-5_by_model"] = {name: float((srv.last_kkt[srv.last_model == i] <= 1e-5).mean())
+                                          for i, name in enumerate(srv.model_names) if (srv.last_model == i).any()}
+        e["gpu_launches"] = srv.launches - launches0
+        e["workload"] = ("Poisson 20k req/s over 400 concurrent episodes (quadruped SRBD and biped SRBD, "
+                         "alternating), N uniform in [20, 200], 200-tick episodes at staggered ages (ended episodes "
+                         "are replaced by cold ones), state drift N(0, 0.01^2) per tick, 8 GB admission budget, "
+                         "32 streams; 0.5 s warm-up of the same episodes, then 2 s measured; " +
+                         ("one warp per instance" if key == "mixed" else
+                          "horizons >= 64 on the time-parallel team kernel (8 warps per instance)"))
+        if key == "mixed":
+            out.update(e)
+        else:
+            out[key] = e
+        es.close()
+        srv.close()
     # the latency target's case: 4096 robots (N = 50 quadruped episodes that keep running) at rising rates
     for drift, key in ((0.0, "envs4096_n50"), (0.01, "envs4096_n50_drift")):
         srv = MPCServer(default_models(), n_max=50, budget_bytes=8 << 30, opts=opts, drift_std=drift, streams=32,
@@ -422,13 +425,13 @@ def run_served(dev, opts):
         served_workload(srv, 4096, 300000.0, 4096 * 10 / 300000.0, seed=3, **kw)  # ~10 ticks per robot first
         sweep = []
         for rate in ((50000.0, 150000.0, 300000.0) if drift == 0.0 else (150000.0,)):
-            served_workload(srv, 4096, rate, 0.2, seed=4, **kw)
+            served_workload(srv, 4096, rate, 0.5, seed=4, **kw)
             l4, w4 = served_workload(srv, 4096, rate, 1.0, seed=5, **kw)
             sweep.append(_served_entry(srv, l4, w4, rate))
         out[key] = {"sweep": sweep,
                     "workload": "4096 concurrent quadruped SRBD episodes, N = 50, 5 SQP iterations, %s; each tick "
                                 "x0 <- X[1] of the shifted warm start%s; 32 streams; ~10 ticks per robot before the "
-                                "first window, 0.2 s warm-up per rate, 1 s measured" %
+                                "first window, 0.5 s warm-up per rate, 1 s measured" %
                                 ("no drift" if drift == 0.0 else "drift N(0, 0.01^2)",
                                  "" if drift == 0.0 else " + drift")}
         es.close()

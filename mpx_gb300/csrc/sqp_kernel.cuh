@@ -546,7 +546,7 @@ __device__ __forceinline__ void gj_block4(float* h, int s0, int lane, float* CT,
 
 // ----------------------------------------------------------------- chunk elements
 // Accumulators of a time-parallel chunk's element while its Riccati sweep
-// runs from a zero terminal cost (see riccati_sweep, ELEM = true): the
+// runs from a zero terminal cost (see riccati_sweep, ELEM = 2): the
 // closed-loop affine map x_e = Phi x_t + phi from stage t to the chunk end and
 // the Gramian G = sum Phi_{t+1->e} B Quu^-1 B' Phi_{t+1->e}'.  Column-major,
 // column stride FS.  Also the outputs of the chunk combination (sqp_team.cuh).
@@ -609,11 +609,11 @@ __device__ __forceinline__ void riccati_terminal(int N, WarpSmem<M>& sm, const S
 // function of stage t (into the shared P) and the gains.
 //   STORE: write gains K = [K | k], the closed loop (A + BK, Bk + c) over F's
 //          first columns, and P to the scratch (the forward sweep reads them).
-//   ELEM:  accumulate the chunk element in es (ElemSmem): Phi, phi, G of the
-//          map from stage t to hi under this sweep's policy.  On entry the
-//          caller has set es->Phi[0] = I; on return es->G, es->phi and
-//          es->cur hold the result.
-template <class M, bool STORE, bool ELEM>
+//   ELEM:  1: accumulate the closed-loop affine map x_hi = Phi x_t + phi of
+//          this sweep's policy in es (ElemSmem); 2: also the Gramian G of the
+//          chunk element.  On entry the caller has set es->Phi[0] = I; on
+//          return es->Phi[es->cur], es->phi (and es->G) hold the result.
+template <class M, bool STORE, int ELEM>
 __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int hi, WarpSmem<M>& sm, const Scratch<M>& s,
                                               ElemSmem<M>* es, int* status, int lane) {
   typedef Dims<M> D;
@@ -622,7 +622,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
   const int j = lane;
   if (hi <= lo) return;
   int cur = 0;
-  float gcol[FS];  // ELEM: column j of G (state lanes), phi (lane JA)
+  float gcol[FS];  // ELEM 2: column j of G (state lanes); ELEM >= 1: phi (lane JA)
 #pragma unroll
   for (int i = 0; i < FS; ++i) gcol[i] = 0.0f;
   BlockRegs<NZ * FS> fpre;
@@ -714,7 +714,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
       if (a == j) h[a] += sp.reg;
     // ---- chunk element: Phi B_t, and row j of it as an extra right-hand side of the elimination
     float v[NZ];
-    if (ELEM) {
+    if (ELEM == 2) {
       const float* Phc = es->Phi[cur];
       if (j >= NX && j < JA) {
         float pb[FS];
@@ -737,7 +737,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
     }
     // ---- block Gauss-Jordan elimination of the control pivots
 #pragma unroll
-    for (int s0 = NX; s0 < JA; s0 += 4) gj_block4<NZ, ELEM, NX, NU>(h, s0, lane, sm.CT, status, v);
+    for (int s0 = NX; s0 < JA; s0 += 4) gj_block4<NZ, ELEM == 2, NX, NU>(h, s0, lane, sm.CT, status, v);
     // ---- gains, closed loop, new value function
     float* Kt = s.K + (size_t)t * NP * NU;
     float* Fo = s.F + (size_t)t * NZ * FS;
@@ -765,7 +765,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
       if (STORE) st_vec<FS>(Fo + slot * FS, cl);
 #pragma unroll
       for (int i = 0; i < NX; ++i) sm.Praw[col * LDP + i] = h[i];
-      if (ELEM) {  // Phi <- Phi (A + B K), phi <- phi + Phi (B k + c), G <- G + (Phi B) Quu^-1 (Phi B)'
+      if (ELEM >= 1) {  // Phi <- Phi (A + B K), phi <- phi + Phi (B k + c), G <- G + (Phi B) Quu^-1 (Phi B)'
         const float* Phc = es->Phi[cur];
         float pn[FS];
 #pragma unroll
@@ -782,7 +782,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
         if (j < NX) {
           st_vec<FS>(es->Phi[cur ^ 1] + j * FS, pn);
 #pragma unroll
-          for (int a = 0; a < NU; ++a) {
+          for (int a = 0; a < (ELEM == 2 ? NU : 0); ++a) {
             const float ya = v[NX + a];
 #pragma unroll
             for (int q = 0; q < FS / 4; ++q) {
@@ -797,7 +797,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
         }
       }
     }
-    if (ELEM) cur ^= 1;
+    if (ELEM >= 1) cur ^= 1;
     __syncwarp();
     {
       float* Pt = s.P + (size_t)t * NP * LDP;
@@ -822,8 +822,8 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
     }
     __syncwarp();
   }
-  if (ELEM) {
-    if (j < NX) st_vec<FS>(es->G + j * FS, gcol);
+  if (ELEM >= 1) {
+    if (ELEM == 2 && j < NX) st_vec<FS>(es->G + j * FS, gcol);
     if (j == JA) st_vec<FS>(es->phi, gcol);
     if (j == 0) es->cur = cur;
     __syncwarp();
@@ -991,7 +991,7 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
     // whole-warp fence: phase-1 stores are complete before the block loads
     __threadfence_block();
     __syncwarp();
-    riccati_sweep<M, true, false>(sp, 0, N, sm, s, nullptr, &status, lane);
+    riccati_sweep<M, true, 0>(sp, 0, N, sm, s, nullptr, &status, lane);
     // ================================================ phase 3: forward sweep
     __threadfence_block();
     __syncwarp();

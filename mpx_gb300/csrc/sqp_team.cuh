@@ -14,10 +14,13 @@
 //  2m. warp 0 combines the elements from the last chunk backwards: the true
 //      value function at each chunk start,
 //          Z = (I + G P_e)^-1 [Phi | phi - G p_e],
-//          P_s = J + Phi' P_e Z_Phi,  p_s = eta + Phi' (P_e z + p_e),
-//      and the chunk-boundary states forwards, x_e = Z_Phi x_s + z;
+//          P_s = J + Phi' P_e Z_Phi,  p_s = eta + Phi' (P_e z + p_e);
 //  2b. every warp but the last re-runs its chunk's sweep from the true value
-//      at its end (gains, closed loop and value functions to the scratch);
+//      at its end (gains, closed loop and value functions to the scratch) and
+//      composes the chunk's true closed-loop affine map x_e = Phi x_s + phi;
+//  2f. warp 0 composes those maps from dx_0 = c_0: the state steps at the
+//      chunk starts (the forward pass as composed affine maps, consistent
+//      with each chunk's own forward sweep);
 //  3.  every warp runs its chunk's forward sweep from its boundary state.
 //
 // The linearisation (phase 1) and the merit line search (phase 4) are
@@ -69,8 +72,7 @@ __device__ __forceinline__ void team_bounds(int N, int* bounds) {
 }
 
 // Warp 0: combine the chunk elements from the last chunk backwards (true
-// value at every chunk start into el[c].Pin, end-state maps into el[c].Z),
-// then the state steps at the chunk starts, xb[0] = c_0 given.
+// value at every chunk start into el[c].Pin; el[c].Z is [Z_Phi | z]).
 template <class M, int W>
 __device__ __forceinline__ void team_combine(TeamSmem<M, W>& ts, int lane) {
   typedef Dims<M> D;
@@ -177,13 +179,21 @@ __device__ __forceinline__ void team_combine(TeamSmem<M, W>& ts, int lane) {
     }
     __syncwarp();
   }
-  // ---- state steps at the chunk starts
+}
+
+// Warp 0: the state steps at the chunk starts, xb[c+1] = Phi_c xb[c] + phi_c
+// over the chunks' true closed-loop maps (xb[0] = c_0 given).
+template <class M, int W>
+__device__ __forceinline__ void team_boundary_states(TeamSmem<M, W>& ts, int lane) {
+  typedef Dims<M> D;
+  constexpr int NX = D::NX, FS = D::FS;
   for (int c = 0; c + 1 < W; ++c) {
     const ElemSmem<M>& el = ts.el[c];
+    const float* Phi = el.Phi[el.cur];
     if (lane < NX) {
-      float a = el.Z[NX * FS + lane];
+      float a = el.phi[lane];
 #pragma unroll
-      for (int k = 0; k < NX; ++k) a += el.Z[k * FS + lane] * ts.xb[c][k];
+      for (int k = 0; k < NX; ++k) a += Phi[k * FS + lane] * ts.xb[c][k];
       ts.xb[c + 1][lane] = a;
     }
     __syncwarp();
@@ -244,7 +254,7 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     // ================================================ phase 2a: chunk elements; the last chunk exactly
     if (last) {
       riccati_terminal<M, true>(N, sm, s, lane);
-      riccati_sweep<M, true, false>(sp, lo, hi, sm, s, nullptr, &status, lane);
+      riccati_sweep<M, true, 0>(sp, lo, hi, sm, s, nullptr, &status, lane);
       for (int e = lane; e < NP * LDP; e += 32) el.Pin[e] = sm.P[e];
     } else {
       for (int e = lane; e < NP * LDP; e += 32) sm.P[e] = 0.0f;
@@ -253,7 +263,7 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
         el.Phi[0][e] = (rr == cc) ? 1.0f : 0.0f;
       }
       __syncwarp();
-      riccati_sweep<M, false, true>(sp, lo, hi, sm, s, &el, &status, lane);
+      riccati_sweep<M, false, 2>(sp, lo, hi, sm, s, &el, &status, lane);
     }
     if (warp == 0 && lane < NX) ts.xb[0][lane] = x0[lane] - X[lane];
     __syncthreads();
@@ -264,11 +274,18 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     if (!last) {
       const float* Pe = ts.el[warp + 1].Pin;
       for (int e = lane; e < NP * LDP; e += 32) sm.P[e] = Pe[e];
+      for (int e = lane; e < NX * FS; e += 32) {
+        const int cc = e / FS, rr = e - cc * FS;
+        el.Phi[0][e] = (rr == cc) ? 1.0f : 0.0f;
+      }
       __syncwarp();
-      riccati_sweep<M, true, false>(sp, lo, hi, sm, s, nullptr, &status, lane);
+      riccati_sweep<M, true, 1>(sp, lo, hi, sm, s, &el, &status, lane);
     }
     __threadfence_block();
-    __syncwarp();
+    __syncthreads();
+    // ================================================ phase 2f: chunk-boundary states
+    if (warp == 0) team_boundary_states<M, W>(ts, lane);
+    __syncthreads();
     // ================================================ phase 3: chunk forward sweeps
     double a_gd = 0.0, a_lc = 0.0, a_vc = 0.0, a_cs = 0.0;
     float c_init = 0.0f;
@@ -355,7 +372,13 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     if (!isfinite(X[e]) || !isfinite(V[e])) bad = 1;
   for (int e = tid; e < N * NU; e += NT)
     if (!isfinite(U[e])) bad = 1;
-  const int st = __syncthreads_or(status | (bad ? ST_NAN : 0));
+  // bitwise OR of the status words over the block (__syncthreads_or would give a 0/1 predicate)
+  int st = warp_or(status | (bad ? ST_NAN : 0));
+  __syncthreads();
+  if (lane == 0) ts.red[warp][0] = (double)st;
+  __syncthreads();
+  st = 0;
+  for (int w = 0; w < W; ++w) st |= (int)ts.red[w][0];
   if (bp.status && tid == 0) bp.status[b] = st;
   if (bp.first && warp == 0) {
     float* f = bp.first + (size_t)bidx * (NU + 4);

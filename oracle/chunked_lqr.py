@@ -24,11 +24,15 @@ elements obtained from a chunk-local Riccati sweep:
    chunk, so a short sequential scan): given the true value (P_e, p_e) at
    e_c,
        Z = (I + G P_e)^-1 [Phi | phi - G p_e]
-       P_s = J + Phi' P_e Z_Phi,   p_s = eta + Phi' (P_e z + p_e),
-   and the chunk's end state is x_e = Z_Phi x_s + z.
-3. The boundary states follow forwards from dx_0 = c_0; each chunk then
-   re-runs its Riccati sweep from its true terminal value and its forward
-   sweep from its boundary state, both chunk-local.
+       P_s = J + Phi' P_e Z_Phi,   p_s = eta + Phi' (P_e z + p_e)
+   (the chunk's optimal end state would be x_e = Z_Phi x_s + z).
+3. Each chunk re-runs its Riccati sweep from its true terminal value and
+   composes the closed-loop affine map of its true gains, x_e = Phi' x_s +
+   phi'.  The boundary states follow forwards from dx_0 = c_0 through those
+   maps (the forward pass as composed affine maps; in exact arithmetic the
+   same as Z_Phi x_s + z, and in float32 consistent with each chunk's own
+   forward sweep), and each chunk runs its forward sweep from its boundary
+   state.
 
 riccati() is the sequential recursion (the oracle's riccati_solve,
 oracle.hpp) on the same data, for comparison.
@@ -121,26 +125,35 @@ def chunked_solve(H, g, A, B, c, bounds, reg=0.0):
     # step 1 (parallel over chunks); the last chunk is solved from the true terminal cost
     elems = [chunk_element(H, g, A, B, c, bounds[w], bounds[w + 1], reg) for w in range(W - 1)]
     Kl, kl, Pl, pl = riccati(H, g, A, B, c, reg, bounds[W - 1], N)
-    # step 2: values at the chunk starts, backwards; end-state maps
-    Pv, pv, maps = {N: Pl[N]}, {N: pl[N]}, {}
+    # step 2: values at the chunk starts, backwards
+    Pv, pv = {N: Pl[N]}, {N: pl[N]}
     Pv[bounds[W - 1]], pv[bounds[W - 1]] = Pl[bounds[W - 1]], pl[bounds[W - 1]]
     for w in range(W - 2, -1, -1):
         e = bounds[w + 1]
-        Pv[bounds[w]], pv[bounds[w]], ZPhi, z = combine(elems[w], Pv[e], pv[e])
-        maps[w] = (ZPhi, z)
-    # boundary states forwards
-    xb = {0: c[0].copy()}
-    for w in range(W - 1):
-        ZPhi, z = maps[w]
-        xb[bounds[w + 1]] = ZPhi @ xb[bounds[w]] + z
-    # step 3 (parallel over chunks): local Riccati from the true end value, local forward sweep
-    out = dict(K={}, k={}, P={}, p={}, dx={}, du={}, lam={})
+        Pv[bounds[w]], pv[bounds[w]], _, _ = combine(elems[w], Pv[e], pv[e])
+    # step 3 (parallel over chunks): local Riccati from the true end value and its closed-loop map
+    local, maps = {}, {}
     for w in range(W):
         lo, hi = bounds[w], bounds[w + 1]
         if w == W - 1:
-            K, k, Ps, ps = Kl, kl, Pl, pl
-        else:
-            K, k, Ps, ps = riccati(H, g, A, B, c, reg, lo, hi, Pv[hi], pv[hi])
+            local[w] = (Kl, kl, Pl, pl)
+            continue
+        K, k, Ps, ps = riccati(H, g, A, B, c, reg, lo, hi, Pv[hi], pv[hi])
+        local[w] = (K, k, Ps, ps)
+        Phi, phi = np.eye(n, dtype=A[0].dtype), np.zeros(n, A[0].dtype)  # map from stage t+1 to hi
+        for t in range(hi - 1, lo - 1, -1):
+            phi = phi + Phi @ (B[t] @ k[t] + c[t + 1])
+            Phi = Phi @ (A[t] + B[t] @ K[t])
+        maps[w] = (Phi, phi)
+    # boundary states forwards through the composed maps
+    xb = {0: c[0].copy()}
+    for w in range(W - 1):
+        Phi, phi = maps[w]
+        xb[bounds[w + 1]] = Phi @ xb[bounds[w]] + phi
+    out = dict(K={}, k={}, P={}, p={}, dx={}, du={}, lam={})
+    for w in range(W):
+        lo, hi = bounds[w], bounds[w + 1]
+        K, k, Ps, ps = local[w]
         dx, du, lam = forward(A, B, c, K, k, Ps, ps, xb[lo], lo, hi)
         for t in range(lo, hi):
             out["K"][t], out["k"][t], out["du"][t] = K[t], k[t], du[t]
