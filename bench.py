@@ -290,7 +290,7 @@ def fp64_error(tr, opts, stream, sample=64):
                     "instances" % len(idx)}
 
 
-def dropin_wrapper(dev, steps, warmup, n_env=BATCH):
+def dropin_wrapper(dev, steps, warmup, n_env=BATCH, smooth=False):
     """End to end through the drop-in API: BatchedMPCControllerWrapper.run (the
     interface of mpx/utils/mpc_wrapper_srbd.py:91-141) on the reference's SRBD
     model and config (quaternion state, N = 25, the reference's barrier) for
@@ -301,8 +301,12 @@ def dropin_wrapper(dev, steps, warmup, n_env=BATCH):
     import torch
     from mpx_gb300 import configs
     from mpx_gb300.wrappers import BatchedMPCControllerWrapper
+    from mpx_gb300 import problem as P
     cfg = configs.srbd_quadruped()
-    w = BatchedMPCControllerWrapper(cfg, n_env, device=dev)
+    desc = None
+    if smooth:
+        desc = dataclasses.replace(P.quadruped_quat13(cfg), barrier_kind=1, barrier_masked=1, cone_eps2=1.0)
+    w = BatchedMPCControllerWrapper(cfg, n_env, device=dev, desc=desc)
     rng = np.random.default_rng(5)
     x0 = np.tile(w.initial_state, (n_env, 1)).astype(np.float32)
     x0[:, :3] += rng.normal(0.0, 0.01, (n_env, 3)).astype(np.float32)
@@ -334,7 +338,9 @@ def dropin_wrapper(dev, steps, warmup, n_env=BATCH):
            "kkt_frac_le_1e-5": float((kkt <= 1e-5).mean()), "kkt_median": float(np.median(kkt)),
            "what": "%d environments through BatchedMPCControllerWrapper.run with host numpy arrays every tick "
                    "(timer, reference generator, solve, shift: 4 launches), host wall clock; model SRBD_QUAT13 "
-                   "with the reference's barrier, config mpx/config/config_srbd.py (N = 25)" % n_env}
+                   "with %s, config mpx/config/config_srbd.py (N = 25)" %
+                   (n_env, "the smooth stance-masked barrier (cone smoothing 1 N)" if smooth else
+                    "the reference's penalty barrier")}
     w.solver.close()
     return res
 
@@ -661,6 +667,7 @@ def run_ours(args, rank, world, local_rank):
     dropin = None
     if not args.profile and rank == 0 and not args.no_dropin:
         dropin = dropin_wrapper(dev, min(args.steps, 20), args.warmup)
+        dropin["smooth_barrier"] = dropin_wrapper(dev, min(args.steps, 20), args.warmup, smooth=True)
 
     # ---------------- CPU baseline (oracle, rank 0)
     cpu = None

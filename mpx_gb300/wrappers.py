@@ -117,9 +117,15 @@ class BatchedMPCControllerWrapper:
     mpc_frequency, timer_t, duty_factor, step_freq, step_height,
     clearence_speed, p0, quat0, p_legs0, n, mass, inertia, u_ref, W, ...)."""
 
-    def __init__(self, config, n_env, opts=None, device=None, limited_memory=False, wb_model=None):
+    def __init__(self, config, n_env, opts=None, device=None, limited_memory=False, wb_model=None, desc=None):
         """wb_model: an mjcf.RigidBodyModel for whole_body_run (default: the
-        MJCF at config.model_path with config.contact_frame / body_name)."""
+        MJCF at config.model_path with config.contact_frame / body_name).
+        desc: the quaternion model's description (default: the reference's
+        own, problem.quadruped_quat13(config), with its penalty barrier); a
+        description with barrier_kind=1, barrier_masked=1 and cone_eps2=1
+        selects the smooth, stance-masked barrier with which the SQP
+        converges (the reference's clipped, unmasked penalty defeats the
+        merit line search)."""
         self.config = config
         self.n_env = int(n_env)
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -138,7 +144,9 @@ class BatchedMPCControllerWrapper:
         self.initial_state = np.concatenate([np.asarray(config.p0, dtype=np.float32),
                                              np.asarray(config.quat0, dtype=np.float32),
                                              np.zeros(6, dtype=np.float32)])
-        self.desc = P.quadruped_quat13(config, mu=float(getattr(config, "mu", 0.7)))
+        self.desc = desc or P.quadruped_quat13(config, mu=float(getattr(config, "mu", 0.7)))
+        if self.desc.model != P.MODEL_SRBD_QUAT13:
+            raise ValueError("the SRBD wrapper runs the quaternion model (MODEL_SRBD_QUAT13)")
         self.opts = opts or P.SolverOptions()
         self.solver = Solver(self.desc, self.opts, n_max=self.N, batch_max=self.n_env, device=self.dev)
         self.L = _lib.load()

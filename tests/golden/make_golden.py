@@ -725,13 +725,9 @@ def main_wb(ref_root, out):
     print("wrote", out)
 
 
-# Where the reference checkout is read from unless given on the command line
-# or in MPX_REFERENCE.
-DEFAULT_REFERENCE = "/root/reference"
-
-
 def reference_root():
-    return os.environ.get("MPX_REFERENCE", DEFAULT_REFERENCE)
+    """The reference checkout named by MPX_REFERENCE ("" when unset)."""
+    return os.environ.get("MPX_REFERENCE", "")
 
 
 if __name__ == "__main__":

@@ -69,6 +69,8 @@ def main(ref, outdir):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPX_REFERENCE", "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPX_REFERENCE", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "mpx")):
+        sys.exit("usage: make_wb_fixture.py <reference checkout containing mpx/> [out dir] (or set MPX_REFERENCE)")
     outdir = sys.argv[2] if len(sys.argv) > 2 else os.path.dirname(os.path.abspath(__file__))
     main(ref, outdir)

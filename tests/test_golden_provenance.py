@@ -22,7 +22,7 @@ def _reference():
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     root = mod.reference_root()
-    if not os.path.isdir(os.path.join(root, "mpx")):
+    if not root or not os.path.isdir(os.path.join(root, "mpx")):
         pytest.skip("no reference checkout (MPX_REFERENCE)")
     return root
 
