@@ -466,12 +466,13 @@ def run_ours(args, rank, world, local_rank):
                               random_phase=True)
     opts = P.SolverOptions(sqp_iters=SQP_ITERS)
     tuned = None
-    wpb, bps = 0, 0
+    wpb, bps, tw, tm = 0, 0, 0, 0
     if not args.no_autotune and not args.profile:
         from mpx_gb300.autotune import tune
         tuned = tune(wl, opts, device=dev)
-        wpb, bps = tuned["best"]
-    tr = TickRunner(wl, opts, device=dev, drift_std=DRIFT, warps_per_block=wpb, blocks_per_sm=bps)
+        wpb, bps, tw, tm = tuned["best"]
+    tick_opts = dataclasses.replace(opts, team_warps=tw, team_min_horizon=tm) if tw else opts
+    tr = TickRunner(wl, tick_opts, device=dev, drift_std=DRIFT, warps_per_block=wpb, blocks_per_sm=bps)
     stream = torch.cuda.Stream(device=dev)
     n, m = wl.desc.n, wl.desc.m
     with torch.cuda.stream(stream):
@@ -739,9 +740,12 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
         "geometry": tr.solver.geometry(),
         "autotune": None if tuned is None else {
-            "best": {"warps_per_block": tuned["best"][0], "blocks_per_sm": tuned["best"][1] or "auto"},
+            "best": {"warps_per_block": tuned["best"][0], "blocks_per_sm": tuned["best"][1] or "auto",
+                     "warps_per_instance": tuned["best"][2] or 1, "team_min_horizon": tuned["best"][3]},
             "cached": tuned["cached"],
-            "ms_per_solve": {"%dx%s" % (r["wpb"], r["bps"] or "auto"): r.get("ms") for r in tuned["table"]}},
+            "ms_per_solve": {("%dx%s" % (r["wpb"], r["bps"] or "auto")) +
+                             (" team8>=%d" % r["team_min_horizon"] if r.get("team_warps") else ""): r.get("ms")
+                             for r in tuned["table"]}},
     }
     if not args.no_other and not args.profile:
         line["other_configs"] = other_configs(args, rank, world, local_rank)

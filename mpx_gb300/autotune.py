@@ -1,13 +1,19 @@
 """Launch-geometry autotuner for the batched solve.
 
 The persistent solve kernel runs one instance per warp; its grid is
-(SMs x blocks per SM) blocks of `warps_per_block` warps.  The best pair
+(SMs x blocks per SM) blocks of `warps_per_block` warps.  Long horizons can
+instead go to the time-parallel team kernel, 8 warps per instance, from a
+horizon threshold on (`team_warps`, `team_min_horizon`).  The best choice
 depends on the model (registers, shared memory per warp), the horizon mix and
-the batch size, so it is measured: each candidate solves the caller's own
-batch a few times (CUDA events, after a warm-up solve) and the fastest is
-kept.  Results are cached per (GPU, model, n_max, batch, SQP iterations) in a
-JSON file (MPXG_TUNE_CACHE, default ~/.cache/mpxg/tune.json).
+the batch size, so it is measured: each candidate (warps per block, blocks
+per SM, warps per instance, team threshold) solves the caller's own batch a
+few times (CUDA events, after a warm-up solve) and the fastest is kept.  A
+batched solve ends when its last instance does, so the time measured is both
+the batch's latency and its throughput.  Results are cached per (GPU,
+model, n_max, batch, SQP iterations) in a JSON file (MPXG_TUNE_CACHE,
+default ~/.cache/mpxg/tune.json).
 """
+import dataclasses
 import json
 import os
 
@@ -15,7 +21,15 @@ import torch
 
 from .solver import Solver
 
-DEFAULT_CANDIDATES = [(wpb, bps) for wpb in (1, 2, 4) for bps in (0, 2, 3, 4)]
+# (warps per block, blocks per SM, warps per instance, team threshold); 0 = default
+DEFAULT_CANDIDATES = ([(wpb, bps, 0, 0) for wpb in (1, 2, 4) for bps in (0, 2, 3, 4)] +
+                      [(4, 0, 8, tmin) for tmin in (32, 64, 128)])
+
+
+def _full(c):
+    """A candidate as (wpb, bps, team_warps, team_min_horizon)."""
+    c = tuple(c)
+    return c + (0, 0) if len(c) == 2 else c
 
 
 def _cache_path():
@@ -45,8 +59,10 @@ def _store(cache):
         pass
 
 
-def time_geometry(wl, opts, warps_per_block, blocks_per_sm, reps=5, device=None):
+def time_geometry(wl, opts, warps_per_block, blocks_per_sm, reps=5, device=None, team_warps=0, team_min_horizon=0):
     """Mean ms of one batched solve of workload `wl` with this geometry."""
+    if team_warps:
+        opts = dataclasses.replace(opts, team_warps=team_warps, team_min_horizon=team_min_horizon)
     s = Solver(wl.desc, opts, n_max=wl.n_max, batch_max=wl.batch, device=device,
                warps_per_block=warps_per_block, blocks_per_sm=blocks_per_sm)
     try:
@@ -66,9 +82,11 @@ def time_geometry(wl, opts, warps_per_block, blocks_per_sm, reps=5, device=None)
 
 
 def tune(wl, opts, candidates=None, reps=5, use_cache=True, device=None):
-    """Measure every (warps_per_block, blocks_per_sm) candidate on `wl` (0 =
-    the occupancy-derived default) and return dict(best=(wpb, bps),
-    ms=..., table=[{wpb, bps, ms, geometry}, ...], cached=bool)."""
+    """Measure every candidate (warps_per_block, blocks_per_sm[, team_warps,
+    team_min_horizon]) on `wl` (0 = the occupancy-derived default, no team
+    path) and return dict(best=(wpb, bps, team_warps, team_min_horizon),
+    ms=..., table=[{wpb, bps, team_warps, team_min_horizon, ms, geometry},
+    ...], cached=bool)."""
     key = _key(wl.desc, opts, wl.n_max, wl.batch)
     cache = _load() if use_cache else {}
     if use_cache and key in cache:
@@ -77,18 +95,24 @@ def tune(wl, opts, candidates=None, reps=5, use_cache=True, device=None):
         r["cached"] = True
         return r
     table = []
-    for wpb, bps in (candidates or DEFAULT_CANDIDATES):
+    for wpb, bps, tw, tm in map(_full, candidates or DEFAULT_CANDIDATES):
+        row = dict(wpb=wpb, bps=bps, team_warps=tw, team_min_horizon=tm)
         try:
-            ms, geo = time_geometry(wl, opts, wpb, bps, reps=reps, device=device)
+            if tw:
+                ms, geo = time_geometry(wl, opts, wpb, bps, reps=reps, device=device, team_warps=tw,
+                                        team_min_horizon=tm)
+            else:
+                ms, geo = time_geometry(wl, opts, wpb, bps, reps=reps, device=device)
         except Exception as e:  # e.g. a geometry the device cannot hold
-            table.append(dict(wpb=wpb, bps=bps, ms=None, error=str(e)[:120]))
+            table.append(dict(row, ms=None, error=str(e)[:120]))
             continue
-        table.append(dict(wpb=wpb, bps=bps, ms=ms, geometry=geo))
+        table.append(dict(row, ms=ms, geometry=geo))
     ok = [r for r in table if r.get("ms") is not None]
     if not ok:
         raise RuntimeError("autotune: no candidate geometry ran: %s" % table)
     best = min(ok, key=lambda r: r["ms"])
-    res = dict(best=(best["wpb"], best["bps"]), ms=best["ms"], table=table, cached=False)
+    res = dict(best=(best["wpb"], best["bps"], best["team_warps"], best["team_min_horizon"]), ms=best["ms"],
+               table=table, cached=False)
     if use_cache:
         cache[key] = dict(best=list(res["best"]), ms=res["ms"], table=table)
         _store(cache)

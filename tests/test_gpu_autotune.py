@@ -15,8 +15,9 @@ def test_tune_picks_the_fastest_measured_candidate(cuda, tmp_path, monkeypatch):
     monkeypatch.setenv("MPXG_TUNE_CACHE", str(tmp_path / "tune.json"))
     wl = P.quadruped_workload(64, horizons=(20, 40), seed=3, model=P.MODEL_SRBD_RPY12)
     opts = P.SolverOptions(sqp_iters=2)
-    r = tune(wl, opts, candidates=[(2, 0), (4, 0), (1, 2)], reps=2)
+    r = tune(wl, opts, candidates=[(2, 0), (4, 0), (1, 2), (4, 0, 8, 16)], reps=2)
     ms = [t["ms"] for t in r["table"]]
+    assert None not in ms  # the team candidate (8 warps per instance from N = 16 on) ran too
     assert r["ms"] == min(ms) and not r["cached"]
     assert tune(wl, opts, candidates=[(2, 0)], reps=1)["cached"]     # second call: from the cache
 
