@@ -775,6 +775,7 @@ def other_configs(args, rank, world, local_rank):
         if "tensor" in l4:
             entry["tf32_mma_tflops"] = l4["tensor"]["achieved_tflops"]
             entry["tensor_frac"] = l4["tensor"]["frac"]
+        entry["sqp"] = {k: l4["sqp"][k] for k in ("value", "ms_per_step", "iters", "kkt_max", "kkt_median")}
         out["lqr_eq_512_n72_m30_p12_N100_" + label] = entry
     w = run_wb(a, rank, world, local_rank, emit=False)
     out["wb_interface_4096_aliengo"] = {"metric": "whole-body interface evaluations/s", "value": w["value"],
@@ -1007,9 +1008,54 @@ def run_lqr_eq(args, rank, world, local_rank, emit=True):
                           "peak_source": "TF32 = half the measured bf16 dense rate (MEASURED_PEAKS.json bf16_tflops)",
                           "flops": "TF32 MMA work issued per stage (padded tiles, 3 MMAs per split product) = %d"
                                    % mma}
+    line["sqp"] = lqr_eq_sqp_leg(L, io, dv, outs, ws, stream, method, args.steps, dev)
     if rank == 0 and emit:
         print(json.dumps(line), flush=True)
     return line
+
+
+def lqr_eq_sqp_leg(L, io, dv, outs, ws, stream, method, steps, dev, iters=2):
+    """The same problems through SQP iterations (mpxg_lqr_eq_sqp): every step
+    restarts from the zero iterate, forms the step problem at the iterate,
+    solves it with the constrained Riccati and takes the full step, `iters`
+    times, then evaluates the KKT residual.  Reports solves/s and the KKT
+    residuals reached."""
+    import torch
+    from mpx_gb300 import _lib
+    from mpx_gb300.solver import _ptr, _stream_handle
+    B, N, n, m, ne = io.batch, io.N, io.n, io.m, io.n_eq
+    sio = _lib.LqEqSqpIO()
+    sio.lq = io
+    step = torch.empty(int(L.mpxg_lqr_eq_sqp_workspace_bytes(B, N, n, m, ne)) // 4, device=dev)
+    kkt = torch.empty(B, 3, device=dev)
+    sio.iters, sio.method, sio.kkt, sio.step = iters, method, _ptr(kkt), _ptr(step)
+    hs = _stream_handle(stream)
+
+    def solve():
+        outs["X"].zero_()
+        outs["U"].zero_()
+        _lib.check(L.mpxg_lqr_eq_sqp(hs, ctypes.byref(sio)), None, "mpxg_lqr_eq_sqp")
+
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            solve()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for _ in range(steps):
+            solve()
+        ev[1].record(stream)
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / steps
+    k = kkt.cpu().numpy()
+    return {"metric": "constrained LQ SQP solves/s (%d iterations from the zero iterate + KKT)" % iters,
+            "value": B / (ms / 1000.0), "ms_per_step": ms, "iters": iters,
+            "kkt_max": float(np.nanmax(k[:, 2])), "kkt_median": float(np.median(k[:, 2])),
+            "primal_max": float(np.nanmax(k[:, 0])), "dual_rel_max": float(np.nanmax(k[:, 1])),
+            "launches_per_step": 3 * iters + 2,
+            "note": "launches: per iteration step data, constrained Riccati, step; then KKT and its finish "
+                    "(plus two memsets of the iterate)"}
 
 
 # ------------------------------------------------------------ whole-body interface workload

@@ -333,6 +333,32 @@ mpxg_status mpxg_lqr_eq_solve(void* stream, const mpxg_lq_eq_io* io);
  * bounded wait leaves that problem's X non-finite. */
 mpxg_status mpxg_lqr_eq_solve_method(void* stream, const mpxg_lq_eq_io* io, int method);
 
+/* SQP iterations on the equality-constrained LQ problem of `lq` (config 4's
+ * large linearised problems through the SQP path of optimizers.mpc,
+ * mpx/utils/mpc_wrapper_srbd.py:124-132; solver module absent from the
+ * reference tree).  Each iteration forms the step problem at the iterate
+ * (defects c' = A x + B u + c - x+, gradients q' = Q x + M u + q,
+ * r' = M'x + R u + r, constraint residuals e' = e - C x - D u, x0 - x_0),
+ * solves it with mpxg_lqr_eq_solve_method (`method`) and takes the full step
+ * (the problem is linear-quadratic: the Newton step is exact, and a second
+ * iteration refines float32's rounding).  lq.X [B,N+1,n] and lq.U [B,N,m]
+ * hold the starting iterate on entry and the result on return; lq.lam,
+ * lq.nu, lq.K, lq.k, lq.Knu, lq.knu receive the multipliers and gains of
+ * the last step; lq.workspace as for mpxg_lqr_eq_solve.  kkt (optional)
+ * [B,3] = (primal residual, dual residual / (1 + max |gradient|), max) of
+ * the result.  iters = 0 only evaluates kkt at the caller's X, U, lam, nu.
+ * step: device workspace of
+ * mpxg_lqr_eq_sqp_workspace_bytes(batch, N, n, m, n_eq) bytes. */
+typedef struct {
+  mpxg_lq_eq_io lq;
+  int iters;
+  int method;
+  float* kkt;
+  float* step;
+} mpxg_lq_eq_sqp_io;
+size_t mpxg_lqr_eq_sqp_workspace_bytes(int batch, int N, int n, int m, int n_eq);
+mpxg_status mpxg_lqr_eq_sqp(void* stream, const mpxg_lq_eq_sqp_io* io);
+
 /* Allocation-free batched solve.  No counterpart in the reference.  For
  * callers that cannot allocate device memory when they solve (a real-time
  * loop that forbids cudaMalloc after start-up, or a plugin host that hands

@@ -68,6 +68,11 @@ class LqEqIO(ctypes.Structure):
                     "K", "k", "Knu", "knu", "X", "U", "lam", "nu", "workspace")]
 
 
+class LqEqSqpIO(ctypes.Structure):
+    _fields_ = [("lq", LqEqIO), ("iters", ctypes.c_int), ("method", ctypes.c_int), ("kkt", ctypes.c_void_p),
+                ("step", ctypes.c_void_p)]
+
+
 class BatchIO(ctypes.Structure):
     _fields_ = [("batch", ctypes.c_int), ("slot", ctypes.c_void_p), ("horizon", ctypes.c_void_p),
                 ("x0", ctypes.c_void_p), ("X_in", ctypes.c_void_p), ("U_in", ctypes.c_void_p),
@@ -119,7 +124,7 @@ class WbModel(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_xla_prepare", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_solve_vjp",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_xla_prepare", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_lqr_eq_sqp_workspace_bytes", "mpxg_lqr_eq_sqp", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
@@ -178,6 +183,10 @@ def load(build_if_missing=True):
     L.mpxg_lqr_eq_solve.restype = ctypes.c_int
     L.mpxg_lqr_eq_solve_method.argtypes = [vp, ctypes.POINTER(LqEqIO), ctypes.c_int]
     L.mpxg_lqr_eq_solve_method.restype = ctypes.c_int
+    L.mpxg_lqr_eq_sqp_workspace_bytes.argtypes = [ctypes.c_int] * 5
+    L.mpxg_lqr_eq_sqp_workspace_bytes.restype = ctypes.c_size_t
+    L.mpxg_lqr_eq_sqp.argtypes = [vp, ctypes.POINTER(LqEqSqpIO)]
+    L.mpxg_lqr_eq_sqp.restype = ctypes.c_int
     L.mpxg_wb_terms.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 7
     L.mpxg_wb_terms.restype = ctypes.c_int
     L.mpxg_wb_interface.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 10

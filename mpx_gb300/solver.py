@@ -328,6 +328,45 @@ def lqr_eq_solve(A, B, c, Q, R, M, q, r, C, D, e, x0, stream=None, method=0):
     return out
 
 
+def lqr_eq_sqp(A, B, c, Q, R, M, q, r, C, D, e, x0, X, U, iters=2, stream=None, method=0, lam=None, nu=None):
+    """SQP iterations on the batched equality-constrained LQ problem
+    (mpxg_lqr_eq_sqp) from the iterate X [B,N+1,n], U [B,N,m]: each iteration
+    solves the step problem at the iterate with the constrained Riccati
+    (method 0 tensor cores, 1 CUDA cores) and takes the full step.  Returns
+    dict X, U (the result), lam, nu (its multipliers), K, k, Knu, knu (the
+    last step's gains), kkt [B,3] (primal residual, relative dual residual,
+    their maximum).  iters=0 evaluates kkt at X, U and the given lam, nu."""
+    L = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    names = ("A", "Bm", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+    t = [torch.as_tensor(a).to(device=dev, dtype=_F32).contiguous() for a in (A, B, c, Q, R, M, q, r, C, D, e, x0)]
+    Bsz, N, n, _ = t[0].shape
+    m, ne = t[1].shape[-1], t[8].shape[-2]
+    out = dict(K=torch.empty(Bsz, N, m, n, device=dev), k=torch.empty(Bsz, N, m, device=dev),
+               Knu=torch.empty(Bsz, N, ne, n, device=dev), knu=torch.empty(Bsz, N, ne, device=dev),
+               X=torch.as_tensor(X).to(device=dev, dtype=_F32).contiguous().clone(),
+               U=torch.as_tensor(U).to(device=dev, dtype=_F32).contiguous().clone(),
+               lam=torch.empty(Bsz, N + 1, n, device=dev), nu=torch.empty(Bsz, N, ne, device=dev),
+               kkt=torch.empty(Bsz, 3, device=dev))
+    if lam is not None:
+        out["lam"].copy_(torch.as_tensor(lam, dtype=_F32))
+    if nu is not None:
+        out["nu"].copy_(torch.as_tensor(nu, dtype=_F32))
+    ws = torch.empty(max(int(L.mpxg_lqr_eq_workspace_bytes(Bsz, N, n)) // 4, 1), device=dev)
+    step = torch.empty(max(int(L.mpxg_lqr_eq_sqp_workspace_bytes(Bsz, N, n, m, ne)) // 4, 1), device=dev)
+    io = _lib.LqEqSqpIO()
+    io.lq.batch, io.lq.N, io.lq.n, io.lq.m, io.lq.n_eq = Bsz, N, n, m, ne
+    for name, ten in zip(names, t):
+        setattr(io.lq, name, _ptr(ten))
+    for name in ("K", "k", "Knu", "knu", "X", "U", "lam", "nu"):
+        setattr(io.lq, name, _ptr(out[name]))
+    io.lq.workspace = _ptr(ws)
+    io.iters, io.method, io.kkt, io.step = int(iters), int(method), _ptr(out["kkt"]), _ptr(step)
+    _lib.check(L.mpxg_lqr_eq_sqp(_stream_handle(stream), ctypes.byref(io)), None, "mpxg_lqr_eq_sqp")
+    out["_keep"] = (t, ws, step)
+    return out
+
+
 def gait_tables(stream, desc, batch, n_max, x0, X, U, V, v_ref, leg_time, reference, parameter, gait, mode,
                 slot=None, horizon=None, drift_std=0.0, seed=0):
     """mpxg_gait_tables for `batch` entries (pool rows `slot`); `gait` =

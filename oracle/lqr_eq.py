@@ -115,3 +115,52 @@ def dense_lqr_eq(A, B, c, Q, R, M, q, r, C, D, e, x0):
     lam = -mult[:nd].reshape(N + 1, n)
     nu = mult[nd:].reshape(N, pq)
     return X, U, lam, nu
+
+
+def step_data(A, B, c, Q, R, M, q, r, C, D, e, x0, X, U):
+    """The step problem's data at the iterate (X, U): defects
+    c' = A x + B u + c - x+, cost gradients q' = Q x + M u + q (terminal
+    Q_N x_N + q_N), r' = M'x + R u + r, constraint residuals
+    e' = e - C x - D u, and x0' = x0 - x_0.  The step (dX, dU) solves the LQ
+    problem with the same matrices and these vectors."""
+    N = A.shape[0]
+    cs = np.einsum("tij,tj->ti", A, X[:N]) + np.einsum("tij,tj->ti", B, U) + c - X[1:]
+    qs = np.einsum("tij,tj->ti", Q, X).copy()
+    qs[:N] += np.einsum("tij,tj->ti", M, U)
+    qs += q
+    rs = np.einsum("tji,tj->ti", M, X[:N]) + np.einsum("tij,tj->ti", R, U) + r
+    es = e - np.einsum("tij,tj->ti", C, X[:N]) - np.einsum("tij,tj->ti", D, U)
+    return cs, qs, rs, es, x0 - X[0]
+
+
+def sqp_eq(A, B, c, Q, R, M, q, r, C, D, e, x0, X, U, iters=1, dtype=np.float64):
+    """SQP on the constrained LQ problem from the iterate (X, U): each
+    iteration solves the step problem (step_data) with riccati_eq and takes
+    the full step.  The problem is linear-quadratic, so one iteration lands
+    on riccati_eq's direct solution up to rounding.  Returns dict X, U, lam,
+    nu (multipliers of the result) and K, k, Knu, knu of the last step."""
+    f = lambda a: np.asarray(a, dtype=dtype)
+    A, B, c, Q, R, M, q, r, C, D, e, x0, X, U = map(f, (A, B, c, Q, R, M, q, r, C, D, e, x0, X, U))
+    X, U = X.copy(), U.copy()
+    for _ in range(iters):
+        cs, qs, rs, es, xs = step_data(A, B, c, Q, R, M, q, r, C, D, e, x0, X, U)
+        s = riccati_eq(A, B, cs, Q, R, M, qs, rs, C, D, es, xs, dtype=dtype)
+        X, U = X + s["X"], U + s["U"]
+    return dict(s, X=X, U=U)
+
+
+def kkt_eq(A, B, c, Q, R, M, q, r, C, D, e, x0, X, U, lam, nu):
+    """KKT residual of (X, U, lam, nu): primal = max |defect|, |C x + D u - e|,
+    |x0 - x_0|; dual = max |g_x + A'lam+ + C'nu - lam| (t = 1..N-1),
+    |g_N - lam_N|, |g_u + B'lam+ + D'nu| (t = 0..N-1), relative to
+    1 + max |gradient| (g_x = Q x + M u + q, g_u = M'x + R u + r).  lam_0 is
+    the multiplier of x_0 = x0 and has no stationarity row.  Returns
+    (primal, relative dual, max of the two)."""
+    N = A.shape[0]
+    cs, qs, rs, es, xs = step_data(A, B, c, Q, R, M, q, r, C, D, e, x0, X, U)
+    primal = max(np.abs(cs).max(), np.abs(es).max(), np.abs(xs).max())
+    dx = qs[:N] + np.einsum("tji,tj->ti", A, lam[1:]) + np.einsum("tji,tj->ti", C, nu) - lam[:N]
+    du = rs + np.einsum("tji,tj->ti", B, lam[1:]) + np.einsum("tji,tj->ti", D, nu)
+    dual = max(np.abs(dx[1:]).max() if N > 1 else 0.0, np.abs(qs[N] - lam[N]).max(), np.abs(du).max())
+    rel = dual / (1.0 + max(np.abs(qs).max(), np.abs(rs).max()))
+    return primal, rel, max(primal, rel)

@@ -119,3 +119,82 @@ def test_lqr_eq_two_waves(cuda, method):
             e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
             e32 = np.abs(o32[k] - o[k]).max() / np.abs(o[k]).max()
             assert e < max(2e-4, 8.0 * e32), (k, b, e, e32)
+
+
+KEYS_EQ = ("A", "B", "c", "Q", "R", "M", "q", "r", "C", "D", "e", "x0")
+
+
+def _eq_case(B, n, m, ne, N, seed):
+    d = P.random_lq_eq(B, n=n, m=m, n_eq=ne, N=N, seed=seed)
+    if n == 8:
+        d["M"] = 0.002 * np.random.default_rng(3).normal(size=d["M"].shape)
+        d["r"] = np.random.default_rng(4).normal(size=d["r"].shape)
+    rng = np.random.default_rng(seed + 1)
+    X0, U0 = rng.normal(size=(B, N + 1, n)), rng.normal(size=(B, N, m))
+    return d, X0, U0
+
+
+@pytest.mark.parametrize("method", [0, 1])
+@pytest.mark.parametrize("n,m,ne,N,B", [(8, 5, 2, 6, 3), (16, 8, 4, 20, 3), (72, 30, 12, 100, 2)])
+def test_lqr_eq_sqp_matches_oracle(cuda, n, m, ne, N, B, method):
+    """Two SQP iterations from a random iterate on the GPU against the FP64
+    oracle's solution (one SQP iteration of an LQ problem is its direct
+    solution): 2e-4 relative, or 8x the error of the oracle's own float32
+    SQP where conditioning puts float32 near that.  The KKT residual the GPU
+    reports is at the float32 level of the oracle's own float32 run."""
+    from mpx_gb300.solver import lqr_eq_sqp
+    from oracle.lqr_eq import kkt_eq, riccati_eq, sqp_eq
+    d, X0, U0 = _eq_case(B, n, m, ne, N, seed=n + N)
+    g = lqr_eq_sqp(*[d[k] for k in KEYS_EQ], X0, U0, iters=2, method=method)
+    torch.cuda.synchronize()
+    kkt = g["kkt"].cpu().numpy()
+    for b in range(B):
+        args = [d[k][b] for k in KEYS_EQ]
+        o = riccati_eq(*args)
+        o32 = sqp_eq(*args, X0[b], U0[b], iters=2, dtype=np.float32)
+        for k in ("X", "U", "lam", "nu"):
+            a = g[k][b].cpu().numpy()
+            e = np.abs(a - o[k]).max() / np.abs(o[k]).max()
+            e32 = np.abs(o32[k] - o[k]).max() / np.abs(o[k]).max()
+            assert e < max(2e-4, 8.0 * e32), (k, b, e, e32)
+        k32 = kkt_eq(*args, *[o32[k].astype(np.float64) for k in ("X", "U", "lam", "nu")])
+        assert np.isfinite(kkt[b]).all() and kkt[b, 2] < max(1e-4, 8.0 * k32[2]), (b, kkt[b], k32)
+
+
+@pytest.mark.parametrize("n,m,ne,N", [(8, 5, 2, 6), (72, 30, 12, 40)])
+def test_lqr_eq_kkt_evaluation(cuda, n, m, ne, N):
+    """iters = 0 evaluates the KKT residual of the caller's point: at points
+    off the solution (a random iterate, a perturbed costate or multiplier)
+    the GPU's float32 residual matches the FP64 oracle's within 1e-3
+    relative; a component left on the solution sits at float32 rounding
+    (absolute 2e-5)."""
+    from mpx_gb300.solver import lqr_eq_sqp
+    from oracle.lqr_eq import kkt_eq, riccati_eq
+    B = 3
+    d, X0, U0 = _eq_case(B, n, m, ne, N, seed=11)
+    sol = [riccati_eq(*[d[k][b] for k in KEYS_EQ]) for b in range(B)]
+    X = np.stack([s["X"] for s in sol]); U = np.stack([s["U"] for s in sol])
+    lam = np.stack([s["lam"] for s in sol]); nu = np.stack([s["nu"] for s in sol])
+    X[0] = X0[0]                  # instance 0: a random iterate (primal and dual off)
+    lam[1, N // 2, 1] += 0.5      # instance 1: one costate off
+    nu[2, N // 3, 0] += 0.5       # instance 2: one multiplier off
+    g = lqr_eq_sqp(*[d[k] for k in KEYS_EQ], X, U, iters=0, lam=lam, nu=nu)
+    torch.cuda.synchronize()
+    kkt = g["kkt"].cpu().numpy()
+    for b in range(B):
+        f32 = lambda a: a.astype(np.float32).astype(np.float64)
+        o = kkt_eq(*[f32(d[k][b]) for k in KEYS_EQ], f32(X[b]), f32(U[b]), f32(lam[b]), f32(nu[b]))
+        assert o[2] > 1e-3, (b, o)
+        assert np.allclose(kkt[b], o, rtol=1e-3, atol=2e-5), (b, kkt[b], o)
+        assert abs(kkt[b, 2] - o[2]) <= 1e-3 * o[2], (b, kkt[b], o)
+    assert np.array_equal(g["X"].cpu().numpy(), X.astype(np.float32))  # iters = 0 leaves the point
+
+
+def test_lqr_eq_sqp_rejects_bad_arguments(cuda):
+    from mpx_gb300._lib import MpxgError
+    from mpx_gb300.solver import lqr_eq_sqp
+    d, X0, U0 = _eq_case(1, 8, 5, 2, 4, seed=2)
+    with pytest.raises(MpxgError):
+        lqr_eq_sqp(*[d[k] for k in KEYS_EQ], X0, U0, iters=101)
+    with pytest.raises(MpxgError):
+        lqr_eq_sqp(*[d[k] for k in KEYS_EQ], X0, U0, iters=1, method=2)
