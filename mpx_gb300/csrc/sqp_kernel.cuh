@@ -112,6 +112,23 @@ __device__ __forceinline__ void st_vec(float* __restrict__ dst, const float* src
   for (int r = (N / 4) * 4; r < N; ++r) dst[r] = src[r];
 }
 
+// 16-byte asynchronous global -> shared copies (L2 only), in commit groups
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+// FLOATS floats (a multiple of 4, both ends 16-byte aligned) spread over the warp's lanes
+template <int FLOATS>
+__device__ __forceinline__ void cp_async_block(float* dst, const float* src, int lane) {
+#pragma unroll
+  for (int q = lane; q < FLOATS / 4; q += 32) cp_async16(dst + 4 * q, src + 4 * q);
+}
+
 template <class M>
 struct Dims {
   static constexpr int NX = M::NX, NU = M::NU;
@@ -120,12 +137,16 @@ struct Dims {
   static constexpr int NP = NX + 1;           // value-function rows: x, affine
   static constexpr int LDP = rup4(NP);        // shared / scratch column stride of P
   static constexpr int FS = rup4(NX);         // scratch column stride of F
+  static constexpr int FTS = rup4(NZ);        // shared row stride of F's rows (WarpSmem::FT)
   static constexpr int LD = (M::LEGS == 4) ? 3 : 6;  // controls per leg / foot
   static constexpr int QB = M::IDENT_RES ? 0 : 4;    // quaternion Gauss-Newton block
   // per-stage cost data: gradient (NX+NU), barrier blocks, quaternion block, cost value
   static constexpr int G_GRAD = 0, G_HB = NX + NU, G_QQ = G_HB + M::LEGS * LD * LD, G_L = G_QQ + QB * QB;
   static constexpr int GS = rup4(G_L + 1);
   static constexpr int RS = rup4(NU + NX);    // forward-sweep partial row
+  // staged stage blocks (WarpSmem::stg): the backward sweep stages F at 0 and
+  // G at NZ * FS; the forward sweep stages P, K, F and G at SP, SK, SF, SG
+  static constexpr int SP = 0, SK = NP * LDP, SF = SK + NP * NU, SG = SF + NZ * FS, STG = SG + GS;
   static constexpr int TANG = 2;              // tangents per dual-number pass
 };
 
@@ -135,39 +156,11 @@ struct __align__(16) WarpSmem {
   float w[24];
   float P[D::NP * D::LDP];     // value function of stage t+1, column-major
   float Praw[D::NP * D::LDP];  // unsymmetrised new value function
-  float F[D::NZ * D::LDP];     // columns of the augmented dynamics F of stage t
+  float FT[D::NX * D::FTS];    // rows 0..n-1 of stage t's F (the backward sweep's F'T products)
   float CT[D::NZ * 4];         // pivot block columns, row-interleaved
   float red[(D::NX + 1) * D::RS];
-  float G[D::GS];              // cost data of stage t
   float dx[16];
-};
-
-// Cooperative, coalesced copy of one contiguous scratch block (FLOATS floats,
-// a multiple of 4) into per-lane float4 registers: lane l holds float4 l, l+32, ...
-template <int FLOATS>
-struct BlockRegs {
-  static constexpr int Q = FLOATS / 4;
-  static constexpr int PER = (Q + 31) / 32;
-  float4 v[PER];
-  __device__ __forceinline__ void load(const float* src, int lane) {
-#pragma unroll
-    for (int r = 0; r < PER; ++r) {
-      const int q = lane + 32 * r;
-      if (q < Q) v[r] = *reinterpret_cast<const float4*>(src + 4 * q);
-    }
-  }
-  // store with the block's column stride CS remapped to the shared stride SS
-  template <int CS, int SS>
-  __device__ __forceinline__ void store_cols(float* dst, int lane) const {
-#pragma unroll
-    for (int r = 0; r < PER; ++r) {
-      const int q = lane + 32 * r;
-      if (q < Q) {
-        const int col = (4 * q) / CS, row = (4 * q) - col * CS;
-        *reinterpret_cast<float4*>(dst + col * SS + row) = v[r];
-      }
-    }
-  }
+  float stg[2][D::STG];        // stage blocks copied in by cp.async, double-buffered
 };
 
 template <class M>
@@ -625,20 +618,22 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
   float gcol[FS];  // ELEM 2: column j of G (state lanes); ELEM >= 1: phi (lane JA)
 #pragma unroll
   for (int i = 0; i < FS; ++i) gcol[i] = 0.0f;
-  BlockRegs<NZ * FS> fpre;
-  BlockRegs<D::GS> gpre;
-  fpre.load(s.F + (size_t)(hi - 1) * NZ * FS, lane);
-  gpre.load(s.G + (size_t)(hi - 1) * D::GS, lane);
+  // stage t's F and cost data G are copied into sm.stg[buf] by cp.async one
+  // stage ahead (the copy of t - 1 runs while stage t is eliminated)
+  auto stage_in = [&](int t, int b) {
+    cp_async_block<NZ * FS>(sm.stg[b], s.F + (size_t)t * NZ * FS, lane);
+    cp_async_block<D::GS>(sm.stg[b] + NZ * FS, s.G + (size_t)t * D::GS, lane);
+  };
+  stage_in(hi - 1, 0);
+  cp_async_commit();
+  int buf = 0;
   for (int t = hi - 1; t >= lo; --t) {
-    // ---- stage t's F columns and cost data into shared memory; prefetch t-1
-    fpre.template store_cols<FS, LDP>(sm.F, lane);
-    gpre.template store_cols<D::GS, D::GS>(sm.G, lane);
-    if (t > lo) {
-      fpre.load(s.F + (size_t)(t - 1) * NZ * FS, lane);
-      gpre.load(s.G + (size_t)(t - 1) * D::GS, lane);
-    }
+    if (t > lo) stage_in(t - 1, buf ^ 1);
+    cp_async_commit();
+    cp_async_wait<1>();  // stage t's copies (all but the newest group) have landed
     __syncwarp();
-    const float* Gt = sm.G;
+    const float* Fr = sm.stg[buf];
+    const float* Gt = Fr + NZ * FS;
     // ---- column j of F and of the cost model G
     float fcol[NP], h[NZ];
 #pragma unroll
@@ -648,12 +643,15 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
     if (j < NZ) {
 #pragma unroll
       for (int q = 0; q < FS / 4; ++q) {
-        const float4 v = *reinterpret_cast<const float4*>(sm.F + j * LDP + 4 * q);
+        const float4 v = *reinterpret_cast<const float4*>(Fr + j * FS + 4 * q);
         if (4 * q < NX) fcol[4 * q] = v.x;
         if (4 * q + 1 < NX) fcol[4 * q + 1] = v.y;
         if (4 * q + 2 < NX) fcol[4 * q + 2] = v.z;
         if (4 * q + 3 < NX) fcol[4 * q + 3] = v.w;
       }
+      // F's rows for the F'T products: lane j writes column j of them
+#pragma unroll
+      for (int r = 0; r < NX; ++r) sm.FT[r * D::FTS + j] = fcol[r];
     }
     fcol[NX] = (j == JA) ? 1.0f : 0.0f;
     if (j < NX) {
@@ -684,31 +682,41 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
 #pragma unroll
       for (int i = 0; i < JA; ++i) h[i] = Gt[D::G_GRAD + i];
     }
-    if (j == JA) sm.F[JA * LDP + NX] = 1.0f;  // the affine column's last row
     __syncwarp();
     // ---- T = P F[:, j];  H[:, j] = G[:, j] + F^T T
-    float tv[LDP];
+    // T over the NP rows of P (fcol[NX] is 1 on the affine lane, else 0); then
+    // F^T T as NX rank-1 updates with the rows of F, each advancing NZ
+    // independent sums, and F's last row (1 in the affine column) adds T[NX]
+    // to H[JA, j].
+    float tv[NP];
 #pragma unroll
-    for (int i = 0; i < LDP; ++i) tv[i] = 0.0f;
+    for (int i = 0; i < NP; ++i) tv[i] = 0.0f;
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
       const float fk = fcol[k];
+      const float* pk = sm.P + k * LDP;
 #pragma unroll
-      for (int q = 0; q < LDP / 4; ++q) {
-        const float4 pv = *reinterpret_cast<const float4*>(sm.P + k * LDP + 4 * q);
+      for (int q = 0; q < NP / 4; ++q) {
+        const float4 pv = *reinterpret_cast<const float4*>(pk + 4 * q);
         tv[4 * q] += pv.x * fk; tv[4 * q + 1] += pv.y * fk; tv[4 * q + 2] += pv.z * fk; tv[4 * q + 3] += pv.w * fk;
       }
+#pragma unroll
+      for (int r = (NP / 4) * 4; r < NP; ++r) tv[r] += pk[r] * fk;
     }
 #pragma unroll
-    for (int i = 0; i < NZ; ++i) {
-      float a = h[i];
+    for (int r = 0; r < NX; ++r) {
+      const float tr = tv[r];
+      const float* fr = sm.FT + r * D::FTS;
 #pragma unroll
-      for (int q = 0; q < LDP / 4; ++q) {
-        const float4 fv = *reinterpret_cast<const float4*>(sm.F + i * LDP + 4 * q);
-        a += fv.x * tv[4 * q] + fv.y * tv[4 * q + 1] + fv.z * tv[4 * q + 2] + fv.w * tv[4 * q + 3];
+      for (int q = 0; q < D::FTS / 4; ++q) {
+        const float4 fv = *reinterpret_cast<const float4*>(fr + 4 * q);
+        if (4 * q < NZ) h[4 * q] += fv.x * tr;
+        if (4 * q + 1 < NZ) h[4 * q + 1] += fv.y * tr;
+        if (4 * q + 2 < NZ) h[4 * q + 2] += fv.z * tr;
+        if (4 * q + 3 < NZ) h[4 * q + 3] += fv.w * tr;
       }
-      h[i] = a;
     }
+    h[JA] += tv[NX];
 #pragma unroll
     for (int a = NX; a < JA; ++a)
       if (a == j) h[a] += sp.reg;
@@ -755,7 +763,7 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
       for (int a = 0; a < NU; ++a)
 #pragma unroll
         for (int q = 0; q < FS / 4; ++q) {
-          const float4 bv = *reinterpret_cast<const float4*>(sm.F + (NX + a) * LDP + 4 * q);
+          const float4 bv = *reinterpret_cast<const float4*>(Fr + (NX + a) * FS + 4 * q);
           cl[4 * q] += bv.x * kc[a]; cl[4 * q + 1] += bv.y * kc[a];
           cl[4 * q + 2] += bv.z * kc[a]; cl[4 * q + 3] += bv.w * kc[a];
         }
@@ -821,7 +829,9 @@ __device__ __forceinline__ void riccati_sweep(const SqpParams& sp, int lo, int h
       }
     }
     __syncwarp();
+    buf ^= 1;
   }
+  cp_async_wait<0>();
   if (ELEM >= 1) {
     if (ELEM == 2 && j < NX) st_vec<FS>(es->G + j * FS, gcol);
     if (j == JA) st_vec<FS>(es->phi, gcol);
@@ -846,44 +856,47 @@ __device__ __forceinline__ void forward_sweep(int lo, int hi, bool last, float c
   constexpr int NX = D::NX, NU = D::NU, NZ = D::NZ, JA = D::JA, NP = D::NP, LDP = D::LDP, FS = D::FS;
   constexpr int RS = D::RS;
   float c_cur = c_init;
-  BlockRegs<NP * LDP> ppre;
-  BlockRegs<NP * NU> kpre;
-  BlockRegs<NZ * FS> fpre3;
-  BlockRegs<D::GS> gpre3;
-  ppre.load(s.P + (size_t)lo * NP * LDP, lane);
-  kpre.load(s.K + (size_t)lo * NP * NU, lane);
-  fpre3.load(s.F + (size_t)lo * NZ * FS, lane);
-  gpre3.load(s.G + (size_t)lo * D::GS, lane);
+  // stage t's blocks are copied into sm.stg[buf] by cp.async one stage ahead,
+  // only what this sweep reads: P's columns 0..n-1, the gradient rows of G
+  // and, for t < hi, the gains K and F's closed-loop columns 0..n and its
+  // defect column
+  constexpr int GG = (NX + NU + 3) / 4 * 4;
+  static_assert(D::G_GRAD == 0 && GG <= D::GS, "gradient rows lead the cost data");
+  auto stage_in = [&](int t, int b, bool kf) {
+    float* d = sm.stg[b];
+    cp_async_block<NX * LDP>(d + D::SP, s.P + (size_t)t * NP * LDP, lane);
+    cp_async_block<GG>(d + D::SG, s.G + (size_t)t * D::GS, lane);
+    if (kf) {
+      cp_async_block<NP * NU>(d + D::SK, s.K + (size_t)t * NP * NU, lane);
+      cp_async_block<(NX + 1) * FS>(d + D::SF, s.F + (size_t)t * NZ * FS, lane);
+      cp_async_block<FS>(d + D::SF + JA * FS, s.F + (size_t)t * NZ * FS + JA * FS, lane);
+    }
+  };
   const int tend = last ? hi : hi - 1;  // last stage whose costate this sweep writes
+  stage_in(lo, 0, lo < hi);
+  cp_async_commit();
+  int buf = 0;
   float vnext = (lane < NX) ? V[lo * NX + lane] : 0.0f;  // V of the next stage, loaded a stage ahead
   for (int t = lo; t <= tend; ++t) {
     const float vt = vnext;
     if (lane < NX && t + 1 <= tend) vnext = V[(t + 1) * NX + lane];
-    // ---- stage t's value function, gains, closed loop and cost data; prefetch t+1
-    ppre.template store_cols<LDP, LDP>(sm.P, lane);
-    gpre3.template store_cols<D::GS, D::GS>(sm.G, lane);
-    if (t < hi) {
-      kpre.template store_cols<NU, NU>(sm.Praw, lane);
-      fpre3.template store_cols<FS, LDP>(sm.F, lane);
-    }
-    if (t + 1 <= tend) {
-      ppre.load(s.P + (size_t)(t + 1) * NP * LDP, lane);
-      gpre3.load(s.G + (size_t)(t + 1) * D::GS, lane);
-    }
-    if (t + 1 < hi) {
-      kpre.load(s.K + (size_t)(t + 1) * NP * NU, lane);
-      fpre3.load(s.F + (size_t)(t + 1) * NZ * FS, lane);
-    }
+    if (t + 1 <= tend) stage_in(t + 1, buf ^ 1, t + 1 < hi);
+    cp_async_commit();
+    cp_async_wait<1>();  // stage t's copies have landed
     __syncwarp();
+    const float* Pr = sm.stg[buf] + D::SP;
+    const float* Kr = sm.stg[buf] + D::SK;
+    const float* Fr = sm.stg[buf] + D::SF;
+    const float* Gr = sm.stg[buf] + D::SG;
     if (lane < NX) {
       const float dxi = sm.dx[lane];
-      float lam = sm.P[lane * LDP + NX];
+      float lam = Pr[lane * LDP + NX];
 #pragma unroll
-      for (int k = 0; k < NX; ++k) lam += sm.P[lane * LDP + k] * sm.dx[k];
+      for (int k = 0; k < NX; ++k) lam += Pr[lane * LDP + k] * sm.dx[k];
       *a_lc += (double)((lam - 2.0f * vt) * c_cur);
       *a_vc += (double)(vt * c_cur);
       *a_cs += (double)(c_cur * c_cur);
-      *a_gd += (double)(sm.G[D::G_GRAD + lane] * dxi);
+      *a_gd += (double)(Gr[D::G_GRAD + lane] * dxi);
       s.L[t * NX + lane] = lam;
       s.dX[t * NX + lane] = dxi;
     }
@@ -893,9 +906,9 @@ __device__ __forceinline__ void forward_sweep(int lo, int hi, bool last, float c
       const float sc = (lane == JA) ? 1.0f : sm.dx[col];
       float* rw = sm.red + col * RS;
 #pragma unroll
-      for (int a = 0; a < NU; ++a) rw[a] = sm.Praw[col * NU + a] * sc;
+      for (int a = 0; a < NU; ++a) rw[a] = Kr[col * NU + a] * sc;
 #pragma unroll
-      for (int i = 0; i < NX; ++i) rw[NU + i] = sm.F[col * LDP + i] * sc;
+      for (int i = 0; i < NX; ++i) rw[NU + i] = Fr[col * FS + i] * sc;
     }
     __syncwarp();
     float sum = 0.0f;
@@ -903,16 +916,18 @@ __device__ __forceinline__ void forward_sweep(int lo, int hi, bool last, float c
 #pragma unroll
       for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + lane];
       s.dU[t * NU + lane] = sum;
-      *a_gd += (double)(sm.G[D::G_GRAD + NX + lane] * sum);
+      *a_gd += (double)(Gr[D::G_GRAD + NX + lane] * sum);
     } else if (lane >= 16 && lane < 16 + NX) {
 #pragma unroll
       for (int r2 = 0; r2 <= NX; ++r2) sum += sm.red[r2 * RS + NU + (lane - 16)];
     }
-    if (lane < NX) c_cur = sm.F[JA * LDP + lane];  // defect of stage t pairs with V_{t+1}
+    if (lane < NX) c_cur = Fr[JA * FS + lane];  // defect of stage t pairs with V_{t+1}
     __syncwarp();
     if (lane >= 16 && lane < 16 + NX) sm.dx[lane - 16] = sum;
     __syncwarp();
+    buf ^= 1;
   }
+  cp_async_wait<0>();
   __syncwarp();
 }
 
@@ -956,7 +971,7 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   if (lane < 24) sm.w[lane] = bp.w[(size_t)b * 24 + lane];
   // zero padding rows of the shared P / F columns (read by the float4 products)
   for (int e = lane; e < NP * LDP; e += 32) { sm.P[e] = 0.0f; sm.Praw[e] = 0.0f; }
-  for (int e = lane; e < NZ * LDP; e += 32) sm.F[e] = 0.0f;
+  for (int e = lane; e < NX * D::FTS; e += 32) sm.FT[e] = 0.0f;
   __syncwarp();
 
   float rho = sp.rho0;

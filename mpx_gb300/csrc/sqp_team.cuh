@@ -236,7 +236,7 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     for (int e = tid; e < N * NU; e += NT) U[e] = bp.U_in[uo + e];
   if (lane < 24) sm.w[lane] = bp.w[(size_t)b * 24 + lane];
   for (int e = lane; e < NP * LDP; e += 32) { sm.P[e] = 0.0f; sm.Praw[e] = 0.0f; }
-  for (int e = lane; e < NZ * LDP; e += 32) sm.F[e] = 0.0f;
+  for (int e = lane; e < NX * D::FTS; e += 32) sm.FT[e] = 0.0f;
   if (tid == 0) team_bounds<W>(N, ts.bounds);
   __syncthreads();
   const int lo = ts.bounds[warp], hi = ts.bounds[warp + 1];

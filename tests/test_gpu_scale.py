@@ -85,8 +85,13 @@ def test_batched_tick_4096_matches_oracle(oracle, cuda):
     eg, e32 = _errors(g, o, s["horizon"]), _errors(o32, o, s["horizon"])
     for key in ("X", "U", "V", "K", "k"):
         assert eg[key] < max(1e-4, 3.0 * e32[key]), (key, eg[key], e32[key])
+    # the GPU result is as good a KKT point as the oracle's (FP64 evaluation):
+    # within 2x the FP64 run's residual, or 3x the oracle's own float32 run's
+    # (near the 1e-5 gate float32 rounding sets the residual)
     kg = oracle.kkt_residual(wl.desc, s["x0"], g["X"], g["U"], g["V"], s["ref"], s["par"], W, s["horizon"])
-    assert np.all(kg[:, 2] <= np.maximum(2.0 * o["kkt"][:, 2], 1e-5)), (kg[:, 2].max(), o["kkt"][:, 2].max())
+    k32 = oracle.kkt_residual(wl.desc, s["x0"], o32["X"], o32["U"], o32["V"], s["ref"], s["par"], W, s["horizon"])
+    bound = np.maximum(np.maximum(2.0 * o["kkt"][:, 2], 3.0 * k32[:, 2]), 1e-5)
+    assert np.all(kg[:, 2] <= bound), (kg[:, 2].max(), o["kkt"][:, 2].max(), k32[:, 2].max())
     assert np.all(g["status"] == 0), g["status"]
 
 
