@@ -468,8 +468,10 @@ def run_ours(args, rank, world, local_rank):
     tuned = None
     wpb, bps, tw, tm = 0, 0, 0, 0
     if not args.no_autotune and not args.profile:
-        from mpx_gb300.autotune import tune
-        tuned = tune(wl, opts, device=dev)
+        # geometry measured on the steady-state tick this bench times (a cold
+        # first tick runs more line-search trials and favours other shapes)
+        from mpx_gb300.autotune import tune, warm_workload
+        tuned = tune(warm_workload(wl, opts, device=dev, drift_std=DRIFT), opts, device=dev, tag="warm")
         wpb, bps, tw, tm = tuned["best"]
     tick_opts = dataclasses.replace(opts, team_warps=tw, team_min_horizon=tm) if tw else opts
     tr = TickRunner(wl, tick_opts, device=dev, drift_std=DRIFT, warps_per_block=wpb, blocks_per_sm=bps)

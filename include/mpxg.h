@@ -286,6 +286,48 @@ typedef struct {
 } mpxg_gait_args;
 mpxg_status mpxg_gait_tables(void* stream, const mpxg_gait_args* args);
 
+/* Device work queue (continuous batching without a launch per batch): one
+ * persistent SQP kernel on `stream` drains a queue that the host fills while
+ * it runs.  `pool` describes the instances the queue may solve (as for
+ * mpxg_solve, pool->batch rows, no slot map; pool->first is ignored): the
+ * host updates a row's inputs, then mpxg_queue_push(row) publishes it; the
+ * kernel solves it exactly as mpxg_solve's one-warp kernels would and flags
+ * it done, and mpxg_queue_result copies its result row (m controls, the KKT
+ * triple, the status) to the host.  The ring holds `capacity` tickets: a
+ * push whose ring entry still holds an unfinished ticket returns
+ * MPXG_ERR_NOT_READY.  Every wait of the kernel is bounded: a warp waiting
+ * longer than idle_timeout_ns (1 ms .. 60 s, %globaltimer) for work gives up,
+ * and the queue then reports MPXG_ERR_TIMEOUT (push, result, finish) instead
+ * of hanging.  mpxg_queue_finish lets the kernel drain what was pushed,
+ * waits for it, frees the queue and returns MPXG_ERR_TIMEOUT if a wait ran
+ * out.  Stands in for the reference's one-call-per-tick loop
+ * (mpx/utils/mpc_wrapper.py:297-365). */
+typedef struct mpxg_queue mpxg_queue;
+mpxg_status mpxg_queue_start(mpxg_handle* h, void* stream, const mpxg_batch_io* pool, int capacity,
+                             long long idle_timeout_ns, mpxg_queue** out);
+mpxg_status mpxg_queue_push(mpxg_queue* q, int row, long long* ticket);
+mpxg_status mpxg_queue_result(mpxg_queue* q, long long ticket, float* row_out);
+mpxg_status mpxg_queue_finish(mpxg_queue* q);
+
+/* One persistent SQP launch over the batches of two handles of different
+ * models, so that a mix of robot models takes a single solve launch (the
+ * served stream's quadrupeds and bipeds; the reference serves one model per
+ * optimizers.mpc call, mpx/utils/mpc_wrapper_srbd.py:124-132).  Built pairs
+ * (a, b): (MPXG_MODEL_SRBD_RPY12, MPXG_MODEL_BIPED_WRENCH12) and
+ * (MPXG_MODEL_SRBD_QUAT13, MPXG_MODEL_BIPED_WRENCH12); the handles must
+ * share n_max and the device and stay alive while the mixed handle is used.
+ * Each instance is solved by one warp with its own handle's model and
+ * options, in the same order of operations as mpxg_solve's one-warp kernels
+ * (the time-parallel team path is not used), so a result does not depend on
+ * the mix it was solved in.  The queue serves the longest horizons of both
+ * batches first when both carry horizons.  io_a / io_b as for mpxg_solve on
+ * a / b (either batch may be 0).  The mixed handle owns its own scratch:
+ * mpxg_mixed_create allocates, mpxg_solve_mixed does not. */
+typedef struct mpxg_mixed mpxg_mixed;
+mpxg_status mpxg_mixed_create(mpxg_handle* a, mpxg_handle* b, mpxg_mixed** out);
+void mpxg_mixed_destroy(mpxg_mixed* mx);
+mpxg_status mpxg_solve_mixed(mpxg_mixed* mx, void* stream, const mpxg_batch_io* io_a, const mpxg_batch_io* io_b);
+
 /* Time-varying LQR in absolute coordinates for a batch (isolated KKT/LQR):
  * x_{t+1} = A_t x_t + B_t u_t + c_t, cost 1/2 x'Qx + x'Mu + 1/2 u'Ru + q'x + r'u,
  * terminal Q[N], q[N].  A [B,N,n,n], Bm [B,N,n,m], c [B,N,n], Q [B,N+1,n,n],
@@ -408,6 +450,8 @@ typedef struct {
   float drift_std;          /* per-tick state drift N(0, drift_std^2) added on the device */
   unsigned int seed;
   mpxg_solver_opts opts;
+  int mixed_launch;         /* nonzero (two models of a built mpxg_mixed pair): each step solves both
+                               models' ticks in one mixed-model launch; its scratch comes off the budget */
 } mpxg_server_desc;
 
 typedef struct {

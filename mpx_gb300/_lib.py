@@ -53,7 +53,8 @@ class ServedModel(ctypes.Structure):
 class ServerDesc(ctypes.Structure):
     _fields_ = [("n_models", ctypes.c_int), ("models", ctypes.POINTER(ServedModel)), ("n_max", ctypes.c_int),
                 ("budget_bytes", ctypes.c_size_t), ("max_slots", ctypes.c_int), ("streams", ctypes.c_int),
-                ("drift_std", ctypes.c_float), ("seed", ctypes.c_uint), ("opts", SolverOpts)]
+                ("drift_std", ctypes.c_float), ("seed", ctypes.c_uint), ("opts", SolverOpts),
+                ("mixed_launch", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -124,7 +125,7 @@ class WbModel(ctypes.Structure):
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
-           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_xla_prepare", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_lqr_eq_sqp_workspace_bytes", "mpxg_lqr_eq_sqp", "mpxg_solve_vjp",
+           "mpxg_lqr_workspace_bytes", "mpxg_lqr_solve", "mpxg_solve_noalloc", "mpxg_evaluate", "mpxg_xla_solve", "mpxg_xla_solve_vjp", "mpxg_xla_prepare", "mpxg_lqr_eq_workspace_bytes", "mpxg_lqr_eq_solve", "mpxg_lqr_eq_solve_method", "mpxg_lqr_eq_sqp_workspace_bytes", "mpxg_lqr_eq_sqp", "mpxg_mixed_create", "mpxg_mixed_destroy", "mpxg_solve_mixed", "mpxg_queue_start", "mpxg_queue_push", "mpxg_queue_result", "mpxg_queue_finish", "mpxg_solve_vjp",
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
@@ -187,6 +188,20 @@ def load(build_if_missing=True):
     L.mpxg_lqr_eq_sqp_workspace_bytes.restype = ctypes.c_size_t
     L.mpxg_lqr_eq_sqp.argtypes = [vp, ctypes.POINTER(LqEqSqpIO)]
     L.mpxg_lqr_eq_sqp.restype = ctypes.c_int
+    L.mpxg_mixed_create.argtypes = [vp, vp, ctypes.POINTER(vp)]
+    L.mpxg_mixed_create.restype = ctypes.c_int
+    L.mpxg_mixed_destroy.argtypes = [vp]
+    L.mpxg_mixed_destroy.restype = None
+    L.mpxg_solve_mixed.argtypes = [vp, vp, ctypes.POINTER(BatchIO), ctypes.POINTER(BatchIO)]
+    L.mpxg_solve_mixed.restype = ctypes.c_int
+    L.mpxg_queue_start.argtypes = [vp, vp, ctypes.POINTER(BatchIO), ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(vp)]
+    L.mpxg_queue_start.restype = ctypes.c_int
+    L.mpxg_queue_push.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+    L.mpxg_queue_push.restype = ctypes.c_int
+    L.mpxg_queue_result.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_float)]
+    L.mpxg_queue_result.restype = ctypes.c_int
+    L.mpxg_queue_finish.argtypes = [vp]
+    L.mpxg_queue_finish.restype = ctypes.c_int
     L.mpxg_wb_terms.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 7
     L.mpxg_wb_terms.restype = ctypes.c_int
     L.mpxg_wb_interface.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int] + [vp] * 10

@@ -36,9 +36,10 @@ def _cache_path():
     return os.environ.get("MPXG_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "mpxg", "tune.json"))
 
 
-def _key(desc, opts, n_max, batch):
+def _key(desc, opts, n_max, batch, tag=""):
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
-    return "%s|model%d|n_max%d|batch%d|iters%d" % (name, desc.model, n_max, batch, opts.sqp_iters)
+    key = "%s|model%d|n_max%d|batch%d|iters%d" % (name, desc.model, n_max, batch, opts.sqp_iters)
+    return key + ("|" + tag if tag else "")
 
 
 def _load():
@@ -57,6 +58,26 @@ def _store(cache):
             json.dump(cache, f, indent=1)
     except OSError:
         pass
+
+
+def warm_workload(wl, opts, ticks=3, device=None, drift_std=0.0):
+    """The inputs of a steady-state control tick of `wl`: `ticks` warm ticks
+    (shift, tables, solve) with the default geometry, then the next tick's
+    shift and tables, copied back as a host Workload."""
+    from . import problem as P
+    from .tick import TickRunner
+    tr = TickRunner(wl, opts, device=device, drift_std=drift_std)
+    try:
+        tr.first_tick()
+        for _ in range(ticks):
+            tr.tick()
+        tr.shift()
+        tr.tables()
+        torch.cuda.synchronize()
+        h = lambda t: t.cpu().numpy()
+        return P.Workload(wl.desc, h(tr.x0), h(tr.X), h(tr.U), h(tr.V), h(tr.ref), h(tr.par), wl.W, h(tr.horizon))
+    finally:
+        tr.solver.close()
 
 
 def time_geometry(wl, opts, warps_per_block, blocks_per_sm, reps=5, device=None, team_warps=0, team_min_horizon=0):
@@ -81,13 +102,15 @@ def time_geometry(wl, opts, warps_per_block, blocks_per_sm, reps=5, device=None,
         s.close()
 
 
-def tune(wl, opts, candidates=None, reps=5, use_cache=True, device=None):
+def tune(wl, opts, candidates=None, reps=5, use_cache=True, device=None, tag=""):
     """Measure every candidate (warps_per_block, blocks_per_sm[, team_warps,
     team_min_horizon]) on `wl` (0 = the occupancy-derived default, no team
     path) and return dict(best=(wpb, bps, team_warps, team_min_horizon),
     ms=..., table=[{wpb, bps, team_warps, team_min_horizon, ms, geometry},
-    ...], cached=bool)."""
-    key = _key(wl.desc, opts, wl.n_max, wl.batch)
+    ...], cached=bool).  `tag` names the kind of state `wl` holds (e.g.
+    "warm" for a steady-state tick, whose line searches and convergence
+    differ from a cold start's) in the cache key."""
+    key = _key(wl.desc, opts, wl.n_max, wl.batch, tag)
     cache = _load() if use_cache else {}
     if use_cache and key in cache:
         r = dict(cache[key])

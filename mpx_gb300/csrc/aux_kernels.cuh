@@ -339,16 +339,26 @@ __global__ void gait_tables_kernel(mpxg_gait_args g, int nx, int nu, int legs, i
 //
 // n_long (optional) receives the number of entries with a horizon of at least
 // split_h: the queue prefix the time-parallel team kernel takes.
+//
+// A second batch (batch2 entries, slot2 / horizon2) may be ordered together
+// with the first: its entry i is queue code batch + i (the mixed-model
+// launch).
 __global__ void __launch_bounds__(1024) order_by_horizon_kernel(int batch, int n_max, const int* __restrict__ slot,
                                                                 const int* __restrict__ horizon, int* __restrict__ order,
-                                                                int split_h = 0, int* __restrict__ n_long = nullptr) {
+                                                                int split_h = 0, int* __restrict__ n_long = nullptr,
+                                                                int batch2 = 0, const int* __restrict__ slot2 = nullptr,
+                                                                const int* __restrict__ horizon2 = nullptr) {
   extern __shared__ int bins[];       // n_max + 1 bins: bin j holds horizon n_max - j; bin n_max: invalid
   __shared__ int warp_tot[32];
   const int nb = n_max + 1;
+  const int total = batch + batch2;
+  auto hor = [&](int i) {
+    return i < batch ? horizon[slot ? slot[i] : i] : horizon2[slot2 ? slot2[i - batch] : i - batch];
+  };
   for (int j = threadIdx.x; j < nb; j += blockDim.x) bins[j] = 0;
   __syncthreads();
-  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
-    const int h = horizon[slot ? slot[i] : i];
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int h = hor(i);
     atomicAdd(&bins[(h >= 1 && h <= n_max) ? n_max - h : n_max], 1);
   }
   __syncthreads();
@@ -378,10 +388,10 @@ __global__ void __launch_bounds__(1024) order_by_horizon_kernel(int batch, int n
   for (int j = lo; j < hi; ++j) { const int c = bins[j]; bins[j] = run; run += c; }
   __syncthreads();
   if (n_long && threadIdx.x == 0)  // bins now hold start offsets; horizon h sits in bin n_max - h
-    *n_long = (split_h < 1) ? batch : (split_h > n_max ? 0 : bins[n_max - split_h + 1]);
+    *n_long = (split_h < 1) ? total : (split_h > n_max ? 0 : bins[n_max - split_h + 1]);
   __syncthreads();
-  for (int i = threadIdx.x; i < batch; i += blockDim.x) {
-    const int h = horizon[slot ? slot[i] : i];
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int h = hor(i);
     order[atomicAdd(&bins[(h >= 1 && h <= n_max) ? n_max - h : n_max], 1)] = i;
   }
 }

@@ -14,6 +14,7 @@ namespace mpxg {
 struct ModelConst;
 struct SqpParams;
 struct BatchPtrs;
+struct QueueArgs;
 
 // Launchers of one compiled model's kernels.
 struct SqpOps {
@@ -32,7 +33,21 @@ struct SqpOps {
   cudaError_t (*launch_evaluate)(const ModelConst& mc, int batch, int n_max, const int* horizon, const float* x0,
                                  const float* X, const float* U, const float* reference, const float* parameter,
                                  const float* w, float* g, float* c, cudaStream_t st);
+  // persistent kernel draining a device work queue (sqp_queue.cuh)
+  cudaError_t (*launch_queue)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, const QueueArgs& q,
+                              int blocks, int wpb, cudaStream_t st);
 };
+
+// Launchers of the mixed-model kernel of one model pair (sqp_mixed.cu).
+struct MixedArgs;
+struct MixedOps {
+  size_t smem_per_warp;                    // dynamic shared memory per warp (the larger model's)
+  long long (*scratch_floats)(int n_max);  // per-warp scratch (the larger model's)
+  int (*resident_blocks)(int wpb);
+  cudaError_t (*launch)(const MixedArgs& p, int blocks, int wpb, cudaStream_t st);
+};
+// The pair's table (null: the pair (model_a, model_b) is not built).
+const MixedOps* mixed_ops(int model_a, int model_b);
 
 const SqpOps& sqp_ops_quat13();
 const SqpOps& sqp_ops_rpy12();

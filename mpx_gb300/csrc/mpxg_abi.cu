@@ -13,11 +13,13 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/mpxg.h"
 #include "aux_kernels.cuh"
 #include "internal.h"
 #include "sqp_kernel.cuh"  // the structs the launchers take; the kernels are compiled in sqp_<model>.cu
+#include "sqp_queue.cuh"
 
 using namespace mpxg;
 
@@ -238,8 +240,8 @@ static mpxg_status check_io(mpxg_handle* h, const mpxg_batch_io* io) {
   if (!h) return fail(nullptr, MPXG_ERR_INVALID_ARG, "null handle");
   if (!io) return fail(h, MPXG_ERR_INVALID_ARG, "null io");
   if (io->batch < 0 || io->batch > h->desc.batch_max) return fail(h, MPXG_ERR_INVALID_ARG, "batch exceeds batch_max");
-  if (!io->x0 || !io->X_in || !io->U_in || !io->V_in || !io->reference || !io->parameter || !io->w || !io->X ||
-      !io->U || !io->V)
+  if (io->batch > 0 && (!io->x0 || !io->X_in || !io->U_in || !io->V_in || !io->reference || !io->parameter ||
+                        !io->w || !io->X || !io->U || !io->V))
     return fail(h, MPXG_ERR_INVALID_ARG, "required pointer is null");
   return MPXG_OK;
 }
@@ -336,6 +338,278 @@ mpxg_status mpxg_solve_plain(mpxg_handle* h, void* stream, const mpxg_batch_io* 
     s = dispatch(h, st, bp, 1, 1);
     if (s != MPXG_OK) return s;
   }
+  return MPXG_OK;
+}
+
+}  // extern "C"
+
+// A mixed-model launcher: the scratch, slot bitmap and work counters of the
+// pair's kernel (the handles keep their own for their single-model solves).
+struct mpxg_mixed {
+  mpxg_handle* h[2] = {nullptr, nullptr};
+  const MixedOps* ops = nullptr;
+  int num_sms = 0, wpb = 4, blocks_per_sm = 0, n_slots = 0;
+  long long scratch_stride = 0;
+  float* scratch = nullptr;
+  unsigned int* slot_bits = nullptr;
+  int* error = nullptr;
+  static constexpr int kRing = 64, kCounterStride = 32;
+  int* counters = nullptr;  // 2 kRing entries: eager solves, then captured ones
+  int* orders = nullptr;    // per entry: batch_max(a) + batch_max(b) queue codes
+  int order_stride = 0;
+  cudaEvent_t ring_ev[kRing] = {};
+  bool ring_used[kRing] = {};
+  int ring_next = 0, capture_next = 0;
+};
+
+extern "C" {
+
+void mpxg_mixed_destroy(mpxg_mixed* mx) {
+  if (!mx) return;
+  if (mx->scratch) cudaFree(mx->scratch);
+  if (mx->slot_bits) cudaFree(mx->slot_bits);
+  if (mx->counters) cudaFree(mx->counters);
+  if (mx->orders) cudaFree(mx->orders);
+  for (int i = 0; i < mpxg_mixed::kRing; ++i)
+    if (mx->ring_ev[i]) cudaEventDestroy(mx->ring_ev[i]);
+  delete mx;
+}
+
+mpxg_status mpxg_mixed_create(mpxg_handle* a, mpxg_handle* b, mpxg_mixed** out) {
+  if (!a || !b || !out) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_mixed_create: null argument");
+  *out = nullptr;
+  const MixedOps* ops = mixed_ops(a->desc.model, b->desc.model);
+  if (!ops)
+    return fail(nullptr, MPXG_ERR_UNSUPPORTED,
+                "mpxg_mixed_create: model pair not built (SRBD_RPY12 or SRBD_QUAT13 with BIPED_WRENCH12)");
+  if (a->desc.n_max != b->desc.n_max || a->device != b->device)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_mixed_create: the handles must share n_max and the device");
+  mpxg_mixed* mx = new mpxg_mixed();
+  mx->h[0] = a;
+  mx->h[1] = b;
+  mx->ops = ops;
+  mx->num_sms = a->num_sms;
+  mx->blocks_per_sm = ops->resident_blocks(mx->wpb);
+  mx->n_slots = mx->num_sms * mx->blocks_per_sm * mx->wpb;
+  mx->scratch_stride = ops->scratch_floats(a->desc.n_max);
+  mx->order_stride = a->desc.batch_max + b->desc.batch_max;
+  const size_t nwords = ((size_t)mx->n_slots + 31) / 32;
+  const size_t ctr_bytes = (size_t)2 * mpxg_mixed::kRing * mpxg_mixed::kCounterStride * sizeof(int);
+  const size_t order_bytes = (size_t)2 * mpxg_mixed::kRing * (size_t)mx->order_stride * sizeof(int);
+  if (cudaMalloc(&mx->scratch, (size_t)mx->scratch_stride * sizeof(float) * (size_t)mx->n_slots) != cudaSuccess ||
+      cudaMalloc(&mx->slot_bits, nwords * 4 + 256) != cudaSuccess ||
+      cudaMalloc(&mx->counters, ctr_bytes) != cudaSuccess || cudaMalloc(&mx->orders, order_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    mpxg_mixed_destroy(mx);
+    return fail(nullptr, MPXG_ERR_OUT_OF_MEMORY, "mpxg_mixed_create: scratch allocation failed");
+  }
+  mx->error = reinterpret_cast<int*>(mx->slot_bits + nwords);
+  for (int i = 0; i < mpxg_mixed::kRing; ++i)
+    if (cudaEventCreateWithFlags(&mx->ring_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      mpxg_mixed_destroy(mx);
+      return fail(nullptr, MPXG_ERR_CUDA, "mpxg_mixed_create: cudaEventCreate failed");
+    }
+  cudaError_t e = cudaMemset(mx->slot_bits, 0, nwords * 4 + 256);
+  if (e == cudaSuccess) e = cudaMemset(mx->counters, 0, ctr_bytes);
+  if (e != cudaSuccess) {
+    mpxg_mixed_destroy(mx);
+    return cuda_fail(nullptr, e, "mpxg_mixed_create: cudaMemset");
+  }
+  *out = mx;
+  return MPXG_OK;
+}
+
+mpxg_status mpxg_solve_mixed(mpxg_mixed* mx, void* stream, const mpxg_batch_io* io_a, const mpxg_batch_io* io_b) {
+  if (!mx) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_solve_mixed: null handle");
+  mpxg_handle* ha = mx->h[0];
+  mpxg_handle* hb = mx->h[1];
+  mpxg_status s = check_io(ha, io_a);
+  if (s != MPXG_OK) return fail(nullptr, s, std::string("mpxg_solve_mixed: first batch: ") + ha->err);
+  s = check_io(hb, io_b);
+  if (s != MPXG_OK) return fail(nullptr, s, std::string("mpxg_solve_mixed: second batch: ") + hb->err);
+  const int total = io_a->batch + io_b->batch;
+  if (total == 0) return MPXG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(nullptr, MPXG_ERR_CUDA, "mpxg_solve_mixed: cudaStreamIsCapturing failed");
+  }
+  const bool eager = cap == cudaStreamCaptureStatusNone;
+  int r;
+  if (eager) {
+    r = mx->ring_next;
+    mx->ring_next = (r + 1) % mpxg_mixed::kRing;
+    if (mx->ring_used[r]) {  // the solve that last used this entry has finished
+      cudaError_t e = cudaStreamWaitEvent(st, mx->ring_ev[r], 0);
+      if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaStreamWaitEvent");
+    }
+  } else {
+    r = mpxg_mixed::kRing + mx->capture_next;
+    mx->capture_next = (mx->capture_next + 1) % mpxg_mixed::kRing;
+  }
+  MixedArgs p;
+  p.mc[0] = ha->mc; p.mc[1] = hb->mc;
+  p.sp[0] = ha->sp; p.sp[1] = hb->sp;
+  p.bp[0] = make_ptrs(ha, io_a);
+  p.bp[1] = make_ptrs(hb, io_b);
+  p.total = total;
+  p.counter = mx->counters + (size_t)r * mpxg_mixed::kCounterStride;
+  p.scratch = mx->scratch;
+  p.scratch_stride = mx->scratch_stride;
+  p.slot_bits = mx->slot_bits;
+  p.n_slots = mx->n_slots;
+  p.error = mx->error;
+  p.order = nullptr;
+  cudaError_t e = cudaMemsetAsync(p.counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemsetAsync");
+  if ((io_a->batch == 0 || io_a->horizon) && (io_b->batch == 0 || io_b->horizon)) {  // longest first, both batches
+    int* order = mx->orders + (size_t)r * mx->order_stride;
+    const int n_max = ha->desc.n_max;
+    order_by_horizon_kernel<<<1, 1024, (size_t)(n_max + 1) * sizeof(int), st>>>(
+        io_a->batch, n_max, io_a->slot, io_a->horizon, order, 0, nullptr, io_b->batch, io_b->slot, io_b->horizon);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "order_by_horizon_kernel launch");
+    p.order = order;
+  }
+  int blocks = mx->num_sms * mx->blocks_per_sm;
+  const int need = (total + mx->wpb - 1) / mx->wpb;
+  if (need < blocks) blocks = need;
+  e = mx->ops->launch(p, blocks, mx->wpb, st);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "sqp_mixed_kernel launch");
+  if (!eager) return MPXG_OK;
+  e = cudaEventRecord(mx->ring_ev[r], st);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaEventRecord");
+  mx->ring_used[r] = true;
+  return MPXG_OK;
+}
+
+}  // extern "C"
+
+// A running device work queue: the ring, flags and result rows live in one
+// block of mapped pinned host memory (the kernel reads and writes them in
+// place); the claim counter lives on the device.
+struct mpxg_queue {
+  mpxg_handle* h = nullptr;
+  cudaStream_t stream = nullptr;
+  int capacity = 0, rows = 0, row_len = 0;
+  int* host = nullptr;        // [entries cap | done cap | tail | stop | status | pad] then result rows
+  int* dev = nullptr;         // the same block seen from the device
+  int* head = nullptr;        // device claim counter
+  long long next_ticket = 0;
+  std::vector<int> ring_row;  // pool row of the ticket at each ring entry
+  int* entries() { return host; }
+  int* done() { return host + capacity; }
+  int* tail() { return host + 2 * capacity; }
+  int* stop() { return host + 2 * capacity + 1; }
+  int* status() { return host + 2 * capacity + 2; }
+  size_t rows_offset() const { return ((size_t)2 * capacity + 4 + 3) / 4 * 4; }  // ints, 16-byte aligned
+  float* result_rows() { return reinterpret_cast<float*>(host + rows_offset()); }
+};
+
+static void queue_free(mpxg_queue* q) {
+  if (q->host) cudaFreeHost(q->host);
+  if (q->head) cudaFree(q->head);
+  delete q;
+}
+
+extern "C" {
+
+mpxg_status mpxg_queue_start(mpxg_handle* h, void* stream, const mpxg_batch_io* pool, int capacity,
+                             long long idle_timeout_ns, mpxg_queue** out) {
+  if (!h || !pool || !out) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_queue_start: null argument");
+  *out = nullptr;
+  mpxg_status s = check_io(h, pool);
+  if (s != MPXG_OK) return s;
+  if (pool->batch < 1 || pool->slot || capacity < 1 || capacity > (1 << 20) || idle_timeout_ns < 1000000LL ||
+      idle_timeout_ns > 60000000000LL)
+    return fail(h, MPXG_ERR_INVALID_ARG,
+                "mpxg_queue_start: pool of >= 1 rows without a slot map, capacity 1..2^20, idle timeout 1 ms..60 s");
+  mpxg_queue* q = new mpxg_queue();
+  q->h = h;
+  q->stream = (cudaStream_t)stream;
+  q->capacity = capacity;
+  q->rows = pool->batch;
+  q->row_len = h->desc.m + 4;
+  q->ring_row.assign(capacity, -1);
+  const size_t bytes = q->rows_offset() * sizeof(int) + (size_t)q->rows * q->row_len * sizeof(float);
+  if (cudaHostAlloc(reinterpret_cast<void**>(&q->host), bytes, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer(reinterpret_cast<void**>(&q->dev), q->host, 0) != cudaSuccess ||
+      cudaMalloc(&q->head, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    queue_free(q);
+    return fail(h, MPXG_ERR_OUT_OF_MEMORY, "mpxg_queue_start: mapped host allocation failed");
+  }
+  std::memset(q->host, 0, bytes);
+  cudaError_t e = cudaMemsetAsync(q->head, 0, sizeof(int), q->stream);
+  if (e != cudaSuccess) {
+    queue_free(q);
+    return cuda_fail(h, e, "mpxg_queue_start: cudaMemsetAsync");
+  }
+  BatchPtrs bp = make_ptrs(h, pool);
+  bp.slot = nullptr;
+  bp.first = reinterpret_cast<float*>(q->dev + q->rows_offset());
+  QueueArgs qa;
+  qa.entries = q->dev;
+  qa.done = q->dev + capacity;
+  qa.tail = q->dev + 2 * capacity;
+  qa.stop = q->dev + 2 * capacity + 1;
+  qa.status = q->dev + 2 * capacity + 2;
+  qa.head = q->head;
+  qa.capacity = capacity;
+  qa.timeout_ns = idle_timeout_ns;
+  const int wpb = h->warps_per_block;
+  const int blocks = h->num_sms * h->blocks_per_sm_lat;
+  e = sqp_ops(h->desc.model)->launch_queue(h->mc, h->sp, bp, qa, blocks, wpb, q->stream);
+  if (e != cudaSuccess) {
+    queue_free(q);
+    return cuda_fail(h, e, "sqp_queue_kernel launch");
+  }
+  *out = q;
+  return MPXG_OK;
+}
+
+mpxg_status mpxg_queue_push(mpxg_queue* q, int row, long long* ticket) {
+  if (!q || !ticket) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_queue_push: null argument");
+  if (row < 0 || row >= q->rows) return fail(q->h, MPXG_ERR_INVALID_ARG, "mpxg_queue_push: row outside the pool");
+  if (__atomic_load_n(q->status(), __ATOMIC_ACQUIRE) & QUEUE_TIMEOUT)
+    return fail(q->h, MPXG_ERR_TIMEOUT, "mpxg_queue_push: the queue kernel timed out waiting and has stopped");
+  const long long t = q->next_ticket;
+  if (t >= 0x7ffffffe) return fail(q->h, MPXG_ERR_INVALID_ARG, "mpxg_queue_push: ticket space exhausted");
+  const int k = (int)(t % q->capacity);
+  if (t >= q->capacity && __atomic_load_n(q->done() + k, __ATOMIC_ACQUIRE) != (int)(t - q->capacity) + 1)
+    return MPXG_ERR_NOT_READY;  // the ring entry's previous ticket has not finished yet
+  q->entries()[k] = row;
+  q->ring_row[k] = row;
+  __atomic_store_n(q->tail(), (int)(t + 1), __ATOMIC_RELEASE);
+  q->next_ticket = t + 1;
+  *ticket = t;
+  return MPXG_OK;
+}
+
+mpxg_status mpxg_queue_result(mpxg_queue* q, long long ticket, float* row_out) {
+  if (!q || !row_out) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_queue_result: null argument");
+  if (ticket < 0 || ticket >= q->next_ticket || ticket < q->next_ticket - q->capacity)
+    return fail(q->h, MPXG_ERR_INVALID_ARG, "mpxg_queue_result: ticket not pushed or its ring entry reused");
+  const int k = (int)(ticket % q->capacity);
+  if (__atomic_load_n(q->done() + k, __ATOMIC_ACQUIRE) != (int)ticket + 1)
+    return (__atomic_load_n(q->status(), __ATOMIC_ACQUIRE) & QUEUE_TIMEOUT) ? MPXG_ERR_TIMEOUT : MPXG_ERR_NOT_READY;
+  const float* src = q->result_rows() + (size_t)q->ring_row[k] * q->row_len;
+  for (int i = 0; i < q->row_len; ++i) row_out[i] = src[i];
+  return MPXG_OK;
+}
+
+mpxg_status mpxg_queue_finish(mpxg_queue* q) {
+  if (!q) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_queue_finish: null queue");
+  __atomic_store_n(q->stop(), 1, __ATOMIC_RELEASE);
+  const cudaError_t e = cudaStreamSynchronize(q->stream);  // bounded: every wait of the kernel is
+  const int st = __atomic_load_n(q->status(), __ATOMIC_ACQUIRE);
+  mpxg_handle* h = q->h;
+  queue_free(q);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mpxg_queue_finish: cudaStreamSynchronize");
+  if (st & QUEUE_TIMEOUT) return fail(h, MPXG_ERR_TIMEOUT, "mpxg_queue_finish: a warp's wait for work timed out");
+  if (st & QUEUE_NO_SLOT) return fail(h, MPXG_ERR_CUDA, "mpxg_queue_finish: a warp found no scratch slot");
   return MPXG_OK;
 }
 

@@ -50,10 +50,16 @@ struct Ticket {
   mpxg_result res;
 };
 
-struct Batch {
-  int model = 0, stream = 0;
+// A launched batch: one model's tickets, or (mixed launch) two models' parts.
+struct Part {
+  int model = 0;
   Staging* st = nullptr;
   std::vector<long long> tickets;
+};
+struct Batch {
+  int stream = 0;
+  std::vector<Part> parts;
+  cudaEvent_t ev() const { return parts.front().st->ev; }
 };
 
 inline bool model_layout(int model, int* n, int* m, int* legs, int* rc, int* pc) {
@@ -85,6 +91,8 @@ struct mpxg_server {
   std::unordered_map<long long, mpxg_srv::Ticket> tickets;
   long long next_ticket = 1;
   std::vector<mpxg_srv::Batch> inflight;
+  mpxg_mixed* mixed = nullptr;  // mixed-model launches (mixed_launch): pools mix[0], mix[1]
+  int mix[2] = {0, 1};
   std::deque<long long> done;
   unsigned int seed = 0;
   long long launches = 0;
@@ -164,15 +172,19 @@ inline void fill_gait(const Pool& p, int n_max, mpxg_gait_args* a) {
   a->v_ref = p.vref; a->leg_time = p.lt; a->reference = p.ref; a->parameter = p.par;
 }
 
-// Launch one batch of `ticks` (all of model `mi`, episodes distinct and idle).
-inline mpxg_status launch(mpxg_server* s, int mi, std::vector<long long>& ticks) {
-  Pool& p = s->pools[mi];
+// Stage one model's part of a batch on `stream`: order the tickets longest
+// horizon first, upload their slots, shift the warm starts and rebuild the
+// gait tables.  Fills the solve io of the part.
+inline mpxg_status prepare_part(mpxg_server* s, Part& part, cudaStream_t stream, mpxg_batch_io* io) {
+  Pool& p = s->pools[part.model];
+  std::vector<long long>& ticks = part.tickets;
   std::sort(ticks.begin(), ticks.end(), [&](long long a, long long b) {
     return s->eps[s->tickets[a].episode].horizon > s->eps[s->tickets[b].episode].horizon;
   });
   const int nb = (int)ticks.size();
   Staging* st = get_staging(s, p);
   if (!st) return MPXG_ERR_OUT_OF_MEMORY;
+  part.st = st;
   int nw = 0, nc = 0;
   for (int i = 0; i < nb; ++i) {
     const Episode& e = s->eps[s->tickets[ticks[i]].episode];
@@ -187,10 +199,6 @@ inline mpxg_status launch(mpxg_server* s, int mi, std::vector<long long>& ticks)
     e.cold = false;
     e.running = true;
   }
-  int si = 0;  // an idle stream (the caller checked that one exists)
-  while (si < (int)s->streams.size() && s->stream_busy[si]) ++si;
-  if (si == (int)s->streams.size()) return fail(s, MPXG_ERR_INVALID_ARG, "server: no idle stream");
-  cudaStream_t stream = s->streams[si];
   cudaError_t ce = cudaMemcpyAsync(st->slot_d, st->slot_h, (size_t)(nb + nw + nc) * sizeof(int),
                                    cudaMemcpyHostToDevice, stream);
   if (ce != cudaSuccess) return cuda_err(s, ce, "server: slot copy");
@@ -212,27 +220,55 @@ inline mpxg_status launch(mpxg_server* s, int mi, std::vector<long long>& ticks)
     r = mpxg_gait_tables(stream, &a);
     if (r != MPXG_OK) return fail(s, r, std::string("server: gait tables: ") + mpxg_last_error(nullptr));
   }
-  mpxg_batch_io io;
-  std::memset(&io, 0, sizeof(io));
-  io.batch = nb; io.slot = st->slot_d; io.horizon = p.horizon;
-  io.x0 = p.x0; io.X_in = p.X; io.U_in = p.U; io.V_in = p.V;
-  io.reference = p.ref; io.parameter = p.par; io.w = p.w;
-  io.X = p.X; io.U = p.U; io.V = p.V; io.kkt = p.kkt; io.status = p.status; io.first = st->res_d;
-  r = mpxg_solve(p.h, stream, &io);
-  if (r != MPXG_OK) return fail(s, r, std::string("server: solve: ") + mpxg_last_error(p.h));
-  ce = cudaMemcpyAsync(st->res_h, st->res_d, (size_t)nb * (p.mu + 4) * sizeof(float), cudaMemcpyDeviceToHost,
-                       stream);
-  if (ce == cudaSuccess) ce = cudaEventRecord(st->ev, stream);
+  std::memset(io, 0, sizeof(*io));
+  io->batch = nb; io->slot = st->slot_d; io->horizon = p.horizon;
+  io->x0 = p.x0; io->X_in = p.X; io->U_in = p.U; io->V_in = p.V;
+  io->reference = p.ref; io->parameter = p.par; io->w = p.w;
+  io->X = p.X; io->U = p.U; io->V = p.V; io->kkt = p.kkt; io->status = p.status; io->first = st->res_d;
+  s->launches += (nw ? 2 : 0) + (nc ? 1 : 0);
+  return MPXG_OK;
+}
+
+// Launch one batch: the parts' tickets (per part one model, episodes
+// distinct and idle); one part goes through mpxg_solve of its pool's handle,
+// two parts through one mixed-model solve.
+inline mpxg_status launch(mpxg_server* s, std::vector<Part> parts) {
+  int si = 0;  // an idle stream (the caller checked that one exists)
+  while (si < (int)s->streams.size() && s->stream_busy[si]) ++si;
+  if (si == (int)s->streams.size()) return fail(s, MPXG_ERR_INVALID_ARG, "server: no idle stream");
+  cudaStream_t stream = s->streams[si];
+  mpxg_batch_io io[2];
+  int nt = 0;
+  for (size_t k = 0; k < parts.size(); ++k) {
+    mpxg_status r = prepare_part(s, parts[k], stream, &io[k]);
+    if (r != MPXG_OK) return r;
+    nt += io[k].batch;
+  }
+  mpxg_status r;
+  if (parts.size() == 2) {
+    r = mpxg_solve_mixed(s->mixed, stream, &io[0], &io[1]);
+    if (r != MPXG_OK) return fail(s, r, std::string("server: mixed solve: ") + mpxg_last_error(nullptr));
+    s->launches += 2;  // order + solve
+  } else {
+    Pool& p = s->pools[parts[0].model];
+    r = mpxg_solve(p.h, stream, &io[0]);
+    if (r != MPXG_OK) return fail(s, r, std::string("server: solve: ") + mpxg_last_error(p.h));
+    s->launches += io[0].batch > p.total_warps ? 2 : 1;
+  }
+  for (size_t k = 0; k < parts.size(); ++k) {
+    const Pool& p = s->pools[parts[k].model];
+    cudaError_t ce = cudaMemcpyAsync(parts[k].st->res_h, parts[k].st->res_d, (size_t)io[k].batch * (p.mu + 4) * sizeof(float),
+                                     cudaMemcpyDeviceToHost, stream);
+    if (ce != cudaSuccess) return cuda_err(s, ce, "server: result copy");
+  }
+  cudaError_t ce = cudaEventRecord(parts[0].st->ev, stream);
   if (ce != cudaSuccess) return cuda_err(s, ce, "server: result copy");
-  s->launches += (nw ? 2 : 0) + (nc ? 1 : 0) + (nb > p.total_warps ? 2 : 1);
   Batch b;
-  b.model = mi;
   b.stream = si;
   s->stream_busy[si] = 1;
-  b.st = st;
-  b.tickets = ticks;
+  b.parts = std::move(parts);
   s->inflight.push_back(std::move(b));
-  s->queued -= nb;
+  s->queued -= nt;
   return MPXG_OK;
 }
 
@@ -248,17 +284,18 @@ inline void reap(mpxg_server* s, size_t i) {
   Batch b = std::move(s->inflight[i]);
   s->inflight.erase(s->inflight.begin() + i);
   s->stream_busy[b.stream] = 0;
-  Pool& p = s->pools[b.model];
-  for (size_t i = 0; i < b.tickets.size(); ++i) {
-    Ticket& t = s->tickets[b.tickets[i]];
-    const float* row = b.st->res_h + i * (p.mu + 4);
-    t.res.ticket = b.tickets[i];
+  for (Part& part : b.parts) {
+  Pool& p = s->pools[part.model];
+  for (size_t i = 0; i < part.tickets.size(); ++i) {
+    Ticket& t = s->tickets[part.tickets[i]];
+    const float* row = part.st->res_h + i * (p.mu + 4);
+    t.res.ticket = part.tickets[i];
     t.res.episode = t.episode;
     for (int a = 0; a < 12; ++a) t.res.u0[a] = a < p.mu ? row[a] : 0.0f;
     for (int k = 0; k < 3; ++k) t.res.kkt[k] = row[p.mu + k];
     t.res.status = (int)row[p.mu + 3];
     t.done = true;
-    s->done.push_back(b.tickets[i]);
+    s->done.push_back(part.tickets[i]);
     auto it = s->eps.find(t.episode);
     if (it != s->eps.end()) {
       Episode& e = it->second;
@@ -267,7 +304,8 @@ inline void reap(mpxg_server* s, size_t i) {
       if (--e.busy == 0 && e.retiring) retire(s, t.episode);
     }
   }
-  p.idle.push_back(b.st);
+  p.idle.push_back(part.st);
+  }
 }
 
 }  // namespace mpxg_srv
@@ -282,7 +320,30 @@ mpxg_status mpxg_server_create(const mpxg_server_desc* d, mpxg_server** out) {
   mpxg_server* s = new mpxg_server();
   s->d = *d;
   s->seed = d->seed;
-  const size_t share = d->budget_bytes / (size_t)d->n_models;
+  size_t budget = d->budget_bytes;
+  const MixedOps* mops = nullptr;
+  if (d->mixed_launch) {  // one mixed-model solve per step: a built pair of two models, its scratch off the budget
+    if (d->n_models == 2) {
+      const int m0 = d->models[0].desc.model, m1 = d->models[1].desc.model;
+      if ((mops = mixed_ops(m0, m1))) { s->mix[0] = 0; s->mix[1] = 1; }
+      else if ((mops = mixed_ops(m1, m0))) { s->mix[0] = 1; s->mix[1] = 0; }
+    }
+    if (!mops) {
+      mpxg_server_destroy(s);
+      return fail_lib(MPXG_ERR_UNSUPPORTED, "mpxg_server_create: mixed_launch needs two models of a built pair");
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t mixed = (size_t)mops->scratch_floats(d->n_max) * sizeof(float) *
+                         ((size_t)sms * mops->resident_blocks(4) * 4);
+    if (mixed >= budget) {
+      mpxg_server_destroy(s);
+      return fail_lib(MPXG_ERR_BUDGET, "mpxg_server_create: the budget does not hold the mixed-model scratch");
+    }
+    budget -= mixed;
+  }
+  const size_t share = budget / (size_t)d->n_models;
   s->pools.resize(d->n_models);
   for (int i = 0; i < d->n_models; ++i) {
     Pool& p = s->pools[i];
@@ -331,6 +392,11 @@ mpxg_status mpxg_server_create(const mpxg_server_desc* d, mpxg_server** out) {
     p.free_slots.reserve(p.cap);
     for (int k = p.cap - 1; k >= 0; --k) p.free_slots.push_back(k);
   }
+  if (mops && mpxg_mixed_create(s->pools[s->mix[0]].h, s->pools[s->mix[1]].h, &s->mixed) != MPXG_OK) {
+    std::string m = mpxg_last_error(nullptr);
+    mpxg_server_destroy(s);
+    return fail_lib(MPXG_ERR_OUT_OF_MEMORY, "mpxg_server_create: " + m);
+  }
   for (int k = 0; k < d->streams; ++k) {
     cudaStream_t st;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
@@ -348,8 +414,10 @@ mpxg_status mpxg_server_create(const mpxg_server_desc* d, mpxg_server** out) {
 void mpxg_server_destroy(mpxg_server* s) {
   if (!s) return;
   for (cudaStream_t st : s->streams) cudaStreamSynchronize(st);
-  for (auto& b : s->inflight) s->pools[b.model].idle.push_back(b.st);
+  for (auto& b : s->inflight)
+    for (auto& part : b.parts) s->pools[part.model].idle.push_back(part.st);
   s->inflight.clear();
+  if (s->mixed) mpxg_mixed_destroy(s->mixed);
   for (auto& p : s->pools) mpxg_srv::free_pool(p);
   for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
   delete s;
@@ -450,19 +518,19 @@ mpxg_status mpxg_server_step(mpxg_server* s, int block, int* launched, int* fini
   if (!s) return MPXG_ERR_INVALID_ARG;
   int nfin = 0, nlaunch = 0;
   if (block && !s->inflight.empty()) {  // wait for the oldest running batch
-    cudaError_t e = cudaEventSynchronize(s->inflight.front().st->ev);
+    cudaError_t e = cudaEventSynchronize(s->inflight.front().ev());
     if (e != cudaSuccess) return cuda_err(s, e, "mpxg_server_step");
   }
   for (size_t i = 0; i < s->inflight.size();) {  // collect every finished batch, in any order
-    cudaError_t e = cudaEventQuery(s->inflight[i].st->ev);
+    cudaError_t e = cudaEventQuery(s->inflight[i].ev());
     if (e == cudaErrorNotReady) { ++i; continue; }
     if (e != cudaSuccess) return cuda_err(s, e, "mpxg_server_step");
-    nfin += (int)s->inflight[i].tickets.size();
+    for (const auto& part : s->inflight[i].parts) nfin += (int)part.tickets.size();
     reap(s, i);
   }
-  for (size_t mi = 0; mi < s->pools.size() && (int)s->inflight.size() < (int)s->streams.size(); ++mi) {
+  // the idle episodes' pending tickets of pool mi (claimed for a batch)
+  auto take = [&](int mi) {
     Pool& p = s->pools[mi];
-    if (p.pending.empty()) continue;
     std::vector<long long> batch, later;
     batch.reserve(p.pending.size());
     for (long long tk : p.pending) {
@@ -472,12 +540,34 @@ mpxg_status mpxg_server_step(mpxg_server* s, int block, int* launched, int* fini
       batch.push_back(tk);
     }
     p.pending.swap(later);
-    if (batch.empty()) continue;
     for (long long tk : batch) s->eps[s->tickets[tk].episode].running = false;
-    const int n = (int)batch.size();
-    mpxg_status r = launch(s, (int)mi, batch);
-    if (r != MPXG_OK) return r;
-    nlaunch += n;
+    return batch;
+  };
+  if (s->mixed) {  // both models' ticks in one mixed-model solve
+    if ((int)s->inflight.size() < (int)s->streams.size()) {
+      std::vector<Part> parts(2);
+      for (int k = 0; k < 2; ++k) {
+        parts[k].model = s->mix[k];
+        parts[k].tickets = take(s->mix[k]);
+      }
+      const int n = (int)(parts[0].tickets.size() + parts[1].tickets.size());
+      if (n > 0) {
+        mpxg_status r = launch(s, std::move(parts));
+        if (r != MPXG_OK) return r;
+        nlaunch += n;
+      }
+    }
+  } else {
+    for (size_t mi = 0; mi < s->pools.size() && (int)s->inflight.size() < (int)s->streams.size(); ++mi) {
+      std::vector<Part> parts(1);
+      parts[0].model = (int)mi;
+      parts[0].tickets = take((int)mi);
+      const int n = (int)parts[0].tickets.size();
+      if (n == 0) continue;
+      mpxg_status r = launch(s, std::move(parts));
+      if (r != MPXG_OK) return r;
+      nlaunch += n;
+    }
   }
   if (launched) *launched = nlaunch;
   if (finished) *finished = nfin;
@@ -512,7 +602,8 @@ mpxg_status mpxg_server_completed(mpxg_server* s, mpxg_result* results, int max,
 mpxg_status mpxg_server_stats(const mpxg_server* s, int* queued, int* running, long long* launches) {
   if (!s) return MPXG_ERR_INVALID_ARG;
   int run = 0;
-  for (const auto& b : s->inflight) run += (int)b.tickets.size();
+  for (const auto& b : s->inflight)
+    for (const auto& part : b.parts) run += (int)part.tickets.size();
   if (queued) *queued = s->queued;
   if (running) *running = run;
   if (launches) *launches = s->launches;

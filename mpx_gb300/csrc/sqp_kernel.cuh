@@ -90,6 +90,24 @@ __device__ inline int claim_scratch_slot(unsigned int* bits, int n_slots, int pr
   return -1;
 }
 
+// Arguments of the mixed-model launch (sqp_mixed.cuh): two models' batches
+// served from one queue.  Queue entry i is code order[i] (identity if null):
+// codes below bp[0].batch are model 0's batch entries, the others model 1's
+// entry code - bp[0].batch.
+struct MixedArgs {
+  ModelConst mc[2];
+  SqpParams sp[2];
+  BatchPtrs bp[2];
+  const int* order;
+  int total;
+  int* counter;
+  float* scratch;
+  long long scratch_stride;
+  unsigned int* slot_bits;
+  int n_slots;
+  int* error;
+};
+
 constexpr int rup4(int v) { return (v + 3) / 4 * 4; }
 
 // n floats from a 16-byte aligned address into registers (float4 where possible)

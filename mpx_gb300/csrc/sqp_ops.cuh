@@ -5,6 +5,7 @@
 #include "evaluate_kernel.cuh"
 #include "internal.h"
 #include "sqp_kernel.cuh"
+#include "sqp_queue.cuh"
 #include "sqp_team.cuh"
 
 namespace mpxg {
@@ -84,9 +85,20 @@ struct SqpLaunch {
                                                    c);
     return cudaGetLastError();
   }
+  static cudaError_t launch_queue(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, const QueueArgs& q,
+                                  int blocks, int wpb, cudaStream_t st) {
+    const size_t smem = sizeof(WarpSmem<M>) * (size_t)wpb;
+    auto fn = sqp_queue_kernel<M>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    fn<<<blocks, wpb * 32, smem, st>>>(mc, sp, bp, q);
+    return cudaGetLastError();
+  }
   static const SqpOps& ops() {
     static const SqpOps o = {sizeof(WarpSmem<M>), &scratch, &resident_blocks, &launch, &launch_vjp,
-                             &team_resident_blocks, &launch_team, &launch_evaluate};
+                             &team_resident_blocks, &launch_team, &launch_evaluate, &launch_queue};
     return o;
   }
 };

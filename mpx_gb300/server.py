@@ -48,10 +48,13 @@ class MPCServer:
     offsets (legs x 3), W (24 x 24 diagonal), phase0 (legs,)).  The budget is
     split evenly between the models; each model's pool holds as many slots as
     fit after its solver scratch.  `completed` keeps the last `keep_completed`
-    results that poll() returned, oldest first."""
+    results that poll() returned, oldest first.  mixed_launch=True (two
+    models of a built pair, e.g. the rpy12 quadruped and the biped): every
+    step solves both models' ticks in one mixed-model launch
+    (mpxg_solve_mixed), whose scratch is taken off the budget first."""
 
     def __init__(self, models, n_max=200, budget_bytes=8 << 30, opts=None, streams=32, device=None, drift_std=0.01,
-                 seed=0, max_slots=None, keep_completed=1 << 16):
+                 seed=0, max_slots=None, keep_completed=1 << 16, mixed_launch=False):
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.opts = opts or P.SolverOptions()
         self.n_max = int(n_max)
@@ -80,6 +83,7 @@ class MPCServer:
         d.n_models, d.models, d.n_max = len(names), arr, self.n_max
         d.budget_bytes, d.max_slots, d.streams = int(budget_bytes), int(max_slots or 0), int(streams)
         d.drift_std, d.seed, d.opts = float(drift_std), int(seed) & 0xFFFFFFFF, solver_opts(self.opts)
+        d.mixed_launch = int(bool(mixed_launch))
         self._models = arr
         h = ctypes.c_void_p()
         with torch.cuda.device(self.dev):

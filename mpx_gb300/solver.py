@@ -274,6 +274,108 @@ class Solver:
         return Xo, Uo, Vo
 
 
+class MixedSolver:
+    """One persistent launch over the batches of two solvers of different
+    models (mpxg_solve_mixed): e.g. quadrupeds on `a` and bipeds on `b`.
+    Each instance gives the bits its own solver's one-warp solve gives."""
+
+    def __init__(self, a: Solver, b: Solver):
+        self.a, self.b, self.L = a, b, _lib.load()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(a.device):
+            st = self.L.mpxg_mixed_create(a.handle, b.handle, ctypes.byref(h))
+        _lib.check(st, None, "mpxg_mixed_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.L.mpxg_mixed_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, batch_a, batch_b, stream=None, want_gains=False):
+        """batch_a / batch_b: tuples (x0, X0, U0, V0, reference, parameter, W,
+        horizon) for solver a / b.  Returns (out_a, out_b) as Solver.solve."""
+        outs, ios, keep = [], [], []
+        for s, args in ((self.a, batch_a), (self.b, batch_b)):
+            p = s.prepare(*args)
+            out = s.empty_outputs(p[0].shape[0], want_gains)
+            ios.append(s.io(*p, out))
+            outs.append(out)
+            keep.append(p)
+        with torch.cuda.device(self.a.device):
+            st = self.L.mpxg_solve_mixed(self.handle, _stream_handle(stream), ctypes.byref(ios[0]), ctypes.byref(ios[1]))
+        _lib.check(st, None, "mpxg_solve_mixed")
+        for out, p in zip(outs, keep):
+            out["_keep"] = p
+        return outs[0], outs[1]
+
+
+MPXG_ERR_TIMEOUT, MPXG_ERR_NOT_READY = 5, 7
+
+
+class SolveQueue:
+    """Device work queue (mpxg_queue_*): one persistent kernel on `stream`
+    solves the rows of `pool` (x0, X0, U0, V0, reference, parameter, W,
+    horizon -- as Solver.solve takes them) as the host pushes them, while it
+    runs.  `inputs` holds the device copies of the pool (update a row there
+    before pushing it again), `out` the X, U, V, kkt, status outputs.  Every
+    wait of the kernel is bounded by `idle_timeout_s`: a warp that waits
+    longer for work stops, and push / result / finish then raise with
+    "timeout" instead of blocking."""
+
+    def __init__(self, solver: Solver, pool, capacity=1024, idle_timeout_s=1.0, stream=None):
+        x0, X0, U0, V0, reference, parameter, w, horizon = solver.prepare(*pool)
+        self.inputs = dict(x0=x0, X=X0, U=U0, V=V0, reference=reference, parameter=parameter, w=w, horizon=horizon)
+        self.out = solver.empty_outputs(x0.shape[0])
+        self._io = solver.io(x0, X0, U0, V0, reference, parameter, w, horizon, self.out)
+        self.solver, self.L, self.m = solver, solver.L, solver.desc.m
+        h = ctypes.c_void_p()
+        with torch.cuda.device(solver.device):
+            st = self.L.mpxg_queue_start(solver.handle, _stream_handle(stream), ctypes.byref(self._io), int(capacity),
+                                         int(idle_timeout_s * 1e9), ctypes.byref(h))
+        _lib.check(st, solver.handle, "mpxg_queue_start")
+        self.handle = h
+
+    def push(self, row):
+        """Publish pool row `row`; returns its ticket, or None while the ring
+        entry it needs still holds an unfinished ticket."""
+        t = ctypes.c_longlong()
+        st = self.L.mpxg_queue_push(self.handle, int(row), ctypes.byref(t))
+        if st == MPXG_ERR_NOT_READY:
+            return None
+        _lib.check(st, self.solver.handle, "mpxg_queue_push")
+        return t.value
+
+    def result(self, ticket):
+        """The ticket's result row [m controls, KKT triple, status] once
+        solved, else None."""
+        row = (ctypes.c_float * (self.m + 4))()
+        st = self.L.mpxg_queue_result(self.handle, int(ticket), row)
+        if st == MPXG_ERR_NOT_READY:
+            return None
+        _lib.check(st, self.solver.handle, "mpxg_queue_result")
+        return np.frombuffer(row, dtype=np.float32).copy()
+
+    def finish(self):
+        """Let the kernel drain what was pushed, wait for it and free the queue."""
+        if self.handle is None:
+            return
+        h, self.handle = self.handle, None
+        _lib.check(self.L.mpxg_queue_finish(h), self.solver.handle, "mpxg_queue_finish")
+
+    def __del__(self):
+        try:
+            self.finish()
+        except Exception:
+            pass
+
+
 def lqr_solve(A, B, c, Q, R, M, q, r, x0, method=0, stream=None):
     """Batched time-varying LQR (absolute coordinates) on the device.
     Shapes as in include/mpxg.h mpxg_lqr_solve.  Returns dict K, k, X, U, lam."""

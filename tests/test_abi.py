@@ -238,3 +238,20 @@ def test_missing_library_raises(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib._build, "LIB", str(tmp_path / "libmpxg.so"))
     with pytest.raises(_lib.MpxgError, match="not built"):
         _lib.load(build_if_missing=False)
+
+
+def test_queue_and_mixed_reject_null_arguments():
+    """The device work queue and the mixed-model launch refuse null handles
+    and arguments before touching a device."""
+    from mpx_gb300 import _lib
+    L = _lib.load()
+    q = ctypes.c_void_p()
+    assert L.mpxg_queue_start(None, None, None, 4, 10 ** 9, ctypes.byref(q)) == 1
+    t = ctypes.c_longlong()
+    assert L.mpxg_queue_push(None, 0, ctypes.byref(t)) == 1
+    assert L.mpxg_queue_result(None, 0, None) == 1
+    assert L.mpxg_queue_finish(None) == 1
+    mx = ctypes.c_void_p()
+    assert L.mpxg_mixed_create(None, None, ctypes.byref(mx)) == 1
+    assert L.mpxg_solve_mixed(None, None, None, None) == 1
+    L.mpxg_mixed_destroy(None)

@@ -52,7 +52,10 @@ def test_cache_key_separates_workloads(tmp_path, monkeypatch):
     for wl in (_workload(batch=64), _workload(batch=128), _workload(n_max=100), _workload(model=2)):
         assert not autotune.tune(wl, opts, candidates=[(1, 0), (2, 0)], reps=1)["cached"]
     assert not autotune.tune(_workload(), types.SimpleNamespace(sqp_iters=3), candidates=[(1, 0)], reps=1)["cached"]
-    assert len(json.load(open(tmp_path / "tune.json"))) == 5
+    # a warm-tick state is tuned and cached apart from the cold start of the same shape
+    assert not autotune.tune(_workload(), opts, candidates=[(1, 0)], reps=1, tag="warm")["cached"]
+    assert autotune.tune(_workload(), opts, candidates=[(1, 0)], reps=1, tag="warm")["cached"]
+    assert len(json.load(open(tmp_path / "tune.json"))) == 6
 
 
 def test_no_candidate_runs(tmp_path, monkeypatch):
