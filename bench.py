@@ -355,6 +355,46 @@ def _served_entry(srv, lat, wall, offered):
             "nan_status": int(((srv.last_status & 1) != 0).sum())}
 
 
+def queue_latency(dev, opts, N=50, pool=64, reps=200):
+    """Round trip of one request through the device work queue (a persistent
+    kernel already running; push -> result row on the host, no launch per
+    request), and the time to drain `pool` requests pushed at once."""
+    import time
+    from mpx_gb300 import problem as P
+    from mpx_gb300.solver import SolveQueue, Solver
+    wl = P.quadruped_workload(pool, horizons=(N,), seed=3, model=P.MODEL_SRBD_RPY12, v_range=(-1, 1),
+                              random_phase=True)
+    s = Solver(wl.desc, opts, n_max=N, batch_max=pool, device=dev)
+    q = SolveQueue(s, (wl.x0, wl.X0, wl.U0, wl.V0, wl.reference, wl.parameter, wl.W, wl.horizon), capacity=4096,
+                   idle_timeout_s=10.0)
+
+    def wait(t):
+        while True:
+            r = q.result(t)
+            if r is not None:
+                return r
+
+    lat = []
+    for k in range(reps + 10):
+        t0 = time.perf_counter()
+        wait(q.push(k % pool))
+        if k >= 10:
+            lat.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    ts = [q.push(r) for r in range(pool)]
+    for t in ts:
+        wait(t)
+    burst = time.perf_counter() - t0
+    q.finish()
+    s.close()
+    lat = np.asarray(lat)
+    return {"round_trip_ms": {"p50": 1e3 * float(np.percentile(lat, 50)), "p99": 1e3 * float(np.percentile(lat, 99))},
+            "burst_%d_ms" % pool: 1e3 * burst,
+            "what": "quadruped SRBD N = %d, 5 SQP iterations: one request pushed into the running queue kernel's "
+                    "ring and its result row read back on the host, %d times; then %d requests at once" %
+                    (N, reps, pool)}
+
+
 def lone_latency(dev, opts, horizons=(50, 100, 200), reps=10):
     """Latency of one lone solve (batch 1, CUDA events around the launch) of
     the roll-pitch-yaw quadruped and the biped: one warp per instance (the
@@ -398,10 +438,13 @@ def run_served(dev, opts):
     from mpx_gb300.server import EpisodeStream, MPCServer, default_models, served_workload
     out = {}
     # config 3: the mixed stream, 200-tick episodes with state drift, one warp per instance; then the same
-    # stream with horizons of 64 and more on the time-parallel team kernel (8 warps per instance)
-    for key, o3 in (("mixed", opts), ("mixed_team8", dataclasses.replace(opts, team_warps=8, team_min_horizon=64))):
+    # stream with horizons of 64 and more on the time-parallel team kernel (8 warps per instance), and with
+    # both models' ticks of a step in one mixed-model launch
+    for key, o3, mixed in (("mixed", opts, False),
+                           ("mixed_team8", dataclasses.replace(opts, team_warps=8, team_min_horizon=64), False),
+                           ("mixed_one_launch", opts, True)):
         srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=o3, drift_std=0.01, streams=32,
-                        device=dev)
+                        device=dev, mixed_launch=mixed)
         es = EpisodeStream(srv, seed=1)
         served_workload(srv, 400, 20000.0, 0.5, seed=1, stream=es, stagger=True)
         launches0 = srv.launches
@@ -414,8 +457,10 @@ def run_served(dev, opts):
                          "alternating), N uniform in [20, 200], 200-tick episodes at staggered ages (ended episodes "
                          "are replaced by cold ones), state drift N(0, 0.01^2) per tick, 8 GB admission budget, "
                          "32 streams; 0.5 s warm-up of the same episodes, then 2 s measured; " +
-                         ("one warp per instance" if key == "mixed" else
-                          "horizons >= 64 on the time-parallel team kernel (8 warps per instance)"))
+                         {"mixed": "one warp per instance",
+                          "mixed_team8": "horizons >= 64 on the time-parallel team kernel (8 warps per instance)",
+                          "mixed_one_launch": "one warp per instance, both models' ticks of a step in one "
+                                              "mixed-model launch (mpxg_solve_mixed)"}[key])
         if key == "mixed":
             out.update(e)
         else:
@@ -665,6 +710,7 @@ def run_ours(args, rank, world, local_rank):
 
     # ---------------- one lone solve: one warp vs the time-parallel team kernel
     lone = lone_latency(dev, opts) if (not args.profile and rank == 0) else None
+    queue = queue_latency(dev, opts) if (not args.profile and rank == 0) else None
 
     # ---------------- end to end through the drop-in wrapper API (reference model and config)
     dropin = None
@@ -732,6 +778,7 @@ def run_ours(args, rank, world, local_rank):
         "n50": n50,
         "fp64_error": fp64,
         "lone_solve_latency_ms": lone,
+        "device_queue": queue,
         "e2e_dropin": dropin,
         "vjp": vjp,
         "served": served,

@@ -559,8 +559,10 @@ mpxg_status mpxg_queue_start(mpxg_handle* h, void* stream, const mpxg_batch_io* 
   qa.head = q->head;
   qa.capacity = capacity;
   qa.timeout_ns = idle_timeout_ns;
+  // one block per SM: as many concurrent solves as SMs x warps per block, and
+  // few idle warps polling the ring in host memory
   const int wpb = h->warps_per_block;
-  const int blocks = h->num_sms * h->blocks_per_sm_lat;
+  const int blocks = h->num_sms;
   e = sqp_ops(h->desc.model)->launch_queue(h->mc, h->sp, bp, qa, blocks, wpb, q->stream);
   if (e != cudaSuccess) {
     queue_free(q);

@@ -51,8 +51,8 @@ __device__ inline int queue_next(const QueueArgs& q, int* ticket) {
     if (ld_acquire_sys(q.tail) > i) return ld_acquire_sys(q.entries + (i % q.capacity));
     if (ld_acquire_sys(q.stop)) return -1;
     if ((long long)(global_ns() - t0) > q.timeout_ns) break;
-    __nanosleep(ns);
-    ns = ns < 16384 ? 2 * ns : 16384;
+    __nanosleep(ns);  // back off to 32 us: keeps the idle warps' polls of host memory rare
+    ns = ns < 32768 ? 2 * ns : 32768;
   }
   atomicOr(q.status, QUEUE_TIMEOUT);
   return -1;

@@ -38,27 +38,38 @@ struct Cap {
 using CapAny = Cap<MPXG_WB_MAX_BODY, MPXG_WB_MAX_DOF, MPXG_WB_MAX_CONTACT, 2, 1>;
 using CapQuad = Cap<16, 20, 4, 3, 9>;
 
-struct Args {
-  const float *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd, *u;
+// The kernels are generic over the scalar T: float for every entry point,
+// double for the whole-body SQP's central-difference Jacobians (wb_sqp.cu).
+template <class T>
+struct ArgsT {
+  const T *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd, *u;
   const int* contact;
-  float *M, *bias, *cpos, *J, *cvel, *tau, *x_next;
-  int sq, sv;        // row strides of qpos and qvel (floats)
-  float dt, alpha;   // the dynamics step
+  T *M, *bias, *cpos, *J, *cvel, *tau, *x_next;
+  int sq, sv;        // row strides of qpos and qvel (elements)
+  T dt, alpha;       // the dynamics step
 };
+using Args = ArgsT<float>;
+
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+__device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
+__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
 
 enum { MODE_TERMS = 0, MODE_INTERFACE = 1, MODE_STEP = 2 };
 
-template <class C>
+template <class C, class T = float>
 struct Warp {
   static constexpr int MB = C::MB, MD = C::MD, MR = C::MR;
-  float quat[MB][4], R[MB][9], xp[MB][3];
-  float S[MD][6];                 // per dof: (omega; linear velocity at o)
-  float V[MB][6], F[MB][6], Fc[MB][6];
-  float Ib[MB][10], Ic[MB][10];   // (m, h = m c, J_o upper triangle xx xy xz yy yz zz)
-  float M[MD][MD + 1];
-  float J[MD][MR + 1];
-  float bias[MD], qpos[MD + 4], qvel[MD], w[MD];
-  float cpos[MR], cvel[MR], a[MR], y[MR];
+  T quat[MB][4], R[MB][9], xp[MB][3];
+  T S[MD][6];                 // per dof: (omega; linear velocity at o)
+  T V[MB][6], F[MB][6], Fc[MB][6];
+  T Ib[MB][10], Ic[MB][10];   // (m, h = m c, J_o upper triangle xx xy xz yy yz zz)
+  T M[MD][MD + 1];
+  T J[MD][MR + 1];
+  T bias[MD], qpos[MD + 4], qvel[MD], w[MD];
+  T cpos[MR], cvel[MR], a[MR], y[MR];
   int dof_body[MD], depth[MB], par[MB], jtyp[MB], dadr[MB];
   unsigned anc[MB];               // bit a set: a is b or an ancestor of b
 };
@@ -66,44 +77,50 @@ struct Warp {
 __host__ __device__ __forceinline__ int ndof(int jt) { return jt == 1 ? 6 : (jt >= 2 ? 1 : 0); }
 __host__ __device__ __forceinline__ int nqpos(int jt) { return jt == 1 ? 7 : (jt >= 2 ? 1 : 0); }
 
-__device__ __forceinline__ void cross3(const float* a, const float* b, float* c) {
+template <class A, class B, class T>
+__device__ __forceinline__ void cross3(const A* a, const B* b, T* c) {
   c[0] = a[1] * b[2] - a[2] * b[1];
   c[1] = a[2] * b[0] - a[0] * b[2];
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
-__device__ __forceinline__ void quat_mul(const float* a, const float* b, float* c) {  // c = a b, (w, x, y, z)
+template <class A, class B, class T>
+__device__ __forceinline__ void quat_mul(const A* a, const B* b, T* c) {  // c = a b, (w, x, y, z)
   c[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
   c[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
   c[2] = a[0] * b[2] - a[1] * b[3] + a[2] * b[0] + a[3] * b[1];
   c[3] = a[0] * b[3] + a[1] * b[2] - a[2] * b[1] + a[3] * b[0];
 }
 // a quaternion of (near) zero norm becomes the identity, as MuJoCo does
-__device__ __forceinline__ void quat_normalize(float* q) {
-  const float n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+template <class T>
+__device__ __forceinline__ void quat_normalize(T* q) {
+  const T n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
   if (!(n2 > 1e-30f)) {
-    q[0] = 1.0f; q[1] = q[2] = q[3] = 0.0f;
+    q[0] = T(1.0); q[1] = q[2] = q[3] = T(0.0);
     return;
   }
-  const float s = rsqrtf(n2);
+  const T s = rsqrt_t(n2);
 #pragma unroll
   for (int i = 0; i < 4; ++i) q[i] *= s;
 }
 // rotation matrix (row-major, world from body) of a unit quaternion
-__device__ __forceinline__ void quat_mat(const float* q, float* R) {
-  const float w = q[0], x = q[1], y = q[2], z = q[3];
-  R[0] = 1.0f - 2.0f * (y * y + z * z); R[1] = 2.0f * (x * y - w * z); R[2] = 2.0f * (x * z + w * y);
-  R[3] = 2.0f * (x * y + w * z); R[4] = 1.0f - 2.0f * (x * x + z * z); R[5] = 2.0f * (y * z - w * x);
-  R[6] = 2.0f * (x * z - w * y); R[7] = 2.0f * (y * z + w * x); R[8] = 1.0f - 2.0f * (x * x + y * y);
+template <class A, class T>
+__device__ __forceinline__ void quat_mat(const A* q, T* R) {
+  const T w = q[0], x = q[1], y = q[2], z = q[3];
+  R[0] = T(1.0) - T(2.0) * (y * y + z * z); R[1] = T(2.0) * (x * y - w * z); R[2] = T(2.0) * (x * z + w * y);
+  R[3] = T(2.0) * (x * y + w * z); R[4] = T(1.0) - T(2.0) * (x * x + z * z); R[5] = T(2.0) * (y * z - w * x);
+  R[6] = T(2.0) * (x * z - w * y); R[7] = T(2.0) * (y * z + w * x); R[8] = T(1.0) - T(2.0) * (x * x + y * y);
 }
-__device__ __forceinline__ void mat_vec(const float* R, const float* v, float* o) {
+template <class A, class B, class T>
+__device__ __forceinline__ void mat_vec(const A* R, const B* v, T* o) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) o[i] = R[3 * i] * v[0] + R[3 * i + 1] * v[1] + R[3 * i + 2] * v[2];
 }
 // spatial inertia (m, h, J_o) times a motion (w; v): (J w + h × v; m v + w × h)
-__device__ __forceinline__ void inert_mul(const float* I, const float* s, float* o) {
-  const float m = I[0], h[3] = {I[1], I[2], I[3]};
-  const float Jxx = I[4], Jxy = I[5], Jxz = I[6], Jyy = I[7], Jyz = I[8], Jzz = I[9];
-  float hv[3], wh[3];
+template <class T>
+__device__ __forceinline__ void inert_mul(const T* I, const T* s, T* o) {
+  const T m = I[0], h[3] = {I[1], I[2], I[3]};
+  const T Jxx = I[4], Jxy = I[5], Jxz = I[6], Jyy = I[7], Jyz = I[8], Jzz = I[9];
+  T hv[3], wh[3];
   cross3(h, s + 3, hv);
   cross3(s, h, wh);
   o[0] = Jxx * s[0] + Jxy * s[1] + Jxz * s[2] + hv[0];
@@ -113,8 +130,9 @@ __device__ __forceinline__ void inert_mul(const float* I, const float* s, float*
   for (int i = 0; i < 3; ++i) o[3 + i] = m * s[3 + i] + wh[i];
 }
 // motion cross motion: (w; v) ×m (w2; v2) = (w × w2; w × v2 + v × w2)
-__device__ __forceinline__ void crm(const float* a, const float* b, float* o) {
-  float t[3];
+template <class T>
+__device__ __forceinline__ void crm(const T* a, const T* b, T* o) {
+  T t[3];
   cross3(a, b, o);
   cross3(a, b + 3, o + 3);
   cross3(a + 3, b, t);
@@ -122,15 +140,17 @@ __device__ __forceinline__ void crm(const float* a, const float* b, float* o) {
   for (int i = 0; i < 3; ++i) o[3 + i] += t[i];
 }
 // motion cross force: (w; v) ×f (n; f) = (w × n + v × f; w × f)
-__device__ __forceinline__ void crf(const float* a, const float* f, float* o) {
-  float t[3];
+template <class T>
+__device__ __forceinline__ void crf(const T* a, const T* f, T* o) {
+  T t[3];
   cross3(a, f, o);
   cross3(a + 3, f + 3, t);
   cross3(a, f + 3, o + 3);
 #pragma unroll
   for (int i = 0; i < 3; ++i) o[i] += t[i];
 }
-__device__ __forceinline__ float dot6(const float* a, const float* b) {
+template <class T>
+__device__ __forceinline__ T dot6(const T* a, const T* b) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
 }
 
@@ -138,18 +158,18 @@ __device__ __forceinline__ float dot6(const float* a, const float* b) {
 // matrix: lane c holds column c in col[0..N).  Without pivoting (the matrices
 // here are symmetric positive definite); afterwards the columns right of the
 // pivots hold the solutions.
-template <int N>
-__device__ __forceinline__ void gj_lanes(float (&col)[N], int n) {
+template <int N, class T>
+__device__ __forceinline__ void gj_lanes(T (&col)[N], int n) {
   const unsigned full = 0xffffffffu;
 #pragma unroll
   for (int k = 0; k < N; ++k) {
     if (k < n) {
-      const float dk = __shfl_sync(full, col[k], k);
-      const float yk = col[k] / dk;
+      const T dk = __shfl_sync(full, col[k], k);
+      const T yk = col[k] / dk;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         if (i < n && i != k) {
-          const float gik = __shfl_sync(full, col[i], k);
+          const T gik = __shfl_sync(full, col[i], k);
           col[i] -= gik * yk;
         }
       }
@@ -165,22 +185,22 @@ __device__ __forceinline__ void gj_lanes(float (&col)[N], int n) {
 //   v+ = qdot + (z + Y f) dt,  p+ = p + v+ dt,  quat+ = quat * exp(w+ dt / 2),
 //   q+ = q + dq+ dt;  x+ = [p+, quat+, q+, v+, contact points at x, f].
 // Requires a free root, nq = nv + 1 and nv + 3 C + 1 <= 32 (host checks).
-template <class C>
-__device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C>& s, const Args& a, size_t e, int lane) {
+template <class C, class T>
+__device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, const ArgsT<T>& a, size_t e, int lane) {
   constexpr int MD = C::MD, MR = C::MR;
   const int nv = m.nv, nq = m.nq, nc = m.n_contact, nr = 3 * nc;
   // [M | J | tau - bias], lane c holding column c
-  float col[MD];
+  T col[MD];
 #pragma unroll
   for (int i = 0; i < MD; ++i) {
-    float g = 0.0f;
+    T g = T(0.0);
     if (i < nv) {
       if (lane < nv)
         g = s.M[i][lane];
       else if (lane < nv + nr)
         g = s.J[i][lane - nv];
       else if (lane == nv + nr)
-        g = (i >= 6 ? a.u[e * (nv - 6) + (i - 6)] : 0.0f) - s.bias[i];
+        g = (i >= 6 ? a.u[e * (nv - 6) + (i - 6)] : T(0.0)) - s.bias[i];
     }
     col[i] = g;
   }
@@ -198,20 +218,20 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C>& s, const A
   }
   __syncwarp();
   // [J'Y | -J'z - 2 alpha J'qdot] over the contact rows
-  float c2[MR];
+  T c2[MR];
 #pragma unroll
   for (int r = 0; r < MR; ++r) {
-    float g = 0.0f;
+    T g = T(0.0);
     if (r < nr) {
       if (lane < nr) {
         for (int i = 0; i < nv; ++i) g += s.J[i][r] * s.M[i][lane];
       } else if (lane == nr) {
-        float jz = 0.0f, jv = 0.0f;
+        T jz = T(0.0), jv = T(0.0);
         for (int i = 0; i < nv; ++i) {
           jz += s.J[i][r] * s.w[i];
           jv += s.J[i][r] * s.qvel[i];
         }
-        g = -jz - 2.0f * a.alpha * jv;
+        g = -jz - T(2.0) * a.alpha * jv;
       }
     }
     c2[r] = g;
@@ -220,28 +240,28 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C>& s, const A
   if (lane == nr) {
 #pragma unroll
     for (int r = 0; r < MR; ++r)
-      if (r < nr) s.y[r] = c2[r] * (float)a.contact[e * nc + r / 3];
+      if (r < nr) s.y[r] = c2[r] * (T)a.contact[e * nc + r / 3];
   }
   __syncwarp();
   // v+ (in the bias storage, no longer needed)
   if (lane < nv) {
-    float acc = s.w[lane];
+    T acc = s.w[lane];
     for (int r = 0; r < nr; ++r) acc += s.M[lane][r] * s.y[r];
     s.bias[lane] = s.qvel[lane] + acc * a.dt;
   }
   __syncwarp();
   const int nx = nq + nv + 2 * nr;
-  float* xo = a.x_next + e * nx;
-  const float dt = a.dt;
+  T* xo = a.x_next + e * nx;
+  const T dt = a.dt;
   if (lane < 3) xo[lane] = s.qpos[lane] + s.bias[lane] * dt;
   if (lane == 3) {  // quat * exp(w dt / 2), w in the body frame, renormalised
-    const float w0 = s.bias[3], w1 = s.bias[4], w2 = s.bias[5];
-    const float n = sqrtf(w0 * w0 + w1 * w1 + w2 * w2);
-    const float inv = n > 0.0f ? 1.0f / n : 0.0f;
-    float sh, ch;
-    sincosf(0.5f * n * dt, &sh, &ch);
-    const float qr[4] = {ch, w0 * inv * sh, w1 * inv * sh, w2 * inv * sh};
-    float qn[4];
+    const T w0 = s.bias[3], w1 = s.bias[4], w2 = s.bias[5];
+    const T n = sqrt_t(w0 * w0 + w1 * w1 + w2 * w2);
+    const T inv = n > T(0.0) ? T(1.0) / n : T(0.0);
+    T sh, ch;
+    sincos_t(T(0.5) * n * dt, &sh, &ch);
+    const T qr[4] = {ch, w0 * inv * sh, w1 * inv * sh, w2 * inv * sh};
+    T qn[4];
     quat_mul(s.qpos + 3, qr, qn);
     quat_normalize(qn);
 #pragma unroll
@@ -259,15 +279,15 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C>& s, const A
 // precede children, one joint per body, the free joint only on body 0, dof and
 // qpos addresses dense in body order, contacts on existing bodies) and fit the
 // capacity C: nbody <= MB, nv <= MD, nq <= MD + 4, 3 x contacts <= MR.
-template <int MODE, class C>
+template <int MODE, class C, class T = float>
 __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch,
-                                                                 Args a) {
+                                                                 ArgsT<T> a) {
   constexpr int MB = C::MB, MR = C::MR;
-  __shared__ Warp<C> sw[C::NW];
+  __shared__ Warp<C, T> sw[C::NW];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int env = blockIdx.x * C::NW + wid;
   if (env >= batch) return;  // the whole warp leaves; no block-wide barrier follows
-  Warp<C>& s = sw[wid];
+  Warp<C, T>& s = sw[wid];
   const unsigned full = 0xffffffffu;
   const int nb = m.nbody, nq = m.nq, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
   for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * a.sq + i];
@@ -300,14 +320,14 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   for (int d = 0; d <= maxd; ++d) {
     if (lane < nb && s.depth[lane] == d) {
       const int b = lane, p = s.par[b], jt = s.jtyp[b];
-      float q[4], x[3];
+      T q[4], x[3];
       if (jt == 1) {
-        const float* qp = s.qpos + m.qpos_adr[b];
+        const T* qp = s.qpos + m.qpos_adr[b];
         x[0] = qp[0]; x[1] = qp[1]; x[2] = qp[2];
         q[0] = qp[3]; q[1] = qp[4]; q[2] = qp[5]; q[3] = qp[6];
       } else {
-        float pq[4] = {1.0f, 0.0f, 0.0f, 0.0f}, px[3] = {0.0f, 0.0f, 0.0f};
-        float pR[9] = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+        T pq[4] = {T(1.0), T(0.0), T(0.0), T(0.0)}, px[3] = {T(0.0), T(0.0), T(0.0)};
+        T pR[9] = {T(1.0), T(0.0), T(0.0), T(0.0), T(1.0), T(0.0), T(0.0), T(0.0), T(1.0)};
         if (p >= 0) {
 #pragma unroll
           for (int i = 0; i < 4; ++i) pq[i] = s.quat[p][i];
@@ -316,24 +336,24 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
 #pragma unroll
           for (int i = 0; i < 9; ++i) pR[i] = s.R[p][i];
         }
-        float bp[3];
+        T bp[3];
         mat_vec(pR, m.body_pos[b], bp);
 #pragma unroll
         for (int i = 0; i < 3; ++i) x[i] = px[i] + bp[i];
         quat_mul(pq, m.body_quat[b], q);
         if (jt >= 2) {
-          float Rb[9], t[3];
+          T Rb[9], t[3];
           quat_mat(q, Rb);
-          const float qj = s.qpos[m.qpos_adr[b]];
+          const T qj = s.qpos[m.qpos_adr[b]];
           if (jt == 2) {  // rotate about the axis through the anchor
-            float anchor[3];
+            T anchor[3];
             mat_vec(Rb, m.jnt_pos[b], t);
 #pragma unroll
             for (int i = 0; i < 3; ++i) anchor[i] = x[i] + t[i];
-            float sh, ch;
-            sincosf(0.5f * qj, &sh, &ch);
-            const float qa[4] = {ch, sh * m.jnt_axis[b][0], sh * m.jnt_axis[b][1], sh * m.jnt_axis[b][2]};
-            float qn[4];
+            T sh, ch;
+            sincos_t(T(0.5) * qj, &sh, &ch);
+            const T qa[4] = {ch, sh * m.jnt_axis[b][0], sh * m.jnt_axis[b][1], sh * m.jnt_axis[b][2]};
+            T qn[4];
             quat_mul(q, qa, qn);
             quat_normalize(qn);
 #pragma unroll
@@ -358,19 +378,19 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
     }
     __syncwarp();
   }
-  const float o[3] = {s.xp[0][0], s.xp[0][1], s.xp[0][2]};
+  const T o[3] = {s.xp[0][0], s.xp[0][1], s.xp[0][2]};
   // ---- 2. dof axes and body inertias about o
   if (lane < nb) {
     const int b = lane, jt = s.jtyp[b], da = s.dadr[b];
-    const float* R = s.R[b];
-    const float* xb = s.xp[b];
-    float c[3];
+    const T* R = s.R[b];
+    const T* xb = s.xp[b];
+    T c[3];
     mat_vec(R, m.com[b], c);
 #pragma unroll
     for (int i = 0; i < 3; ++i) c[i] += xb[i] - o[i];
     // I_world = R I R'
     const float* Il = m.inertia[b];
-    float RI[9], Iw[9];
+    T RI[9], Iw[9];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -379,53 +399,53 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int k = 0; k < 3; ++k) Iw[3 * i + k] = RI[3 * i] * R[3 * k] + RI[3 * i + 1] * R[3 * k + 1] + RI[3 * i + 2] * R[3 * k + 2];
-    const float ms = m.mass[b], cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-    float* Ib = s.Ib[b];
+    const T ms = m.mass[b], cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    T* Ib = s.Ib[b];
     Ib[0] = ms;
     Ib[1] = ms * c[0]; Ib[2] = ms * c[1]; Ib[3] = ms * c[2];
     Ib[4] = Iw[0] + ms * (cc - c[0] * c[0]);
-    Ib[5] = 0.5f * (Iw[1] + Iw[3]) - ms * c[0] * c[1];
-    Ib[6] = 0.5f * (Iw[2] + Iw[6]) - ms * c[0] * c[2];
+    Ib[5] = T(0.5) * (Iw[1] + Iw[3]) - ms * c[0] * c[1];
+    Ib[6] = T(0.5) * (Iw[2] + Iw[6]) - ms * c[0] * c[2];
     Ib[7] = Iw[4] + ms * (cc - c[1] * c[1]);
-    Ib[8] = 0.5f * (Iw[5] + Iw[7]) - ms * c[1] * c[2];
+    Ib[8] = T(0.5) * (Iw[5] + Iw[7]) - ms * c[1] * c[2];
     Ib[9] = Iw[8] + ms * (cc - c[2] * c[2]);
-    float r[3];
+    T r[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) r[i] = o[i] - xb[i];
     if (jt == 1) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float* St = s.S[da + k];
-        St[0] = St[1] = St[2] = 0.0f;
-        St[3] = k == 0 ? 1.0f : 0.0f; St[4] = k == 1 ? 1.0f : 0.0f; St[5] = k == 2 ? 1.0f : 0.0f;
-        float* Sr = s.S[da + 3 + k];
+        T* St = s.S[da + k];
+        St[0] = St[1] = St[2] = T(0.0);
+        St[3] = k == 0 ? T(1.0) : T(0.0); St[4] = k == 1 ? T(1.0) : T(0.0); St[5] = k == 2 ? T(1.0) : T(0.0);
+        T* Sr = s.S[da + 3 + k];
         Sr[0] = R[k]; Sr[1] = R[3 + k]; Sr[2] = R[6 + k];
         cross3(Sr, r, Sr + 3);
       }
     } else if (jt == 2) {
-      float* Sj = s.S[da];
-      float t[3];
+      T* Sj = s.S[da];
+      T t[3];
       mat_vec(R, m.jnt_axis[b], Sj);
       mat_vec(R, m.jnt_pos[b], t);
-      float ra[3];
+      T ra[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) ra[i] = r[i] - t[i];  // o - anchor
       cross3(Sj, ra, Sj + 3);
     } else if (jt == 3) {
-      float* Sj = s.S[da];
-      Sj[0] = Sj[1] = Sj[2] = 0.0f;
+      T* Sj = s.S[da];
+      Sj[0] = Sj[1] = Sj[2] = T(0.0);
       mat_vec(R, m.jnt_axis[b], Sj + 3);
     }
   }
   __syncwarp();
   // ---- 3. velocities
   if (lane < nb) {
-    float Vb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    T Vb[6] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
     int b = lane;
     for (int g = 0; g < MB && b >= 0; ++g, b = s.par[b]) {
       const int nd = ndof(s.jtyp[b]), da = s.dadr[b];
       for (int k = 0; k < nd; ++k) {
-        const float qd = s.qvel[da + k];
+        const T qd = s.qvel[da + k];
 #pragma unroll
         for (int i = 0; i < 6; ++i) Vb[i] += s.S[da + k][i] * qd;
       }
@@ -436,20 +456,20 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   __syncwarp();
   // accelerations at qacc = 0 and the bias force of each body
   if (lane < nb) {
-    float A[6] = {0.0f, 0.0f, 0.0f, -m.gravity[0], -m.gravity[1], -m.gravity[2]};
+    T A[6] = {T(0.0), T(0.0), T(0.0), -m.gravity[0], -m.gravity[1], -m.gravity[2]};
     int b = lane;
     for (int g = 0; g < MB && b >= 0; ++g, b = s.par[b]) {
       const int jt = s.jtyp[b], nd = ndof(jt), da = s.dadr[b];
       // the free joint's translation axes are fixed in the world: no derivative
       for (int k = (jt == 1 ? 3 : 0); k < nd; ++k) {
-        float t[6];
+        T t[6];
         crm(s.V[b], s.S[da + k], t);
-        const float qd = s.qvel[da + k];
+        const T qd = s.qvel[da + k];
 #pragma unroll
         for (int i = 0; i < 6; ++i) A[i] += t[i] * qd;
       }
     }
-    float IA[6], IV[6], t[6];
+    T IA[6], IV[6], t[6];
     inert_mul(s.Ib[lane], A, IA);
     inert_mul(s.Ib[lane], s.V[lane], IV);
     crf(s.V[lane], IV, t);
@@ -459,9 +479,9 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   __syncwarp();
   // subtree sums
   if (lane < nb) {
-    float Fc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, Ic[10];
+    T Fc[6] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)}, Ic[10];
 #pragma unroll
-    for (int i = 0; i < 10; ++i) Ic[i] = 0.0f;
+    for (int i = 0; i < 10; ++i) Ic[i] = T(0.0);
     for (int d = lane; d < nb; ++d) {
       if ((s.anc[d] >> lane) & 1u) {
 #pragma unroll
@@ -478,7 +498,7 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   // contact points
   if (lane < nc) {
     const int gb = m.contact_point_body[lane];
-    float t[3];
+    T t[3];
     mat_vec(s.R[gb], m.contact_point_pos[lane], t);
 #pragma unroll
     for (int i = 0; i < 3; ++i) s.cpos[3 * lane + i] = s.xp[gb][i] + t[i];
@@ -488,18 +508,18 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   if (lane < nv) {
     const int j = lane, bj = s.dof_body[j];
     s.bias[j] = dot6(s.S[j], s.Fc[bj]);
-    float Fj[6];
+    T Fj[6];
     inert_mul(s.Ic[bj], s.S[j], Fj);
     for (int i = 0; i <= j; ++i) {
-      const float v = ((s.anc[bj] >> s.dof_body[i]) & 1u) ? dot6(s.S[i], Fj) : 0.0f;
+      const T v = ((s.anc[bj] >> s.dof_body[i]) & 1u) ? dot6(s.S[i], Fj) : T(0.0);
       s.M[i][j] = v;
       s.M[j][i] = v;
     }
     s.M[j][j] += m.armature[j];
     for (int c = 0; c < nc; ++c) {
-      float jp[3] = {0.0f, 0.0f, 0.0f};
+      T jp[3] = {T(0.0), T(0.0), T(0.0)};
       if ((s.anc[m.contact_jac_body[c]] >> bj) & 1u) {
-        float r[3], t[3];
+        T r[3], t[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) r[i] = s.cpos[3 * c + i] - o[i];
         cross3(s.S[j], r, t);
@@ -512,7 +532,7 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   }
   __syncwarp();
   if (lane < nr) {
-    float v = 0.0f;
+    T v = T(0.0);
     for (int j = 0; j < nv; ++j) v += s.J[j][lane] * s.qvel[j];
     s.cvel[lane] = v;
   }
@@ -535,7 +555,7 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   }
   // ---- the interface (mpc_utils.py:300-311)
   if (lane < nr) {
-    float v = 0.0f;
+    T v = T(0.0);
     for (int q = 0; q < nr; ++q)
       v += a.Kp[lane * nr + q] * (a.foot_ref[e * nr + q] - s.cpos[q]) +
            a.Kd[lane * nr + q] * (a.foot_ref_dot[e * nr + q] - s.cvel[q]);
@@ -543,10 +563,10 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   }
   __syncwarp();
   // y = (J'J)^-1 a by Gauss-Jordan on [J'J | a], lane c holding column c
-  float col[MR];
+  T col[MR];
 #pragma unroll
   for (int i = 0; i < MR; ++i) {
-    float g = 0.0f;
+    T g = T(0.0);
     if (i < nr) {
       if (lane < nr) {
         for (int j = 0; j < nv; ++j) g += s.J[j][i] * s.J[j][lane];
@@ -564,19 +584,19 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   }
   __syncwarp();
   if (lane < nv) {  // w = pinv(J') a = J y
-    float v = 0.0f;
+    T v = T(0.0);
     for (int r = 0; r < nr; ++r) v += s.J[lane][r] * s.y[r];
     s.w[lane] = v;
   }
   __syncwarp();
   if (lane >= 6 && lane < nv) {
     const int j = lane;
-    float mw = 0.0f, jg = 0.0f;
+    T mw = T(0.0), jg = T(0.0);
     for (int i = 0; i < nv; ++i) mw += s.M[j][i] * s.w[i];
     for (int r = 0; r < nr; ++r) jg += s.J[j][r] * a.grf[e * nr + r];
-    const float fb = s.bias[j] + mw, mpc = -jg;
-    const float msk = (float)a.contact[e * nc + (j - 6) / 3];
-    a.tau[e * (nv - 6) + (j - 6)] = mpc * msk + (1.0f - msk) * fb;
+    const T fb = s.bias[j] + mw, mpc = -jg;
+    const T msk = (T)a.contact[e * nc + (j - 6) / 3];
+    a.tau[e * (nv - 6) + (j - 6)] = mpc * msk + (T(1.0) - msk) * fb;
   }
   if (a.J)
     for (int i = lane; i < nv * nr; i += 32) a.J[e * nv * nr + i] = s.J[i / nr][i % nr];
