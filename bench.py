@@ -78,7 +78,7 @@ def parse():
     ap.add_argument("--no-n50", action="store_true", help="skip the fixed-horizon N=50 section")
     ap.add_argument("--no-dropin", action="store_true", help="skip the drop-in wrapper end-to-end section")
     ap.add_argument("--no-autotune", action="store_true", help="use the default launch geometry")
-    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq", "wb"],
+    ap.add_argument("--workload", default="mpc", choices=["mpc", "lqr", "lqr_eq", "wb", "wb_sqp"],
                     help="mpc: the batched SRBD MPC tick (default); lqr: the isolated LQR solve; lqr_eq: the "
                          "equality-constrained n=72 LQ solve")
     ap.add_argument("--lqr-method", type=int, default=0, choices=[0, 1],
@@ -829,6 +829,10 @@ def other_configs(args, rank, world, local_rank):
     w = run_wb(a, rank, world, local_rank, emit=False)
     out["wb_interface_4096_aliengo"] = {"metric": "whole-body interface evaluations/s", "value": w["value"],
                                         "us_per_call": w["us_per_call"], "e2e": w["e2e"]["value"]}
+    a.steps = 10
+    ws = run_wb_sqp(a, rank, world, local_rank, emit=False)
+    out["wb_sqp_aliengo_N25"] = {"metric": ws["metric"], "value": ws["value"], "ms_per_step": ws["ms_per_step"],
+                                 "lone": ws["lone"], "batch": ws["batch"]}
     return out
 
 
@@ -1230,6 +1234,82 @@ def run_wb(args, rank, world, local_rank, emit=True):
     return line
 
 
+# ------------------------------------------------------------ whole-body SQP workload
+WBS_N, WBS_ITERS, WBS_BATCH = 25, 5, 64
+
+
+def run_wb_sqp(args, rank, world, local_rank, emit=True):
+    """--workload wb_sqp: the whole-body MPC solve of mpc_wrapper.py's
+    wrappers (mpxg_wb_sqp; aliengo, config_aliengo.py: N = 25, dt = 0.02,
+    its W), 5 SQP iterations per control tick, warm-started from the shifted
+    previous solution with x0 = X[1] of it, on seeded synthetic instances
+    (problem.wb_workload).  Two figures: one instance per solve (the
+    single-environment MPCControllerWrapper; p50/p99 over the timed ticks),
+    and a batch of 64 (the batched wrapper) in solves/s."""
+    import torch
+    from mpx_gb300 import configs, mjcf, problem
+    from mpx_gb300.replicas import max_over_ranks
+    from mpx_gb300.wholebody import WholeBodyModel, WholeBodySQP
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    fix = os.path.join(ROOT, "tests", "golden", "aliengo_wb.npz")
+    model = mjcf.load_npz(fix)
+    d = np.load(fix)
+    cfg = configs.aliengo_wb()
+    wb = WholeBodyModel(model, device=dev)
+    N = WBS_N
+    Bb = WBS_BATCH if args.batch == BATCH else int(args.batch)
+    steps = max(3, min(args.steps, 30))
+    res = {}
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    for label, B in (("lone", 1), ("batch", Bb)):
+        wl = problem.wb_workload(B, N, d["q0"], d["p_legs0"], float(np.sum(model.mass)), seed=21 + 1000 * rank)
+        sqp = WholeBodySQP(wb, N=N, batch_max=B, iters=WBS_ITERS)
+        ref = torch.as_tensor(wl["reference"], device=dev)
+        cont = torch.as_tensor(wl["contact"], device=dev)
+        Wd = torch.as_tensor(cfg.W_diag, device=dev)
+        out = sqp.solve(wl["x0"], wl["X0"], wl["U0"], wl["V0"], ref, cont, Wd, iters=12)
+        sh = lambda a: torch.cat([a[:, 1:], a[:, -1:]], 1)
+        times, kkts = [], []
+        for tick in range(max(args.warmup, 3) + steps):
+            X, U, V = out["X"], out["U"], out["V"]
+            ref, cont = sh(ref), sh(cont)
+            x0, Xs, Us, Vs = X[:, 1].contiguous(), sh(X), sh(U), sh(V)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = sqp.solve(x0, Xs, Us, Vs, ref, cont, Wd, inplace=True)
+            e1.record()
+            torch.cuda.synchronize()
+            if tick >= max(args.warmup, 3):
+                times.append(e0.elapsed_time(e1))
+                kkts.append(out["kkt"][:, 2].cpu().numpy())
+        t = np.array(times)
+        kk = np.concatenate(kkts)
+        res[label] = {"batch": B, "ms_p50": float(np.percentile(t, 50)), "ms_p99": float(np.percentile(t, 99)),
+                      "solves_per_s": B / (float(np.mean(t)) / 1000.0),
+                      "kkt_frac_le_1e-5": float(np.mean(kk <= 1e-5)), "kkt_median": float(np.median(kk)),
+                      "ticks": len(times)}
+    clk = clocks.stop()
+    ms = max_over_ranks(res["batch"]["ms_p50"], device=dev)
+    line = {
+        "metric": "whole-body MPC solves/s (aliengo, 61 states, N = 25, 5 SQP iterations)",
+        "value": world * Bb / (ms / 1000.0), "unit": "solves/s", "n_gpus": world, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 (Riccati) / fp64 (model, differences, merit)",
+        "data": "synthetic (seeded trotting references and perturbed standing states)",
+        "config": {"workload": "%d aliengo whole-body MPCs, N = %d, %d SQP iterations per warm tick" % (Bb, N, WBS_ITERS),
+                   "parallelism": "replicas"},
+        "lone": res["lone"], "batch": res["batch"],
+        "gpu_launches": (6 * WBS_ITERS + 4) * steps,
+        "clocks": clk,
+    }
+    if rank == 0 and emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1247,6 +1327,8 @@ def main():
         run_lqr_eq(args, rank, world, local_rank)
     elif args.workload == "wb":
         run_wb(args, rank, world, local_rank)
+    elif args.workload == "wb_sqp":
+        run_wb_sqp(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1:

@@ -569,6 +569,56 @@ mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batc
 mpxg_status mpxg_wb_step(void* stream, const mpxg_wb_model* model, int batch, float dt, float alpha, const float* x,
                          const float* u, const int* contact, float* x_next);
 
+/* SQP iterations of the whole-body MPC for a batch: the solve that
+ * mpc_wrapper.py's wrappers run each tick (self._solve / self.work,
+ * mpc_wrapper.py:150-158 and 346-354, built at :67 and :236 from
+ * config_aliengo.py / config_go2.py: quadruped_wb_dynamics,
+ * quadruped_wb_obj(True, ...), quadruped_wb_hessian_gn(True, ...)), standing
+ * in for the absent optimizers.mpc as mpxg_solve does for the SRBD model.
+ * x = [qpos, qvel, contact points (3C), contact forces (3C)] (nx = nq + nv +
+ * 6C), u = joint torques (nj = nv - 6).  One iteration at (X, U, V):
+ *   defects c_0 = x0 - X_0, c_{t+1} = f(X_t, U_t, contact_t) - X_{t+1}
+ *     (f = mpxg_wb_step's model, evaluated in float64);
+ *   Jacobians of f by central differences in float64 over qpos, qvel and u
+ *     (h_j = 1e-6 max(1, |z_j|); f does not read the point and force states);
+ *   the cost's exact gradient and the reference's Gauss-Newton blocks
+ *     (objectives.py:77-203), reg added to the control block;
+ *   the step by a float32 Riccati sweep (one 256-thread block per instance);
+ *   the merit line search of mpxg_solve (augmented-Lagrangian merit, rho
+ *     raised to 2 G / |c|^2, Armijo with eta, steps beta^k for k <
+ *     ls_max_trials evaluated together, the first accepted one taken), merit
+ *     terms in float64;
+ *   X += a dX, U += a dU, V += a (lam - V).
+ * x0 [B,nx]; X [B,N+1,nx], U [B,N,nj], V [B,N+1,nx]: the warm start in, the
+ * result out (float32); reference [B,N+1,13+nj+7C] (the whole-body reference
+ * rows: p, quat, q, v, omega, foot positions, contact, forces); contact
+ * [B,N+1,C] int (the dynamics' mask, parameter[t,:C]); W [B,12+3nj+6C] (the
+ * diagonal of the reference's block-diagonal W).  Optional outputs: kkt
+ * [B,3] (primal max |c|, dual residual / (1 + max |gradient|), their max) at
+ * the result, status [B] (MPXG_INST_* bits).  iters = 0 only evaluates kkt.
+ * Built size: nv = 18 with 4 contact points (nx = 61, nj = 12: the aliengo
+ * and go2 configurations); the model must pass mpxg_wb_step's checks.
+ * workspace: device, >= mpxg_wb_sqp_workspace_bytes(model, batch, N) bytes,
+ * 256-byte aligned.  No allocation, no host synchronisation. */
+typedef struct {
+  const mpxg_wb_model* model; /* host pointer */
+  int batch, N, iters;
+  float dt, alpha;            /* step and Baumgarte gain (25 in the reference) */
+  int swing_tracking;         /* quadruped_wb_obj's first argument (True in both configs) */
+  float reg, rho0, ls_beta, ls_eta, ls_skip_tol;
+  int ls_max_trials;          /* 1..8 */
+  const float* x0;
+  float *X, *U, *V;
+  const float* reference;
+  const int* contact;
+  const float* W;
+  float* kkt;
+  int* status;
+  void* workspace;
+} mpxg_wb_sqp_io;
+size_t mpxg_wb_sqp_workspace_bytes(const mpxg_wb_model* model, int batch, int N);
+mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io);
+
 /* Last error message of a handle (or of the library when h is NULL). */
 const char* mpxg_last_error(const mpxg_handle* h);
 const char* mpxg_status_string(int status);

@@ -122,6 +122,17 @@ class WbModel(ctypes.Structure):
                 ("contact_point_pos", (ctypes.c_float * 3) * _C)]
 
 
+class WbSqpIO(ctypes.Structure):
+    """mpxg_wb_sqp_io (include/mpxg.h)."""
+    _fields_ = [("model", ctypes.POINTER(WbModel)), ("batch", ctypes.c_int), ("N", ctypes.c_int),
+                ("iters", ctypes.c_int), ("dt", ctypes.c_float), ("alpha", ctypes.c_float),
+                ("swing_tracking", ctypes.c_int), ("reg", ctypes.c_float), ("rho0", ctypes.c_float),
+                ("ls_beta", ctypes.c_float), ("ls_eta", ctypes.c_float), ("ls_skip_tol", ctypes.c_float),
+                ("ls_max_trials", ctypes.c_int)] + \
+               [(k, ctypes.c_void_p) for k in ("x0", "X", "U", "V", "reference", "contact", "W", "kkt", "status",
+                                                "workspace")]
+
+
 # Exported symbols (every entry point declared in include/mpxg.h).
 EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace_bytes", "mpxg_solve",
            "mpxg_solve_plain", "mpxg_shift_warm_start", "mpxg_timer_run", "mpxg_refgen_srbd", "mpxg_gait_tables",
@@ -129,7 +140,7 @@ EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
-           "mpxg_wb_terms", "mpxg_wb_interface", "mpxg_wb_step"]
+           "mpxg_wb_terms", "mpxg_wb_interface", "mpxg_wb_step", "mpxg_wb_sqp_workspace_bytes", "mpxg_wb_sqp"]
 
 _lib = None
 
@@ -208,6 +219,10 @@ def load(build_if_missing=True):
     L.mpxg_wb_interface.restype = ctypes.c_int
     L.mpxg_wb_step.argtypes = [vp, ctypes.POINTER(WbModel), ctypes.c_int, ctypes.c_float, ctypes.c_float] + [vp] * 4
     L.mpxg_wb_step.restype = ctypes.c_int
+    L.mpxg_wb_sqp_workspace_bytes.argtypes = [ctypes.POINTER(WbModel), ctypes.c_int, ctypes.c_int]
+    L.mpxg_wb_sqp_workspace_bytes.restype = ctypes.c_size_t
+    L.mpxg_wb_sqp.argtypes = [vp, ctypes.POINTER(WbSqpIO)]
+    L.mpxg_wb_sqp.restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_xla_solve_vjp.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmpxg.so")
 SOURCES = ["mpxg_abi.cu", "sqp_rpy12.cu", "sqp_quat13.cu", "sqp_biped12.cu", "sqp_mixed.cu", "lqr.cu", "lqr_eq.cu",
-           "wb.cu"]
+           "wb.cu", "wb_sqp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -63,6 +63,10 @@ inline const SqpOps* sqp_ops(int model) {
   }
 }
 
+// Host checks of a whole-body model (wb.cu): null when the whole-body
+// kernels can index its shared arrays by the model's fields, else why not.
+const char* wb_model_check(const mpxg_wb_model* m);
+
 // The library's last error of this host thread (mpxg_last_error(NULL)).
 std::string& lib_error();
 inline mpxg_status lib_fail(mpxg_status st, const std::string& msg) {

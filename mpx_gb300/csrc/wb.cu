@@ -14,7 +14,7 @@ using namespace mpxg;
 // ---------------------------------------------------------------- whole body
 // The checks the whole-body kernel relies on (it indexes shared arrays by
 // these fields without further bounds tests).
-static const char* wb_check(const mpxg_wb_model* m) {
+const char* mpxg::wb_model_check(const mpxg_wb_model* m) {
   using namespace mpxg::wb;
   if (!m) return "null model";
   if (m->nbody < 1 || m->nbody > MPXG_WB_MAX_BODY) return "nbody out of range 1..32";
@@ -56,7 +56,7 @@ extern "C" {
 mpxg_status mpxg_wb_terms(void* stream, const mpxg_wb_model* model, int batch, const float* qpos, const float* qvel,
                           float* M, float* bias, float* cpos, float* J, float* cvel) {
   using namespace mpxg::wb;
-  if (const char* why = wb_check(model)) return lib_fail(MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_terms: ") + why);
+  if (const char* why = wb_model_check(model)) return lib_fail(MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_terms: ") + why);
   if (batch < 0 || (batch > 0 && (!qpos || !qvel)))
     return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_terms: bad batch or null state");
   if (batch == 0) return MPXG_OK;
@@ -71,7 +71,7 @@ mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batc
                               const float* qvel, const float* grf, const float* foot_ref, const float* foot_ref_dot,
                               const int* contact, const float* Kp, const float* Kd, float* tau, float* J) {
   using namespace mpxg::wb;
-  if (const char* why = wb_check(model))
+  if (const char* why = wb_model_check(model))
     return lib_fail(MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_interface: ") + why);
   if (model->jnt_type[0] != 1 || model->n_contact < 1 || model->nv != 6 + 3 * model->n_contact)
     return lib_fail(MPXG_ERR_INVALID_ARG,
@@ -91,7 +91,7 @@ mpxg_status mpxg_wb_interface(void* stream, const mpxg_wb_model* model, int batc
 mpxg_status mpxg_wb_step(void* stream, const mpxg_wb_model* model, int batch, float dt, float alpha, const float* x,
                          const float* u, const int* contact, float* x_next) {
   using namespace mpxg::wb;
-  if (const char* why = wb_check(model)) return lib_fail(MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_step: ") + why);
+  if (const char* why = wb_model_check(model)) return lib_fail(MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_step: ") + why);
   const int nv = model->nv, nr = 3 * model->n_contact;
   if (model->jnt_type[0] != 1 || model->nq != nv + 1 || model->n_contact < 1 || nr > nv || nv + nr + 1 > 32)
     return lib_fail(MPXG_ERR_INVALID_ARG,

@@ -186,7 +186,8 @@ __device__ __forceinline__ void gj_lanes(T (&col)[N], int n) {
 //   q+ = q + dq+ dt;  x+ = [p+, quat+, q+, v+, contact points at x, f].
 // Requires a free root, nq = nv + 1 and nv + 3 C + 1 <= 32 (host checks).
 template <class C, class T>
-__device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, const ArgsT<T>& a, size_t e, int lane) {
+__device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, const T* u, const int* contact, T dt,
+                                     T alpha, T* xo, int lane) {
   constexpr int MD = C::MD, MR = C::MR;
   const int nv = m.nv, nq = m.nq, nc = m.n_contact, nr = 3 * nc;
   // [M | J | tau - bias], lane c holding column c
@@ -200,7 +201,7 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, cons
       else if (lane < nv + nr)
         g = s.J[i][lane - nv];
       else if (lane == nv + nr)
-        g = (i >= 6 ? a.u[e * (nv - 6) + (i - 6)] : T(0.0)) - s.bias[i];
+        g = (i >= 6 ? u[i - 6] : T(0.0)) - s.bias[i];
     }
     col[i] = g;
   }
@@ -231,7 +232,7 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, cons
           jz += s.J[i][r] * s.w[i];
           jv += s.J[i][r] * s.qvel[i];
         }
-        g = -jz - T(2.0) * a.alpha * jv;
+        g = -jz - T(2.0) * alpha * jv;
       }
     }
     c2[r] = g;
@@ -240,19 +241,16 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, cons
   if (lane == nr) {
 #pragma unroll
     for (int r = 0; r < MR; ++r)
-      if (r < nr) s.y[r] = c2[r] * (T)a.contact[e * nc + r / 3];
+      if (r < nr) s.y[r] = c2[r] * (T)contact[r / 3];
   }
   __syncwarp();
   // v+ (in the bias storage, no longer needed)
   if (lane < nv) {
     T acc = s.w[lane];
     for (int r = 0; r < nr; ++r) acc += s.M[lane][r] * s.y[r];
-    s.bias[lane] = s.qvel[lane] + acc * a.dt;
+    s.bias[lane] = s.qvel[lane] + acc * dt;
   }
   __syncwarp();
-  const int nx = nq + nv + 2 * nr;
-  T* xo = a.x_next + e * nx;
-  const T dt = a.dt;
   if (lane < 3) xo[lane] = s.qpos[lane] + s.bias[lane] * dt;
   if (lane == 3) {  // quat * exp(w dt / 2), w in the body frame, renormalised
     const T w0 = s.bias[3], w1 = s.bias[4], w2 = s.bias[5];
@@ -275,23 +273,15 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, cons
   }
 }
 
-// The model must have passed the host checks of mpxg_wb_terms (parents
-// precede children, one joint per body, the free joint only on body 0, dof and
-// qpos addresses dense in body order, contacts on existing bodies) and fit the
-// capacity C: nbody <= MB, nv <= MD, nq <= MD + 4, 3 x contacts <= MR.
-template <int MODE, class C, class T = float>
-__global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch,
-                                                                 ArgsT<T> a) {
-  constexpr int MB = C::MB, MR = C::MR;
-  __shared__ Warp<C, T> sw[C::NW];
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int env = blockIdx.x * C::NW + wid;
-  if (env >= batch) return;  // the whole warp leaves; no block-wide barrier follows
-  Warp<C, T>& s = sw[wid];
+// Passes 1-4 of the header for the configuration already in s.qpos / s.qvel:
+// kinematics, dof axes, inertias, velocities, bias forces, mass matrix,
+// contact points, their Jacobians and velocities, all left in s.  Every lane
+// of the warp takes part.
+template <class C, class T>
+__device__ __forceinline__ void rb_terms(const mpxg_wb_model& m, Warp<C, T>& s, int lane) {
+  constexpr int MB = C::MB;
   const unsigned full = 0xffffffffu;
-  const int nb = m.nbody, nq = m.nq, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
-  for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * a.sq + i];
-  if (lane < nv) s.qvel[lane] = a.qvel[(size_t)env * a.sv + lane];
+  const int nb = m.nbody, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
   // the tree's indices in shared memory: the chain walks below read them at
   // lane-dependent positions
   if (lane < nb) {
@@ -537,6 +527,26 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
     s.cvel[lane] = v;
   }
   __syncwarp();
+}
+
+// The model must have passed the host checks of mpxg_wb_terms (parents
+// precede children, one joint per body, the free joint only on body 0, dof and
+// qpos addresses dense in body order, contacts on existing bodies) and fit the
+// capacity C: nbody <= MB, nv <= MD, nq <= MD + 4, 3 x contacts <= MR.
+template <int MODE, class C, class T = float>
+__global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_constant__ mpxg_wb_model m, int batch,
+                                                                 ArgsT<T> a) {
+  constexpr int MR = C::MR;
+  __shared__ Warp<C, T> sw[C::NW];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int env = blockIdx.x * C::NW + wid;
+  if (env >= batch) return;  // the whole warp leaves; no block-wide barrier follows
+  Warp<C, T>& s = sw[wid];
+  const int nq = m.nq, nv = m.nv, nc = m.n_contact, nr = 3 * nc;
+  for (int i = lane; i < nq; i += 32) s.qpos[i] = a.qpos[(size_t)env * a.sq + i];
+  if (lane < nv) s.qvel[lane] = a.qvel[(size_t)env * a.sv + lane];
+  __syncwarp();
+  rb_terms(m, s, lane);
   if constexpr (MODE == MODE_TERMS) {
     const size_t e = (size_t)env;
     if (a.M)
@@ -550,7 +560,8 @@ __global__ void __launch_bounds__(32 * C::NW, C::MINB) wb_kernel(const __grid_co
   }
   const size_t e = (size_t)env;
   if constexpr (MODE == MODE_STEP) {
-    step(m, s, a, e, lane);
+    const int nx = nq + nv + 2 * nr;
+    step(m, s, a.u + e * (nv - 6), a.contact + e * nc, a.dt, a.alpha, a.x_next + e * nx, lane);
     return;
   }
   // ---- the interface (mpc_utils.py:300-311)

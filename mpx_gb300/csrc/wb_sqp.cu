@@ -1,0 +1,892 @@
+// Whole-body SQP (mpxg_wb_sqp): the whole-body MPC solve of mpc_wrapper.py's
+// wrappers (quadruped_wb_dynamics, models.py:39-117; quadruped_wb_obj and
+// quadruped_wb_hessian_gn, objectives.py:77-203), one SQP iteration as six
+// launches:
+//   wb_lin_kernel    a warp per (instance, stage, column): the dynamics step
+//                    in float64 at X_t, U_t (the defects' f) and central
+//                    differences of it over one state or control entry
+//                    (a column of A_t or B_t);
+//   wb_quad_kernel   a warp per (instance, stage): defects, stage cost,
+//                    gradient, Gauss-Newton blocks (float64, written float32);
+//   wb_riccati_kernel  a 256-thread block per instance: the float32 Riccati
+//                    sweep over the dense n = 61 stage blocks, forward sweep
+//                    and costates (the block products and eliminations of
+//                    lqr_eq_kernel.cuh, without equality rows);
+//   wb_merit_kernel  a block per instance: directional derivative, penalty
+//                    update, merit at the current iterate;
+//   wb_trial_kernel  a warp per (instance, trial step, stage): the merit's
+//                    stage terms at X + a_k dX for every trial a_k = beta^k at
+//                    once (dynamics step, cost, defect);
+//   wb_accept_kernel a block per instance: the first trial that passes the
+//                    Armijo test (the same choice as trying them in order),
+//                    then the update.
+// The model's float64 arithmetic keeps the central differences accurate to
+// ~1e-9; the Riccati runs in float32 like every other solve here.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "../../include/mpxg.h"
+#include "internal.h"
+#include "lqr_eq_kernel.cuh"
+#include "wb_kernel.cuh"
+
+using namespace mpxg;
+
+namespace {
+
+// quadruped capacity: 16 bodies, 20 dofs, 4 contacts; two warps per block
+// (the float64 per-warp state is ~15 KB)
+using WbCap = wb::Cap<16, 20, 4, 2, 1>;
+constexpr int kNW = WbCap::NW;
+constexpr int kNX = 61, kNU = 12;   // the built Riccati size (nv = 18, 4 contacts)
+constexpr int kMaxX = 64, kMaxU = 16, kMaxRef = 64, kMaxW = 80, kMaxC = 4, kMaxTrials = 8;
+
+struct WbDims {
+  int nq, nv, nj, nc, nr, nx, nz, nR, ncol;
+};
+
+WbDims wb_dims(const mpxg_wb_model& m) {
+  WbDims d{};
+  d.nv = m.nv;
+  d.nq = m.nq;
+  d.nj = m.nv - 6;
+  d.nc = m.n_contact;
+  d.nr = 3 * d.nc;
+  d.nx = d.nq + d.nv + 2 * d.nr;
+  d.nz = d.nq + d.nv;
+  d.nR = 12 + 3 * d.nj + 6 * d.nc;
+  d.ncol = 13 + d.nj + 7 * d.nc;
+  return d;
+}
+
+// Device view of one mpxg_wb_sqp call: the caller's arrays and the workspace.
+struct WbSqp {
+  int B, N, KT, first;
+  WbDims d;
+  double dt, alpha, beta, eta, skip_tol, rho0;
+  float reg;
+  int swing;
+  const float *x0, *ref, *W;
+  const int* contact;
+  float *X, *U, *V;
+  double *fnom, *cd, *sums, *ls, *trial;
+  float *A, *Bm, *c, *x0s, *Q, *R, *M, *q, *r, *K, *k, *dX, *dU, *lam, *Pscr;
+  unsigned* kbits;
+  int* status;
+  float* kkt;
+};
+
+// ---------------------------------------------------------------- cost
+// The relaxed barrier of objectives.py:7-13 and its derivatives where it is
+// smooth (the clipped ranges have zero derivative).
+__device__ __forceinline__ double pen_raw(double c, double a, double s) {
+  const double logb = -a * log(fmin(fmax(c, 1e-10), 1e6));
+  const double t = (c - 2.0 * s) / s;
+  return c > s ? logb : a / 2.0 * (t * t - 1.0) + logb;
+}
+__device__ __forceinline__ double pen(double c, double a, double s) { return fmin(fmax(pen_raw(c, a, s), 0.0), 1e8); }
+__device__ __forceinline__ double pen_d(double c, double a, double s) {
+  const double logd = (c > 1e-10 && c < 1e6) ? -a / c : 0.0;
+  const double d = c > s ? logd : a * (c - 2.0 * s) / (s * s) + logd;
+  const double v = pen(c, a, s);
+  return (v > 0.0 && v < 1e8) ? d : 0.0;
+}
+__device__ __forceinline__ double pen_dd(double c, double a, double s) {
+  const double logdd = (c > 1e-10 && c < 1e6) ? a / (c * c) : 0.0;
+  const double dd = c > s ? logdd : a / (s * s) + logdd;
+  const double raw = pen_raw(c, a, s);
+  return (raw > 0.0 && raw < 1e8) ? fmin(fmax(dd, -1e6), 1e6) : 0.0;
+}
+
+// conj(v) * u as a left-multiplication matrix L(conj v) applied to u
+__device__ __forceinline__ void qconj_mul(const double* v, const double* u, double* o, double L[4][4]) {
+  const double a0 = v[0], a1 = -v[1], a2 = -v[2], a3 = -v[3];
+  const double Lm[4][4] = {{a0, -a1, -a2, -a3}, {a1, a0, -a3, a2}, {a2, a3, a0, -a1}, {a3, -a2, a1, a0}};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    o[i] = Lm[i][0] * u[0] + Lm[i][1] * u[1] + Lm[i][2] * u[2] + Lm[i][3] * u[3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) L[i][k] = Lm[i][k];
+  }
+}
+
+// quat_sub(u, v): the rotation vector of conj(v) u (angle in (-pi, pi]) and,
+// if J, its 3 x 4 Jacobian w.r.t. u (at a zero vector part the limit 2/s I
+// of the smooth map).
+__device__ void quat_sub_d(const double* u, const double* v, double* e, double (*J)[4]) {
+  double q[4], L[4][4];
+  qconj_mul(v, u, q, L);
+  const double s = q[0], n = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  double th = 2.0 * atan2(n, s);
+  if (th > M_PI) th -= 2.0 * M_PI;
+  double a[3] = {0.0, 0.0, 0.0};
+  if (n > 0.0) {
+    a[0] = q[1] / n; a[1] = q[2] / n; a[2] = q[3] / n;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) e[i] = a[i] * th;
+  if (!J) return;
+  double D[3][4];  // d(result)/d(s, w)
+  if (n > 0.0) {
+    const double r2 = s * s + n * n;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      D[i][0] = a[i] * (-2.0 * n / r2);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        D[i][1 + k] = a[i] * a[k] * (2.0 * s / r2) + th * ((i == k ? 1.0 : 0.0) - a[i] * a[k]) / n;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      D[i][0] = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) D[i][1 + k] = i == k ? 2.0 / s : 0.0;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) J[i][k] = D[i][0] * L[0][k] + D[i][1] * L[1][k] + D[i][2] * L[2][k] + D[i][3] * L[3][k];
+}
+
+// Per-warp operands and results of one stage's cost.
+struct CostScr {
+  double x[kMaxX], u[kMaxU], r[kMaxRef], w[kMaxW];
+  double gx[kMaxX], gu[kMaxU], diag[kMaxX], rdiag[kMaxU];
+  double qb[4][4], cb[kMaxC][3][3];
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// One stage of quadruped_wb_obj (objectives.py:77-125; terminal: the t == N
+// branch) at s.x, s.u, s.r, s.w; returns the stage cost on every lane.  With
+// DERIV also its gradient (s.gx, s.gu) and the Gauss-Newton blocks of
+// quadruped_wb_hessian_gn (objectives.py:127-203): the diagonal part of H_xx
+// (s.diag), the quaternion block (s.qb, rows/columns 3..6), the friction-cone
+// blocks (s.cb, the force entries of each contact) and the diagonal H_uu
+// (s.rdiag, without reg); H_xu is zero (no residual row reads both).
+template <bool DERIV>
+__device__ double stage_eval(const WbDims& d, CostScr& s, bool terminal, bool swing, int lane) {
+  const int nj = d.nj, nc = d.nc, nx = d.nx;
+  const int a = 12 + 2 * nj, g0 = 13 + 2 * nj + 3 * nc, rc = 13 + nj + 3 * nc;
+  double acc = 0.0;
+  for (int i = lane; i < nx; i += 32) {
+    double g = 0.0, h = 0.0;
+    if (i < 3) {
+      const double e = s.x[i] - s.r[i], w = s.w[i];
+      acc += w * e * e; g = w * e; h = w;
+    } else if (i < 7) {
+      // the quaternion rows: lane 0 below
+    } else if (i < 13 + nj) {  // q, dp, omega: reference entry i, weight i - 1
+      const double e = s.x[i] - s.r[i], w = s.w[i - 1];
+      acc += w * e * e; g = w * e; h = w;
+    } else if (i < 13 + 2 * nj) {  // dq, its speed limits
+      const double e = s.x[i], w = s.w[i - 1];
+      acc += w * e * e; g = w * e; h = w;
+      if (!terminal) {
+        const double lo = 10.0 + 1e-2 - e, hi = 10.0 + 1e-2 + e;
+        acc += pen(lo, 1.0, 1.0) + pen(hi, 1.0, 1.0);
+        g += 0.5 * (-pen_d(lo, 1.0, 1.0) + pen_d(hi, 1.0, 1.0));
+        h += pen_dd(lo, 0.1, 5.0) + pen_dd(hi, 0.1, 5.0);
+      }
+    } else if (!terminal) {
+      if (i < g0) {  // contact points
+        const int k = i - (13 + 2 * nj);
+        const double cm = swing ? 1.0 : s.r[rc + k / 3];
+        const double e = cm * (s.x[i] - s.r[13 + nj + k]), w = s.w[a + k];
+        acc += w * e * e; g = cm * w * e; h = cm * cm * w;
+      } else {  // contact forces
+        const int k = i - g0;
+        const double e = s.x[i] - s.r[13 + nj + 4 * nc + k], w = s.w[a + 3 * nc + nj + k];
+        acc += w * e * e; g = w * e; h = w;
+      }
+    }
+    if (DERIV) {
+      s.gx[i] = g;
+      s.diag[i] = h;
+    }
+  }
+  if (!terminal) {
+    for (int j = lane; j < nj; j += 32) {  // torques and their limits
+      const double uu = s.u[j], w = s.w[a + 3 * nc + j];
+      const double lo = 44.0 + 1e-2 - uu, hi = 44.0 + 1e-2 + uu;
+      acc += w * uu * uu + pen(lo, 1.0, 1.0) + pen(hi, 1.0, 1.0);
+      if (DERIV) {
+        s.gu[j] = w * uu + 0.5 * (-pen_d(lo, 1.0, 1.0) + pen_d(hi, 1.0, 1.0));
+        s.rdiag[j] = w + pen_dd(lo, 1.0, 1.0) + pen_dd(hi, 1.0, 1.0);
+      }
+    }
+  }
+  if (DERIV) __syncwarp();
+  if (lane == 0) {  // orientation residual quat_sub(quat, quat_ref)
+    double e[3], J[3][4];
+    quat_sub_d(s.x + 3, s.r + 3, e, DERIV ? J : nullptr);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc += s.w[3 + k] * e[k] * e[k];
+    if (DERIV) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        double g = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) g += J[k][c] * s.w[3 + k] * e[k];
+        s.gx[3 + c] = g;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+          double h = 0.0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) h += J[k][c] * s.w[3 + k] * J[k][f];
+          s.qb[c][f] = h;
+        }
+      }
+    }
+  }
+  if (!terminal && lane >= 1 && lane <= nc) {  // friction cone of contact lane - 1
+    const int c = lane - 1;
+    const double on = s.r[rc + c];
+    const double fx = s.x[g0 + 3 * c], fy = s.x[g0 + 3 * c + 1], fz = s.x[g0 + 3 * c + 2];
+    const double sq1 = sqrt(fy * fy + fx * fx + 1e-2);
+    const double cone = 0.5 * fz - sq1;
+    acc += pen(cone, 0.1, 5.0) * on;
+    if (DERIV) {
+      const double dc = 0.5 * pen_d(cone, 0.1, 5.0) * on;
+      s.gx[g0 + 3 * c] += dc * (-fx / sq1);
+      s.gx[g0 + 3 * c + 1] += dc * (-fy / sq1);
+      s.gx[g0 + 3 * c + 2] += dc * 0.5;
+      const double sq2 = sqrt(fy * fy + fx * fx + 1e-1);
+      const double hh = pen_dd(0.5 * fz - sq2, 0.1, 5.0) * on;
+      const double jf[3] = {-fx / sq2, -fy / sq2, 0.5};
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s.cb[c][i][k] = hh * jf[i] * jf[k];
+    }
+  }
+  if (DERIV) __syncwarp();
+  return 0.5 * warp_sum(acc);
+}
+
+// ---------------------------------------------------------------- dynamics
+// Per-warp state of the float64 step.
+struct StepScr {
+  wb::Warp<WbCap, double> w;
+  double xb[kMaxX], ub[kMaxU], f[kMaxX];
+};
+
+// f(x, u) of the step model into s.f (every lane of the warp).
+__device__ __forceinline__ void eval_step(const mpxg_wb_model& m, const WbSqp& p, StepScr& s, const double* x,
+                                          const double* u, const int* contact, int lane) {
+  const int nq = p.d.nq, nv = p.d.nv;
+  for (int i = lane; i < nq; i += 32) s.w.qpos[i] = x[i];
+  if (lane < nv) s.w.qvel[lane] = x[nq + lane];
+  __syncwarp();
+  wb::rb_terms(m, s.w, lane);
+  wb::step(m, s.w, u, contact, p.dt, p.alpha, s.f, lane);
+  __syncwarp();
+}
+
+// A warp per (instance b, stage t < N, column j): j < nz + nj a central
+// difference over state entry j (j < nz) or control j - nz; j = nz + nj the
+// step at (X_t, U_t) itself, into fnom, with the columns of A_t that f does
+// not depend on (points, forces) set to zero.
+__global__ void __launch_bounds__(32 * kNW) wb_lin_kernel(const __grid_constant__ mpxg_wb_model m,
+                                                          const __grid_constant__ WbSqp p) {
+  __shared__ StepScr sw[kNW];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const WbDims& d = p.d;
+  const int ncols = d.nz + d.nj + 1;
+  const long long item = (long long)blockIdx.x * kNW + wid;
+  if (item >= (long long)p.B * p.N * ncols) return;
+  const int b = (int)(item / ((long long)p.N * ncols));
+  const int rem = (int)(item % ((long long)p.N * ncols));
+  const int t = rem / ncols, j = rem % ncols;
+  StepScr& s = sw[wid];
+  const size_t st = (size_t)b * p.N + t;
+  const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * d.nx;
+  const float* Ut = p.U + st * d.nj;
+  for (int i = lane; i < d.nx; i += 32) s.xb[i] = (double)Xt[i];
+  if (lane < d.nj) s.ub[lane] = (double)Ut[lane];
+  const int* ct = p.contact + ((size_t)b * (p.N + 1) + t) * d.nc;
+  __syncwarp();
+  const int nx = d.nx;
+  if (j == d.nz + d.nj) {
+    eval_step(m, p, s, s.xb, s.ub, ct, lane);
+    double* fo = p.fnom + st * nx;
+    for (int i = lane; i < nx; i += 32) fo[i] = s.f[i];
+    float* At = p.A + st * nx * nx;
+    const int nzc = nx - d.nz;
+    for (int e = lane; e < nx * nzc; e += 32) At[(e / nzc) * nx + d.nz + e % nzc] = 0.0f;
+    return;
+  }
+  const bool isx = j < d.nz;
+  const double z = isx ? s.xb[j] : s.ub[j - d.nz];
+  const double h = 1e-6 * fmax(1.0, fabs(z));
+  double fp[2];
+  for (int sgn = 0; sgn < 2; ++sgn) {
+    const double zp = sgn == 0 ? z + h : z - h;
+    __syncwarp();
+    if (lane == 0) {
+      if (isx) s.xb[j] = zp;
+      else s.ub[j - d.nz] = zp;
+    }
+    __syncwarp();
+    eval_step(m, p, s, s.xb, s.ub, ct, lane);
+    if (sgn == 0) {
+      fp[0] = lane < nx ? s.f[lane] : 0.0;
+      fp[1] = lane + 32 < nx ? s.f[lane + 32] : 0.0;
+    }
+  }
+  const double inv = 1.0 / (2.0 * h);
+  for (int q = 0; q < 2; ++q) {
+    const int i = lane + 32 * q;
+    if (i >= nx) break;
+    const float v = (float)((fp[q] - s.f[i]) * inv);
+    if (isx) p.A[st * nx * nx + (size_t)i * nx + j] = v;
+    else p.Bm[st * nx * d.nj + (size_t)i * d.nj + (j - d.nz)] = v;
+  }
+}
+
+__device__ __forceinline__ void load_stage(const WbSqp& p, CostScr& s, int b, int t, int lane) {
+  const WbDims& d = p.d;
+  const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * d.nx;
+  for (int i = lane; i < d.nx; i += 32) s.x[i] = (double)Xt[i];
+  for (int j = lane; j < d.nj; j += 32) s.u[j] = t < p.N ? (double)p.U[((size_t)b * p.N + t) * d.nj + j] : 0.0;
+  const float* rt = p.ref + ((size_t)b * (p.N + 1) + t) * d.ncol;
+  for (int i = lane; i < d.ncol; i += 32) s.r[i] = (double)rt[i];
+  for (int i = lane; i < d.nR; i += 32) s.w[i] = (double)p.W[(size_t)b * d.nR + i];
+}
+
+// A warp per (instance b, stage t <= N): defect c_t (float64 in cd, float32
+// as the step problem's c / x0), the merit's stage terms (cost, V.c, c.c),
+// and the stage's LQ data: q_t, r_t, dense Q_t, R_t (+ reg), M_t = 0.
+__global__ void __launch_bounds__(128) wb_quad_kernel(const __grid_constant__ WbSqp p) {
+  __shared__ CostScr sw[4];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long item = (long long)blockIdx.x * 4 + wid;
+  if (item >= (long long)p.B * (p.N + 1)) return;
+  const int b = (int)(item / (p.N + 1)), t = (int)(item % (p.N + 1));
+  const WbDims& d = p.d;
+  const int nx = d.nx, nj = d.nj;
+  CostScr& s = sw[wid];
+  load_stage(p, s, b, t, lane);
+  __syncwarp();
+  const bool term = t == p.N;
+  const double cost = stage_eval<true>(d, s, term, p.swing != 0, lane);
+  // defect
+  const size_t s1 = (size_t)b * (p.N + 1) + t;
+  const float* Vt = p.V + s1 * nx;
+  double cv = 0.0, cc = 0.0;
+  for (int i = lane; i < nx; i += 32) {
+    const double ci = t == 0 ? (double)p.x0[(size_t)b * nx + i] - s.x[i]
+                             : p.fnom[((size_t)b * p.N + t - 1) * nx + i] - s.x[i];
+    p.cd[s1 * nx + i] = ci;
+    if (t == 0) p.x0s[(size_t)b * nx + i] = (float)ci;
+    else p.c[((size_t)b * p.N + t - 1) * nx + i] = (float)ci;
+    cv += (double)Vt[i] * ci;
+    cc += ci * ci;
+  }
+  cv = warp_sum(cv);
+  cc = warp_sum(cc);
+  if (lane == 0) {
+    p.sums[s1 * 4 + 0] = cost;
+    p.sums[s1 * 4 + 1] = cv;
+    p.sums[s1 * 4 + 2] = cc;
+  }
+  // gradient
+  for (int i = lane; i < nx; i += 32) p.q[s1 * nx + i] = (float)s.gx[i];
+  // dense Q_t: the diagonal, the quaternion block, the cone blocks
+  const int g0 = 13 + 2 * nj + 3 * d.nc;
+  float* Qt = p.Q + s1 * nx * nx;
+  for (int e = lane; e < nx * nx; e += 32) {
+    const int i = e / nx, k = e % nx;
+    double v = i == k ? s.diag[i] : 0.0;
+    if (i >= 3 && i < 7 && k >= 3 && k < 7) v = s.qb[i - 3][k - 3];
+    if (!term && i >= g0 && k >= g0 && (i - g0) / 3 == (k - g0) / 3) v += s.cb[(i - g0) / 3][(i - g0) % 3][(k - g0) % 3];
+    Qt[e] = (float)v;
+  }
+  if (term) return;
+  const size_t sn = (size_t)b * p.N + t;
+  for (int j = lane; j < nj; j += 32) p.r[sn * nj + j] = (float)s.gu[j];
+  float* Rt = p.R + sn * nj * nj;
+  for (int e = lane; e < nj * nj; e += 32) {
+    const int i = e / nj, k = e % nj;
+    Rt[e] = i == k ? (float)(s.rdiag[i] + (double)p.reg) : 0.0f;
+  }
+  float* Mt = p.M + sn * nx * nj;
+  for (int e = lane; e < nx * nj; e += 32) Mt[e] = 0.0f;
+}
+
+// ---------------------------------------------------------------- Riccati
+// Shared-memory layout of the Riccati block (floats): the stage matrices
+// column-major with odd leading dimensions, as lqr_eq_kernel's.
+template <int NX, int NU>
+struct RLay {
+  static constexpr int LX = NX + (NX % 2 == 0 ? 1 : 2), LU = NU + (NU % 2 == 0 ? 1 : 2);
+  static constexpr int P = 0, A = P + NX * LX, PA = A + NX * LX, Q = PA + NX * LX, B = Q + NX * LX, PB = B + NU * LX,
+                       M = PB + NU * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, ZG = QUX + NX * LU,
+                       PAN = (ZG + (NX + 1) * LU + 3) / 4 * 4, V = PAN + 2 * lqeq::kGjBlock * 32;
+  static constexpr int VL = NX + 4;
+  static constexpr int vc = V, vq = vc + VL, vr = vq + VL, vw = vr + VL, vp = vw + VL, vqx = vp + VL, vqu = vqx + VL,
+                       vk = vqu + VL, vx = vk + VL, vu = vx + VL, FLOATS = vu + VL;
+};
+
+// Riccati sweep of the step problem x_{t+1} = A x + B u + c (x_0 = c_0),
+// cost 1/2 x'Qx + 1/2 u'Ru + q'x + r'u (M = 0 is read but adds nothing):
+//   Q_xx = Q + A'PA, Q_ux = M' + B'PA, Q_uu = R + B'PB, q_x = q + A'(Pc + p),
+//   q_u = r + B'(Pc + p), [Z | g] = Q_uu^-1 [Q_ux | q_u], K = -Z, k = -g,
+//   P <- Q_xx - Q_ux'Z (symmetrised), p <- q_x + Q_ux'k;
+// then dX, dU by the forward sweep and lam_t = P_t dX_t + p_t.
+template <int NX, int NU>
+__global__ void __launch_bounds__(lqeq::kThreads, 1) wb_riccati_kernel(mpxg_lq_eq_io io, float* Pscr) {
+  using namespace lqeq;
+  typedef RLay<NX, NU> L;
+  constexpr int LX = L::LX, LU = L::LU;
+  extern __shared__ float4 smem4[];
+  float* s = reinterpret_cast<float*>(smem4);
+  float *P = s + L::P, *sA = s + L::A, *PA = s + L::PA, *sQ = s + L::Q, *sB = s + L::B, *PB = s + L::PB;
+  float *sM = s + L::M, *Quu = s + L::QUU, *Qux = s + L::QUX, *ZG = s + L::ZG, *pan = s + L::PAN;
+  float *vc = s + L::vc, *vq = s + L::vq, *vr = s + L::vr, *vw = s + L::vw, *vp = s + L::vp;
+  float *vqx = s + L::vqx, *vqu = s + L::vqu, *vk = s + L::vk, *vx = s + L::vx, *vu = s + L::vu;
+  const int b = blockIdx.x, N = io.N, tid = threadIdx.x;
+  constexpr int NP = NX + 1;
+  float* Ps = Pscr + (size_t)b * (N + 1) * NP * NX;
+  const size_t sn = (size_t)b * N, sn1 = (size_t)b * (N + 1);
+
+  load_cm<NX, NX>(P, LX, io.Q + (sn1 + N) * NX * NX);
+  load_vec<NX>(vp, io.q + (sn1 + N) * NX);
+  __syncthreads();
+  for (int e = tid; e < NX * NX; e += kThreads) Ps[(size_t)N * NP * NX + e] = P[(e / NX) * LX + e % NX];
+  for (int i = tid; i < NX; i += kThreads) Ps[(size_t)N * NP * NX + NX * NX + i] = vp[i];
+
+  for (int t = N - 1; t >= 0; --t) {
+    load_cm<NX, NX>(sA, LX, io.A + (sn + t) * NX * NX);
+    load_cm<NX, NU>(sB, LX, io.Bm + (sn + t) * NX * NU);
+    load_cm<NX, NX>(sQ, LX, io.Q + (sn1 + t) * NX * NX);
+    load_cm<NX, NU>(sM, LX, io.M + (sn + t) * NX * NU);
+    load_cm<NU, NU>(Quu, LU, io.R + (sn + t) * NU * NU);
+    load_vec<NX>(vc, io.c + (sn + t) * NX);
+    load_vec<NX>(vq, io.q + (sn1 + t) * NX);
+    load_vec<NU>(vr, io.r + (sn + t) * NU);
+    __syncthreads();
+    bmm<NX, NX, NX, false, false, false>(PA, LX, P, LX, sA, LX, 1.0f, nullptr, 0);
+    bmm<NX, NX, NU, false, false, false>(PB, LX, P, LX, sB, LX, 1.0f, nullptr, 0);
+    bmv<NX, NX, false>(vw, P, LX, vc, 1.0f, vp);
+    bmm<NX, NX, NX, true, false, false>(sQ, LX, sA, LX, PA, LX, 1.0f, sQ, LX);    // Q_xx
+    bmm<NU, NX, NX, true, false, true>(Qux, LU, sB, LX, PA, LX, 1.0f, sM, LX);    // Q_ux
+    bmm<NU, NX, NU, true, false, false>(Quu, LU, sB, LX, PB, LX, 1.0f, Quu, LU);  // Q_uu
+    bmv<NX, NX, true>(vqx, sA, LX, vw, 1.0f, vq);                                 // q_x
+    bmv<NU, NX, true>(vqu, sB, LX, vw, 1.0f, vr);                                 // q_u
+    gj_solve<NU, NU + NX + 1, kGjBlock>(pan, [&](int j, float* v) {
+#pragma unroll
+      for (int i = 0; i < NU; ++i)
+        v[i] = j < NU ? Quu[j * LU + i] : (j < NU + NX ? Qux[(j - NU) * LU + i] : vqu[i]);
+    }, [&](int j, const float* v) {
+#pragma unroll
+      for (int i = 0; i < NU; ++i) ZG[(j - NU) * LU + i] = v[i];
+    });
+    {
+      float* Ko = io.K + (sn + t) * NU * NX;
+      float* ko = io.k + (sn + t) * NU;
+      for (int e = tid; e < NU * NX; e += kThreads) Ko[e] = -ZG[(e % NX) * LU + e / NX];
+      for (int a = tid; a < NU; a += kThreads) {
+        vk[a] = -ZG[NX * LU + a];
+        ko[a] = -ZG[NX * LU + a];
+      }
+    }
+    __syncthreads();
+    bmm<NX, NU, NX, true, false, false>(P, LX, Qux, LU, ZG, LU, -1.0f, sQ, LX);
+    bmv<NX, NU, true>(vp, Qux, LU, vk, 1.0f, vqx);
+    for (int e = tid; e < NX * NX; e += kThreads) {
+      const int c = e / NX, r = e % NX;
+      PA[c * LX + r] = 0.5f * (P[c * LX + r] + P[r * LX + c]);
+    }
+    __syncthreads();
+    float* Pt = Ps + (size_t)t * NP * NX;
+    for (int e = tid; e < NX * NX; e += kThreads) {
+      const int c = e / NX, r = e % NX;
+      const float v = PA[c * LX + r];
+      P[c * LX + r] = v;
+      Pt[e] = v;
+    }
+    for (int i = tid; i < NX; i += kThreads) Pt[NX * NX + i] = vp[i];
+    __syncthreads();
+  }
+  static_assert(2 * FwdLay<NX, NU>::STG <= L::V, "forward staging must fit below the vectors");
+  forward_sweep<NX, NU>(io, b, s, s + FwdLay<NX, NU>::STG, vx, vu, vq);
+  __syncthreads();
+  costates<NX, 0>(io, b, Ps, s);
+}
+
+// ---------------------------------------------------------------- merit
+constexpr int kBlk = 256;
+
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBlk / 32; ++w) t += red[w];
+  return t;  // thread 0 only
+}
+
+// ls[b] = (rho, dphi, phi0, skip): G = g.(dX, dU) + (lam - 2V).c,
+// rho <- min(max(rho, 2G / |c|^2), 1e12) when both are positive,
+// dphi = G - rho |c|^2, phi0 = cost + V.c + rho/2 |c|^2.
+__global__ void __launch_bounds__(kBlk) wb_merit_kernel(const __grid_constant__ WbSqp p) {
+  __shared__ double red[kBlk / 32];
+  const int b = blockIdx.x;
+  const WbDims& d = p.d;
+  const size_t nX = (size_t)(p.N + 1) * d.nx, nU = (size_t)p.N * d.nj;
+  const size_t oX = (size_t)b * nX, oU = (size_t)b * nU;
+  double gd = 0.0, lc = 0.0;
+  for (size_t e = threadIdx.x; e < nX; e += kBlk) {
+    gd += (double)p.q[oX + e] * (double)p.dX[oX + e];
+    lc += ((double)p.lam[oX + e] - 2.0 * (double)p.V[oX + e]) * p.cd[oX + e];
+  }
+  for (size_t e = threadIdx.x; e < nU; e += kBlk) gd += (double)p.r[oU + e] * (double)p.dU[oU + e];
+  const double G = block_sum(gd, red) + block_sum(lc, red);
+  if (threadIdx.x != 0) return;
+  double Jc = 0.0, vc = 0.0, cs = 0.0;
+  for (int t = 0; t <= p.N; ++t) {
+    const double* st = p.sums + ((size_t)b * (p.N + 1) + t) * 4;
+    Jc += st[0];
+    vc += st[1];
+    cs += st[2];
+  }
+  double rho = p.first ? p.rho0 : p.ls[b * 8 + 0];
+  if (cs > 0.0 && G > 0.0) rho = fmin(fmax(rho, 2.0 * G / cs), 1e12);
+  const double dphi = G - rho * cs, phi0 = Jc + vc + 0.5 * rho * cs;
+  double* ls = p.ls + b * 8;
+  ls[0] = rho;
+  ls[1] = dphi;
+  ls[2] = phi0;
+  ls[3] = (dphi < -p.skip_tol * (1.0 + fabs(phi0))) ? 0.0 : 1.0;
+  if (p.first && p.status) p.status[b] = 0;
+}
+
+// A warp per (instance b, trial k, stage t <= N): the merit's stage terms at
+// a_k = beta^k: cost_t(X_t + a dX_t, U_t + a dU_t) + V_t(a).c_t(a) +
+// rho/2 |c_t(a)|^2, c_0(a) = x0 - X_0(a), c_t(a) = f(X_{t-1}(a), U_{t-1}(a)) -
+// X_t(a).  Nothing when the iteration takes the full step untested.
+__global__ void __launch_bounds__(32 * kNW) wb_trial_kernel(const __grid_constant__ mpxg_wb_model m,
+                                                            const __grid_constant__ WbSqp p) {
+  __shared__ StepScr sws[kNW];
+  __shared__ CostScr swc[kNW];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long item = (long long)blockIdx.x * kNW + wid;
+  const int N1 = p.N + 1;
+  if (item >= (long long)p.B * p.KT * N1) return;
+  const int b = (int)(item / ((long long)p.KT * N1));
+  const int rem = (int)(item % ((long long)p.KT * N1));
+  const int k = rem / N1, t = rem % N1;
+  const double* ls = p.ls + b * 8;
+  if (ls[3] != 0.0) return;
+  double al = 1.0;
+  for (int i = 0; i < k; ++i) al *= p.beta;
+  const WbDims& d = p.d;
+  const int nx = d.nx, nj = d.nj;
+  StepScr& ss = sws[wid];
+  CostScr& s = swc[wid];
+  const size_t oX = (size_t)b * N1 * nx, oU = (size_t)b * p.N * nj;
+  load_stage(p, s, b, t, lane);
+  __syncwarp();
+  for (int i = lane; i < nx; i += 32) s.x[i] += al * (double)p.dX[oX + (size_t)t * nx + i];
+  if (t < p.N)
+    for (int j = lane; j < nj; j += 32) s.u[j] += al * (double)p.dU[oU + (size_t)t * nj + j];
+  __syncwarp();
+  const double cost = stage_eval<false>(d, s, t == p.N, p.swing != 0, lane);
+  if (t > 0) {
+    const int tp = t - 1;
+    for (int i = lane; i < nx; i += 32)
+      ss.xb[i] = (double)p.X[oX + (size_t)tp * nx + i] + al * (double)p.dX[oX + (size_t)tp * nx + i];
+    for (int j = lane; j < nj; j += 32)
+      ss.ub[j] = (double)p.U[oU + (size_t)tp * nj + j] + al * (double)p.dU[oU + (size_t)tp * nj + j];
+    __syncwarp();
+    eval_step(m, p, ss, ss.xb, ss.ub, p.contact + ((size_t)b * N1 + tp) * d.nc, lane);
+  }
+  double vcs = 0.0, ccs = 0.0;
+  for (int i = lane; i < nx; i += 32) {
+    const double ci = (t == 0 ? (double)p.x0[(size_t)b * nx + i] : ss.f[i]) - s.x[i];
+    const double v = (double)p.V[oX + (size_t)t * nx + i], l = (double)p.lam[oX + (size_t)t * nx + i];
+    vcs += (v + al * (l - v)) * ci;
+    ccs += ci * ci;
+  }
+  vcs = warp_sum(vcs);
+  ccs = warp_sum(ccs);
+  if (lane == 0) p.trial[((size_t)b * p.KT + k) * N1 + t] = cost + vcs + 0.5 * ls[0] * ccs;
+}
+
+// A block per instance: a = 1 when the iteration skips the search, else the
+// first a_k with phi(a_k) - phi0 <= eta a_k dphi (the last trial's step and
+// MPXG_INST_LS_FAIL when none passes); then X += a dX, U += a dU,
+// V += a (lam - V), MPXG_INST_NAN on a non-finite result.
+__global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__ WbSqp p) {
+  __shared__ double s_al;
+  __shared__ int s_bad;
+  const int b = blockIdx.x, N1 = p.N + 1;
+  const double* ls = p.ls + b * 8;
+  if (threadIdx.x == 0) {
+    double al = 1.0;
+    int fail = 0;
+    if (ls[3] == 0.0) {
+      bool ok = false;
+      double a = 1.0;
+      for (int k = 0; k < p.KT; ++k) {
+        double phi = 0.0;
+        const double* tr = p.trial + ((size_t)b * p.KT + k) * N1;
+        for (int t = 0; t < N1; ++t) phi += tr[t];
+        if (phi - ls[2] <= p.eta * a * ls[1]) {
+          ok = true;
+          break;
+        }
+        if (k + 1 < p.KT) a *= p.beta;
+      }
+      al = a;
+      fail = ok ? 0 : MPXG_INST_LS_FAIL;
+    }
+    s_al = al;
+    s_bad = fail;
+  }
+  __syncthreads();
+  const double al = s_al;
+  const WbDims& d = p.d;
+  const size_t nX = (size_t)N1 * d.nx, nU = (size_t)p.N * d.nj;
+  const size_t oX = (size_t)b * nX, oU = (size_t)b * nU;
+  int bad = 0;
+  for (size_t e = threadIdx.x; e < nX; e += kBlk) {
+    const float x = (float)((double)p.X[oX + e] + al * (double)p.dX[oX + e]);
+    const double v0 = (double)p.V[oX + e];
+    const float v = (float)(v0 + al * ((double)p.lam[oX + e] - v0));
+    p.X[oX + e] = x;
+    p.V[oX + e] = v;
+    if (!isfinite(x) || !isfinite(v)) bad = 1;
+  }
+  for (size_t e = threadIdx.x; e < nU; e += kBlk) {
+    const float u = (float)((double)p.U[oU + e] + al * (double)p.dU[oU + e]);
+    p.U[oU + e] = u;
+    if (!isfinite(u)) bad = 1;
+  }
+  if (bad) atomicOr(&s_bad, MPXG_INST_NAN);
+  __syncthreads();
+  if (threadIdx.x == 0 && p.status) p.status[b] |= s_bad;
+}
+
+// ---------------------------------------------------------------- KKT
+// A warp per (instance b, stage t <= N), after wb_lin / wb_quad at the
+// result: primal max |c_t|; dual |q_t + A_t'V_{t+1} - V_t| (1 <= t < N),
+// |q_N - V_N|, |r_t + B_t'V_{t+1}|; max |gradient|; maxima by atomicMax on
+// the float bits (non-negative floats order as their bits).
+__global__ void __launch_bounds__(128) wb_kkt_kernel(const __grid_constant__ WbSqp p) {
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long item = (long long)blockIdx.x * 4 + wid;
+  const int N1 = p.N + 1;
+  if (item >= (long long)p.B * N1) return;
+  const int b = (int)(item / N1), t = (int)(item % N1);
+  const WbDims& d = p.d;
+  const int nx = d.nx, nj = d.nj;
+  const size_t s1 = (size_t)b * N1 + t;
+  double rp = 0.0, rd = 0.0, gm = 0.0;
+  for (int i = lane; i < nx; i += 32) {
+    rp = fmax(rp, fabs(p.cd[s1 * nx + i]));
+    gm = fmax(gm, fabs((double)p.q[s1 * nx + i]));
+  }
+  const float* Vt = p.V + s1 * nx;
+  if (t == p.N) {
+    for (int i = lane; i < nx; i += 32) rd = fmax(rd, fabs((double)p.q[s1 * nx + i] - (double)Vt[i]));
+  } else {
+    const size_t sn = (size_t)b * p.N + t;
+    const float* Vn = Vt + nx;
+    const float* At = p.A + sn * nx * nx;
+    const float* Bt = p.Bm + sn * nx * nj;
+    if (t >= 1) {
+      for (int j = lane; j < nx; j += 32) {
+        double a = 0.0;
+        for (int i = 0; i < nx; ++i) a += (double)At[(size_t)i * nx + j] * (double)Vn[i];
+        rd = fmax(rd, fabs((double)p.q[s1 * nx + j] + a - (double)Vt[j]));
+      }
+    }
+    for (int j = lane; j < nj; j += 32) {
+      double a = 0.0;
+      for (int i = 0; i < nx; ++i) a += (double)Bt[(size_t)i * nj + j] * (double)Vn[i];
+      const double g = (double)p.r[sn * nj + j];
+      gm = fmax(gm, fabs(g));
+      rd = fmax(rd, fabs(g + a));
+    }
+  }
+  rp = warp_max(rp);
+  rd = warp_max(rd);
+  gm = warp_max(gm);
+  if (lane == 0) {
+    unsigned* kb = p.kbits + (size_t)b * 3;
+    atomicMax(kb + 0, __float_as_uint((float)rp));
+    atomicMax(kb + 1, __float_as_uint((float)rd));
+    atomicMax(kb + 2, __float_as_uint((float)gm));
+  }
+}
+
+__global__ void wb_kkt_finish_kernel(int B, unsigned* bits, float* kkt) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const float rp = __uint_as_float(bits[3 * b]), rd = __uint_as_float(bits[3 * b + 1]);
+  const float gm = __uint_as_float(bits[3 * b + 2]);
+  const float dual = rd / (1.0f + gm);
+  kkt[3 * b] = rp;
+  kkt[3 * b + 1] = dual;
+  kkt[3 * b + 2] = fmaxf(rp, dual);
+  bits[3 * b] = bits[3 * b + 1] = bits[3 * b + 2] = 0u;
+}
+
+// ---------------------------------------------------------------- host
+struct WsLayout {
+  size_t fnom, cd, sums, ls, trial, A, Bm, c, x0s, Q, R, M, q, r, K, k, dX, dU, lam, Pscr, kbits, bytes;
+};
+
+WsLayout ws_layout(const WbDims& d, int B, int N) {
+  WsLayout L{};
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += (bytes + 255) & ~size_t(255);
+    return at;
+  };
+  const size_t b = (size_t)B, n = (size_t)N, nx = d.nx, nj = d.nj;
+  L.fnom = take(b * n * nx * 8);
+  L.cd = take(b * (n + 1) * nx * 8);
+  L.sums = take(b * (n + 1) * 4 * 8);
+  L.ls = take(b * 8 * 8);
+  L.trial = take(b * kMaxTrials * (n + 1) * 8);
+  L.A = take(b * n * nx * nx * 4);
+  L.Bm = take(b * n * nx * nj * 4);
+  L.c = take(b * n * nx * 4);
+  L.x0s = take(b * nx * 4);
+  L.Q = take(b * (n + 1) * nx * nx * 4);
+  L.R = take(b * n * nj * nj * 4);
+  L.M = take(b * n * nx * nj * 4);
+  L.q = take(b * (n + 1) * nx * 4);
+  L.r = take(b * n * nj * 4);
+  L.K = take(b * n * nj * nx * 4);
+  L.k = take(b * n * nj * 4);
+  L.dX = take(b * (n + 1) * nx * 4);
+  L.dU = take(b * n * nj * 4);
+  L.lam = take(b * (n + 1) * nx * 4);
+  L.Pscr = take(b * (n + 1) * (nx + 1) * nx * 4);
+  L.kbits = take(b * 3 * 4);
+  L.bytes = o;
+  return L;
+}
+
+const char* wb_sqp_model_problem(const mpxg_wb_model* m) {
+  if (const char* why = wb_model_check(m)) return why;
+  const int nv = m->nv, nr = 3 * m->n_contact;
+  if (m->jnt_type[0] != 1 || m->nq != nv + 1 || m->n_contact < 1 || nr > nv || nv + nr + 1 > 32)
+    return "needs a free root, hinge or slide joints elsewhere, 3 x contacts <= nv and nv + 3 x contacts + 1 <= 32";
+  if (m->nbody > WbCap::MB || nv > WbCap::MD || m->n_contact > kMaxC)
+    return "the whole-body SQP is built for up to 16 bodies, 20 dofs and 4 contacts";
+  const WbDims d = wb_dims(*m);
+  if (d.nx != kNX || d.nj != kNU) return "the whole-body SQP is built for nv = 18 with 4 contacts (nx = 61, nj = 12)";
+  return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t mpxg_wb_sqp_workspace_bytes(const mpxg_wb_model* model, int batch, int N) {
+  if (!model || wb_sqp_model_problem(model) || batch < 0 || N < 1) return 0;
+  return ws_layout(wb_dims(*model), batch, N).bytes;
+}
+
+mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
+  if (!io) return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: null io");
+  if (const char* why = wb_sqp_model_problem(io->model))
+    return lib_fail(MPXG_ERR_INVALID_ARG, std::string("mpxg_wb_sqp: ") + why);
+  if (io->batch < 0 || io->N < 1 || io->iters < 0 || io->ls_max_trials < 1 || io->ls_max_trials > kMaxTrials ||
+      !(io->dt > 0.0f) || !(io->ls_beta > 0.0f && io->ls_beta < 1.0f) || !(io->reg >= 0.0f))
+    return lib_fail(MPXG_ERR_INVALID_ARG,
+                    "mpxg_wb_sqp: needs batch >= 0, N >= 1, iters >= 0, ls_max_trials in 1..8, dt > 0, "
+                    "0 < ls_beta < 1, reg >= 0");
+  if (io->batch == 0) return MPXG_OK;
+  if (!io->x0 || !io->X || !io->U || !io->V || !io->reference || !io->contact || !io->W || !io->workspace)
+    return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: null array");
+  if (((uintptr_t)io->workspace & 255u) != 0)
+    return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: workspace must be 256-byte aligned");
+  const mpxg_wb_model& m = *io->model;
+  const WbDims d = wb_dims(m);
+  const int B = io->batch, N = io->N;
+  const WsLayout L = ws_layout(d, B, N);
+  char* ws = static_cast<char*>(io->workspace);
+  WbSqp p{};
+  p.B = B; p.N = N; p.KT = io->ls_max_trials; p.d = d;
+  p.dt = io->dt; p.alpha = io->alpha; p.beta = io->ls_beta; p.eta = io->ls_eta; p.skip_tol = io->ls_skip_tol;
+  p.rho0 = io->rho0; p.reg = io->reg; p.swing = io->swing_tracking;
+  p.x0 = io->x0; p.ref = io->reference; p.W = io->W; p.contact = io->contact;
+  p.X = io->X; p.U = io->U; p.V = io->V; p.status = io->status; p.kkt = io->kkt;
+  p.fnom = (double*)(ws + L.fnom); p.cd = (double*)(ws + L.cd); p.sums = (double*)(ws + L.sums);
+  p.ls = (double*)(ws + L.ls); p.trial = (double*)(ws + L.trial);
+  p.A = (float*)(ws + L.A); p.Bm = (float*)(ws + L.Bm); p.c = (float*)(ws + L.c); p.x0s = (float*)(ws + L.x0s);
+  p.Q = (float*)(ws + L.Q); p.R = (float*)(ws + L.R); p.M = (float*)(ws + L.M); p.q = (float*)(ws + L.q);
+  p.r = (float*)(ws + L.r); p.K = (float*)(ws + L.K); p.k = (float*)(ws + L.k); p.dX = (float*)(ws + L.dX);
+  p.dU = (float*)(ws + L.dU); p.lam = (float*)(ws + L.lam); p.Pscr = (float*)(ws + L.Pscr);
+  p.kbits = (unsigned*)(ws + L.kbits);
+
+  mpxg_lq_eq_io lq{};
+  lq.batch = B; lq.N = N; lq.n = d.nx; lq.m = d.nj; lq.n_eq = 0;
+  lq.A = p.A; lq.Bm = p.Bm; lq.c = p.c; lq.Q = p.Q; lq.R = p.R; lq.M = p.M; lq.q = p.q; lq.r = p.r;
+  lq.x0 = p.x0s; lq.K = p.K; lq.k = p.k; lq.X = p.dX; lq.U = p.dU; lq.lam = p.lam;
+
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t rsmem = (size_t)RLay<kNX, kNU>::FLOATS * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(wb_riccati_kernel<kNX, kNU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)rsmem);
+  if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: riccati attribute");
+  const long long lin_items = (long long)B * N * (d.nz + d.nj + 1);
+  const long long quad_items = (long long)B * (N + 1);
+  const unsigned lin_blocks = (unsigned)((lin_items + kNW - 1) / kNW);
+  const unsigned quad_blocks = (unsigned)((quad_items + 3) / 4);
+  auto linearise = [&]() -> cudaError_t {
+    wb_lin_kernel<<<lin_blocks, 32 * kNW, 0, st>>>(m, p);
+    wb_quad_kernel<<<quad_blocks, 128, 0, st>>>(p);
+    return cudaGetLastError();
+  };
+  if (io->iters == 0 && p.status) {
+    e = cudaMemsetAsync(p.status, 0, (size_t)B * sizeof(int), st);
+    if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: status");
+  }
+  for (int it = 0; it < io->iters; ++it) {
+    p.first = it == 0;
+    if ((e = linearise()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: linearisation");
+    wb_riccati_kernel<kNX, kNU><<<B, lqeq::kThreads, rsmem, st>>>(lq, p.Pscr);
+    wb_merit_kernel<<<B, kBlk, 0, st>>>(p);
+    const long long tr_items = (long long)B * p.KT * (N + 1);
+    wb_trial_kernel<<<(unsigned)((tr_items + kNW - 1) / kNW), 32 * kNW, 0, st>>>(m, p);
+    wb_accept_kernel<<<B, kBlk, 0, st>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: iteration");
+  }
+  if (io->kkt) {
+    p.first = 0;
+    if ((e = linearise()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: linearisation");
+    e = cudaMemsetAsync(p.kbits, 0, (size_t)B * 3 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: kkt");
+    wb_kkt_kernel<<<quad_blocks, 128, 0, st>>>(p);
+    wb_kkt_finish_kernel<<<(B + 127) / 128, 128, 0, st>>>(B, p.kbits, p.kkt);
+    if ((e = cudaGetLastError()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: kkt");
+  }
+  return MPXG_OK;
+}
+
+}  // extern "C"

@@ -396,3 +396,58 @@ def biped_workload(batch, horizons=(50,), seed=0, v_range=(-0.5, 0.5), random_ph
     wl = Workload(desc, x0, X0, U0, V0, ref, par, W, horizon, leg_time=leg_time, v_ref=v_ref, duty=0.6,
                   step_freq=1.25, height=height)
     return wl
+
+
+def wb_workload(batch, N, q0, feet0, mass, seed=0, dt=0.02, duty=0.65, step_freq=1.35, height=0.33, noise=0.02,
+                v_range=(-0.5, 0.5), step_height=0.06):
+    """Seeded synthetic whole-body MPC instances (aliengo-shaped: 12 joints,
+    4 feet), in the layouts mpxg_wb_sqp takes:
+      x0 [B,61] = [p, quat, q, v, omega, dq, feet (3C), forces (3C)]: a
+        standing pose (q0, height) with N(0, noise) perturbations of the base
+        position, orientation (unit quaternion), joints and velocities;
+      reference [B,N+1,53] rows [p, quat, q, dp, omega, feet, contact, forces]:
+        base moving at v ~ U(v_range) along x at `height`, identity
+        orientation, q0, feet at feet0 (nominal, base frame at the origin)
+        shifted with the base, lifted by step_height along a sine in swing,
+        a trot contact schedule with a random phase, contact forces
+        m g / (feet in contact) on the feet in contact;
+      contact [B,N+1,4] int32 (the same schedule, the dynamics' mask);
+      X0 [B,N+1,61] = tiles of x0, U0 [B,N,12] = 0, V0 [B,N+1,61] = 0."""
+    rng = np.random.default_rng(seed)
+    nj, nc = len(q0), len(feet0) // 3
+    nx = 13 + 2 * nj + 6 * nc
+    q0 = np.asarray(q0, dtype=np.float64)
+    feet0 = np.asarray(feet0, dtype=np.float64).reshape(nc, 3)
+    x0 = np.zeros((batch, nx))
+    x0[:, 0:3] = np.array([0.0, 0.0, height]) + rng.normal(size=(batch, 3)) * noise
+    quat = np.array([1.0, 0.0, 0.0, 0.0]) + rng.normal(size=(batch, 4)) * noise
+    x0[:, 3:7] = quat / np.linalg.norm(quat, axis=1, keepdims=True)
+    x0[:, 7:7 + nj] = q0 + rng.normal(size=(batch, nj)) * noise
+    x0[:, 7 + nj:13 + 2 * nj] = rng.normal(size=(batch, 6 + nj)) * noise
+    x0[:, 13 + 2 * nj:13 + 2 * nj + 3 * nc] = (feet0 + [0.0, 0.0, 0.0]).reshape(-1)
+    v = rng.uniform(v_range[0], v_range[1], size=batch)
+    phase = rng.uniform(0.0, 1.0, size=batch)
+    offs = np.array([0.0, 0.5, 0.5, 0.0])[:nc]
+    t = np.arange(N + 1) * dt
+    ph = (phase[:, None, None] + offs[None, None, :] + step_freq * t[None, :, None]) % 1.0  # [B,N+1,C]
+    contact = (ph < duty).astype(np.int32)
+    ref = np.zeros((batch, N + 1, 13 + nj + 7 * nc))
+    ref[:, :, 0] = x0[:, None, 0] + v[:, None] * t[None, :]
+    ref[:, :, 1] = x0[:, None, 1]
+    ref[:, :, 2] = height
+    ref[:, :, 3] = 1.0
+    ref[:, :, 7:7 + nj] = q0
+    ref[:, :, 7 + nj] = v[:, None]
+    feet = np.broadcast_to(feet0[None, None], (batch, N + 1, nc, 3)).copy()
+    feet[..., 0] += ref[:, :, 0:1] - x0[:, None, 0:1]
+    swing = np.where(contact == 0, np.sin(np.pi * np.clip((ph - duty) / (1.0 - duty), 0.0, 1.0)), 0.0)
+    feet[..., 2] += step_height * swing
+    ref[:, :, 13 + nj:13 + nj + 3 * nc] = feet.reshape(batch, N + 1, 3 * nc)
+    ref[:, :, 13 + nj + 3 * nc:13 + nj + 4 * nc] = contact
+    grf = np.zeros((batch, N + 1, nc, 3))
+    grf[..., 2] = contact * mass * 9.81 / (contact.sum(axis=2, keepdims=True) + 1e-5)
+    ref[:, :, 13 + nj + 4 * nc:] = grf.reshape(batch, N + 1, 3 * nc)
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    x0 = f32(x0)
+    return dict(x0=x0, reference=f32(ref), contact=contact, X0=f32(np.repeat(x0[:, None], N + 1, axis=1)),
+                U0=np.zeros((batch, N, nj), dtype=np.float32), V0=np.zeros((batch, N + 1, nx), dtype=np.float32))

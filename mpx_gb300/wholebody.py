@@ -86,3 +86,66 @@ class WholeBodyModel:
                                        float(alpha), _ptr(x), _ptr(u), _ptr(contact), _ptr(out)), None,
                    "mpxg_wb_step")
         return out
+
+
+class WholeBodySQP:
+    """Batched SQP solve of the whole-body MPC (mpxg_wb_sqp): the solve that
+    mpc_wrapper.py's wrappers call each tick (optimizers.mpc over
+    quadruped_wb_dynamics / quadruped_wb_obj / quadruped_wb_hessian_gn,
+    mpc_wrapper.py:67,150-158,236,346-354).
+
+        sqp = WholeBodySQP(WholeBodyModel.from_mjcf(...), N=25, batch_max=64)
+        out = sqp.solve(x0, X0, U0, V0, reference, contact, W)
+
+    x0 [B,nx], X0 [B,N+1,nx], U0 [B,N,nj], V0 [B,N+1,nx], reference
+    [B,N+1,13+nj+7C], contact [B,N+1,C], W [B,12+3nj+6C] or [12+3nj+6C]
+    (the diagonal of the reference's W) -> dict X, U, V, kkt [B,3], status
+    [B].  The workspace is allocated once, for batch_max instances."""
+
+    def __init__(self, wb, N, batch_max, dt=0.02, alpha=25.0, swing_tracking=True, iters=5, reg=1e-6, rho0=1.0,
+                 ls_beta=0.5, ls_eta=1e-4, ls_skip_tol=1e-7, ls_max_trials=8):
+        self.wb, self.N, self.batch_max, self.iters = wb, int(N), int(batch_max), int(iters)
+        self.nj, self.nc = wb.nv - 6, wb.nc
+        self.nx = wb.nq + wb.nv + 6 * wb.nc
+        self.nR = 12 + 3 * self.nj + 6 * self.nc
+        self.ncol = 13 + self.nj + 7 * self.nc
+        self.dev, self.L = wb.dev, wb.L
+        nbytes = self.L.mpxg_wb_sqp_workspace_bytes(_lib.ctypes.byref(wb.struct), self.batch_max, self.N)
+        if nbytes == 0:
+            raise ValueError("mpxg_wb_sqp does not take this model or size: %s" %
+                             self.L.mpxg_last_error(None).decode())
+        self.workspace = torch.empty(int(nbytes), dtype=torch.uint8, device=self.dev)
+        self.opts = dict(dt=float(dt), alpha=float(alpha), swing_tracking=int(bool(swing_tracking)), reg=float(reg),
+                         rho0=float(rho0), ls_beta=float(ls_beta), ls_eta=float(ls_eta),
+                         ls_skip_tol=float(ls_skip_tol), ls_max_trials=int(ls_max_trials))
+
+    def solve(self, x0, X, U, V, reference, contact, W, iters=None, stream=None, inplace=False, kkt=True):
+        N, nx, nj = self.N, self.nx, self.nj
+        x0 = _dev(x0, self.dev).reshape(-1, nx)
+        B = x0.shape[0]
+        if B > self.batch_max:
+            raise ValueError("batch %d exceeds batch_max %d" % (B, self.batch_max))
+
+        def state(a, shape):
+            t = _dev(a, self.dev)
+            if t.numel() != int(torch.tensor(shape).prod()):
+                raise ValueError("expected %s elements for shape %s, got %s" % (int(torch.tensor(shape).prod()),
+                                                                               shape, tuple(t.shape)))
+            t = t.reshape(shape)
+            return t if inplace else t.clone()
+
+        X, U, V = state(X, (B, N + 1, nx)), state(U, (B, N, nj)), state(V, (B, N + 1, nx))
+        ref = _dev(reference, self.dev).reshape(B, N + 1, self.ncol)
+        cont = _dev(contact, self.dev, torch.int32).reshape(B, N + 1, self.nc)
+        Wd = _dev(W, self.dev)
+        Wd = (Wd.reshape(1, self.nR).expand(B, self.nR) if Wd.numel() == self.nR else Wd.reshape(B, self.nR))
+        Wd = Wd.contiguous()
+        kk = torch.empty(B, 3, device=self.dev) if kkt else None
+        st = torch.empty(B, dtype=torch.int32, device=self.dev)
+        io = _lib.WbSqpIO(model=_lib.ctypes.pointer(self.wb.struct), batch=B, N=N,
+                          iters=self.iters if iters is None else int(iters), **self.opts)
+        for k, t in (("x0", x0), ("X", X), ("U", U), ("V", V), ("reference", ref), ("contact", cont), ("W", Wd),
+                     ("kkt", kk), ("status", st), ("workspace", self.workspace)):
+            setattr(io, k, _ptr(t))
+        _lib.check(self.L.mpxg_wb_sqp(_stream_handle(stream), _lib.ctypes.byref(io)), None, "mpxg_wb_sqp")
+        return dict(X=X, U=U, V=V, kkt=kk, status=st)

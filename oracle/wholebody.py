@@ -293,7 +293,8 @@ def quat_sub(u, v):
 
 def quat_sub_jacobian(u, v):
     """d quat_sub(u, v) / du (3 x 4), from the chain rule through conj(v) * u
-    and the logarithm (theta = 2 atan2(|w|, s), result theta w / |w|)."""
+    and the logarithm (theta = 2 atan2(|w|, s), result theta w / |w|); at a
+    zero vector part w the limit (2 / s) I of d/dw (d/ds = 0)."""
     vc = np.asarray(v, dtype=np.float64) * [1, -1, -1, -1]
     a0, a1, a2, a3 = vc
     L = np.array([[a0, -a1, -a2, -a3], [a1, a0, -a3, a2], [a2, a3, a0, -a1], [a3, -a2, a1, a0]])
@@ -303,6 +304,8 @@ def quat_sub_jacobian(u, v):
     th = 2 * np.arctan2(n, s)
     if th > np.pi:
         th -= 2 * np.pi
+    if n == 0.0:  # the limit of the smooth map at a zero vector part
+        return np.column_stack([np.zeros(3), np.eye(3) * (2.0 / s)]) @ L
     a = w / n
     r2 = s * s + n * n
     d_ds = a * (-2 * n / r2)

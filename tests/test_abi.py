@@ -51,6 +51,7 @@ int main(void) {
   printf("%zu %zu\n", sizeof(mpxg_lq_eq_io), sizeof(mpxg_vjp_io));
   printf("%zu %zu %zu\n", sizeof(mpxg_wb_model), offsetof(mpxg_wb_model, gravity),
          offsetof(mpxg_wb_model, contact_point_pos));
+  printf("%zu %zu\n", sizeof(mpxg_wb_sqp_io), offsetof(mpxg_wb_sqp_io, x0));
   return 0;
 }
 '''
@@ -64,7 +65,7 @@ int main(void) {
                      ctypes.sizeof(_lib.LqIO), ctypes.sizeof(_lib.XlaOpaque), ctypes.sizeof(_lib.ServedModel),
                      ctypes.sizeof(_lib.ServerDesc), ctypes.sizeof(_lib.Result), ctypes.sizeof(_lib.LqEqIO),
                      ctypes.sizeof(_lib.VjpIO), ctypes.sizeof(_lib.WbModel), _lib.WbModel.gravity.offset,
-                     _lib.WbModel.contact_point_pos.offset]
+                     _lib.WbModel.contact_point_pos.offset, ctypes.sizeof(_lib.WbSqpIO), _lib.WbSqpIO.x0.offset]
 
 
 def test_xla_target_rejects_a_malformed_opaque():
@@ -152,6 +153,41 @@ def test_wb_step_rejects_what_it_cannot_hold():
     assert b"<= 32" in L.mpxg_last_error(None)
     S = model.to_struct()
     assert L.mpxg_wb_step(None, ctypes.byref(S), 0, 0.02, 25.0, None, None, None, None) == 0
+
+
+def test_wb_sqp_rejects_before_any_launch():
+    """mpxg_wb_sqp checks the model (the built size nv = 18 with 4 contacts,
+    the step's lane limits), the sizes and the options before it launches;
+    a batch of 0 returns at once."""
+    from mpx_gb300 import _lib, mjcf
+    L = _lib.load()
+    model = mjcf.load_npz(os.path.join(ROOT, "tests", "golden", "aliengo_wb.npz"))
+    S = model.to_struct()
+    fake = 1 << 20  # never dereferenced: the checks fail first
+
+    def io(**kw):
+        o = _lib.WbSqpIO(model=ctypes.pointer(S), batch=0, N=25, iters=5, dt=0.02, alpha=25.0, swing_tracking=1,
+                         reg=1e-6, rho0=1.0, ls_beta=0.5, ls_eta=1e-4, ls_skip_tol=1e-7, ls_max_trials=8)
+        for k in ("x0", "X", "U", "V", "reference", "contact", "W", "workspace"):
+            setattr(o, k, fake)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    assert L.mpxg_wb_sqp(None, ctypes.byref(io())) == 0
+    assert L.mpxg_wb_sqp(None, ctypes.byref(io(ls_max_trials=9))) == 1
+    assert b"ls_max_trials" in L.mpxg_last_error(None)
+    assert L.mpxg_wb_sqp(None, ctypes.byref(io(N=0))) == 1
+    assert L.mpxg_wb_sqp(None, ctypes.byref(io(batch=2, workspace=fake + 16))) == 1
+    assert b"256-byte" in L.mpxg_last_error(None)
+    assert L.mpxg_wb_sqp(None, ctypes.byref(io(batch=2, W=None))) == 1
+    assert b"null" in L.mpxg_last_error(None)
+    assert L.mpxg_wb_sqp_workspace_bytes(ctypes.byref(S), 4, 25) > 4 * 25 * 61 * 61 * 4
+    S2 = model.to_struct()
+    S2.n_contact = 3
+    assert L.mpxg_wb_sqp(None, ctypes.byref(io(model=ctypes.pointer(S2)))) == 1
+    assert b"nv = 18" in L.mpxg_last_error(None)
+    assert L.mpxg_wb_sqp_workspace_bytes(ctypes.byref(S2), 4, 25) == 0
 
 
 def _declarations():
