@@ -1297,7 +1297,7 @@ def run_wb_sqp(args, rank, world, local_rank, emit=True):
         "metric": "whole-body MPC solves/s (aliengo, 61 states, N = 25, 5 SQP iterations)",
         "value": world * Bb / (ms / 1000.0), "unit": "solves/s", "n_gpus": world, "steps": steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 (Riccati) / fp64 (model, differences, merit)",
+        "vs_baseline": None, "dtype": "fp32 (derivatives, Riccati) / fp64 (model step, merit)",
         "data": "synthetic (seeded trotting references and perturbed standing states)",
         "config": {"workload": "%d aliengo whole-body MPCs, N = %d, %d SQP iterations per warm tick" % (Bb, N, WBS_ITERS),
                    "parallelism": "replicas"},

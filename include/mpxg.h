@@ -579,8 +579,9 @@ mpxg_status mpxg_wb_step(void* stream, const mpxg_wb_model* model, int batch, fl
  * 6C), u = joint torques (nj = nv - 6).  One iteration at (X, U, V):
  *   defects c_0 = x0 - X_0, c_{t+1} = f(X_t, U_t, contact_t) - X_{t+1}
  *     (f = mpxg_wb_step's model, evaluated in float64);
- *   Jacobians of f by central differences in float64 over qpos, qvel and u
- *     (h_j = 1e-6 max(1, |z_j|); f does not read the point and force states);
+ *   Jacobians of f over qpos, qvel and u by forward-mode differentiation of
+ *     the step in float32 (exact up to rounding; f does not read the point
+ *     and force states);
  *   the cost's exact gradient and the reference's Gauss-Newton blocks
  *     (objectives.py:77-203), reg added to the control block;
  *   the step by a float32 Riccati sweep (one 256-thread block per instance);

@@ -38,8 +38,9 @@ struct Cap {
 using CapAny = Cap<MPXG_WB_MAX_BODY, MPXG_WB_MAX_DOF, MPXG_WB_MAX_CONTACT, 2, 1>;
 using CapQuad = Cap<16, 20, 4, 3, 9>;
 
-// The kernels are generic over the scalar T: float for every entry point,
-// double for the whole-body SQP's central-difference Jacobians (wb_sqp.cu).
+// The kernels are generic over the scalar T: float for every entry point;
+// the whole-body SQP (wb_sqp.cu) also runs the step in double (defects and
+// merit) and on a forward-mode dual number (its Jacobians).
 template <class T>
 struct ArgsT {
   const T *qpos, *qvel, *grf, *foot_ref, *foot_ref_dot, *Kp, *Kd, *u;
@@ -254,11 +255,19 @@ __device__ __forceinline__ void step(const mpxg_wb_model& m, Warp<C, T>& s, cons
   if (lane < 3) xo[lane] = s.qpos[lane] + s.bias[lane] * dt;
   if (lane == 3) {  // quat * exp(w dt / 2), w in the body frame, renormalised
     const T w0 = s.bias[3], w1 = s.bias[4], w2 = s.bias[5];
-    const T n = sqrt_t(w0 * w0 + w1 * w1 + w2 * w2);
-    const T inv = n > T(0.0) ? T(1.0) / n : T(0.0);
-    T sh, ch;
-    sincos_t(T(0.5) * n * dt, &sh, &ch);
-    const T qr[4] = {ch, w0 * inv * sh, w1 * inv * sh, w2 * inv * sh};
+    const T n2 = w0 * w0 + w1 * w1 + w2 * w2;
+    const T h = T(0.5) * dt;
+    T ch, k;  // cos(h |w|) and sin(h |w|) / |w|
+    if (n2 > T(1e-12)) {
+      const T n = sqrt_t(n2);
+      T sh;
+      sincos_t(h * n, &sh, &ch);
+      k = sh / n;
+    } else {  // the series at a vanishing rate (smooth through |w| = 0)
+      ch = T(1.0) - T(0.5) * h * h * n2;
+      k = h * (T(1.0) - h * h * n2 / T(6.0));
+    }
+    const T qr[4] = {ch, w0 * k, w1 * k, w2 * k};
     T qn[4];
     quat_mul(s.qpos + 3, qr, qn);
     quat_normalize(qn);

@@ -2,10 +2,12 @@
 // wrappers (quadruped_wb_dynamics, models.py:39-117; quadruped_wb_obj and
 // quadruped_wb_hessian_gn, objectives.py:77-203), one SQP iteration as six
 // launches:
-//   wb_lin_kernel    a warp per (instance, stage, column): the dynamics step
-//                    in float64 at X_t, U_t (the defects' f) and central
-//                    differences of it over one state or control entry
-//                    (a column of A_t or B_t);
+//   wb_nominal_kernel  a warp per (instance, stage): the dynamics step in
+//                    float64 at X_t, U_t (the defects' f);
+//   wb_jac_kernel    a warp per (instance, stage, column): the step on a
+//                    forward-mode dual number seeded on one state or control
+//                    entry, in float32: a column of A_t or B_t, exact up to
+//                    float32 rounding;
 //   wb_quad_kernel   a warp per (instance, stage): defects, stage cost,
 //                    gradient, Gauss-Newton blocks (float64, written float32);
 //   wb_riccati_kernel  a 256-thread block per instance: the float32 Riccati
@@ -20,8 +22,9 @@
 //   wb_accept_kernel a block per instance: the first trial that passes the
 //                    Armijo test (the same choice as trying them in order),
 //                    then the update.
-// The model's float64 arithmetic keeps the central differences accurate to
-// ~1e-9; the Riccati runs in float32 like every other solve here.
+// The defects and the merit take the step in float64 (the merit's changes near
+// convergence are ~1e-7 of its value); the derivatives and the Riccati run in
+// float32 like every other solve here.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -34,6 +37,63 @@
 #include "wb_kernel.cuh"
 
 using namespace mpxg;
+
+namespace mpxg {
+namespace wb {
+
+// A forward-mode dual number with one tangent: (value, derivative) in
+// float32.  The templated rigid-body and step code of wb_kernel.cuh runs on
+// it unchanged; every operation carries the derivative by the chain rule.
+struct D1 {
+  float v, d;
+  D1() = default;
+  __device__ __forceinline__ D1(float a) : v(a), d(0.0f) {}
+  __device__ __forceinline__ D1(double a) : v((float)a), d(0.0f) {}
+  __device__ __forceinline__ D1(int a) : v((float)a), d(0.0f) {}
+  __device__ __forceinline__ D1(float a, float b) : v(a), d(b) {}
+};
+__device__ __forceinline__ D1 operator+(D1 a, D1 b) { return D1(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ D1 operator-(D1 a, D1 b) { return D1(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ D1 operator*(D1 a, D1 b) { return D1(a.v * b.v, fmaf(a.v, b.d, a.d * b.v)); }
+__device__ __forceinline__ D1 operator/(D1 a, D1 b) {
+  const float q = a.v / b.v;
+  return D1(q, (a.d - q * b.d) / b.v);
+}
+__device__ __forceinline__ D1 operator-(D1 a) { return D1(-a.v, -a.d); }
+__device__ __forceinline__ D1 operator+(D1 a, float b) { return D1(a.v + b, a.d); }
+__device__ __forceinline__ D1 operator+(float a, D1 b) { return D1(a + b.v, b.d); }
+__device__ __forceinline__ D1 operator-(D1 a, float b) { return D1(a.v - b, a.d); }
+__device__ __forceinline__ D1 operator-(float a, D1 b) { return D1(a - b.v, -b.d); }
+__device__ __forceinline__ D1 operator*(D1 a, float b) { return D1(a.v * b, a.d * b); }
+__device__ __forceinline__ D1 operator*(float a, D1 b) { return D1(a * b.v, a * b.d); }
+__device__ __forceinline__ D1& operator+=(D1& a, D1 b) { return a = a + b; }
+__device__ __forceinline__ D1& operator-=(D1& a, D1 b) { return a = a - b; }
+__device__ __forceinline__ D1& operator*=(D1& a, D1 b) { return a = a * b; }
+__device__ __forceinline__ D1& operator+=(D1& a, float b) { return a = a + b; }
+__device__ __forceinline__ bool operator>(D1 a, D1 b) { return a.v > b.v; }
+__device__ __forceinline__ bool operator<(D1 a, D1 b) { return a.v < b.v; }
+__device__ __forceinline__ bool operator>(D1 a, float b) { return a.v > b; }
+__device__ __forceinline__ bool operator<(D1 a, float b) { return a.v < b; }
+__device__ __forceinline__ D1 sqrt_t(D1 a) {
+  const float r = sqrtf(a.v);
+  return D1(r, a.d / (2.0f * r));
+}
+__device__ __forceinline__ D1 rsqrt_t(D1 a) {
+  const float r = rsqrtf(a.v);
+  return D1(r, -0.5f * r * r * r * a.d);
+}
+__device__ __forceinline__ void sincos_t(D1 a, D1* s, D1* c) {
+  float sv, cv;
+  sincosf(a.v, &sv, &cv);
+  *s = D1(sv, cv * a.d);
+  *c = D1(cv, -sv * a.d);
+}
+__device__ __forceinline__ D1 __shfl_sync(unsigned mask, D1 a, int src) {
+  return D1(::__shfl_sync(mask, a.v, src), ::__shfl_sync(mask, a.d, src));
+}
+
+}  // namespace wb
+}  // namespace mpxg
 
 namespace {
 
@@ -297,64 +357,68 @@ __device__ __forceinline__ void eval_step(const mpxg_wb_model& m, const WbSqp& p
   __syncwarp();
 }
 
-// A warp per (instance b, stage t < N, column j): j < nz + nj a central
-// difference over state entry j (j < nz) or control j - nz; j = nz + nj the
-// step at (X_t, U_t) itself, into fnom, with the columns of A_t that f does
-// not depend on (points, forces) set to zero.
-__global__ void __launch_bounds__(32 * kNW) wb_lin_kernel(const __grid_constant__ mpxg_wb_model m,
-                                                          const __grid_constant__ WbSqp p) {
+// A warp per (instance b, stage t < N): the step at (X_t, U_t) in float64,
+// into fnom, and the columns of A_t that f does not depend on (points,
+// forces) set to zero.
+__global__ void __launch_bounds__(32 * kNW) wb_nominal_kernel(const __grid_constant__ mpxg_wb_model m,
+                                                              const __grid_constant__ WbSqp p) {
   __shared__ StepScr sw[kNW];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const WbDims& d = p.d;
-  const int ncols = d.nz + d.nj + 1;
+  const long long item = (long long)blockIdx.x * kNW + wid;
+  if (item >= (long long)p.B * p.N) return;
+  const int b = (int)(item / p.N), t = (int)(item % p.N);
+  StepScr& s = sw[wid];
+  const size_t st = (size_t)b * p.N + t;
+  const int nx = d.nx;
+  const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * nx;
+  for (int i = lane; i < nx; i += 32) s.xb[i] = (double)Xt[i];
+  if (lane < d.nj) s.ub[lane] = (double)p.U[st * d.nj + lane];
+  __syncwarp();
+  eval_step(m, p, s, s.xb, s.ub, p.contact + ((size_t)b * (p.N + 1) + t) * d.nc, lane);
+  double* fo = p.fnom + st * nx;
+  for (int i = lane; i < nx; i += 32) fo[i] = s.f[i];
+  float* At = p.A + st * nx * nx;
+  const int nzc = nx - d.nz;
+  for (int e = lane; e < nx * nzc; e += 32) At[(e / nzc) * nx + d.nz + e % nzc] = 0.0f;
+}
+
+// Per-warp state of the dual-number step.
+struct JacScr {
+  wb::Warp<WbCap, wb::D1> w;
+  wb::D1 u[kMaxU], f[kMaxX];
+};
+
+// A warp per (instance b, stage t < N, column j < nz + nj): the step at
+// (X_t, U_t) on dual numbers whose tangent is state entry j (j < nz) or
+// control j - nz; the tangents of the result are column j of A_t or B_t.
+__global__ void __launch_bounds__(32 * kNW) wb_jac_kernel(const __grid_constant__ mpxg_wb_model m,
+                                                          const __grid_constant__ WbSqp p) {
+  using wb::D1;
+  __shared__ JacScr sw[kNW];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const WbDims& d = p.d;
+  const int ncols = d.nz + d.nj;
   const long long item = (long long)blockIdx.x * kNW + wid;
   if (item >= (long long)p.B * p.N * ncols) return;
   const int b = (int)(item / ((long long)p.N * ncols));
   const int rem = (int)(item % ((long long)p.N * ncols));
   const int t = rem / ncols, j = rem % ncols;
-  StepScr& s = sw[wid];
+  JacScr& s = sw[wid];
   const size_t st = (size_t)b * p.N + t;
-  const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * d.nx;
-  const float* Ut = p.U + st * d.nj;
-  for (int i = lane; i < d.nx; i += 32) s.xb[i] = (double)Xt[i];
-  if (lane < d.nj) s.ub[lane] = (double)Ut[lane];
-  const int* ct = p.contact + ((size_t)b * (p.N + 1) + t) * d.nc;
+  const int nx = d.nx, nq = d.nq, nv = d.nv;
+  const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * nx;
+  for (int i = lane; i < nq; i += 32) s.w.qpos[i] = D1(Xt[i], i == j ? 1.0f : 0.0f);
+  if (lane < nv) s.w.qvel[lane] = D1(Xt[nq + lane], nq + lane == j ? 1.0f : 0.0f);
+  if (lane < d.nj) s.u[lane] = D1(p.U[st * d.nj + lane], d.nz + lane == j ? 1.0f : 0.0f);
   __syncwarp();
-  const int nx = d.nx;
-  if (j == d.nz + d.nj) {
-    eval_step(m, p, s, s.xb, s.ub, ct, lane);
-    double* fo = p.fnom + st * nx;
-    for (int i = lane; i < nx; i += 32) fo[i] = s.f[i];
-    float* At = p.A + st * nx * nx;
-    const int nzc = nx - d.nz;
-    for (int e = lane; e < nx * nzc; e += 32) At[(e / nzc) * nx + d.nz + e % nzc] = 0.0f;
-    return;
-  }
-  const bool isx = j < d.nz;
-  const double z = isx ? s.xb[j] : s.ub[j - d.nz];
-  const double h = 1e-6 * fmax(1.0, fabs(z));
-  double fp[2];
-  for (int sgn = 0; sgn < 2; ++sgn) {
-    const double zp = sgn == 0 ? z + h : z - h;
-    __syncwarp();
-    if (lane == 0) {
-      if (isx) s.xb[j] = zp;
-      else s.ub[j - d.nz] = zp;
-    }
-    __syncwarp();
-    eval_step(m, p, s, s.xb, s.ub, ct, lane);
-    if (sgn == 0) {
-      fp[0] = lane < nx ? s.f[lane] : 0.0;
-      fp[1] = lane + 32 < nx ? s.f[lane + 32] : 0.0;
-    }
-  }
-  const double inv = 1.0 / (2.0 * h);
-  for (int q = 0; q < 2; ++q) {
-    const int i = lane + 32 * q;
-    if (i >= nx) break;
-    const float v = (float)((fp[q] - s.f[i]) * inv);
-    if (isx) p.A[st * nx * nx + (size_t)i * nx + j] = v;
-    else p.Bm[st * nx * d.nj + (size_t)i * d.nj + (j - d.nz)] = v;
+  wb::rb_terms(m, s.w, lane);
+  wb::step(m, s.w, s.u, p.contact + ((size_t)b * (p.N + 1) + t) * d.nc, D1((float)p.dt), D1((float)p.alpha), s.f,
+           lane);
+  __syncwarp();
+  for (int i = lane; i < nx; i += 32) {
+    if (j < d.nz) p.A[st * nx * nx + (size_t)i * nx + j] = s.f[i].d;
+    else p.Bm[st * nx * d.nj + (size_t)i * d.nj + (j - d.nz)] = s.f[i].d;
   }
 }
 
@@ -854,12 +918,14 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
   cudaError_t e = cudaFuncSetAttribute(wb_riccati_kernel<kNX, kNU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)rsmem);
   if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: riccati attribute");
-  const long long lin_items = (long long)B * N * (d.nz + d.nj + 1);
+  const long long jac_items = (long long)B * N * (d.nz + d.nj);
   const long long quad_items = (long long)B * (N + 1);
-  const unsigned lin_blocks = (unsigned)((lin_items + kNW - 1) / kNW);
+  const unsigned nom_blocks = (unsigned)(((long long)B * N + kNW - 1) / kNW);
+  const unsigned jac_blocks = (unsigned)((jac_items + kNW - 1) / kNW);
   const unsigned quad_blocks = (unsigned)((quad_items + 3) / 4);
   auto linearise = [&]() -> cudaError_t {
-    wb_lin_kernel<<<lin_blocks, 32 * kNW, 0, st>>>(m, p);
+    wb_nominal_kernel<<<nom_blocks, 32 * kNW, 0, st>>>(m, p);
+    wb_jac_kernel<<<jac_blocks, 32 * kNW, 0, st>>>(m, p);
     wb_quad_kernel<<<quad_blocks, 128, 0, st>>>(p);
     return cudaGetLastError();
   };

@@ -3,12 +3,14 @@ the float64 oracle (oracle/wb_sqp.py) on the aliengo model of the reference's
 whole-body configuration (tests/golden/aliengo_wb.npz, config_aliengo.py's
 weights), seeded synthetic instances (mpx_gb300.problem.wb_workload).
 
-Tolerances: the GPU takes the same float64 model, central differences and
-merit terms as the oracle, and solves each step's LQ problem in float32; the
-step (and so the iterate after one iteration) then differs from the oracle's
-by float32 rounding of 61-state Riccati products, ~1e-5 of each quantity's
-scale, and the bounds below are 2e-4 of it.  The line search must pick the
-same step length."""
+Tolerances: the GPU takes the same float64 model step and merit terms as the
+oracle; its Jacobians are exact derivatives of the step evaluated in float32
+(the oracle's: float64 central differences, accurate to ~1e-9) and it solves
+each step's LQ problem in float32.  The step (and so the iterate after one
+iteration) then differs from the oracle's by float32 rounding of the
+derivatives and of 61-state Riccati products, ~1e-5 of each quantity's scale,
+and the bounds below are 2e-4 of it.  The line search must pick the same step
+length."""
 import os
 
 import numpy as np
