@@ -257,6 +257,20 @@ mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt
                              const float* contact, float* liftoff, float* reference, float* parameter,
                              float* foot_ref_dot);
 
+/* Whole-body reference generator (mpx/utils/mpc_utils.py:15-145,
+ * reference_generator, with terrain_orientation when use_terrain_estimation)
+ * for a batch of quadrupeds with 4 contact points.  Inputs [B,...]: t_timer
+ * [B,4], x [B,13+2nj+24] (the whole-body state), foot [B,12], input [B,7],
+ * contact [B,4], liftoff [B,12] (in/out); foot0 [12] and q0 [nj] are host
+ * arrays, mass the robot's mass (the reference's qM[0]).  Outputs:
+ * reference [B,N+1,13+nj+28] rows [p, quat, q0, dp, omega, feet, contact,
+ * forces] and parameter [B,N+1,4] (the contact sequence). */
+mpxg_status mpxg_refgen_wb(void* stream, int batch, int N, int n_joints, float dt, float mass, const float* foot0,
+                           const float* q0, float duty_factor, float step_freq, float step_height,
+                           float clearence_speed, int use_terrain_estimation, const float* t_timer, const float* x,
+                           const float* foot, const float* input, const float* contact, float* liftoff,
+                           float* reference, float* parameter);
+
 /* Gait tables of the synthetic trot / walk workloads, one warp per batch
  * entry and a lane per stage (row slot[b] of every per-instance array, or
  * row b when slot is NULL):

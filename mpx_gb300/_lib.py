@@ -140,7 +140,8 @@ EXPORTS = ["mpxg_create", "mpxg_destroy", "mpxg_query_geometry", "mpxg_workspace
            "mpxg_server_create", "mpxg_server_destroy", "mpxg_server_capacity", "mpxg_server_admit",
            "mpxg_server_reset", "mpxg_server_release", "mpxg_submit", "mpxg_submit_many", "mpxg_server_step", "mpxg_poll",
            "mpxg_server_completed", "mpxg_server_stats", "mpxg_server_last_error", "mpxg_last_error", "mpxg_status_string", "mpxg_version",
-           "mpxg_wb_terms", "mpxg_wb_interface", "mpxg_wb_step", "mpxg_wb_sqp_workspace_bytes", "mpxg_wb_sqp"]
+           "mpxg_wb_terms", "mpxg_wb_interface", "mpxg_wb_step", "mpxg_wb_sqp_workspace_bytes", "mpxg_wb_sqp",
+           "mpxg_refgen_wb"]
 
 _lib = None
 
@@ -223,6 +224,10 @@ def load(build_if_missing=True):
     L.mpxg_wb_sqp_workspace_bytes.restype = ctypes.c_size_t
     L.mpxg_wb_sqp.argtypes = [vp, ctypes.POINTER(WbSqpIO)]
     L.mpxg_wb_sqp.restype = ctypes.c_int
+    L.mpxg_refgen_wb.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, vp, vp,
+                                 ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int] + \
+        [vp] * 8
+    L.mpxg_refgen_wb.restype = ctypes.c_int
     L.mpxg_xla_solve.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]
     L.mpxg_xla_solve.restype = None
     L.mpxg_xla_solve_vjp.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t, vp]

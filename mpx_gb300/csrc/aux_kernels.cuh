@@ -234,6 +234,209 @@ __global__ void refgen_srbd_kernel(RefGenArgs g) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) { lo[3 * i] = lx[i]; lo[3 * i + 1] = ly[i]; lo[3 * i + 2] = lz[i]; }
 }
+
+// Whole-body reference generator (mpx/utils/mpc_utils.py:39-145,
+// reference_generator) for a batch, one thread per instance: the SRBD
+// generator's schedule, feet and base rows above in the whole-body row layout
+// [p, quat, q0, dp, omega, feet (12), contact (4), forces (12)], plus
+//  - the base velocity read at x[7 + nj] (the whole-body state),
+//  - q_ref = q0 and the contact forces m g / (legs in contact) on stance legs,
+//  - with terrain != 0, quat_ref from terrain_orientation (mpc_utils.py:15-37):
+//    the frame [front-back vector of the liftoff points, yaw-rotated y axis,
+//    their normal], each normalised, to a quaternion by the method that picks
+//    the largest of the trace and the diagonal (Shepperd's), normalised;
+//    its pitch rotates the commanded velocity (ref_lin_vel = Ryaw Rpitch v).
+// parameter [B,N+1,4] is the contact sequence.  With terrain = 0 every float
+// step matches the reference's float32 arithmetic.
+struct RefGenWbArgs {
+  int batch, N, nj, nx, terrain;
+  float dt, mass;
+  float foot0[12], q0[MPXG_WB_MAX_DOF];
+  float duty, step_freq, step_height, clearence;
+  const float *t_timer, *x, *foot, *input, *contact;
+  float *liftoff, *reference, *parameter;
+};
+
+__device__ void terrain_quat(const float* lo, const float* Ry, float* q) {
+  float fb[3], lr[3], nr[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) fb[i] = DIV(SUB(SUB(ADD(lo[i], lo[3 + i]), lo[6 + i]), lo[9 + i]), 2.0f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) lr[i] = Ry[3 * i + 1];
+  nr[0] = SUB(MUL(fb[1], lr[2]), MUL(fb[2], lr[1]));
+  nr[1] = SUB(MUL(fb[2], lr[0]), MUL(fb[0], lr[2]));
+  nr[2] = SUB(MUL(fb[0], lr[1]), MUL(fb[1], lr[0]));
+  float* v[3] = {fb, lr, nr};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float n = sqrtf(ADD(ADD(MUL(v[k][0], v[k][0]), MUL(v[k][1], v[k][1])), MUL(v[k][2], v[k][2])));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) v[k][i] = DIV(v[k][i], n);
+  }
+  // m(r, c): column c is fb, lr, nr
+  float m[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) { m[r][0] = fb[r]; m[r][1] = lr[r]; m[r][2] = nr[r]; }
+  const float tr = ADD(ADD(m[0][0], m[1][1]), m[2][2]);
+  const float dec[4] = {m[0][0], m[1][1], m[2][2], tr};
+  int c = 0;
+#pragma unroll
+  for (int i = 1; i < 4; ++i)
+    if (dec[i] > dec[c]) c = i;
+  float xyzw[4];
+  if (c != 3) {
+    const int i = c, j = (i + 1) % 3, k = (j + 1) % 3;
+    xyzw[i] = ADD(SUB(1.0f, tr), MUL(2.0f, m[i][i]));
+    xyzw[j] = ADD(m[j][i], m[i][j]);
+    xyzw[k] = ADD(m[k][i], m[i][k]);
+    xyzw[3] = SUB(m[k][j], m[j][k]);
+  } else {
+    xyzw[0] = SUB(m[2][1], m[1][2]);
+    xyzw[1] = SUB(m[0][2], m[2][0]);
+    xyzw[2] = SUB(m[1][0], m[0][1]);
+    xyzw[3] = ADD(1.0f, tr);
+  }
+  const float n = sqrtf(ADD(ADD(ADD(MUL(xyzw[0], xyzw[0]), MUL(xyzw[1], xyzw[1])), MUL(xyzw[2], xyzw[2])),
+                            MUL(xyzw[3], xyzw[3])));
+  q[0] = DIV(xyzw[3], n);
+  q[1] = DIV(xyzw[0], n);
+  q[2] = DIV(xyzw[1], n);
+  q[3] = DIV(xyzw[2], n);
+}
+
+__global__ void refgen_wb_kernel(RefGenWbArgs g) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.batch) return;
+  const int N = g.N, nj = g.nj, C = 13 + nj + 28;
+  const int cf = 13 + nj, cc = cf + 12, cg = cc + 4;  // feet, contact, forces columns
+  const float* x = g.x + (size_t)b * g.nx;
+  const float* input = g.input + b * 7;
+  const float* foot = g.foot + b * 12;
+  float* lo = g.liftoff + b * 12;
+  float* ref = g.reference + (size_t)b * (N + 1) * C;
+  float* par = g.parameter + (size_t)b * (N + 1) * 4;
+  const float q0 = x[3], q1 = x[4], q2 = x[5], q3 = x[6];
+  const float yaw = atan2f(MUL(2.0f, ADD(MUL(q0, q3), MUL(q1, q2))), SUB(1.0f, MUL(2.0f, ADD(MUL(q2, q2), MUL(q3, q3)))));
+  float sy, cy;
+  sincosf(yaw, &sy, &cy);
+  const float Ry[9] = {cy, -sy, 0.0f, sy, cy, 0.0f, 0.0f, 0.0f, 1.0f};
+  const float lzs = ADD(ADD(ADD(lo[2], lo[5]), lo[8]), lo[11]);
+  const float ph = ADD(input[6], DIV(lzs, 4.0f));
+  const float p[3] = {x[0], x[1], ph};
+  float qr[4] = {1.0f, 0.0f, 0.0f, 0.0f};
+  if (g.terrain) terrain_quat(lo, Ry, qr);
+  const float pitch = asinf(MUL(2.0f, SUB(MUL(qr[0], qr[2]), MUL(qr[3], qr[1]))));
+  float sp, cp;
+  sincosf(pitch, &sp, &cp);
+  const float Rp[9] = {cp, 0.0f, sp, 0.0f, 1.0f, 0.0f, -sp, 0.0f, cp};
+  float M[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      M[3 * r + c] = ADD(ADD(MUL(Ry[3 * r], Rp[c]), MUL(Ry[3 * r + 1], Rp[3 + c])), MUL(Ry[3 * r + 2], Rp[6 + c]));
+  float rlv[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    rlv[r] = ADD(ADD(MUL(M[3 * r], input[0]), MUL(M[3 * r + 1], input[1])), MUL(M[3 * r + 2], input[2]));
+  float fp[12];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const float d = ADD(ADD(MUL(g.foot0[3 * i], Ry[3 * r]), MUL(g.foot0[3 * i + 1], Ry[3 * r + 1])),
+                          MUL(g.foot0[3 * i + 2], Ry[3 * r + 2]));
+      fp[3 * i + r] = ADD(p[r], d);
+    }
+  const float inc = MUL(g.dt, g.step_freq);
+  float cur_t[4];
+  int des[4], early[4];
+  const float thr = ADD(0.5f, MUL(0.5f, g.duty));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    cur_t[i] = g.t_timer[b * 4 + i];
+    timer_step(g.duty, inc, cur_t[i], des[i]);
+    early[i] = (des[i] == 0 && g.contact[b * 4 + i] == 1.0f && cur_t[i] > thr) ? 1 : 0;
+  }
+  const float nrm = sqrtf(ADD(ADD(MUL(rlv[0], rlv[0]), MUL(rlv[1], rlv[1])), MUL(rlv[2], rlv[2])));
+  const float den = ADD(nrm, 1e-6f);
+  float isp[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) isp[r] = MUL(DIV(-rlv[r], den), g.clearence);
+  for (int t = 0; t <= N; ++t) {
+    const float tf = MUL((float)t, g.dt);
+    float* rr = ref + (size_t)t * C;
+    rr[0] = ADD(MUL(tf, rlv[0]), p[0]);
+    rr[1] = ADD(MUL(tf, rlv[1]), p[1]);
+    rr[2] = ph;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) rr[3 + i] = qr[i];
+    for (int j = 0; j < nj; ++j) rr[7 + j] = g.q0[j];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) { rr[7 + nj + r] = rlv[r]; rr[10 + nj + r] = input[3 + r]; }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) { rr[cf + i] = foot[i]; rr[cg + i] = 0.0f; }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { rr[cc + i] = 0.0f; par[t * 4 + i] = 0.0f; }
+  }
+  float lx[4], ly[4], lz[4], nt[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    lx[i] = lo[3 * i]; ly[i] = lo[3 * i + 1]; lz[i] = lo[3 * i + 2];
+    nt[i] = g.t_timer[b * 4 + i];
+  }
+  const float sqh = sqrtf(DIV(input[6], 9.81f));
+  const float* dp = x + 7 + nj;
+  float fh[2][4];
+#pragma unroll
+  for (int d = 0; d < 2; ++d)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float f1 = DIV(MUL(MUL(0.5f, rlv[d]), g.duty), g.step_freq);
+      const float f2 = MUL(sqh, SUB(dp[d], rlv[d]));
+      fh[d][i] = ADD(ADD(f1, f2), fp[3 * i + d]);
+    }
+  const float omd = SUB(1.0f, g.duty);
+  for (int t = 0; t <= N; ++t) {
+    const int tp = (t == 0) ? N : t - 1;  // Python index t-1 wraps to the last row
+    const float* fprev = ref + (size_t)tp * C + cf;
+    float px[4], py[4], pz[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { px[i] = fprev[3 * i]; py[i] = fprev[3 * i + 1]; pz[i] = fprev[3 * i + 2]; }
+    int cs[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) timer_step(g.duty, inc, nt[i], cs[i]);
+    float prev_c[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) prev_c[i] = par[tp * 4 + i];
+    float* rr = ref + (size_t)t * C;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { rr[cc + i] = (float)cs[i]; par[t * 4 + i] = (float)cs[i]; }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (cs[i] == 0 && prev_c[i] != 0.0f) { lx[i] = px[i]; ly[i] = py[i]; lz[i] = pz[i]; }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float s = DIV(SUB(nt[i], g.duty), omd);
+      const bool stance = (cs[i] > 0) || (early[i] == 1);
+      const float sh = ADD(lz[i], g.step_height);
+      float* ft = rr + cf + 3 * i;
+      if (stance) {
+        ft[0] = px[i]; ft[1] = py[i]; ft[2] = pz[i];
+      } else {
+        ft[0] = splineXY(lx[i], fh[0][i], isp[0], s);
+        ft[1] = splineXY(ly[i], fh[1][i], isp[1], s);
+        ft[2] = splineZ(lz[i], lz[i], sh, s);
+      }
+    }
+    const float csum = ADD(ADD(ADD((float)cs[0], (float)cs[1]), (float)cs[2]), (float)cs[3]);
+    const float dn = ADD(csum, 1e-5f);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) rr[cg + 3 * i + 2] = DIV(MUL(MUL((float)cs[i], g.mass), 9.81f), dn);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) { lo[3 * i] = lx[i]; lo[3 * i + 1] = ly[i]; lo[3 * i + 2] = lz[i]; }
+}
 #undef ADD
 #undef SUB
 #undef MUL

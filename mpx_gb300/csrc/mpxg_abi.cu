@@ -748,6 +748,28 @@ mpxg_status mpxg_refgen_srbd(void* stream, int batch, int N, int n_max, float dt
   return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "refgen_srbd_kernel launch");
 }
 
+mpxg_status mpxg_refgen_wb(void* stream, int batch, int N, int n_joints, float dt, float mass, const float* foot0,
+                           const float* q0, float duty_factor, float step_freq, float step_height,
+                           float clearence_speed, int use_terrain_estimation, const float* t_timer, const float* x,
+                           const float* foot, const float* input, const float* contact, float* liftoff,
+                           float* reference, float* parameter) {
+  if (batch < 0 || N < 1 || n_joints < 0 || n_joints > MPXG_WB_MAX_DOF || !foot0 || !q0 || !t_timer || !x ||
+      !foot || !input || !contact || !liftoff || !reference || !parameter)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_refgen_wb: bad arguments");
+  if (batch == 0) return MPXG_OK;
+  RefGenWbArgs g;
+  g.batch = batch; g.N = N; g.nj = n_joints; g.nx = 13 + 2 * n_joints + 24; g.terrain = use_terrain_estimation != 0;
+  g.dt = dt; g.mass = mass;
+  for (int i = 0; i < 12; ++i) g.foot0[i] = foot0[i];  // host arrays
+  for (int i = 0; i < MPXG_WB_MAX_DOF; ++i) g.q0[i] = i < n_joints ? q0[i] : 0.0f;
+  g.duty = duty_factor; g.step_freq = step_freq; g.step_height = step_height; g.clearence = clearence_speed;
+  g.t_timer = t_timer; g.x = x; g.foot = foot; g.input = input; g.contact = contact;
+  g.liftoff = liftoff; g.reference = reference; g.parameter = parameter;
+  refgen_wb_kernel<<<(batch + 127) / 128, 128, 0, (cudaStream_t)stream>>>(g);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MPXG_OK : cuda_fail(nullptr, e, "refgen_wb_kernel launch");
+}
+
 }  // extern "C"
 
 // ============================================================================

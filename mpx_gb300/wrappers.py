@@ -36,6 +36,7 @@ from . import _lib
 from . import mjcf
 from . import problem as P
 from .solver import Solver, _ptr, _stream_handle
+from .wb_wrappers import WholeBodyBatchedController, WholeBodyController, is_whole_body
 from .wholebody import WholeBodyModel
 
 
@@ -270,7 +271,12 @@ class MPCControllerWrapper:
     on a compiled SRBD model.  The state is the floating base [p, quat, v, omega]
     read from qpos[:7] and qvel[:6]; foot positions are given by the caller."""
 
-    def __init__(self, config, limited_memory=False, opts=None, device=None, desc=None):
+    def __init__(self, config, limited_memory=False, opts=None, device=None, desc=None, model=None):
+        self._wb = None
+        if is_whole_body(config):  # the reference's own whole-body configurations (config_aliengo, config_go2)
+            self._wb = WholeBodyController(config, limited_memory, model=model, device=device, opts=opts)
+            self.config = config
+            return
         self.config = config
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.mpc_frequency = float(config.mpc_frequency)
@@ -312,9 +318,14 @@ class MPCControllerWrapper:
         return np.concatenate([qpos[:7], qvel[:6]])
 
     def run(self, qpos, qvel, input, contact, foot_op=None):
-        """mpc_wrapper.py:297-365.  Returns (grf, q, dq): the first control and
-        the floating-base pose/velocity of the plan (the reference returns joint
-        torques from its whole-body model)."""
+        """mpc_wrapper.py:297-365.  With a whole-body configuration this is the
+        reference's controller (wb_wrappers.WholeBodyController): returns
+        (tau, q, dq), the joint torques clipped to the configuration's limits
+        and the planned joint positions and velocities.  With a compiled SRBD
+        model it returns (grf, q, dq): the first control and the floating-base
+        pose/velocity of the plan."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.run(qpos, qvel, input, contact)
         x0 = self._state(qpos, qvel)
         foot = np.asarray(foot_op if foot_op is not None else self.foot0 + np.tile(x0[:3], 4), dtype=np.float32)
         inp = np.asarray(input, dtype=np.float32).copy()
@@ -343,10 +354,14 @@ class MPCControllerWrapper:
     def save_state(self):
         """Checkpoint of the warm start and gait state as host tensors (the
         reference keeps them in attributes, mpc_wrapper.py:367-385)."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.save_state()
         return _save_state(self, self.STATE)
 
     def load_state(self, state):
         """Resume from save_state()."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.load_state(state)
         _load_state(self, self.STATE, state)
 
     def _update_and_extract(self, X, U, V, x0):
@@ -360,6 +375,8 @@ class MPCControllerWrapper:
 
     def reset(self, qpos, qvel, foot=None):
         """mpc_wrapper.py:367-385."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.reset(qpos, qvel)
         x0 = self._state(qpos, qvel)
         self.contact_time = _to_dev(np.asarray(self.config.timer_t, dtype=np.float32).reshape(1, 4), self.dev)
         lo = self.foot0 if foot is None else np.asarray(foot, dtype=np.float32)
@@ -375,6 +392,8 @@ class MPCControllerWrapper:
         ([N+1, 17] and [N+1, 16] for the compiled SRBD model); by default
         they come, as in the reference (:411), from
         config.reference(N+1, dt, n_joints, n_contact, p_legs0, q0)."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.runOffline(qpos, qvel, reference, parameter, max_iter)
         if reference is None or parameter is None:
             make = getattr(self.config, "reference", None)
             if make is None:
@@ -431,9 +450,14 @@ class BatchedDataMPCWrapper:
     model.  `data` is an mpx_data (a dict of device tensors with a leading env
     dimension); a plain dict with the same keys is accepted too."""
 
-    def __init__(self, config, n_env, limited_memory=False, opts=None, device=None, desc=None):
+    def __init__(self, config, n_env, limited_memory=False, opts=None, device=None, desc=None, model=None):
         self.config = config
         self.n_env = int(n_env)
+        self._wb = None
+        if is_whole_body(config):  # the reference's own whole-body configurations
+            self._wb = WholeBodyBatchedController(config, n_env, limited_memory, model=model, device=device,
+                                                  opts=opts)
+            return
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.N = int(config.N)
         self.shift = int(1 / (config.dt * config.mpc_frequency))
@@ -448,6 +472,8 @@ class BatchedDataMPCWrapper:
 
     def make_data(self):
         """mpc_wrapper.py:100-113, for all environments at once."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.make_data()
         B, N = self.n_env, self.N
         dev = self.dev
         W = np.diag(np.asarray(self.config.W, dtype=np.float64)).astype(np.float32)
@@ -464,7 +490,10 @@ class BatchedDataMPCWrapper:
 
     def run(self, data, x0, input, foot_op=None):
         """mpc_wrapper.py:115-170: timer, reference, solve, NaN-guarded warm
-        start; returns (data, grf)."""
+        start; returns (data, grf), or with a whole-body configuration
+        (data, tau) as the reference does."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.run(data, x0, input)
         B, N, dev, st = self.n_env, self.N, self.dev, _stream_handle(None)
         x0 = _to_dev(x0, dev).reshape(B, -1)
         inp = _to_dev(input, dev).reshape(B, 7)
@@ -502,7 +531,10 @@ class BatchedDataMPCWrapper:
     def reset(self, data, qpos, qvel=None, foot=None):
         """mpc_wrapper.py:172-192, called as there with (data, qpos, qvel,
         foot): the compiled model's state is the floating base, qpos[:, :7]
-        followed by qvel[:, :6].  Called as (data, x0), qpos is that state."""
+        followed by qvel[:, :6].  Called as (data, x0), qpos is that state.
+        With a whole-body configuration the state is [qpos, qvel, foot, 0]."""
+        if getattr(self, "_wb", None) is not None:
+            return self._wb.reset(data, qpos, qvel, foot)
         B, N, dev = self.n_env, self.N, self.dev
         x0 = _to_dev(qpos, dev).reshape(B, -1)
         if qvel is not None:

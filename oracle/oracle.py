@@ -9,7 +9,7 @@ oracle/build_oracle.py) and exposes numpy-level helpers:
   * lqr_solve(...)      sequential-Riccati LQR in absolute coordinates
   * dense_lqr(...)      the same LQR by one dense KKT solve (numpy), the
                         ground truth the Riccati recursion is checked against
-  * dynamics/cost/linearize/penalty, timer_run, refgen_srbd
+  * dynamics/cost/linearize/penalty, timer_run, refgen_srbd, refgen_wb
 
 See oracle.hpp for what each restates (reference file:line) and the parity
 status ("parity unpinned" for the SQP/KKT solver).
@@ -246,6 +246,22 @@ def refgen_srbd(N, dt, mass, foot0, duty_factor, step_freq, step_height, clearen
                       f(clearence_speed), _fp(_f32(t_timer)), _fp(_f32(x)), _fp(_f32(foot)), _fp(_f32(input)),
                       _fp(_f32(contact)), _fp(lo), _fp(ref), _fp(par), _fp(frd))
     return ref, par, lo, frd
+
+
+def refgen_wb(N, nj, dt, mass, foot0, q0, duty_factor, step_freq, step_height, clearence_speed, terrain, t_timer, x,
+              foot, input, contact, liftoff):
+    """One instance of the whole-body reference generator (FP32; terrain:
+    use_terrain_estimation).  Returns (reference[N+1,13+nj+28],
+    parameter[N+1,4], liftoff[12])."""
+    L = lib()
+    lo = _f32(liftoff).copy()
+    ref = np.zeros((N + 1, 13 + nj + 28), dtype=np.float32)
+    par = np.zeros((N + 1, 4), dtype=np.float32)
+    f = ctypes.c_float
+    L.orc_refgen_wb(int(N), int(nj), f(dt), f(mass), _fp(_f32(foot0)), _fp(_f32(q0)), f(duty_factor), f(step_freq),
+                    f(step_height), f(clearence_speed), int(terrain), _fp(_f32(t_timer)), _fp(_f32(x)),
+                    _fp(_f32(foot)), _fp(_f32(input)), _fp(_f32(contact)), _fp(lo), _fp(ref), _fp(par))
+    return ref, par, lo
 
 
 def lqr_solve(A, Bm, c, Q, R, M, q, r, x0, precision=64, n_threads=0):

@@ -244,6 +244,19 @@ int orc_refgen_srbd(int N, float dt, float mass, const float* foot0, float duty_
   return 0;
 }
 
+// Whole-body reference generator (mpc_utils.py:15-145), FP32, one instance.
+int orc_refgen_wb(int N, int nj, float dt, float mass, const float* foot0, const float* q0, float duty_factor,
+                  float step_freq, float step_height, float clearence_speed, int terrain, const float* t_timer,
+                  const float* x, const float* foot, const float* input, const float* contact, float* liftoff,
+                  float* reference, float* parameter) {
+  RefGenCfg g;
+  g.N = N; g.dt = dt; g.n_contact = 4; g.mass = mass;
+  for (int i = 0; i < 12; ++i) g.foot0[i] = foot0[i];
+  g.duty_factor = duty_factor; g.step_freq = step_freq; g.step_height = step_height; g.clearence_speed = clearence_speed;
+  refgen_wb(g, nj, q0, terrain, t_timer, x, foot, input, contact, liftoff, reference, parameter);
+  return 0;
+}
+
 // Model FLOPs of one non-terminal stage at (x, u) (flops.hpp): out = {f,
 // f with [A B], l, the linearisation, one line-search trial}.
 void orc_stage_flops(const orc_model* md, const double* x, const double* u, const double* ref, const double* par,

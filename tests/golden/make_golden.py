@@ -346,6 +346,44 @@ def _quat_sub(u, v):
 
 
 # ----------------------------------------------------------------- install
+class _Rotation:
+    """jax.scipy.spatial.transform.Rotation.from_matrix(m).as_quat() (x, y, z,
+    w) in the active float type, by the published algorithm jax's Rotation
+    follows (scipy's before it orthogonalised its input): pick the largest of
+    the diagonal and the trace, form the quaternion from that pivot, and
+    normalise it; no orthogonalisation of a matrix whose columns are not
+    orthogonal (scipy >= 1.11 projects such a matrix first, so it cannot
+    stand in)."""
+
+    def __init__(self, q):
+        self.q = q
+
+    @classmethod
+    def from_matrix(cls, m):
+        m = np.asarray(m, dtype=DT["f"])
+        f = DT["f"]
+        tr = f(f(m[0, 0] + m[1, 1]) + m[2, 2])
+        dec = [m[0, 0], m[1, 1], m[2, 2], tr]
+        c = int(np.argmax(dec))
+        q = np.zeros(4, dtype=f)
+        if c != 3:
+            i, j, k = c, (c + 1) % 3, (c + 2) % 3
+            q[i] = f(f(1.0 - tr) + f(2.0 * m[i, i]))
+            q[j] = f(m[j, i] + m[i, j])
+            q[k] = f(m[k, i] + m[i, k])
+            q[3] = f(m[k, j] - m[j, k])
+        else:
+            q[0] = f(m[2, 1] - m[1, 2])
+            q[1] = f(m[0, 2] - m[2, 0])
+            q[2] = f(m[1, 0] - m[0, 1])
+            q[3] = f(1.0 + tr)
+        n = f(np.sqrt(f(f(f(q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3])))
+        return cls(q / n)
+
+    def as_quat(self):
+        return _wrap(np.asarray(self.q, dtype=DT["f"]))
+
+
 def install_shim():
     jnp = types.ModuleType("jax.numpy")
     for name in ("sqrt", "square", "cos", "sin", "arctan2", "arcsin", "log", "clip", "cross", "logical_and",
@@ -363,6 +401,7 @@ def install_shim():
     jnp.pi = np.pi
     jnp.float32 = np.float32
     jnp.kron = lambda a, b: _wrap(np.kron(*_prep([a, b])))
+    jnp.roll = lambda a, k: _wrap(np.roll(np.asarray(a), k))
     jnp.eye = lambda n, dtype=None: _wrap(np.eye(n, dtype=DT["f"]))
     linalg = types.ModuleType("jax.numpy.linalg")
     linalg.norm = _norm
@@ -387,7 +426,7 @@ def install_shim():
     scipy.linalg = sl
     st = types.ModuleType("jax.scipy.spatial")
     stt = types.ModuleType("jax.scipy.spatial.transform")
-    stt.Rotation = None
+    stt.Rotation = _Rotation
     st.transform = stt
     scipy.spatial = st
     jax.scipy = scipy
@@ -725,16 +764,71 @@ def main_wb(ref_root, out):
     print("wrote", out)
 
 
+def main_wbref(ref_root, out):
+    """The whole-body reference generator (mpc_utils.py:15-145,
+    reference_generator with terrain_orientation) with config_aliengo
+    constants, on seeded states, both terrain settings."""
+    install_shim()
+    _install_fake_mjx()
+    mo = load(ref_root, "mpx/utils/models.py", "ref_models")
+    ob = load(ref_root, "mpx/utils/objectives.py", "ref_objectives")
+    pkg, utils = types.ModuleType("mpx"), types.ModuleType("mpx.utils")
+    utils.models, utils.objectives, pkg.utils = mo, ob, utils
+    sys.modules.update({"mpx": pkg, "mpx.utils": utils, "mpx.utils.models": mo, "mpx.utils.objectives": ob})
+    cfg = load(ref_root, "mpx/config/config_aliengo.py", "ref_config_aliengo")
+    mu = load(ref_root, "mpx/utils/mpc_utils.py", "ref_mpc_utils")
+    rng = np.random.default_rng(77)
+    nj, nc = int(cfg.n_joints), int(cfg.n_contact)
+    foot0 = np.asarray(cfg.p_legs0, dtype=np.float32)
+    q0 = np.asarray(cfg.q0, dtype=np.float32)
+    mass = np.float32(42.0)
+    R = 12
+    ins = dict(t_timer=rng.uniform(0, 1, (R, 4)), x=np.zeros((R, 13 + 2 * nj + 6 * nc)), foot=np.zeros((R, 12)),
+               input=np.zeros((R, 7)), contact=rng.integers(0, 2, (R, 4)).astype(np.float64),
+               liftoff=np.zeros((R, 12)))
+    for r in range(R):
+        q = rng.normal(0, 0.1, 4); q[0] += 1; q /= np.linalg.norm(q)
+        ins["x"][r] = np.concatenate([rng.normal(0, 0.1, 3) + [0, 0, 0.33], q, q0 + rng.normal(0, 0.1, nj),
+                                      rng.normal(0, 0.3, 6 + nj), foot0 + rng.normal(0, 0.02, 12),
+                                      rng.normal(0, 30, 12)])
+        ins["foot"][r] = foot0 + rng.normal(0, 0.02, 12)
+        ins["input"][r] = np.concatenate([rng.uniform(-1, 1, 3), rng.uniform(-0.5, 0.5, 3), [cfg.initial_height]])
+        ins["liftoff"][r] = ins["foot"][r] + rng.normal(0, 0.01 if r % 2 else 0.05, 12)
+    g = {}
+    for k in ins:
+        ins[k] = ins[k].astype(np.float32)
+        g["wbref_in_" + k] = ins[k]
+    for terrain in (False, True):
+        outs = {"reference": [], "parameter": [], "liftoff": []}
+        for r in range(R):
+            ref, par, lo = mu.reference_generator(
+                terrain, cfg.N, cfg.dt, nj, nc, float(mass), _wrap(foot0), _wrap(q0),
+                _wrap(ins["t_timer"][r]), _wrap(ins["x"][r]), _wrap(ins["foot"][r]), _wrap(ins["input"][r]),
+                np.float32(cfg.duty_factor), np.float32(cfg.step_freq), np.float32(cfg.step_height),
+                _wrap(ins["liftoff"][r]), _wrap(ins["contact"][r]), np.float32(0.4))
+            outs["reference"].append(np.asarray(ref)); outs["parameter"].append(np.asarray(par))
+            outs["liftoff"].append(np.asarray(lo))
+        for k, v in outs.items():
+            g["wbref_%s_%s" % ("terrain" if terrain else "flat", k)] = np.stack(v).astype(np.float32)
+    g["wbref_cfg"] = np.array([cfg.N, cfg.dt, mass, cfg.duty_factor, cfg.step_freq, cfg.step_height, 0.4],
+                              dtype=np.float64)
+    g["wbref_foot0"] = foot0
+    g["wbref_q0"] = q0
+    np.savez_compressed(out, **g)
+    print("wrote", out)
+
+
 def reference_root():
     """The reference checkout named by MPX_REFERENCE ("" when unset)."""
     return os.environ.get("MPX_REFERENCE", "")
 
 
 if __name__ == "__main__":
-    wb = "--wb" in sys.argv
-    argv = [a for a in sys.argv[1:] if a != "--wb"]
+    wb, wbref = "--wb" in sys.argv, "--wbref" in sys.argv
+    argv = [a for a in sys.argv[1:] if a not in ("--wb", "--wbref")]
     ref_root = argv[0] if argv else reference_root()
-    out = argv[1] if len(argv) > 1 else os.path.join(HERE, "wb_golden.npz" if wb else "srbd_golden.npz")
+    default = "wb_golden.npz" if wb else ("wb_refgen.npz" if wbref else "srbd_golden.npz")
+    out = argv[1] if len(argv) > 1 else os.path.join(HERE, default)
     if not ref_root or not os.path.isdir(os.path.join(ref_root, "mpx")):
-        sys.exit("usage: make_golden.py <reference checkout containing mpx/> [--wb] [out.npz]")
-    (main_wb if wb else main)(ref_root, out)
+        sys.exit("usage: make_golden.py <reference checkout containing mpx/> [--wb | --wbref] [out.npz]")
+    (main_wb if wb else (main_wbref if wbref else main))(ref_root, out)

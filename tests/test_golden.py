@@ -83,3 +83,26 @@ def test_gauss_newton_hessian(oracle):
         for blk, gold in ((H[:n, :n], G["hess_Q"][i]), (H[n:, n:], G["hess_R"][i]), (H[:n, n:], G["hess_M"][i])):
             scale = max(1.0, np.abs(gold).max())
             assert np.abs(blk - gold).max() <= 1e-5 * scale, (i, np.abs(blk - gold).max(), scale)
+
+
+def test_oracle_wb_refgen_matches_golden():
+    """oracle.refgen_wb (the whole-body generator, mpc_utils.py:15-145) against
+    the reference's own reference_generator run under the numpy stand-in
+    (tests/golden/wb_refgen.npz), both terrain settings: the contact schedule
+    and liftoff bookkeeping exactly, the float rows to 1e-6 relative (the
+    yaw's float32 sin/cos differ by an ulp between numpy and glibc)."""
+    from oracle import oracle as O
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "wb_refgen.npz"))
+    cfg = g["wbref_cfg"]
+    N = int(cfg[0])
+    for tag, terrain in (("flat", 0), ("terrain", 1)):
+        for r in range(g["wbref_in_x"].shape[0]):
+            ref, par, lo = O.refgen_wb(N, 12, cfg[1], cfg[2], g["wbref_foot0"], g["wbref_q0"], cfg[3], cfg[4],
+                                       cfg[5], cfg[6], terrain, *(g["wbref_in_" + k][r] for k in
+                                                                 ("t_timer", "x", "foot", "input", "contact",
+                                                                  "liftoff")))
+            want = g["wbref_%s_reference" % tag][r]
+            assert np.array_equal(par, g["wbref_%s_parameter" % tag][r]), (tag, r)
+            assert np.array_equal(ref[:, 37:41], want[:, 37:41]), (tag, r)
+            assert (np.abs(ref - want) / (1.0 + np.abs(want))).max() < 1e-6, (tag, r)
+            assert np.abs(lo - g["wbref_%s_liftoff" % tag][r]).max() < 1e-6, (tag, r)

@@ -45,6 +45,8 @@ def test_srbd_and_whole_body_vectors_regenerate_bit_for_bit(tmp_path):
     _same(os.path.join(GOLDEN, "srbd_golden.npz"), tmp_path / "srbd.npz")
     _run(os.path.join(GOLDEN, "make_golden.py"), ref, "--wb", str(tmp_path / "wb.npz"))
     _same(os.path.join(GOLDEN, "wb_golden.npz"), tmp_path / "wb.npz")
+    _run(os.path.join(GOLDEN, "make_golden.py"), ref, "--wbref", str(tmp_path / "wbref.npz"))
+    _same(os.path.join(GOLDEN, "wb_refgen.npz"), tmp_path / "wbref.npz")
 
 
 def test_robot_model_fixtures_regenerate_bit_for_bit(tmp_path):
