@@ -20,12 +20,16 @@ Differences from the reference, by necessity:
   * Python callables (cost, dynamics, hessian_approx) cannot cross the C ABI:
     the model is one of the compiled ids (problem.ModelDesc).
   * `limited_memory` is accepted and ignored.
-  * MuJoCo is not available: foot positions that the reference computes with
-    mujoco forward kinematics (mpc_wrapper.py:313-316) are passed in by the
-    caller (`foot_op`).  The whole-body torque mapping (mpc_utils.py:275-313)
-    runs on libmpxg's own rigid-body kernel (mpx_gb300.wholebody) over the
-    robot's MJCF (`config.model_path`, read by mpx_gb300.mjcf) or a model
-    passed as `wb_model`.
+  * MuJoCo is not available.  With a whole-body configuration (the
+    reference's config_aliengo / config_go2), MPCControllerWrapper and
+    BatchedDataMPCWrapper hand over to mpx_gb300.wb_wrappers, which computes
+    the feet by libmpxg's own rigid-body kernel over the robot's MJCF
+    (`config.model_path`, read by mpx_gb300.mjcf, or a parsed `model=`) and
+    returns the reference's (tau, q, dq) / (data, tau).  With a compiled SRBD
+    model the foot positions (mpc_wrapper.py:313-316) are passed in by the
+    caller (`foot_op`).  The SRBD wrapper's whole-body torque mapping
+    (mpc_utils.py:275-313) runs on the same rigid-body kernel
+    (mpx_gb300.wholebody) over the MJCF or a model passed as `wb_model`.
 """
 import os
 
