@@ -1302,7 +1302,7 @@ def run_wb_sqp(args, rank, world, local_rank, emit=True):
         "config": {"workload": "%d aliengo whole-body MPCs, N = %d, %d SQP iterations per warm tick" % (Bb, N, WBS_ITERS),
                    "parallelism": "replicas"},
         "lone": res["lone"], "batch": res["batch"],
-        "gpu_launches": (6 * WBS_ITERS + 4) * steps,
+        "gpu_launches": (8 * WBS_ITERS + 4) * steps,
         "clocks": clk,
     }
     if rank == 0 and emit:

@@ -1,13 +1,13 @@
 // Whole-body SQP (mpxg_wb_sqp): the whole-body MPC solve of mpc_wrapper.py's
 // wrappers (quadruped_wb_dynamics, models.py:39-117; quadruped_wb_obj and
-// quadruped_wb_hessian_gn, objectives.py:77-203), one SQP iteration as six
-// launches:
-//   wb_nominal_kernel  a warp per (instance, stage): the dynamics step in
-//                    float64 at X_t, U_t (the defects' f);
-//   wb_jac_kernel    a warp per (instance, stage, column): the step on a
-//                    forward-mode dual number seeded on one state or control
-//                    entry, in float32: a column of A_t or B_t, exact up to
-//                    float32 rounding;
+// quadruped_wb_hessian_gn, objectives.py:77-203), one SQP iteration as
+// eight launches:
+//   wb_lin_kernel    a warp per (instance, stage): the dynamics step in
+//                    float64 at X_t, U_t (the defects' f); and in the same
+//                    launch a warp per (instance, stage, column): the step on
+//                    a forward-mode dual number seeded on one state or
+//                    control entry, in float32: a column of A_t or B_t, exact
+//                    up to float32 rounding;
 //   wb_quad_kernel   a warp per (instance, stage): defects, stage cost,
 //                    gradient, Gauss-Newton blocks (float64, written float32);
 //   wb_riccati_kernel  a 256-thread block per instance: the float32 Riccati
@@ -17,11 +17,12 @@
 //   wb_merit_kernel  a block per instance: directional derivative, penalty
 //                    update, merit at the current iterate;
 //   wb_trial_kernel  a warp per (instance, trial step, stage): the merit's
-//                    stage terms at X + a_k dX for every trial a_k = beta^k at
-//                    once (dynamics step, cost, defect);
-//   wb_accept_kernel a block per instance: the first trial that passes the
-//                    Armijo test (the same choice as trying them in order),
-//                    then the update.
+//                    stage terms at X + a_k dX (dynamics step, cost, defect),
+//                    launched for the full step, then for every shorter trial
+//                    a_k = beta^k at once for the instances that reject it;
+//   wb_accept_kernel a block per instance after each trial launch: the first
+//                    trial that passes the Armijo test (the same choice as
+//                    trying them in order), then the update.
 // The defects and the merit take the step in float64 (the merit's changes near
 // convergence are ~1e-7 of its value); the derivatives and the Riccati run in
 // float32 like every other solve here.
@@ -125,6 +126,7 @@ WbDims wb_dims(const mpxg_wb_model& m) {
 // Device view of one mpxg_wb_sqp call: the caller's arrays and the workspace.
 struct WbSqp {
   int B, N, KT, first;
+  int k_lo, k_hi, phase;  // trial steps of this wb_trial_kernel launch; wb_accept_kernel's pass
   WbDims d;
   double dt, alpha, beta, eta, skip_tol, rho0;
   float reg;
@@ -360,15 +362,10 @@ __device__ __forceinline__ void eval_step(const mpxg_wb_model& m, const WbSqp& p
 // A warp per (instance b, stage t < N): the step at (X_t, U_t) in float64,
 // into fnom, and the columns of A_t that f does not depend on (points,
 // forces) set to zero.
-__global__ void __launch_bounds__(32 * kNW) wb_nominal_kernel(const __grid_constant__ mpxg_wb_model m,
-                                                              const __grid_constant__ WbSqp p) {
-  __shared__ StepScr sw[kNW];
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+__device__ __forceinline__ void nominal_item(const mpxg_wb_model& m, const WbSqp& p, StepScr& s, long long item,
+                                             int lane) {
   const WbDims& d = p.d;
-  const long long item = (long long)blockIdx.x * kNW + wid;
-  if (item >= (long long)p.B * p.N) return;
   const int b = (int)(item / p.N), t = (int)(item % p.N);
-  StepScr& s = sw[wid];
   const size_t st = (size_t)b * p.N + t;
   const int nx = d.nx;
   const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * nx;
@@ -392,19 +389,13 @@ struct JacScr {
 // A warp per (instance b, stage t < N, column j < nz + nj): the step at
 // (X_t, U_t) on dual numbers whose tangent is state entry j (j < nz) or
 // control j - nz; the tangents of the result are column j of A_t or B_t.
-__global__ void __launch_bounds__(32 * kNW) wb_jac_kernel(const __grid_constant__ mpxg_wb_model m,
-                                                          const __grid_constant__ WbSqp p) {
+__device__ __forceinline__ void jac_item(const mpxg_wb_model& m, const WbSqp& p, JacScr& s, long long item, int lane) {
   using wb::D1;
-  __shared__ JacScr sw[kNW];
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const WbDims& d = p.d;
   const int ncols = d.nz + d.nj;
-  const long long item = (long long)blockIdx.x * kNW + wid;
-  if (item >= (long long)p.B * p.N * ncols) return;
   const int b = (int)(item / ((long long)p.N * ncols));
   const int rem = (int)(item % ((long long)p.N * ncols));
   const int t = rem / ncols, j = rem % ncols;
-  JacScr& s = sw[wid];
   const size_t st = (size_t)b * p.N + t;
   const int nx = d.nx, nq = d.nq, nv = d.nv;
   const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * nx;
@@ -420,6 +411,27 @@ __global__ void __launch_bounds__(32 * kNW) wb_jac_kernel(const __grid_constant_
     if (j < d.nz) p.A[st * nx * nx + (size_t)i * nx + j] = s.f[i].d;
     else p.Bm[st * nx * d.nj + (size_t)i * d.nj + (j - d.nz)] = s.f[i].d;
   }
+}
+
+// The linearisation's dynamics in one launch: warps 0 .. B N - 1 take the
+// float64 steps at (X_t, U_t) (nominal_item), the following B N (nz + nj)
+// warps the dual-number columns (jac_item); the long float64 chains start
+// first and the two kinds overlap on the SMs.
+__global__ void __launch_bounds__(32 * kNW) wb_lin_kernel(const __grid_constant__ mpxg_wb_model m,
+                                                          const __grid_constant__ WbSqp p) {
+  __shared__ union Scr {
+    StepScr nom[kNW];
+    JacScr jac[kNW];
+  } sw;
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long nom = (long long)p.B * p.N, nom_blocks = (nom + kNW - 1) / kNW;
+  if (blockIdx.x < nom_blocks) {
+    const long long item = (long long)blockIdx.x * kNW + wid;
+    if (item < nom) nominal_item(m, p, sw.nom[wid], item, lane);
+    return;
+  }
+  const long long item = (long long)(blockIdx.x - nom_blocks) * kNW + wid;
+  if (item < nom * (p.d.nz + p.d.nj)) jac_item(m, p, sw.jac[wid], item, lane);
 }
 
 __device__ __forceinline__ void load_stage(const WbSqp& p, CostScr& s, int b, int t, int lane) {
@@ -643,21 +655,23 @@ __global__ void __launch_bounds__(kBlk) wb_merit_kernel(const __grid_constant__ 
   if (p.first && p.status) p.status[b] = 0;
 }
 
-// A warp per (instance b, trial k, stage t <= N): the merit's stage terms at
-// a_k = beta^k: cost_t(X_t + a dX_t, U_t + a dU_t) + V_t(a).c_t(a) +
-// rho/2 |c_t(a)|^2, c_0(a) = x0 - X_0(a), c_t(a) = f(X_{t-1}(a), U_{t-1}(a)) -
-// X_t(a).  Nothing when the iteration takes the full step untested.
+// A warp per (instance b, trial k in [k_lo, k_hi), stage t <= N): the
+// merit's stage terms at a_k = beta^k: cost_t(X_t + a dX_t, U_t + a dU_t) +
+// V_t(a).c_t(a) + rho/2 |c_t(a)|^2, c_0(a) = x0 - X_0(a),
+// c_t(a) = f(X_{t-1}(a), U_{t-1}(a)) - X_t(a).  Nothing for an instance
+// whose search is over (ls[3] != 0: the full step taken untested, or a step
+// already accepted).
 __global__ void __launch_bounds__(32 * kNW) wb_trial_kernel(const __grid_constant__ mpxg_wb_model m,
                                                             const __grid_constant__ WbSqp p) {
   __shared__ StepScr sws[kNW];
   __shared__ CostScr swc[kNW];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long item = (long long)blockIdx.x * kNW + wid;
-  const int N1 = p.N + 1;
-  if (item >= (long long)p.B * p.KT * N1) return;
-  const int b = (int)(item / ((long long)p.KT * N1));
-  const int rem = (int)(item % ((long long)p.KT * N1));
-  const int k = rem / N1, t = rem % N1;
+  const int N1 = p.N + 1, nk = p.k_hi - p.k_lo;
+  if (item >= (long long)p.B * nk * N1) return;
+  const int b = (int)(item / ((long long)nk * N1));
+  const int rem = (int)(item % ((long long)nk * N1));
+  const int k = p.k_lo + rem / N1, t = rem % N1;
   const double* ls = p.ls + b * 8;
   if (ls[3] != 0.0) return;
   double al = 1.0;
@@ -695,22 +709,39 @@ __global__ void __launch_bounds__(32 * kNW) wb_trial_kernel(const __grid_constan
   if (lane == 0) p.trial[((size_t)b * p.KT + k) * N1 + t] = cost + vcs + 0.5 * ls[0] * ccs;
 }
 
-// A block per instance: a = 1 when the iteration skips the search, else the
-// first a_k with phi(a_k) - phi0 <= eta a_k dphi (the last trial's step and
-// MPXG_INST_LS_FAIL when none passes); then X += a dX, U += a dU,
+// A block per instance, in two passes around the two trial launches.
+// Pass 0 (after the full step's trial): a = 1 when the iteration skips the
+// search or the full step passes phi(1) - phi0 <= eta dphi; otherwise the
+// instance stays searching and nothing is updated (with ls_max_trials = 1
+// the full step is taken with MPXG_INST_LS_FAIL).  Pass 1 (after the trials
+// k >= 1): for the instances still searching, the first a_k that passes, or
+// the last trial's step and MPXG_INST_LS_FAIL.  The choice is that of
+// trying 1, beta, beta^2, ... in order.  Then X += a dX, U += a dU,
 // V += a (lam - V), MPXG_INST_NAN on a non-finite result.
 __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__ WbSqp p) {
   __shared__ double s_al;
-  __shared__ int s_bad;
+  __shared__ int s_bad, s_go;
   const int b = blockIdx.x, N1 = p.N + 1;
-  const double* ls = p.ls + b * 8;
+  double* ls = p.ls + b * 8;
   if (threadIdx.x == 0) {
     double al = 1.0;
-    int fail = 0;
-    if (ls[3] == 0.0) {
+    int fail = 0, go = 1;
+    if (p.phase == 0) {
+      if (ls[3] == 0.0) {
+        double phi = 0.0;
+        const double* tr = p.trial + ((size_t)b * p.KT) * N1;
+        for (int t = 0; t < N1; ++t) phi += tr[t];
+        if (phi - ls[2] <= p.eta * ls[1]) ls[3] = 1.0;
+        else if (p.KT == 1) { fail = MPXG_INST_LS_FAIL; ls[3] = 1.0; }
+        else go = 0;  // pass 1 decides
+      }
+    } else if (ls[3] != 0.0) {
+      go = 0;  // decided in pass 0
+    } else {
       bool ok = false;
       double a = 1.0;
-      for (int k = 0; k < p.KT; ++k) {
+      for (int k = 1; k < p.KT; ++k) {
+        a *= p.beta;
         double phi = 0.0;
         const double* tr = p.trial + ((size_t)b * p.KT + k) * N1;
         for (int t = 0; t < N1; ++t) phi += tr[t];
@@ -718,15 +749,17 @@ __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__
           ok = true;
           break;
         }
-        if (k + 1 < p.KT) a *= p.beta;
       }
       al = a;
       fail = ok ? 0 : MPXG_INST_LS_FAIL;
+      ls[3] = 1.0;
     }
     s_al = al;
     s_bad = fail;
+    s_go = go;
   }
   __syncthreads();
+  if (!s_go) return;
   const double al = s_al;
   const WbDims& d = p.d;
   const size_t nX = (size_t)N1 * d.nx, nU = (size_t)p.N * d.nj;
@@ -920,12 +953,10 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
   if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: riccati attribute");
   const long long jac_items = (long long)B * N * (d.nz + d.nj);
   const long long quad_items = (long long)B * (N + 1);
-  const unsigned nom_blocks = (unsigned)(((long long)B * N + kNW - 1) / kNW);
-  const unsigned jac_blocks = (unsigned)((jac_items + kNW - 1) / kNW);
+  const unsigned lin_blocks = (unsigned)(((long long)B * N + kNW - 1) / kNW + (jac_items + kNW - 1) / kNW);
   const unsigned quad_blocks = (unsigned)((quad_items + 3) / 4);
   auto linearise = [&]() -> cudaError_t {
-    wb_nominal_kernel<<<nom_blocks, 32 * kNW, 0, st>>>(m, p);
-    wb_jac_kernel<<<jac_blocks, 32 * kNW, 0, st>>>(m, p);
+    wb_lin_kernel<<<lin_blocks, 32 * kNW, 0, st>>>(m, p);
     wb_quad_kernel<<<quad_blocks, 128, 0, st>>>(p);
     return cudaGetLastError();
   };
@@ -938,9 +969,17 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
     if ((e = linearise()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: linearisation");
     wb_riccati_kernel<kNX, kNU><<<B, lqeq::kThreads, rsmem, st>>>(lq, p.Pscr);
     wb_merit_kernel<<<B, kBlk, 0, st>>>(p);
-    const long long tr_items = (long long)B * p.KT * (N + 1);
-    wb_trial_kernel<<<(unsigned)((tr_items + kNW - 1) / kNW), 32 * kNW, 0, st>>>(m, p);
+    // the full step first; the shorter steps only for instances that reject it
+    p.k_lo = 0; p.k_hi = 1; p.phase = 0;
+    const long long tr0 = (long long)B * (N + 1);
+    wb_trial_kernel<<<(unsigned)((tr0 + kNW - 1) / kNW), 32 * kNW, 0, st>>>(m, p);
     wb_accept_kernel<<<B, kBlk, 0, st>>>(p);
+    if (p.KT > 1) {
+      p.k_lo = 1; p.k_hi = p.KT; p.phase = 1;
+      const long long tr1 = (long long)B * (p.KT - 1) * (N + 1);
+      wb_trial_kernel<<<(unsigned)((tr1 + kNW - 1) / kNW), 32 * kNW, 0, st>>>(m, p);
+      wb_accept_kernel<<<B, kBlk, 0, st>>>(p);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: iteration");
   }
   if (io->kkt) {
