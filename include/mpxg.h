@@ -139,7 +139,10 @@ typedef struct {
   int* status;
   float* first;            /* optional [batch, m+4], indexed by batch entry b (not by slot):
                               first control U[0], kkt[3], status -- the per-tick result
-                              a controller reads back */
+                              a controller reads back.  Each row's status entry is written
+                              last, after a system-scope fence, so `first` may point into
+                              mapped host memory and a reader may take a row as complete
+                              once its status entry changes */
 } mpxg_batch_io;
 
 typedef struct mpxg_handle mpxg_handle;

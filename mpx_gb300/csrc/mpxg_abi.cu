@@ -46,6 +46,13 @@ struct mpxg_handle {
   cudaEvent_t ring_ev[kRing] = {};
   bool ring_used[kRing] = {};
   int ring_next = 0, capture_next = 0;
+  // With the team path: the team kernel of a solve runs on a side stream,
+  // forked from the solve's stream after the ordering kernel and joined
+  // before the solve's end, so that it overlaps the one-warp kernel (ring
+  // entry r forks and joins with its own events; side stream r % kSide).
+  static constexpr int kSide = 32;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork_ev[2 * kRing] = {}, join_ev[2 * kRing] = {};
   ModelConst mc;
   SqpParams sp;
   std::string err;
@@ -195,6 +202,19 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
       return fail(nullptr, MPXG_ERR_CUDA, "mpxg_create: cudaEventCreate failed");
     }
   }
+  if (h->team_blocks > 0) {
+    bool ok = true;
+    for (int i = 0; i < mpxg_handle::kSide && ok; ++i)
+      ok = cudaStreamCreateWithFlags(&h->side[i], cudaStreamNonBlocking) == cudaSuccess;
+    for (int i = 0; i < 2 * mpxg_handle::kRing && ok; ++i)
+      ok = cudaEventCreateWithFlags(&h->fork_ev[i], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&h->join_ev[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      mpxg_destroy(h);
+      return fail(nullptr, MPXG_ERR_CUDA, "mpxg_create: side stream or event creation failed");
+    }
+  }
   e = cudaMemset(h->slot_bits, 0, nwords * 4 + 256);
   if (e == cudaSuccess) e = cudaMemset(h->counters, 0, ctr_bytes);
   if (e != cudaSuccess) { mpxg_destroy(h); return cuda_fail(nullptr, e, "mpxg_create: cudaMemset"); }
@@ -223,6 +243,12 @@ void mpxg_destroy(mpxg_handle* h) {
   if (h->orders) cudaFree(h->orders);
   for (int i = 0; i < mpxg_handle::kRing; ++i)
     if (h->ring_ev[i]) cudaEventDestroy(h->ring_ev[i]);
+  for (int i = 0; i < 2 * mpxg_handle::kRing; ++i) {
+    if (h->fork_ev[i]) cudaEventDestroy(h->fork_ev[i]);
+    if (h->join_ev[i]) cudaEventDestroy(h->join_ev[i]);
+  }
+  for (int i = 0; i < mpxg_handle::kSide; ++i)
+    if (h->side[i]) cudaStreamDestroy(h->side[i]);
   delete h;
 }
 
@@ -299,12 +325,25 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
     if (e != cudaSuccess) return cuda_fail(h, e, "order_by_horizon_kernel launch");
     bp.order = order;
   }
+  bool joined = true;
   if (team) {
     BatchPtrs tb = bp;
     tb.split = io->horizon ? bp.counter + 2 : nullptr;  // no horizons: every instance has n_max >= the minimum
     const int blocks = std::min(io->batch, h->team_blocks);
-    e = sqp_ops(h->desc.model)->launch_team(h->mc, h->sp, tb, blocks, st);
+    cudaStream_t ts = st;
+    if (io->horizon) {  // both kernels may have work: the team kernel on a side stream, overlapping
+      ts = h->side[r % mpxg_handle::kSide];
+      e = cudaEventRecord(h->fork_ev[r], st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ts, h->fork_ev[r], 0);
+      if (e != cudaSuccess) return cuda_fail(h, e, "mpxg_solve: fork");
+      joined = false;
+    }
+    e = sqp_ops(h->desc.model)->launch_team(h->mc, h->sp, tb, blocks, ts);
     if (e != cudaSuccess) return cuda_fail(h, e, "sqp_team_kernel launch");
+    if (!joined) {
+      e = cudaEventRecord(h->join_ev[r], ts);
+      if (e != cudaSuccess) return cuda_fail(h, e, "mpxg_solve: join");
+    }
     if (!io->horizon) {  // every instance went to the team kernel
       if (!eager) return MPXG_OK;
       e = cudaEventRecord(h->ring_ev[r], st);
@@ -321,6 +360,10 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
   const int need = (io->batch + wpb - 1) / wpb;
   if (need < blocks) blocks = need;
   mpxg_status s2 = dispatch(h, st, bp, blocks, wpb, tput);
+  if (!joined) {  // the solve ends when both kernels have
+    e = cudaStreamWaitEvent(st, h->join_ev[r], 0);
+    if (e != cudaSuccess) return cuda_fail(h, e, "mpxg_solve: join wait");
+  }
   if (s2 != MPXG_OK || !eager) return s2;
   e = cudaEventRecord(h->ring_ev[r], st);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");

@@ -20,8 +20,8 @@ namespace mpxg_srv {
 struct Staging {
   int* slot_h = nullptr;   // pinned: [batch slots | warm slots | cold slots]
   int* slot_d = nullptr;
-  float* res_h = nullptr;  // pinned result rows [cap, m+4]
-  float* res_d = nullptr;
+  float* res_h = nullptr;  // mapped pinned result rows [cap, m+4], written by the solve kernels
+  float* res_d = nullptr;  // the device address of res_h
   cudaEvent_t ev = nullptr;
 };
 
@@ -55,6 +55,10 @@ struct Part {
   int model = 0;
   Staging* st = nullptr;
   std::vector<long long> tickets;
+  std::vector<char> got;     // ticket i's result row already delivered
+  std::vector<int> episode;  // ticket i's episode, and its result status once delivered (a
+  std::vector<int> status;   // delivered ticket may be consumed by the client before the reap)
+  size_t next = 0;           // rows before this one are all delivered
 };
 struct Batch {
   int stream = 0;
@@ -124,7 +128,6 @@ inline void free_pool(Pool& p) {
     cudaFreeHost(st->slot_h);
     cudaFree(st->slot_d);
     cudaFreeHost(st->res_h);
-    cudaFree(st->res_d);
     cudaEventDestroy(st->ev);
     delete st;
   }
@@ -143,14 +146,14 @@ inline Staging* get_staging(mpxg_server* s, Pool& p) {
   const size_t rows = (size_t)p.cap * (p.mu + 4) * sizeof(float);
   if (cudaMallocHost(&st->slot_h, 3 * (size_t)p.cap * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&st->slot_d, 3 * (size_t)p.cap * sizeof(int)) != cudaSuccess ||
-      cudaMallocHost(&st->res_h, rows) != cudaSuccess || cudaMalloc(&st->res_d, rows) != cudaSuccess ||
+      cudaHostAlloc((void**)&st->res_h, rows, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&st->res_d, st->res_h, 0) != cudaSuccess ||
       cudaEventCreateWithFlags(&st->ev, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     s->err = "server: staging allocation failed";
     if (st->slot_h) cudaFreeHost(st->slot_h);
     if (st->slot_d) cudaFree(st->slot_d);
     if (st->res_h) cudaFreeHost(st->res_h);
-    if (st->res_d) cudaFree(st->res_d);
     delete st;
     return nullptr;
   }
@@ -220,6 +223,9 @@ inline mpxg_status prepare_part(mpxg_server* s, Part& part, cudaStream_t stream,
     r = mpxg_gait_tables(stream, &a);
     if (r != MPXG_OK) return fail(s, r, std::string("server: gait tables: ") + mpxg_last_error(nullptr));
   }
+  // the rows' status entries read "not yet written" until the kernel writes them
+  for (int i = 0; i < nb; ++i) st->res_h[(size_t)i * (p.mu + 4) + p.mu + 3] = std::nanf("");
+  __atomic_thread_fence(__ATOMIC_SEQ_CST);  // visible before the launch that overwrites them
   std::memset(io, 0, sizeof(*io));
   io->batch = nb; io->slot = st->slot_d; io->horizon = p.horizon;
   io->x0 = p.x0; io->X_in = p.X; io->U_in = p.U; io->V_in = p.V;
@@ -255,14 +261,17 @@ inline mpxg_status launch(mpxg_server* s, std::vector<Part> parts) {
     if (r != MPXG_OK) return fail(s, r, std::string("server: solve: ") + mpxg_last_error(p.h));
     s->launches += io[0].batch > p.total_warps ? 2 : 1;
   }
-  for (size_t k = 0; k < parts.size(); ++k) {
-    const Pool& p = s->pools[parts[k].model];
-    cudaError_t ce = cudaMemcpyAsync(parts[k].st->res_h, parts[k].st->res_d, (size_t)io[k].batch * (p.mu + 4) * sizeof(float),
-                                     cudaMemcpyDeviceToHost, stream);
-    if (ce != cudaSuccess) return cuda_err(s, ce, "server: result copy");
-  }
+  // the result rows arrive in mapped host memory as each instance finishes;
+  // the event marks the batch's end (its warm starts written, its streams free)
   cudaError_t ce = cudaEventRecord(parts[0].st->ev, stream);
-  if (ce != cudaSuccess) return cuda_err(s, ce, "server: result copy");
+  if (ce != cudaSuccess) return cuda_err(s, ce, "server: event");
+  for (Part& part : parts) {
+    part.got.assign(part.tickets.size(), 0);
+    part.status.assign(part.tickets.size(), 0);
+    part.episode.resize(part.tickets.size());
+    for (size_t i = 0; i < part.tickets.size(); ++i) part.episode[i] = s->tickets[part.tickets[i]].episode;
+    part.next = 0;
+  }
   Batch b;
   b.stream = si;
   s->stream_busy[si] = 1;
@@ -280,6 +289,48 @@ inline void retire(mpxg_server* s, int episode) {
 }
 
 // Reap running batch i (its event has completed).
+// Deliver ticket i of a part from its result row (in mapped host memory).
+inline void deliver(mpxg_server* s, Part& part, size_t i) {
+  const Pool& p = s->pools[part.model];
+  Ticket& t = s->tickets[part.tickets[i]];
+  const float* row = part.st->res_h + i * (p.mu + 4);
+  t.res.ticket = part.tickets[i];
+  t.res.episode = t.episode;
+  for (int a = 0; a < 12; ++a) t.res.u0[a] = a < p.mu ? row[a] : 0.0f;
+  for (int k = 0; k < 3; ++k) t.res.kkt[k] = row[p.mu + k];
+  const float sv = row[p.mu + 3];
+  t.res.status = sv == sv ? (int)sv : MPXG_INST_NAN;  // a row the solve never wrote reads as failed
+  t.done = true;
+  s->done.push_back(part.tickets[i]);
+  part.got[i] = 1;
+  part.status[i] = t.res.status;
+}
+
+// Deliver the rows of running batches that have arrived: a row whose status
+// entry is no longer the NaN written before the launch (the kernel writes it
+// last, after a system-scope fence; the acquire load orders the reads of the
+// row's other entries after it).  The episodes stay claimed until the batch
+// is reaped, when its warm starts are complete on the device.
+inline int deliver_arrived(mpxg_server* s) {
+  int n = 0;
+  for (Batch& b : s->inflight)
+    for (Part& part : b.parts) {
+      const Pool& p = s->pools[part.model];
+      for (size_t i = part.next; i < part.tickets.size(); ++i) {
+        if (part.got[i]) continue;
+        const unsigned* w = reinterpret_cast<const unsigned*>(part.st->res_h + i * (p.mu + 4) + p.mu + 3);
+        const unsigned bits = __atomic_load_n(w, __ATOMIC_ACQUIRE);
+        float v;
+        std::memcpy(&v, &bits, sizeof(v));
+        if (v != v) continue;  // not written yet
+        deliver(s, part, i);
+        ++n;
+      }
+      while (part.next < part.tickets.size() && part.got[part.next]) ++part.next;
+    }
+  return n;
+}
+
 inline void reap(mpxg_server* s, size_t i) {
   Batch b = std::move(s->inflight[i]);
   s->inflight.erase(s->inflight.begin() + i);
@@ -287,21 +338,13 @@ inline void reap(mpxg_server* s, size_t i) {
   for (Part& part : b.parts) {
   Pool& p = s->pools[part.model];
   for (size_t i = 0; i < part.tickets.size(); ++i) {
-    Ticket& t = s->tickets[part.tickets[i]];
-    const float* row = part.st->res_h + i * (p.mu + 4);
-    t.res.ticket = part.tickets[i];
-    t.res.episode = t.episode;
-    for (int a = 0; a < 12; ++a) t.res.u0[a] = a < p.mu ? row[a] : 0.0f;
-    for (int k = 0; k < 3; ++k) t.res.kkt[k] = row[p.mu + k];
-    t.res.status = (int)row[p.mu + 3];
-    t.done = true;
-    s->done.push_back(part.tickets[i]);
-    auto it = s->eps.find(t.episode);
+    if (!part.got[i]) deliver(s, part, i);
+    auto it = s->eps.find(part.episode[i]);
     if (it != s->eps.end()) {
       Episode& e = it->second;
-      if (t.res.status & MPXG_INST_NAN) e.cold = true;  // NaN fallback: cold start next tick
+      if (part.status[i] & MPXG_INST_NAN) e.cold = true;  // NaN fallback: cold start next tick
       e.running = false;
-      if (--e.busy == 0 && e.retiring) retire(s, t.episode);
+      if (--e.busy == 0 && e.retiring) retire(s, part.episode[i]);
     }
   }
   p.idle.push_back(part.st);
@@ -521,11 +564,13 @@ mpxg_status mpxg_server_step(mpxg_server* s, int block, int* launched, int* fini
     cudaError_t e = cudaEventSynchronize(s->inflight.front().ev());
     if (e != cudaSuccess) return cuda_err(s, e, "mpxg_server_step");
   }
+  nfin += deliver_arrived(s);  // results of instances that finished, before their batch ends
   for (size_t i = 0; i < s->inflight.size();) {  // collect every finished batch, in any order
     cudaError_t e = cudaEventQuery(s->inflight[i].ev());
     if (e == cudaErrorNotReady) { ++i; continue; }
     if (e != cudaSuccess) return cuda_err(s, e, "mpxg_server_step");
-    for (const auto& part : s->inflight[i].parts) nfin += (int)part.tickets.size();
+    for (const auto& part : s->inflight[i].parts)
+      for (char g : part.got) nfin += g ? 0 : 1;
     reap(s, i);
   }
   // the idle episodes' pending tickets of pool mi (claimed for a batch)

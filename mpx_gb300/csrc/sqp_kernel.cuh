@@ -1127,9 +1127,13 @@ __device__ void solve_instance(const ModelConst& mc, const SqpParams& sp, const 
   if (bp.first) {
     float* f = bp.first + (size_t)bidx * (NU + 4);
     if (lane < NU) f[lane] = U[lane];
+    if (lane == 0 && !(bp.kkt && sp.compute_kkt)) { f[NU] = 0.0f; f[NU + 1] = 0.0f; f[NU + 2] = 0.0f; }
+    __syncwarp();
     if (lane == 0) {
-      f[NU + 3] = (float)status;
-      if (!(bp.kkt && sp.compute_kkt)) { f[NU] = 0.0f; f[NU + 1] = 0.0f; f[NU + 2] = 0.0f; }
+      // the row's other entries, then its status word: a reader of a row in
+      // mapped host memory takes a written status word as the row's arrival
+      __threadfence_system();
+      *(volatile float*)(f + NU + 3) = (float)status;
     }
   }
   (void)LD;

@@ -385,7 +385,11 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     if (lane < NU) f[lane] = U[lane];
     if (lane == 0) {
       f[NU] = kk[0]; f[NU + 1] = kk[1]; f[NU + 2] = kk[2];
-      f[NU + 3] = (float)st;
+    }
+    __syncwarp();
+    if (lane == 0) {  // the status word last (see sqp_kernel.cuh)
+      __threadfence_system();
+      *(volatile float*)(f + NU + 3) = (float)st;
     }
   }
   __syncthreads();  // the block's shared memory is reused by its next instance
