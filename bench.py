@@ -832,7 +832,7 @@ def other_configs(args, rank, world, local_rank):
     a.steps = 10
     ws = run_wb_sqp(a, rank, world, local_rank, emit=False)
     out["wb_sqp_aliengo_N25"] = {"metric": ws["metric"], "value": ws["value"], "ms_per_step": ws["ms_per_step"],
-                                 "lone": ws["lone"], "batch": ws["batch"]}
+                                 "lone": ws["lone"], "batch": ws["batch"], "wrapper": ws["wrapper"]}
     return out
 
 
@@ -1291,6 +1291,32 @@ def run_wb_sqp(args, rank, world, local_rank, emit=True):
                       "solves_per_s": B / (float(np.mean(t)) / 1000.0),
                       "kkt_frac_le_1e-5": float(np.mean(kk <= 1e-5)), "kkt_median": float(np.median(kk)),
                       "ticks": len(times)}
+    # the drop-in controller end to end: MPCControllerWrapper(config_aliengo).run(qpos, qvel, input,
+    # contact) from host arrays to (tau, q, dq) on the host -- feet by forward kinematics, timer,
+    # reference generator, solve, shift (mpc_wrapper.py:297-365)
+    from mpx_gb300.mpc_wrapper import MPCControllerWrapper
+    ctrl = MPCControllerWrapper(cfg, model=model, device=dev)
+    rng = np.random.default_rng(5 + rank)
+    qpos = np.concatenate([cfg.p0 + rng.normal(0, 0.01, 3), [1.0, 0.0, 0.0, 0.0], cfg.q0]).astype(np.float32)
+    qvel = rng.normal(0, 0.05, 18).astype(np.float32)
+    inp = np.array([0.3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0], dtype=np.float32)
+    cont = np.ones(4, dtype=np.float32)
+    import contextlib
+    with contextlib.redirect_stdout(sys.stderr):  # reset() prints as the reference's does
+        ctrl.reset(qpos, qvel)
+    wt = []
+    for tick in range(max(args.warmup, 3) + steps):
+        t0 = time.perf_counter()
+        tau, q, dq = ctrl.run(qpos, qvel, inp, cont)
+        t1 = time.perf_counter()
+        if tick >= max(args.warmup, 3):
+            wt.append((t1 - t0) * 1e3)
+    wt = np.array(wt)
+    res["wrapper"] = {"what": "MPCControllerWrapper(config_aliengo).run(qpos, qvel, input, contact) -> (tau, q, dq), "
+                              "host numpy in and out, wall clock per call",
+                      "ms_p50": float(np.percentile(wt, 50)), "ms_p99": float(np.percentile(wt, 99)),
+                      "h2d_bytes_per_step": int(qpos.nbytes + qvel.nbytes + inp.nbytes + cont.nbytes),
+                      "d2h_bytes_per_step": int(3 * 12 * 4), "finite": bool(np.all(np.isfinite(tau)))}
     clk = clocks.stop()
     ms = max_over_ranks(res["batch"]["ms_p50"], device=dev)
     line = {
@@ -1301,7 +1327,7 @@ def run_wb_sqp(args, rank, world, local_rank, emit=True):
         "data": "synthetic (seeded trotting references and perturbed standing states)",
         "config": {"workload": "%d aliengo whole-body MPCs, N = %d, %d SQP iterations per warm tick" % (Bb, N, WBS_ITERS),
                    "parallelism": "replicas"},
-        "lone": res["lone"], "batch": res["batch"],
+        "lone": res["lone"], "batch": res["batch"], "wrapper": res["wrapper"],
         "gpu_launches": (8 * WBS_ITERS + 4) * steps,
         "clocks": clk,
     }

@@ -102,7 +102,7 @@ namespace {
 // (the float64 per-warp state is ~15 KB)
 using WbCap = wb::Cap<16, 20, 4, 2, 1>;
 constexpr int kNW = WbCap::NW;
-constexpr int kNX = 61, kNU = 12;   // the built Riccati size (nv = 18, 4 contacts)
+constexpr int kNX = 61, kNU = 12, kNZ = 37;  // the built Riccati size (nv = 18, 4 contacts); kNZ = nq + nv
 constexpr int kMaxX = 64, kMaxU = 16, kMaxRef = 64, kMaxW = 80, kMaxC = 4, kMaxTrials = 8;
 
 struct WbDims {
@@ -519,12 +519,16 @@ struct RLay {
 };
 
 // Riccati sweep of the step problem x_{t+1} = A x + B u + c (x_0 = c_0),
-// cost 1/2 x'Qx + 1/2 u'Ru + q'x + r'u (M = 0 is read but adds nothing):
+// cost 1/2 x'Qx + x'Mu + 1/2 u'Ru + q'x + r'u:
 //   Q_xx = Q + A'PA, Q_ux = M' + B'PA, Q_uu = R + B'PB, q_x = q + A'(Pc + p),
 //   q_u = r + B'(Pc + p), [Z | g] = Q_uu^-1 [Q_ux | q_u], K = -Z, k = -g,
 //   P <- Q_xx - Q_ux'Z (symmetrised), p <- q_x + Q_ux'k;
-// then dX, dU by the forward sweep and lam_t = P_t dX_t + p_t.
-template <int NX, int NU>
+// then dX, dU by the forward sweep and lam_t = P_t dX_t + p_t.  Columns
+// NZ..NX-1 of every A_t are zero (the whole-body step does not read the
+// contact-point and force states): P A, A'(P A), B'(P A) and A'w are formed
+// over the first NZ columns only, and the rest of Q_xx, Q_ux and q_x is
+// Q, M' and q.
+template <int NX, int NU, int NZ>
 __global__ void __launch_bounds__(lqeq::kThreads, 1) wb_riccati_kernel(mpxg_lq_eq_io io, float* Pscr) {
   using namespace lqeq;
   typedef RLay<NX, NU> L;
@@ -556,14 +560,20 @@ __global__ void __launch_bounds__(lqeq::kThreads, 1) wb_riccati_kernel(mpxg_lq_e
     load_vec<NX>(vq, io.q + (sn1 + t) * NX);
     load_vec<NU>(vr, io.r + (sn + t) * NU);
     __syncthreads();
-    bmm<NX, NX, NX, false, false, false>(PA, LX, P, LX, sA, LX, 1.0f, nullptr, 0);
+    bmm<NX, NX, NZ, false, false, false>(PA, LX, P, LX, sA, LX, 1.0f, nullptr, 0);
     bmm<NX, NX, NU, false, false, false>(PB, LX, P, LX, sB, LX, 1.0f, nullptr, 0);
     bmv<NX, NX, false>(vw, P, LX, vc, 1.0f, vp);
-    bmm<NX, NX, NX, true, false, false>(sQ, LX, sA, LX, PA, LX, 1.0f, sQ, LX);    // Q_xx
-    bmm<NU, NX, NX, true, false, true>(Qux, LU, sB, LX, PA, LX, 1.0f, sM, LX);    // Q_ux
+    bmm<NZ, NX, NZ, true, false, false>(sQ, LX, sA, LX, PA, LX, 1.0f, sQ, LX);    // Q_xx (its A-block)
+    bmm<NU, NX, NZ, true, false, true>(Qux, LU, sB, LX, PA, LX, 1.0f, sM, LX);    // Q_ux (its A-columns)
+    for (int e = threadIdx.x; e < NU * (NX - NZ); e += kThreads) {                // Q_ux = M' elsewhere
+      const int a = e % NU, i = NZ + e / NU;
+      Qux[i * LU + a] = sM[a * LX + i];
+    }
     bmm<NU, NX, NU, true, false, false>(Quu, LU, sB, LX, PB, LX, 1.0f, Quu, LU);  // Q_uu
-    bmv<NX, NX, true>(vqx, sA, LX, vw, 1.0f, vq);                                 // q_x
+    bmv<NZ, NX, true>(vqx, sA, LX, vw, 1.0f, vq);                                 // q_x (A-part)
+    for (int i = NZ + threadIdx.x; i < NX; i += kThreads) vqx[i] = vq[i];          // q_x = q elsewhere
     bmv<NU, NX, true>(vqu, sB, LX, vw, 1.0f, vr);                                 // q_u
+    __syncthreads();
     gj_solve<NU, NU + NX + 1, kGjBlock>(pan, [&](int j, float* v) {
 #pragma unroll
       for (int i = 0; i < NU; ++i)
@@ -948,7 +958,7 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
 
   cudaStream_t st = (cudaStream_t)stream;
   const size_t rsmem = (size_t)RLay<kNX, kNU>::FLOATS * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(wb_riccati_kernel<kNX, kNU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(wb_riccati_kernel<kNX, kNU, kNZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)rsmem);
   if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: riccati attribute");
   const long long jac_items = (long long)B * N * (d.nz + d.nj);
@@ -967,7 +977,7 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
   for (int it = 0; it < io->iters; ++it) {
     p.first = it == 0;
     if ((e = linearise()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: linearisation");
-    wb_riccati_kernel<kNX, kNU><<<B, lqeq::kThreads, rsmem, st>>>(lq, p.Pscr);
+    wb_riccati_kernel<kNX, kNU, kNZ><<<B, lqeq::kThreads, rsmem, st>>>(lq, p.Pscr);
     wb_merit_kernel<<<B, kBlk, 0, st>>>(p);
     // the full step first; the shorter steps only for instances that reject it
     p.k_lo = 0; p.k_hi = 1; p.phase = 0;

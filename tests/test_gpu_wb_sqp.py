@@ -114,3 +114,17 @@ def test_warm_tick_iteration_matches_oracle(cuda):
         assert got["status"][b] == r["status"], b
         for k in ("X", "U", "V"):
             assert rel_err(got[k][b], r[k]) < 2e-4, (b, k, rel_err(got[k][b], r[k]))
+
+
+def test_benchmarked_size_iteration_matches_oracle(cuda):
+    """The benchmarked size (aliengo, N = 25, config_aliengo's horizon): one
+    iteration from the cold start against the oracle's."""
+    B, N = 1, 25
+    model, cfg, wl = setup(B, N, seed=11)
+    sqp = WholeBodySQP(WholeBodyModel(model, device=cuda), N=N, batch_max=B)
+    args = [wl[k] for k in ("x0", "X0", "U0", "V0", "reference", "contact")]
+    got = {k: v.cpu().numpy() for k, v in sqp.solve(*args, cfg.W_diag, iters=1).items()}
+    _, _, res = oracle_iters(model, cfg, wl, 0, 1)
+    assert got["status"][0] == res[0]["status"]
+    for k in ("X", "U", "V"):
+        assert rel_err(got[k][0], res[0][k]) < 2e-4, (k, rel_err(got[k][0], res[0][k]))
