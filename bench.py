@@ -793,7 +793,7 @@ def run_ours(args, rank, world, local_rank):
                      "warps_per_instance": tuned["best"][2] or 1, "team_min_horizon": tuned["best"][3]},
             "cached": tuned["cached"],
             "ms_per_solve": {("%dx%s" % (r["wpb"], r["bps"] or "auto")) +
-                             (" team8>=%d" % r["team_min_horizon"] if r.get("team_warps") else ""): r.get("ms")
+                             (" team%d>=%d" % (r["team_warps"], r["team_min_horizon"]) if r.get("team_warps") else ""): r.get("ms")
                              for r in tuned["table"]}},
     }
     if not args.no_other and not args.profile:

@@ -102,11 +102,11 @@ typedef struct {
   int compute_kkt;     /* 1: evaluate the KKT residual of the result */
   int warps_per_block; /* 0: default (4); at most 4 */
   int blocks_per_sm;   /* 0: default (tuned) */
-  int team_warps;      /* 0 or 1: one warp per instance; 8: instances whose horizon is at
-                          least team_min_horizon are solved by a block of 8 warps each, the
-                          KKT step split over the horizon (time-parallel Riccati and forward
-                          sweeps); the choice depends on the horizon only, so a result does
-                          not depend on the rest of its batch */
+  int team_warps;      /* 0 or 1: one warp per instance; 4 or 8: instances whose horizon is
+                          at least team_min_horizon are solved by a block of 4 or 8 warps each,
+                          the KKT step split over the horizon in as many chunks (time-parallel
+                          Riccati and forward sweeps); the choice depends on the horizon only,
+                          so a result does not depend on the rest of its batch */
   int team_min_horizon;
 } mpxg_solver_opts;
 

@@ -23,7 +23,7 @@ from .solver import Solver
 
 # (warps per block, blocks per SM, warps per instance, team threshold); 0 = default
 DEFAULT_CANDIDATES = ([(wpb, bps, 0, 0) for wpb in (1, 2, 4) for bps in (0, 2, 3, 4)] +
-                      [(4, 0, 8, tmin) for tmin in (32, 64, 128)])
+                      [(4, 0, tw, tmin) for tw in (4, 8) for tmin in (32, 64, 128)])
 
 
 def _full(c):

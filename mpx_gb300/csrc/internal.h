@@ -26,9 +26,9 @@ struct SqpOps {
                         bool tput, cudaStream_t st);
   cudaError_t (*launch_vjp)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks, int wpb,
                             cudaStream_t st);
-  // time-parallel team kernel, W warps per instance (W = 8); occupancy of it
-  int (*team_resident_blocks)();
-  cudaError_t (*launch_team)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks,
+  // time-parallel team kernel, `warps` (4 or 8) warps per instance; occupancy of it
+  int (*team_resident_blocks)(int warps);
+  cudaError_t (*launch_team)(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks, int warps,
                              cudaStream_t st);
   cudaError_t (*launch_evaluate)(const ModelConst& mc, int batch, int n_max, const int* horizon, const float* x0,
                                  const float* X, const float* U, const float* reference, const float* parameter,

@@ -30,7 +30,8 @@ struct mpxg_handle {
   int num_sms = 0;
   int warps_per_block = 0, blocks_per_sm = 0, total_warps = 0;  // throughput variant (large batches)
   int blocks_per_sm_lat = 0;                                     // latency variant
-  int team_blocks = 0;                 // team kernel: resident blocks of 8 warps (0: no team path)
+  int team_blocks = 0;                 // team kernel: resident blocks (0: no team path)
+  int team_warps = 0;                  // warps (horizon chunks) per team instance: 4 or 8
   int team_min_horizon = 0;
   long long scratch_stride = 0;
   int n_slots = 0;                     // scratch slots: most warps resident at once
@@ -165,8 +166,10 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (o->sqp_iters < 0 || o->ls_max_trials < 1) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: bad options");
   if (o->warps_per_block < 0 || o->warps_per_block > 4 || o->blocks_per_sm < 0)
     return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: warps_per_block must be 0..4 (128-thread blocks)");
-  if (!(o->team_warps == 0 || o->team_warps == 1 || o->team_warps == 8) || o->team_min_horizon < 0)
-    return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: team_warps must be 0, 1 or 8 and team_min_horizon >= 0");
+  if (!(o->team_warps == 0 || o->team_warps == 1 || o->team_warps == 4 || o->team_warps == 8) ||
+      o->team_min_horizon < 0)
+    return fail(nullptr, MPXG_ERR_INVALID_ARG,
+                "mpxg_create: team_warps must be 0, 1, 4 or 8 and team_min_horizon >= 0");
   if (!(d->dt > 0.0f) || !(d->mass > 0.0f)) return fail(nullptr, MPXG_ERR_INVALID_ARG, "mpxg_create: dt and mass must be > 0");
   mpxg_handle* h = new mpxg_handle();
   h->desc = *d;
@@ -177,10 +180,11 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   if (e != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaDeviceGetAttribute"); }
   launch_geometry(d, o, &h->warps_per_block, &h->blocks_per_sm, &h->blocks_per_sm_lat);
   h->total_warps = h->num_sms * h->blocks_per_sm * h->warps_per_block;
-  if (o->team_warps == 8) {
-    // the team kernel needs at least 8 stages (one per warp)
-    h->team_min_horizon = std::max(o->team_min_horizon, 8);
-    h->team_blocks = h->num_sms * sqp_ops(d->model)->team_resident_blocks();
+  if (o->team_warps == 4 || o->team_warps == 8) {
+    // the team kernel needs at least one stage per warp
+    h->team_warps = o->team_warps;
+    h->team_min_horizon = std::max(o->team_min_horizon, o->team_warps);
+    h->team_blocks = h->num_sms * sqp_ops(d->model)->team_resident_blocks(o->team_warps);
   }
   h->scratch_stride = scratch_stride_for(d->model, d->n_max);
   h->n_slots = scratch_slots(d->model, h->warps_per_block, h->num_sms);
@@ -338,7 +342,7 @@ mpxg_status mpxg_solve(mpxg_handle* h, void* stream, const mpxg_batch_io* io) {
       if (e != cudaSuccess) return cuda_fail(h, e, "mpxg_solve: fork");
       joined = false;
     }
-    e = sqp_ops(h->desc.model)->launch_team(h->mc, h->sp, tb, blocks, ts);
+    e = sqp_ops(h->desc.model)->launch_team(h->mc, h->sp, tb, blocks, h->team_warps, ts);
     if (e != cudaSuccess) return cuda_fail(h, e, "sqp_team_kernel launch");
     if (!joined) {
       e = cudaEventRecord(h->join_ev[r], ts);

@@ -52,28 +52,35 @@ struct SqpLaunch {
     sqp_vjp_kernel<M><<<blocks, wpb * 32, smem, st>>>(mc, sp, bp);
     return cudaGetLastError();
   }
-  static constexpr int kTeamWarps = 8;
-  static int team_resident_blocks() {
+  // Team kernels of 8 and 4 warps per instance (the horizon in 8 or 4 chunks).
+  template <int W>
+  static int team_blocks_w() {
     int nb = 0;
-    const size_t smem = sizeof(TeamSmem<M, kTeamWarps>);
-    auto fn = sqp_team_kernel<M, kTeamWarps>;
+    const size_t smem = sizeof(TeamSmem<M, W>);
+    auto fn = sqp_team_kernel<M, W>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kTeamWarps, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * W, smem) != cudaSuccess) {
       cudaGetLastError();
       return 1;
     }
     return nb > 0 ? nb : 1;
   }
-  static cudaError_t launch_team(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks,
-                                 cudaStream_t st) {
-    const size_t smem = sizeof(TeamSmem<M, kTeamWarps>);
-    auto fn = sqp_team_kernel<M, kTeamWarps>;
+  static int team_resident_blocks(int warps) { return warps == 4 ? team_blocks_w<4>() : team_blocks_w<8>(); }
+  template <int W>
+  static cudaError_t launch_team_w(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks,
+                                   cudaStream_t st) {
+    const size_t smem = sizeof(TeamSmem<M, W>);
+    auto fn = sqp_team_kernel<M, W>;
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    fn<<<blocks, 32 * kTeamWarps, smem, st>>>(mc, sp, bp);
+    fn<<<blocks, 32 * W, smem, st>>>(mc, sp, bp);
     return cudaGetLastError();
+  }
+  static cudaError_t launch_team(const ModelConst& mc, const SqpParams& sp, const BatchPtrs& bp, int blocks,
+                                 int warps, cudaStream_t st) {
+    return warps == 4 ? launch_team_w<4>(mc, sp, bp, blocks, st) : launch_team_w<8>(mc, sp, bp, blocks, st);
   }
   static cudaError_t launch_evaluate(const ModelConst& mc, int batch, int n_max, const int* horizon, const float* x0,
                                      const float* X, const float* U, const float* reference, const float* parameter,

@@ -89,7 +89,7 @@ class SolverOptions:
     rho0: float = 1.0           # initial augmented-Lagrangian penalty
     ls_skip_tol: float = 1e-7   # |predicted merit change| below this x (1+|merit|): take the full step
     compute_kkt: bool = True    # evaluate the KKT residual of the result on the device
-    team_warps: int = 0         # 8: horizons >= team_min_horizon are solved time-parallel by 8 warps each
+    team_warps: int = 0         # 4 or 8: horizons >= team_min_horizon are solved time-parallel by 4 or 8 warps each
     team_min_horizon: int = 64
 
 

@@ -146,7 +146,8 @@ class Solver:
         """Kernel launches of one mpxg_solve: the solve, the longest-first
         ordering when needed, and the time-parallel team kernel beside the
         one-warp kernel when the team path is on."""
-        team = int(getattr(self.opts, "team_warps", 0)) == 8 and max(8, int(self.opts.team_min_horizon)) <= self.n_max
+        tw = int(getattr(self.opts, "team_warps", 0))
+        team = tw in (4, 8) and max(tw, int(self.opts.team_min_horizon)) <= self.n_max
         n = 1
         if horizon and (batch > self.total_warps or team):
             n += 1

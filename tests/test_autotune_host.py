@@ -89,3 +89,4 @@ def test_warps_per_instance_is_a_candidate(tmp_path, monkeypatch):
     assert {(row["team_warps"], row["team_min_horizon"]) for row in r["table"]} == {(0, 0), (8, 64), (8, 128)}
     assert all(len(c) == 4 for c in autotune.DEFAULT_CANDIDATES)
     assert any(c[2] == 8 for c in autotune.DEFAULT_CANDIDATES)
+    assert any(c[2] == 4 for c in autotune.DEFAULT_CANDIDATES)

@@ -1,4 +1,4 @@
-"""The time-parallel team kernel (sqp_team.cuh: one block of 8 warps per
+"""The time-parallel team kernel (sqp_team.cuh: one block of 8 or 4 warps per
 instance, the KKT step split over the horizon) against the FP64 oracle, and
 its place in a batch: instances at or above team_min_horizon go to the team
 kernel, the rest to the one-warp kernel, by horizon alone, so that every
@@ -71,9 +71,14 @@ def test_team_cold_iterations_match_oracle(oracle, cuda, model, iters):
     assert np.all(g["status"] & 1 == 0)
 
 
-@pytest.mark.parametrize("model", MODELS)
-def test_team_near_converged_parity(oracle, cuda, model):
+@pytest.mark.parametrize("model,warps", [(m, 8) for m in MODELS] +
+                         [(P.MODEL_SRBD_RPY12, 4), (P.MODEL_BIPED_WRENCH12, 4)])
+def test_team_near_converged_parity(oracle, cuda, model, warps):
+    """Near convergence (from the oracle's 15-iteration solution), two team
+    iterations against the oracle's: 8 warps (8 horizon chunks) for every
+    model, 4 warps for a quadruped and the biped."""
     wl = workload(model, 4, (80, 150), seed=33)
+    TEAM = dict(team_warps=warps, team_min_horizon=64)
     o15 = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=15), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
                            wl.parameter, wl.W, wl.horizon)
     warm = P.Workload(wl.desc, wl.x0, o15["X"].astype(np.float32), o15["U"].astype(np.float32),
@@ -102,12 +107,14 @@ def test_team_near_converged_parity(oracle, cuda, model):
         assert eg < max(1e-4, 3.0 * e32), (key, eg, e32)
 
 
-def test_team_results_do_not_depend_on_the_batch(cuda):
+@pytest.mark.parametrize("warps", [8, 4])
+def test_team_results_do_not_depend_on_the_batch(cuda, warps):
     """Long horizons go to the team kernel and short ones to the one-warp
-    kernel in one solve call; each result equals the instance solved alone,
-    and the short ones equal the one-warp path's with the team path off."""
+    kernel in one solve call (the two kernels overlapping on two streams);
+    each result equals the instance solved alone, and the short ones equal
+    the one-warp path's with the team path off."""
     wl = workload(P.MODEL_SRBD_RPY12, 10, (20, 40, 63, 64, 100, 150), seed=35)
-    opts = P.SolverOptions(sqp_iters=3, **TEAM)
+    opts = P.SolverOptions(sqp_iters=3, team_warps=warps, team_min_horizon=64)
     mix = solve(wl, opts, want_gains=False)
     off = solve(wl, P.SolverOptions(sqp_iters=3), want_gains=False)
     sub = solve(wl, opts, want_gains=False, idx=[7, 2, 9])
