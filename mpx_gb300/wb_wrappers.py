@@ -183,9 +183,12 @@ class WholeBodyController(_WbCommon):
     def runOffline(self, qpos, qvel, reference=None, parameter=None, max_iter=100):
         """mpc_wrapper.py:387-468 on caller-given whole-body tables
         (reference [N+1, 13+nj+7C], parameter [N+1, C]; the reference takes
-        them from config.reference): single SQP iterations until the
-        reference's stop rule (:465) on the KKT residual's primal part and
-        the change of the objective."""
+        them from config.reference): single SQP iterations, the warm start's
+        first 13 + nj columns set to the reference's (:419), until the
+        reference's stop rule (:465) holds with the KKT residual standing in
+        for its objective: the residual changed by less than 1e-3 and
+        max |c|^2 < 1e-5 (the reference's sum of c^2 over its defects).
+        Returns (X, U, reference, the iterates' X)."""
         if reference is None or parameter is None:
             make = getattr(self.config, "reference", None)
             if make is None:
@@ -204,10 +207,10 @@ class WholeBodyController(_WbCommon):
             X, U, V = out["X"], out["U"], out["V"]
             outputs.append(X[0].cpu().numpy())
             kkt = out["kkt"][0].cpu().numpy()
-            cost = float(kkt[2])
-            if last - cost < 1e-3 and float(kkt[0]) ** 2 < 1e-5:
+            res = float(kkt[2])
+            if last - res < 1e-3 and float(kkt[0]) ** 2 < 1e-5:
                 break
-            last = cost
+            last = res
         self.X0, self.U0, self.V0 = X, U, V
         return X, U, ref, outputs
 
