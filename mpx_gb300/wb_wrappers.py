@@ -49,6 +49,17 @@ def _w_diag(config):
     return W.astype(np.float32)
 
 
+def _sqp_kwargs(opts):
+    """WholeBodySQP's options from a dict of them or from the SolverOptions
+    the wrappers take for the SRBD models (iterations, line search, reg, rho0)."""
+    if opts is None:
+        return {}
+    if isinstance(opts, dict):
+        return dict(opts)
+    return dict(iters=int(opts.sqp_iters), reg=float(opts.reg), rho0=float(opts.rho0), ls_beta=float(opts.ls_beta),
+                ls_eta=float(opts.ls_eta), ls_skip_tol=float(opts.ls_skip_tol), ls_max_trials=int(opts.ls_max_trials))
+
+
 def _model(config, model):
     if model is not None:
         return model
@@ -69,8 +80,7 @@ class _WbCommon:
         self.mass = float(np.sum(self.wb.model.mass))
         self.mpc_frequency = float(config.mpc_frequency)
         self.shift = int(1 / (config.dt * config.mpc_frequency))
-        o = dict(opts or {})
-        self.sqp = WholeBodySQP(self.wb, self.N, batch_max=batch, dt=float(config.dt), iters=o.pop("iters", 5), **o)
+        self.sqp = WholeBodySQP(self.wb, self.N, batch_max=batch, dt=float(config.dt), **_sqp_kwargs(opts))
         self.W = _dev(_w_diag(config), self.dev)
         self.foot0 = np.asarray(config.p_legs0, dtype=np.float32)
         self.q0 = np.asarray(config.q0, dtype=np.float32)
