@@ -162,3 +162,26 @@ def test_save_and_load_state_round_trip():
     s.X0 = torch.zeros(1, N + 1, 13)
     s.load_state(st)
     assert torch.equal(s.X0, torch.ones(1, N + 1, 13))
+
+
+def test_whole_body_configurations_are_recognised():
+    """mpc_wrapper.py's controllers hand whole-body configurations (13 + 2 nj
+    + 6 C states, config_aliengo / config_go2) to the whole-body solve and
+    keep the SRBD ones; W must be diagonal; SolverOptions map onto the
+    whole-body solve's options."""
+    import numpy as np
+    from mpx_gb300 import configs, problem as P, wb_wrappers
+    wb, srbd = configs.aliengo_wb(), configs.srbd_quadruped()
+    assert wb_wrappers.is_whole_body(wb) and not wb_wrappers.is_whole_body(srbd)
+    assert wb.n == 61 and wb_wrappers._w_diag(wb).shape == (72,)
+    W = np.diag(wb.W_diag.astype(np.float64))
+    W[0, 1] = 1.0
+    bad = types.SimpleNamespace(W=W)
+    try:
+        wb_wrappers._w_diag(bad)
+        raise AssertionError("a W with off-diagonal entries was accepted")
+    except ValueError:
+        pass
+    kw = wb_wrappers._sqp_kwargs(P.SolverOptions(sqp_iters=3, ls_max_trials=6))
+    assert kw["iters"] == 3 and kw["ls_max_trials"] == 6
+    assert wb_wrappers._sqp_kwargs(None) == {} and wb_wrappers._sqp_kwargs({"iters": 2}) == {"iters": 2}
