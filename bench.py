@@ -441,7 +441,8 @@ def run_served(dev, opts):
     # stream with horizons of 64 and more on the time-parallel team kernel (8 warps per instance), and with
     # both models' ticks of a step in one mixed-model launch
     for key, o3, mixed in (("mixed", opts, False),
-                           ("mixed_team8", dataclasses.replace(opts, team_warps=8, team_min_horizon=64), False),
+                           ("mixed_team8", dataclasses.replace(opts, team_warps=8, team_min_horizon=64,
+                                                               team_exact_last=True), False),
                            ("mixed_one_launch", opts, True)):
         srv = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=o3, drift_std=0.01, streams=32,
                         device=dev, mixed_launch=mixed)
@@ -458,7 +459,9 @@ def run_served(dev, opts):
                          "are replaced by cold ones), state drift N(0, 0.01^2) per tick, 8 GB admission budget, "
                          "32 streams; 0.5 s warm-up of the same episodes, then 2 s measured; " +
                          {"mixed": "one warp per instance",
-                          "mixed_team8": "horizons >= 64 on the time-parallel team kernel (8 warps per instance)",
+                          "mixed_team8": "horizons >= 64 on the time-parallel team kernel (8 warps per instance, "
+                                         "the last SQP iteration's KKT step as one sequential sweep: "
+                                         "team_exact_last)",
                           "mixed_one_launch": "one warp per instance, both models' ticks of a step in one "
                                               "mixed-model launch (mpxg_solve_mixed)"}[key])
         if key == "mixed":

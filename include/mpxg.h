@@ -108,6 +108,9 @@ typedef struct {
                           Riccati and forward sweeps); the choice depends on the horizon only,
                           so a result does not depend on the rest of its batch */
   int team_min_horizon;
+  int team_exact_last; /* nonzero: the team kernel takes its last SQP iteration's KKT step as one
+                          sequential sweep over the whole horizon (the one-warp kernel's accuracy
+                          for the returned duals, at the latency of one sequential sweep) */
 } mpxg_solver_opts;
 
 /* One batched solve.  Layout: x0 [B,n]; X,V [B,n_max+1,n]; U [B,n_max,m];

@@ -37,7 +37,7 @@ class SolverOpts(ctypes.Structure):
                 ("ls_eta", ctypes.c_float), ("reg", ctypes.c_float), ("rho0", ctypes.c_float),
                 ("ls_skip_tol", ctypes.c_float), ("compute_kkt", ctypes.c_int),
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("team_warps", ctypes.c_int), ("team_min_horizon", ctypes.c_int)]
+                ("team_warps", ctypes.c_int), ("team_min_horizon", ctypes.c_int), ("team_exact_last", ctypes.c_int)]
 
 
 class XlaOpaque(ctypes.Structure):

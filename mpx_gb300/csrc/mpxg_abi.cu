@@ -226,6 +226,7 @@ mpxg_status mpxg_create(const mpxg_problem_desc* d, const mpxg_solver_opts* o, m
   SqpParams& sp = h->sp;
   sp.sqp_iters = o->sqp_iters; sp.ls_max_trials = o->ls_max_trials; sp.ls_beta = o->ls_beta; sp.ls_eta = o->ls_eta;
   sp.reg = o->reg; sp.rho0 = o->rho0; sp.ls_skip_tol = o->ls_skip_tol; sp.compute_kkt = o->compute_kkt;
+  sp.team_exact_last = o->team_exact_last;
   *out = h;
   return MPXG_OK;
 }
@@ -915,7 +916,7 @@ extern "C" mpxg_status mpxg_solve_noalloc(const mpxg_problem_desc* d, const mpxg
   if (io->batch == 0) return MPXG_OK;
 
   const ModelConst mc = model_const(d);
-  SqpParams sp;
+  SqpParams sp{};
   sp.sqp_iters = o->sqp_iters; sp.ls_max_trials = o->ls_max_trials; sp.ls_beta = o->ls_beta; sp.ls_eta = o->ls_eta;
   sp.reg = o->reg; sp.rho0 = o->rho0; sp.ls_skip_tol = o->ls_skip_tol; sp.compute_kkt = o->compute_kkt;
 

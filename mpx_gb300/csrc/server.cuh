@@ -450,6 +450,23 @@ mpxg_status mpxg_server_create(const mpxg_server_desc* d, mpxg_server** out) {
     s->streams.push_back(st);
     s->stream_busy.push_back(0);
   }
+  // A batch's staging (pinned slot ids and mapped result rows) is taken per
+  // launch; allocate as many per pool as batches can run at once now, so
+  // that no pinned allocation (milliseconds, and synchronising) lands in the
+  // served stream
+  for (Pool& p : s->pools) {
+    std::vector<Staging*> made;
+    for (int k = 0; k < d->streams; ++k) {
+      Staging* st = get_staging(s, p);
+      if (!st) {
+        for (Staging* m : made) p.idle.push_back(m);
+        mpxg_server_destroy(s);
+        return fail_lib(MPXG_ERR_OUT_OF_MEMORY, "mpxg_server_create: staging allocation failed");
+      }
+      made.push_back(st);
+    }
+    for (Staging* m : made) p.idle.push_back(m);
+  }
   *out = s;
   return MPXG_OK;
 }

@@ -35,6 +35,7 @@ struct SqpParams {
   int sqp_iters, ls_max_trials;
   float ls_beta, ls_eta, reg, rho0, ls_skip_tol;
   int compute_kkt;
+  int team_exact_last;  // team kernel: the last iteration's KKT step as one sequential sweep
 };
 
 struct BatchPtrs {

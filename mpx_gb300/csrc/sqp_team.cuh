@@ -245,6 +245,10 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
   float rho = sp.rho0;
   int status = 0;
   for (int it = 0; it < sp.sqp_iters; ++it) {
+    // team_exact_last: the last iteration's KKT step as one sequential sweep
+    // over the whole horizon by the last warp (the others idle through it)
+    const bool seq = sp.team_exact_last && it + 1 == sp.sqp_iters;
+    const int lo_i = seq ? 0 : lo, hi_i = seq ? (last ? N : 0) : hi;
     // ================================================ phase 1: linearise all stages
     float lsum = 0.0f, dummy = 0.0f;
     for (int t = tid; t <= N; t += NT)
@@ -254,9 +258,9 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     // ================================================ phase 2a: chunk elements; the last chunk exactly
     if (last) {
       riccati_terminal<M, true>(N, sm, s, lane);
-      riccati_sweep<M, true, 0>(sp, lo, hi, sm, s, nullptr, &status, lane);
+      riccati_sweep<M, true, 0>(sp, lo_i, hi_i, sm, s, nullptr, &status, lane);
       for (int e = lane; e < NP * LDP; e += 32) el.Pin[e] = sm.P[e];
-    } else {
+    } else if (!seq) {
       for (int e = lane; e < NP * LDP; e += 32) sm.P[e] = 0.0f;
       for (int e = lane; e < NX * FS; e += 32) {
         const int cc = e / FS, rr = e - cc * FS;
@@ -268,10 +272,10 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     if (warp == 0 && lane < NX) ts.xb[0][lane] = x0[lane] - X[lane];
     __syncthreads();
     // ================================================ phase 2m: combine the chunks
-    if (warp == 0) team_combine<M, W>(ts, lane);
+    if (warp == 0 && !seq) team_combine<M, W>(ts, lane);
     __syncthreads();
     // ================================================ phase 2b: chunk sweeps from the true values
-    if (!last) {
+    if (!last && !seq) {
       const float* Pe = ts.el[warp + 1].Pin;
       for (int e = lane; e < NP * LDP; e += 32) sm.P[e] = Pe[e];
       for (int e = lane; e < NX * FS; e += 32) {
@@ -284,16 +288,18 @@ __device__ void solve_instance_team(const ModelConst& mc, const SqpParams& sp, c
     __threadfence_block();
     __syncthreads();
     // ================================================ phase 2f: chunk-boundary states
-    if (warp == 0) team_boundary_states<M, W>(ts, lane);
+    if (warp == 0 && !seq) team_boundary_states<M, W>(ts, lane);
     __syncthreads();
     // ================================================ phase 3: chunk forward sweeps
     double a_gd = 0.0, a_lc = 0.0, a_vc = 0.0, a_cs = 0.0;
-    float c_init = 0.0f;
-    if (lane < NX) {
-      sm.dx[lane] = ts.xb[warp][lane];
-      c_init = (lo == 0) ? x0[lane] - X[lane] : s.F[(size_t)(lo - 1) * NZ * FS + JA * FS + lane];
+    if (!seq || last) {
+      float c_init = 0.0f;
+      if (lane < NX) {
+        sm.dx[lane] = ts.xb[seq ? 0 : warp][lane];
+        c_init = (lo_i == 0) ? x0[lane] - X[lane] : s.F[(size_t)(lo_i - 1) * NZ * FS + JA * FS + lane];
+      }
+      forward_sweep<M>(lo_i, hi_i, last, c_init, V, sm, s, lane, &a_gd, &a_lc, &a_vc, &a_cs);
     }
-    forward_sweep<M>(lo, hi, last, c_init, V, sm, s, lane, &a_gd, &a_lc, &a_vc, &a_cs);
     __threadfence_block();
     const double gd = block_sum<W>(a_gd, ts.red, 0), lc = block_sum<W>(a_lc, ts.red, 1);
     const double vc = block_sum<W>(a_vc, ts.red, 2), cs = block_sum<W>(a_cs, ts.red, 3);

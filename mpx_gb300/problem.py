@@ -91,6 +91,7 @@ class SolverOptions:
     compute_kkt: bool = True    # evaluate the KKT residual of the result on the device
     team_warps: int = 0         # 4 or 8: horizons >= team_min_horizon are solved time-parallel by 4 or 8 warps each
     team_min_horizon: int = 64
+    team_exact_last: bool = False  # the team kernel's last KKT step as one sequential sweep (accurate duals)
 
 
 # ----------------------------------------------------------------- models

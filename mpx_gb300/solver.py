@@ -56,6 +56,7 @@ def solver_opts(opts, warps_per_block=0, blocks_per_sm=0):
     o.warps_per_block = int(warps_per_block); o.blocks_per_sm = int(blocks_per_sm)
     o.team_warps = int(getattr(opts, "team_warps", 0))
     o.team_min_horizon = int(getattr(opts, "team_min_horizon", 64))
+    o.team_exact_last = int(bool(getattr(opts, "team_exact_last", False)))
     return o
 
 

@@ -71,14 +71,16 @@ def test_team_cold_iterations_match_oracle(oracle, cuda, model, iters):
     assert np.all(g["status"] & 1 == 0)
 
 
-@pytest.mark.parametrize("model,warps", [(m, 8) for m in MODELS] +
-                         [(P.MODEL_SRBD_RPY12, 4), (P.MODEL_BIPED_WRENCH12, 4)])
-def test_team_near_converged_parity(oracle, cuda, model, warps):
+@pytest.mark.parametrize("model,warps,exact_last", [(m, 8, False) for m in MODELS] +
+                         [(P.MODEL_SRBD_RPY12, 4, False), (P.MODEL_BIPED_WRENCH12, 4, False),
+                          (P.MODEL_BIPED_WRENCH12, 8, True)])
+def test_team_near_converged_parity(oracle, cuda, model, warps, exact_last):
     """Near convergence (from the oracle's 15-iteration solution), two team
     iterations against the oracle's: 8 warps (8 horizon chunks) for every
-    model, 4 warps for a quadruped and the biped."""
+    model, 4 warps for a quadruped and the biped, and 8 warps with the last
+    iteration's step taken sequentially (team_exact_last) for the biped."""
     wl = workload(model, 4, (80, 150), seed=33)
-    TEAM = dict(team_warps=warps, team_min_horizon=64)
+    TEAM = dict(team_warps=warps, team_min_horizon=64, team_exact_last=exact_last)
     o15 = oracle.sqp_solve(wl.desc, P.SolverOptions(sqp_iters=15), wl.x0, wl.X0, wl.U0, wl.V0, wl.reference,
                            wl.parameter, wl.W, wl.horizon)
     warm = P.Workload(wl.desc, wl.x0, o15["X"].astype(np.float32), o15["U"].astype(np.float32),
