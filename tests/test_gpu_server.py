@@ -1,4 +1,6 @@
 """Serving: continuous batching over resident episode slots."""
+import time
+
 import numpy as np
 import pytest
 import torch
@@ -122,3 +124,37 @@ def test_release_waits_for_queued_tick(cuda):
     assert len(s.completed) == 1 and s.completed[0][1] == "A"
     s.admit("B", "quadruped", x0_of(s, "quadruped", 2), 30)   # freed once the tick completed
     s.close()
+
+
+def test_each_ticket_is_delivered_when_its_own_solve_ends(cuda):
+    """A short-horizon tick and a long one in the same batch: the short one's
+    result reaches the host while the long one is still being solved (the
+    rows land in mapped host memory, status entry last), and each result
+    equals the one a second server gives after draining."""
+    def run(early):
+        s = MPCServer(default_models(), n_max=200, budget_bytes=8 << 30, opts=P.SolverOptions(sqp_iters=5),
+                      drift_std=0.0)
+        s.admit("long", "quadruped", x0_of(s, "quadruped", 1), 200, v_ref=0.3, phase=0.2)
+        s.admit("short", "quadruped", x0_of(s, "quadruped", 2), 20, v_ref=0.3, phase=0.6)
+        s.submit("long")
+        s.submit("short")
+        s.launch_pending()
+        got = {}
+        if early:
+            deadline = time.perf_counter() + 10.0
+            while "short" not in got and time.perf_counter() < deadline:
+                for d in s.poll():
+                    got[d[1]] = d
+            assert "short" in got
+            assert "long" not in got  # the N = 200 solve takes ms longer than the N = 20 one
+        s.drain()
+        for d in s.completed:
+            got[d[1]] = d
+        s.close()
+        return got
+
+    early, late = run(True), run(False)
+    for k in ("long", "short"):
+        np.testing.assert_array_equal(early[k][3], late[k][3])
+        np.testing.assert_array_equal(early[k][4], late[k][4])
+        assert early[k][5] == late[k][5]
