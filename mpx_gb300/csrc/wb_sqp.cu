@@ -127,6 +127,10 @@ WbDims wb_dims(const mpxg_wb_model& m) {
 struct WbSqp {
   int B, N, KT, first;
   int k_lo, k_hi, phase;  // trial steps of this wb_trial_kernel launch; wb_accept_kernel's pass
+  // float64 steps per block (1 or kNW) of wb_lin_kernel's nominal part and
+  // of wb_trial_kernel: one while a launch has fewer steps than the SMs
+  // hold at kNW, so that each step has an SM's FP64 pipe to itself
+  int nom_pb, trial_pb;
   WbDims d;
   double dt, alpha, beta, eta, skip_tol, rho0;
   float reg;
@@ -424,10 +428,10 @@ __global__ void __launch_bounds__(32 * kNW) wb_lin_kernel(const __grid_constant_
     JacScr jac[kNW];
   } sw;
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long nom = (long long)p.B * p.N, nom_blocks = (nom + kNW - 1) / kNW;
+  const long long nom = (long long)p.B * p.N, nom_blocks = (nom + p.nom_pb - 1) / p.nom_pb;
   if (blockIdx.x < nom_blocks) {
-    const long long item = (long long)blockIdx.x * kNW + wid;
-    if (item < nom) nominal_item(m, p, sw.nom[wid], item, lane);
+    const long long item = (long long)blockIdx.x * p.nom_pb + wid;
+    if (wid < p.nom_pb && item < nom) nominal_item(m, p, sw.nom[wid], item, lane);
     return;
   }
   const long long item = (long long)(blockIdx.x - nom_blocks) * kNW + wid;
@@ -505,17 +509,153 @@ __global__ void __launch_bounds__(128) wb_quad_kernel(const __grid_constant__ Wb
 }
 
 // ---------------------------------------------------------------- Riccati
+// Columns NZ..NX-1 of every A_t are zero (the whole-body step does not read
+// the contact-point and force states), so a stage's products are taken over
+// the NC = NZ + NU columns of [A_Z | B] (A_Z the first NZ columns of A) and
+// one more column: c_t, which P turns into P c + p.
+//
 // Shared-memory layout of the Riccati block (floats): the stage matrices
-// column-major with odd leading dimensions, as lqr_eq_kernel's.
-template <int NX, int NU>
+// column-major with odd leading dimensions, as lqr_eq_kernel's.  T, the
+// value function before symmetrisation, spans AB and PAB (both dead by then).
+template <int NX, int NU, int NZ>
 struct RLay {
+  static constexpr int NC = NZ + NU;
   static constexpr int LX = NX + (NX % 2 == 0 ? 1 : 2), LU = NU + (NU % 2 == 0 ? 1 : 2);
-  static constexpr int P = 0, A = P + NX * LX, PA = A + NX * LX, Q = PA + NX * LX, B = Q + NX * LX, PB = B + NU * LX,
-                       M = PB + NU * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, ZG = QUX + NX * LU,
+  static constexpr int P = 0, AB = P + NX * LX, PAB = AB + (NC + 1) * LX, T = AB, Q = PAB + (NC + 1) * LX,
+                       M = Q + NX * LX, QUU = M + NU * LX, QUX = QUU + NU * LU, ZG = QUX + NX * LU,
                        PAN = (ZG + (NX + 1) * LU + 3) / 4 * 4, V = PAN + 2 * lqeq::kGjBlock * 32;
   static constexpr int VL = NX + 4;
-  static constexpr int vc = V, vq = vc + VL, vr = vq + VL, vw = vr + VL, vp = vw + VL, vqx = vp + VL, vqu = vqx + VL,
-                       vk = vqu + VL, vx = vk + VL, vu = vx + VL, FLOATS = vu + VL;
+  static constexpr int vq = V, vr = vq + VL, vp = vr + VL, vqx = vp + VL, vqu = vqx + VL, vx = vqu + VL,
+                       vu = vx + VL, FLOATS = vu + VL;
+  static_assert(2 * (NC + 1) * LX >= NX * LX, "T fits in AB and PAB");
+};
+
+// out(r, c) = sum_l X(r, l) Y(l, c) over 16 x 16 threads, the tiling and
+// summation order of lqeq::bmm, each result handed to ep(r, c, sum) rather
+// than stored.  Ends with a barrier.
+template <int ROWS, int INNER, int COLS, bool TX, bool TY, class Ep>
+__device__ __forceinline__ void bmm_ep(const float* X, int ldx, const float* Y, int ldy, Ep ep) {
+  constexpr int TR = (ROWS + 15) / 16, TC = (COLS + 15) / 16;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[TR][TC];
+#pragma unroll
+  for (int i = 0; i < TR; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j) acc[i][j] = 0.0f;
+#pragma unroll 2
+  for (int l = 0; l < INNER; ++l) {
+    float xa[TR], yb[TC];
+#pragma unroll
+    for (int i = 0; i < TR; ++i) {
+      const int r = ty + 16 * i;
+      xa[i] = (r < ROWS) ? (TX ? X[r * ldx + l] : X[l * ldx + r]) : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+      const int c = tx + 16 * j;
+      yb[j] = (c < COLS) ? (TY ? Y[l * ldy + c] : Y[c * ldy + l]) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < TR; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j) acc[i][j] += xa[i] * yb[j];
+  }
+#pragma unroll
+  for (int i = 0; i < TR; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+      const int r = ty + 16 * i, c = tx + 16 * j;
+      if (r < ROWS && c < COLS) ep(r, c, acc[i][j]);
+    }
+  __syncthreads();
+}
+
+// One stage's step-problem data held in registers: issued (global loads) at
+// the top of the stage before it, committed to shared memory at that
+// stage's end, so the loads' latency hides behind its products.
+template <int NX, int NU, int NZ>
+struct StagePre {
+  typedef RLay<NX, NU, NZ> L;
+  static constexpr int TH = lqeq::kThreads, NC = L::NC, LX = L::LX, LU = L::LU;
+  static constexpr int nA = (NX * NZ + TH - 1) / TH, nB = (NX * NU + TH - 1) / TH, nQ = (NX * NX + TH - 1) / TH,
+                       nR = (NU * NU + TH - 1) / TH, nV = (NX + TH - 1) / TH;
+  static_assert(NU <= TH, "one thread per entry of r");
+  float a[nA], bm[nB], q[nQ], m[nB], r[nR], c[nV], vq[nV], vr;
+
+  __device__ __forceinline__ void issue(const mpxg_lq_eq_io& io, size_t sn, size_t sn1, int t) {
+    const int tid = threadIdx.x;
+    const float* A = io.A + (sn + t) * NX * NX;
+    const float* Bm = io.Bm + (sn + t) * NX * NU;
+    const float* Q = io.Q + (sn1 + t) * NX * NX;
+    const float* M = io.M + (sn + t) * NX * NU;
+    const float* R = io.R + (sn + t) * NU * NU;
+#pragma unroll
+    for (int i = 0; i < nA; ++i) {
+      const int e = tid + TH * i;
+      a[i] = e < NX * NZ ? __ldg(A + (e / NZ) * NX + e % NZ) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < nB; ++i) {
+      const int e = tid + TH * i;
+      bm[i] = e < NX * NU ? __ldg(Bm + e) : 0.0f;
+      m[i] = e < NX * NU ? __ldg(M + e) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < nQ; ++i) {
+      const int e = tid + TH * i;
+      q[i] = e < NX * NX ? __ldg(Q + e) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < nR; ++i) {
+      const int e = tid + TH * i;
+      r[i] = e < NU * NU ? __ldg(R + e) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < nV; ++i) {
+      const int e = tid + TH * i;
+      c[i] = e < NX ? __ldg(io.c + (sn + t) * NX + e) : 0.0f;
+      vq[i] = e < NX ? __ldg(io.q + (sn1 + t) * NX + e) : 0.0f;
+    }
+    vr = tid < NU ? __ldg(io.r + (sn + t) * NU + tid) : 0.0f;
+  }
+
+  // row-major sources to column-major shared memory: A_Z, B and c into the
+  // columns of AB, Q, M, R into Q_uu's slot, q and r
+  __device__ __forceinline__ void commit(float* s) const {
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < nA; ++i) {
+      const int e = tid + TH * i;
+      if (e < NX * NZ) s[L::AB + (e % NZ) * LX + e / NZ] = a[i];
+    }
+#pragma unroll
+    for (int i = 0; i < nB; ++i) {
+      const int e = tid + TH * i;
+      if (e < NX * NU) {
+        s[L::AB + (NZ + e % NU) * LX + e / NU] = bm[i];
+        s[L::M + (e % NU) * LX + e / NU] = m[i];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < nQ; ++i) {
+      const int e = tid + TH * i;
+      if (e < NX * NX) s[L::Q + (e % NX) * LX + e / NX] = q[i];
+    }
+#pragma unroll
+    for (int i = 0; i < nR; ++i) {
+      const int e = tid + TH * i;
+      if (e < NU * NU) s[L::QUU + (e % NU) * LU + e / NU] = r[i];
+    }
+#pragma unroll
+    for (int i = 0; i < nV; ++i) {
+      const int e = tid + TH * i;
+      if (e < NX) {
+        s[L::AB + NC * LX + e] = c[i];
+        s[L::vq + e] = vq[i];
+      }
+    }
+    if (tid < NU) s[L::vr + tid] = vr;
+  }
 };
 
 // Riccati sweep of the step problem x_{t+1} = A x + B u + c (x_0 = c_0),
@@ -523,57 +663,58 @@ struct RLay {
 //   Q_xx = Q + A'PA, Q_ux = M' + B'PA, Q_uu = R + B'PB, q_x = q + A'(Pc + p),
 //   q_u = r + B'(Pc + p), [Z | g] = Q_uu^-1 [Q_ux | q_u], K = -Z, k = -g,
 //   P <- Q_xx - Q_ux'Z (symmetrised), p <- q_x + Q_ux'k;
-// then dX, dU by the forward sweep and lam_t = P_t dX_t + p_t.  Columns
-// NZ..NX-1 of every A_t are zero (the whole-body step does not read the
-// contact-point and force states): P A, A'(P A), B'(P A) and A'w are formed
-// over the first NZ columns only, and the rest of Q_xx, Q_ux and q_x is
-// Q, M' and q.
+// then dX, dU by the forward sweep and lam_t = P_t dX_t + p_t.  A stage is
+// four block products: [P A_Z | P B | P c + p]; [A_Z | B]' times that
+// (Q_xx's A-block, Q_ux's A-columns, Q_uu, q_x's A-part, q_u); the pivot
+// solve; [Q_xx - Q_ux'Z | q_x - Q_ux'g].  Off the A-columns Q_xx, Q_ux and
+// q_x are Q, M' and q.
 template <int NX, int NU, int NZ>
 __global__ void __launch_bounds__(lqeq::kThreads, 1) wb_riccati_kernel(mpxg_lq_eq_io io, float* Pscr) {
   using namespace lqeq;
-  typedef RLay<NX, NU> L;
-  constexpr int LX = L::LX, LU = L::LU;
+  typedef RLay<NX, NU, NZ> L;
+  constexpr int LX = L::LX, LU = L::LU, NC = L::NC;
   extern __shared__ float4 smem4[];
   float* s = reinterpret_cast<float*>(smem4);
-  float *P = s + L::P, *sA = s + L::A, *PA = s + L::PA, *sQ = s + L::Q, *sB = s + L::B, *PB = s + L::PB;
-  float *sM = s + L::M, *Quu = s + L::QUU, *Qux = s + L::QUX, *ZG = s + L::ZG, *pan = s + L::PAN;
-  float *vc = s + L::vc, *vq = s + L::vq, *vr = s + L::vr, *vw = s + L::vw, *vp = s + L::vp;
-  float *vqx = s + L::vqx, *vqu = s + L::vqu, *vk = s + L::vk, *vx = s + L::vx, *vu = s + L::vu;
+  float *P = s + L::P, *AB = s + L::AB, *PAB = s + L::PAB, *T = s + L::T, *sQ = s + L::Q, *sM = s + L::M;
+  float *Quu = s + L::QUU, *Qux = s + L::QUX, *ZG = s + L::ZG, *pan = s + L::PAN;
+  float *vq = s + L::vq, *vr = s + L::vr, *vp = s + L::vp, *vqx = s + L::vqx, *vqu = s + L::vqu;
+  float *vx = s + L::vx, *vu = s + L::vu;
   const int b = blockIdx.x, N = io.N, tid = threadIdx.x;
   constexpr int NP = NX + 1;
   float* Ps = Pscr + (size_t)b * (N + 1) * NP * NX;
   const size_t sn = (size_t)b * N, sn1 = (size_t)b * (N + 1);
 
+  StagePre<NX, NU, NZ> pre;
+  pre.issue(io, sn, sn1, N - 1);
   load_cm<NX, NX>(P, LX, io.Q + (sn1 + N) * NX * NX);
   load_vec<NX>(vp, io.q + (sn1 + N) * NX);
+  pre.commit(s);
   __syncthreads();
   for (int e = tid; e < NX * NX; e += kThreads) Ps[(size_t)N * NP * NX + e] = P[(e / NX) * LX + e % NX];
   for (int i = tid; i < NX; i += kThreads) Ps[(size_t)N * NP * NX + NX * NX + i] = vp[i];
 
   for (int t = N - 1; t >= 0; --t) {
-    load_cm<NX, NX>(sA, LX, io.A + (sn + t) * NX * NX);
-    load_cm<NX, NU>(sB, LX, io.Bm + (sn + t) * NX * NU);
-    load_cm<NX, NX>(sQ, LX, io.Q + (sn1 + t) * NX * NX);
-    load_cm<NX, NU>(sM, LX, io.M + (sn + t) * NX * NU);
-    load_cm<NU, NU>(Quu, LU, io.R + (sn + t) * NU * NU);
-    load_vec<NX>(vc, io.c + (sn + t) * NX);
-    load_vec<NX>(vq, io.q + (sn1 + t) * NX);
-    load_vec<NU>(vr, io.r + (sn + t) * NU);
-    __syncthreads();
-    bmm<NX, NX, NZ, false, false, false>(PA, LX, P, LX, sA, LX, 1.0f, nullptr, 0);
-    bmm<NX, NX, NU, false, false, false>(PB, LX, P, LX, sB, LX, 1.0f, nullptr, 0);
-    bmv<NX, NX, false>(vw, P, LX, vc, 1.0f, vp);
-    bmm<NZ, NX, NZ, true, false, false>(sQ, LX, sA, LX, PA, LX, 1.0f, sQ, LX);    // Q_xx (its A-block)
-    bmm<NU, NX, NZ, true, false, true>(Qux, LU, sB, LX, PA, LX, 1.0f, sM, LX);    // Q_ux (its A-columns)
-    for (int e = threadIdx.x; e < NU * (NX - NZ); e += kThreads) {                // Q_ux = M' elsewhere
+    if (t > 0) pre.issue(io, sn, sn1, t - 1);
+    bmm_ep<NX, NX, NC + 1, false, false>(P, LX, AB, LX, [&](int r, int c, float v) {
+      PAB[c * LX + r] = c < NC ? v : v + vp[r];
+    });
+    for (int e = tid; e < NU * (NX - NZ); e += kThreads) {  // Q_ux = M' off the A-columns
       const int a = e % NU, i = NZ + e / NU;
       Qux[i * LU + a] = sM[a * LX + i];
     }
-    bmm<NU, NX, NU, true, false, false>(Quu, LU, sB, LX, PB, LX, 1.0f, Quu, LU);  // Q_uu
-    bmv<NZ, NX, true>(vqx, sA, LX, vw, 1.0f, vq);                                 // q_x (A-part)
-    for (int i = NZ + threadIdx.x; i < NX; i += kThreads) vqx[i] = vq[i];          // q_x = q elsewhere
-    bmv<NU, NX, true>(vqu, sB, LX, vw, 1.0f, vr);                                 // q_u
-    __syncthreads();
+    for (int i = NZ + tid; i < NX; i += kThreads) vqx[i] = vq[i];  // q_x = q off the A-columns
+    bmm_ep<NC, NX, NC + 1, true, false>(AB, LX, PAB, LX, [&](int r, int c, float v) {
+      if (c == NC) {
+        if (r < NZ) vqx[r] = v + vq[r];
+        else vqu[r - NZ] = v + vr[r - NZ];
+      } else if (r < NZ) {
+        if (c < NZ) sQ[c * LX + r] = v + sQ[c * LX + r];
+      } else if (c < NZ) {
+        Qux[c * LU + (r - NZ)] = v + sM[(r - NZ) * LX + c];
+      } else {
+        Quu[(c - NZ) * LU + (r - NZ)] = v + Quu[(c - NZ) * LU + (r - NZ)];
+      }
+    });
     gj_solve<NU, NU + NX + 1, kGjBlock>(pan, [&](int j, float* v) {
 #pragma unroll
       for (int i = 0; i < NU; ++i)
@@ -586,28 +727,25 @@ __global__ void __launch_bounds__(lqeq::kThreads, 1) wb_riccati_kernel(mpxg_lq_e
       float* Ko = io.K + (sn + t) * NU * NX;
       float* ko = io.k + (sn + t) * NU;
       for (int e = tid; e < NU * NX; e += kThreads) Ko[e] = -ZG[(e % NX) * LU + e / NX];
-      for (int a = tid; a < NU; a += kThreads) {
-        vk[a] = -ZG[NX * LU + a];
-        ko[a] = -ZG[NX * LU + a];
-      }
+      for (int a = tid; a < NU; a += kThreads) ko[a] = -ZG[NX * LU + a];
     }
-    __syncthreads();
-    bmm<NX, NU, NX, true, false, false>(P, LX, Qux, LU, ZG, LU, -1.0f, sQ, LX);
-    bmv<NX, NU, true>(vp, Qux, LU, vk, 1.0f, vqx);
-    for (int e = tid; e < NX * NX; e += kThreads) {
-      const int c = e / NX, r = e % NX;
-      PA[c * LX + r] = 0.5f * (P[c * LX + r] + P[r * LX + c]);
-    }
-    __syncthreads();
+    bmm_ep<NX, NU, NX + 1, true, false>(Qux, LU, ZG, LU, [&](int r, int c, float v) {
+      if (c < NX) T[c * LX + r] = -v + sQ[c * LX + r];
+      else vp[r] = -v + vqx[r];
+    });
     float* Pt = Ps + (size_t)t * NP * NX;
     for (int e = tid; e < NX * NX; e += kThreads) {
       const int c = e / NX, r = e % NX;
-      const float v = PA[c * LX + r];
+      const float v = 0.5f * (T[c * LX + r] + T[r * LX + c]);
       P[c * LX + r] = v;
       Pt[e] = v;
     }
     for (int i = tid; i < NX; i += kThreads) Pt[NX * NX + i] = vp[i];
     __syncthreads();
+    if (t > 0) {
+      pre.commit(s);
+      __syncthreads();
+    }
   }
   static_assert(2 * FwdLay<NX, NU>::STG <= L::V, "forward staging must fit below the vectors");
   forward_sweep<NX, NU>(io, b, s, s + FwdLay<NX, NU>::STG, vx, vu, vq);
@@ -676,9 +814,9 @@ __global__ void __launch_bounds__(32 * kNW) wb_trial_kernel(const __grid_constan
   __shared__ StepScr sws[kNW];
   __shared__ CostScr swc[kNW];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long item = (long long)blockIdx.x * kNW + wid;
+  const long long item = (long long)blockIdx.x * p.trial_pb + wid;
   const int N1 = p.N + 1, nk = p.k_hi - p.k_lo;
-  if (item >= (long long)p.B * nk * N1) return;
+  if (wid >= p.trial_pb || item >= (long long)p.B * nk * N1) return;
   const int b = (int)(item / ((long long)nk * N1));
   const int rem = (int)(item % ((long long)nk * N1));
   const int k = p.k_lo + rem / N1, t = rem % N1;
@@ -957,13 +1095,20 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
   lq.x0 = p.x0s; lq.K = p.K; lq.k = p.k; lq.X = p.dX; lq.U = p.dU; lq.lam = p.lam;
 
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t rsmem = (size_t)RLay<kNX, kNU>::FLOATS * sizeof(float);
+  const size_t rsmem = (size_t)RLay<kNX, kNU, kNZ>::FLOATS * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(wb_riccati_kernel<kNX, kNU, kNZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)rsmem);
   if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: riccati attribute");
+  int dev = 0, sms = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return lib_cuda_fail(e, "mpxg_wb_sqp: device");
+  const auto per_block = [&](long long steps) { return steps < (long long)sms * kNW ? 1 : kNW; };
+  const auto blocks = [](long long items, int pb) { return (unsigned)((items + pb - 1) / pb); };
   const long long jac_items = (long long)B * N * (d.nz + d.nj);
   const long long quad_items = (long long)B * (N + 1);
-  const unsigned lin_blocks = (unsigned)(((long long)B * N + kNW - 1) / kNW + (jac_items + kNW - 1) / kNW);
+  p.nom_pb = per_block((long long)B * N);
+  const unsigned lin_blocks = blocks((long long)B * N, p.nom_pb) + blocks(jac_items, kNW);
   const unsigned quad_blocks = (unsigned)((quad_items + 3) / 4);
   auto linearise = [&]() -> cudaError_t {
     wb_lin_kernel<<<lin_blocks, 32 * kNW, 0, st>>>(m, p);
@@ -982,12 +1127,14 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
     // the full step first; the shorter steps only for instances that reject it
     p.k_lo = 0; p.k_hi = 1; p.phase = 0;
     const long long tr0 = (long long)B * (N + 1);
-    wb_trial_kernel<<<(unsigned)((tr0 + kNW - 1) / kNW), 32 * kNW, 0, st>>>(m, p);
+    p.trial_pb = per_block(tr0);
+    wb_trial_kernel<<<blocks(tr0, p.trial_pb), 32 * kNW, 0, st>>>(m, p);
     wb_accept_kernel<<<B, kBlk, 0, st>>>(p);
     if (p.KT > 1) {
       p.k_lo = 1; p.k_hi = p.KT; p.phase = 1;
       const long long tr1 = (long long)B * (p.KT - 1) * (N + 1);
-      wb_trial_kernel<<<(unsigned)((tr1 + kNW - 1) / kNW), 32 * kNW, 0, st>>>(m, p);
+      p.trial_pb = per_block(tr1);
+      wb_trial_kernel<<<blocks(tr1, p.trial_pb), 32 * kNW, 0, st>>>(m, p);
       wb_accept_kernel<<<B, kBlk, 0, st>>>(p);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: iteration");
