@@ -579,6 +579,11 @@ def run_ours(args, rank, world, local_rank):
     solve_avg = sum(solve_ms) / len(solve_ms)
     kkt = tr.out["kkt"][:, 2].float().cpu().numpy()
     status = tr.out["status"].cpu().numpy()
+    # the reference's own stopping test (mpx/utils/mpc_wrapper.py:452-465): the squared defects of each
+    # instance's solution summed, sum(c * c) < 1e-5, by the library's residual evaluator
+    _, c_ev = tr.solver.evaluate(tr.x0, tr.X, tr.U, tr.ref, tr.par, tr.w, tr.horizon, stream=stream)
+    torch.cuda.synchronize()
+    sum_c2 = (c_ev.double() ** 2).sum(dim=(1, 2)).cpu().numpy()
 
     # ---------------- the batch's error against the FP64 oracle (64 sampled instances)
     fp64 = fp64_error(tr, opts, stream) if (not args.profile and rank == 0) else None
@@ -768,7 +773,11 @@ def run_ours(args, rank, world, local_rank):
         "batched_vs_plain": (value / world) / plain["solves_per_s"] if plain else None,
         "kkt": {"median": float(np.median(kkt)), "p99": float(np.percentile(kkt, 99)),
                 "frac_le_1e-5": float((kkt <= 1e-5).mean()), "status_nonzero": int((status != 0).sum()),
-                "status_bits": status_bits(status)},
+                "status_bits": status_bits(status),
+                "sum_c2": {"median": float(np.median(sum_c2)), "max": float(sum_c2.max()),
+                           "frac_lt_1e-5": float((sum_c2 < 1e-5).mean()),
+                           "what": "the reference's stopping test, sum of squared dynamics and initial-state "
+                                   "defects per instance (mpc_wrapper.py:465)"}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "sqp_kernel<ModelRpy12>",
                      "solve_ms": solve_avg, "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},

@@ -288,7 +288,6 @@ inline void retire(mpxg_server* s, int episode) {
   s->eps.erase(it);
 }
 
-// Reap running batch i (its event has completed).
 // Deliver ticket i of a part from its result row (in mapped host memory).
 inline void deliver(mpxg_server* s, Part& part, size_t i) {
   const Pool& p = s->pools[part.model];
@@ -331,23 +330,25 @@ inline int deliver_arrived(mpxg_server* s) {
   return n;
 }
 
+// Reap running batch i (its event has completed): deliver the rows not yet
+// delivered, release the episodes and the staging.
 inline void reap(mpxg_server* s, size_t i) {
   Batch b = std::move(s->inflight[i]);
   s->inflight.erase(s->inflight.begin() + i);
   s->stream_busy[b.stream] = 0;
   for (Part& part : b.parts) {
-  Pool& p = s->pools[part.model];
-  for (size_t i = 0; i < part.tickets.size(); ++i) {
-    if (!part.got[i]) deliver(s, part, i);
-    auto it = s->eps.find(part.episode[i]);
-    if (it != s->eps.end()) {
-      Episode& e = it->second;
-      if (part.status[i] & MPXG_INST_NAN) e.cold = true;  // NaN fallback: cold start next tick
-      e.running = false;
-      if (--e.busy == 0 && e.retiring) retire(s, part.episode[i]);
+    Pool& p = s->pools[part.model];
+    for (size_t k = 0; k < part.tickets.size(); ++k) {
+      if (!part.got[k]) deliver(s, part, k);  // the event has completed: every row is written
+      auto it = s->eps.find(part.episode[k]);
+      if (it != s->eps.end()) {
+        Episode& e = it->second;
+        if (part.status[k] & MPXG_INST_NAN) e.cold = true;  // NaN fallback: cold start next tick
+        e.running = false;
+        if (--e.busy == 0 && e.retiring) retire(s, part.episode[k]);
+      }
     }
-  }
-  p.idle.push_back(part.st);
+    p.idle.push_back(part.st);
   }
 }
 
