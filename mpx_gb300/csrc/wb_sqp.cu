@@ -139,6 +139,11 @@ struct WbSqp {
   const int* contact;
   float *X, *U, *V;
   double *fnom, *cd, *sums, *ls, *trial;
+  // f of every trial step at its stages [B, KT, N, nx], and per instance the
+  // accepted trial + 1 (0: the iterate's f is not cached), so that the next
+  // linearisation takes the accepted step's f instead of recomputing it
+  double* fcache;
+  int* fvalid;
   float *A, *Bm, *c, *x0s, *Q, *R, *M, *q, *r, *K, *k, *dX, *dU, *lam, *Pscr;
   unsigned* kbits;
   int* status;
@@ -372,13 +377,19 @@ __device__ __forceinline__ void nominal_item(const mpxg_wb_model& m, const WbSqp
   const int b = (int)(item / p.N), t = (int)(item % p.N);
   const size_t st = (size_t)b * p.N + t;
   const int nx = d.nx;
-  const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * nx;
-  for (int i = lane; i < nx; i += 32) s.xb[i] = (double)Xt[i];
-  if (lane < d.nj) s.ub[lane] = (double)p.U[st * d.nj + lane];
-  __syncwarp();
-  eval_step(m, p, s, s.xb, s.ub, p.contact + ((size_t)b * (p.N + 1) + t) * d.nc, lane);
   double* fo = p.fnom + st * nx;
-  for (int i = lane; i < nx; i += 32) fo[i] = s.f[i];
+  const int kv = p.fvalid[b];
+  if (kv > 0) {  // the accepted trial evaluated f at exactly this (X_t, U_t)
+    const double* fc = p.fcache + (((size_t)b * p.KT + (kv - 1)) * p.N + t) * nx;
+    for (int i = lane; i < nx; i += 32) fo[i] = fc[i];
+  } else {
+    const float* Xt = p.X + ((size_t)b * (p.N + 1) + t) * nx;
+    for (int i = lane; i < nx; i += 32) s.xb[i] = (double)Xt[i];
+    if (lane < d.nj) s.ub[lane] = (double)p.U[st * d.nj + lane];
+    __syncwarp();
+    eval_step(m, p, s, s.xb, s.ub, p.contact + ((size_t)b * (p.N + 1) + t) * d.nc, lane);
+    for (int i = lane; i < nx; i += 32) fo[i] = s.f[i];
+  }
   float* At = p.A + st * nx * nx;
   const int nzc = nx - d.nz;
   for (int e = lane; e < nx * nzc; e += 32) At[(e / nzc) * nx + d.nz + e % nzc] = 0.0f;
@@ -831,25 +842,29 @@ __global__ void __launch_bounds__(32 * kNW) wb_trial_kernel(const __grid_constan
   const size_t oX = (size_t)b * N1 * nx, oU = (size_t)b * p.N * nj;
   load_stage(p, s, b, t, lane);
   __syncwarp();
-  for (int i = lane; i < nx; i += 32) s.x[i] += al * (double)p.dX[oX + (size_t)t * nx + i];
+  // the trial point as wb_accept_kernel stores it (float32 of the same fma),
+  // so that the accepted trial's f is the next linearisation's
+  for (int i = lane; i < nx; i += 32) s.x[i] = (double)(float)fma(al, (double)p.dX[oX + (size_t)t * nx + i], s.x[i]);
   if (t < p.N)
-    for (int j = lane; j < nj; j += 32) s.u[j] += al * (double)p.dU[oU + (size_t)t * nj + j];
+    for (int j = lane; j < nj; j += 32) s.u[j] = (double)(float)fma(al, (double)p.dU[oU + (size_t)t * nj + j], s.u[j]);
   __syncwarp();
   const double cost = stage_eval<false>(d, s, t == p.N, p.swing != 0, lane);
   if (t > 0) {
     const int tp = t - 1;
     for (int i = lane; i < nx; i += 32)
-      ss.xb[i] = (double)p.X[oX + (size_t)tp * nx + i] + al * (double)p.dX[oX + (size_t)tp * nx + i];
+      ss.xb[i] = (double)(float)fma(al, (double)p.dX[oX + (size_t)tp * nx + i], (double)p.X[oX + (size_t)tp * nx + i]);
     for (int j = lane; j < nj; j += 32)
-      ss.ub[j] = (double)p.U[oU + (size_t)tp * nj + j] + al * (double)p.dU[oU + (size_t)tp * nj + j];
+      ss.ub[j] = (double)(float)fma(al, (double)p.dU[oU + (size_t)tp * nj + j], (double)p.U[oU + (size_t)tp * nj + j]);
     __syncwarp();
     eval_step(m, p, ss, ss.xb, ss.ub, p.contact + ((size_t)b * N1 + tp) * d.nc, lane);
+    double* fc = p.fcache + (((size_t)b * p.KT + k) * p.N + tp) * nx;
+    for (int i = lane; i < nx; i += 32) fc[i] = ss.f[i];
   }
   double vcs = 0.0, ccs = 0.0;
   for (int i = lane; i < nx; i += 32) {
     const double ci = (t == 0 ? (double)p.x0[(size_t)b * nx + i] : ss.f[i]) - s.x[i];
     const double v = (double)p.V[oX + (size_t)t * nx + i], l = (double)p.lam[oX + (size_t)t * nx + i];
-    vcs += (v + al * (l - v)) * ci;
+    vcs += (double)(float)fma(al, l - v, v) * ci;
     ccs += ci * ci;
   }
   vcs = warp_sum(vcs);
@@ -873,14 +888,14 @@ __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__
   double* ls = p.ls + b * 8;
   if (threadIdx.x == 0) {
     double al = 1.0;
-    int fail = 0, go = 1;
+    int fail = 0, go = 1, kv = 0;  // kv: the taken trial + 1, 0 for a step taken untested
     if (p.phase == 0) {
       if (ls[3] == 0.0) {
         double phi = 0.0;
         const double* tr = p.trial + ((size_t)b * p.KT) * N1;
         for (int t = 0; t < N1; ++t) phi += tr[t];
-        if (phi - ls[2] <= p.eta * ls[1]) ls[3] = 1.0;
-        else if (p.KT == 1) { fail = MPXG_INST_LS_FAIL; ls[3] = 1.0; }
+        if (phi - ls[2] <= p.eta * ls[1]) { ls[3] = 1.0; kv = 1; }
+        else if (p.KT == 1) { fail = MPXG_INST_LS_FAIL; ls[3] = 1.0; kv = 1; }
         else go = 0;  // pass 1 decides
       }
     } else if (ls[3] != 0.0) {
@@ -888,6 +903,7 @@ __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__
     } else {
       bool ok = false;
       double a = 1.0;
+      kv = p.KT;  // the last trial when none passes
       for (int k = 1; k < p.KT; ++k) {
         a *= p.beta;
         double phi = 0.0;
@@ -895,6 +911,7 @@ __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__
         for (int t = 0; t < N1; ++t) phi += tr[t];
         if (phi - ls[2] <= p.eta * a * ls[1]) {
           ok = true;
+          kv = k + 1;
           break;
         }
       }
@@ -905,6 +922,7 @@ __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__
     s_al = al;
     s_bad = fail;
     s_go = go;
+    if (go) p.fvalid[b] = kv;
   }
   __syncthreads();
   if (!s_go) return;
@@ -914,15 +932,15 @@ __global__ void __launch_bounds__(kBlk) wb_accept_kernel(const __grid_constant__
   const size_t oX = (size_t)b * nX, oU = (size_t)b * nU;
   int bad = 0;
   for (size_t e = threadIdx.x; e < nX; e += kBlk) {
-    const float x = (float)((double)p.X[oX + e] + al * (double)p.dX[oX + e]);
+    const float x = (float)fma(al, (double)p.dX[oX + e], (double)p.X[oX + e]);
     const double v0 = (double)p.V[oX + e];
-    const float v = (float)(v0 + al * ((double)p.lam[oX + e] - v0));
+    const float v = (float)fma(al, (double)p.lam[oX + e] - v0, v0);
     p.X[oX + e] = x;
     p.V[oX + e] = v;
     if (!isfinite(x) || !isfinite(v)) bad = 1;
   }
   for (size_t e = threadIdx.x; e < nU; e += kBlk) {
-    const float u = (float)((double)p.U[oU + e] + al * (double)p.dU[oU + e]);
+    const float u = (float)fma(al, (double)p.dU[oU + e], (double)p.U[oU + e]);
     p.U[oU + e] = u;
     if (!isfinite(u)) bad = 1;
   }
@@ -998,7 +1016,7 @@ __global__ void wb_kkt_finish_kernel(int B, unsigned* bits, float* kkt) {
 
 // ---------------------------------------------------------------- host
 struct WsLayout {
-  size_t fnom, cd, sums, ls, trial, A, Bm, c, x0s, Q, R, M, q, r, K, k, dX, dU, lam, Pscr, kbits, bytes;
+  size_t fnom, cd, sums, ls, trial, fcache, fvalid, A, Bm, c, x0s, Q, R, M, q, r, K, k, dX, dU, lam, Pscr, kbits, bytes;
 };
 
 WsLayout ws_layout(const WbDims& d, int B, int N) {
@@ -1015,6 +1033,8 @@ WsLayout ws_layout(const WbDims& d, int B, int N) {
   L.sums = take(b * (n + 1) * 4 * 8);
   L.ls = take(b * 8 * 8);
   L.trial = take(b * kMaxTrials * (n + 1) * 8);
+  L.fcache = take(b * kMaxTrials * n * nx * 8);
+  L.fvalid = take(b * 4);
   L.A = take(b * n * nx * nx * 4);
   L.Bm = take(b * n * nx * nj * 4);
   L.c = take(b * n * nx * 4);
@@ -1083,6 +1103,7 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
   p.X = io->X; p.U = io->U; p.V = io->V; p.status = io->status; p.kkt = io->kkt;
   p.fnom = (double*)(ws + L.fnom); p.cd = (double*)(ws + L.cd); p.sums = (double*)(ws + L.sums);
   p.ls = (double*)(ws + L.ls); p.trial = (double*)(ws + L.trial);
+  p.fcache = (double*)(ws + L.fcache); p.fvalid = (int*)(ws + L.fvalid);
   p.A = (float*)(ws + L.A); p.Bm = (float*)(ws + L.Bm); p.c = (float*)(ws + L.c); p.x0s = (float*)(ws + L.x0s);
   p.Q = (float*)(ws + L.Q); p.R = (float*)(ws + L.R); p.M = (float*)(ws + L.M); p.q = (float*)(ws + L.q);
   p.r = (float*)(ws + L.r); p.K = (float*)(ws + L.K); p.k = (float*)(ws + L.k); p.dX = (float*)(ws + L.dX);
@@ -1115,6 +1136,8 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
     wb_quad_kernel<<<quad_blocks, 128, 0, st>>>(p);
     return cudaGetLastError();
   };
+  e = cudaMemsetAsync(p.fvalid, 0, (size_t)B * sizeof(int), st);  // the first linearisation computes f
+  if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: fvalid");
   if (io->iters == 0 && p.status) {
     e = cudaMemsetAsync(p.status, 0, (size_t)B * sizeof(int), st);
     if (e != cudaSuccess) return lib_cuda_fail(e, "mpxg_wb_sqp: status");
