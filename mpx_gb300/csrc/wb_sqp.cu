@@ -543,7 +543,8 @@ struct RLay {
 
 // out(r, c) = sum_l X(r, l) Y(l, c) over 16 x 16 threads, the tiling and
 // summation order of lqeq::bmm, each result handed to ep(r, c, sum) rather
-// than stored.  Ends with a barrier.
+// than stored; the inner loop unrolled 4 deep, so that a warp has four
+// steps' shared-memory loads in flight.  Ends with a barrier.
 template <int ROWS, int INNER, int COLS, bool TX, bool TY, class Ep>
 __device__ __forceinline__ void bmm_ep(const float* X, int ldx, const float* Y, int ldy, Ep ep) {
   constexpr int TR = (ROWS + 15) / 16, TC = (COLS + 15) / 16;
@@ -553,7 +554,7 @@ __device__ __forceinline__ void bmm_ep(const float* X, int ldx, const float* Y, 
   for (int i = 0; i < TR; ++i)
 #pragma unroll
     for (int j = 0; j < TC; ++j) acc[i][j] = 0.0f;
-#pragma unroll 2
+#pragma unroll 4
   for (int l = 0; l < INNER; ++l) {
     float xa[TR], yb[TC];
 #pragma unroll
