@@ -1086,6 +1086,12 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
     return lib_fail(MPXG_ERR_INVALID_ARG,
                     "mpxg_wb_sqp: needs batch >= 0, N >= 1, iters >= 0, ls_max_trials in 1..8, dt > 0, "
                     "0 < ls_beta < 1, reg >= 0");
+  {  // the launch grids: a block per warp item of B N (nz + nj) columns or B (ls_max_trials - 1) (N + 1) trials
+    const WbDims d0 = wb_dims(*io->model);
+    const long long per = d0.nz + d0.nj > kMaxTrials ? d0.nz + d0.nj : kMaxTrials;
+    if ((long long)io->batch * ((long long)io->N + 1) * per > 0x7fffffffLL)
+      return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: batch x (N + 1) x 49 must stay below 2^31 (launch grids)");
+  }
   if (io->batch == 0) return MPXG_OK;
   if (!io->x0 || !io->X || !io->U || !io->V || !io->reference || !io->contact || !io->W || !io->workspace)
     return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: null array");
