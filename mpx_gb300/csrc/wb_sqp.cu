@@ -1056,6 +1056,14 @@ WsLayout ws_layout(const WbDims& d, int B, int N) {
   return L;
 }
 
+// The launch grids stay below 2^31 blocks: a block per warp item of the
+// B N (nz + nj) dual-number columns or the B (ls_max_trials - 1) (N + 1)
+// line-search trials at most.
+bool wb_sqp_grid_ok(const WbDims& d, int batch, int N) {
+  const long long per = d.nz + d.nj > kMaxTrials ? d.nz + d.nj : kMaxTrials;
+  return (long long)batch * ((long long)N + 1) * per <= 0x7fffffffLL;
+}
+
 const char* wb_sqp_model_problem(const mpxg_wb_model* m) {
   if (const char* why = wb_model_check(m)) return why;
   const int nv = m->nv, nr = 3 * m->n_contact;
@@ -1073,7 +1081,8 @@ const char* wb_sqp_model_problem(const mpxg_wb_model* m) {
 extern "C" {
 
 size_t mpxg_wb_sqp_workspace_bytes(const mpxg_wb_model* model, int batch, int N) {
-  if (!model || wb_sqp_model_problem(model) || batch < 0 || N < 1) return 0;
+  if (!model || wb_sqp_model_problem(model) || batch < 0 || N < 1 || !wb_sqp_grid_ok(wb_dims(*model), batch, N))
+    return 0;
   return ws_layout(wb_dims(*model), batch, N).bytes;
 }
 
@@ -1086,12 +1095,8 @@ mpxg_status mpxg_wb_sqp(void* stream, const mpxg_wb_sqp_io* io) {
     return lib_fail(MPXG_ERR_INVALID_ARG,
                     "mpxg_wb_sqp: needs batch >= 0, N >= 1, iters >= 0, ls_max_trials in 1..8, dt > 0, "
                     "0 < ls_beta < 1, reg >= 0");
-  {  // the launch grids: a block per warp item of B N (nz + nj) columns or B (ls_max_trials - 1) (N + 1) trials
-    const WbDims d0 = wb_dims(*io->model);
-    const long long per = d0.nz + d0.nj > kMaxTrials ? d0.nz + d0.nj : kMaxTrials;
-    if ((long long)io->batch * ((long long)io->N + 1) * per > 0x7fffffffLL)
-      return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: batch x (N + 1) x 49 must stay below 2^31 (launch grids)");
-  }
+  if (!wb_sqp_grid_ok(wb_dims(*io->model), io->batch, io->N))
+    return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: batch x (N + 1) x 49 must stay below 2^31 (launch grids)");
   if (io->batch == 0) return MPXG_OK;
   if (!io->x0 || !io->X || !io->U || !io->V || !io->reference || !io->contact || !io->W || !io->workspace)
     return lib_fail(MPXG_ERR_INVALID_ARG, "mpxg_wb_sqp: null array");

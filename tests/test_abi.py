@@ -180,6 +180,7 @@ def test_wb_sqp_rejects_before_any_launch():
     assert L.mpxg_wb_sqp(None, ctypes.byref(io(N=0))) == 1
     assert L.mpxg_wb_sqp(None, ctypes.byref(io(batch=1 << 20, N=100))) == 1  # grids past 2^31 blocks
     assert b"launch grids" in L.mpxg_last_error(None)
+    assert L.mpxg_wb_sqp_workspace_bytes(ctypes.byref(S), 1 << 20, 100) == 0
     assert L.mpxg_wb_sqp(None, ctypes.byref(io(batch=2, workspace=fake + 16))) == 1
     assert b"256-byte" in L.mpxg_last_error(None)
     assert L.mpxg_wb_sqp(None, ctypes.byref(io(batch=2, W=None))) == 1
