@@ -90,3 +90,72 @@ def test_one_iteration_reduces_the_kkt_residual():
     assert k1[0] < k0[0] and k1[1] < k0[1], (k0, k1)  # primal and dual parts both fall
     # the step satisfies the linearised dynamics it was computed from
     assert np.abs(r["dX"][0] - r["c"][0]).max() < 1e-9
+
+
+def _dense_lq_kkt(A, B, c, Q, R, M, q, r, x0):
+    """The LQ step problem as one dense KKT system: variables [x_0..x_N,
+    u_0..u_{N-1}], constraints x_0 = x0 and x_{t+1} - A_t x_t - B_t u_t = c_t,
+    cost sum 1/2 x'Qx + x'Mu + 1/2 u'Ru + q'x + r'u.  Returns X, U and the
+    constraints' multipliers nu (stationarity H z + g + E' nu = 0)."""
+    N, n, m = len(A), x0.size, B[0].shape[1]
+    nz = (N + 1) * n + N * m
+    xi = lambda t: slice(t * n, (t + 1) * n)
+    ui = lambda t: slice((N + 1) * n + t * m, (N + 1) * n + (t + 1) * m)
+    H, g = np.zeros((nz, nz)), np.zeros(nz)
+    for t in range(N + 1):
+        H[xi(t), xi(t)] = Q[t]
+        g[xi(t)] = q[t]
+        if t < N:
+            H[ui(t), ui(t)] = R[t]
+            H[xi(t), ui(t)] = M[t]
+            H[ui(t), xi(t)] = M[t].T
+            g[ui(t)] = r[t]
+    E, e = np.zeros(((N + 1) * n, nz)), np.zeros((N + 1) * n)
+    E[xi(0), xi(0)] = np.eye(n)
+    e[xi(0)] = x0
+    for t in range(N):
+        E[xi(t + 1), xi(t + 1)] = np.eye(n)
+        E[xi(t + 1), xi(t)] = -A[t]
+        E[xi(t + 1), ui(t)] = -B[t]
+        e[xi(t + 1)] = c[t]
+    K = np.block([[H, E.T], [E, np.zeros((E.shape[0], E.shape[0]))]])
+    sol = np.linalg.solve(K, np.concatenate([-g, e]))
+    z, nu = sol[:nz], sol[nz:]
+    X = np.stack([z[xi(t)] for t in range(N + 1)])
+    U = np.stack([z[ui(t)] for t in range(N)])
+    return X, U, nu.reshape(N + 1, n)
+
+
+@pytest.mark.parametrize("structured", [False, True])
+def test_step_riccati_equals_dense_kkt(structured):
+    """The oracle's Riccati step (the one the GPU's 61-state Riccati is
+    checked against) equals a dense KKT solve of the same LQ problem, with
+    its costates the negated constraint multipliers; both for a general
+    problem and for the whole-body structure (the contact-point and force
+    columns of A zero, M = 0)."""
+    from oracle.wb_sqp import _riccati
+    rng = np.random.default_rng(31 if structured else 30)
+    N, n, m, nzc = 5, 61, 12, 37
+    A, B, c, Q, R, M, q, r = [], [], [], [], [], [], [], []
+    for t in range(N + 1):
+        L = rng.normal(size=(n, n))
+        Q.append(L @ L.T / n + 0.1 * np.eye(n))
+        q.append(rng.normal(size=n))
+        if t == N:
+            break
+        a = np.eye(n) + 0.05 * rng.normal(size=(n, n))
+        if structured:
+            a[:, nzc:] = 0.0
+        A.append(a)
+        B.append(0.1 * rng.normal(size=(n, m)))
+        c.append(0.1 * rng.normal(size=n))
+        R.append(np.eye(m))
+        M.append(np.zeros((n, m)) if structured else 0.02 * rng.normal(size=(n, m)))
+        r.append(rng.normal(size=m))
+    x0 = rng.normal(size=n)
+    dX, dU, lam = _riccati(A, B, c, Q, R, M, q, r, x0)
+    X, U, nu = _dense_lq_kkt(A, B, c, Q, R, M, q, r, x0)
+    scale = lambda a: 1.0 + np.abs(a).max()
+    assert np.abs(dX - X).max() < 1e-9 * scale(X)
+    assert np.abs(dU - U).max() < 1e-9 * scale(U)
+    assert np.abs(lam + nu).max() < 1e-9 * scale(nu)
